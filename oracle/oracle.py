@@ -1,0 +1,252 @@
+"""ctypes wrapper of the CPU oracle (oracle/toast_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by the CPU-baseline leg of bench.py, as the checker.  The product path
+never imports it.
+
+``forward_path`` restates the reference's caller sequence for one problem:
+source/measurement vectors (src/supertoast/fwdfem.cc:127-176,
+src/python/toastmodule.cc:1189-1220), assembly and preconditioner reset
+(src/libstoast/fwdsolver.cc:493-505), forward and adjoint CalcFields (653-750),
+ProjectAll (1415-1447) and the nodal Jacobian (src/libstoast/jacobian.cc:441-497,
+738-802).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "toast_oracle.c")
+LIB = os.path.join(HERE, "libtoast_oracle.so")
+
+_lib = None
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_up = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library in place (gcc, a second or two)."""
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        tmp = LIB + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-o", tmp, SRC, "-lm", "-lpthread"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        L.tor_mesh_create.restype = C.c_void_p
+        L.tor_mesh_create.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ip]
+        L.tor_mesh_free.argtypes = [C.c_void_p]
+        L.tor_mesh_nnz.restype = C.c_int
+        L.tor_mesh_nnz.argtypes = [C.c_void_p]
+        L.tor_mesh_csr.argtypes = [C.c_void_p, _ip, _ip]
+        L.tor_mesh_bndnodes.argtypes = [C.c_void_p, _up]
+        L.tor_mesh_elsize.argtypes = [C.c_void_p, _dp]
+        L.tor_pull_to_boundary.restype = C.c_int
+        L.tor_pull_to_boundary.argtypes = [C.c_void_p, _dp, _dp]
+        L.tor_qvec_gaussian.argtypes = [C.c_void_p, _dp, C.c_double, C.c_int, _dp]
+        L.tor_assemble.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, C.c_int, _dp]
+        L.tor_solve.restype = C.c_int
+        L.tor_solve.argtypes = [C.c_int, _ip, _ip, _dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int,
+                                C.c_int, _dp, _dp, _ip, _dp, C.c_int]
+        L.tor_ic_factor.restype = C.c_int
+        L.tor_ic_factor.argtypes = [C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp, _dp]
+        L.tor_project.argtypes = [C.c_int, C.c_int, _dp, _dp, _ip, _ip, C.c_int, C.c_int, _dp]
+        L.tor_jacobian.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int, C.c_int,
+                                   _dp, C.c_int]
+        L.tor_a_keijzer.restype = C.c_double
+        L.tor_a_keijzer.argtypes = [C.c_double]
+        _lib = L
+    return _lib
+
+
+def _cview(z: np.ndarray) -> np.ndarray:
+    """complex128 array -> interleaved float64 view (contiguous)."""
+    return np.ascontiguousarray(z).view(np.float64)
+
+
+class Mesh:
+    """Oracle-side mesh: geometry, boundary marking and the CSR pattern."""
+
+    def __init__(self, coords: np.ndarray, elems: np.ndarray):
+        self.coords = np.ascontiguousarray(coords, np.float64)
+        self.elems = np.ascontiguousarray(elems, np.int32)
+        self.dim = self.coords.shape[1]
+        self.n = self.coords.shape[0]
+        self.ne = self.elems.shape[0]
+        self._h = lib().tor_mesh_create(self.dim, self.n, self.coords.ravel(), self.ne, self.elems.ravel())
+        nnz = lib().tor_mesh_nnz(self._h)
+        self.rowptr = np.zeros(self.n + 1, np.int32)
+        self.colidx = np.zeros(nnz, np.int32)
+        lib().tor_mesh_csr(self._h, self.rowptr, self.colidx)
+        self.bnd = np.zeros(self.n, np.uint8)
+        lib().tor_mesh_bndnodes(self._h, self.bnd)
+        self.size = np.zeros(self.ne)
+        lib().tor_mesh_elsize(self._h, self.size)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().tor_mesh_free(self._h)
+            self._h = None
+
+    @property
+    def nnz(self) -> int:
+        return int(self.colidx.shape[0])
+
+    def pull_to_boundary(self, p) -> np.ndarray:
+        out = np.zeros(self.dim)
+        rc = lib().tor_pull_to_boundary(self._h, np.ascontiguousarray(p, np.float64), out)
+        if rc:
+            raise RuntimeError("PullToBoundary: no boundary side found")
+        return out
+
+    def qvec_gaussian(self, cnt, w, neumann=True) -> np.ndarray:
+        out = np.zeros(self.n)
+        lib().tor_qvec_gaussian(self._h, np.ascontiguousarray(cnt, np.float64), float(w), int(neumann), out)
+        return out
+
+    def assemble(self, cmua, ckap, c2a, omega: float, cplx: bool) -> np.ndarray:
+        val = np.zeros(self.nnz * (2 if cplx else 1))
+        lib().tor_assemble(self._h, np.ascontiguousarray(cmua, np.float64), np.ascontiguousarray(ckap, np.float64),
+                           np.ascontiguousarray(c2a, np.float64), float(omega), int(cplx), val)
+        return val.view(np.complex128) if cplx else val
+
+
+def a_keijzer(n: float) -> float:
+    return lib().tor_a_keijzer(float(n))
+
+
+def optical_coefficients(mua, mus, nref):
+    """Nodal cmua, ckappa, c2a (src/python/toastmodule.cc:1536-1541, c0 = 0.3 mm/ps)."""
+    c0 = 0.3
+    mua = np.asarray(mua, float); mus = np.asarray(mus, float); nref = np.asarray(nref, float)
+    cmua = mua * c0 / nref
+    ckap = c0 / (3.0 * nref * (mua + mus))
+    c2a = np.array([c0 / (2.0 * r * a_keijzer(r)) for r in nref])
+    return cmua, ckap, c2a
+
+
+METHODS = {"CG": 0, "BICGSTAB": 1, "GMRES": 2}
+PRECONS = {"NONE": 0, "DIAG": 1, "ICH": 2, "DILU": 0}  # DILU is built as no preconditioner (fwdsolver.cc:149-153)
+
+
+def solve(rowptr, colidx, val, B, method="BICGSTAB", precon="ICH", tol=1e-10, maxit=0, nthreads=1, X0=None):
+    """Solve A x_q = b_q for every row of B (nrhs x n).  Returns X, its, errs."""
+    cplx = np.iscomplexobj(val)
+    n = rowptr.shape[0] - 1
+    B = np.ascontiguousarray(B, np.complex128 if cplx else np.float64)
+    nrhs = B.shape[0]
+    X = np.zeros_like(B) if X0 is None else np.array(X0, dtype=B.dtype, copy=True)
+    its = np.zeros(nrhs, np.int32)
+    errs = np.zeros(nrhs)
+    nf = lib().tor_solve(n, np.ascontiguousarray(rowptr, np.int32), np.ascontiguousarray(colidx, np.int32),
+                         _cview(val) if cplx else np.ascontiguousarray(val, np.float64), int(cplx),
+                         METHODS[method], PRECONS[precon], float(tol), int(maxit), nrhs,
+                         _cview(B).ravel() if cplx else B.ravel(), _cview(X).reshape(-1) if cplx else X.reshape(-1),
+                         its, errs, int(nthreads))
+    if nf:
+        raise RuntimeError(f"oracle solve: {nf} right-hand sides failed (breakdown)")
+    return X, its, errs
+
+
+def ic_factor(rowptr, colidx, val):
+    cplx = np.iscomplexobj(val)
+    n = rowptr.shape[0] - 1
+    nl = int((rowptr[-1] - n) // 2) + n
+    Lr = np.zeros(n + 1, np.int32)
+    Lc = np.zeros(max(nl, 1), np.int32)
+    Lv = np.zeros(max(nl, 1) * (2 if cplx else 1))
+    d = np.zeros(n * (2 if cplx else 1))
+    got = lib().tor_ic_factor(n, rowptr, colidx, _cview(val) if cplx else np.ascontiguousarray(val, np.float64),
+                              int(cplx), Lr, Lc, Lv, d)
+    Lc = Lc[:got]
+    Lv = Lv[:got * (2 if cplx else 1)]
+    if cplx:
+        return Lr, Lc, Lv.view(np.complex128), d.view(np.complex128)
+    return Lr, Lc, Lv, d
+
+
+def project(phi, mvec, link_ofs, link_m, logscale=True):
+    cplx = np.iscomplexobj(phi)
+    nq, n = phi.shape
+    nqm = int(link_ofs[-1])
+    out = np.zeros(nqm * (2 if cplx else 1))
+    lib().tor_project(n, nq, _cview(phi).ravel() if cplx else np.ascontiguousarray(phi, np.float64).ravel(),
+                      _cview(mvec.astype(np.complex128)).ravel() if cplx else np.ascontiguousarray(mvec, np.float64).ravel(),
+                      np.ascontiguousarray(link_ofs, np.int32), np.ascontiguousarray(link_m, np.int32),
+                      int(cplx), int(logscale), out)
+    return out.view(np.complex128) if cplx else out
+
+
+def jacobian(mesh: Mesh, dphi, aphi, proj_lin, link_ofs, link_m, logscale=True, nthreads=1):
+    cplx = np.iscomplexobj(dphi)
+    nq, n = dphi.shape
+    nm = aphi.shape[0]
+    nqm = int(link_ofs[-1])
+    J = np.zeros((2 * nqm, 2 * n) if cplx else (2 * nqm, n))
+    lib().tor_jacobian(mesh._h, nq, nm,
+                       _cview(dphi).ravel() if cplx else np.ascontiguousarray(dphi, np.float64).ravel(),
+                       _cview(aphi).ravel() if cplx else np.ascontiguousarray(aphi, np.float64).ravel(),
+                       _cview(proj_lin).ravel() if cplx else np.ascontiguousarray(proj_lin, np.float64).ravel(),
+                       np.ascontiguousarray(link_ofs, np.int32), np.ascontiguousarray(link_m, np.int32),
+                       int(cplx), int(logscale), J.reshape(-1), int(nthreads))
+    return J
+
+
+@dataclass
+class PathResult:
+    qvec: np.ndarray
+    mvec: np.ndarray
+    sysval: np.ndarray
+    dphi: np.ndarray
+    aphi: np.ndarray
+    proj: np.ndarray           # linear projections (nQM)
+    logproj: np.ndarray        # log projections
+    J: np.ndarray | None
+    its_fwd: np.ndarray
+    its_adj: np.ndarray
+    times: dict = field(default_factory=dict)
+
+
+def forward_path(mesh: Mesh, Q, M, link_ofs, link_m, mua, mus, nref, freq_mhz=0.0, qwidth=2.0, mwidth=2.0,
+                 method=None, precon="ICH", tol=1e-10, maxit=0, jac=True, nthreads=1) -> PathResult:
+    """The whole forward path on the CPU, as the reference's callers run it."""
+    cplx = freq_mhz != 0.0
+    method = method or ("BICGSTAB" if cplx else "CG")
+    cmua, ckap, c2a = optical_coefficients(mua, mus, nref)
+    omega = freq_mhz * 2.0 * np.pi * 1e-6
+    qvec = np.stack([mesh.qvec_gaussian(q, qwidth) for q in Q])
+    mvec = np.stack([mesh.qvec_gaussian(m, mwidth) * c2a for m in M])
+    t = {}
+    t0 = time.perf_counter()
+    val = mesh.assemble(cmua, ckap, c2a, omega, cplx)
+    t["assemble"] = time.perf_counter() - t0
+    dt = np.complex128 if cplx else np.float64
+    t0 = time.perf_counter()
+    dphi, itf, _ = solve(mesh.rowptr, mesh.colidx, val, qvec.astype(dt), method, precon, tol, maxit, nthreads)
+    t["fwd"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    aphi, ita, _ = solve(mesh.rowptr, mesh.colidx, val, mvec.astype(dt), method, precon, tol, maxit, nthreads)
+    t["adj"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    proj = project(dphi, mvec.astype(dt), link_ofs, link_m, logscale=False)
+    lproj = project(dphi, mvec.astype(dt), link_ofs, link_m, logscale=True)
+    t["proj"] = time.perf_counter() - t0
+    J = None
+    if jac:
+        t0 = time.perf_counter()
+        J = jacobian(mesh, dphi, aphi, proj, link_ofs, link_m, True, nthreads)
+        t["jac"] = time.perf_counter() - t0
+    return PathResult(qvec, mvec, val, dphi, aphi, proj, lproj, J, itf, ita, t)

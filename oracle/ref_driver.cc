@@ -1,0 +1,290 @@
+// ref_driver.cc -- runs the reference's own forward path (compiled from the
+// reference tree by oracle/Makefile.ref) on one problem and writes the results
+// as raw little-endian binary, so that the oracle restatement and the GPU path
+// can be compared against the reference itself.
+//
+// The call sequence mirrors the reference's own callers:
+//   src/supertoast/fwdfem.cc:56-250        (fields + ProjectAll, LOG data)
+//   src/python/toastmodule.cc:1514-1574    (CalcJacobian, complex)
+//   src/python/toastmodule.cc:1630-1684    (CalcJacobianCW, real)
+//   src/python/toastmodule.cc:1189-1220    (measurement vectors scaled by c2a)
+//
+// Usage (key=value arguments):
+//   ref_driver mesh=M.msh (qm=F.qm | optodes=O.bin) out=PREFIX
+//              dtype=real|complex solver=CG|BICGSTAB|GMRES precon=NONE|DIAG|ICH
+//              tol=1e-10 maxit=0 freq=100 qwidth=2 mwidth=2 nth=1
+//              (params=P.bin | mua=0.025 mus=2 nref=1.4) jac=0|1 fields=0|1
+//              sysmat=0|1 qsub=0 msub=0
+// optodes.bin: int32 dim,nQ,nM ; nQ*dim doubles ; nM*dim doubles (all-to-all links)
+// params.bin : n*3 doubles, node-major (mua, mus', nref)
+// qsub/msub  : if >0, only the first qsub sources / msub detectors are solved
+//              (bounded CPU baseline samples); the Jacobian is then skipped.
+#include "stoastlib.h"
+#include <fstream>
+#include <iostream>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+using namespace std;
+
+static map<string, string> g_args;
+static string arg(const char* k, const char* def) {
+    auto it = g_args.find(k);
+    return it == g_args.end() ? string(def) : it->second;
+}
+
+static void wbin(const string& fn, const void* p, size_t bytes) {
+    FILE* f = fopen(fn.c_str(), "wb");
+    if (!f) { fprintf(stderr, "cannot write %s\n", fn.c_str()); exit(2); }
+    if (bytes) fwrite(p, 1, bytes, f);
+    fclose(f);
+}
+
+static std::vector<char> rbin(const string& fn) {
+    FILE* f = fopen(fn.c_str(), "rb");
+    if (!f) { fprintf(stderr, "cannot read %s\n", fn.c_str()); exit(2); }
+    fseek(f, 0, SEEK_END); long sz = ftell(f); fseek(f, 0, SEEK_SET);
+    std::vector<char> buf(sz);
+    if (sz && fread(buf.data(), 1, sz, f) != (size_t)sz) exit(2);
+    fclose(f);
+    return buf;
+}
+
+// Sets the QMMesh link tables for all-to-all links without LoadQM (positions
+// are used exactly as given; InitM is not run because nothing on the path
+// reads Mel/Mcosingder).
+static void setup_optodes(QMMesh& mesh, const string& fn) {
+    std::vector<char> b = rbin(fn);
+    const int* hdr = (const int*)b.data();
+    int dim = hdr[0], nq = hdr[1], nm = hdr[2];
+    const double* xy = (const double*)(b.data() + 3 * sizeof(int));
+    mesh.nQ = nq; mesh.nM = nm;
+    mesh.Q = new Point[nq]; mesh.M = new Point[nm];
+    for (int i = 0; i < nq; i++) { mesh.Q[i].New(dim); for (int d = 0; d < dim; d++) mesh.Q[i][d] = xy[i * dim + d]; }
+    for (int i = 0; i < nm; i++) { mesh.M[i].New(dim); for (int d = 0; d < dim; d++) mesh.M[i][d] = xy[(nq + i) * dim + d]; }
+    mesh.nQMref = new int[nq]; mesh.Qofs = new int[nq];
+    mesh.QMref = new int*[nq]; mesh.QMofs = new int*[nq];
+    for (int q = 0; q < nq; q++) {
+        mesh.nQMref[q] = nm;
+        mesh.Qofs[q] = q * nm;
+        mesh.QMref[q] = new int[nm];
+        mesh.QMofs[q] = new int[nm];
+        for (int m = 0; m < nm; m++) { mesh.QMref[q][m] = m; mesh.QMofs[q][m] = q * nm + m; }
+    }
+    mesh.nQM = nq * nm;
+}
+
+template <class T> static const double* rawd(const TVector<T>& v) {
+    return (const double*)v.data_buffer();
+}
+
+int main(int argc, char** argv) {
+    for (int i = 1; i < argc; i++) {
+        const char* eq = strchr(argv[i], '=');
+        if (!eq) { fprintf(stderr, "bad arg %s\n", argv[i]); return 2; }
+        g_args[string(argv[i], eq - argv[i])] = string(eq + 1);
+    }
+    const double c0 = 0.3;
+    string out = arg("out", "ref");
+    bool cplx = arg("dtype", "complex") == "complex";
+    string solver = arg("solver", cplx ? "BICGSTAB" : "CG");
+    string precon = arg("precon", "ICH");
+    double tol = atof(arg("tol", "1e-10").c_str());
+    int maxit = atoi(arg("maxit", "0").c_str());
+    double freq = atof(arg("freq", cplx ? "100" : "0").c_str());
+    double qwidth = atof(arg("qwidth", "2").c_str());
+    double mwidth = atof(arg("mwidth", "2").c_str());
+    int nth = atoi(arg("nth", "1").c_str());
+    bool want_jac = atoi(arg("jac", "0").c_str()) != 0;
+    bool want_fields = atoi(arg("fields", "0").c_str()) != 0;
+    bool want_sys = atoi(arg("sysmat", "0").c_str()) != 0;
+    int qsub = atoi(arg("qsub", "0").c_str());
+    int msub = atoi(arg("msub", "0").c_str());
+
+    Task_Init(nth);
+    toastVerbosity = 0;
+
+    QMMesh mesh;
+    {
+        ifstream ifs(arg("mesh", "").c_str());
+        ifs >> mesh;
+        mesh.Setup();
+    }
+    if (g_args.count("qm")) {
+        ifstream ifs(arg("qm", "").c_str());
+        mesh.LoadQM(ifs);
+    } else {
+        setup_optodes(mesh, arg("optodes", ""));
+    }
+    int n = mesh.nlen(), nQ = mesh.nQ, nM = mesh.nM, nQM = mesh.nQM;
+    int dim = mesh.Dimension();
+
+    RVector mua(n), mus(n), ref(n);
+    if (g_args.count("params")) {
+        std::vector<char> b = rbin(arg("params", ""));
+        const double* p = (const double*)b.data();
+        for (int i = 0; i < n; i++) { mua[i] = p[3 * i]; mus[i] = p[3 * i + 1]; ref[i] = p[3 * i + 2]; }
+    } else {
+        mua = atof(arg("mua", "0.025").c_str());
+        mus = atof(arg("mus", "2").c_str());
+        ref = atof(arg("nref", "1.4").c_str());
+    }
+    Solution msol(OT_NPARAM, n);
+    msol.SetParam(OT_CMUA, mua * c0 / ref);
+    msol.SetParam(OT_CKAPPA, c0 / (3.0 * ref * (mua + mus)));
+    msol.SetParam(OT_N, ref);
+    RVector c2a(n);
+    for (int i = 0; i < n; i++) c2a[i] = c0 / (2.0 * ref[i] * A_Keijzer(ref[i]));
+    msol.SetParam(OT_C2A, c2a);
+    double omega = freq * 2.0 * Pi * 1e-6;
+
+    // detector positions as used (after LoadQM/InitM pulled them to the boundary)
+    {
+        std::vector<double> optpos;
+        for (int i = 0; i < nQ; i++) for (int d = 0; d < dim; d++) optpos.push_back(mesh.Q[i][d]);
+        for (int i = 0; i < nM; i++) for (int d = 0; d < dim; d++) optpos.push_back(mesh.M[i][d]);
+        wbin(out + "_optodes.bin", optpos.data(), optpos.size() * sizeof(double));
+    }
+
+    PreconType pt = precon == "ICH" ? PRECON_ICH : precon == "DIAG" ? PRECON_DIAG
+                  : precon == "DILU" ? PRECON_DILU : PRECON_NULL;
+    int nq_solve = qsub > 0 ? min(qsub, nQ) : nQ;
+    int nm_solve = msub > 0 ? min(msub, nM) : nM;
+    bool sampled = qsub > 0 || msub > 0;
+
+    FILE* info = fopen((out + "_info.txt").c_str(), "w");
+    fprintf(info, "n %d\nnQ %d\nnM %d\nnQM %d\ndim %d\nelen %d\n", n, nQ, nM, nQM, dim, mesh.elen());
+
+    if (cplx) {
+        CCompRowMatrix qvec(nQ, n), mvec(nM, n);
+        for (int i = 0; i < nQ; i++) {
+            CVector q(n);
+            SetReal(q, QVec_Gaussian(mesh, mesh.Q[i], qwidth, SRCMODE_NEUMANN));
+            qvec.SetRow(i, q);
+        }
+        for (int i = 0; i < nM; i++) {
+            CVector m(n);
+            SetReal(m, QVec_Gaussian(mesh, mesh.M[i], mwidth, SRCMODE_NEUMANN) * c2a);
+            mvec.SetRow(i, m);
+        }
+        CFwdSolver FWS(&mesh, solver.c_str(), tol);
+        FWS.SetPrecon(pt);
+        FWS.SetLinSolverMaxit(maxit);
+        FWS.SetDataScaling(DATA_LOG);
+        FWS.Allocate();
+        double t0 = walltic();
+        FWS.Reset(msol, omega);
+        fprintf(info, "t_reset %.9g\n", walltoc(t0));
+        if (want_sys) {
+            const CCompRowMatrix& F = *FWS.F;
+            wbin(out + "_rowptr.bin", F.rowptr, (n + 1) * sizeof(int));
+            wbin(out + "_colidx.bin", F.colidx, F.nVal() * sizeof(int));
+            wbin(out + "_sysval.bin", F.ValPtr(), F.nVal() * sizeof(std::complex<double>));
+        }
+        CVector* dphi = new CVector[nQ];
+        CVector* aphi = new CVector[nM];
+        for (int i = 0; i < nQ; i++) dphi[i].New(n);
+        for (int i = 0; i < nM; i++) aphi[i].New(n);
+        IterativeSolverResult res;
+        CCompRowMatrix qs(nq_solve, n), ms(nm_solve, n);
+        for (int i = 0; i < nq_solve; i++) qs.SetRow(i, qvec.Row(i));
+        for (int i = 0; i < nm_solve; i++) ms.SetRow(i, mvec.Row(i));
+        t0 = walltic();
+        FWS.CalcFields(qs, dphi, &res);
+        fprintf(info, "t_fwd %.9g\nit_fwd %d\nerr_fwd %.6g\n", walltoc(t0), res.it_count, res.rel_err);
+        t0 = walltic();
+        FWS.CalcFields(ms, aphi, &res);
+        fprintf(info, "t_adj %.9g\nit_adj %d\nerr_adj %.6g\n", walltoc(t0), res.it_count, res.rel_err);
+        if (!sampled) {
+            t0 = walltic();
+            CVector proj = FWS.ProjectAll(mvec, dphi, DATA_LIN);
+            CVector lproj = FWS.ProjectAll(mvec, dphi, DATA_LOG);
+            fprintf(info, "t_proj %.9g\n", walltoc(t0));
+            wbin(out + "_proj.bin", rawd(proj), nQM * sizeof(std::complex<double>));
+            wbin(out + "_logproj.bin", rawd(lproj), nQM * sizeof(std::complex<double>));
+            if (want_jac) {
+                RDenseMatrix J(2 * nQM, 2 * n);
+                t0 = walltic();
+                GenerateJacobian(0, &mesh, dphi, aphi, &proj, DATA_LOG, J);
+                fprintf(info, "t_jac %.9g\n", walltoc(t0));
+                wbin(out + "_J.bin", J.ValPtr(), (size_t)2 * nQM * 2 * n * sizeof(double));
+            }
+        }
+        if (want_fields) {
+            FILE* f = fopen((out + "_dphi.bin").c_str(), "wb");
+            for (int i = 0; i < nq_solve; i++) fwrite(rawd(dphi[i]), sizeof(std::complex<double>), n, f);
+            fclose(f);
+            f = fopen((out + "_aphi.bin").c_str(), "wb");
+            for (int i = 0; i < nm_solve; i++) fwrite(rawd(aphi[i]), sizeof(std::complex<double>), n, f);
+            fclose(f);
+        }
+        delete[] dphi;
+        delete[] aphi;
+    } else {
+        RCompRowMatrix qvec(nQ, n), mvec(nM, n);
+        for (int i = 0; i < nQ; i++) qvec.SetRow(i, QVec_Gaussian(mesh, mesh.Q[i], qwidth, SRCMODE_NEUMANN));
+        for (int i = 0; i < nM; i++) mvec.SetRow(i, QVec_Gaussian(mesh, mesh.M[i], mwidth, SRCMODE_NEUMANN) * c2a);
+        RFwdSolver FWS(&mesh, solver.c_str(), tol);
+        FWS.SetPrecon(pt);
+        FWS.SetLinSolverMaxit(maxit);
+        FWS.SetDataScaling(DATA_LOG);
+        FWS.Allocate();
+        double t0 = walltic();
+        FWS.Reset(msol, 0);
+        fprintf(info, "t_reset %.9g\n", walltoc(t0));
+        if (want_sys) {
+            const RCompRowMatrix& F = *FWS.F;
+            wbin(out + "_rowptr.bin", F.rowptr, (n + 1) * sizeof(int));
+            wbin(out + "_colidx.bin", F.colidx, F.nVal() * sizeof(int));
+            wbin(out + "_sysval.bin", F.ValPtr(), F.nVal() * sizeof(double));
+        }
+        RVector* dphi = new RVector[nQ];
+        RVector* aphi = new RVector[nM];
+        for (int i = 0; i < nQ; i++) dphi[i].New(n);
+        for (int i = 0; i < nM; i++) aphi[i].New(n);
+        IterativeSolverResult res;
+        RCompRowMatrix qs(nq_solve, n), ms(nm_solve, n);
+        for (int i = 0; i < nq_solve; i++) qs.SetRow(i, qvec.Row(i));
+        for (int i = 0; i < nm_solve; i++) ms.SetRow(i, mvec.Row(i));
+        t0 = walltic();
+        FWS.CalcFields(qs, dphi, &res);
+        fprintf(info, "t_fwd %.9g\nit_fwd %d\nerr_fwd %.6g\n", walltoc(t0), res.it_count, res.rel_err);
+        t0 = walltic();
+        FWS.CalcFields(ms, aphi, &res);
+        fprintf(info, "t_adj %.9g\nit_adj %d\nerr_adj %.6g\n", walltoc(t0), res.it_count, res.rel_err);
+        if (!sampled) {
+            t0 = walltic();
+            RVector proj = FWS.ProjectAll(mvec, dphi, DATA_LIN);
+            RVector lproj = FWS.ProjectAll(mvec, dphi, DATA_LOG);
+            fprintf(info, "t_proj %.9g\n", walltoc(t0));
+            wbin(out + "_proj.bin", rawd(proj), nQM * sizeof(double));
+            wbin(out + "_logproj.bin", rawd(lproj), nQM * sizeof(double));
+            if (want_jac) {
+                RDenseMatrix Jmua, Jkap;
+                t0 = walltic();
+                GenerateJacobian_cw(0, &mesh, mvec, dphi, aphi, DATA_LOG, &Jmua, &Jkap);
+                fprintf(info, "t_jac %.9g\n", walltoc(t0));
+                FILE* f = fopen((out + "_J.bin").c_str(), "wb");
+                fwrite(Jmua.ValPtr(), sizeof(double), (size_t)nQM * n, f);
+                fwrite(Jkap.ValPtr(), sizeof(double), (size_t)nQM * n, f);
+                fclose(f);
+            }
+        }
+        if (want_fields) {
+            FILE* f = fopen((out + "_dphi.bin").c_str(), "wb");
+            for (int i = 0; i < nq_solve; i++) fwrite(rawd(dphi[i]), sizeof(double), n, f);
+            fclose(f);
+            f = fopen((out + "_aphi.bin").c_str(), "wb");
+            for (int i = 0; i < nm_solve; i++) fwrite(rawd(aphi[i]), sizeof(double), n, f);
+            fclose(f);
+        }
+        delete[] dphi;
+        delete[] aphi;
+    }
+    fclose(info);
+    return 0;
+}

@@ -1,0 +1,1203 @@
+/*
+ * toast_oracle.c -- CPU restatement of the Toast++ FEM diffusion forward path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle: the tests, the
+ * smoke check and the CPU-baseline leg of bench.py call it to check (and to
+ * time beside) the CUDA path.  No product code links or calls it.
+ *
+ * Each function restates the reference algorithm it cites (paths are within
+ * the toastpp project).  Floating-point operation order follows the reference
+ * wherever it is cheap to do so, so that results agree with the reference to
+ * round-off.  Parity is pinned in tests/ against the reference's shipped golden
+ * vectors (test/2D/fwdfem/testdata.zip, test/3D/fwdfem/testdata.zip) and
+ * against the reference compiled from source (oracle/Makefile.ref).
+ *
+ * Conventions: node and element indices are 0-based; complex arrays are
+ * interleaved (re, im) doubles; matrices are CSR with sorted columns.
+ */
+#include <complex.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef double _Complex zd;
+
+/* ------------------------------------------------------------------------ */
+/* Mesh                                                                      */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    int dim, n, ne, nn;       /* nn = nodes per element (3 Tri3, 4 Tet4) */
+    double *x;                /* n*dim */
+    int *el;                  /* ne*nn */
+    double *geo;              /* per element: Tri3 a0..2 b0..2 c0..2 ; Tet4 a,b,c,d (16) */
+    double *size;             /* ne */
+    double *side_size;        /* Tet4: ne*4 face areas */
+    unsigned char *bndside;   /* ne*nside */
+    unsigned char *bndnode;   /* n */
+    double *intdd;            /* ne*nn*nn */
+    double *intbff;           /* ne*nn*nn */
+    int *rowptr, *colidx;     /* CSR pattern */
+    int nnz;
+} tor_mesh;
+
+static const int TRI_SN[3][2] = {{0, 1}, {1, 2}, {2, 0}};              /* tri3.cc:123-127 */
+static const int TET_SN[4][3] = {{0, 1, 2}, {0, 3, 1}, {0, 2, 3}, {1, 3, 2}}; /* tet4.cc:175-181 */
+
+static double pt_dist(const double *a, const double *b, int dim)
+{   /* point.cc:33-41 */
+    double d2 = 0.0;
+    for (int i = 0; i < dim; i++) d2 += (a[i] - b[i]) * (a[i] - b[i]);
+    return sqrt(d2);
+}
+
+/* Triangle3::Initialise (tri3.cc:79-88) and Tetrahedron4::Initialise
+   (tet4.cc:113-141): geometry coefficients and size. */
+static void element_geometry(tor_mesh *m, int e)
+{
+    const int *nd = m->el + (size_t)e * m->nn;
+    double *g = m->geo + (size_t)e * 16;
+    if (m->dim == 2) {
+        double x0 = m->x[2 * nd[0]], y0 = m->x[2 * nd[0] + 1];
+        double x1 = m->x[2 * nd[1]], y1 = m->x[2 * nd[1] + 1];
+        double x2 = m->x[2 * nd[2]], y2 = m->x[2 * nd[2] + 1];
+        g[0] = x1 * y2 - x2 * y1; g[3] = y1 - y2; g[6] = x2 - x1;
+        g[1] = x2 * y0 - x0 * y2; g[4] = y2 - y0; g[7] = x0 - x2;
+        g[2] = x0 * y1 - x1 * y0; g[5] = y0 - y1; g[8] = x1 - x0;
+        m->size[e] = 0.5 * (g[0] + g[1] + g[2]);  /* tri3.cc:184-189 */
+    } else {
+        const double *p0 = m->x + 3 * nd[0], *p1 = m->x + 3 * nd[1];
+        const double *p2 = m->x + 3 * nd[2], *p3 = m->x + 3 * nd[3];
+        double x0 = p0[0], y0 = p0[1], z0 = p0[2], x1 = p1[0], y1 = p1[1], z1 = p1[2];
+        double x2 = p2[0], y2 = p2[1], z2 = p2[2], x3 = p3[0], y3 = p3[1], z3 = p3[2];
+        double *a = g, *b = g + 4, *c = g + 8, *d = g + 12;
+        a[0] = x1*(y2*z3-y3*z2) - x2*(y1*z3-y3*z1) + x3*(y1*z2-y2*z1);
+        a[1] = x0*(y3*z2-y2*z3) - x2*(y3*z0-y0*z3) + x3*(y2*z0-y0*z2);
+        a[2] = x0*(y1*z3-y3*z1) - x1*(y0*z3-y3*z0) + x3*(y0*z1-y1*z0);
+        a[3] = x0*(y2*z1-y1*z2) - x1*(y2*z0-y0*z2) + x2*(y1*z0-y0*z1);
+        b[0] = y1*(z3-z2) + y2*(z1-z3) + y3*(z2-z1);
+        b[1] = y0*(z2-z3) + y2*(z3-z0) + y3*(z0-z2);
+        b[2] = y0*(z3-z1) + y1*(z0-z3) + y3*(z1-z0);
+        b[3] = y0*(z1-z2) + y1*(z2-z0) + y2*(z0-z1);
+        c[0] = x1*(z2-z3) + x2*(z3-z1) + x3*(z1-z2);
+        c[1] = x0*(z3-z2) + x2*(z0-z3) + x3*(z2-z0);
+        c[2] = x0*(z1-z3) + x1*(z3-z0) + x3*(z0-z1);
+        c[3] = x0*(z2-z1) + x1*(z0-z2) + x2*(z1-z0);
+        d[0] = x1*(y3-y2) + x2*(y1-y3) + x3*(y2-y1);
+        d[1] = x0*(y2-y3) + x2*(y3-y0) + x3*(y0-y2);
+        d[2] = x0*(y3-y1) + x1*(y0-y3) + x3*(y1-y0);
+        d[3] = x0*(y1-y2) + x1*(y2-y0) + x2*(y0-y1);
+        for (int sd = 0; sd < 4; sd++) {  /* TriangleArea, tet4.cc:15-25 */
+            const double *q1 = m->x + 3 * nd[TET_SN[sd][0]];
+            const double *q2 = m->x + 3 * nd[TET_SN[sd][1]];
+            const double *q3 = m->x + 3 * nd[TET_SN[sd][2]];
+            double aa = pt_dist(q1, q2, 3), bb = pt_dist(q2, q3, 3), cc = pt_dist(q3, q1, 3);
+            double s = 0.5 * (aa + bb + cc);
+            m->side_size[(size_t)e * 4 + sd] = sqrt(s * (s - aa) * (s - bb) * (s - cc));
+        }
+        m->size[e] = (1.0 / 6.0) * (a[0] + a[1] + a[2] + a[3]);  /* tet4.cc:1010-1013 */
+    }
+}
+
+typedef struct { int nd[3]; int el, sd; } siderec;
+
+static int side_cmp(const void *a, const void *b)
+{
+    const siderec *s1 = a, *s2 = b;
+    for (int k = 0; k < 3; k++) {
+        if (s1->nd[k] < s2->nd[k]) return -1;
+        if (s1->nd[k] > s2->nd[k]) return 1;
+    }
+    return 0;
+}
+
+/* Mesh::MarkBoundary (mesh.cc:1614-1705): a side is on the boundary when no
+   other element shares it; its nodes become boundary nodes. */
+static void mark_boundary(tor_mesh *m)
+{
+    int nside = m->dim == 2 ? 3 : 4, nsn = m->dim == 2 ? 2 : 3;
+    size_t slen = (size_t)m->ne * nside;
+    siderec *sd = malloc(slen * sizeof(siderec));
+    for (int e = 0; e < m->ne; e++)
+        for (int s = 0; s < nside; s++) {
+            siderec *r = sd + (size_t)e * nside + s;
+            r->el = e; r->sd = s; r->nd[2] = -1;
+            for (int k = 0; k < nsn; k++)
+                r->nd[k] = m->el[(size_t)e * m->nn + (m->dim == 2 ? TRI_SN[s][k] : TET_SN[s][k])];
+            for (int j = 0; j < nsn - 1; j++)
+                for (int k = j + 1; k < nsn; k++)
+                    if (r->nd[j] > r->nd[k]) { int t = r->nd[j]; r->nd[j] = r->nd[k]; r->nd[k] = t; }
+        }
+    qsort(sd, slen, sizeof(siderec), side_cmp);
+    memset(m->bndnode, 0, m->n);
+    memset(m->bndside, 0, slen);
+    for (size_t i = 0; i < slen; i++) {
+        int isbnd = 1;
+        if (i > 0 && side_cmp(sd + i, sd + i - 1) == 0) isbnd = 0;
+        if (isbnd && i + 1 < slen && side_cmp(sd + i, sd + i + 1) == 0) isbnd = 0;
+        if (isbnd) {
+            m->bndside[(size_t)sd[i].el * nside + sd[i].sd] = 1;
+            for (int k = 0; k < nsn; k++) m->bndnode[sd[i].nd[k]] = 1;
+        }
+    }
+    free(sd);
+}
+
+/* Element_Unstructured::PostInitialisation (element.cc:540-545):
+   intdd = ComputeIntDD, intbff = ComputeBndIntFF. */
+static void element_tables(tor_mesh *m, int e)
+{
+    int nn = m->nn;
+    double *dd = m->intdd + (size_t)e * nn * nn, *bff = m->intbff + (size_t)e * nn * nn;
+    const double *g = m->geo + (size_t)e * 16;
+    double sz = m->size[e];
+    memset(bff, 0, sizeof(double) * nn * nn);
+    if (m->dim == 2) {
+        const double *b = g + 3, *c = g + 6;
+        double scale = 0.25 / sz;  /* tri3.cc:490-506 */
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j <= i; j++)
+                dd[i * 3 + j] = dd[j * 3 + i] = scale * (b[i] * b[j] + c[i] * c[j]);
+        const int *nd = m->el + (size_t)e * 3;
+        for (int s = 0; s < 3; s++) {  /* tri3.cc:561-582 */
+            if (!m->bndside[(size_t)e * 3 + s]) continue;
+            int n0 = TRI_SN[s][0], n1 = TRI_SN[s][1];
+            double dx = m->x[2 * nd[n0]] - m->x[2 * nd[n1]];
+            double dy = m->x[2 * nd[n0] + 1] - m->x[2 * nd[n1] + 1];
+            double d = hypot(dx, dy);
+            for (int i = 0; i < 3; i++) {
+                if (i != n0 && i != n1) continue;
+                bff[i * 3 + i] += d / 3.0;
+                for (int j = 0; j < i; j++)
+                    if (j == n0 || j == n1) bff[i * 3 + j] += d / 6.0;
+            }
+        }
+        for (int i = 0; i < 3; i++) for (int j = 0; j < i; j++) bff[j * 3 + i] = bff[i * 3 + j];
+    } else {
+        const double *b = g + 4, *c = g + 8, *d = g + 12;
+        double scale = 1.0 / (36.0 * sz);  /* tet4.cc:1016-1031 */
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j <= i; j++)
+                dd[i * 4 + j] = dd[j * 4 + i] = scale * (b[j] * b[i] + c[j] * c[i] + d[j] * d[i]);
+        /* ComputeBndIntFF (tet4.cc:1109-1122) with sym_bndintff tables (1039-1068) */
+        static const int T[4][4][4] = {
+            {{2,1,1,0},{1,2,1,0},{1,1,2,0},{0,0,0,0}},
+            {{2,1,0,1},{1,2,0,1},{0,0,0,0},{1,1,0,2}},
+            {{2,0,1,1},{0,0,0,0},{1,0,2,1},{1,0,1,2}},
+            {{0,0,0,0},{0,2,1,1},{0,1,2,1},{0,1,1,2}}};
+        for (int s = 0; s < 4; s++) {
+            if (!m->bndside[(size_t)e * 4 + s]) continue;
+            double ss = m->side_size[(size_t)e * 4 + s];
+            for (int i = 0; i < 4; i++)
+                for (int j = 0; j < 4; j++)
+                    bff[i * 4 + j] += (T[s][i][j] * (2.0 / 24.0)) * ss;
+        }
+    }
+}
+
+typedef struct { int n1, n2; } ipair;
+static int ipair_cmp(const void *a, const void *b)
+{
+    const ipair *p = a, *q = b;
+    if (p->n1 != q->n1) return p->n1 < q->n1 ? -1 : 1;
+    if (p->n2 != q->n2) return p->n2 < q->n2 ? -1 : 1;
+    return 0;
+}
+
+/* Mesh::SparseRowStructure (mesh.cc:422-549): all node pairs that share an
+   element, sorted by (row, col) and deduplicated, diagonal included. */
+static void csr_pattern(tor_mesh *m)
+{
+    size_t np = (size_t)m->ne * m->nn * m->nn, p = 0;
+    ipair *pr = malloc(np * sizeof(ipair));
+    for (int e = 0; e < m->ne; e++)
+        for (int i = 0; i < m->nn; i++)
+            for (int j = 0; j < m->nn; j++) {
+                pr[p].n1 = m->el[(size_t)e * m->nn + i];
+                pr[p].n2 = m->el[(size_t)e * m->nn + j];
+                p++;
+            }
+    qsort(pr, np, sizeof(ipair), ipair_cmp);
+    size_t nz = 0;
+    for (size_t i = 0; i < np; i++)
+        if (i == 0 || ipair_cmp(pr + i, pr + nz - 1) != 0) pr[nz++] = pr[i];
+    m->nnz = (int)nz;
+    m->rowptr = calloc(m->n + 1, sizeof(int));
+    m->colidx = malloc(nz * sizeof(int));
+    for (size_t i = 0; i < nz; i++) { m->rowptr[pr[i].n1 + 1]++; m->colidx[i] = pr[i].n2; }
+    for (int i = 0; i < m->n; i++) m->rowptr[i + 1] += m->rowptr[i];
+    free(pr);
+}
+
+tor_mesh *tor_mesh_create(int dim, int n, const double *coords, int ne, const int *elnodes)
+{
+    tor_mesh *m = calloc(1, sizeof(tor_mesh));
+    m->dim = dim; m->n = n; m->ne = ne; m->nn = dim == 2 ? 3 : 4;
+    int nside = dim == 2 ? 3 : 4;
+    m->x = malloc(sizeof(double) * n * dim);
+    memcpy(m->x, coords, sizeof(double) * n * dim);
+    m->el = malloc(sizeof(int) * ne * m->nn);
+    memcpy(m->el, elnodes, sizeof(int) * ne * m->nn);
+    m->geo = calloc((size_t)ne * 16, sizeof(double));
+    m->size = calloc(ne, sizeof(double));
+    m->side_size = calloc((size_t)ne * 4, sizeof(double));
+    m->bndside = calloc((size_t)ne * nside, 1);
+    m->bndnode = calloc(n, 1);
+    m->intdd = calloc((size_t)ne * m->nn * m->nn, sizeof(double));
+    m->intbff = calloc((size_t)ne * m->nn * m->nn, sizeof(double));
+    for (int e = 0; e < ne; e++) element_geometry(m, e);  /* Mesh::Setup, mesh.cc:96-158 */
+    mark_boundary(m);
+    for (int e = 0; e < ne; e++) element_tables(m, e);
+    csr_pattern(m);
+    return m;
+}
+
+void tor_mesh_free(tor_mesh *m)
+{
+    if (!m) return;
+    free(m->x); free(m->el); free(m->geo); free(m->size); free(m->side_size);
+    free(m->bndside); free(m->bndnode); free(m->intdd); free(m->intbff);
+    free(m->rowptr); free(m->colidx); free(m);
+}
+
+int tor_mesh_nnz(const tor_mesh *m) { return m->nnz; }
+void tor_mesh_csr(const tor_mesh *m, int *rowptr, int *colidx)
+{
+    memcpy(rowptr, m->rowptr, sizeof(int) * (m->n + 1));
+    memcpy(colidx, m->colidx, sizeof(int) * m->nnz);
+}
+void tor_mesh_bndnodes(const tor_mesh *m, unsigned char *out) { memcpy(out, m->bndnode, m->n); }
+void tor_mesh_elsize(const tor_mesh *m, double *out) { memcpy(out, m->size, sizeof(double) * m->ne); }
+
+/* ------------------------------------------------------------------------ */
+/* Element integrals                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* Triangle3::IntPFF (tri3.cc:325-353) */
+static double tri_intpff(const tor_mesh *m, int e, int i, int j, const double *P)
+{
+    const int *nd = m->el + (size_t)e * 3;
+    static const double i30 = 1.0 / 30.0;
+    double sz = m->size[e];
+    double p0 = P[nd[0]], p1 = P[nd[1]], p2 = P[nd[2]];
+    if (i < j) { int t = i; i = j; j = t; }
+    switch (i * 3 + j) {
+    case 0: return sz * i30 * (3.0 * p0 + p1 + p2);
+    case 3: return sz * i30 * (p0 + p1 + 0.5 * p2);
+    case 4: return sz * i30 * (p0 + 3.0 * p1 + p2);
+    case 6: return sz * i30 * (p0 + 0.5 * p1 + p2);
+    case 7: return sz * i30 * (0.5 * p0 + p1 + p2);
+    default: return sz * i30 * (p0 + p1 + 3.0 * p2);
+    }
+}
+
+/* 4x4 planes of the Tet4 IntFFF tensor (tet4.cc:49-77), scaled by 1/120 */
+static const int TET_FFF[4][4][4] = {
+    {{6,2,2,2},{2,2,1,1},{2,1,2,1},{2,1,1,2}},
+    {{2,2,1,1},{2,6,2,2},{1,2,2,1},{1,2,1,2}},
+    {{2,1,2,1},{1,2,2,1},{2,2,6,2},{1,1,2,2}},
+    {{2,1,1,2},{1,2,1,2},{1,1,2,2},{2,2,2,6}}};
+
+/* Tetrahedron4::IntPFF (tet4.cc:371-378) */
+static double tet_intpff(const tor_mesh *m, int e, int i, int j, const double *P)
+{
+    const int *nd = m->el + (size_t)e * 4;
+    return (TET_FFF[0][i][j] / 120.0 * P[nd[0]] + TET_FFF[1][i][j] / 120.0 * P[nd[1]] +
+            TET_FFF[2][i][j] / 120.0 * P[nd[2]] + TET_FFF[3][i][j] / 120.0 * P[nd[3]]) * m->size[e];
+}
+
+/* Tetrahedron4::IntFDD (tet4.cc:380-412), independent of the first index */
+static double tet_intfdd(const tor_mesh *m, int e, int j, int k)
+{
+    if (j > k) { int t = j; j = k; k = t; }
+    const double *g = m->geo + (size_t)e * 16;
+    const double *b = g + 4, *c = g + 8, *d = g + 12;
+    double scale = 1.0 / (144.0 * m->size[e]);
+    return (b[j] * b[k] + c[j] * c[k] + d[j] * d[k]) * scale;
+}
+
+/* Element IntPDD: tri3.h:208-209 and tet4.cc:414-419 */
+static double el_intpdd(const tor_mesh *m, int e, int i, int j, const double *P)
+{
+    const int *nd = m->el + (size_t)e * m->nn;
+    if (m->dim == 2)
+        return m->intdd[(size_t)e * 9 + i * 3 + j] * ((P[nd[0]] + P[nd[1]] + P[nd[2]]) / 3.0);
+    double res = 0.0;
+    for (int k = 0; k < 4; k++) res += P[nd[k]];
+    return res * tet_intfdd(m, e, i, j);
+}
+
+/* Element BndIntPFF: tri3.h:217-218 (intbff x nodal mean) and tet4.cc:819-832
+   (exact face integral) */
+static const int TET_BFFF[4][4][4][4] = {
+    { {{6,2,2,0},{2,2,1,0},{2,1,2,0},{0,0,0,0}}, {{2,2,1,0},{2,6,2,0},{1,2,2,0},{0,0,0,0}},
+      {{2,1,2,0},{1,2,2,0},{2,2,6,0},{0,0,0,0}}, {{0}} },
+    { {{6,2,0,2},{2,2,0,1},{0,0,0,0},{2,1,0,2}}, {{2,2,0,1},{2,6,0,2},{0,0,0,0},{1,2,0,2}},
+      {{0}}, {{2,1,0,2},{1,2,0,2},{0,0,0,0},{2,2,0,6}} },
+    { {{6,0,2,2},{0,0,0,0},{2,0,2,1},{2,0,1,2}}, {{0}},
+      {{2,0,2,1},{0,0,0,0},{2,0,6,2},{1,0,2,2}}, {{2,0,1,2},{0,0,0,0},{1,0,2,2},{2,0,2,6}} },
+    { {{0}}, {{0,0,0,0},{0,6,2,2},{0,2,2,1},{0,2,1,2}},
+      {{0,0,0,0},{0,2,2,1},{0,2,6,2},{0,1,2,2}}, {{0,0,0,0},{0,2,1,2},{0,1,2,2},{0,2,2,6}} } };
+
+static double el_bndintpff(const tor_mesh *m, int e, int i, int j, const double *P)
+{
+    const int *nd = m->el + (size_t)e * m->nn;
+    if (m->dim == 2)
+        return m->intbff[(size_t)e * 9 + i * 3 + j] * ((P[nd[0]] + P[nd[1]] + P[nd[2]]) / 3.0);
+    double res = 0.0;
+    int any = 0;
+    for (int sd = 0; sd < 4; sd++) any |= m->bndside[(size_t)e * 4 + sd];
+    if (!any) return 0.0;
+    for (int sd = 0; sd < 4; sd++) {
+        if (!m->bndside[(size_t)e * 4 + sd]) continue;
+        double sres = 0.0;
+        for (int k = 0; k < 4; k++) sres += P[nd[k]] * (TET_BFFF[sd][k][i][j] * (2.0 / 120.0));
+        res += sres * m->side_size[(size_t)e * 4 + sd];
+    }
+    return res;
+}
+
+/* Element IntFF(i,j): tri3.cc:285-292 (full_intff * size), tet4.cc:348-355 */
+static double el_intff(const tor_mesh *m, int e, int i, int j)
+{
+    if (m->dim == 2) return ((i == j ? 2.0 : 1.0) * (1.0 / 12.0)) * m->size[e];
+    return ((i == j ? 2.0 : 1.0) * (1.0 / 20.0)) * m->size[e];
+}
+
+/* Element IntFFF(i,j,k): tri3.cc:294-297 (intfff_scale table), tet4.cc:357-361 */
+static double el_intfff(const tor_mesh *m, int e, int i, int j, int k)
+{
+    if (m->dim == 2) {
+        static const int idx[3][3][3] = {
+            {{2,1,1},{1,1,0},{1,0,1}},{{1,1,0},{1,2,1},{0,1,1}},{{1,0,1},{0,1,1},{1,1,2}}};
+        static const double scl[3] = {1.0 / 60.0, 1.0 / 30.0, 1.0 / 10.0};
+        return m->size[e] * scl[idx[i][j][k]];
+    }
+    return TET_FFF[i][j][k] / 120.0 * m->size[e];
+}
+
+/* Element IntFDD(i,j,k): tri3.h:196-197 (intdd * 0.3333333333), tet4.cc:380-412 */
+static double el_intfdd(const tor_mesh *m, int e, int i, int j, int k)
+{
+    (void)i;
+    if (m->dim == 2) return m->intdd[(size_t)e * 9 + j * 3 + k] * 0.3333333333;
+    return tet_intfdd(m, e, j, k);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Assembly: TFwdSolver::AssembleSystemMatrix (fwdsolver.cc:337-357 real,    */
+/* 404-424 complex) via AddToSysMatrix/AddToElMatrix (mesh.cc:1958-2282).    */
+/* ------------------------------------------------------------------------ */
+
+static int csr_find(const int *rowptr, const int *colidx, int r, int c)
+{
+    int lo = rowptr[r], hi = rowptr[r + 1] - 1;
+    while (lo <= hi) {
+        int mid = (lo + hi) >> 1;
+        if (colidx[mid] == c) return mid;
+        if (colidx[mid] < c) lo = mid + 1; else hi = mid - 1;
+    }
+    return -1;
+}
+
+/* val: nnz doubles (real) or 2*nnz interleaved (complex).  Each nodal term is
+   accumulated over all elements into a zeroed temporary and then added into F,
+   the order the reference's assembly engine uses with one thread
+   (mesh.cc:2135-2167); the i*omega*IntFF term is added directly (2252-2282). */
+void tor_assemble(const tor_mesh *m, const double *cmua, const double *ckap, const double *c2a,
+                  double omega, int cplx, double *val)
+{
+    int nnz = m->nnz, nn = m->nn;
+    double *tmp = malloc(sizeof(double) * nnz);
+    memset(val, 0, sizeof(double) * nnz * (cplx ? 2 : 1));
+    for (int mode = 0; mode < 3; mode++) {
+        const double *P = mode == 0 ? cmua : mode == 1 ? ckap : c2a;
+        memset(tmp, 0, sizeof(double) * nnz);
+        for (int e = 0; e < m->ne; e++) {
+            const int *nd = m->el + (size_t)e * nn;
+            for (int i = 0; i < nn; i++)
+                for (int j = 0; j < nn; j++) {
+                    double v;
+                    if (mode == 0) v = m->dim == 2 ? tri_intpff(m, e, i, j, P) : tet_intpff(m, e, i, j, P);
+                    else if (mode == 1) v = el_intpdd(m, e, i, j, P);
+                    else v = el_bndintpff(m, e, i, j, P);
+                    tmp[csr_find(m->rowptr, m->colidx, nd[i], nd[j])] += v;
+                }
+        }
+        for (int k = 0; k < nnz; k++) val[cplx ? 2 * k : k] += tmp[k];
+    }
+    if (cplx) {
+        for (int e = 0; e < m->ne; e++) {
+            const int *nd = m->el + (size_t)e * nn;
+            for (int i = 0; i < nn; i++)
+                for (int j = 0; j < nn; j++)
+                    val[2 * csr_find(m->rowptr, m->colidx, nd[i], nd[j]) + 1] += el_intff(m, e, i, j) * omega;
+        }
+    }
+    free(tmp);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Source and measurement vectors: QVec_Gaussian (source.cc:19-56)           */
+/* ------------------------------------------------------------------------ */
+
+void tor_qvec_gaussian(const tor_mesh *m, const double *cnt, double w, int neumann, double *q)
+{
+    double w2 = w * w;
+    double fac1 = 1.0 / (sqrt(2.0 * M_PI) * w);
+    if (m->dim == 3) fac1 /= (sqrt(2.0 * M_PI) * w);
+    if (!neumann) fac1 /= (sqrt(2.0 * M_PI) * w);
+    double fac2 = -0.5 / w2;
+    memset(q, 0, sizeof(double) * m->n);
+    for (int e = 0; e < m->ne; e++) {
+        const int *nd = m->el + (size_t)e * m->nn;
+        for (int i = 0; i < m->nn; i++) {
+            int is = nd[i];
+            if (neumann && !m->bndnode[is]) continue;
+            double d = pt_dist(cnt, m->x + (size_t)is * m->dim, m->dim);
+            double s = exp(d * d * fac2) * fac1;
+            for (int j = 0; j < m->nn; j++) {
+                int js = nd[j];
+                if (neumann) {
+                    if (m->bndnode[js]) q[js] += s * m->intbff[(size_t)e * m->nn * m->nn + i * m->nn + j];
+                } else {
+                    q[js] += s * el_intff(m, e, i, j);
+                }
+            }
+        }
+    }
+}
+
+/* Mesh::PullToBoundary (mesh.cc:1052-1111) for P1 elements: project p in the
+   local coordinates of the first element around the nearest boundary node
+   whose boundary side contains the projection.  Returns 0 on success. */
+int tor_pull_to_boundary(const tor_mesh *m, const double *p, double *pshift)
+{
+    int dim = m->dim, nmin = -1;
+    double dmin = 1e10;
+    for (int k = 0; k < m->n; k++) {
+        if (!m->bndnode[k]) continue;
+        double d = pt_dist(p, m->x + (size_t)k * dim, dim);
+        if (d < dmin) { dmin = d; nmin = k; }
+    }
+    /* Triangle3::LNormal (tri3.cc:172-182), Tetrahedron4::LNormal (tet4.cc:254-266) */
+    static const double LN2[3][2] = {{0, -1}, {0.7071067814, 0.7071067814}, {-1, 0}};
+    static const double LN3[4][3] = {{0, 0, -1}, {0, -1, 0}, {-1, 0, 0},
+                                     {0.577350269, 0.577350269, 0.577350269}};
+    for (int e = 0; e < m->ne; e++) {
+        const int *nd = m->el + (size_t)e * m->nn;
+        int has = 0;
+        for (int i = 0; i < m->nn; i++) has |= nd[i] == nmin;
+        if (!has) continue;
+        const double *g = m->geo + (size_t)e * 16;
+        double ploc[3], nloc[3];
+        int nside = dim == 2 ? 3 : 4;
+        for (int sd = 0; sd < nside; sd++) {
+            int bnd = 1;  /* Element::BndSideList (element.cc:338-348) */
+            for (int k = 0; k < (dim == 2 ? 2 : 3); k++)
+                if (!m->bndnode[nd[dim == 2 ? TRI_SN[sd][k] : TET_SN[sd][k]]]) { bnd = 0; break; }
+            if (!bnd) continue;
+            const double *q0 = m->x + (size_t)nd[dim == 2 ? TRI_SN[sd][0] : TET_SN[sd][0]] * dim;
+            if (dim == 2) {  /* Triangle3::Local (tri3.cc:134-144) */
+                double scale = 1.0 / (g[0] + g[1] + g[2]);
+                ploc[0] = (g[1] + g[4] * p[0] + g[7] * p[1]) * scale;
+                ploc[1] = (g[2] + g[5] * p[0] + g[8] * p[1]) * scale;
+                nloc[0] = (g[1] + g[4] * q0[0] + g[7] * q0[1]) * scale;
+                nloc[1] = (g[2] + g[5] * q0[0] + g[8] * q0[1]) * scale;
+                double pd = (ploc[0] - nloc[0]) * LN2[sd][0] + (ploc[1] - nloc[1]) * LN2[sd][1];
+                double l0 = ploc[0] - LN2[sd][0] * pd, l1 = ploc[1] - LN2[sd][1] * pd;
+                if (l0 + 1e-8 >= 0.0 && l1 + 1e-8 >= 0.0 && l0 + l1 - 1e-8 <= 1.0) {  /* LContains, pad=true (tri3.cc:191-200) */
+                    double u[3] = {1.0 - l0 - l1, l0, l1};  /* LocalShapeF + Element::Global */
+                    for (int c = 0; c < 2; c++) {
+                        pshift[c] = 0.0;
+                        for (int j = 0; j < 3; j++) pshift[c] += u[j] * m->x[(size_t)nd[j] * 2 + c];
+                    }
+                    return 0;
+                }
+            } else {  /* Tetrahedron4::Local (tet4.cc:186-196) */
+                const double *a = g, *b = g + 4, *c = g + 8, *d = g + 12;
+                double scale = 1.0 / (a[0] + a[1] + a[2] + a[3]);
+                for (int r = 0; r < 3; r++) {
+                    ploc[r] = (a[r + 1] + b[r + 1] * p[0] + c[r + 1] * p[1] + d[r + 1] * p[2]) * scale;
+                    nloc[r] = (a[r + 1] + b[r + 1] * q0[0] + c[r + 1] * q0[1] + d[r + 1] * q0[2]) * scale;
+                }
+                double pd = 0.0;
+                for (int r = 0; r < 3; r++) pd += (ploc[r] - nloc[r]) * LN3[sd][r];
+                double l[3];
+                for (int r = 0; r < 3; r++) l[r] = ploc[r] - LN3[sd][r] * pd;
+                if (l[0] + 1e-8 >= 0.0 && l[1] + 1e-8 >= 0.0 && l[2] + 1e-8 >= 0.0 &&
+                    l[0] + l[1] + l[2] - 1e-8 <= 1.0) {  /* LContains, pad=true (tet4.cc:268-279) */
+                    double u[4] = {1.0 - l[0] - l[1] - l[2], l[0], l[1], l[2]};
+                    for (int cc = 0; cc < 3; cc++) {
+                        pshift[cc] = 0.0;
+                        for (int j = 0; j < 4; j++) pshift[cc] += u[j] * m->x[(size_t)nd[j] * 3 + cc];
+                    }
+                    return 0;
+                }
+            }
+        }
+    }
+    return 1;  /* the reference falls back to PullToBoundary_old here */
+}
+
+/* ------------------------------------------------------------------------ */
+/* Preconditioners                                                            */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    int type;             /* 0 none, 1 diag, 2 ich */
+    int n, cplx;
+    zd *idiag;            /* diag */
+    int *Lrowptr, *Lcolidx;   /* ich: strict lower pattern */
+    zd *Lval, *d;
+    int *Ccolptr, *Crowidx, *Cvofs;  /* column access of L */
+} precon_t;
+
+/* TCompRowMatrix::CalculateIncompleteCholeskyFillin (crmatrix_imp.hpp:2077-2102)
+   and IncompleteCholeskyFactorize (2166-2203) with recover=true; complex
+   comparisons use squared magnitudes (mathdef.h:128-132). */
+static void ic_factor(int n, const int *rowptr, const int *colidx, const zd *A, int cplx, precon_t *P)
+{
+    const double EPS = 1e-10;
+    int nl = 0;
+    P->Lrowptr = calloc(n + 1, sizeof(int));
+    for (int i = 0; i < n; i++) {
+        int nc = 0;
+        for (int j = rowptr[i]; j < rowptr[i + 1]; j++) { if (colidx[j] < i) nc++; else break; }
+        P->Lrowptr[i + 1] = P->Lrowptr[i] + nc;
+    }
+    nl = P->Lrowptr[n];
+    P->Lcolidx = malloc(sizeof(int) * (nl ? nl : 1));
+    for (int i = 0, c = 0; i < n; i++)
+        for (int j = rowptr[i]; j < rowptr[i + 1]; j++) { if (colidx[j] < i) P->Lcolidx[c++] = colidx[j]; else break; }
+    P->Lval = calloc(nl ? nl : 1, sizeof(zd));
+    P->d = calloc(n > 0 ? (size_t)n : 1, sizeof(zd));
+    int *Lr = P->Lrowptr, *Lc = P->Lcolidx;
+    zd *Lv = P->Lval;
+    for (int i = 0; i < n; i++) {
+        zd diag = 0;
+        int kd = csr_find(rowptr, colidx, i, i);
+        if (kd >= 0) diag = A[kd];
+        zd x = 0;
+        for (int j = Lr[i]; j < Lr[i + 1]; j++) x += Lv[j] * Lv[j];
+        int pos;
+        if (cplx) {
+            double nd = creal(diag) * creal(diag) + cimag(diag) * cimag(diag);
+            double nx = creal(x) * creal(x) + cimag(x) * cimag(x);
+            pos = nd > nx;
+        } else {
+            pos = creal(diag) > creal(x);
+        }
+        if (pos) P->d[i] = cplx ? csqrt(diag - x) : sqrt(creal(diag) - creal(x));
+        else P->d[i] = EPS;
+        for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+            int j = colidx[k];
+            if (j <= i) continue;
+            zd Aj = A[k], v;
+            if (i) {
+                /* row_mult (crmatrix_imp.hpp:1971-2009): sum_{c<i} L(i,c) L(j,c) */
+                zd s = 0;
+                int i1 = Lr[i], e1 = Lr[i + 1], i2 = Lr[j], e2 = Lr[j + 1];
+                while (i1 < e1 && i2 < e2) {
+                    int c1 = Lc[i1], c2 = Lc[i2];
+                    if (c1 > i - 1 || c2 > i - 1) break;
+                    if (c1 < c2) i1++;
+                    else if (c1 > c2) i2++;
+                    else { s += Lv[i1] * Lv[i2]; i1++; i2++; }
+                }
+                v = cplx ? (Aj - s) / P->d[i] : (creal(Aj) - creal(s)) / creal(P->d[i]);
+            } else {
+                v = cplx ? Aj / P->d[i] : creal(Aj) / creal(P->d[i]);
+            }
+            int kk = csr_find(Lr, Lc, j, i);
+            Lv[kk] = v;
+        }
+    }
+    /* SetColAccess: column view, rows ascending within each column */
+    P->Ccolptr = calloc(n + 1, sizeof(int));
+    P->Crowidx = malloc(sizeof(int) * (nl ? nl : 1));
+    P->Cvofs = malloc(sizeof(int) * (nl ? nl : 1));
+    for (int k = 0; k < nl; k++) P->Ccolptr[Lc[k] + 1]++;
+    for (int i = 0; i < n; i++) P->Ccolptr[i + 1] += P->Ccolptr[i];
+    int *fill = calloc(n, sizeof(int));
+    for (int r = 0; r < n; r++)
+        for (int k = Lr[r]; k < Lr[r + 1]; k++) {
+            int c = Lc[k], pos = P->Ccolptr[c] + fill[c]++;
+            P->Crowidx[pos] = r; P->Cvofs[pos] = k;
+        }
+    free(fill);
+}
+
+static void precon_setup(int n, const int *rowptr, const int *colidx, const zd *A, int cplx, int type, precon_t *P)
+{
+    memset(P, 0, sizeof(*P));
+    P->type = type; P->n = n; P->cplx = cplx;
+    if (type == 1) {  /* TPrecon_Diag::Reset (precon_imp.hpp:56-64) */
+        P->idiag = malloc(sizeof(zd) * n);
+        for (int i = 0; i < n; i++) {
+            int k = csr_find(rowptr, colidx, i, i);
+            zd dg = k >= 0 ? A[k] : 0;
+            P->idiag[i] = (creal(dg) != 0 || cimag(dg) != 0) ? (cplx ? 1.0 / dg : 1.0 / creal(dg)) : 1.0;
+        }
+    } else if (type == 2) {
+        ic_factor(n, rowptr, colidx, A, cplx, P);
+    }
+}
+
+static void precon_free(precon_t *P)
+{
+    free(P->idiag); free(P->Lrowptr); free(P->Lcolidx); free(P->Lval); free(P->d);
+    free(P->Ccolptr); free(P->Crowidx); free(P->Cvofs);
+}
+
+/* TPrecon_*::Apply; IC apply is CholeskySubst (crmatrix_imp.hpp:2267-2295).
+   b and x may alias. */
+static void precon_apply(const precon_t *P, const zd *b, zd *x)
+{
+    int n = P->n;
+    if (P->type == 0) { if (x != b) memcpy(x, b, sizeof(zd) * n); return; }
+    if (P->type == 1) {
+        for (int i = 0; i < n; i++) x[i] = P->cplx ? b[i] * P->idiag[i] : creal(b[i]) * creal(P->idiag[i]);
+        return;
+    }
+    const int *Lr = P->Lrowptr, *Lc = P->Lcolidx;
+    const zd *Lv = P->Lval, *d = P->d;
+    if (P->cplx) {
+        for (int i = 0; i < n; i++) {
+            zd s = b[i];
+            for (int k = Lr[i]; k < Lr[i + 1]; k++) s -= Lv[k] * x[Lc[k]];
+            x[i] = s / d[i];
+        }
+        for (int i = n - 1; i >= 0; i--) {
+            zd s = x[i];
+            for (int k = P->Ccolptr[i + 1] - 1; k >= P->Ccolptr[i]; k--) s -= Lv[P->Cvofs[k]] * x[P->Crowidx[k]];
+            x[i] = s / d[i];
+        }
+    } else {
+        for (int i = 0; i < n; i++) {
+            double s = creal(b[i]);
+            for (int k = Lr[i]; k < Lr[i + 1]; k++) s -= creal(Lv[k]) * creal(x[Lc[k]]);
+            x[i] = s / creal(d[i]);
+        }
+        for (int i = n - 1; i >= 0; i--) {
+            double s = creal(x[i]);
+            for (int k = P->Ccolptr[i + 1] - 1; k >= P->Ccolptr[i]; k--)
+                s -= creal(Lv[P->Cvofs[k]]) * creal(x[P->Crowidx[k]]);
+            x[i] = s / creal(d[i]);
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Krylov solvers                                                             */
+/* ------------------------------------------------------------------------ */
+
+typedef struct { int n; const int *rowptr, *colidx; const zd *val; int cplx; } spmat;
+
+/* TCompRowMatrix::Ax (crmatrix_imp.hpp:1172-1189) */
+static void spmv(const spmat *A, const zd *x, zd *y)
+{
+    for (int r = 0; r < A->n; r++) {
+        zd s = 0;
+        if (A->cplx) for (int k = A->rowptr[r]; k < A->rowptr[r + 1]; k++) s += A->val[k] * x[A->colidx[k]];
+        else {
+            double sr = 0;
+            for (int k = A->rowptr[r]; k < A->rowptr[r + 1]; k++) sr += creal(A->val[k]) * creal(x[A->colidx[k]]);
+            s = sr;
+        }
+        y[r] = s;
+    }
+}
+
+/* l2norm (vector_imp.hpp:1116-1120, 1290-1298): sqrt(sum |v_i|^2) with |.| = abs */
+static double l2norm(const zd *v, int n)
+{
+    double s = 0.0;
+    for (int i = 0; i < n; i++) { double t = cabs(v[i]); s += t * t; }
+    return sqrt(s);
+}
+
+/* PCG (matrix_imp.hpp:93-154), real */
+static int pcg_real(const spmat *A, const zd *bz, zd *xz, double *tol, const precon_t *P, int maxit)
+{
+    int n = A->n, niter;
+    double dnew, dold, alpha, beta, err = 0, bnorm;
+    if (!maxit) maxit = n + 1;
+    zd *r = malloc(sizeof(zd) * n), *d = malloc(sizeof(zd) * n), *q = malloc(sizeof(zd) * n);
+    spmv(A, xz, r);
+    for (int i = 0; i < n; i++) r[i] = creal(bz[i]) - creal(r[i]);
+    if (P->type) precon_apply(P, r, d); else memcpy(d, r, sizeof(zd) * n);
+    dnew = 0; for (int i = 0; i < n; i++) dnew += creal(r[i]) * creal(d[i]);
+    bnorm = l2norm(bz, n);
+    for (niter = 0; niter < maxit; niter++) {
+        spmv(A, d, q);
+        double dq = 0; for (int i = 0; i < n; i++) dq += creal(d[i]) * creal(q[i]);
+        alpha = dnew / dq;
+        if (!alpha || isnan(alpha)) break;
+        for (int i = 0; i < n; i++) xz[i] = creal(xz[i]) + creal(d[i]) * alpha;
+        for (int i = 0; i < n; i++) r[i] = creal(r[i]) - creal(q[i]) * alpha;
+        dold = dnew;
+        if (P->type) {
+            precon_apply(P, r, q);
+            dnew = 0; for (int i = 0; i < n; i++) dnew += creal(r[i]) * creal(q[i]);
+            beta = dnew / dold;
+            for (int i = 0; i < n; i++) { double t = creal(d[i]) * beta; d[i] = t + creal(q[i]); }
+        } else {
+            dnew = 0; for (int i = 0; i < n; i++) dnew += creal(r[i]) * creal(r[i]);
+            beta = dnew / dold;
+            for (int i = 0; i < n; i++) { double t = creal(d[i]) * beta; d[i] = t + creal(r[i]); }
+        }
+        if (!beta || isnan(beta)) break;
+        err = l2norm(r, n);
+        if (err <= *tol * bnorm) break;
+    }
+    *tol = err / bnorm;
+    free(r); free(d); free(q);
+    return niter;
+}
+
+/* Re(conj(a) b) summed, the scalar the reference's complex BiCGSTAB uses */
+static double redot(const zd *a, const zd *b, int n)
+{
+    double s = 0.0;
+    for (int i = 0; i < n; i++) s += creal(a[i]) * creal(b[i]) + cimag(a[i]) * cimag(b[i]);
+    return s;
+}
+
+/* BiCGSTAB, complex specialisation with real scalars (matrix_imp.hpp:350-413) */
+static int bicgstab_cplx(const spmat *A, const zd *b, zd *x, double *tol, const precon_t *P, int maxit, int *fail)
+{
+    int n = A->n, niter;
+    double err = 0, bnorm, rho = 0, rhop, alpha = 0, beta, omega = 0, aden, onum, oden;
+    if (!maxit) maxit = n + 1;
+    zd *r = malloc(sizeof(zd) * n), *rd = malloc(sizeof(zd) * n), *p = malloc(sizeof(zd) * n);
+    zd *pd = malloc(sizeof(zd) * n), *v = malloc(sizeof(zd) * n), *s = malloc(sizeof(zd) * n);
+    zd *sd = malloc(sizeof(zd) * n), *t = malloc(sizeof(zd) * n);
+    spmv(A, x, r);
+    for (int i = 0; i < n; i++) rd[i] = r[i] = b[i] - r[i];
+    bnorm = l2norm(b, n);
+    *fail = 0;
+    for (niter = 0; niter < maxit; niter++) {
+        rhop = rho;
+        rho = redot(rd, r, n);
+        if (rho == 0.0) { *fail = 1; break; }  /* xASSERT in the reference */
+        if (!niter) memcpy(p, r, sizeof(zd) * n);
+        else {
+            beta = (rho * alpha) / (rhop * omega);
+            for (int i = 0; i < n; i++) p[i] = r[i] + (p[i] - v[i] * omega) * beta;
+        }
+        precon_apply(P, p, pd);
+        spmv(A, pd, v);
+        aden = redot(rd, v, n);
+        alpha = rho / aden;
+        for (int i = 0; i < n; i++) s[i] = r[i] - v[i] * alpha;
+        precon_apply(P, s, sd);
+        spmv(A, sd, t);
+        onum = redot(t, s, n);
+        oden = redot(t, t, n);
+        omega = onum / oden;
+        for (int i = 0; i < n; i++) {
+            x[i] += pd[i] * alpha + sd[i] * omega;
+            r[i] = s[i] - t[i] * omega;
+        }
+        err = l2norm(r, n);
+        if (err <= *tol * bnorm) break;
+        if (omega == 0.0) break;
+    }
+    *tol = err / bnorm;
+    free(r); free(rd); free(p); free(pd); free(v); free(s); free(sd); free(t);
+    return niter;
+}
+
+/* BiCGSTAB, generic (real) version (matrix_imp.hpp:479-547) */
+static int bicgstab_real(const spmat *A, const zd *bz, zd *xz, double *tol, const precon_t *P, int maxit)
+{
+    int n = A->n, niter;
+    double rho = 0, alpha = 0, aden, beta, bden, omega = 0, err = 0, bnorm;
+    if (!maxit) maxit = n + 1;
+    double *r = malloc(8 * n), *rd = malloc(8 * n), *p = malloc(8 * n), *s = malloc(8 * n), *t = malloc(8 * n), *v = malloc(8 * n);
+    zd *pd = malloc(sizeof(zd) * n), *sd = malloc(sizeof(zd) * n), *tz = malloc(sizeof(zd) * n);
+    spmv(A, xz, tz);
+    for (int i = 0; i < n; i++) rd[i] = r[i] = creal(bz[i]) - creal(tz[i]);
+    bnorm = l2norm(bz, n);
+    for (niter = 0; niter < maxit; niter++) {
+        bden = rho;
+        rho = 0; for (int i = 0; i < n; i++) rho += rd[i] * r[i];
+        if (!rho) break;
+        if (!niter) memcpy(p, r, 8 * n);
+        else {
+            beta = (rho * alpha) / (bden * omega);
+            for (int i = 0; i < n; i++) p[i] = r[i] + beta * (p[i] - omega * v[i]);
+        }
+        for (int i = 0; i < n; i++) tz[i] = p[i];
+        precon_apply(P, tz, pd);
+        spmv(A, pd, tz);
+        for (int i = 0; i < n; i++) v[i] = creal(tz[i]);
+        aden = 0; for (int i = 0; i < n; i++) aden += rd[i] * v[i];
+        alpha = rho / aden;
+        for (int i = 0; i < n; i++) s[i] = r[i] - alpha * v[i];
+        err = 0; for (int i = 0; i < n; i++) err += fabs(s[i]) * fabs(s[i]);
+        err = sqrt(err);
+        if (err < *tol * bnorm) {
+            for (int i = 0; i < n; i++) xz[i] = creal(xz[i]) + alpha * creal(pd[i]);
+            break;
+        }
+        for (int i = 0; i < n; i++) tz[i] = s[i];
+        precon_apply(P, tz, sd);
+        spmv(A, sd, tz);
+        for (int i = 0; i < n; i++) t[i] = creal(tz[i]);
+        double ts = 0, tt = 0;
+        for (int i = 0; i < n; i++) ts += t[i] * s[i];
+        for (int i = 0; i < n; i++) tt += t[i] * t[i];
+        omega = ts / tt;
+        for (int i = 0; i < n; i++) {
+            xz[i] = creal(xz[i]) + (alpha * creal(pd[i]) + omega * creal(sd[i]));
+            r[i] = s[i] - omega * t[i];
+        }
+        err = 0; for (int i = 0; i < n; i++) err += fabs(r[i]) * fabs(r[i]);
+        err = sqrt(err);
+        if (err <= *tol * bnorm) break;
+        if (omega == 0.0) break;
+    }
+    *tol = err / bnorm;
+    free(r); free(rd); free(p); free(s); free(t); free(v); free(pd); free(sd); free(tz);
+    return niter;
+}
+
+/* gmres (gmres_imp.hpp:39-230), restart 20 (gsmatrix_imp.hpp:539), complex */
+static int gmres_cplx(const spmat *A, const zd *b, zd *x, double *elim, const precon_t *P, int restart, int maxit)
+{
+    int N = A->n, M = restart, MAXC = maxit ? maxit : N + 1;
+    int j, k, l, cycle;
+    double norm_b, norm_v, norm_x, tmp;
+    zd *y = calloc(M, sizeof(zd)), *s = calloc(M + 1, sizeof(zd));
+    zd *c1 = calloc(M, sizeof(zd)), *c2 = calloc(M, sizeof(zd));
+    zd *H = calloc((size_t)M * (M + 1), sizeof(zd));
+#define HH(a, b) H[(a) * (M + 1) + (b)]
+    zd **v = malloc(sizeof(zd *) * (M + 1));
+    for (j = 0; j <= M; j++) v[j] = calloc(N, sizeof(zd));
+    zd *Mb = malloc(sizeof(zd) * N), *w = malloc(sizeof(zd) * N);
+    memcpy(Mb, b, sizeof(zd) * N);
+    precon_apply(P, Mb, Mb);
+    norm_b = l2norm(Mb, N);
+    norm_x = l2norm(x, N);
+    cycle = j = 0;
+    if (norm_x < *elim * N) memcpy(v[0], Mb, sizeof(zd) * N);
+    else {
+        spmv(A, x, v[0]);
+        precon_apply(P, v[0], v[0]);
+        for (int i = 0; i < N; i++) v[0][i] = Mb[i] - v[0][i];
+    }
+    while (((norm_v = l2norm(v[0], N)) > *elim * norm_b) && (cycle < MAXC)) {
+        s[0] = norm_v;
+        for (int i = 0; i < N; i++) v[0][i] = v[0][i] / s[0];
+        j = -1;
+        cycle++;
+        while ((norm_x = cabs(s[j + 1])) > *elim * norm_b && (j < M - 1) && (cycle < MAXC)) {
+            j++;
+            zd *vj1 = v[j + 1];
+            spmv(A, v[j], w);
+            precon_apply(P, w, vj1);
+            for (k = 0; k <= j; k++) {
+                zd *vk = v[k], sum = 0;
+                for (int i = 0; i < N; i++) sum += vj1[i] * conj(vk[i]);
+                HH(j, k) = sum;
+                for (int i = 0; i < N; i++) vj1[i] -= sum * vk[i];
+            }
+            tmp = l2norm(vj1, N);
+            HH(j, j + 1) = tmp;
+            tmp = 1.0 / tmp;
+            for (int i = 0; i < N; i++) vj1[i] *= tmp;
+            for (k = 0; k < j; k++) {
+                zd h1 = c1[k] * HH(j, k) + c2[k] * HH(j, k + 1);
+                zd h2 = -c2[k] * HH(j, k) + c1[k] * HH(j, k + 1);
+                HH(j, k) = h1;
+                HH(j, k + 1) = h2;
+            }
+            zd r = csqrt(HH(j, j) * HH(j, j) + HH(j, j + 1) * HH(j, j + 1));
+            c1[j] = HH(j, j) / r;
+            c2[j] = HH(j, j + 1) / r;
+            HH(j, j) = r;
+            HH(j, j + 1) = 0.0;
+            s[j + 1] = -c2[j] * s[j];
+            s[j] = s[j] * c1[j];
+        }
+        for (l = j; l >= 0; l--) {
+            y[l] = s[l] / HH(l, l);
+            for (k = l - 1; k >= 0; k--) s[k] = s[k] - HH(l, k) * y[l];
+        }
+        for (l = j; l >= 0; l--)
+            for (int i = 0; i < N; i++) x[i] = x[i] + y[l] * v[l][i];
+        spmv(A, x, v[0]);
+        precon_apply(P, v[0], v[0]);
+        for (int i = 0; i < N; i++) v[0][i] = Mb[i] - v[0][i];
+    }
+#undef HH
+    *elim = norm_v / norm_b;
+    for (j = 0; j <= M; j++) free(v[j]);
+    free(v); free(y); free(s); free(c1); free(c2); free(H); free(Mb); free(w);
+    return cycle;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Multi-source solve: TFwdSolver::CalcFields (fwdsolver.cc:653-750), sources */
+/* split over threads in contiguous ranges like CalcFields_engine (618-643).  */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    const spmat *A; const precon_t *P;
+    int method, maxit, nrhs, q0, q1;
+    double tol;
+    const double *B; double *X; int *its; double *errs; int *fails;
+} solve_job;
+
+static void *solve_worker(void *arg)
+{
+    solve_job *J = arg;
+    int n = J->A->n;
+    zd *b = malloc(sizeof(zd) * n), *x = malloc(sizeof(zd) * n);
+    for (int q = J->q0; q < J->q1; q++) {
+        for (int i = 0; i < n; i++) {
+            if (J->A->cplx) { b[i] = J->B[2 * ((size_t)q * n + i)] + I * J->B[2 * ((size_t)q * n + i) + 1];
+                              x[i] = J->X[2 * ((size_t)q * n + i)] + I * J->X[2 * ((size_t)q * n + i) + 1]; }
+            else { b[i] = J->B[(size_t)q * n + i]; x[i] = J->X[(size_t)q * n + i]; }
+        }
+        double tol = J->tol;
+        int it = -1, fail = 0;
+        if (J->method == 0 && !J->A->cplx) it = pcg_real(J->A, b, x, &tol, J->P, J->maxit);
+        else if (J->method == 1 && J->A->cplx) it = bicgstab_cplx(J->A, b, x, &tol, J->P, J->maxit, &fail);
+        else if (J->method == 1) it = bicgstab_real(J->A, b, x, &tol, J->P, J->maxit);
+        else if (J->method == 2 && J->A->cplx) it = gmres_cplx(J->A, b, x, &tol, J->P, 20, J->maxit);
+        else fail = 2;
+        for (int i = 0; i < n; i++) {
+            if (J->A->cplx) { J->X[2 * ((size_t)q * n + i)] = creal(x[i]); J->X[2 * ((size_t)q * n + i) + 1] = cimag(x[i]); }
+            else J->X[(size_t)q * n + i] = creal(x[i]);
+        }
+        J->its[q] = it; J->errs[q] = tol; J->fails[q] = fail;
+    }
+    free(b); free(x);
+    return NULL;
+}
+
+/* method: 0 CG (real), 1 BiCGSTAB, 2 GMRES(20) (complex).  precon: 0 none,
+   1 diag, 2 IC(0).  B, X: nrhs x n (complex interleaved when cplx); X holds
+   the initial guess on entry.  Returns 0, or the number of failed solves. */
+int tor_solve(int n, const int *rowptr, const int *colidx, const double *val, int cplx,
+              int method, int precon, double tol, int maxit, int nrhs,
+              const double *B, double *X, int *its, double *errs, int nthreads)
+{
+    int nnz = rowptr[n];
+    zd *A = malloc(sizeof(zd) * (nnz ? nnz : 1));
+    for (int k = 0; k < nnz; k++) A[k] = cplx ? val[2 * k] + I * val[2 * k + 1] : val[k];
+    spmat S = {n, rowptr, colidx, A, cplx};
+    precon_t P;
+    precon_setup(n, rowptr, colidx, A, cplx, precon, &P);
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > nrhs) nthreads = nrhs > 0 ? nrhs : 1;
+    int *fails = calloc(nrhs > 0 ? nrhs : 1, sizeof(int));
+    solve_job *jobs = malloc(sizeof(solve_job) * nthreads);
+    pthread_t *th = malloc(sizeof(pthread_t) * nthreads);
+    for (int t = 0; t < nthreads; t++) {
+        solve_job j = {&S, &P, method, maxit, nrhs, (t * nrhs) / nthreads, ((t + 1) * nrhs) / nthreads,
+                       tol, B, X, its, errs, fails};
+        jobs[t] = j;
+        if (nthreads > 1) pthread_create(&th[t], NULL, solve_worker, &jobs[t]);
+        else solve_worker(&jobs[t]);
+    }
+    if (nthreads > 1) for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    int nf = 0;
+    for (int q = 0; q < nrhs; q++) nf += fails[q] != 0;
+    free(fails); free(jobs); free(th); free(A);
+    precon_free(&P);
+    return nf;
+}
+
+/* IC(0) factor as a standalone entry point (for kernel-level parity tests).
+   Lrowptr: n+1, Lcolidx/Lval: nnz_L (Lval complex interleaved when cplx), d: n. */
+int tor_ic_factor(int n, const int *rowptr, const int *colidx, const double *val, int cplx,
+                  int *Lrowptr, int *Lcolidx, double *Lval, double *d)
+{
+    int nnz = rowptr[n];
+    zd *A = malloc(sizeof(zd) * (nnz ? nnz : 1));
+    for (int k = 0; k < nnz; k++) A[k] = cplx ? val[2 * k] + I * val[2 * k + 1] : val[k];
+    precon_t P;
+    precon_setup(n, rowptr, colidx, A, cplx, 2, &P);
+    int nl = P.Lrowptr[n];
+    memcpy(Lrowptr, P.Lrowptr, sizeof(int) * (n + 1));
+    memcpy(Lcolidx, P.Lcolidx, sizeof(int) * nl);
+    for (int k = 0; k < nl; k++) {
+        if (cplx) { Lval[2 * k] = creal(P.Lval[k]); Lval[2 * k + 1] = cimag(P.Lval[k]); }
+        else Lval[k] = creal(P.Lval[k]);
+    }
+    for (int i = 0; i < n; i++) {
+        if (cplx) { d[2 * i] = creal(P.d[i]); d[2 * i + 1] = cimag(P.d[i]); }
+        else d[i] = creal(P.d[i]);
+    }
+    precon_free(&P);
+    free(A);
+    return nl;
+}
+
+/* ------------------------------------------------------------------------ */
+/* ProjectAll (fwdsolver.cc:1415-1447): y_qm = dot(phi_q, mvec_m), non-       */
+/* conjugating, over the linked detectors in link order; LOG gives log(y).   */
+/* ------------------------------------------------------------------------ */
+
+void tor_project(int n, int nq, const double *phi, const double *mvec_dense, const int *link_ofs,
+                 const int *link_m, int cplx, int logscale, double *proj)
+{
+    for (int q = 0; q < nq; q++)
+        for (int l = link_ofs[q]; l < link_ofs[q + 1]; l++) {
+            int m = link_m[l];
+            if (cplx) {
+                zd s = 0;
+                for (int i = 0; i < n; i++) {
+                    zd a = phi[2 * ((size_t)q * n + i)] + I * phi[2 * ((size_t)q * n + i) + 1];
+                    zd b = mvec_dense[2 * ((size_t)m * n + i)] + I * mvec_dense[2 * ((size_t)m * n + i) + 1];
+                    s += a * b;
+                }
+                if (logscale) s = clog(s);
+                proj[2 * l] = creal(s); proj[2 * l + 1] = cimag(s);
+            } else {
+                double s = 0;
+                for (int i = 0; i < n; i++) s += phi[(size_t)q * n + i] * mvec_dense[(size_t)m * n + i];
+                proj[l] = logscale ? log(s) : s;
+            }
+        }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Nodal Jacobian: GenerateJacobian_mesh (jacobian.cc:441-497) for complex    */
+/* fields and GenerateJacobian_cw_mesh (738-802) + RowScale (160-177) for CW. */
+/* IntFG (806-835) and IntGradFGradG (839-872) are restated element by        */
+/* element with the same summation order.                                     */
+/* ------------------------------------------------------------------------ */
+
+static void intfg_pair(const tor_mesh *m, const zd *f, const zd *g, int kap, zd *tmp)
+{
+    memset(tmp, 0, sizeof(zd) * m->n);
+    for (int e = 0; e < m->ne; e++) {
+        const int *nd = m->el + (size_t)e * m->nn;
+        for (int i = 0; i < m->nn; i++) {
+            int bs = nd[i];
+            for (int j = 0; j < m->nn; j++) {
+                int nj = nd[j];
+                zd sum = (f[nj] * g[nj]) * (kap ? el_intfdd(m, e, i, j, j) : el_intfff(m, e, i, j, j));
+                for (int k = 0; k < j; k++) {
+                    int nk = nd[k];
+                    sum += (f[nj] * g[nk] + f[nk] * g[nj]) * (kap ? el_intfdd(m, e, i, j, k) : el_intfff(m, e, i, j, k));
+                }
+                tmp[bs] += sum;
+            }
+        }
+    }
+}
+
+static void intfg_pair_real(const tor_mesh *m, const double *f, const double *g, int kap, double *tmp)
+{
+    memset(tmp, 0, sizeof(double) * m->n);
+    for (int e = 0; e < m->ne; e++) {
+        const int *nd = m->el + (size_t)e * m->nn;
+        for (int i = 0; i < m->nn; i++) {
+            int bs = nd[i];
+            for (int j = 0; j < m->nn; j++) {
+                int nj = nd[j];
+                double sum = (f[nj] * g[nj]) * (kap ? el_intfdd(m, e, i, j, j) : el_intfff(m, e, i, j, j));
+                for (int k = 0; k < j; k++) {
+                    int nk = nd[k];
+                    sum += (f[nj] * g[nk] + f[nk] * g[nj]) * (kap ? el_intfdd(m, e, i, j, k) : el_intfff(m, e, i, j, k));
+                }
+                tmp[bs] += sum;
+            }
+        }
+    }
+}
+
+typedef struct {
+    const tor_mesh *m; int nq, nm, cplx, logscale, q0, q1;
+    const double *dphi, *aphi, *proj; const int *link_ofs, *link_m; double *J; int nqm;
+} jac_job;
+
+static void *jac_worker(void *arg)
+{
+    jac_job *jb = arg;
+    const tor_mesh *m = jb->m;
+    int n = m->n, nqm = jb->nqm;
+    if (jb->cplx) {
+        zd *f = malloc(sizeof(zd) * n), *g = malloc(sizeof(zd) * n);
+        zd *pm = malloc(sizeof(zd) * n), *pk = malloc(sizeof(zd) * n);
+        for (int q = jb->q0; q < jb->q1; q++) {
+            for (int i = 0; i < n; i++) f[i] = jb->dphi[2 * ((size_t)q * n + i)] + I * jb->dphi[2 * ((size_t)q * n + i) + 1];
+            for (int l = jb->link_ofs[q]; l < jb->link_ofs[q + 1]; l++) {
+                int mm = jb->link_m[l];
+                for (int i = 0; i < n; i++) g[i] = jb->aphi[2 * ((size_t)mm * n + i)] + I * jb->aphi[2 * ((size_t)mm * n + i) + 1];
+                intfg_pair(m, f, g, 0, pm);
+                intfg_pair(m, f, g, 1, pk);
+                if (jb->logscale) {
+                    zd y = jb->proj[2 * l] + I * jb->proj[2 * l + 1];
+                    for (int k = 0; k < n; k++) { pm[k] = pm[k] / y; pk[k] = pk[k] / y; }
+                }
+                double *r0 = jb->J + (size_t)l * 2 * n, *r1 = jb->J + (size_t)(l + nqm) * 2 * n;
+                for (int k = 0; k < n; k++) {
+                    r0[k] = -creal(pm[k]); r1[k] = -cimag(pm[k]);
+                    r0[k + n] = -creal(pk[k]); r1[k + n] = -cimag(pk[k]);
+                }
+            }
+        }
+        free(f); free(g); free(pm); free(pk);
+    } else {
+        double *pm = malloc(sizeof(double) * n), *pk = malloc(sizeof(double) * n);
+        for (int q = jb->q0; q < jb->q1; q++) {
+            const double *f = jb->dphi + (size_t)q * n;
+            for (int l = jb->link_ofs[q]; l < jb->link_ofs[q + 1]; l++) {
+                const double *g = jb->aphi + (size_t)jb->link_m[l] * n;
+                intfg_pair_real(m, f, g, 0, pm);
+                intfg_pair_real(m, f, g, 1, pk);
+                double sc = jb->logscale ? 1.0 / jb->proj[l] : 1.0;
+                double *rm = jb->J + (size_t)l * n, *rk = jb->J + (size_t)(nqm + l) * n;
+                for (int k = 0; k < n; k++) {
+                    rm[k] = -pm[k];
+                    rk[k] = -pk[k];
+                    if (jb->logscale) { rm[k] *= sc; rk[k] *= sc; }
+                }
+            }
+        }
+        free(pm); free(pk);
+    }
+    return NULL;
+}
+
+/* Complex: J is (2 nQM) x (2 n) row-major, rows [Re; Im], columns [mua | kappa].
+   Real (CW): J holds Jmua (nQM x n) followed by Jkap (nQM x n).
+   proj: the linear projections (complex interleaved or real) used for LOG. */
+void tor_jacobian(const tor_mesh *m, int nq, int nm, const double *dphi, const double *aphi,
+                  const double *proj, const int *link_ofs, const int *link_m, int cplx, int logscale,
+                  double *J, int nthreads)
+{
+    int nqm = link_ofs[nq];
+    (void)nm;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > nq) nthreads = nq > 0 ? nq : 1;
+    jac_job *jobs = malloc(sizeof(jac_job) * nthreads);
+    pthread_t *th = malloc(sizeof(pthread_t) * nthreads);
+    for (int t = 0; t < nthreads; t++) {
+        jac_job jb = {m, nq, nm, cplx, logscale, (t * nq) / nthreads, ((t + 1) * nq) / nthreads,
+                      dphi, aphi, proj, link_ofs, link_m, J, nqm};
+        jobs[t] = jb;
+        if (nthreads > 1) pthread_create(&th[t], NULL, jac_worker, &jobs[t]);
+        else jac_worker(&jobs[t]);
+    }
+    if (nthreads > 1) for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    free(jobs); free(th);
+}
+
+/* A_Keijzer (param.cc:24-32) */
+double tor_a_keijzer(double n)
+{
+    double th = asin(1.0 / n);
+    double costh = fabs(cos(th));
+    double R0 = ((n - 1.0) * (n - 1.0)) / ((n + 1.0) * (n + 1.0));
+    return (2.0 / (1.0 - R0) - 1.0 + costh * costh * costh) / (1.0 - costh * costh);
+}
