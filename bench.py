@@ -1,0 +1,398 @@
+"""Benchmark of the forward path on the 3D 30k-node cylinder (100 MHz).
+
+One step = one request through tg_forward_path: assembly + IC(0) factor,
+80 forward and 80 adjoint source solves (BiCGSTAB + ICH), ProjectAll (linear
+and log) and the full nodal Jacobian (12800 x 61620).  The metric is
+source-solves/s (forward + adjoint) of whole requests, so every solve carries
+its share of assembly, projection and Jacobian.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--precision mixed|fp64] [--tol T]
+
+--impl reference times the CPU restatement of the reference (oracle/, the
+reference's algorithm with threads over sources) on this host's cores, on a
+bounded sample of each request, extrapolated to whole requests.
+Prints one JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "source-solves/s (fwd+adj, whole requests incl. assembly, ProjectAll, Jacobian), 3D 30k-node cylinder 100 MHz"
+UNIT = "source-solves/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--tol", type=float, default=1e-12)
+    ap.add_argument("--no-compare", action="store_true", help="skip the FP64 comparison legs")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    return ap.parse_args()
+
+
+def problem():
+    from toastpp_gb300 import workloads
+    return workloads.cylinder(seed=0, freq_mhz=100.0)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                f = [x.strip() for x in out.stdout.strip().split(",")]
+                if len(f) >= 7:
+                    self.samples.append(f)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (oracle port; test infrastructure used here only as the baseline)
+# ---------------------------------------------------------------------------
+def cpu_request_time(P, nsrc_sample=16, nq_jac_sample=8, threads=None, tol=1e-12):
+    """Time one request on the host cores: full assembly + IC factor, a sample of
+    the source solves and of the Jacobian rows; extrapolate to the whole request."""
+    from oracle import oracle as O
+    threads = threads or os.cpu_count() or 1
+    m = O.Mesh(P.coords, P.elems)
+    cm, ck, ca = O.optical_coefficients(P.mua, P.mus, P.nref)
+    omega = P.freq_mhz * 2 * np.pi * 1e-6
+    nq, nm = P.qm.nQ, P.qm.nM
+    t0 = time.perf_counter()
+    val = m.assemble(cm, ck, ca, omega, True)
+    O.ic_factor(m.rowptr, m.colidx, val)
+    t_reset = time.perf_counter() - t0
+    rng = np.random.default_rng(7)
+    qs = rng.choice(nq, size=min(nsrc_sample, nq), replace=False)
+    ms = rng.choice(nm, size=min(nsrc_sample, nm), replace=False)
+    qvec = np.stack([m.qvec_gaussian(P.qm.Q[i], P.qwidth) for i in range(nq)]).astype(np.complex128)
+    mvec = np.stack([m.qvec_gaussian(P.qm.M[i], P.mwidth) * ca for i in range(nm)]).astype(np.complex128)
+    t0 = time.perf_counter()
+    dphi_s, itq, _ = O.solve(m.rowptr, m.colidx, val, qvec[qs], "BICGSTAB", "ICH", tol, 0, threads)
+    aphi_s, itm, _ = O.solve(m.rowptr, m.colidx, val, mvec[ms], "BICGSTAB", "ICH", tol, 0, threads)
+    t_solve = time.perf_counter() - t0
+    nsolved = len(qs) + len(ms)
+    # Jacobian sample: nq_jac_sample sources x all detectors (one thread per source)
+    jq = min(nq_jac_sample, len(qs))
+    links_ofs = np.arange(jq + 1, dtype=np.int32) * len(ms)
+    links_m = np.tile(np.arange(len(ms), dtype=np.int32), jq)
+    proj = O.project(dphi_s[:jq], mvec[ms], links_ofs, links_m, logscale=False)
+    t0 = time.perf_counter()
+    O.jacobian(m, dphi_s[:jq], aphi_s, proj, links_ofs, links_m, True, threads)
+    t_jac = time.perf_counter() - t0
+    pairs_sample = jq * len(ms)
+    t_full = t_reset + t_solve * (nq + nm) / nsolved + t_jac * (nq * nm) / pairs_sample
+    sample = (f"full assembly+IC(0) factor, {len(qs)}+{len(ms)} of {nq}+{nm} BiCGSTAB+ICH solves, "
+              f"Jacobian rows of {pairs_sample} of {nq * nm} links; extrapolated linearly to one request")
+    return dict(t_request=t_full, t_reset=t_reset, t_solve_sample=t_solve, t_jac_sample=t_jac,
+                its_per_src=float(np.mean(np.concatenate([itq, itm]))), threads=threads, sample=sample)
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    P = problem()
+    nsolves = P.qm.nQ + P.qm.nM
+    times = []
+    info = None
+    for s in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        info = cpu_request_time(P, nsrc_sample=8, nq_jac_sample=4, tol=args.tol)
+        if s >= args.warmup:
+            times.append(info["t_request"])
+    t = float(np.mean(times))
+    val = nsolves / t
+    line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "complex-f64", "data": "synthetic (seeded mesh, optodes, inclusions)",
+            "config": {"workload": "3D cylinder R25 H50, 30810 nodes, 169128 tets, 100 MHz, 80+80 optodes, "
+                                   f"BiCGSTAB+ICH tol {args.tol}, nodal Jacobian 12800x61620",
+                       "parallelism": "threads over sources (host)"},
+            "impl": "reference",
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": info["threads"], "kind": "port",
+                             "sample": info["sample"]},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from toastpp_gb300 import build as B
+    B.build()
+    from toastpp_gb300 import capi
+
+    P = problem()
+    n, nq, nm = P.n, P.qm.nQ, P.qm.nM
+    nqm = P.qm.nQM
+    gm = capi.Mesh(P.coords, P.elems)
+    cm, ck, ca = capi.optical_coefficients(P.mua, P.mus, P.nref)
+    omega = capi.omega_of(P.freq_mhz)
+    qvec = gm.qvec_gaussian(P.qm.Q, P.qwidth).astype(np.complex128)
+    mvec = (gm.qvec_gaussian(P.qm.M, P.mwidth) * ca[None, :]).astype(np.complex128)
+    links = capi.Links(P.qm.link_ofs, P.qm.link_m)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    j_fp32 = args.precision == "mixed"
+
+    def dtensor(a):
+        a = np.ascontiguousarray(a)
+        if np.iscomplexobj(a):
+            a = a.view(np.float64)
+        return torch.from_numpy(a.copy()).to(dev)
+
+    d_cm, d_ck, d_ca = dtensor(cm), dtensor(ck), dtensor(ca)
+    d_q, d_m = dtensor(qvec), dtensor(mvec)
+    d_proj = torch.empty(2 * nqm, dtype=torch.float64, device=dev)
+    d_lproj = torch.empty(2 * nqm, dtype=torch.float64, device=dev)
+    d_J = torch.empty((2 * nqm, 2 * n), dtype=torch.float32 if j_fp32 else torch.float64, device=dev)
+    torch.cuda.synchronize()
+
+    s = capi.FwdSolver(gm, "BICGSTAB", args.tol, "ICH", True, precision=args.precision)
+    s.set_stream(stream.cuda_stream)
+    res = (capi.TgResult * (nq + nm))()
+
+    def step():
+        s.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, d_proj, d_lproj, d_J,
+                           j_fp32, capi.MEM_DEVICE, res)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    # timed region: device-resident inputs; J (>= 3 GB per step) flushes L2 every step
+    s.profile((1 << capi.PROF_SPMM) | (1 << capi.PROF_SWEEP) | (1 << capi.PROF_JAC) | (1 << capi.PROF_ASM)
+              | (1 << capi.PROF_PROJ))
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    l0 = capi.launch_count()
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            evs[i][0].record(stream)
+            step()
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = capi.launch_count() - l0
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = float(np.sum(step_ms))
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    prof = {c: s.profile_read(c) for c in (capi.PROF_SPMM, capi.PROF_SWEEP, capi.PROF_JAC, capi.PROF_ASM,
+                                           capi.PROF_PROJ)}
+    s.profile(0)
+    its = [r.it_count for r in res]
+    nsolves = nq + nm
+    value = ws * nsolves * args.steps / (total_ms / 1e3)
+
+    # roofline of the dominant class (algorithmic bytes per launch / event-timed duration)
+    mdev = gm
+    nnz = mdev.nnz
+    k_f = nq
+    names = {capi.PROF_SPMM: "spmm_dot_kernel (complex FP32 SpMM k=80)", capi.PROF_SWEEP: "IC(0) level sweeps",
+             capi.PROF_JAC: "jacobian_kernel", capi.PROF_ASM: "assembly + IC(0) factor",
+             capi.PROF_PROJ: "project_kernel"}
+    dom = max(prof, key=lambda c: prof[c][0])
+    vb = 8 if args.precision == "mixed" else 16
+    jb = 4 if j_fp32 else 8
+    if dom == capi.PROF_JAC:
+        # J write + fields read once + CSR pattern (per launch)
+        alg_bytes = 2 * nqm * 2 * n * jb + (nq + nm) * n * vb + (n + 1 + nnz) * 4
+    elif dom == capi.PROF_SPMM:
+        alg_bytes = nnz * (vb + 4) + 4 * (n + 1) + 2 * n * k_f * vb
+    else:
+        alg_bytes = None
+    dom_ms, dom_cnt = prof[dom]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    roof = None
+    if alg_bytes and dom_cnt:
+        ach = alg_bytes / (dom_ms / dom_cnt / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": names[dom], "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                "traffic": None, "algorithmic_bytes_per_launch": alg_bytes,
+                "launch_ms": dom_ms / dom_cnt}
+    shares = {names[c]: {"ms_per_step": prof[c][0] / args.steps, "launches_or_scopes": prof[c][1]}
+              for c in prof}
+
+    # ---- e2e through the C ABI with host buffers (pinned), copies inside the timed region
+    e2e = None
+    if rank == 0 or ws > 1:
+        h_cm, h_ck, h_ca = (torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for x in (cm, ck, ca))
+        h_q = torch.from_numpy(qvec.view(np.float64).copy()).pin_memory()
+        h_m = torch.from_numpy(mvec.view(np.float64).copy()).pin_memory()
+        h_proj = torch.empty(2 * nqm, dtype=torch.float64).pin_memory()
+        h_lproj = torch.empty(2 * nqm, dtype=torch.float64).pin_memory()
+        h_J = torch.empty((2 * nqm, 2 * n), dtype=torch.float32 if j_fp32 else torch.float64).pin_memory()
+        ksteps = max(1, min(args.steps, 3))
+        s.forward_path_raw(h_cm, h_ck, h_ca, omega, nq, h_q, nm, h_m, links, None, None, h_proj, h_lproj, h_J,
+                           j_fp32, capi.MEM_HOST)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ksteps):
+            s.forward_path_raw(h_cm, h_ck, h_ca, omega, nq, h_q, nm, h_m, links, None, None, h_proj, h_lproj, h_J,
+                               j_fp32, capi.MEM_HOST)
+        torch.cuda.synchronize()
+        te = time.perf_counter() - t0
+        h2d = 3 * n * 8 + (nq + nm) * n * 16 + (nq + 1 + nqm) * 4
+        d2h = 2 * nqm * 16 + h_J.numel() * h_J.element_size()
+        e2e = {"value": ws * nsolves * ksteps / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "steps": ksteps}
+
+    line = None
+    if rank == 0:
+        # ---- FP64 comparison legs (same request, plain FP64)
+        compare = {}
+        if not args.no_compare:
+            s64 = capi.FwdSolver(gm, "BICGSTAB", args.tol, "ICH", True, precision="fp64")
+            s64.set_stream(stream.cuda_stream)
+            d_J64 = torch.empty((2 * nqm, 2 * n), dtype=torch.float64, device=dev)
+            p64 = torch.empty_like(d_proj)
+            lp64 = torch.empty_like(d_lproj)
+            s64.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, p64, lp64, d_J64, 0,
+                                 capi.MEM_DEVICE)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            s64.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, p64, lp64, d_J64, 0,
+                                 capi.MEM_DEVICE)
+            b.record(stream)
+            torch.cuda.synchronize()
+            t64 = a.elapsed_time(b) / 1e3
+            compare["fp64_batched"] = {"value": nsolves / t64, "unit": UNIT, "ms_per_request": t64 * 1e3}
+            # boundary-data agreement of the measured path with plain FP64 (same tolerance)
+            lp = d_lproj.cpu().numpy().view(np.complex128)
+            lr = lp64.cpu().numpy().view(np.complex128)
+            cm_err = float(np.max(np.abs(lp - lr) / np.maximum(np.abs(lp), np.abs(lr))))
+            l2_err = float(np.linalg.norm(d_proj.cpu().numpy() - p64.cpu().numpy()) / np.linalg.norm(p64.cpu().numpy()))
+            compare["boundary_data_err_vs_fp64"] = {"cmpvec_max_rel_log": cm_err, "l2_rel_linear": l2_err}
+            Jm = d_J.float().cpu()
+            J64 = d_J64.cpu()
+            compare["jacobian_err_vs_fp64_l2"] = float(torch.linalg.norm((Jm.double() - J64).flatten()) /
+                                                       torch.linalg.norm(J64.flatten()))
+            del d_J64, Jm, J64
+            # plain per-source FP64 (one right-hand side per solve), sampled
+            s1 = capi.FwdSolver(gm, "BICGSTAB", args.tol, "ICH", True, precision="fp64")
+            s1.reset(cm, ck, ca, omega)
+            ns = 4
+            t0 = time.perf_counter()
+            for i in range(ns):
+                s1.calc_fields(qvec[i:i + 1])
+            tps = (time.perf_counter() - t0) / ns
+            compare["fp64_per_source_solve"] = {"value": 1.0 / tps, "unit": "source-solves/s (solve only)",
+                                                "sample": f"{ns} single-RHS solves"}
+            compare["speedup_vs_fp64_per_source_solve_only"] = None
+        cpu = None
+        if not args.no_cpu:
+            info = cpu_request_time(P, tol=args.tol)
+            cpu = {"value": nsolves / info["t_request"], "unit": UNIT, "cores": info["threads"], "kind": "port",
+                   "sample": info["sample"], "its_per_src": info["its_per_src"]}
+        clocks = clk.summary()
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "complex-f32 inner / complex-f64 refinement" if args.precision == "mixed" else "complex-f64",
+            "data": "synthetic (seeded mesh, optodes, inclusions)",
+            "config": {"workload": f"3D cylinder R25 H50, {n} nodes, {gm.ne} tets, 100 MHz, {nq}+{nm} optodes, "
+                                   f"BiCGSTAB+ICH tol {args.tol}, {args.precision}, nodal Jacobian "
+                                   f"{2 * nqm}x{2 * n} ({'fp32' if j_fp32 else 'fp64'})",
+                       "parallelism": f"replicas x{ws} (one request per GPU)",
+                       "l2": "each step writes the >=3 GB Jacobian, larger than L2"},
+            "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+            "jacobians_per_s": ws * args.steps / (total_ms / 1e3),
+            "iterations_per_source": float(np.mean(its)),
+            "roofline": roof, "kernel_time_per_step": shares,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clocks, "wall_s": wall, "compare": compare,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,164 @@
+/*
+ * toastgpu.h -- C ABI of the GB300 forward-path library (libtoastgpu.so).
+ *
+ * Drop-in boundary for Toast++'s FEM diffusion forward path.  Every entry
+ * point replaces one piece of the reference's C++ interface (paths are within
+ * the toastpp project):
+ *
+ *   tg_mesh_create        Mesh::Setup + MarkBoundary + SparseRowStructure
+ *                         (src/libfe/mesh.cc:96-158, 1614-1705, 422-549)
+ *   tg_solver_create      TFwdSolver<T>::TFwdSolver(mesh, solver, tol) + SetPrecon
+ *                         + Allocate (src/libstoast/fwdsolver.h:85-104, 140, 229;
+ *                         fwdsolver.cc:17-34, 143-153, 156-292)
+ *   tg_solver_set         SetLinSolver / SetLinSolverMaxit (fwdsolver.h:187, 208)
+ *   tg_solver_reset       TFwdSolver<T>::Reset = AssembleSystemMatrix + precon->Reset
+ *                         (fwdsolver.cc:337-357, 404-424, 467-505)
+ *   tg_solver_matrix      read access to TFwdSolver::F (fwdsolver.h:393-409)
+ *   tg_calc_fields        TFwdSolver<T>::CalcFields (fwdsolver.cc:653-750)
+ *   tg_project_all        ProjectAll (fwdsolver.h:44-47, fwdsolver.cc:1415-1447)
+ *   tg_jacobian           GenerateJacobian(raster=0, ...) nodal basis
+ *                         (src/libstoast/jacobian.h:62-82, jacobian.cc:441-497) and
+ *                         GenerateJacobian_cw (jacobian.h:101-147, jacobian.cc:132-196, 738-802)
+ *   tg_qvec_gaussian      QVec_Gaussian (src/libstoast/source.cc:19-56)
+ *   tg_forward_path       the caller sequence of CalcJacobian / CalcJacobianCW
+ *                         (src/python/toastmodule.cc:1514-1574, 1630-1684) in one call
+ *
+ * Conventions
+ *   - Every function returns TG_OK (0) or an error code; tg_last_error() gives
+ *     the message of the calling thread's last error.  Nothing calls exit().
+ *     (The reference reports errors through xERROR -> exit(1), error.cc:37-70.)
+ *   - Node and element indices are 0-based, int32.  Elements: 3-noded
+ *     triangles (dim 2) or 4-noded tetrahedra (dim 3), positively oriented.
+ *   - Complex arrays are interleaved (re, im) doubles.
+ *   - Fields and source vectors are source-major: array[q * n + i] (one
+ *     TVector<T> per source, as CalcFields takes TVector<T> phi[nQ]).
+ *   - mem = TG_MEM_HOST: pointers are host memory (the library copies);
+ *     mem = TG_MEM_DEVICE: pointers are device memory of the current device.
+ *   - A tg_solver serialises its own calls on its CUDA stream; distinct
+ *     solvers may be used from distinct host threads.
+ */
+#ifndef TOASTGPU_H
+#define TOASTGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TG_OK 0
+#define TG_ERR_ARG 1           /* invalid argument */
+#define TG_ERR_STATE 2         /* call out of order (e.g. solve before reset) */
+#define TG_ERR_CUDA 3          /* CUDA runtime error */
+#define TG_ERR_NOMEM 4         /* device allocation failed */
+#define TG_ERR_UNSUPPORTED 5   /* combination not implemented */
+#define TG_ERR_BREAKDOWN 6     /* a Krylov solve broke down (rho == 0) */
+
+/* LSOLVER / ITMETHOD values (fwdsolver.h:19-21, gsmatrix.h:43-44) */
+#define TG_SOLVER_CG 0
+#define TG_SOLVER_BICGSTAB 1
+#define TG_SOLVER_GMRES 2
+
+/* PreconType (src/libmath/precon.h:23-32).  DILU is accepted and, as in
+   TFwdSolver::Allocate (fwdsolver.cc:149-153), solved without a preconditioner. */
+#define TG_PRECON_NONE 0
+#define TG_PRECON_DIAG 1
+#define TG_PRECON_ICH 2
+#define TG_PRECON_DILU 3
+
+/* arithmetic of the solve: FP64 throughout, or FP32/complex-FP32 inner solves
+   inside FP64 iterative refinement */
+#define TG_PREC_FP64 0
+#define TG_PREC_MIXED 1
+
+#define TG_MEM_HOST 0
+#define TG_MEM_DEVICE 1
+
+/* DataScale (fwdsolver.h:28-30) */
+#define TG_DATA_LIN 1
+#define TG_DATA_LOG 2
+
+typedef struct tg_mesh_s *tg_mesh;
+typedef struct tg_solver_s *tg_solver;
+
+/* IterativeSolverResult (src/libmath/matrix.h:34-37), per right-hand side */
+typedef struct {
+    int it_count;      /* iterations (inner iterations summed for the mixed path) */
+    int status;        /* 0 converged, 1 maxit reached, 2 breakdown */
+    double rel_err;    /* final |r| / |b| */
+} tg_result;
+
+/* ---- mesh ---------------------------------------------------------------- */
+int tg_mesh_create(int dim, int n, const double *coords, int ne, const int *elnodes, tg_mesh *out);
+int tg_mesh_destroy(tg_mesh mesh);
+/* n, ne, nnz of the CSR pattern, number of boundary nodes, IC(0) levels
+   (forward and backward sweep depth) */
+int tg_mesh_info(tg_mesh mesh, int *n, int *ne, int *nnz, int *nbnd, int *nlev_fwd, int *nlev_bwd);
+int tg_mesh_csr(tg_mesh mesh, int *rowptr, int *colidx);
+int tg_mesh_boundary(tg_mesh mesh, unsigned char *bndnode);
+/* QVec_Gaussian for npos centres (pos: npos x dim); Neumann mode reproduces the
+   boundary source of source.cc:19-56.  out: npos x n, host memory. */
+int tg_qvec_gaussian(tg_mesh mesh, int npos, const double *pos, double width, int neumann, double *out);
+
+/* ---- forward solver ------------------------------------------------------ */
+int tg_solver_create(tg_mesh mesh, int is_complex, int method, int precon, double tol, int maxit,
+                     int precision, tg_solver *out);
+int tg_solver_destroy(tg_solver s);
+int tg_solver_set(tg_solver s, double tol, int maxit);
+/* a cudaStream_t; 0 selects the solver's own stream */
+int tg_solver_set_stream(tg_solver s, void *stream);
+int tg_solver_sync(tg_solver s);
+/* Reset(sol, omega): nodal cmua, ckappa, c2a (length n); omega in rad/ps
+   (0 for real systems).  Assembles F and factors the preconditioner on the GPU. */
+int tg_solver_reset(tg_solver s, const double *cmua, const double *ckappa, const double *c2a,
+                    double omega, int mem);
+/* copy of the assembled system matrix values in CSR order (nnz reals or
+   nnz complex) */
+int tg_solver_matrix(tg_solver s, double *val, int mem);
+/* CalcFields: solve F phi_q = qvec_q for nrhs right-hand sides.  phi holds
+   the initial guess on entry (zeros, as CalcFields callers allocate it).
+   res (host, optional): per right-hand side result. */
+int tg_calc_fields(tg_solver s, int nrhs, const double *qvec, double *phi, int mem, tg_result *res);
+/* ProjectAll: proj[l] = dot(phi_q, mvec_m) (non-conjugating) for link l of
+   source q with detector m = link_m[l], l in [link_ofs[q], link_ofs[q+1]);
+   scale = TG_DATA_LOG returns log (complex log: Re = ln|y|, Im = arg y). */
+int tg_project_all(tg_solver s, int nq, const double *phi, int nm, const double *mvec,
+                   const int *link_ofs, const int *link_m, int scale, double *proj, int mem);
+/* Nodal-basis Jacobian.  Complex: J is (2 nQM) x (2 n) row-major, rows
+   [Re; Im] of -PMDF, columns [mua | kappa].  Real (CW): J is Jmua (nQM x n)
+   followed by Jkap (nQM x n).  With scale = TG_DATA_LOG each row is divided by
+   the linear projection proj[l] (complex for complex systems).
+   out_fp32 != 0 stores J as float instead of double. */
+int tg_jacobian(tg_solver s, int nq, const double *dphi, int nm, const double *aphi,
+                const double *proj, const int *link_ofs, const int *link_m, int scale,
+                void *J, int out_fp32, int mem);
+
+/* The whole path for one request: Reset, CalcFields(qvec), CalcFields(mvec),
+   ProjectAll (LIN and LOG) and the Jacobian, on the solver's stream.  Any of
+   dphi/aphi/proj/logproj/J may be NULL to skip returning it (J NULL skips the
+   Jacobian).  res: 2*nq... per-source results, forward then adjoint (host). */
+int tg_forward_path(tg_solver s, const double *cmua, const double *ckappa, const double *c2a,
+                    double omega, int nq, const double *qvec, int nm, const double *mvec,
+                    const int *link_ofs, const int *link_m, double *dphi, double *aphi,
+                    double *proj, double *logproj, void *J, int j_fp32, int mem, tg_result *res);
+
+/* ---- measurement (no counterpart in the reference: its timing is
+   tic/toc/walltic around calls, src/libmath/timing.h:4-20) ----------------- */
+/* kernel classes for tg_solver_profile's mask (bit = 1 << class) */
+#define TG_PROF_SPMM 0      /* SpMM / SpMV with fused dot partials */
+#define TG_PROF_SWEEP 1     /* one IC(0) apply: all forward + backward level kernels */
+#define TG_PROF_VEC 2       /* (reserved) */
+#define TG_PROF_JAC 3       /* the Jacobian kernel */
+#define TG_PROF_ASM 4       /* assembly + preconditioner factorisation */
+#define TG_PROF_PROJ 5      /* projection kernel */
+/* record CUDA events around the launches of the selected classes (clears the record) */
+int tg_solver_profile(tg_solver s, int mask);
+/* total device time and number of recorded launches of one class */
+int tg_solver_profile_read(tg_solver s, int cls, double *total_ms, int *count);
+/* number of kernels this library has launched in this process */
+int tg_launch_count(long long *count);
+
+const char *tg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TOASTGPU_H */

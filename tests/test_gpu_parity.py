@@ -1,0 +1,108 @@
+"""GPU path vs the CPU oracle on small seeded meshes, through the C ABI."""
+import numpy as np
+import pytest
+
+from toastpp_gb300 import capi
+from tests.gpu_util import gpu_problem_inputs, rel2, relmax, small_cyl, small_disc
+
+pytestmark = pytest.mark.gpu
+
+CASES = [("disc_cw", lambda: small_disc(0.0)), ("disc_fd", lambda: small_disc(100.0)),
+         ("cyl_cw", lambda: small_cyl(0.0)), ("cyl_fd", lambda: small_cyl(100.0))]
+
+
+@pytest.fixture(scope="module", params=CASES, ids=[c[0] for c in CASES])
+def case(request, oracle_mod):
+    P = request.param[1]()
+    om = oracle_mod.Mesh(P.coords, P.elems)
+    gm = capi.Mesh(P.coords, P.elems)
+    return P, om, gm
+
+
+def test_mesh_structure(case):
+    P, om, gm = case
+    rp, ci = gm.csr()
+    assert np.array_equal(rp, om.rowptr) and np.array_equal(ci, om.colidx)
+    assert np.array_equal(gm.boundary(), om.bnd)
+
+
+def test_source_vectors(case):
+    P, om, gm = case
+    q_gpu = gm.qvec_gaussian(P.qm.Q, P.qwidth)
+    q_ref = np.stack([om.qvec_gaussian(q, P.qwidth) for q in P.qm.Q])
+    assert relmax(q_gpu, q_ref) < 1e-14
+
+
+def test_assembly(case):
+    P, om, gm = case
+    cm, ck, ca = capi.optical_coefficients(P.mua, P.mus, P.nref)
+    omega = capi.omega_of(P.freq_mhz)
+    s = capi.FwdSolver(gm, "BICGSTAB" if P.complex else "CG", 1e-10, "ICH", P.complex)
+    s.reset(cm, ck, ca, omega)
+    F = s.system_matrix()
+    Fr = om.assemble(cm, ck, ca, omega, P.complex)
+    assert relmax(F, Fr) < 1e-13
+
+
+@pytest.mark.parametrize("precon", ["ICH", "DIAG", "NONE"])
+def test_solve_fp64(case, oracle_mod, precon):
+    P, om, gm = case
+    cm, ck, ca, qvec, mvec = gpu_problem_inputs(P, gm)
+    omega = capi.omega_of(P.freq_mhz)
+    method = "BICGSTAB" if P.complex else "CG"
+    s = capi.FwdSolver(gm, method, 1e-14, precon, P.complex)
+    s.reset(cm, ck, ca, omega)
+    phi, res = s.calc_fields(qvec)
+    val = om.assemble(cm, ck, ca, omega, P.complex)
+    Xr, its, errs = oracle_mod.solve(om.rowptr, om.colidx, val, qvec.astype(phi.dtype), method, precon, 1e-14)
+    assert rel2(phi, Xr) < 1e-10
+    assert all(r[1] == 0 for r in res), res
+    gits = np.array([r[0] for r in res])
+    assert np.all(np.abs(gits - its) <= 2), (gits, its)
+
+
+def test_project_and_jacobian(case, oracle_mod):
+    P, om, gm = case
+    cm, ck, ca, qvec, mvec = gpu_problem_inputs(P, gm)
+    omega = capi.omega_of(P.freq_mhz)
+    method = "BICGSTAB" if P.complex else "CG"
+    s = capi.FwdSolver(gm, method, 1e-13, "ICH", P.complex)
+    L = capi.Links(P.qm.link_ofs, P.qm.link_m)
+    out = s.forward_path(cm, ck, ca, omega, qvec, mvec, L)
+    ref = oracle_mod.forward_path(om, P.qm.Q, P.qm.M, P.qm.link_ofs, P.qm.link_m, P.mua, P.mus, P.nref,
+                                  P.freq_mhz, P.qwidth, P.mwidth, method, "ICH", 1e-13)
+    assert rel2(out["dphi"], ref.dphi) < 1e-10
+    assert rel2(out["aphi"], ref.aphi) < 1e-10
+    assert relmax(out["proj"], ref.proj) < 1e-9
+    assert relmax(out["logproj"], ref.logproj) < 1e-9
+    assert rel2(out["J"], ref.J) < 1e-10
+    # the stand-alone entry points agree with the fused path
+    lp = s.project_all(mvec, out["dphi"], L, capi.DATA_LOG)
+    assert relmax(lp, out["logproj"]) < 1e-13
+    J2 = s.jacobian(out["dphi"], out["aphi"], out["proj"], L)
+    assert rel2(J2, out["J"]) < 1e-13
+
+
+def test_mixed_precision_boundary_data(case, oracle_mod):
+    P, om, gm = case
+    cm, ck, ca, qvec, mvec = gpu_problem_inputs(P, gm)
+    omega = capi.omega_of(P.freq_mhz)
+    method = "BICGSTAB" if P.complex else "CG"
+    L = capi.Links(P.qm.link_ofs, P.qm.link_m)
+    # far-detector data are ~1e-7 of the near ones, so an elementwise 1e-8
+    # bound needs both solves converged to round-off (the reference's own
+    # golden tests use tol 1e-15 for the same reason)
+    s = capi.FwdSolver(gm, method, 1e-15, "ICH", P.complex, precision="mixed")
+    out = s.forward_path(cm, ck, ca, omega, qvec, mvec, L)
+    ref = oracle_mod.forward_path(om, P.qm.Q, P.qm.M, P.qm.link_ofs, P.qm.link_m, P.mua, P.mus, P.nref,
+                                  P.freq_mhz, P.qwidth, P.mwidth, method, "ICH", 1e-15, jac=True)
+    # boundary data: log amplitude within 1e-8 (cmpvec, elementwise), phase
+    # within 1e-7 (the bound of the reference's own complex golden tests,
+    # test/2D/fwdfem/Makefile:60-174), linear data within 1e-10 (L2)
+    lp, lr = np.asarray(out["logproj"]), np.asarray(ref.logproj)
+    assert relmax(lp.real, lr.real) < 1e-8
+    if P.complex:
+        assert relmax(lp.imag, lr.imag) < 1e-7
+    assert rel2(out["proj"], ref.proj) < 1e-10
+    # Jacobian from FP32 arithmetic: report-level agreement
+    assert rel2(out["J"], ref.J) < 1e-5

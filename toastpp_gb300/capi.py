@@ -1,0 +1,290 @@
+"""ctypes binding of libtoastgpu.so (include/toastgpu.h) and a Python mirror of
+the reference's TFwdSolver interface (src/libstoast/fwdsolver.h:77-508) on top
+of it.
+
+Host arrays are numpy; device arrays are anything with ``data_ptr()`` (torch
+CUDA tensors), passed with ``mem=MEM_DEVICE``.  The library must exist: there
+is no CPU fallback, and loading fails loudly when it is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtoastgpu.so")
+
+SOLVERS = {"CG": 0, "BICGSTAB": 1, "GMRES": 2}
+PRECONS = {"NONE": 0, "DIAG": 1, "ICH": 2, "DILU": 3}
+PRECISIONS = {"fp64": 0, "mixed": 1}
+MEM_HOST, MEM_DEVICE = 0, 1
+DATA_LIN, DATA_LOG = 1, 2
+
+EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
+           "tg_qvec_gaussian", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_stream",
+           "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
+           "tg_jacobian", "tg_forward_path", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count",
+           "tg_last_error"]
+PROF_SPMM, PROF_SWEEP, PROF_VEC, PROF_JAC, PROF_ASM, PROF_PROJ = range(6)
+
+
+class ToastGPUError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"toastgpu error {code}: {msg}")
+        self.code = code
+
+
+class TgResult(C.Structure):
+    _fields_ = [("it_count", C.c_int), ("status", C.c_int), ("rel_err", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with toastpp_gb300.build.build()")
+        L = C.CDLL(LIB_PATH)
+        vp, ip, dp, i_, d_ = C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_int, C.c_double
+        sig = {
+            "tg_mesh_create": [i_, i_, vp, i_, vp, C.POINTER(C.c_void_p)],
+            "tg_mesh_destroy": [vp],
+            "tg_mesh_info": [vp, ip, ip, ip, ip, ip, ip],
+            "tg_mesh_csr": [vp, vp, vp],
+            "tg_mesh_boundary": [vp, vp],
+            "tg_qvec_gaussian": [vp, i_, vp, d_, i_, vp],
+            "tg_solver_create": [vp, i_, i_, i_, d_, i_, i_, C.POINTER(C.c_void_p)],
+            "tg_solver_destroy": [vp],
+            "tg_solver_set": [vp, d_, i_],
+            "tg_solver_set_stream": [vp, vp],
+            "tg_solver_sync": [vp],
+            "tg_solver_reset": [vp, dp, dp, dp, d_, i_],
+            "tg_solver_matrix": [vp, dp, i_],
+            "tg_calc_fields": [vp, i_, dp, dp, i_, vp],
+            "tg_project_all": [vp, i_, dp, i_, dp, vp, vp, i_, dp, i_],
+            "tg_jacobian": [vp, i_, dp, i_, dp, dp, vp, vp, i_, vp, i_, i_],
+            "tg_forward_path": [vp, dp, dp, dp, d_, i_, dp, i_, dp, vp, vp, dp, dp, dp, dp, vp, i_, i_, vp],
+            "tg_solver_profile": [vp, i_],
+            "tg_solver_profile_read": [vp, i_, C.POINTER(C.c_double), ip],
+            "tg_launch_count": [C.POINTER(C.c_longlong)],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        L.tg_last_error.restype = C.c_char_p
+        L.tg_last_error.argtypes = []
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise ToastGPUError(rc, lib().tg_last_error().decode())
+
+
+def _ptr(a):
+    """Pointer of a numpy array (host) or a tensor with data_ptr() (device); None -> NULL."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return C.c_void_p(a.ctypes.data)
+
+
+def _f64(a, cplx):
+    a = np.ascontiguousarray(a, dtype=np.complex128 if cplx else np.float64)
+    return a
+
+
+class Mesh:
+    """tg_mesh: a P1 triangle or tetrahedron mesh with its CSR and IC(0) structure."""
+
+    def __init__(self, coords, elems):
+        coords = np.ascontiguousarray(coords, np.float64)
+        elems = np.ascontiguousarray(elems, np.int32)
+        self.dim = coords.shape[1]
+        self.n = coords.shape[0]
+        self.ne = elems.shape[0]
+        h = C.c_void_p()
+        _check(lib().tg_mesh_create(self.dim, self.n, _ptr(coords), self.ne, _ptr(elems), C.byref(h)))
+        self._h = h
+        v = [C.c_int() for _ in range(6)]
+        _check(lib().tg_mesh_info(self._h, *[C.byref(x) for x in v]))
+        self.nnz, self.nbnd, self.nlev_fwd, self.nlev_bwd = v[2].value, v[3].value, v[4].value, v[5].value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tg_mesh_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def csr(self):
+        rp = np.zeros(self.n + 1, np.int32)
+        ci = np.zeros(self.nnz, np.int32)
+        _check(lib().tg_mesh_csr(self._h, _ptr(rp), _ptr(ci)))
+        return rp, ci
+
+    def boundary(self):
+        b = np.zeros(self.n, np.uint8)
+        _check(lib().tg_mesh_boundary(self._h, _ptr(b)))
+        return b
+
+    def qvec_gaussian(self, pos, width, neumann=True):
+        pos = np.ascontiguousarray(np.atleast_2d(pos), np.float64)
+        out = np.zeros((pos.shape[0], self.n))
+        _check(lib().tg_qvec_gaussian(self._h, pos.shape[0], _ptr(pos), float(width), int(neumann), _ptr(out)))
+        return out
+
+
+@dataclass
+class Links:
+    """QMMesh link list: link_ofs[q]..link_ofs[q+1] index link_m (detector per measurement)."""
+
+    ofs: np.ndarray
+    m: np.ndarray
+
+    @staticmethod
+    def all_to_all(nq, nm):
+        return Links(np.arange(nq + 1, dtype=np.int32) * nm, np.tile(np.arange(nm, dtype=np.int32), nq))
+
+    @property
+    def nqm(self):
+        return int(self.ofs[-1])
+
+
+class FwdSolver:
+    """TFwdSolver<T> on the GPU: T = complex<double> when ``complex`` else double.
+
+    Names follow the reference: Reset, CalcFields, ProjectAll, plus
+    GenerateJacobian / GenerateJacobian_cw through ``jacobian``.
+    """
+
+    def __init__(self, mesh: Mesh, solver="BICGSTAB", tol=1e-10, precon="ICH", complex=True, maxit=0,
+                 precision="fp64"):
+        self.mesh = mesh
+        self.complex = bool(complex)
+        self.precision = precision
+        h = C.c_void_p()
+        _check(lib().tg_solver_create(mesh._h, int(self.complex), SOLVERS[solver.upper()], PRECONS[precon.upper()],
+                                      float(tol), int(maxit), PRECISIONS[precision], C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tg_solver_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def set_stream(self, stream_handle):
+        """Launch on an external cudaStream_t (an int handle, e.g. torch's
+        ``torch.cuda.current_stream().cuda_stream``); 0 restores the own stream."""
+        _check(lib().tg_solver_set_stream(self._h, C.c_void_p(stream_handle or None)))
+
+    def profile(self, mask):
+        _check(lib().tg_solver_profile(self._h, int(mask)))
+
+    def profile_read(self, cls):
+        ms, cnt = C.c_double(), C.c_int()
+        _check(lib().tg_solver_profile_read(self._h, int(cls), C.byref(ms), C.byref(cnt)))
+        return ms.value, cnt.value
+
+    def forward_path_raw(self, cmua, ckap, c2a, omega, nq, qvec, nm, mvec, links: Links, dphi, aphi, proj, lproj, J,
+                         j_fp32, mem, res=None):
+        """tg_forward_path with caller-owned buffers (numpy or device tensors)."""
+        _check(lib().tg_forward_path(self._h, _ptr(cmua), _ptr(ckap), _ptr(c2a), float(omega), nq, _ptr(qvec), nm,
+                                     _ptr(mvec), _ptr(links.ofs), _ptr(links.m), _ptr(dphi), _ptr(aphi), _ptr(proj),
+                                     _ptr(lproj), _ptr(J), int(j_fp32), mem, res))
+
+    def set_tol(self, tol, maxit=0):
+        _check(lib().tg_solver_set(self._h, float(tol), int(maxit)))
+
+    def reset(self, cmua, ckap, c2a, omega=0.0, mem=MEM_HOST):
+        if mem == MEM_HOST:
+            cmua, ckap, c2a = (np.ascontiguousarray(x, np.float64) for x in (cmua, ckap, c2a))
+        _check(lib().tg_solver_reset(self._h, _ptr(cmua), _ptr(ckap), _ptr(c2a), float(omega), mem))
+
+    def system_matrix(self):
+        out = np.zeros(self.mesh.nnz, np.complex128 if self.complex else np.float64)
+        _check(lib().tg_solver_matrix(self._h, _ptr(out), MEM_HOST))
+        return out
+
+    def calc_fields(self, qvec, phi0=None):
+        """Solve for every row of qvec (nrhs x n).  Returns (phi, results)."""
+        q = _f64(qvec, self.complex)
+        phi = np.zeros_like(q) if phi0 is None else _f64(phi0, self.complex).copy()
+        res = (TgResult * q.shape[0])()
+        _check(lib().tg_calc_fields(self._h, q.shape[0], _ptr(q), _ptr(phi), MEM_HOST, res))
+        return phi, [(r.it_count, r.status, r.rel_err) for r in res]
+
+    def project_all(self, mvec, phi, links: Links, scale=DATA_LOG):
+        phi = _f64(phi, self.complex)
+        mv = _f64(mvec, self.complex)
+        out = np.zeros(links.nqm, np.complex128 if self.complex else np.float64)
+        _check(lib().tg_project_all(self._h, phi.shape[0], _ptr(phi), mv.shape[0], _ptr(mv), _ptr(links.ofs),
+                                    _ptr(links.m), scale, _ptr(out), MEM_HOST))
+        return out
+
+    def jacobian(self, dphi, aphi, proj, links: Links, scale=DATA_LOG, fp32=False):
+        dphi = _f64(dphi, self.complex)
+        aphi = _f64(aphi, self.complex)
+        n, nqm = self.mesh.n, links.nqm
+        J = np.zeros((2 * nqm, 2 * n if self.complex else n), np.float32 if fp32 else np.float64)
+        pr = None if proj is None else _f64(proj, self.complex)
+        _check(lib().tg_jacobian(self._h, dphi.shape[0], _ptr(dphi), aphi.shape[0], _ptr(aphi), _ptr(pr),
+                                 _ptr(links.ofs), _ptr(links.m), scale, _ptr(J), int(fp32), MEM_HOST))
+        return J
+
+    def forward_path(self, cmua, ckap, c2a, omega, qvec, mvec, links: Links, want_fields=True, want_jac=True,
+                     j_fp32=False):
+        """One request through tg_forward_path with host buffers."""
+        q = _f64(qvec, self.complex)
+        mv = _f64(mvec, self.complex)
+        n, nq, nm, nqm = self.mesh.n, q.shape[0], mv.shape[0], links.nqm
+        dt = np.complex128 if self.complex else np.float64
+        dphi = np.zeros((nq, n), dt) if want_fields else None
+        aphi = np.zeros((nm, n), dt) if want_fields else None
+        proj = np.zeros(nqm, dt)
+        lproj = np.zeros(nqm, dt)
+        J = np.zeros((2 * nqm, 2 * n if self.complex else n), np.float32 if j_fp32 else np.float64) if want_jac else None
+        res = (TgResult * (nq + nm))()
+        cm, ck, ca = (np.ascontiguousarray(x, np.float64) for x in (cmua, ckap, c2a))
+        _check(lib().tg_forward_path(self._h, _ptr(cm), _ptr(ck), _ptr(ca), float(omega), nq, _ptr(q), nm, _ptr(mv),
+                                     _ptr(links.ofs), _ptr(links.m), _ptr(dphi), _ptr(aphi), _ptr(proj), _ptr(lproj),
+                                     _ptr(J), int(j_fp32), MEM_HOST, res))
+        its = [(r.it_count, r.status, r.rel_err) for r in res]
+        return dict(dphi=dphi, aphi=aphi, proj=proj, logproj=lproj, J=J, results=its)
+
+
+def launch_count():
+    c = C.c_longlong()
+    _check(lib().tg_launch_count(C.byref(c)))
+    return c.value
+
+
+def optical_coefficients(mua, mus, nref):
+    """cmua, ckappa, c2a from mua, mus', n (src/python/toastmodule.cc:1536-1541;
+    A_Keijzer, src/libfe/param.cc:24-32; c0 = 0.3 mm/ps)."""
+    c0 = 0.3
+    mua = np.asarray(mua, float)
+    mus = np.asarray(mus, float)
+    nref = np.asarray(nref, float)
+    th = np.arcsin(1.0 / nref)
+    costh = np.abs(np.cos(th))
+    R0 = ((nref - 1.0) * (nref - 1.0)) / ((nref + 1.0) * (nref + 1.0))
+    A = (2.0 / (1.0 - R0) - 1.0 + costh * costh * costh) / (1.0 - costh * costh)
+    return mua * c0 / nref, c0 / (3.0 * nref * (mua + mus)), c0 / (2.0 * nref * A)
+
+
+def omega_of(freq_mhz):
+    """Modulation frequency [MHz] -> omega [rad/ps] (src/supertoast/fwdfem.cc:116)."""
+    return freq_mhz * 2.0 * np.pi * 1e-6

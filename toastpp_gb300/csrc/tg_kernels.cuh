@@ -1,0 +1,609 @@
+// tg_kernels.cuh -- device kernels of the forward path.
+//
+// Block-vector layout: node-major, X[i * ld + c] (ld >= k right-hand sides).
+// Dot products that steer the Krylov methods are computed in a fixed order
+// that does not depend on how many right-hand sides share the launch: every
+// ROW_TILE-row tile of a column is summed sequentially in row order into a
+// partial (one thread per column), and the partials of a column are reduced by
+// reduce_finalize_kernel in a fixed tree.  A column therefore gets bitwise the
+// same scalars alone and inside any batch.
+#pragma once
+#include "tg_common.cuh"
+#include "tg_mesh.cuh"
+
+namespace tg {
+
+// Per-column Krylov state (one right-hand side each).  active: 1 iterating,
+// 0 finished, -1 finishing on the |s| test of the real BiCGSTAB variant.
+struct ColState {
+    double rho, rhop, alpha, omega, beta, dnew, dold, bnorm, err, tol;
+    int its, active, status, maxit;
+};
+
+// ---------------------------------------------------------------------------
+// Assembly: one thread per CSR entry gathers its element contributions in
+// element order, mode by mode, as TFwdSolver::AssembleSystemMatrix does with
+// one thread (src/libstoast/fwdsolver.cc:337-357, 404-424; AddToElMatrix,
+// src/libfe/mesh.cc:1958-2129; AddToSysMatrix iCFF, mesh.cc:2252-2282).
+// ---------------------------------------------------------------------------
+
+__constant__ int c_tet_fff[4][4][4] = {  // Tet4 IntFFF planes x120 (tet4.cc:49-77)
+    {{6,2,2,2},{2,2,1,1},{2,1,2,1},{2,1,1,2}},
+    {{2,2,1,1},{2,6,2,2},{1,2,2,1},{1,2,1,2}},
+    {{2,1,2,1},{1,2,2,1},{2,2,6,2},{1,1,2,2}},
+    {{2,1,1,2},{1,2,1,2},{1,1,2,2},{2,2,2,6}}};
+__constant__ int c_tet_bfff[4][4][4][4] = {  // Tet4 face IntFFF tables x60 (tet4.cc:724-817)
+    { {{6,2,2,0},{2,2,1,0},{2,1,2,0},{0,0,0,0}}, {{2,2,1,0},{2,6,2,0},{1,2,2,0},{0,0,0,0}},
+      {{2,1,2,0},{1,2,2,0},{2,2,6,0},{0,0,0,0}}, {{0,0,0,0},{0,0,0,0},{0,0,0,0},{0,0,0,0}} },
+    { {{6,2,0,2},{2,2,0,1},{0,0,0,0},{2,1,0,2}}, {{2,2,0,1},{2,6,0,2},{0,0,0,0},{1,2,0,2}},
+      {{0,0,0,0},{0,0,0,0},{0,0,0,0},{0,0,0,0}}, {{2,1,0,2},{1,2,0,2},{0,0,0,0},{2,2,0,6}} },
+    { {{6,0,2,2},{0,0,0,0},{2,0,2,1},{2,0,1,2}}, {{0,0,0,0},{0,0,0,0},{0,0,0,0},{0,0,0,0}},
+      {{2,0,2,1},{0,0,0,0},{2,0,6,2},{1,0,2,2}}, {{2,0,1,2},{0,0,0,0},{1,0,2,2},{2,0,2,6}} },
+    { {{0,0,0,0},{0,0,0,0},{0,0,0,0},{0,0,0,0}}, {{0,0,0,0},{0,6,2,2},{0,2,2,1},{0,2,1,2}},
+      {{0,0,0,0},{0,2,2,1},{0,2,6,2},{0,1,2,2}}, {{0,0,0,0},{0,2,1,2},{0,1,2,2},{0,2,2,6}} } };
+
+// Triangle3::IntPFF (tri3.cc:325-353)
+__device__ __forceinline__ double tri_intpff(double sz, int i, int j, double p0, double p1, double p2)
+{
+    const double i30 = 1.0 / 30.0;
+    if (i < j) { int t = i; i = j; j = t; }
+    switch (i * 3 + j) {
+    case 0: return sz * i30 * (3.0 * p0 + p1 + p2);
+    case 3: return sz * i30 * (p0 + p1 + 0.5 * p2);
+    case 4: return sz * i30 * (p0 + 3.0 * p1 + p2);
+    case 6: return sz * i30 * (p0 + 0.5 * p1 + p2);
+    case 7: return sz * i30 * (0.5 * p0 + p1 + p2);
+    default: return sz * i30 * (p0 + p1 + 3.0 * p2);
+    }
+}
+
+template <bool CPLX>
+__global__ void assemble_kernel(MeshDev m, const double* __restrict__ cmua, const double* __restrict__ ckap,
+                                const double* __restrict__ c2a, double omega, double* __restrict__ val)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.nnz) return;
+    double pff = 0.0, pdd = 0.0, bnd = 0.0, iff = 0.0;
+    for (int c = m.asm_ptr[k]; c < m.asm_ptr[k + 1]; c++) {
+        int code = m.asm_list[c];
+        int e = code >> 4, i = (code >> 2) & 3, j = code & 3;
+        const double* r = m.rec + (size_t)e * EL_REC;
+        const int* nd = m.el + (size_t)e * m.nn;
+        double sz = r[0];
+        if (m.dim == 2) {
+            pff += tri_intpff(sz, i, j, cmua[nd[0]], cmua[nd[1]], cmua[nd[2]]);
+            pdd += r[1 + i * 3 + j] * ((ckap[nd[0]] + ckap[nd[1]] + ckap[nd[2]]) / 3.0);
+            bnd += r[10 + i * 3 + j] * ((c2a[nd[0]] + c2a[nd[1]] + c2a[nd[2]]) / 3.0);
+            if (CPLX) iff += (((i == j ? 2.0 : 1.0) * (1.0 / 12.0)) * sz) * omega;
+        } else {
+            double p0 = cmua[nd[0]], p1 = cmua[nd[1]], p2 = cmua[nd[2]], p3 = cmua[nd[3]];
+            pff += (c_tet_fff[0][i][j] / 120.0 * p0 + c_tet_fff[1][i][j] / 120.0 * p1 +
+                    c_tet_fff[2][i][j] / 120.0 * p2 + c_tet_fff[3][i][j] / 120.0 * p3) * sz;
+            double res = 0.0;
+            for (int q = 0; q < 4; q++) res += ckap[nd[q]];
+            pdd += res * r[1 + i * 4 + j];
+            int mask = (int)r[21];
+            double b = 0.0;
+            if (mask) {
+                for (int sd = 0; sd < 4; sd++) {
+                    if (!(mask & (1 << sd))) continue;
+                    double sres = 0.0;
+                    for (int q = 0; q < 4; q++) sres += c2a[nd[q]] * (c_tet_bfff[sd][q][i][j] * (2.0 / 120.0));
+                    b += sres * r[17 + sd];
+                }
+            }
+            bnd += b;
+            if (CPLX) iff += (((i == j ? 2.0 : 1.0) * (1.0 / 20.0)) * sz) * omega;
+        }
+    }
+    double v = 0.0;
+    v += pff;
+    v += pdd;
+    v += bnd;
+    if (CPLX) { val[2 * k] = v; val[2 * k + 1] = iff; }
+    else val[k] = v;
+}
+
+// ---------------------------------------------------------------------------
+// IC(0) factorisation, one kernel per level of the forward dependency graph
+// (IncompleteCholeskyFactorize, src/libmath/crmatrix_imp.hpp:2166-2203, with
+// recover = true; complex pivots compared by squared magnitude,
+// src/libmath/mathdef.h:128-132).  Row i of L is complete when its level runs.
+// ---------------------------------------------------------------------------
+template <class V>
+__global__ void ic_factor_level(MeshDev m, const int* __restrict__ rows, int nrows, const V* __restrict__ A,
+                                V* __restrict__ L, V* __restrict__ dinv)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nrows) return;
+    int i = rows[t];
+    V diag = A[m.diagpos[i]];
+    V x = vzero<V>();
+    int l0 = m.Lrowptr[i], l1 = m.Lrowptr[i + 1];
+    for (int k = l0; k < l1; k++) x = vfma(x, L[k], L[k]);
+    V di;
+    bool pos = vt<V>::cplx ? (nrm2(diag) > nrm2(x)) : (re(diag) > re(x));
+    if (pos) {
+        if constexpr (vt<V>::cplx) di = csqrt_d(vsub(diag, x));
+        else di = sqrt(diag - x);
+    } else {
+        if constexpr (vt<V>::cplx) di = V{1e-10, 0.0};
+        else di = 1e-10;
+    }
+    for (int u = m.Ucolptr[i]; u < m.Ucolptr[i + 1]; u++) {
+        int j = m.Urow[u];
+        // row_mult (crmatrix_imp.hpp:1971-2009): sum over c < i of L(i,c) L(j,c)
+        V s = vzero<V>();
+        int a = l0, b = m.Lrowptr[j], be = m.Lrowptr[j + 1];
+        while (a < l1 && b < be) {
+            int ca = m.Lcolidx[a], cb = m.Lcolidx[b];
+            if (cb >= i) break;
+            if (ca < cb) a++;
+            else if (ca > cb) b++;
+            else { s = vfma(s, L[a], L[b]); a++; b++; }
+        }
+        V aij = A[m.Lapos[m.Umap[u]]];  // a_ji = a_ij (symmetric pattern and values)
+        L[m.Umap[u]] = vdiv(vsub(aij, s), di);
+    }
+    dinv[i] = vrecip(di);
+}
+
+// Lower pattern value positions: L(j,i) lives at Umap[u] for column i; its A
+// entry a_ji is at Lapos[Umap[u]].
+
+// ---------------------------------------------------------------------------
+// Level-scheduled triangular sweeps of the IC(0) apply (CholeskySubst,
+// crmatrix_imp.hpp:2267-2295): forward (L + D) y = b by rows, backward
+// (D + L^T) x = y by columns.  lane -> (row within warp group, column).
+// ---------------------------------------------------------------------------
+template <class V, class S>
+__global__ void ic_fwd_level(MeshDev m, const int* __restrict__ rows, int nrows, int k, int ld, int cw,
+                             const V* __restrict__ L, const V* __restrict__ dinv, const V* __restrict__ b,
+                             V* __restrict__ y, const ColState* __restrict__ st)
+{
+    int gw = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    int lane = threadIdx.x & 31;
+    int rpw = 32 / cw;                         // rows per warp
+    int ncg = (k + cw - 1) / cw;               // column groups
+    int item = gw * rpw + lane / cw;           // (row, column group) item
+    if (item >= nrows * ncg) return;
+    int r = item / ncg, cg = item % ncg;
+    int c = cg * cw + (lane % cw);
+    if (c >= k || (st && st[c].active != 1)) return;
+    int i = rows[r];
+    V s = b[(size_t)i * ld + c];
+    for (int q = m.Lrowptr[i]; q < m.Lrowptr[i + 1]; q++) s = vfms(s, L[q], y[(size_t)m.Lcolidx[q] * ld + c]);
+    y[(size_t)i * ld + c] = vmul(s, dinv[i]);
+}
+
+template <class V, class S>
+__global__ void ic_bwd_level(MeshDev m, const int* __restrict__ rows, int nrows, int k, int ld, int cw,
+                             const V* __restrict__ L, const V* __restrict__ dinv, V* __restrict__ x,
+                             const ColState* __restrict__ st)
+{
+    int gw = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    int lane = threadIdx.x & 31;
+    int rpw = 32 / cw;
+    int ncg = (k + cw - 1) / cw;
+    int item = gw * rpw + lane / cw;
+    if (item >= nrows * ncg) return;
+    int r = item / ncg, cg = item % ncg;
+    int c = cg * cw + (lane % cw);
+    if (c >= k || (st && st[c].active != 1)) return;
+    int i = rows[r];
+    V s = x[(size_t)i * ld + c];
+    for (int u = m.Ucolptr[i + 1] - 1; u >= m.Ucolptr[i]; u--) s = vfms(s, L[m.Umap[u]], x[(size_t)m.Urow[u] * ld + c]);
+    x[(size_t)i * ld + c] = vmul(s, dinv[i]);
+}
+
+// ---------------------------------------------------------------------------
+// SpMM y = A x with optional fused dot partials over ROW_TILE-row tiles:
+//   part0[c] = sum Re(conj(w) y)      (w != null)
+//   part1[c] = sum |y|^2              (want_n2)
+// One block per row tile.  Partials are written to part[(c * np + p) * ntiles + tile].
+// ---------------------------------------------------------------------------
+template <class V>
+__global__ void spmm_dot_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ colidx,
+                                const V* __restrict__ A, int k, int ld, const V* __restrict__ x,
+                                V* __restrict__ y, const V* __restrict__ w, bool want_n2,
+                                double* __restrict__ part, int np, int ntiles, const ColState* __restrict__ st)
+{
+    int tile = blockIdx.x;
+    int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    int cw = k >= 32 ? 32 : (k >= 16 ? 16 : (k >= 8 ? 8 : (k >= 4 ? 4 : (k >= 2 ? 2 : 1))));
+    int ncg = (k + cw - 1) / cw;
+    int rpw = 32 / cw;
+    int warp = threadIdx.x / 32, lane = threadIdx.x & 31, nwarp = blockDim.x / 32;
+    int items = (r1 - r0) * ncg;
+    for (int it = warp * rpw + lane / cw; it < items; it += nwarp * rpw) {
+        int r = r0 + it / ncg, c = (it % ncg) * cw + (lane % cw);
+        if (c >= k || (st && st[c].active != 1)) continue;
+        V s = vzero<V>();
+        for (int q = rowptr[r]; q < rowptr[r + 1]; q++) s = vfma(s, A[q], x[(size_t)colidx[q] * ld + c]);
+        y[(size_t)r * ld + c] = s;
+    }
+    if (!w && !want_n2) return;
+    __syncthreads();
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+        if (st && st[c].active != 1) continue;
+        double d0 = 0.0, d1 = 0.0;
+        for (int r = r0; r < r1; r++) {
+            V yv = y[(size_t)r * ld + c];
+            if (w) d0 += (double)redot(w[(size_t)r * ld + c], yv);
+            if (want_n2) d1 += (double)nrm2(yv);
+        }
+        int p = 0;
+        if (w) part[((size_t)c * np + p++) * ntiles + tile] = d0;
+        if (want_n2) part[((size_t)c * np + p) * ntiles + tile] = d1;
+    }
+}
+
+// single right-hand side: warp per row, lanes over the row's entries
+template <class V>
+__global__ void spmv1_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ colidx,
+                             const V* __restrict__ A, const V* __restrict__ x, V* __restrict__ y)
+{
+    int r = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x & 31;
+    if (r >= n) return;
+    V s = vzero<V>();
+    for (int q = rowptr[r] + lane; q < rowptr[r + 1]; q += 32) s = vfma(s, A[q], x[colidx[q]]);
+    for (int o = 16; o; o >>= 1) {
+        if constexpr (vt<V>::cplx) { s.x += __shfl_down_sync(0xffffffffu, s.x, o); s.y += __shfl_down_sync(0xffffffffu, s.y, o); }
+        else s += __shfl_down_sync(0xffffffffu, s, o);
+    }
+    if (lane == 0) y[r] = s;
+}
+
+// ---------------------------------------------------------------------------
+// Per-column Krylov state and the deterministic reduce + finalize step.
+// ---------------------------------------------------------------------------
+
+
+enum Phase : int {
+    PH_BNORM = 0,        // part0 = |b|^2 -> bnorm; (re)activate
+    PH_BICG_RHO0,        // part0 = rd.r  -> rho (iteration 0)
+    PH_BICG_ALPHA,       // part0 = rd.v  -> alpha = rho / aden
+    PH_BICG_S,           // part0 = |s|^2 (real variant early exit)
+    PH_BICG_OMEGA,       // part0 = t.s, part1 = |t|^2 -> omega
+    PH_BICG_END,         // part0 = |r|^2, part1 = rd.r -> err, convergence, next beta/rho
+    PH_PCG_INIT,         // part0 = r.d -> dnew
+    PH_PCG_ALPHA,        // part0 = d.q -> alpha
+    PH_PCG_END,          // part0 = r.q (dnew), part1 = |r|^2 -> beta, err, convergence
+    PH_RESID,            // part0 = |r|^2 -> err (refinement residual)
+};
+
+template <int NP>
+__global__ void reduce_finalize_kernel(int k, int ntiles, const double* __restrict__ part, ColState* __restrict__ st,
+                                       int phase, int real_variant, int iter_base)
+{
+    int c = blockIdx.x;
+    if (c >= k) return;
+    __shared__ double sh[NP][256];
+    double acc[NP];
+    for (int p = 0; p < NP; p++) acc[p] = 0.0;
+    for (int t = threadIdx.x; t < ntiles; t += 256)
+        for (int p = 0; p < NP; p++) acc[p] += part[((size_t)c * NP + p) * ntiles + t];
+    for (int p = 0; p < NP; p++) sh[p][threadIdx.x] = acc[p];
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int p = 0; p < NP; p++) sh[p][threadIdx.x] += sh[p][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x) return;
+    ColState& S = st[c];
+    double v0 = sh[0][0], v1 = NP > 1 ? sh[NP - 1][0] : 0.0;
+    switch (phase) {
+    case PH_BNORM:
+        // columns the caller switched off stay off (refinement steps)
+        S.bnorm = sqrt(v0);
+        S.its = 0; S.status = 0; S.err = 0.0;
+        S.active = (S.active == 1 && S.bnorm > 0.0) ? 1 : 0;
+        break;
+    case PH_BICG_RHO0:
+        if (!S.active) break;
+        S.rho = v0;
+        if (v0 == 0.0) { S.active = 0; S.status = 2; S.its = iter_base; }
+        break;
+    case PH_BICG_ALPHA:
+        if (!S.active) break;
+        S.alpha = S.rho / v0;
+        break;
+    case PH_BICG_S:
+        if (!S.active) break;
+        S.err = sqrt(v0);  // real variant only: |s| < tol |b| ends the solve (matrix_imp.hpp:512-517)
+        if (real_variant && S.err < S.tol * S.bnorm) { S.active = -1; }  // -1: finish with x += alpha pd
+        break;
+    case PH_BICG_OMEGA:
+        if (S.active != 1) break;
+        S.omega = v0 / v1;
+        break;
+    case PH_BICG_END: {
+        if (S.active == -1) { S.active = 0; S.status = 0; break; }
+        if (!S.active) break;
+        S.err = sqrt(v0);
+        S.its++;
+        if (S.err <= S.tol * S.bnorm) { S.active = 0; S.status = 0; S.its--; break; }
+        if (S.omega == 0.0) { S.active = 0; S.status = 1; S.its--; break; }
+        if (S.its >= S.maxit) { S.active = 0; S.status = 1; break; }
+        S.rhop = S.rho;
+        S.rho = v1;
+        if (v1 == 0.0) { S.active = 0; S.status = 2; S.its--; break; }
+        S.beta = (S.rho * S.alpha) / (S.rhop * S.omega);
+        break;
+    }
+    case PH_PCG_INIT:
+        if (!S.active) break;
+        S.dnew = v0;
+        break;
+    case PH_PCG_ALPHA:
+        if (!S.active) break;
+        S.alpha = S.dnew / v0;
+        if (S.alpha == 0.0 || isnan(S.alpha)) { S.active = 0; S.status = 2; S.err = S.err; }
+        break;
+    case PH_PCG_END: {
+        if (!S.active) break;
+        S.dold = S.dnew;
+        S.dnew = v0;
+        S.beta = S.dnew / S.dold;
+        S.its++;
+        if (S.beta == 0.0 || isnan(S.beta)) { S.active = 0; S.status = 2; S.its--; break; }
+        S.err = sqrt(v1);
+        if (S.err <= S.tol * S.bnorm) { S.active = 0; S.status = 0; S.its--; break; }
+        if (S.its >= S.maxit) { S.active = 0; S.status = 1; break; }
+        break;
+    }
+    case PH_RESID:
+        S.err = sqrt(v0);
+        break;
+    }
+}
+
+// generic column dot partials over row tiles: part0 = sum Re(conj(a) b), optional part1 = sum Re(conj(c) d)
+template <class V>
+__global__ void dot_tiles_kernel(int n, int k, int ld, const V* __restrict__ a, const V* __restrict__ b,
+                                 const V* __restrict__ c2, const V* __restrict__ d2, double* __restrict__ part,
+                                 int np, int ntiles, const ColState* __restrict__ st)
+{
+    int tile = blockIdx.x;
+    int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+        if (st && st[c].active != 1) continue;
+        double d0 = 0.0, d1 = 0.0;
+        for (int r = r0; r < r1; r++) {
+            size_t o = (size_t)r * ld + c;
+            d0 += (double)redot(a[o], b[o]);
+            if (c2) d1 += (double)redot(c2[o], d2[o]);
+        }
+        part[((size_t)c * np) * ntiles + tile] = d0;
+        if (c2) part[((size_t)c * np + 1) * ntiles + tile] = d1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// BiCGSTAB elementwise steps (matrix_imp.hpp:350-413 complex, 479-547 real).
+// S = real scalar type of V.  ColState is read per column.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool col_on(const ColState* st, int c) { return st[c].active == 1; }
+
+// p = r (first iteration) or r + beta (p - omega v); for diagonal/no
+// preconditioner also pd = M^-1 p.  precon: 0 none, 1 diag.
+template <class V, class S>
+__global__ void bicg_p_kernel(int n, int k, int ld, const ColState* st, int first, const V* __restrict__ r,
+                              V* __restrict__ p, const V* __restrict__ v, V* __restrict__ pd,
+                              const V* __restrict__ idiag, int precon)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * k) return;
+    int i = (int)(t / k), c = (int)(t % k);
+    if (!col_on(st, c)) return;
+    size_t o = (size_t)i * ld + c;
+    V pv;
+    if (first) pv = r[o];
+    else {
+        S beta = (S)st[c].beta, omega = (S)st[c].omega;
+        pv = vadd(r[o], vscale(vsub(p[o], vscale(v[o], omega)), beta));
+    }
+    p[o] = pv;
+    if (precon == 1) pd[o] = vmul(pv, idiag[i]);
+    else if (precon == 0) pd[o] = pv;
+}
+
+// s = r - alpha v with |s|^2 partials; sd = M^-1 s for diag/none
+template <class V, class S>
+__global__ void bicg_s_kernel(int n, int k, int ld, const ColState* st, const V* __restrict__ r,
+                              const V* __restrict__ v, V* __restrict__ s, V* __restrict__ sd,
+                              const V* __restrict__ idiag, int precon, double* __restrict__ part, int ntiles)
+{
+    int tile = blockIdx.x;
+    int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+        if (!col_on(st, c)) continue;
+        S alpha = (S)st[c].alpha;
+        double acc = 0.0;
+        for (int i = r0; i < r1; i++) {
+            size_t o = (size_t)i * ld + c;
+            V sv = vsub(r[o], vscale(v[o], alpha));
+            s[o] = sv;
+            if (precon == 1) sd[o] = vmul(sv, idiag[i]);
+            else if (precon == 0) sd[o] = sv;
+            acc += (double)nrm2(sv);
+        }
+        part[(size_t)c * ntiles + tile] = acc;
+    }
+}
+
+// x += alpha pd + omega sd ; r = s - omega t ; partials |r|^2, Re(conj(rd) r).
+// Columns that ended on |s| (real variant) take x += alpha pd only.
+template <class V, class S>
+__global__ void bicg_xr_kernel(int n, int k, int ld, const ColState* st, V* __restrict__ x, V* __restrict__ r,
+                               const V* __restrict__ rd, const V* __restrict__ pd, const V* __restrict__ sd,
+                               const V* __restrict__ s, const V* __restrict__ t, double* __restrict__ part, int ntiles)
+{
+    int tile = blockIdx.x;
+    int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+        int a = st[c].active;
+        if (a == 0) continue;
+        S alpha = (S)st[c].alpha, omega = (S)st[c].omega;
+        double n2 = 0.0, rr = 0.0;
+        for (int i = r0; i < r1; i++) {
+            size_t o = (size_t)i * ld + c;
+            if (a == -1) { x[o] = vadd(x[o], vscale(pd[o], alpha)); continue; }
+            x[o] = vadd(x[o], vadd(vscale(pd[o], alpha), vscale(sd[o], omega)));
+            V rv = vsub(s[o], vscale(t[o], omega));
+            r[o] = rv;
+            n2 += (double)nrm2(rv);
+            rr += (double)redot(rd[o], rv);
+        }
+        part[((size_t)c * 2) * ntiles + tile] = n2;
+        part[((size_t)c * 2 + 1) * ntiles + tile] = rr;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// PCG elementwise steps (matrix_imp.hpp:93-154)
+// ---------------------------------------------------------------------------
+// x += alpha d ; r -= alpha q ; for diag/none: z = M^-1 r and partials r.z, |r|^2
+template <class V, class S>
+__global__ void pcg_xr_kernel(int n, int k, int ld, const ColState* st, V* __restrict__ x, V* __restrict__ r,
+                              const V* __restrict__ d, const V* __restrict__ q, V* __restrict__ z,
+                              const V* __restrict__ idiag, int precon, double* __restrict__ part, int ntiles)
+{
+    int tile = blockIdx.x;
+    int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+        if (!col_on(st, c)) continue;
+        S alpha = (S)st[c].alpha;
+        double rz = 0.0, n2 = 0.0;
+        for (int i = r0; i < r1; i++) {
+            size_t o = (size_t)i * ld + c;
+            x[o] = vadd(x[o], vscale(d[o], alpha));
+            V rv = vsub(r[o], vscale(q[o], alpha));
+            r[o] = rv;
+            if (precon != 2) {
+                V zv = precon == 1 ? vmul(rv, idiag[i]) : rv;
+                z[o] = zv;
+                rz += (double)redot(rv, zv);
+                n2 += (double)nrm2(rv);
+            }
+        }
+        if (precon != 2) {
+            part[((size_t)c * 2) * ntiles + tile] = rz;
+            part[((size_t)c * 2 + 1) * ntiles + tile] = n2;
+        }
+    }
+}
+
+// d = d beta + z
+template <class V, class S>
+__global__ void pcg_d_kernel(int n, int k, int ld, const ColState* st, V* __restrict__ d, const V* __restrict__ z)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * k) return;
+    int i = (int)(t / k), c = (int)(t % k);
+    if (!col_on(st, c)) return;
+    size_t o = (size_t)i * ld + c;
+    d[o] = vadd(vscale(d[o], (S)st[c].beta), z[o]);
+}
+
+// ---------------------------------------------------------------------------
+// small elementwise helpers
+// ---------------------------------------------------------------------------
+// r = b - r (in place on r), rd = r, optional |b|^2 partials are separate
+template <class V>
+__global__ void resid_kernel(int n, int k, int ld, const V* __restrict__ b, V* __restrict__ r, V* __restrict__ rd)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * k) return;
+    size_t o = (size_t)(t / k) * ld + (t % k);
+    V v = vsub(b[o], r[o]);
+    r[o] = v;
+    if (rd) rd[o] = v;
+}
+
+template <class V>
+__global__ void scale_diag_kernel(int n, int k, int ld, const V* __restrict__ a, const V* __restrict__ idiag,
+                                  V* __restrict__ out, int precon)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * k) return;
+    int i = (int)(t / k);
+    size_t o = (size_t)i * ld + (t % k);
+    out[o] = precon == 1 ? vmul(a[o], idiag[i]) : a[o];
+}
+
+// source-major (q*n + i) <-> node-major (i*ld + q) transposes with precision cast
+template <class To, class From>
+__global__ void to_nodemajor_kernel(int n, int k, int ld, const From* __restrict__ src, To* __restrict__ dst)
+{
+    __shared__ From tile[32][33];
+    int i0 = blockIdx.x * 32, q0 = blockIdx.y * 32;
+    for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+        int q = q0 + yy, i = i0 + threadIdx.x;
+        if (q < k && i < n) tile[yy][threadIdx.x] = src[(size_t)q * n + i];
+    }
+    __syncthreads();
+    for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+        int i = i0 + yy, q = q0 + threadIdx.x;
+        if (q < k && i < n) dst[(size_t)i * ld + q] = vcast<To, From>(tile[threadIdx.x][yy]);
+    }
+}
+
+template <class To, class From>
+__global__ void to_srcmajor_kernel(int n, int k, int ld, const From* __restrict__ src, To* __restrict__ dst)
+{
+    __shared__ From tile[32][33];
+    int i0 = blockIdx.x * 32, q0 = blockIdx.y * 32;
+    for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+        int i = i0 + yy, q = q0 + threadIdx.x;
+        if (q < k && i < n) tile[yy][threadIdx.x] = src[(size_t)i * ld + q];
+    }
+    __syncthreads();
+    for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+        int q = q0 + yy, i = i0 + threadIdx.x;
+        if (q < k && i < n) dst[(size_t)q * n + i] = vcast<To, From>(tile[threadIdx.x][yy]);
+    }
+}
+
+template <class To, class From>
+__global__ void cast_kernel(size_t cnt, const From* __restrict__ a, To* __restrict__ b)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < cnt) b[t] = vcast<To, From>(a[t]);
+}
+
+// x += e (refinement update, FP64 x, low-precision e)
+template <class V, class E>
+__global__ void add_correction_kernel(size_t cnt, V* __restrict__ x, const E* __restrict__ e)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < cnt) x[t] = vadd(x[t], vcast<V, E>(e[t]));
+}
+
+// 1/diag(A) for the Diag preconditioner (TPrecon_Diag::Reset,
+// src/libmath/precon_imp.hpp:56-64): 1 where the diagonal is zero.
+template <class V>
+__global__ void diag_inv_kernel(int n, const int* __restrict__ diagpos, const V* __restrict__ A, V* __restrict__ out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    V d = A[diagpos[i]];
+    bool z = re(d) == 0 && im(d) == 0;
+    if constexpr (vt<V>::cplx) out[i] = z ? V{1.0, 0.0} : vrecip(d);
+    else out[i] = z ? 1.0 : 1.0 / d;
+}
+
+__global__ void count_active_kernel(int k, const ColState* __restrict__ cst, int* out)
+{
+    __shared__ int s;
+    if (threadIdx.x == 0) s = 0;
+    __syncthreads();
+    int c = 0;
+    for (int i = threadIdx.x; i < k; i += blockDim.x) c += cst[i].active != 0;
+    atomicAdd(&s, c);
+    __syncthreads();
+    if (threadIdx.x == 0) *out = s;
+}
+
+}  // namespace tg

@@ -1,0 +1,964 @@
+// tg_solver.cu -- forward solver object, batched Krylov engines and the C ABI.
+#include <algorithm>
+#include <atomic>
+#include <utility>
+#include <cstdarg>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "../../include/toastgpu.h"
+#include "tg_jac.cuh"
+
+namespace tg {
+
+static thread_local std::string g_err;
+void set_error(const char* fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+}
+const char* last_error() { return g_err.c_str(); }
+
+// ---------------------------------------------------------------------------
+// launch accounting and opt-in per-class kernel timing
+// ---------------------------------------------------------------------------
+static std::atomic<long long> g_nlaunch{0};
+
+template <typename... KArgs, typename... Args>
+static inline void launch(void (*k)(KArgs...), dim3 g, dim3 b, size_t sm, cudaStream_t st, Args&&... args)
+{
+    k<<<g, b, sm, st>>>(std::forward<Args>(args)...);
+    g_nlaunch.fetch_add(1, std::memory_order_relaxed);
+}
+
+enum ProfClass { PC_SPMM = 0, PC_SWEEP, PC_VEC, PC_JAC, PC_ASM, PC_PROJ, PC_N };
+
+struct Profiler {
+    int mask = 0;
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[PC_N];
+    size_t used = 0;
+    cudaEvent_t get()
+    {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            TG_CUDA(cudaEventCreate(&e));
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    ~Profiler() { for (auto e : pool) cudaEventDestroy(e); }
+};
+
+struct ProfScope {
+    Profiler* p;
+    int cls;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr;
+    ProfScope(Profiler* p_, int c, cudaStream_t s) : p(p_), cls(c), st(s)
+    {
+        if (p && (p->mask >> cls & 1)) { a = p->get(); cudaEventRecord(a, st); }
+    }
+    ~ProfScope()
+    {
+        if (a) { cudaEvent_t b = p->get(); cudaEventRecord(b, st); p->ev[cls].push_back({a, b}); }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { if (p) cudaFree(p); }
+    void* ensure(size_t b)
+    {
+        if (b <= bytes && p) return p;
+        if (p) { cudaFree(p); p = nullptr; bytes = 0; }
+        if (b == 0) b = 16;
+        if (cudaMalloc(&p, b) != cudaSuccess) {
+            cudaGetLastError();
+            throw Error{TG_ERR_NOMEM, "device allocation of " + std::to_string(b) + " bytes failed"};
+        }
+        bytes = b;
+        return p;
+    }
+    template <class T> T* as() const { return (T*)p; }
+};
+
+static inline unsigned cdiv_u(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+// ---------------------------------------------------------------------------
+// Krylov engine for one value type.  Vectors are node-major n x k (ld = k).
+// ---------------------------------------------------------------------------
+template <class V>
+struct Engine {
+    using S = typename vt<V>::R;
+    Mesh* mesh = nullptr;
+    cudaStream_t st = 0;
+    const V* A = nullptr;      // system values
+    const V* L = nullptr;      // IC(0) lower factor
+    const V* dinv = nullptr;   // 1 / IC diagonal
+    const V* idiag = nullptr;  // 1 / diag(A) (Diag preconditioner)
+    int precon = 0;            // 0 none, 1 diag, 2 ich
+    Profiler* prof = nullptr;
+    DBuf w[9], part, cs, cnt;
+    int* h_cnt = nullptr;
+
+    ~Engine() { if (h_cnt) cudaFreeHost(h_cnt); }
+
+    V* vec(int i, size_t nk) { return (V*)w[i].ensure(nk * sizeof(V)); }
+    int ntiles() const { return (int)cdiv_u(mesh->d.n, ROW_TILE); }
+    double* parts(int k, int np) { return (double*)part.ensure((size_t)k * np * ntiles() * sizeof(double)); }
+    unsigned rowblk(int k) const { return (unsigned)std::min(256, std::max(32, (k + 31) / 32 * 32)); }
+
+    void spmm(int k, const V* x, V* y, const V* wv, bool n2, ColState* cst, double* pt, int np)
+    {
+        const MeshDev& m = mesh->d;
+        ProfScope ps(prof, PC_SPMM, st);
+        launch(spmm_dot_kernel<V>, ntiles(), 256, 0, st, m.n, m.rowptr, m.colidx, A, k, k, x, y, wv, n2, pt, np,
+                                                     ntiles(), cst);
+    }
+    template <int NP>
+    void finalize(int k, ColState* cst, int phase, int real_variant = 0, int iter = 0)
+    {
+        launch(reduce_finalize_kernel<NP>, k, 256, 0, st, k, ntiles(), part.as<double>(), cst, phase, real_variant, iter);
+    }
+    static int colw(int k) { return k >= 32 ? 32 : (k >= 16 ? 16 : (k >= 8 ? 8 : (k >= 4 ? 4 : (k >= 2 ? 2 : 1)))); }
+
+    // out = M^-1 in for the IC(0) preconditioner (level-scheduled sweeps)
+    void ic_apply(int k, const V* in, V* out, const ColState* cst)
+    {
+        const MeshDev& m = mesh->d;
+        ProfScope ps(prof, PC_SWEEP, st);
+        int cw = colw(k), ncg = (k + cw - 1) / cw, rpw = 32 / cw;
+        const std::vector<int>& fp = mesh->fwd_lev_ptr_h;
+        for (size_t l = 0; l + 1 < fp.size(); l++) {
+            int nr = fp[l + 1] - fp[l];
+            size_t warps = cdiv_u((size_t)nr * ncg, rpw);
+            launch(ic_fwd_level<V, S>, cdiv_u(warps * 32, 256), 256, 0, st, m, m.fwd_lev_rows + fp[l], nr, k, k, cw, L,
+                                                                       dinv, in, out, cst);
+        }
+        const std::vector<int>& bp = mesh->bwd_lev_ptr_h;
+        for (size_t l = 0; l + 1 < bp.size(); l++) {
+            int nr = bp[l + 1] - bp[l];
+            size_t warps = cdiv_u((size_t)nr * ncg, rpw);
+            launch(ic_bwd_level<V, S>, cdiv_u(warps * 32, 256), 256, 0, st, m, m.bwd_lev_rows + bp[l], nr, k, k, cw, L,
+                                                                       dinv, out, cst);
+        }
+    }
+
+    int count_active(int k, ColState* cst)
+    {
+        if (!h_cnt) TG_CUDA(cudaMallocHost(&h_cnt, sizeof(int)));
+        int* dc = (int*)cnt.ensure(sizeof(int));
+        launch(count_active_kernel, 1, 256, 0, st, k, cst, dc);
+        TG_CUDA(cudaMemcpyAsync(h_cnt, dc, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+        return *h_cnt;
+    }
+
+    // B, X: device node-major n x k.  cst: per-column state with tol/maxit set.
+    void solve(int method, int k, const V* B, V* X, ColState* cst, bool zero_guess)
+    {
+        const MeshDev& m = mesh->d;
+        size_t nk = (size_t)m.n * k;
+        unsigned eg = cdiv_u(nk, 256);
+        V* R = vec(0, nk);
+        // r = b - A x
+        if (zero_guess) TG_CUDA(cudaMemcpyAsync(R, B, nk * sizeof(V), cudaMemcpyDeviceToDevice, st));
+        else {
+            spmm(k, X, R, nullptr, false, nullptr, nullptr, 0);
+            launch(resid_kernel<V>, eg, 256, 0, st, m.n, k, k, B, R, nullptr);
+        }
+        double* pt = parts(k, 2);
+        launch(dot_tiles_kernel<V>, ntiles(), rowblk(k), 0, st, m.n, k, k, B, B, nullptr, nullptr, pt, 1, ntiles(), nullptr);
+        finalize<1>(k, cst, PH_BNORM);
+        int maxit = 0;
+        {
+            // maxit is per column but identical within one call; read it back from the first column
+            ColState h;
+            TG_CUDA(cudaMemcpyAsync(&h, cst, sizeof(ColState), cudaMemcpyDeviceToHost, st));
+            TG_CUDA(cudaStreamSynchronize(st));
+            maxit = h.maxit;
+        }
+        if (method == TG_SOLVER_BICGSTAB) bicgstab(k, X, cst, maxit);
+        else if (method == TG_SOLVER_CG) pcg(k, X, cst, maxit);
+        else throw Error{TG_ERR_UNSUPPORTED, "solver method not implemented on the GPU"};
+    }
+
+    void bicgstab(int k, V* X, ColState* cst, int maxit)
+    {
+        const MeshDev& m = mesh->d;
+        size_t nk = (size_t)m.n * k;
+        unsigned eg = cdiv_u(nk, 256);
+        V *R = vec(0, nk), *RD = vec(1, nk), *P = vec(2, nk), *PD = vec(3, nk), *Vv = vec(4, nk);
+        V *Sv = vec(5, nk), *SD = vec(6, nk), *T = vec(7, nk);
+        TG_CUDA(cudaMemcpyAsync(RD, R, nk * sizeof(V), cudaMemcpyDeviceToDevice, st));
+        double* pt = parts(k, 2);
+        launch(dot_tiles_kernel<V>, ntiles(), rowblk(k), 0, st, m.n, k, k, RD, R, nullptr, nullptr, pt, 1, ntiles(), cst);
+        finalize<1>(k, cst, PH_BICG_RHO0);
+        int pmode = precon == 2 ? 2 : precon;
+        const int real_variant = vt<V>::cplx ? 0 : 1;
+        for (int it = 0; it < maxit; it++) {
+            launch(bicg_p_kernel<V, S>, eg, 256, 0, st, m.n, k, k, cst, it == 0, R, P, Vv, PD, idiag, pmode);
+            if (pmode == 2) ic_apply(k, P, PD, cst);
+            spmm(k, PD, Vv, RD, false, cst, pt, 1);
+            finalize<1>(k, cst, PH_BICG_ALPHA);
+            launch(bicg_s_kernel<V, S>, ntiles(), rowblk(k), 0, st, m.n, k, k, cst, R, Vv, Sv, SD, idiag, pmode, pt, ntiles());
+            finalize<1>(k, cst, PH_BICG_S, real_variant);
+            if (pmode == 2) ic_apply(k, Sv, SD, cst);
+            spmm(k, SD, T, Sv, true, cst, pt, 2);
+            finalize<2>(k, cst, PH_BICG_OMEGA);
+            launch(bicg_xr_kernel<V, S>, ntiles(), rowblk(k), 0, st, m.n, k, k, cst, X, R, RD, PD, SD, Sv, T, pt, ntiles());
+            finalize<2>(k, cst, PH_BICG_END);
+            if ((it & 3) == 3 || it + 1 == maxit)
+                if (count_active(k, cst) == 0) break;
+        }
+    }
+
+    void pcg(int k, V* X, ColState* cst, int maxit)
+    {
+        const MeshDev& m = mesh->d;
+        size_t nk = (size_t)m.n * k;
+        unsigned eg = cdiv_u(nk, 256);
+        V *R = vec(0, nk), *D = vec(1, nk), *Q = vec(2, nk), *Z = vec(3, nk);
+        double* pt = parts(k, 2);
+        if (precon == 2) ic_apply(k, R, Z, cst);
+        else launch(scale_diag_kernel<V>, eg, 256, 0, st, m.n, k, k, R, idiag, Z, precon);
+        TG_CUDA(cudaMemcpyAsync(D, Z, nk * sizeof(V), cudaMemcpyDeviceToDevice, st));
+        launch(dot_tiles_kernel<V>, ntiles(), rowblk(k), 0, st, m.n, k, k, R, Z, nullptr, nullptr, pt, 1, ntiles(), cst);
+        finalize<1>(k, cst, PH_PCG_INIT);
+        for (int it = 0; it < maxit; it++) {
+            spmm(k, D, Q, D, false, cst, pt, 1);
+            finalize<1>(k, cst, PH_PCG_ALPHA);
+            launch(pcg_xr_kernel<V, S>, ntiles(), rowblk(k), 0, st, m.n, k, k, cst, X, R, D, Q, Z, idiag, precon, pt, ntiles());
+            if (precon == 2) {
+                ic_apply(k, R, Z, cst);
+                launch(dot_tiles_kernel<V>, ntiles(), rowblk(k), 0, st, m.n, k, k, R, Z, R, R, pt, 2, ntiles(), cst);
+            }
+            finalize<2>(k, cst, PH_PCG_END);
+            launch(pcg_d_kernel<V, S>, eg, 256, 0, st, m.n, k, k, cst, D, Z);
+            if ((it & 3) == 3 || it + 1 == maxit)
+                if (count_active(k, cst) == 0) break;
+        }
+    }
+};
+
+__global__ void init_cols_kernel(int k, ColState* cst, double tol, int maxit)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    ColState s;
+    memset(&s, 0, sizeof(s));
+    s.tol = tol;
+    s.maxit = maxit;
+    s.active = 1;
+    cst[c] = s;
+}
+
+// inner columns follow the outer ones: inactive outer -> inactive inner
+__global__ void init_inner_kernel(int k, const ColState* outer, ColState* inner, double tol, int maxit)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    ColState s;
+    memset(&s, 0, sizeof(s));
+    s.tol = tol;
+    s.maxit = maxit;
+    s.active = outer[c].active;
+    inner[c] = s;
+}
+
+// outer refinement bookkeeping: err = |r| from PH_RESID, converge test
+__global__ void refine_check_kernel(int k, ColState* outer, const ColState* inner, int step, int maxsteps)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    ColState& o = outer[c];
+    if (inner) o.its += inner[c].its + (inner[c].status == 0 ? 1 : 0);
+    if (!o.active) return;
+    if (o.err <= o.tol * o.bnorm) { o.active = 0; o.status = 0; return; }
+    if (step >= maxsteps) { o.active = 0; o.status = 1; }
+}
+
+template <class V>
+__global__ void mask_vec_kernel(int n, int k, const ColState* cst, V* x)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * k) return;
+    int c = (int)(t % k);
+    if (cst[c].active != 1) x[t] = vzero<V>();
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+// ---------------------------------------------------------------------------
+// solver object
+// ---------------------------------------------------------------------------
+struct tg_mesh_s {
+    std::unique_ptr<Mesh> m;
+};
+
+struct tg_solver_s {
+    Mesh* mesh = nullptr;
+    int cplx = 0, method = 1, precon = 2, precision = 0, maxit = 0;
+    double tol = 1e-10;
+    cudaStream_t stream = 0, own = 0;
+    bool reset_done = false;
+    DBuf val64, val32, L64, L32, dinv64, dinv32, idiag64, idiag32, params;
+    Engine<double> er64;
+    Engine<float> er32;
+    Engine<cd> ec64;
+    Engine<cf> ec32;
+    DBuf B, X, X32, B32, cs_outer, cs_inner, io_a, io_b, tmp, jout;
+    DBuf jF, jG, jpair, jyinv, plink_q, plink_m, psup, pnsup, pflag, pMsup, plin, plog;
+    DBuf fp_bq, fp_xq, fp_bm, fp_xm, fp_lin, fp_log;
+    Profiler prof;
+    std::mutex mu;
+};
+
+static int fail(const Error& e)
+{
+    set_error("%s", e.msg.c_str());
+    return e.code;
+}
+
+#define API_BEGIN try {
+#define API_END                                              \
+    }                                                        \
+    catch (const Error& e) { return fail(e); }               \
+    catch (const std::bad_alloc&) { set_error("host allocation failed"); return TG_ERR_NOMEM; } \
+    catch (...) { set_error("unknown error"); return TG_ERR_ARG; }                              \
+    return TG_OK;
+
+static size_t vsize(int cplx, bool fp32) { return (cplx ? 2 : 1) * (fp32 ? 4 : 8); }
+
+template <class V> static Engine<V>& engine(tg_solver s);
+template <> Engine<double>& engine<double>(tg_solver s) { return s->er64; }
+template <> Engine<float>& engine<float>(tg_solver s) { return s->er32; }
+template <> Engine<cd>& engine<cd>(tg_solver s) { return s->ec64; }
+template <> Engine<cf>& engine<cf>(tg_solver s) { return s->ec32; }
+
+// copies a host or device input of `bytes` to device memory; returns device pointer
+static const void* dev_in(tg_solver s, const void* p, size_t bytes, int mem, DBuf& stage)
+{
+    if (mem == TG_MEM_DEVICE) return p;
+    void* d = stage.ensure(bytes);
+    TG_CUDA(cudaMemcpyAsync(d, p, bytes, cudaMemcpyHostToDevice, s->stream));
+    return d;
+}
+
+template <class V64>
+static void setup_engine(tg_solver s, Engine<V64>& e64)
+{
+    e64.mesh = s->mesh; e64.st = s->stream; e64.precon = s->precon == TG_PRECON_DILU ? 0 : s->precon;
+    e64.A = s->val64.as<V64>(); e64.L = s->L64.as<V64>(); e64.dinv = s->dinv64.as<V64>();
+    e64.idiag = s->idiag64.as<V64>();
+    e64.prof = &s->prof;
+}
+
+template <class V64, class V32>
+static void do_reset(tg_solver s, const double* cmua, const double* ckap, const double* c2a, double omega, int mem)
+{
+    const MeshDev& m = s->mesh->d;
+    size_t nb = (size_t)m.n * sizeof(double);
+    double* P = (double*)s->params.ensure(3 * nb);
+    cudaMemcpyKind kind = mem == TG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    TG_CUDA(cudaMemcpyAsync(P, cmua, nb, kind, s->stream));
+    TG_CUDA(cudaMemcpyAsync(P + m.n, ckap, nb, kind, s->stream));
+    TG_CUDA(cudaMemcpyAsync(P + 2 * m.n, c2a, nb, kind, s->stream));
+    V64* A = (V64*)s->val64.ensure((size_t)m.nnz * sizeof(V64));
+    ProfScope ps(&s->prof, PC_ASM, s->stream);
+    launch(assemble_kernel<vt<V64>::cplx>, cdiv_u(m.nnz, 256), 256, 0, s->stream, m, P, P + m.n, P + 2 * m.n, omega,
+                                                                             (double*)A);
+    int pre = s->precon == TG_PRECON_DILU ? 0 : s->precon;
+    V64* idg = (V64*)s->idiag64.ensure((size_t)m.n * sizeof(V64));
+    launch(diag_inv_kernel<V64>, cdiv_u(m.n, 256), 256, 0, s->stream, m.n, m.diagpos, A, idg);
+    if (pre == TG_PRECON_ICH) {
+        V64* L = (V64*)s->L64.ensure((size_t)std::max(m.nnzL, 1) * sizeof(V64));
+        V64* dinv = (V64*)s->dinv64.ensure((size_t)m.n * sizeof(V64));
+        const std::vector<int>& fp = s->mesh->fwd_lev_ptr_h;
+        for (size_t l = 0; l + 1 < fp.size(); l++) {
+            int nr = fp[l + 1] - fp[l];
+            launch(ic_factor_level<V64>, cdiv_u(nr, 128), 128, 0, s->stream, m, m.fwd_lev_rows + fp[l], nr, A, L, dinv);
+        }
+    }
+    if (s->precision == TG_PREC_MIXED) {
+        launch(cast_kernel<V32, V64>, cdiv_u(m.nnz, 256), 256, 0, s->stream, m.nnz, A, (V32*)s->val32.ensure(m.nnz * sizeof(V32)));
+        launch(cast_kernel<V32, V64>, cdiv_u(m.n, 256), 256, 0, s->stream, m.n, idg, (V32*)s->idiag32.ensure(m.n * sizeof(V32)));
+        if (pre == TG_PRECON_ICH) {
+            launch(cast_kernel<V32, V64>, cdiv_u(std::max(m.nnzL, 1), 256), 256, 0, s->stream, 
+                m.nnzL, s->L64.as<V64>(), (V32*)s->L32.ensure((size_t)std::max(m.nnzL, 1) * sizeof(V32)));
+            launch(cast_kernel<V32, V64>, cdiv_u(m.n, 256), 256, 0, s->stream, m.n, s->dinv64.as<V64>(),
+                                                                          (V32*)s->dinv32.ensure(m.n * sizeof(V32)));
+        }
+    }
+    TG_CUDA(cudaGetLastError());
+}
+
+
+
+
+struct LinkHost {
+    std::vector<int> q, m, pair;
+};
+
+static LinkHost make_links(int nq, int nm, const int* link_ofs, const int* link_m)
+{
+    LinkHost L;
+    TG_CHECK(link_ofs[0] == 0, TG_ERR_ARG, "link_ofs must start at 0");
+    int nqm = link_ofs[nq];
+    TG_CHECK(nqm >= 0 && (nqm == 0 || link_m), TG_ERR_ARG, "bad link list");
+    L.q.resize(nqm); L.m.resize(nqm); L.pair.assign((size_t)nq * nm, -1);
+    for (int q = 0; q < nq; q++) {
+        TG_CHECK(link_ofs[q + 1] >= link_ofs[q], TG_ERR_ARG, "link_ofs not ascending");
+        for (int l = link_ofs[q]; l < link_ofs[q + 1]; l++) {
+            int m = link_m[l];
+            TG_CHECK(m >= 0 && m < nm, TG_ERR_ARG, "link detector index out of range");
+            TG_CHECK(L.pair[(size_t)q * nm + m] < 0, TG_ERR_ARG, "duplicate link");
+            L.q[l] = q; L.m[l] = m;
+            L.pair[(size_t)q * nm + m] = l;
+        }
+    }
+    return L;
+}
+
+template <class T>
+static void upload_async(tg_solver s, DBuf& b, const std::vector<T>& v)
+{
+    void* p = b.ensure(std::max<size_t>(v.size(), 1) * sizeof(T));
+    if (!v.empty()) TG_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s->stream));
+}
+
+// ---------------------------------------------------------------------------
+// core steps on device data (node-major n x k blocks)
+// ---------------------------------------------------------------------------
+// Solve F X = B for k right-hand sides; X holds the initial guess.
+template <class V64, class V32>
+static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co)
+{
+    const MeshDev& m = s->mesh->d;
+    int n = m.n;
+    size_t nk = (size_t)n * k;
+    int maxit = s->maxit > 0 ? s->maxit : n + 1;  // maxit 0 means n+1 (matrix_imp.hpp:103)
+    launch(init_cols_kernel, cdiv_u(k, 128), 128, 0, s->stream, k, co, s->tol, maxit);
+    Engine<V64>& e64 = engine<V64>(s);
+    setup_engine(s, e64);
+    if (s->precision == TG_PREC_FP64) {
+        e64.solve(s->method, k, B, X, co, false);
+        return;
+    }
+    // FP64 iterative refinement around FP32 / complex-FP32 inner solves:
+    // r = b - F x in FP64, solve F e = r in FP32 to a loose tolerance,
+    // x += e in FP64, until |r| <= tol |b| per column.
+    Engine<V32>& e32 = engine<V32>(s);
+    e32.mesh = s->mesh; e32.st = s->stream; e32.precon = e64.precon;
+    e32.A = s->val32.as<V32>(); e32.L = s->L32.as<V32>(); e32.dinv = s->dinv32.as<V32>();
+    e32.idiag = s->idiag32.as<V32>();
+    e32.prof = &s->prof;
+    V64* R = (V64*)s->tmp.ensure(nk * sizeof(V64));
+    V32* R32 = (V32*)s->B32.ensure(nk * sizeof(V32));
+    V32* E32 = (V32*)s->X32.ensure(nk * sizeof(V32));
+    ColState* ci = (ColState*)s->cs_inner.ensure(sizeof(ColState) * k);
+    double* pt = e64.parts(k, 1);
+    e64.spmm(k, X, R, nullptr, false, nullptr, nullptr, 0);
+    launch(resid_kernel<V64>, cdiv_u(nk, 256), 256, 0, s->stream, n, k, k, B, R, nullptr);
+    launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, B, B, nullptr, nullptr, pt, 1,
+                                                                      e64.ntiles(), nullptr);
+    e64.template finalize<1>(k, co, PH_BNORM);
+    const int max_outer = 12;
+    const double inner_tol = 1e-5;
+    for (int step = 0; step <= max_outer; step++) {
+        launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, R, R, nullptr, nullptr, pt, 1,
+                                                                          e64.ntiles(), nullptr);
+        e64.template finalize<1>(k, co, PH_RESID);
+        launch(refine_check_kernel, cdiv_u(k, 128), 128, 0, s->stream, k, co, step ? ci : nullptr, step, max_outer);
+        if (e64.count_active(k, co) == 0) break;
+        launch(cast_kernel<V32, V64>, cdiv_u(nk, 256), 256, 0, s->stream, nk, R, R32);
+        TG_CUDA(cudaMemsetAsync(E32, 0, nk * sizeof(V32), s->stream));
+        launch(init_inner_kernel, cdiv_u(k, 128), 128, 0, s->stream, k, co, ci, inner_tol, maxit);
+        e32.solve(s->method, k, R32, E32, ci, true);
+        launch(mask_vec_kernel<V32>, cdiv_u(nk, 256), 256, 0, s->stream, n, k, co, E32);
+        launch(add_correction_kernel<V64, V32>, cdiv_u(nk, 256), 256, 0, s->stream, nk, X, E32);
+        e64.spmm(k, X, R, nullptr, false, nullptr, nullptr, 0);
+        launch(resid_kernel<V64>, cdiv_u(nk, 256), 256, 0, s->stream, n, k, k, B, R, nullptr);
+    }
+}
+
+static void read_results(tg_solver s, int k, const ColState* co, tg_result* res)
+{
+    std::vector<ColState> h(k);
+    TG_CUDA(cudaMemcpyAsync(h.data(), co, sizeof(ColState) * k, cudaMemcpyDeviceToHost, s->stream));
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+    for (int c = 0; c < k; c++) {
+        res[c].it_count = h[c].its;
+        res[c].status = h[c].status;
+        res[c].rel_err = h[c].bnorm > 0 ? h[c].err / h[c].bnorm : 0.0;
+    }
+}
+
+// Projections y_l for node-major fields X (n x ldx) and source-major device
+// detector vectors mvec (nm x n).  lin/lg: device outputs (either may be null).
+template <class V>
+static void project_nm(tg_solver s, const V* X, int ldx, int nm, const V* mvec, const LinkHost& L,
+                       V* lin, V* lg)
+{
+    const MeshDev& m = s->mesh->d;
+    int n = m.n, nqm = (int)L.q.size();
+    if (nqm == 0) return;
+    int* flag = (int*)s->pflag.ensure((size_t)n * sizeof(int));
+    int* sup = (int*)s->psup.ensure((size_t)n * sizeof(int));
+    int* nsup = (int*)s->pnsup.ensure(sizeof(int));
+    V* Msup = (V*)s->pMsup.ensure((size_t)n * std::max(nm, 1) * sizeof(V));
+    launch(support_flag_kernel<V>, cdiv_u(n, 256), 256, 0, s->stream, n, nm, mvec, flag);
+    launch(support_scan_kernel, 1, 1024, 0, s->stream, n, flag, sup, nsup);
+    launch(support_gather_kernel<V>, cdiv_u((size_t)n * nm, 256), 256, 0, s->stream, n, nm, nsup, sup, mvec, Msup);
+    upload_async(s, s->plink_q, L.q);
+    upload_async(s, s->plink_m, L.m);
+    ProfScope ps(&s->prof, PC_PROJ, s->stream);
+    launch(project_kernel<V>, cdiv_u((size_t)nqm * 32, 256), 256, 0, s->stream, 
+        nsup, sup, X, ldx, Msup, nm, s->plink_q.as<int>(), s->plink_m.as<int>(), nqm, lg != nullptr, lin, lg);
+    TG_CUDA(cudaGetLastError());
+}
+
+template <class VC>
+static void launch_jacobian(tg_solver s, int nq, const VC* F, int nm, const VC* G, const LinkHost& L,
+                            const VC* yinv, void* J, int out_fp32)
+{
+    const MeshDev& m = s->mesh->d;
+    upload_async(s, s->jpair, L.pair);
+    JacArgs<VC> a;
+    a.m = m; a.nq = nq; a.nm = nm; a.nqm = (int)L.q.size();
+    a.F = F; a.ldf = nq; a.G = G; a.ldg = nm;
+    a.pairidx = s->jpair.as<int>(); a.yinv = yinv; a.J = J; a.out_fp32 = out_fp32;
+    // the largest CSR row span of a node tile sets the shared-memory size
+    const std::vector<int>& rp = s->mesh->h.rowptr;
+    int rmax = 0;
+    for (int k0 = 0; k0 < m.n; k0 += JT_NODES) rmax = std::max(rmax, rp[std::min(m.n, k0 + JT_NODES)] - rp[k0]);
+    size_t smem = (size_t)rmax * (3 * JT_M + JT_Q) * sizeof(VC);
+    TG_CHECK(smem <= 220 * 1024, TG_ERR_UNSUPPORTED, "mesh node degree too high for the Jacobian tile");
+    TG_CUDA(cudaFuncSetAttribute(jacobian_kernel<VC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid(cdiv_u(m.n, JT_NODES), cdiv_u(nm, JT_M));
+    ProfScope ps(&s->prof, PC_JAC, s->stream);
+    launch(jacobian_kernel<VC>, grid, JT_Q * JT_M, smem, s->stream, a);
+    TG_CUDA(cudaGetLastError());
+}
+
+// Jacobian from node-major FP64 fields; the mixed path computes it in FP32
+// from FP32 copies of the (refined) fields.  ylin: device linear projections or null.
+template <class V64, class V32>
+static void jacobian_nm(tg_solver s, int nq, const V64* F, int nm, const V64* G, const LinkHost& L,
+                        const V64* ylin, void* J, int out_fp32)
+{
+    const MeshDev& m = s->mesh->d;
+    int n = m.n, nqm = (int)L.q.size();
+    if (s->precision == TG_PREC_MIXED) {
+        V32* F32 = (V32*)s->jF.ensure((size_t)n * nq * sizeof(V32));
+        V32* G32 = (V32*)s->jG.ensure((size_t)n * nm * sizeof(V32));
+        launch(cast_kernel<V32, V64>, cdiv_u((size_t)n * nq, 256), 256, 0, s->stream, (size_t)n * nq, F, F32);
+        launch(cast_kernel<V32, V64>, cdiv_u((size_t)n * nm, 256), 256, 0, s->stream, (size_t)n * nm, G, G32);
+        V32* yi = nullptr;
+        if (ylin) {
+            yi = (V32*)s->jyinv.ensure((size_t)std::max(nqm, 1) * sizeof(V32));
+            launch(recip_cast_kernel<V32, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, ylin, yi);
+        }
+        launch_jacobian<V32>(s, nq, F32, nm, G32, L, yi, J, out_fp32);
+    } else {
+        V64* yi = nullptr;
+        if (ylin) {
+            yi = (V64*)s->jyinv.ensure((size_t)std::max(nqm, 1) * sizeof(V64));
+            launch(recip_cast_kernel<V64, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, ylin, yi);
+        }
+        launch_jacobian<V64>(s, nq, F, nm, G, L, yi, J, out_fp32);
+    }
+}
+
+template <class V>
+static void src_to_nm(tg_solver s, int n, int k, const V* src, V* dst)
+{
+    launch(to_nodemajor_kernel<V, V>, dim3(cdiv_u(n, 32), cdiv_u(k, 32)), dim3(32, 8), 0, s->stream, n, k, k, src, dst);
+}
+template <class V>
+static void nm_to_src(tg_solver s, int n, int k, const V* nm, V* dst)
+{
+    launch(to_srcmajor_kernel<V, V>, dim3(cdiv_u(n, 32), cdiv_u(k, 32)), dim3(32, 8), 0, s->stream, n, k, k, nm, dst);
+}
+
+// ---------------------------------------------------------------------------
+// API bodies (templated on the FP64 / low-precision value pair)
+// ---------------------------------------------------------------------------
+template <class V64, class V32>
+static void api_calc_fields(tg_solver s, int k, const double* qvec, double* phi, int mem, tg_result* res)
+{
+    int n = s->mesh->d.n;
+    size_t bytes = (size_t)n * k * sizeof(V64);
+    const V64* Qs = (const V64*)dev_in(s, qvec, bytes, mem, s->io_a);
+    const V64* Ps = (const V64*)dev_in(s, phi, bytes, mem, s->io_b);
+    V64* B = (V64*)s->B.ensure(bytes);
+    V64* X = (V64*)s->X.ensure(bytes);
+    src_to_nm(s, n, k, Qs, B);
+    src_to_nm(s, n, k, Ps, X);
+    ColState* co = (ColState*)s->cs_outer.ensure(sizeof(ColState) * k);
+    solve_nm<V64, V32>(s, k, B, X, co);
+    V64* out = mem == TG_MEM_DEVICE ? (V64*)phi : (V64*)s->io_b.ensure(bytes);
+    nm_to_src(s, n, k, X, out);
+    TG_CUDA(cudaGetLastError());
+    if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(phi, out, bytes, cudaMemcpyDeviceToHost, s->stream));
+    if (res) read_results(s, k, co, res);
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+template <class V64>
+static void api_project(tg_solver s, int nq, const double* phi, int nm, const double* mvec, const LinkHost& L,
+                        int scale, double* proj, int mem)
+{
+    int n = s->mesh->d.n, nqm = (int)L.q.size();
+    const V64* P = (const V64*)dev_in(s, phi, (size_t)nq * n * sizeof(V64), mem, s->io_a);
+    const V64* Mv = (const V64*)dev_in(s, mvec, (size_t)nm * n * sizeof(V64), mem, s->io_b);
+    V64* X = (V64*)s->X.ensure((size_t)nq * n * sizeof(V64));
+    src_to_nm(s, n, nq, P, X);
+    V64* out = mem == TG_MEM_DEVICE ? (V64*)proj : (V64*)s->plin.ensure((size_t)nqm * sizeof(V64));
+    project_nm<V64>(s, X, nq, nm, Mv, L, scale == TG_DATA_LIN ? out : nullptr, scale == TG_DATA_LOG ? out : nullptr);
+    if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(proj, out, (size_t)nqm * sizeof(V64), cudaMemcpyDeviceToHost, s->stream));
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+template <class V64, class V32>
+static void api_jacobian(tg_solver s, int nq, const double* dphi, int nm, const double* aphi, const double* proj,
+                         const LinkHost& L, int scale, void* J, int out_fp32, int mem)
+{
+    int n = s->mesh->d.n, nqm = (int)L.q.size();
+    const V64* Fs = (const V64*)dev_in(s, dphi, (size_t)nq * n * sizeof(V64), mem, s->io_a);
+    const V64* Gs = (const V64*)dev_in(s, aphi, (size_t)nm * n * sizeof(V64), mem, s->io_b);
+    V64* F = (V64*)s->X.ensure((size_t)nq * n * sizeof(V64));
+    V64* G = (V64*)s->tmp.ensure((size_t)nm * n * sizeof(V64));
+    src_to_nm(s, n, nq, Fs, F);
+    src_to_nm(s, n, nm, Gs, G);
+    const V64* yl = scale == TG_DATA_LOG ? (const V64*)dev_in(s, proj, (size_t)nqm * sizeof(V64), mem, s->plin) : nullptr;
+    size_t jbytes = (size_t)2 * nqm * (vt<V64>::cplx ? 2 * n : n) * (out_fp32 ? 4 : 8);
+    void* Jd = mem == TG_MEM_DEVICE ? J : s->jout.ensure(jbytes);
+    jacobian_nm<V64, V32>(s, nq, F, nm, G, L, yl, Jd, out_fp32);
+    if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(J, Jd, jbytes, cudaMemcpyDeviceToHost, s->stream));
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+template <class V64, class V32>
+static void api_forward_path(tg_solver s, const double* cmua, const double* ckap, const double* c2a, double omega,
+                             int nq, const double* qvec, int nm, const double* mvec, const LinkHost& L,
+                             double* dphi, double* aphi, double* proj, double* logproj, void* J, int j_fp32, int mem,
+                             tg_result* res)
+{
+    const MeshDev& m = s->mesh->d;
+    int n = m.n, nqm = (int)L.q.size();
+    do_reset<V64, V32>(s, cmua, ckap, c2a, omega, mem);
+    s->reset_done = true;
+    size_t qb = (size_t)nq * n * sizeof(V64), mb = (size_t)nm * n * sizeof(V64);
+    const V64* Qs = (const V64*)dev_in(s, qvec, qb, mem, s->io_a);
+    const V64* Ms = (const V64*)dev_in(s, mvec, mb, mem, s->io_b);
+    V64* Bq = (V64*)s->fp_bq.ensure(qb);
+    V64* Xq = (V64*)s->fp_xq.ensure(qb);
+    V64* Bm = (V64*)s->fp_bm.ensure(mb);
+    V64* Xm = (V64*)s->fp_xm.ensure(mb);
+    src_to_nm(s, n, nq, Qs, Bq);
+    src_to_nm(s, n, nm, Ms, Bm);
+    TG_CUDA(cudaMemsetAsync(Xq, 0, qb, s->stream));
+    TG_CUDA(cudaMemsetAsync(Xm, 0, mb, s->stream));
+    ColState* co = (ColState*)s->cs_outer.ensure(sizeof(ColState) * std::max(nq, nm));
+    solve_nm<V64, V32>(s, nq, Bq, Xq, co);
+    if (res) read_results(s, nq, co, res);
+    // the mvec rows are the adjoint sources (toastmodule.cc:1556-1557)
+    solve_nm<V64, V32>(s, nm, Bm, Xm, co);
+    if (res) read_results(s, nm, co, res + nq);
+    V64* ylin = (V64*)s->fp_lin.ensure((size_t)std::max(nqm, 1) * sizeof(V64));
+    V64* ylog = (V64*)s->fp_log.ensure((size_t)std::max(nqm, 1) * sizeof(V64));
+    project_nm<V64>(s, Xq, nq, nm, Ms, L, ylin, ylog);
+    if (J) {
+        size_t jbytes = (size_t)2 * nqm * (vt<V64>::cplx ? 2 * n : n) * (j_fp32 ? 4 : 8);
+        void* Jd = mem == TG_MEM_DEVICE ? J : s->jout.ensure(jbytes);
+        jacobian_nm<V64, V32>(s, nq, Xq, nm, Xm, L, ylin, Jd, j_fp32);
+        if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(J, Jd, jbytes, cudaMemcpyDeviceToHost, s->stream));
+    }
+    auto out_field = [&](double* dst, const V64* src_nm, int k, DBuf& stage) {
+        if (!dst) return;
+        size_t b = (size_t)k * n * sizeof(V64);
+        V64* o = mem == TG_MEM_DEVICE ? (V64*)dst : (V64*)stage.ensure(b);
+        nm_to_src(s, n, k, src_nm, o);
+        if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(dst, o, b, cudaMemcpyDeviceToHost, s->stream));
+    };
+    out_field(dphi, Xq, nq, s->io_a);
+    out_field(aphi, Xm, nm, s->io_b);
+    auto out_small = [&](double* dst, const V64* src) {
+        if (!dst) return;
+        TG_CUDA(cudaMemcpyAsync(dst, src, (size_t)nqm * sizeof(V64),
+                                mem == TG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s->stream));
+    };
+    out_small(proj, ylin);
+    out_small(logproj, ylog);
+    TG_CUDA(cudaGetLastError());
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* tg_last_error(void) { return tg::last_error(); }
+
+int tg_mesh_create(int dim, int n, const double* coords, int ne, const int* elnodes, tg_mesh* out)
+{
+    API_BEGIN
+    TG_CHECK(out, TG_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    auto h = std::make_unique<tg_mesh_s>();
+    h->m.reset(mesh_build(dim, n, coords, ne, elnodes));
+    *out = h.release();
+    API_END
+}
+
+int tg_mesh_destroy(tg_mesh mesh)
+{
+    API_BEGIN
+    delete mesh;
+    API_END
+}
+
+int tg_mesh_info(tg_mesh mesh, int* n, int* ne, int* nnz, int* nbnd, int* nlev_fwd, int* nlev_bwd)
+{
+    API_BEGIN
+    TG_CHECK(mesh, TG_ERR_ARG, "mesh is NULL");
+    const MeshDev& d = mesh->m->d;
+    if (n) *n = d.n;
+    if (ne) *ne = d.ne;
+    if (nnz) *nnz = d.nnz;
+    if (nbnd) { int c = 0; for (unsigned char b : mesh->m->h.bndnode) c += b; *nbnd = c; }
+    if (nlev_fwd) *nlev_fwd = d.nlev_fwd;
+    if (nlev_bwd) *nlev_bwd = d.nlev_bwd;
+    API_END
+}
+
+int tg_mesh_csr(tg_mesh mesh, int* rowptr, int* colidx)
+{
+    API_BEGIN
+    TG_CHECK(mesh && rowptr && colidx, TG_ERR_ARG, "NULL argument");
+    const MeshHost& h = mesh->m->h;
+    memcpy(rowptr, h.rowptr.data(), h.rowptr.size() * sizeof(int));
+    memcpy(colidx, h.colidx.data(), h.colidx.size() * sizeof(int));
+    API_END
+}
+
+int tg_mesh_boundary(tg_mesh mesh, unsigned char* bnd)
+{
+    API_BEGIN
+    TG_CHECK(mesh && bnd, TG_ERR_ARG, "NULL argument");
+    memcpy(bnd, mesh->m->h.bndnode.data(), mesh->m->h.bndnode.size());
+    API_END
+}
+
+int tg_qvec_gaussian(tg_mesh mesh, int npos, const double* pos, double width, int neumann, double* out)
+{
+    API_BEGIN
+    TG_CHECK(mesh && (npos == 0 || (pos && out)), TG_ERR_ARG, "NULL argument");
+    TG_CHECK(width > 0, TG_ERR_ARG, "width must be positive");
+    const MeshHost& h = mesh->m->h;
+    for (int p = 0; p < npos; p++)
+        qvec_gaussian_host(h, pos + (size_t)p * h.dim, width, neumann != 0, out + (size_t)p * h.n);
+    API_END
+}
+
+int tg_solver_create(tg_mesh mesh, int is_complex, int method, int precon, double tol, int maxit, int precision,
+                     tg_solver* out)
+{
+    API_BEGIN
+    TG_CHECK(mesh && out, TG_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    TG_CHECK(method == TG_SOLVER_CG || method == TG_SOLVER_BICGSTAB || method == TG_SOLVER_GMRES, TG_ERR_ARG,
+             "unknown solver method");
+    TG_CHECK(precon >= TG_PRECON_NONE && precon <= TG_PRECON_DILU, TG_ERR_ARG, "unknown preconditioner");
+    TG_CHECK(precision == TG_PREC_FP64 || precision == TG_PREC_MIXED, TG_ERR_ARG, "unknown precision");
+    TG_CHECK(tol > 0, TG_ERR_ARG, "tolerance must be positive");
+    TG_CHECK(maxit >= 0, TG_ERR_ARG, "maxit must be >= 0");
+    TG_CHECK(method != TG_SOLVER_GMRES, TG_ERR_UNSUPPORTED, "GMRES is not implemented on the GPU yet");
+    TG_CHECK(!(method == TG_SOLVER_CG && is_complex), TG_ERR_UNSUPPORTED, "CG is only implemented for real systems");
+    auto s = std::make_unique<tg_solver_s>();
+    s->mesh = mesh->m.get();
+    s->cplx = is_complex != 0; s->method = method; s->precon = precon; s->tol = tol;
+    s->maxit = maxit; s->precision = precision;
+    TG_CUDA(cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking));
+    s->stream = s->own;
+    *out = s.release();
+    API_END
+}
+
+int tg_solver_destroy(tg_solver s)
+{
+    API_BEGIN
+    if (!s) return TG_OK;
+    cudaStreamSynchronize(s->stream);
+    cudaStream_t own = s->own;
+    delete s;
+    if (own) cudaStreamDestroy(own);
+    API_END
+}
+
+int tg_solver_set(tg_solver s, double tol, int maxit)
+{
+    API_BEGIN
+    TG_CHECK(s && tol > 0 && maxit >= 0, TG_ERR_ARG, "invalid argument");
+    s->tol = tol; s->maxit = maxit;
+    API_END
+}
+
+int tg_solver_set_stream(tg_solver s, void* stream)
+{
+    API_BEGIN
+    TG_CHECK(s, TG_ERR_ARG, "solver is NULL");
+    s->stream = stream ? (cudaStream_t)stream : s->own;
+    API_END
+}
+
+int tg_solver_sync(tg_solver s)
+{
+    API_BEGIN
+    TG_CHECK(s, TG_ERR_ARG, "solver is NULL");
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+    API_END
+}
+
+int tg_solver_reset(tg_solver s, const double* cmua, const double* ckappa, const double* c2a, double omega, int mem)
+{
+    API_BEGIN
+    TG_CHECK(s && cmua && ckappa && c2a, TG_ERR_ARG, "NULL argument");
+    TG_CHECK(s->cplx || omega == 0.0, TG_ERR_ARG, "nonzero omega for a real system");
+    std::lock_guard<std::mutex> g(s->mu);
+    if (s->cplx) do_reset<cd, cf>(s, cmua, ckappa, c2a, omega, mem);
+    else do_reset<double, float>(s, cmua, ckappa, c2a, omega, mem);
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+    s->reset_done = true;
+    API_END
+}
+
+int tg_solver_matrix(tg_solver s, double* val, int mem)
+{
+    API_BEGIN
+    TG_CHECK(s && val, TG_ERR_ARG, "NULL argument");
+    TG_CHECK(s->reset_done, TG_ERR_STATE, "tg_solver_reset has not been called");
+    size_t b = (size_t)s->mesh->d.nnz * vsize(s->cplx, false);
+    TG_CUDA(cudaMemcpyAsync(val, s->val64.p, b, mem == TG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                            s->stream));
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+    API_END
+}
+
+int tg_calc_fields(tg_solver s, int nrhs, const double* qvec, double* phi, int mem, tg_result* res)
+{
+    API_BEGIN
+    TG_CHECK(s, TG_ERR_ARG, "solver is NULL");
+    TG_CHECK(nrhs >= 0, TG_ERR_ARG, "nrhs < 0");
+    if (nrhs == 0) return TG_OK;
+    TG_CHECK(qvec && phi, TG_ERR_ARG, "NULL argument");
+    TG_CHECK(s->reset_done, TG_ERR_STATE, "tg_solver_reset has not been called");
+    std::lock_guard<std::mutex> g(s->mu);
+    if (s->cplx) api_calc_fields<cd, cf>(s, nrhs, qvec, phi, mem, res);
+    else api_calc_fields<double, float>(s, nrhs, qvec, phi, mem, res);
+    API_END
+}
+
+int tg_project_all(tg_solver s, int nq, const double* phi, int nm, const double* mvec, const int* link_ofs,
+                   const int* link_m, int scale, double* proj, int mem)
+{
+    API_BEGIN
+    TG_CHECK(s && link_ofs && proj && phi && mvec, TG_ERR_ARG, "NULL argument");
+    TG_CHECK(nq >= 0 && nm >= 0, TG_ERR_ARG, "negative count");
+    TG_CHECK(scale == TG_DATA_LIN || scale == TG_DATA_LOG, TG_ERR_ARG, "scale must be TG_DATA_LIN or TG_DATA_LOG");
+    std::lock_guard<std::mutex> g(s->mu);
+    LinkHost L = make_links(nq, nm, link_ofs, link_m);
+    if (L.q.empty()) return TG_OK;
+    if (s->cplx) api_project<cd>(s, nq, phi, nm, mvec, L, scale, proj, mem);
+    else api_project<double>(s, nq, phi, nm, mvec, L, scale, proj, mem);
+    API_END
+}
+
+int tg_jacobian(tg_solver s, int nq, const double* dphi, int nm, const double* aphi, const double* proj,
+                const int* link_ofs, const int* link_m, int scale, void* J, int out_fp32, int mem)
+{
+    API_BEGIN
+    TG_CHECK(s && dphi && aphi && link_ofs && J, TG_ERR_ARG, "NULL argument");
+    TG_CHECK(scale == TG_DATA_LIN || (scale == TG_DATA_LOG && proj), TG_ERR_ARG, "log data needs the projections");
+    std::lock_guard<std::mutex> g(s->mu);
+    LinkHost L = make_links(nq, nm, link_ofs, link_m);
+    if (L.q.empty()) return TG_OK;
+    if (s->cplx) api_jacobian<cd, cf>(s, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
+    else api_jacobian<double, float>(s, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
+    API_END
+}
+
+int tg_forward_path(tg_solver s, const double* cmua, const double* ckappa, const double* c2a, double omega, int nq,
+                    const double* qvec, int nm, const double* mvec, const int* link_ofs, const int* link_m,
+                    double* dphi, double* aphi, double* proj, double* logproj, void* J, int j_fp32, int mem,
+                    tg_result* res)
+{
+    API_BEGIN
+    TG_CHECK(s && cmua && ckappa && c2a && qvec && mvec && link_ofs, TG_ERR_ARG, "NULL argument");
+    TG_CHECK(nq > 0 && nm > 0, TG_ERR_ARG, "need at least one source and one detector");
+    TG_CHECK(s->cplx || omega == 0.0, TG_ERR_ARG, "nonzero omega for a real system");
+    std::lock_guard<std::mutex> g(s->mu);
+    LinkHost L = make_links(nq, nm, link_ofs, link_m);
+    if (s->cplx)
+        api_forward_path<cd, cf>(s, cmua, ckappa, c2a, omega, nq, qvec, nm, mvec, L, dphi, aphi, proj, logproj, J,
+                                 j_fp32, mem, res);
+    else
+        api_forward_path<double, float>(s, cmua, ckappa, c2a, omega, nq, qvec, nm, mvec, L, dphi, aphi, proj, logproj,
+                                        J, j_fp32, mem, res);
+    API_END
+}
+
+int tg_solver_profile(tg_solver s, int mask)
+{
+    API_BEGIN
+    TG_CHECK(s, TG_ERR_ARG, "solver is NULL");
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+    s->prof.mask = mask;
+    for (auto& v : s->prof.ev) v.clear();
+    s->prof.used = 0;
+    API_END
+}
+
+int tg_solver_profile_read(tg_solver s, int cls, double* total_ms, int* count)
+{
+    API_BEGIN
+    TG_CHECK(s && cls >= 0 && cls < PC_N, TG_ERR_ARG, "invalid argument");
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+    double t = 0.0;
+    for (auto& pr : s->prof.ev[cls]) {
+        float ms = 0.f;
+        TG_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
+        t += ms;
+    }
+    if (total_ms) *total_ms = t;
+    if (count) *count = (int)s->prof.ev[cls].size();
+    API_END
+}
+
+int tg_launch_count(long long* count)
+{
+    API_BEGIN
+    TG_CHECK(count, TG_ERR_ARG, "count is NULL");
+    *count = g_nlaunch.load();
+    API_END
+}
+
+}  // extern "C"
