@@ -140,6 +140,25 @@ int tg_forward_path(tg_solver s, const double *cmua, const double *ckappa, const
                     const int *link_ofs, const int *link_m, double *dphi, double *aphi,
                     double *proj, double *logproj, void *J, int j_fp32, int mem, tg_result *res);
 
+/* ---- fixed-scratch variant (no counterpart in the reference) -------------
+   ProjectAll for callers that cannot call cudaMalloc (a device memory pool
+   owned by another runtime, real-time loops that must not allocate, plug-ins
+   whose host forbids allocation).  Same result as tg_project_all, but phi,
+   mvec and proj are device memory (source-major, as tg_project_all), the
+   link list is host memory, and the scratch lives in one fixed file-scope
+   device array of TG_NOALLOC_SCRATCH_BYTES held by every GPU that loads the
+   library.  No cudaMalloc/cudaFree or allocating routine is called.
+   - Problems whose scratch does not fit (about 4 (2n + nQ + nQM) bytes plus
+     the detector vectors on their support, nsup x nM values) are rejected
+     with TG_ERR_UNSUPPORTED and a message; use tg_project_all for them.
+   - The first call on a device looks up the array's device address
+     (cudaGetSymbolAddress); make that first call before any stream capture.
+   - All calls share the array: calls that overlap on the GPU race, so
+     serialise them.  The call synchronises the solver's stream. */
+#define TG_NOALLOC_SCRATCH_BYTES (8 * 1024 * 1024)
+int tg_project_all_noalloc(tg_solver s, int nq, const double *phi, int nm, const double *mvec,
+                           const int *link_ofs, const int *link_m, int scale, double *proj);
+
 /* ---- measurement (no counterpart in the reference: its timing is
    tic/toc/walltic around calls, src/libmath/timing.h:4-20) ----------------- */
 /* kernel classes for tg_solver_profile's mask (bit = 1 << class) */

@@ -26,7 +26,7 @@ DATA_LIN, DATA_LOG = 1, 2
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
            "tg_qvec_gaussian", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
-           "tg_jacobian", "tg_forward_path", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count",
+           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count",
            "tg_last_error"]
 PROF_SPMM, PROF_SWEEP, PROF_VEC, PROF_JAC, PROF_ASM, PROF_PROJ = range(6)
 
@@ -69,6 +69,7 @@ def lib():
             "tg_project_all": [vp, i_, dp, i_, dp, vp, vp, i_, dp, i_],
             "tg_jacobian": [vp, i_, dp, i_, dp, dp, vp, vp, i_, vp, i_, i_],
             "tg_forward_path": [vp, dp, dp, dp, d_, i_, dp, i_, dp, vp, vp, dp, dp, dp, dp, vp, i_, i_, vp],
+            "tg_project_all_noalloc": [vp, i_, dp, i_, dp, vp, vp, i_, dp],
             "tg_solver_profile": [vp, i_],
             "tg_solver_profile_read": [vp, i_, C.POINTER(C.c_double), ip],
             "tg_launch_count": [C.POINTER(C.c_longlong)],
@@ -233,6 +234,12 @@ class FwdSolver:
         _check(lib().tg_project_all(self._h, phi.shape[0], _ptr(phi), mv.shape[0], _ptr(mv), _ptr(links.ofs),
                                     _ptr(links.m), scale, _ptr(out), MEM_HOST))
         return out
+
+    def project_all_noalloc(self, d_phi, nq, d_mvec, nm, links: Links, scale, d_proj):
+        """tg_project_all_noalloc: device inputs/outputs, fixed device scratch,
+        no device allocation by the library."""
+        _check(lib().tg_project_all_noalloc(self._h, int(nq), _ptr(d_phi), int(nm), _ptr(d_mvec), _ptr(links.ofs),
+                                            _ptr(links.m), int(scale), _ptr(d_proj)))
 
     def jacobian(self, dphi, aphi, proj, links: Links, scale=DATA_LOG, fp32=False):
         dphi = _f64(dphi, self.complex)

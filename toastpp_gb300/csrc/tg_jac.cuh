@@ -23,7 +23,7 @@ __global__ void support_flag_kernel(int n, int nm, const V* __restrict__ mvec, i
 }
 
 // ordered compaction by one block (deterministic): sup = indices with flag set
-__global__ void support_scan_kernel(int n, const int* __restrict__ flag, int* __restrict__ sup, int* __restrict__ nsup)
+static __global__ void support_scan_kernel(int n, const int* __restrict__ flag, int* __restrict__ sup, int* __restrict__ nsup)
 {
     __shared__ int cnt[1024];
     int t = threadIdx.x, nt = blockDim.x;

@@ -27,12 +27,12 @@ struct ColState {
 // src/libfe/mesh.cc:1958-2129; AddToSysMatrix iCFF, mesh.cc:2252-2282).
 // ---------------------------------------------------------------------------
 
-__constant__ int c_tet_fff[4][4][4] = {  // Tet4 IntFFF planes x120 (tet4.cc:49-77)
+static __constant__ int c_tet_fff[4][4][4] = {  // Tet4 IntFFF planes x120 (tet4.cc:49-77)
     {{6,2,2,2},{2,2,1,1},{2,1,2,1},{2,1,1,2}},
     {{2,2,1,1},{2,6,2,2},{1,2,2,1},{1,2,1,2}},
     {{2,1,2,1},{1,2,2,1},{2,2,6,2},{1,1,2,2}},
     {{2,1,1,2},{1,2,1,2},{1,1,2,2},{2,2,2,6}}};
-__constant__ int c_tet_bfff[4][4][4][4] = {  // Tet4 face IntFFF tables x60 (tet4.cc:724-817)
+static __constant__ int c_tet_bfff[4][4][4][4] = {  // Tet4 face IntFFF tables x60 (tet4.cc:724-817)
     { {{6,2,2,0},{2,2,1,0},{2,1,2,0},{0,0,0,0}}, {{2,2,1,0},{2,6,2,0},{1,2,2,0},{0,0,0,0}},
       {{2,1,2,0},{1,2,2,0},{2,2,6,0},{0,0,0,0}}, {{0,0,0,0},{0,0,0,0},{0,0,0,0},{0,0,0,0}} },
     { {{6,2,0,2},{2,2,0,1},{0,0,0,0},{2,1,0,2}}, {{2,2,0,1},{2,6,0,2},{0,0,0,0},{1,2,0,2}},
@@ -594,7 +594,7 @@ __global__ void diag_inv_kernel(int n, const int* __restrict__ diagpos, const V*
     else out[i] = z ? 1.0 : 1.0 / d;
 }
 
-__global__ void count_active_kernel(int k, const ColState* __restrict__ cst, int* out)
+static __global__ void count_active_kernel(int k, const ColState* __restrict__ cst, int* out)
 {
     __shared__ int s;
     if (threadIdx.x == 0) s = 0;

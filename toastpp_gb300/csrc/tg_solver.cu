@@ -961,4 +961,14 @@ int tg_launch_count(long long* count)
     API_END
 }
 
+// internal accessor for the fixed-scratch entry point (tg_noalloc.cu)
+__attribute__((visibility("hidden"))) int tg_solver_internal(tg_solver s, int* n, int* cplx, cudaStream_t* stream)
+{
+    if (!s) return TG_ERR_ARG;
+    *n = s->mesh->d.n;
+    *cplx = s->cplx;
+    *stream = s->stream;
+    return TG_OK;
+}
+
 }  // extern "C"
