@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--tol", type=float, default=1e-12)
+    ap.add_argument("--inner-tol", type=float, default=1e-4, help="mixed path: inner FP32 solve tolerance")
+    ap.add_argument("--inner-order", type=int, default=1, help="mixed path: inner IC(0) ordering, 1 colour, 0 natural")
     ap.add_argument("--no-compare", action="store_true", help="skip the FP64 comparison legs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     return ap.parse_args()
@@ -198,7 +200,8 @@ def run_gpu(args):
     mvec = (gm.qvec_gaussian(P.qm.M, P.mwidth) * ca[None, :]).astype(np.complex128)
     links = capi.Links(P.qm.link_ofs, P.qm.link_m)
     dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream(device=dev)   # the library launches on this stream
+    torch.cuda.set_stream(stream)
     j_fp32 = args.precision == "mixed"
 
     def dtensor(a):
@@ -216,6 +219,8 @@ def run_gpu(args):
 
     s = capi.FwdSolver(gm, "BICGSTAB", args.tol, "ICH", True, precision=args.precision)
     s.set_stream(stream.cuda_stream)
+    if args.precision == "mixed":
+        s.set_refinement(args.inner_tol, 12, args.inner_order)
     res = (capi.TgResult * (nq + nm))()
 
     def step():
@@ -256,10 +261,11 @@ def run_gpu(args):
     value = ws * nsolves * args.steps / (total_ms / 1e3)
 
     # roofline of the dominant class (algorithmic bytes per launch / event-timed duration)
-    mdev = gm
-    nnz = mdev.nnz
-    k_f = nq
-    names = {capi.PROF_SPMM: "spmm_dot_kernel (complex FP32 SpMM k=80)", capi.PROF_SWEEP: "IC(0) level sweeps",
+    nnz = gm.nnz
+    k_f = nq + nm          # forward and adjoint sources share one batch
+    nnz_l = (nnz - n) // 2
+    names = {capi.PROF_SPMM: f"spmm_dot_kernel (complex SpMM, k={nq + nm})",
+             capi.PROF_SWEEP: f"IC(0) apply: {gm.nlev_fwd}+{gm.nlev_bwd} level kernels (ic_fwd_level/ic_bwd_level) in one graph",
              capi.PROF_JAC: "jacobian_kernel", capi.PROF_ASM: "assembly + IC(0) factor",
              capi.PROF_PROJ: "project_kernel"}
     dom = max(prof, key=lambda c: prof[c][0])
@@ -270,6 +276,8 @@ def run_gpu(args):
         alg_bytes = 2 * nqm * 2 * n * jb + (nq + nm) * n * vb + (n + 1 + nnz) * 4
     elif dom == capi.PROF_SPMM:
         alg_bytes = nnz * (vb + 4) + 4 * (n + 1) + 2 * n * k_f * vb
+    elif dom == capi.PROF_SWEEP:
+        alg_bytes = 2 * (nnz_l * (vb + 4) + 4 * (n + 1)) + n * vb + 4 * n * k_f * vb
     else:
         alg_bytes = None
     dom_ms, dom_cnt = prof[dom]
@@ -369,7 +377,8 @@ def run_gpu(args):
             "dtype": "complex-f32 inner / complex-f64 refinement" if args.precision == "mixed" else "complex-f64",
             "data": "synthetic (seeded mesh, optodes, inclusions)",
             "config": {"workload": f"3D cylinder R25 H50, {n} nodes, {gm.ne} tets, 100 MHz, {nq}+{nm} optodes, "
-                                   f"BiCGSTAB+ICH tol {args.tol}, {args.precision}, nodal Jacobian "
+                                   f"BiCGSTAB+ICH tol {args.tol}, {args.precision}"
+                                   f"{f' (inner FP32 tol {args.inner_tol})' if args.precision == 'mixed' else ''}, nodal Jacobian "
                                    f"{2 * nqm}x{2 * n} ({'fp32' if j_fp32 else 'fp64'})",
                        "parallelism": f"replicas x{ws} (one request per GPU)",
                        "l2": "each step writes the >=3 GB Jacobian, larger than L2"},

@@ -103,6 +103,14 @@ int tg_solver_create(tg_mesh mesh, int is_complex, int method, int precon, doubl
                      int precision, tg_solver *out);
 int tg_solver_destroy(tg_solver s);
 int tg_solver_set(tg_solver s, double tol, int maxit);
+/* mixed precision only: relative tolerance of each FP32 inner solve (default
+   1e-4), the maximum number of FP64 refinement steps (default 12) and the
+   elimination ordering of the inner IC(0) preconditioner: 1 (default) a
+   colour-major ordering of a greedy colouring, whose colour classes are the
+   levels of the triangular sweeps, or 0 the natural ordering of the reference.
+   The FP64 path always factors in the natural ordering.  Takes effect at the
+   next tg_solver_reset. */
+int tg_solver_set_refinement(tg_solver s, double inner_tol, int max_outer, int inner_ordering);
 /* a cudaStream_t; 0 selects the solver's own stream */
 int tg_solver_set_stream(tg_solver s, void *stream);
 int tg_solver_sync(tg_solver s);

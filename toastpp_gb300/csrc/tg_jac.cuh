@@ -62,7 +62,8 @@ __global__ void recip_cast_kernel(int cnt, const From* __restrict__ y, To* __res
 }
 
 template <class V>
-__global__ void project_kernel(const int* __restrict__ nsup_p, const int* __restrict__ sup, const V* __restrict__ X, int ldx,
+__global__ void project_kernel(const int* __restrict__ nsup_p, const int* __restrict__ sup,
+                               const int* __restrict__ perm, const V* __restrict__ X, int ldx,
                                const V* __restrict__ Msup, int nm, const int* __restrict__ link_q,
                                const int* __restrict__ link_m, int nqm, int logscale, V* __restrict__ lin,
                                V* __restrict__ lg)
@@ -71,7 +72,7 @@ __global__ void project_kernel(const int* __restrict__ nsup_p, const int* __rest
     if (l >= nqm) return;
     int q = link_q[l], m = link_m[l], nsup = *nsup_p;
     V s = vzero<V>();
-    for (int t = lane; t < nsup; t += 32) s = vfma(s, X[(size_t)sup[t] * ldx + q], Msup[(size_t)t * nm + m]);
+    for (int t = lane; t < nsup; t += 32) s = vfma(s, X[(size_t)perm[sup[t]] * ldx + q], Msup[(size_t)t * nm + m]);
     for (int o = 16; o; o >>= 1) {
         if constexpr (vt<V>::cplx) { s.x += __shfl_down_sync(0xffffffffu, s.x, o); s.y += __shfl_down_sync(0xffffffffu, s.y, o); }
         else s += __shfl_down_sync(0xffffffffu, s, o);
@@ -95,16 +96,18 @@ __global__ void project_kernel(const int* __restrict__ nsup_p, const int* __rest
 // g = adjoint field, no conjugation).  J = -Re / -Im of PMDF (divided by the
 // linear projection for log data, PMDF_log 76-79).
 //
-// CTA: JT_NODES consecutive nodes x JT_M detectors, looping over sources in
-// chunks of JT_Q; thread (qq, mm) writes JT_NODES consecutive J columns.
-// ---------------------------------------------------------------------------
-constexpr int JT_NODES = 8, JT_M = 8, JT_Q = 16;
+// CTA: KT consecutive nodes (one per lane) x JM detectors, looping over the
+// sources in chunks of JQ.  Phase B builds Hm/Hk for the tile in shared
+// memory (thread = node x detector); phase C gives each lane JR_Q sources x
+// JR_M detectors of its node, so a warp writes KT consecutive J columns
+// (coalesced) for each of its pairs.
+constexpr int JM = 8, JQ = 8, JR_Q = 2, JR_M = 4;
 
 template <class V>
 struct JacArgs {
     MeshDev m;
     int nq, nm, nqm;
-    const V* F; int ldf;          // forward fields, node-major
+    const V* F; int ldf;          // forward fields, node-major (column q of row i at i*ldf + q)
     const V* G; int ldg;          // adjoint fields, node-major
     const int* pairidx;           // nq*nm -> link index or -1
     const V* yinv;                // per link 1/y (log data) or null
@@ -129,113 +132,133 @@ __device__ __forceinline__ double el_intfdd(const MeshDev& m, const double* r, i
     return r[1 + j * 4 + l];                                  // tet4.cc:380-412
 }
 
-template <class V>
-__global__ void __launch_bounds__(JT_Q * JT_M) jacobian_kernel(JacArgs<V> a)
+template <class V, class OUT>
+__device__ __forceinline__ void jac_store(OUT* J, size_t idx, typename vt<V>::R v) { J[idx] = (OUT)v; }
+
+template <class V, int KT>
+__global__ void __launch_bounds__(256) jacobian_kernel(JacArgs<V> a)
 {
     using S = typename vt<V>::R;
     extern __shared__ __align__(16) unsigned char jsm[];
     const MeshDev& m = a.m;
-    int k0 = blockIdx.x * JT_NODES;
-    int m0 = blockIdx.y * JT_M;
-    int kend = min(m.n, k0 + JT_NODES);
-    int base = m.rowptr[k0];
-    int R = m.rowptr[kend] - base;
-    V* Gs = (V*)jsm;                    // R x JT_M
-    V* Hm = Gs + (size_t)R * JT_M;      // R x JT_M
-    V* Hk = Hm + (size_t)R * JT_M;      // R x JT_M
-    V* Fs = Hk + (size_t)R * JT_M;      // R x JT_Q
-    int tid = threadIdx.x, nt = blockDim.x;
-    for (int e = tid; e < R * JT_M; e += nt) {
-        int rr = e / JT_M, mm = e % JT_M;
-        int mg = m0 + mm;
-        Gs[e] = mg < a.nm ? a.G[(size_t)m.colidx[base + rr] * a.ldg + mg] : vzero<V>();
+    const int k0 = blockIdx.x * KT;
+    const int m0 = blockIdx.y * JM;
+    const int kend = min(m.n, k0 + KT);
+    const int base = m.jrowptr[k0];
+    const int R = m.jrowptr[kend] - base;
+    V* Gs = (V*)jsm;                    // R x JM
+    V* Hm = Gs + (size_t)R * JM;        // R x JM
+    V* Hk = Hm + (size_t)R * JM;        // R x JM
+    V* Fs = Hk + (size_t)R * JM;        // R x JQ
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int e = tid; e < R * JM; e += nt) {
+        int rr = e / JM, mm = e % JM, mg = m0 + mm;
+        Gs[e] = mg < a.nm ? a.G[(size_t)m.jcolidx[base + rr] * a.ldg + mg] : vzero<V>();
         Hm[e] = vzero<V>();
         Hk[e] = vzero<V>();
     }
     __syncthreads();
-    // Phase B: H for each node of the tile (thread = node x detector)
-    for (int w = tid; w < JT_NODES * JT_M; w += nt) {
-        int t = w / JT_M, mm = w % JT_M;
-        int k = k0 + t;
+    // Phase B: Hm/Hk rows of every node of the tile; thread = (node, detector).
+    // The IntFFF weights of P1 elements are size/D x {6 all equal, 2 two equal,
+    // 1 distinct} (D = 60 triangles, 120 tetrahedra), so for the element node
+    // i = k:  sum_l IntFFF(i,j,l) g_l = size/D (2 SG + 4 g_i) for j = i and
+    // size/D (SG + g_i + g_j) otherwise, SG = sum of g over the element.
+    for (int w = tid; w < KT * JM; w += nt) {
+        int t = w / JM, mm = w % JM, k = k0 + t;
         if (k >= kend) continue;
-        int rs = m.rowptr[k], re_ = m.rowptr[k + 1];
+        const int rk = m.jrowptr[k] - base;
+        const S inv_d = (S)(m.dim == 2 ? 1.0 / 60.0 : 1.0 / 120.0);
         for (int p = m.nel_ptr[k]; p < m.nel_ptr[k + 1]; p++) {
-            int code = m.nel_list[p];
-            int e = code >> 2, i = code & 3;
-            const int* nd = m.el + (size_t)e * m.nn;
+            const int code = m.nel_list[p];
+            const int e = code >> 2, i = code & 3;
+            const unsigned pk = m.nel_pos[p];
             const double* r = m.rec + (size_t)e * EL_REC;
             int pos[4];
-            for (int j = 0; j < m.nn; j++) {  // position of node(e,j) in row k
-                int lo = rs, hi = re_ - 1, target = nd[j];
-                while (lo < hi) { int mid = (lo + hi) >> 1; if (m.colidx[mid] < target) lo = mid + 1; else hi = mid; }
-                pos[j] = lo - base;
-            }
+            V g[4];
+            V sg = vzero<V>();
             for (int j = 0; j < m.nn; j++) {
-                V hm = Hm[pos[j] * JT_M + mm], hk = Hk[pos[j] * JT_M + mm];
-                for (int l = 0; l < m.nn; l++) {
-                    V g = Gs[pos[l] * JT_M + mm];
-                    hm = vadd(hm, vscale(g, (S)el_intfff(m, r, i, j, l)));
-                    hk = vadd(hk, vscale(g, (S)el_intfdd(m, r, j, l)));
-                }
-                Hm[pos[j] * JT_M + mm] = hm;
-                Hk[pos[j] * JT_M + mm] = hk;
+                pos[j] = rk + (int)((pk >> (8 * j)) & 255u);
+                g[j] = Gs[pos[j] * JM + mm];
+                sg = vadd(sg, g[j]);
+            }
+            const S cf = (S)r[0] * inv_d;
+            for (int j = 0; j < m.nn; j++) {
+                V wm = j == i ? vadd(vscale(sg, (S)2), vscale(g[i], (S)4)) : vadd(vadd(sg, g[i]), g[j]);
+                V hk = vzero<V>();
+                for (int l = 0; l < m.nn; l++) hk = vadd(hk, vscale(g[l], (S)el_intfdd(m, r, j, l)));
+                Hm[pos[j] * JM + mm] = vadd(Hm[pos[j] * JM + mm], vscale(wm, cf));
+                Hk[pos[j] * JM + mm] = vadd(Hk[pos[j] * JM + mm], hk);
             }
         }
     }
     __syncthreads();
-    int qq = tid / JT_M, mm = tid % JT_M;
-    int mg = m0 + mm;
-    int n = m.n;
-    for (int q0 = 0; q0 < a.nq; q0 += JT_Q) {
-        for (int e = tid; e < R * JT_Q; e += nt) {
-            int rr = e / JT_Q, c = e % JT_Q;
-            Fs[e] = (q0 + c) < a.nq ? a.F[(size_t)m.colidx[base + rr] * a.ldf + q0 + c] : vzero<V>();
+    // Phase C: lane = node of the tile; warp = a group of JR_Q x JR_M pairs
+    const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+    const int t = lane, k = k0 + t;
+    const bool kin = (t < KT) && (k < kend);
+    const int rb = kin ? m.jrowptr[k] - base : 0, re2 = kin ? m.jrowptr[k + 1] - base : 0;
+    const int n = m.n;
+    constexpr int GQ = JQ / JR_Q, GM = JM / JR_M;  // pair groups per chunk
+    for (int q0 = 0; q0 < a.nq; q0 += JQ) {
+        for (int e = tid; e < R * JQ; e += nt) {
+            int rr = e / JQ, c = e % JQ;
+            Fs[e] = (q0 + c) < a.nq ? a.F[(size_t)m.jcolidx[base + rr] * a.ldf + q0 + c] : vzero<V>();
         }
         __syncthreads();
-        int q = q0 + qq;
-        int l = (q < a.nq && mg < a.nm) ? a.pairidx[(size_t)q * a.nm + mg] : -1;
-        if (l >= 0) {
-            V yi = a.yinv ? a.yinv[l] : vzero<V>();
-            S om[JT_NODES], ok[JT_NODES], oim[JT_NODES], oik[JT_NODES];
-            for (int t = 0; t < JT_NODES; t++) {
-                int k = k0 + t;
-                V am = vzero<V>(), ak = vzero<V>();
-                if (k < kend) {
-                    for (int rr = m.rowptr[k] - base; rr < m.rowptr[k + 1] - base; rr++) {
-                        V f = Fs[rr * JT_Q + qq];
-                        am = vfma(am, f, Hm[rr * JT_M + mm]);
-                        ak = vfma(ak, f, Hk[rr * JT_M + mm]);
+        for (int grp = warp; grp < GQ * GM; grp += nwarp) {
+            int qq0 = (grp / GM) * JR_Q, mm0 = (grp % GM) * JR_M;
+            V am[JR_Q][JR_M], ak[JR_Q][JR_M];
+#pragma unroll
+            for (int a1 = 0; a1 < JR_Q; a1++)
+#pragma unroll
+                for (int b1 = 0; b1 < JR_M; b1++) { am[a1][b1] = vzero<V>(); ak[a1][b1] = vzero<V>(); }
+            for (int rr = rb; rr < re2; rr++) {
+                V f[JR_Q], hm[JR_M], hk[JR_M];
+#pragma unroll
+                for (int a1 = 0; a1 < JR_Q; a1++) f[a1] = Fs[rr * JQ + qq0 + a1];
+#pragma unroll
+                for (int b1 = 0; b1 < JR_M; b1++) { hm[b1] = Hm[rr * JM + mm0 + b1]; hk[b1] = Hk[rr * JM + mm0 + b1]; }
+#pragma unroll
+                for (int a1 = 0; a1 < JR_Q; a1++)
+#pragma unroll
+                    for (int b1 = 0; b1 < JR_M; b1++) {
+                        am[a1][b1] = vfma(am[a1][b1], f[a1], hm[b1]);
+                        ak[a1][b1] = vfma(ak[a1][b1], f[a1], hk[b1]);
                     }
-                }
-                if (a.yinv) { am = vmul(am, yi); ak = vmul(ak, yi); }
-                om[t] = -re(am); ok[t] = -re(ak); oim[t] = -im(am); oik[t] = -im(ak);
             }
-            int cnt = kend - k0;
-            if constexpr (vt<V>::cplx) {
-                size_t r0 = (size_t)l * 2 * n, r1 = (size_t)(l + a.nqm) * 2 * n;
-                if (a.out_fp32) {
-                    float* J = (float*)a.J;
-                    for (int t = 0; t < cnt; t++) {
-                        J[r0 + k0 + t] = (float)om[t]; J[r1 + k0 + t] = (float)oim[t];
-                        J[r0 + n + k0 + t] = (float)ok[t]; J[r1 + n + k0 + t] = (float)oik[t];
-                    }
-                } else {
-                    double* J = (double*)a.J;
-                    for (int t = 0; t < cnt; t++) {
-                        J[r0 + k0 + t] = om[t]; J[r1 + k0 + t] = oim[t];
-                        J[r0 + n + k0 + t] = ok[t]; J[r1 + n + k0 + t] = oik[t];
+            if (!kin) continue;
+#pragma unroll
+            for (int a1 = 0; a1 < JR_Q; a1++)
+#pragma unroll
+                for (int b1 = 0; b1 < JR_M; b1++) {
+                    int q = q0 + qq0 + a1, mg = m0 + mm0 + b1;
+                    if (q >= a.nq || mg >= a.nm) continue;
+                    int l = a.pairidx[(size_t)q * a.nm + mg];
+                    if (l < 0) continue;
+                    V xm = am[a1][b1], xk = ak[a1][b1];
+                    if (a.yinv) { V yi = a.yinv[l]; xm = vmul(xm, yi); xk = vmul(xk, yi); }
+                    if constexpr (vt<V>::cplx) {
+                        size_t r0 = (size_t)l * 2 * n + k, r1 = (size_t)(l + a.nqm) * 2 * n + k;
+                        if (a.out_fp32) {
+                            float* J = (float*)a.J;
+                            J[r0] = (float)-re(xm); J[r1] = (float)-im(xm);
+                            J[r0 + n] = (float)-re(xk); J[r1 + n] = (float)-im(xk);
+                        } else {
+                            double* J = (double*)a.J;
+                            J[r0] = -re(xm); J[r1] = -im(xm);
+                            J[r0 + n] = -re(xk); J[r1 + n] = -im(xk);
+                        }
+                    } else {
+                        size_t r0 = (size_t)l * n + k, r1 = (size_t)(l + a.nqm) * n + k;
+                        if (a.out_fp32) {
+                            float* J = (float*)a.J;
+                            J[r0] = (float)-xm; J[r1] = (float)-xk;
+                        } else {
+                            double* J = (double*)a.J;
+                            J[r0] = -xm; J[r1] = -xk;
+                        }
                     }
                 }
-            } else {
-                size_t r0 = (size_t)l * n, r1 = (size_t)(l + a.nqm) * n;
-                if (a.out_fp32) {
-                    float* J = (float*)a.J;
-                    for (int t = 0; t < cnt; t++) { J[r0 + k0 + t] = (float)om[t]; J[r1 + k0 + t] = (float)ok[t]; }
-                } else {
-                    double* J = (double*)a.J;
-                    for (int t = 0; t < cnt; t++) { J[r0 + k0 + t] = om[t]; J[r1 + k0 + t] = ok[t]; }
-                }
-            }
         }
         __syncthreads();
     }

@@ -105,21 +105,31 @@ __global__ void assemble_kernel(MeshDev m, const double* __restrict__ cmua, cons
 }
 
 // ---------------------------------------------------------------------------
-// IC(0) factorisation, one kernel per level of the forward dependency graph
-// (IncompleteCholeskyFactorize, src/libmath/crmatrix_imp.hpp:2166-2203, with
+// IC(0) (IncompleteCholeskyFactorize, src/libmath/crmatrix_imp.hpp:2166-2203,
 // recover = true; complex pivots compared by squared magnitude,
-// src/libmath/mathdef.h:128-132).  Row i of L is complete when its level runs.
+// src/libmath/mathdef.h:128-132) and its apply (CholeskySubst,
+// crmatrix_imp.hpp:2267-2295: forward (L + D) y = b by rows, backward
+// (D + L^T) x = y by columns), both scheduled by levels of the dependency
+// graph of the natural ordering, so the arithmetic is the reference's.
+// L(j,i) lives at Umap[u] for column i; its A entry a_ji is at Lapos[Umap[u]].
+// ---------------------------------------------------------------------------
+// Whole IC(0) apply in one launch: one CTA per group of CG right-hand-side
+// columns walks every forward level, then every backward level, of the
+// dependency schedule; the only synchronisation is __syncthreads between
+// levels (the columns of one CTA never depend on another CTA).  Rows of a
+// level are spread over the CTA's threads; each thread does CG columns.
 // ---------------------------------------------------------------------------
 template <class V>
-__global__ void ic_factor_level(MeshDev m, const int* __restrict__ rows, int nrows, const V* __restrict__ A,
+__global__ void ic_factor_level(MeshDev m, ICDev ic, const int* __restrict__ rows, int nrows, const V* __restrict__ A,
                                 V* __restrict__ L, V* __restrict__ dinv)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nrows) return;
     int i = rows[t];
+    const int ikey = ic.key[i];
     V diag = A[m.diagpos[i]];
     V x = vzero<V>();
-    int l0 = m.Lrowptr[i], l1 = m.Lrowptr[i + 1];
+    int l0 = ic.Lrowptr[i], l1 = ic.Lrowptr[i + 1];
     for (int k = l0; k < l1; k++) x = vfma(x, L[k], L[k]);
     V di;
     bool pos = vt<V>::cplx ? (nrm2(diag) > nrm2(x)) : (re(diag) > re(x));
@@ -130,34 +140,28 @@ __global__ void ic_factor_level(MeshDev m, const int* __restrict__ rows, int nro
         if constexpr (vt<V>::cplx) di = V{1e-10, 0.0};
         else di = 1e-10;
     }
-    for (int u = m.Ucolptr[i]; u < m.Ucolptr[i + 1]; u++) {
-        int j = m.Urow[u];
-        // row_mult (crmatrix_imp.hpp:1971-2009): sum over c < i of L(i,c) L(j,c)
+    for (int u = ic.Ucolptr[i]; u < ic.Ucolptr[i + 1]; u++) {
+        int j = ic.Urow[u];
+        // row_mult (crmatrix_imp.hpp:1971-2009): sum over columns ranked before i of L(i,c) L(j,c)
         V s = vzero<V>();
-        int a = l0, b = m.Lrowptr[j], be = m.Lrowptr[j + 1];
+        int a = l0, b = ic.Lrowptr[j], be = ic.Lrowptr[j + 1];
         while (a < l1 && b < be) {
-            int ca = m.Lcolidx[a], cb = m.Lcolidx[b];
-            if (cb >= i) break;
+            int ca = ic.Lkey[a], cb = ic.Lkey[b];  // ranks in the elimination ordering (the merge order)
+            if (cb >= ikey) break;
             if (ca < cb) a++;
             else if (ca > cb) b++;
             else { s = vfma(s, L[a], L[b]); a++; b++; }
         }
-        V aij = A[m.Lapos[m.Umap[u]]];  // a_ji = a_ij (symmetric pattern and values)
-        L[m.Umap[u]] = vdiv(vsub(aij, s), di);
+        V aij = A[ic.Lapos[ic.Umap[u]]];  // a_ji = a_ij (symmetric pattern and values)
+        L[ic.Umap[u]] = vdiv(vsub(aij, s), di);
     }
     dinv[i] = vrecip(di);
 }
 
-// Lower pattern value positions: L(j,i) lives at Umap[u] for column i; its A
-// entry a_ji is at Lapos[Umap[u]].
-
-// ---------------------------------------------------------------------------
-// Level-scheduled triangular sweeps of the IC(0) apply (CholeskySubst,
-// crmatrix_imp.hpp:2267-2295): forward (L + D) y = b by rows, backward
-// (D + L^T) x = y by columns.  lane -> (row within warp group, column).
-// ---------------------------------------------------------------------------
+// Level-scheduled sweeps of the IC(0) apply: one kernel per level, spread
+// over the whole GPU (lane -> (row of the level, column)).
 template <class V, class S>
-__global__ void ic_fwd_level(MeshDev m, const int* __restrict__ rows, int nrows, int k, int ld, int cw,
+__global__ void ic_fwd_level(ICDev ic, const int* __restrict__ rows, int nrows, int k, int ld, int cw,
                              const V* __restrict__ L, const V* __restrict__ dinv, const V* __restrict__ b,
                              V* __restrict__ y, const ColState* __restrict__ st)
 {
@@ -172,12 +176,12 @@ __global__ void ic_fwd_level(MeshDev m, const int* __restrict__ rows, int nrows,
     if (c >= k || (st && st[c].active != 1)) return;
     int i = rows[r];
     V s = b[(size_t)i * ld + c];
-    for (int q = m.Lrowptr[i]; q < m.Lrowptr[i + 1]; q++) s = vfms(s, L[q], y[(size_t)m.Lcolidx[q] * ld + c]);
+    for (int q = ic.Lrowptr[i]; q < ic.Lrowptr[i + 1]; q++) s = vfms(s, L[q], y[(size_t)ic.Lcolidx[q] * ld + c]);
     y[(size_t)i * ld + c] = vmul(s, dinv[i]);
 }
 
 template <class V, class S>
-__global__ void ic_bwd_level(MeshDev m, const int* __restrict__ rows, int nrows, int k, int ld, int cw,
+__global__ void ic_bwd_level(ICDev ic, const int* __restrict__ rows, int nrows, int k, int ld, int cw,
                              const V* __restrict__ L, const V* __restrict__ dinv, V* __restrict__ x,
                              const ColState* __restrict__ st)
 {
@@ -192,9 +196,303 @@ __global__ void ic_bwd_level(MeshDev m, const int* __restrict__ rows, int nrows,
     if (c >= k || (st && st[c].active != 1)) return;
     int i = rows[r];
     V s = x[(size_t)i * ld + c];
-    for (int u = m.Ucolptr[i + 1] - 1; u >= m.Ucolptr[i]; u--) s = vfms(s, L[m.Umap[u]], x[(size_t)m.Urow[u] * ld + c]);
+    for (int u = ic.Ucolptr[i + 1] - 1; u >= ic.Ucolptr[i]; u--) s = vfms(s, L[ic.Umap[u]], x[(size_t)ic.Urow[u] * ld + c]);
     x[(size_t)i * ld + c] = vmul(s, dinv[i]);
 }
+
+
+// ---------------------------------------------------------------------------
+// Tile dot partials.  A ROW_TILE-row tile is split into TILE_RG interleaved
+// row groups (rows r0+g, r0+g+TILE_RG, ...); each (group, column) is summed
+// sequentially by one thread, and the groups are then added in ascending
+// order.  The order depends only on the row numbering, never on k.
+// ---------------------------------------------------------------------------
+constexpr int TILE_RG = 8;
+constexpr int TILE_CK = 128;  // columns per chunk of the shared-memory staging
+
+struct TileAcc {
+    // sh: [np][TILE_RG][TILE_CK]
+    double* sh;
+    __device__ void put(int p, int g, int cc, double v) { sh[(p * TILE_RG + g) * TILE_CK + cc] = v; }
+    __device__ double sum(int p, int cc) const
+    {
+        double a = 0.0;
+        for (int g = 0; g < TILE_RG; g++) a += sh[(p * TILE_RG + g) * TILE_CK + cc];
+        return a;
+    }
+};
+
+// y-dots of a tile: part0 = sum Re(conj(w) y) (w != null), part1 = sum |y|^2
+template <class V>
+__device__ __forceinline__ void tile_dots(int r0, int r1, int k, int ld, const V* __restrict__ y,
+                                          const V* __restrict__ w, bool want_n2, double* __restrict__ part, int np,
+                                          int ntiles, int tile, const ColState* __restrict__ st)
+{
+    __shared__ double sh[2 * TILE_RG * TILE_CK];
+    TileAcc T{sh};
+    for (int c0 = 0; c0 < k; c0 += TILE_CK) {
+        const int ck = min(TILE_CK, k - c0);
+        for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
+            const int cc = it % ck, g = it / ck, c = c0 + cc;
+            double d0 = 0.0, d1 = 0.0;
+            if (!(st && st[c].active != 1))
+#pragma unroll 4
+                for (int r = r0 + g; r < r1; r += TILE_RG) {
+                    V yv = y[(size_t)r * ld + c];
+                    if (w) d0 += (double)redot(w[(size_t)r * ld + c], yv);
+                    if (want_n2) d1 += (double)nrm2(yv);
+                }
+            T.put(0, g, cc, d0);
+            T.put(1, g, cc, d1);
+        }
+        __syncthreads();
+        for (int cc = threadIdx.x; cc < ck; cc += blockDim.x) {
+            const int c = c0 + cc;
+            if (st && st[c].active != 1) continue;
+            int p = 0;
+            if (w) part[((size_t)c * np + p++) * ntiles + tile] = T.sum(0, cc);
+            if (want_n2) part[((size_t)c * np + p) * ntiles + tile] = T.sum(1, cc);
+        }
+        __syncthreads();
+    }
+}
+
+// warp shuffle of value types
+__device__ __forceinline__ double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ float shfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ cd shfl(cd v, int src) { return cd{__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src)}; }
+__device__ __forceinline__ cf shfl(cf v, int src) { return cf{__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src)}; }
+
+// Sparse row times a block of k >= 32 columns, one warp: the row's (up to 32
+// per pass) indices and values are loaded cooperatively and broadcast by
+// shuffle; lane owns columns lane + 32 j (j < NJ); the gathers of UNR entries
+// are issued together so that many loads are in flight per lane.
+template <class V, int NJ, bool MINUS>
+__device__ __forceinline__ void warp_row_gather(const int* __restrict__ cidx, const V* __restrict__ vals,
+                                                const int* __restrict__ vmap, int q0, int q1, int k, int ld,
+                                                const V* __restrict__ x, V (&acc)[NJ], int lane)
+{
+    constexpr int UNR = 4;
+    for (int base = q0; base < q1; base += 32) {
+        int cnt = min(32, q1 - base);
+        int my_c = 0;
+        V my_v = vzero<V>();
+        if (lane < cnt) {
+            my_c = cidx[base + lane];
+            my_v = vals[vmap ? vmap[base + lane] : base + lane];
+        }
+        for (int e = 0; e < cnt; e += UNR) {
+            int cc[UNR];
+            V av[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; u++) {
+                cc[u] = __shfl_sync(0xffffffffu, my_c, min(e + u, 31));
+                av[u] = shfl(my_v, min(e + u, 31));
+            }
+            V g[UNR][NJ];
+#pragma unroll
+            for (int u = 0; u < UNR; u++)
+#pragma unroll
+                for (int j = 0; j < NJ; j++) {
+                    int c = lane + 32 * j;
+                    g[u][j] = (e + u < cnt && c < k) ? x[(size_t)cc[u] * ld + c] : vzero<V>();
+                }
+#pragma unroll
+            for (int u = 0; u < UNR; u++)
+                if (e + u < cnt)
+#pragma unroll
+                    for (int j = 0; j < NJ; j++)
+                        acc[j] = MINUS ? vfms(acc[j], av[u], g[u][j]) : vfma(acc[j], av[u], g[u][j]);
+        }
+    }
+}
+
+// SpMM for k >= 32 (NJ = ceil(k/32) <= 8): warp per row within a row tile,
+// then the tile-sequential dot partials.
+template <class V, int NJ>
+__global__ void __launch_bounds__(256) spmm_wide_kernel(int n, const int* __restrict__ rowptr,
+                                                        const int* __restrict__ colidx, const V* __restrict__ A, int k,
+                                                        int ld, const V* __restrict__ x, V* __restrict__ y,
+                                                        const V* __restrict__ w, bool want_n2, double* __restrict__ part,
+                                                        int np, int ntiles, const ColState* __restrict__ st)
+{
+    const int tile = blockIdx.x;
+    const int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+    for (int r = r0 + warp; r < r1; r += nwarp) {
+        V acc[NJ];
+#pragma unroll
+        for (int j = 0; j < NJ; j++) acc[j] = vzero<V>();
+        warp_row_gather<V, NJ, false>(colidx, A, nullptr, rowptr[r], rowptr[r + 1], k, ld, x, acc, lane);
+#pragma unroll
+        for (int j = 0; j < NJ; j++) {
+            int c = lane + 32 * j;
+            if (c < k && !(st && st[c].active != 1)) y[(size_t)r * ld + c] = acc[j];
+        }
+    }
+    if (!w && !want_n2) return;
+    __syncthreads();
+    tile_dots<V>(r0, r1, k, ld, y, w, want_n2, part, np, ntiles, tile, st);
+}
+
+// 16-byte words of a block-vector row: P = values per word
+template <class V>
+struct alignas(16) W16 {
+    static constexpr int P = 16 / sizeof(V);
+    V v[P];
+};
+
+// SpMM for k a multiple of W16<V>::P: warp per row of the tile, lane owns the
+// 16-byte words lane + 32 j (j < NW) of the row.  Every lane reads the entry's
+// column and value itself (one broadcast transaction), so an entry costs one
+// address computation and NW 128-bit gathers.
+template <class V, int NW>
+__global__ void __launch_bounds__(256) spmm_vec_kernel(int n, const int* __restrict__ rowptr,
+                                                       const int* __restrict__ colidx, const V* __restrict__ A, int k,
+                                                       int ld, const V* __restrict__ x, V* __restrict__ y,
+                                                       const V* __restrict__ w, bool want_n2,
+                                                       double* __restrict__ part, int np, int ntiles,
+                                                       const ColState* __restrict__ st)
+{
+    constexpr int P = W16<V>::P;
+    const int tile = blockIdx.x;
+    const int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+    const int nwords = k / P, ldw = ld / P;
+    const W16<V>* X = reinterpret_cast<const W16<V>*>(x);
+    W16<V>* Y = reinterpret_cast<W16<V>*>(y);
+    for (int r = r0 + warp; r < r1; r += nwarp) {
+        W16<V> acc[NW];
+#pragma unroll
+        for (int j = 0; j < NW; j++)
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[j].v[p] = vzero<V>();
+        const int q1 = rowptr[r + 1];
+        int q = rowptr[r];
+        for (; q + 2 <= q1; q += 2) {
+            const int c0 = colidx[q], c1 = colidx[q + 1];
+            const V a0 = A[q], a1 = A[q + 1];
+            const W16<V>* x0 = X + (size_t)c0 * ldw;
+            const W16<V>* x1 = X + (size_t)c1 * ldw;
+            W16<V> g0[NW], g1[NW];
+#pragma unroll
+            for (int j = 0; j < NW; j++) {
+                const int wi = lane + 32 * j;
+                if (wi < nwords) { g0[j] = x0[wi]; g1[j] = x1[wi]; }
+            }
+#pragma unroll
+            for (int j = 0; j < NW; j++)
+#pragma unroll
+                for (int p = 0; p < P; p++) {
+                    acc[j].v[p] = vfma(acc[j].v[p], a0, g0[j].v[p]);
+                    acc[j].v[p] = vfma(acc[j].v[p], a1, g1[j].v[p]);
+                }
+        }
+        if (q < q1) {
+            const int c0 = colidx[q];
+            const V a0 = A[q];
+            const W16<V>* x0 = X + (size_t)c0 * ldw;
+#pragma unroll
+            for (int j = 0; j < NW; j++) {
+                const int wi = lane + 32 * j;
+                if (wi < nwords) {
+                    W16<V> g = x0[wi];
+#pragma unroll
+                    for (int p = 0; p < P; p++) acc[j].v[p] = vfma(acc[j].v[p], a0, g.v[p]);
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NW; j++) {
+            const int wi = lane + 32 * j;
+            if (wi >= nwords) continue;
+            if (st) {  // inactive columns keep their values
+                W16<V> o = acc[j];
+                bool all = true;
+#pragma unroll
+                for (int p = 0; p < P; p++) all &= st[wi * P + p].active == 1;
+                if (all) { Y[(size_t)r * ldw + wi] = o; continue; }
+#pragma unroll
+                for (int p = 0; p < P; p++)
+                    if (st[wi * P + p].active == 1) y[(size_t)r * ld + wi * P + p] = o.v[p];
+            } else {
+                Y[(size_t)r * ldw + wi] = acc[j];
+            }
+        }
+    }
+    if (!w && !want_n2) return;
+    __syncthreads();
+    tile_dots<V>(r0, r1, k, ld, y, w, want_n2, part, np, ntiles, tile, st);
+}
+
+// IC(0) level kernel on the level's ELL entries (k >= 32): warp per slot;
+// the slot's entries sit at slot * w, so the row's indices, values, right-hand
+// side and pivot load in one round and the gathers in the next.
+template <class V, int NJ, bool FWD>
+__global__ void __launch_bounds__(256) ic_level_ell(const int* __restrict__ rows, int nrows, int w,
+                                                    const int* __restrict__ ecol, const V* __restrict__ eval, int k,
+                                                    int ld, const V* __restrict__ dinv, const V* __restrict__ b,
+                                                    V* __restrict__ y, const ColState* __restrict__ st)
+{
+    const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (slot >= nrows) return;
+    const int i = rows[slot];
+    const V di = dinv[i];
+    V acc[NJ];
+#pragma unroll
+    for (int j = 0; j < NJ; j++) {
+        int c = lane + 32 * j;
+        acc[j] = c < k ? (FWD ? b[(size_t)i * ld + c] : y[(size_t)i * ld + c]) : vzero<V>();
+    }
+    constexpr int UNR = 4;
+    for (int base = 0; base < w; base += 32) {
+        const int cnt = min(32, w - base);
+        int my_c = -1;
+        V my_v = vzero<V>();
+        if (lane < cnt) {
+            my_c = ecol[(size_t)slot * w + base + lane];
+            my_v = eval[(size_t)slot * w + base + lane];
+        }
+        for (int e = 0; e < cnt; e += UNR) {
+            int cc[UNR];
+            V av[UNR];
+#pragma unroll
+            for (int u = 0; u < UNR; u++) {
+                cc[u] = __shfl_sync(0xffffffffu, my_c, min(e + u, 31));
+                av[u] = shfl(my_v, min(e + u, 31));
+            }
+            V g[UNR][NJ];
+#pragma unroll
+            for (int u = 0; u < UNR; u++)
+#pragma unroll
+                for (int j = 0; j < NJ; j++) {
+                    int c = lane + 32 * j;
+                    g[u][j] = (e + u < cnt && cc[u] >= 0 && c < k) ? y[(size_t)cc[u] * ld + c] : vzero<V>();
+                }
+#pragma unroll
+            for (int u = 0; u < UNR; u++)
+                if (e + u < cnt && cc[u] >= 0)
+#pragma unroll
+                    for (int j = 0; j < NJ; j++) acc[j] = vfms(acc[j], av[u], g[u][j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NJ; j++) {
+        int c = lane + 32 * j;
+        if (c < k && !(st && st[c].active != 1)) y[(size_t)i * ld + c] = vmul(acc[j], di);
+    }
+}
+
+// factor values into the ELL layouts (padding -> 0)
+template <class V>
+__global__ void ell_gather_kernel(int cnt, const int* __restrict__ src, const V* __restrict__ L, V* __restrict__ out)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt) return;
+    int q = src[t];
+    out[t] = q >= 0 ? L[q] : vzero<V>();
+}
+
 
 // ---------------------------------------------------------------------------
 // SpMM y = A x with optional fused dot partials over ROW_TILE-row tiles:
@@ -224,18 +522,7 @@ __global__ void spmm_dot_kernel(int n, const int* __restrict__ rowptr, const int
     }
     if (!w && !want_n2) return;
     __syncthreads();
-    for (int c = threadIdx.x; c < k; c += blockDim.x) {
-        if (st && st[c].active != 1) continue;
-        double d0 = 0.0, d1 = 0.0;
-        for (int r = r0; r < r1; r++) {
-            V yv = y[(size_t)r * ld + c];
-            if (w) d0 += (double)redot(w[(size_t)r * ld + c], yv);
-            if (want_n2) d1 += (double)nrm2(yv);
-        }
-        int p = 0;
-        if (w) part[((size_t)c * np + p++) * ntiles + tile] = d0;
-        if (want_n2) part[((size_t)c * np + p) * ntiles + tile] = d1;
-    }
+    tile_dots<V>(r0, r1, k, ld, y, w, want_n2, part, np, ntiles, tile, st);
 }
 
 // single right-hand side: warp per row, lanes over the row's entries
@@ -359,24 +646,39 @@ __global__ void reduce_finalize_kernel(int k, int ntiles, const double* __restri
     }
 }
 
-// generic column dot partials over row tiles: part0 = sum Re(conj(a) b), optional part1 = sum Re(conj(c) d)
+// generic column dot partials over row tiles: part0 = sum Re(conj(a) b),
+// optional part1 = sum Re(conj(c2) d2)
 template <class V>
 __global__ void dot_tiles_kernel(int n, int k, int ld, const V* __restrict__ a, const V* __restrict__ b,
                                  const V* __restrict__ c2, const V* __restrict__ d2, double* __restrict__ part,
                                  int np, int ntiles, const ColState* __restrict__ st)
 {
-    int tile = blockIdx.x;
-    int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
-    for (int c = threadIdx.x; c < k; c += blockDim.x) {
-        if (st && st[c].active != 1) continue;
-        double d0 = 0.0, d1 = 0.0;
-        for (int r = r0; r < r1; r++) {
-            size_t o = (size_t)r * ld + c;
-            d0 += (double)redot(a[o], b[o]);
-            if (c2) d1 += (double)redot(c2[o], d2[o]);
+    __shared__ double sh[2 * TILE_RG * TILE_CK];
+    TileAcc T{sh};
+    const int tile = blockIdx.x;
+    const int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    for (int c0 = 0; c0 < k; c0 += TILE_CK) {
+        const int ck = min(TILE_CK, k - c0);
+        for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
+            const int cc = it % ck, g = it / ck, c = c0 + cc;
+            double d0 = 0.0, d1 = 0.0;
+            if (!(st && st[c].active != 1))
+                for (int r = r0 + g; r < r1; r += TILE_RG) {
+                    size_t o = (size_t)r * ld + c;
+                    d0 += (double)redot(a[o], b[o]);
+                    if (c2) d1 += (double)redot(c2[o], d2[o]);
+                }
+            T.put(0, g, cc, d0);
+            T.put(1, g, cc, d1);
         }
-        part[((size_t)c * np) * ntiles + tile] = d0;
-        if (c2) part[((size_t)c * np + 1) * ntiles + tile] = d1;
+        __syncthreads();
+        for (int cc = threadIdx.x; cc < ck; cc += blockDim.x) {
+            const int c = c0 + cc;
+            if (st && st[c].active != 1) continue;
+            part[((size_t)c * np) * ntiles + tile] = T.sum(0, cc);
+            if (c2) part[((size_t)c * np + 1) * ntiles + tile] = T.sum(1, cc);
+        }
+        __syncthreads();
     }
 }
 
@@ -415,21 +717,33 @@ __global__ void bicg_s_kernel(int n, int k, int ld, const ColState* st, const V*
                               const V* __restrict__ v, V* __restrict__ s, V* __restrict__ sd,
                               const V* __restrict__ idiag, int precon, double* __restrict__ part, int ntiles)
 {
-    int tile = blockIdx.x;
-    int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
-    for (int c = threadIdx.x; c < k; c += blockDim.x) {
-        if (!col_on(st, c)) continue;
-        S alpha = (S)st[c].alpha;
-        double acc = 0.0;
-        for (int i = r0; i < r1; i++) {
-            size_t o = (size_t)i * ld + c;
-            V sv = vsub(r[o], vscale(v[o], alpha));
-            s[o] = sv;
-            if (precon == 1) sd[o] = vmul(sv, idiag[i]);
-            else if (precon == 0) sd[o] = sv;
-            acc += (double)nrm2(sv);
+    __shared__ double sh[2 * TILE_RG * TILE_CK];
+    TileAcc T{sh};
+    const int tile = blockIdx.x;
+    const int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    for (int c0 = 0; c0 < k; c0 += TILE_CK) {
+        const int ck = min(TILE_CK, k - c0);
+        for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
+            const int cc = it % ck, g = it / ck, c = c0 + cc;
+            double acc = 0.0;
+            if (col_on(st, c)) {
+                const S alpha = (S)st[c].alpha;
+#pragma unroll 4
+                for (int i = r0 + g; i < r1; i += TILE_RG) {
+                    size_t o = (size_t)i * ld + c;
+                    V sv = vsub(r[o], vscale(v[o], alpha));
+                    s[o] = sv;
+                    if (precon == 1) sd[o] = vmul(sv, idiag[i]);
+                    else if (precon == 0) sd[o] = sv;
+                    acc += (double)nrm2(sv);
+                }
+            }
+            T.put(0, g, cc, acc);
         }
-        part[(size_t)c * ntiles + tile] = acc;
+        __syncthreads();
+        for (int cc = threadIdx.x; cc < ck; cc += blockDim.x)
+            if (col_on(st, c0 + cc)) part[(size_t)(c0 + cc) * ntiles + tile] = T.sum(0, cc);
+        __syncthreads();
     }
 }
 
@@ -440,24 +754,40 @@ __global__ void bicg_xr_kernel(int n, int k, int ld, const ColState* st, V* __re
                                const V* __restrict__ rd, const V* __restrict__ pd, const V* __restrict__ sd,
                                const V* __restrict__ s, const V* __restrict__ t, double* __restrict__ part, int ntiles)
 {
-    int tile = blockIdx.x;
-    int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
-    for (int c = threadIdx.x; c < k; c += blockDim.x) {
-        int a = st[c].active;
-        if (a == 0) continue;
-        S alpha = (S)st[c].alpha, omega = (S)st[c].omega;
-        double n2 = 0.0, rr = 0.0;
-        for (int i = r0; i < r1; i++) {
-            size_t o = (size_t)i * ld + c;
-            if (a == -1) { x[o] = vadd(x[o], vscale(pd[o], alpha)); continue; }
-            x[o] = vadd(x[o], vadd(vscale(pd[o], alpha), vscale(sd[o], omega)));
-            V rv = vsub(s[o], vscale(t[o], omega));
-            r[o] = rv;
-            n2 += (double)nrm2(rv);
-            rr += (double)redot(rd[o], rv);
+    __shared__ double sh[2 * TILE_RG * TILE_CK];
+    TileAcc T{sh};
+    const int tile = blockIdx.x;
+    const int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    for (int c0 = 0; c0 < k; c0 += TILE_CK) {
+        const int ck = min(TILE_CK, k - c0);
+        for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
+            const int cc = it % ck, g = it / ck, c = c0 + cc;
+            const int a = st[c].active;
+            double n2 = 0.0, rr = 0.0;
+            if (a != 0) {
+                const S alpha = (S)st[c].alpha, omega = (S)st[c].omega;
+#pragma unroll 4
+                for (int i = r0 + g; i < r1; i += TILE_RG) {
+                    size_t o = (size_t)i * ld + c;
+                    if (a == -1) { x[o] = vadd(x[o], vscale(pd[o], alpha)); continue; }
+                    x[o] = vadd(x[o], vadd(vscale(pd[o], alpha), vscale(sd[o], omega)));
+                    V rv = vsub(s[o], vscale(t[o], omega));
+                    r[o] = rv;
+                    n2 += (double)nrm2(rv);
+                    rr += (double)redot(rd[o], rv);
+                }
+            }
+            T.put(0, g, cc, n2);
+            T.put(1, g, cc, rr);
         }
-        part[((size_t)c * 2) * ntiles + tile] = n2;
-        part[((size_t)c * 2 + 1) * ntiles + tile] = rr;
+        __syncthreads();
+        for (int cc = threadIdx.x; cc < ck; cc += blockDim.x) {
+            const int c = c0 + cc;
+            if (st[c].active == 0) continue;
+            part[((size_t)c * 2) * ntiles + tile] = T.sum(0, cc);
+            part[((size_t)c * 2 + 1) * ntiles + tile] = T.sum(1, cc);
+        }
+        __syncthreads();
     }
 }
 
@@ -470,28 +800,42 @@ __global__ void pcg_xr_kernel(int n, int k, int ld, const ColState* st, V* __res
                               const V* __restrict__ d, const V* __restrict__ q, V* __restrict__ z,
                               const V* __restrict__ idiag, int precon, double* __restrict__ part, int ntiles)
 {
-    int tile = blockIdx.x;
-    int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
-    for (int c = threadIdx.x; c < k; c += blockDim.x) {
-        if (!col_on(st, c)) continue;
-        S alpha = (S)st[c].alpha;
-        double rz = 0.0, n2 = 0.0;
-        for (int i = r0; i < r1; i++) {
-            size_t o = (size_t)i * ld + c;
-            x[o] = vadd(x[o], vscale(d[o], alpha));
-            V rv = vsub(r[o], vscale(q[o], alpha));
-            r[o] = rv;
-            if (precon != 2) {
-                V zv = precon == 1 ? vmul(rv, idiag[i]) : rv;
-                z[o] = zv;
-                rz += (double)redot(rv, zv);
-                n2 += (double)nrm2(rv);
+    __shared__ double sh[2 * TILE_RG * TILE_CK];
+    TileAcc T{sh};
+    const int tile = blockIdx.x;
+    const int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    for (int c0 = 0; c0 < k; c0 += TILE_CK) {
+        const int ck = min(TILE_CK, k - c0);
+        for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
+            const int cc = it % ck, g = it / ck, c = c0 + cc;
+            double rz = 0.0, n2 = 0.0;
+            if (col_on(st, c)) {
+                const S alpha = (S)st[c].alpha;
+                for (int i = r0 + g; i < r1; i += TILE_RG) {
+                    size_t o = (size_t)i * ld + c;
+                    x[o] = vadd(x[o], vscale(d[o], alpha));
+                    V rv = vsub(r[o], vscale(q[o], alpha));
+                    r[o] = rv;
+                    if (precon != 2) {
+                        V zv = precon == 1 ? vmul(rv, idiag[i]) : rv;
+                        z[o] = zv;
+                        rz += (double)redot(rv, zv);
+                        n2 += (double)nrm2(rv);
+                    }
+                }
             }
+            T.put(0, g, cc, rz);
+            T.put(1, g, cc, n2);
         }
-        if (precon != 2) {
-            part[((size_t)c * 2) * ntiles + tile] = rz;
-            part[((size_t)c * 2 + 1) * ntiles + tile] = n2;
-        }
+        __syncthreads();
+        if (precon != 2)
+            for (int cc = threadIdx.x; cc < ck; cc += blockDim.x) {
+                const int c = c0 + cc;
+                if (!col_on(st, c)) continue;
+                part[((size_t)c * 2) * ntiles + tile] = T.sum(0, cc);
+                part[((size_t)c * 2 + 1) * ntiles + tile] = T.sum(1, cc);
+            }
+        __syncthreads();
     }
 }
 
@@ -534,8 +878,10 @@ __global__ void scale_diag_kernel(int n, int k, int ld, const V* __restrict__ a,
 }
 
 // source-major (q*n + i) <-> node-major (i*ld + q) transposes with precision cast
+// perm (nullable): natural node -> layout row of the node-major block
 template <class To, class From>
-__global__ void to_nodemajor_kernel(int n, int k, int ld, const From* __restrict__ src, To* __restrict__ dst)
+__global__ void to_nodemajor_kernel(int n, int k, int ld, const From* __restrict__ src, To* __restrict__ dst,
+                                    const int* __restrict__ perm)
 {
     __shared__ From tile[32][33];
     int i0 = blockIdx.x * 32, q0 = blockIdx.y * 32;
@@ -546,18 +892,19 @@ __global__ void to_nodemajor_kernel(int n, int k, int ld, const From* __restrict
     __syncthreads();
     for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
         int i = i0 + yy, q = q0 + threadIdx.x;
-        if (q < k && i < n) dst[(size_t)i * ld + q] = vcast<To, From>(tile[threadIdx.x][yy]);
+        if (q < k && i < n) dst[(size_t)(perm ? perm[i] : i) * ld + q] = vcast<To, From>(tile[threadIdx.x][yy]);
     }
 }
 
 template <class To, class From>
-__global__ void to_srcmajor_kernel(int n, int k, int ld, const From* __restrict__ src, To* __restrict__ dst)
+__global__ void to_srcmajor_kernel(int n, int k, int ld, const From* __restrict__ src, To* __restrict__ dst,
+                                   const int* __restrict__ perm)
 {
     __shared__ From tile[32][33];
     int i0 = blockIdx.x * 32, q0 = blockIdx.y * 32;
     for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
         int i = i0 + yy, q = q0 + threadIdx.x;
-        if (q < k && i < n) tile[yy][threadIdx.x] = src[(size_t)i * ld + q];
+        if (q < k && i < n) tile[yy][threadIdx.x] = src[(size_t)(perm ? perm[i] : i) * ld + q];
     }
     __syncthreads();
     for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
@@ -571,6 +918,16 @@ __global__ void cast_kernel(size_t cnt, const From* __restrict__ a, To* __restri
 {
     size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < cnt) b[t] = vcast<To, From>(a[t]);
+}
+
+// node-major block with leading dimension ld (k used columns) -> dense k columns, cast
+template <class To, class From>
+__global__ void strided_cast_kernel(int n, int k, const From* __restrict__ a, int ld, To* __restrict__ b)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * k) return;
+    size_t i = t / k, c = t % k;
+    b[t] = vcast<To, From>(a[i * ld + c]);
 }
 
 // x += e (refinement update, FP64 x, low-precision e)

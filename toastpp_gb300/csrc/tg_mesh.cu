@@ -187,70 +187,190 @@ static int find_col(const std::vector<int>& rowptr, const std::vector<int>& coli
     return (it != e && *it == c) ? (int)(it - colidx.begin()) : -1;
 }
 
-static void ic_pattern(MeshHost& m)
+// Morton (Z-order) layout of the nodes: rows that are close in space are
+// close in memory, so the neighbours a row gathers are shared by nearby rows.
+static void layout_order(MeshHost& m)
+{
+    int n = m.n, dim = m.dim;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < n; i++)
+        for (int d = 0; d < dim; d++) {
+            lo[d] = std::min(lo[d], m.coords[(size_t)i * dim + d]);
+            hi[d] = std::max(hi[d], m.coords[(size_t)i * dim + d]);
+        }
+    const int bits = dim == 2 ? 16 : 10;
+    std::vector<std::pair<uint64_t, int>> key(n);
+    for (int i = 0; i < n; i++) {
+        uint64_t code = 0;
+        unsigned q[3] = {0, 0, 0};
+        for (int d = 0; d < dim; d++) {
+            double t = hi[d] > lo[d] ? (m.coords[(size_t)i * dim + d] - lo[d]) / (hi[d] - lo[d]) : 0.0;
+            q[d] = (unsigned)std::min((double)((1u << bits) - 1), std::floor(t * (1u << bits)));
+        }
+        for (int b = bits - 1; b >= 0; b--)
+            for (int d = 0; d < dim; d++) code = (code << 1) | ((q[d] >> b) & 1u);
+        key[i] = {code, i};
+    }
+    std::sort(key.begin(), key.end());
+    m.perm.assign(n, 0);
+    m.iperm.assign(n, 0);
+    for (int p = 0; p < n; p++) { m.iperm[p] = key[p].second; m.perm[key[p].second] = p; }
+    // layout CSR: layout row p = natural row iperm[p], entries in natural column order
+    m.lrowptr.assign(n + 1, 0);
+    m.lcolidx.clear();
+    m.lay2nat.clear();
+    m.ldiagpos.assign(n, -1);
+    for (int p = 0; p < n; p++) {
+        int i = m.iperm[p];
+        for (int q = m.rowptr[i]; q < m.rowptr[i + 1]; q++) {
+            if (m.colidx[q] == i) m.ldiagpos[p] = (int)m.lcolidx.size();
+            m.lcolidx.push_back(m.perm[m.colidx[q]]);
+            m.lay2nat.push_back(q);
+        }
+        m.lrowptr[p + 1] = (int)m.lcolidx.size();
+    }
+    m.jcolidx.resize(m.colidx.size());
+    for (size_t q = 0; q < m.colidx.size(); q++) m.jcolidx[q] = m.perm[m.colidx[q]];
+}
+
+// IC(0) structure for the ordering given by key[natural node] (a rank): see ICHost.
+static void ic_pattern(MeshHost& m, const std::vector<int>& keynat, ICHost& c)
 {
     int n = m.n;
-    m.Lrowptr.assign(n + 1, 0);
-    m.Lcolidx.clear();
-    m.Lapos.clear();
-    for (int i = 0; i < n; i++) {
-        for (int k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) {
-            if (m.colidx[k] >= i) break;
-            m.Lcolidx.push_back(m.colidx[k]);
-            m.Lapos.push_back(k);
+    c.key.assign(n, 0);
+    for (int p = 0; p < n; p++) c.key[p] = keynat[m.iperm[p]];
+    c.Lrowptr.assign(n + 1, 0);
+    c.Lcolidx.clear();
+    c.Lapos.clear();
+    c.Lkey.clear();
+    std::vector<std::pair<int, int>> ent;
+    for (int p = 0; p < n; p++) {
+        ent.clear();
+        for (int e = m.lrowptr[p]; e < m.lrowptr[p + 1]; e++) {
+            int kj = c.key[m.lcolidx[e]];
+            if (kj < c.key[p]) ent.push_back({kj, e});
         }
-        m.Lrowptr[i + 1] = (int)m.Lcolidx.size();
+        std::sort(ent.begin(), ent.end());
+        for (auto& pr : ent) {
+            c.Lcolidx.push_back(m.lcolidx[pr.second]);
+            c.Lkey.push_back(pr.first);
+            c.Lapos.push_back(pr.second);
+        }
+        c.Lrowptr[p + 1] = (int)c.Lcolidx.size();
     }
-    int nl = m.Lrowptr[n];
-    // column view: for column i, rows r > i ascending, with the L index
-    m.Ucolptr.assign(n + 1, 0);
-    for (int k = 0; k < nl; k++) m.Ucolptr[m.Lcolidx[k] + 1]++;
-    for (int i = 0; i < n; i++) m.Ucolptr[i + 1] += m.Ucolptr[i];
-    m.Urow.assign(nl, 0);
-    m.Umap.assign(nl, 0);
+    int nl = c.Lrowptr[n];
+    std::vector<int> byrank(n);  // layout rows in ascending rank
+    for (int p = 0; p < n; p++) byrank[p] = p;
+    std::sort(byrank.begin(), byrank.end(), [&](int a, int b) { return c.key[a] < c.key[b]; });
+    c.Ucolptr.assign(n + 1, 0);
+    for (int q = 0; q < nl; q++) c.Ucolptr[c.Lcolidx[q] + 1]++;
+    for (int p = 0; p < n; p++) c.Ucolptr[p + 1] += c.Ucolptr[p];
+    c.Urow.assign(nl, 0);
+    c.Umap.assign(nl, 0);
     std::vector<int> fill(n, 0);
-    for (int r = 0; r < n; r++)
-        for (int k = m.Lrowptr[r]; k < m.Lrowptr[r + 1]; k++) {
-            int c = m.Lcolidx[k], p = m.Ucolptr[c] + fill[c]++;
-            m.Urow[p] = r;
-            m.Umap[p] = k;
+    for (int p : byrank)  // rows of each column in ascending rank
+        for (int q = c.Lrowptr[p]; q < c.Lrowptr[p + 1]; q++) {
+            int col = c.Lcolidx[q], pos = c.Ucolptr[col] + fill[col]++;
+            c.Urow[pos] = p;
+            c.Umap[pos] = q;
         }
-    // level schedules: forward depth through L rows, backward through L columns
-    std::vector<int> lev(n, 0), blev(n, 0);
+    std::vector<int> lev(n, 0), blev(n, 0);  // by layout row
     int nlf = 0, nlb = 0;
-    for (int i = 0; i < n; i++) {
+    for (int p : byrank) {
         int l = 0;
-        for (int k = m.Lrowptr[i]; k < m.Lrowptr[i + 1]; k++) l = std::max(l, lev[m.Lcolidx[k]] + 1);
-        lev[i] = l;
+        for (int q = c.Lrowptr[p]; q < c.Lrowptr[p + 1]; q++) l = std::max(l, lev[c.Lcolidx[q]] + 1);
+        lev[p] = l;
         nlf = std::max(nlf, l + 1);
     }
-    for (int i = n - 1; i >= 0; i--) {
-        int l = 0;
-        for (int k = m.Ucolptr[i]; k < m.Ucolptr[i + 1]; k++) l = std::max(l, blev[m.Urow[k]] + 1);
-        blev[i] = l;
+    for (int t = n - 1; t >= 0; t--) {
+        int p = byrank[t], l = 0;
+        for (int u = c.Ucolptr[p]; u < c.Ucolptr[p + 1]; u++) l = std::max(l, blev[c.Urow[u]] + 1);
+        blev[p] = l;
         nlb = std::max(nlb, l + 1);
     }
-    auto group = [n](const std::vector<int>& lv, int nlev, std::vector<int>& ptr, std::vector<int>& rows) {
+    auto group = [&](const std::vector<int>& lv, int nlev, std::vector<int>& ptr, std::vector<int>& rows) {
         ptr.assign(nlev + 1, 0);
-        for (int i = 0; i < n; i++) ptr[lv[i] + 1]++;
+        for (int p = 0; p < n; p++) ptr[lv[p] + 1]++;
         for (int l = 0; l < nlev; l++) ptr[l + 1] += ptr[l];
         rows.assign(n, 0);
         std::vector<int> f(nlev, 0);
-        for (int i = 0; i < n; i++) rows[ptr[lv[i]] + f[lv[i]]++] = i;
+        for (int p = 0; p < n; p++) rows[ptr[lv[p]] + f[lv[p]]++] = p;  // layout order inside a level
     };
-    group(lev, nlf, m.fwd_lev_ptr, m.fwd_lev_rows);
-    group(blev, nlb, m.bwd_lev_ptr, m.bwd_lev_rows);
+    group(lev, nlf, c.fwd_lev_ptr, c.fwd_lev_rows);
+    group(blev, nlb, c.bwd_lev_ptr, c.bwd_lev_rows);
+    auto ell = [&](bool fwd, const std::vector<int>& ptr, const std::vector<int>& rows, std::vector<int>& w,
+                   std::vector<int>& off, std::vector<int>& col, std::vector<int>& src) {
+        int nlev = (int)ptr.size() - 1;
+        w.assign(nlev, 0);
+        off.assign(nlev + 1, 0);
+        for (int l = 0; l < nlev; l++) {
+            int mw = 1;
+            for (int t = ptr[l]; t < ptr[l + 1]; t++) {
+                int p = rows[t];
+                mw = std::max(mw, fwd ? c.Lrowptr[p + 1] - c.Lrowptr[p] : c.Ucolptr[p + 1] - c.Ucolptr[p]);
+            }
+            w[l] = mw;
+            off[l + 1] = off[l] + (ptr[l + 1] - ptr[l]) * mw;
+        }
+        col.assign(off[nlev], -1);
+        src.assign(off[nlev], -1);
+        for (int l = 0; l < nlev; l++)
+            for (int t = ptr[l]; t < ptr[l + 1]; t++) {
+                int p = rows[t], base = off[l] + (t - ptr[l]) * w[l];
+                if (fwd)
+                    for (int q = c.Lrowptr[p]; q < c.Lrowptr[p + 1]; q++) {
+                        col[base + q - c.Lrowptr[p]] = c.Lcolidx[q];
+                        src[base + q - c.Lrowptr[p]] = q;
+                    }
+                else  // descending rank, the order CholeskySubst subtracts them
+                    for (int u = c.Ucolptr[p + 1] - 1, j = 0; u >= c.Ucolptr[p]; u--, j++) {
+                        col[base + j] = c.Urow[u];
+                        src[base + j] = c.Umap[u];
+                    }
+            }
+    };
+    ell(true, c.fwd_lev_ptr, c.fwd_lev_rows, c.fwd_ell_w, c.fwd_ell_off, c.fwd_ell_col, c.fwd_ell_src);
+    ell(false, c.bwd_lev_ptr, c.bwd_lev_rows, c.bwd_ell_w, c.bwd_ell_off, c.bwd_ell_col, c.bwd_ell_src);
+}
+
+// greedy colouring in natural order; key = colour-major rank (colour, natural index)
+static std::vector<int> colour_key(MeshHost& m)
+{
+    int n = m.n;
+    std::vector<int> col(n, -1);
+    std::vector<int> mark;
+    int nc = 0;
+    for (int i = 0; i < n; i++) {
+        mark.assign(nc + 1, 0);
+        for (int q = m.rowptr[i]; q < m.rowptr[i + 1]; q++) {
+            int j = m.colidx[q];
+            if (j != i && col[j] >= 0) mark[col[j]] = 1;
+        }
+        int c = 0;
+        while (c < nc && mark[c]) c++;
+        col[i] = c;
+        if (c == nc) nc++;
+    }
+    m.ncolors = nc;
+    std::vector<int> cnt(nc + 1, 0);
+    for (int i = 0; i < n; i++) cnt[col[i] + 1]++;
+    for (int c = 0; c < nc; c++) cnt[c + 1] += cnt[c];
+    std::vector<int> key(n);
+    for (int i = 0; i < n; i++) key[i] = cnt[col[i]]++;
+    return key;
 }
 
 static void gather_maps(MeshHost& m)
 {
     int nnz = m.rowptr[m.n];
+    std::vector<int> nat2lay(nnz);
+    for (int e = 0; e < nnz; e++) nat2lay[m.lay2nat[e]] = e;
     std::vector<int> cnt(nnz + 1, 0);
     std::vector<int> slot((size_t)m.ne * m.nn * m.nn);
     for (int e = 0; e < m.ne; e++)
         for (int i = 0; i < m.nn; i++)
             for (int j = 0; j < m.nn; j++) {
-                int k = find_col(m.rowptr, m.colidx, m.el[(size_t)e * m.nn + i], m.el[(size_t)e * m.nn + j]);
+                int k = nat2lay[find_col(m.rowptr, m.colidx, m.el[(size_t)e * m.nn + i], m.el[(size_t)e * m.nn + j])];
                 slot[((size_t)e * m.nn + i) * m.nn + j] = k;
                 cnt[k + 1]++;
             }
@@ -269,11 +389,20 @@ static void gather_maps(MeshHost& m)
         for (int i = 0; i < m.nn; i++) m.nel_ptr[m.el[(size_t)e * m.nn + i] + 1]++;
     for (int i = 0; i < m.n; i++) m.nel_ptr[i + 1] += m.nel_ptr[i];
     m.nel_list.assign(m.nel_ptr[m.n], 0);
+    m.nel_pos.assign(m.nel_ptr[m.n], 0u);
     std::vector<int> g(m.n, 0);
     for (int e = 0; e < m.ne; e++)
         for (int i = 0; i < m.nn; i++) {
             int nd = m.el[(size_t)e * m.nn + i];
-            m.nel_list[m.nel_ptr[nd] + g[nd]++] = e * 4 + i;
+            int slot = m.nel_ptr[nd] + g[nd]++;
+            m.nel_list[slot] = e * 4 + i;
+            unsigned packed = 0;
+            for (int j = 0; j < m.nn; j++) {
+                int p = find_col(m.rowptr, m.colidx, nd, m.el[(size_t)e * m.nn + j]) - m.rowptr[nd];
+                if (p < 0 || p > 255) throw Error{1, "node degree above 255 is not supported"};
+                packed |= (unsigned)p << (8 * j);
+            }
+            m.nel_pos[slot] = packed;
         }
 }
 
@@ -289,10 +418,14 @@ static T* upload(const std::vector<T>& v)
 
 Mesh::~Mesh()
 {
-    void* ptrs[] = {d.rec, d.el, d.rowptr, d.colidx, d.diagpos, d.Lrowptr, d.Lcolidx, d.Lapos, d.Ucolptr,
-                    d.Urow, d.Umap, d.fwd_lev_rows, d.bwd_lev_rows, d.asm_ptr, d.asm_list, d.nel_ptr,
-                    d.nel_list, d.bndnode};
+    void* ptrs[] = {d.rec, d.el, d.rowptr, d.colidx, d.diagpos, d.perm, d.iperm, d.jrowptr, d.jcolidx, d.asm_ptr,
+                    d.asm_list, d.nel_ptr, d.nel_list, d.nel_pos, d.bndnode};
     for (void* p : ptrs) if (p) cudaFree(p);
+    for (auto& g : d.ic) {
+        void* q[] = {g.key, g.Lrowptr, g.Lcolidx, g.Lapos, g.Lkey, g.Ucolptr, g.Urow, g.Umap, g.fwd_lev_rows,
+                     g.bwd_lev_rows, g.fwd_ell_col, g.fwd_ell_src, g.bwd_ell_col, g.bwd_ell_src};
+        for (void* p : q) if (p) cudaFree(p);
+    }
 }
 
 Mesh* mesh_build(int dim, int n, const double* coords, int ne, const int* el)
@@ -312,35 +445,56 @@ Mesh* mesh_build(int dim, int n, const double* coords, int ne, const int* el)
     csr_pattern(m);
     for (int i = 0; i < n; i++)
         if (m.diagpos[i] < 0) { delete M; throw Error{1, "node not referenced by any element"}; }
-    ic_pattern(m);
+    layout_order(m);
+    {
+        std::vector<int> natkey(n);
+        for (int i = 0; i < n; i++) natkey[i] = i;
+        ic_pattern(m, natkey, m.ic[0]);
+        ic_pattern(m, colour_key(m), m.ic[1]);
+    }
     gather_maps(m);
     cudaGetDevice(&M->device);
     MeshDev& d = M->d;
     d.dim = dim; d.n = n; d.ne = ne; d.nn = m.nn;
     d.nnz = m.rowptr[n];
-    d.nnzL = m.Lrowptr[n];
-    d.nlev_fwd = (int)m.fwd_lev_ptr.size() - 1;
-    d.nlev_bwd = (int)m.bwd_lev_ptr.size() - 1;
     d.rec = upload(m.rec);
     d.el = upload(m.el);
-    d.rowptr = upload(m.rowptr);
-    d.colidx = upload(m.colidx);
-    d.diagpos = upload(m.diagpos);
-    d.Lrowptr = upload(m.Lrowptr);
-    d.Lcolidx = upload(m.Lcolidx);
-    d.Lapos = upload(m.Lapos);
-    d.Ucolptr = upload(m.Ucolptr);
-    d.Urow = upload(m.Urow);
-    d.Umap = upload(m.Umap);
-    d.fwd_lev_rows = upload(m.fwd_lev_rows);
-    d.bwd_lev_rows = upload(m.bwd_lev_rows);
+    d.rowptr = upload(m.lrowptr);
+    d.colidx = upload(m.lcolidx);
+    d.diagpos = upload(m.ldiagpos);
+    d.perm = upload(m.perm);
+    d.iperm = upload(m.iperm);
+    d.jrowptr = upload(m.rowptr);
+    d.jcolidx = upload(m.jcolidx);
     d.asm_ptr = upload(m.asm_ptr);
     d.asm_list = upload(m.asm_list);
     d.nel_ptr = upload(m.nel_ptr);
     d.nel_list = upload(m.nel_list);
+    d.nel_pos = upload(m.nel_pos);
     d.bndnode = upload(m.bndnode);
-    M->fwd_lev_ptr_h = m.fwd_lev_ptr;
-    M->bwd_lev_ptr_h = m.bwd_lev_ptr;
+    for (int t = 0; t < 2; t++) {
+        const ICHost& c = m.ic[t];
+        ICDev& g = d.ic[t];
+        g.nnzL = c.Lrowptr[n];
+        g.nlev_fwd = (int)c.fwd_lev_ptr.size() - 1;
+        g.nlev_bwd = (int)c.bwd_lev_ptr.size() - 1;
+        g.nell_fwd = (int)c.fwd_ell_col.size();
+        g.nell_bwd = (int)c.bwd_ell_col.size();
+        g.key = upload(c.key);
+        g.Lrowptr = upload(c.Lrowptr);
+        g.Lcolidx = upload(c.Lcolidx);
+        g.Lapos = upload(c.Lapos);
+        g.Lkey = upload(c.Lkey);
+        g.Ucolptr = upload(c.Ucolptr);
+        g.Urow = upload(c.Urow);
+        g.Umap = upload(c.Umap);
+        g.fwd_lev_rows = upload(c.fwd_lev_rows);
+        g.bwd_lev_rows = upload(c.bwd_lev_rows);
+        g.fwd_ell_col = upload(c.fwd_ell_col);
+        g.fwd_ell_src = upload(c.fwd_ell_src);
+        g.bwd_ell_col = upload(c.bwd_ell_col);
+        g.bwd_ell_src = upload(c.bwd_ell_src);
+    }
     return M;
 }
 

@@ -17,6 +17,25 @@ namespace tg {
 //        [22..31] unused
 constexpr int EL_REC = 32;
 
+// IC(0) pattern for one elimination ordering, in layout positions.  key[p] =
+// rank of layout row p in the ordering; L row p = its neighbours of smaller
+// rank in ascending rank (the factorisation's merge order), U = column view,
+// levels = depth in the dependency graph (rows of a level in layout order),
+// ELL copies of each level's entries for the sweep kernels.
+struct ICHost {
+    std::vector<int> key, Lrowptr, Lcolidx, Lapos, Lkey, Ucolptr, Urow, Umap;
+    std::vector<int> fwd_lev_ptr, fwd_lev_rows, bwd_lev_ptr, bwd_lev_rows;
+    std::vector<int> fwd_ell_w, fwd_ell_off, fwd_ell_col, fwd_ell_src;
+    std::vector<int> bwd_ell_w, bwd_ell_off, bwd_ell_col, bwd_ell_src;
+};
+
+struct ICDev {
+    int nnzL, nlev_fwd, nlev_bwd, nell_fwd, nell_bwd;
+    int *key, *Lrowptr, *Lcolidx, *Lapos, *Lkey, *Ucolptr, *Urow, *Umap;
+    int *fwd_lev_rows, *bwd_lev_rows;
+    int *fwd_ell_col, *fwd_ell_src, *bwd_ell_col, *bwd_ell_src;
+};
+
 struct MeshHost {
     int dim = 0, n = 0, ne = 0, nn = 0;
     std::vector<double> coords;       // n*dim
@@ -25,36 +44,42 @@ struct MeshHost {
     std::vector<double> rec;          // ne*EL_REC element record
     std::vector<unsigned char> bndside, bndnode;
     std::vector<double> intbff;       // ne*nn*nn (source vectors)
-    // CSR pattern of F
+    // CSR pattern of F in the natural (reference) numbering; the host API reports it
     std::vector<int> rowptr, colidx, diagpos;
-    // IC(0): strict lower pattern L (rows), its column view U (for the back
-    // sweep and the factorisation), A positions of each L/U entry
-    std::vector<int> Lrowptr, Lcolidx, Lapos;       // Lapos: index of a_ij in F for L(i,j)
-    std::vector<int> Ucolptr, Urow, Umap;           // column i of L: rows r>i, index into L
-    std::vector<int> fwd_lev_ptr, fwd_lev_rows, bwd_lev_ptr, bwd_lev_rows;
+    // device layout: nodes stored in a spatially coherent (Morton) order.
+    // perm[natural] = layout position, iperm[layout] = natural node.  Layout
+    // rows keep their entries in natural column order, so every row sum is
+    // the reference's; lay2nat[e] = natural CSR entry of layout entry e.
+    std::vector<int> perm, iperm, lrowptr, lcolidx, ldiagpos, lay2nat, Lkey, jcolidx;
+    // IC(0) structures: [0] the natural (reference) ordering, [1] a colour-major
+    // ordering (greedy colouring, colour classes are independent sets) used by
+    // the FP32 inner preconditioner of the mixed path
+    ICHost ic[2];
+    int ncolors = 0;
     // assembly gather map: for F entry k, contributions (el*16 + i*4 + j) in element order
     std::vector<int> asm_ptr, asm_list;
     // node -> (element*4 + local index), element order
     std::vector<int> nel_ptr, nel_list;
+    std::vector<unsigned> nel_pos;
 };
 
 struct MeshDev {
-    int dim, n, ne, nn, nnz, nnzL, nlev_fwd, nlev_bwd;
+    int dim, n, ne, nn, nnz;
     double* rec;
-    int* el;
-    int *rowptr, *colidx, *diagpos;
-    int *Lrowptr, *Lcolidx, *Lapos;
-    int *Ucolptr, *Urow, *Umap;
-    int *fwd_lev_rows, *bwd_lev_rows;
+    int* el;                   // element nodes, natural numbering
+    int *rowptr, *colidx, *diagpos;   // layout CSR (rows and columns in layout positions)
+    int *perm, *iperm;         // natural -> layout, layout -> natural
+    int *jrowptr, *jcolidx;    // natural-row CSR with layout column ids (Jacobian tiles over natural nodes)
+    unsigned *nel_pos;         // per node-element slot: positions of the element nodes in the node's CSR row (4 x uint8)
     int *asm_ptr, *asm_list;
     int *nel_ptr, *nel_list;
     unsigned char* bndnode;
+    ICDev ic[2];
 };
 
 struct Mesh {
     MeshHost h;
     MeshDev d{};
-    std::vector<int> fwd_lev_ptr_h, bwd_lev_ptr_h;
     int device = 0;
     ~Mesh();
 };

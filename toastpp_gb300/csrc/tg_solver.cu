@@ -98,6 +98,57 @@ struct DBuf {
 
 static inline unsigned cdiv_u(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 
+
+// Captured launch sequences (the level kernels of an IC(0) apply or
+// factorisation), keyed by their sizes and buffer pointers and replayed with
+// one cudaGraphLaunch.
+struct GraphCache {
+    struct Entry {
+        std::vector<const void*> key;
+        cudaGraphExec_t exec;
+        long long kernels;
+    };
+    std::vector<Entry> entries;
+    ~GraphCache()
+    {
+        for (auto& e : entries) cudaGraphExecDestroy(e.exec);
+    }
+    template <class F>
+    void run(cudaStream_t st, const std::vector<const void*>& key, F body)
+    {
+        for (auto& e : entries)
+            if (e.key == key) {
+                TG_CUDA(cudaGraphLaunch(e.exec, st));
+                g_nlaunch.fetch_add(e.kernels);
+                return;
+            }
+        cudaGraph_t g = nullptr;
+        long long c0 = g_nlaunch.load();
+        TG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+            body();
+        } catch (...) {
+            cudaStreamEndCapture(st, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        TG_CUDA(cudaStreamEndCapture(st, &g));
+        long long cnt = g_nlaunch.load() - c0;
+        g_nlaunch.fetch_sub(cnt);  // captured, not yet launched
+        cudaGraphExec_t ex = nullptr;
+        cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        TG_CUDA(e);
+        if (entries.size() >= 16) {
+            cudaGraphExecDestroy(entries.front().exec);
+            entries.erase(entries.begin());
+        }
+        entries.push_back({key, ex, cnt});
+        TG_CUDA(cudaGraphLaunch(ex, st));
+        g_nlaunch.fetch_add(cnt);
+    }
+};
+
 // ---------------------------------------------------------------------------
 // Krylov engine for one value type.  Vectors are node-major n x k (ld = k).
 // ---------------------------------------------------------------------------
@@ -110,12 +161,19 @@ struct Engine {
     const V* L = nullptr;      // IC(0) lower factor
     const V* dinv = nullptr;   // 1 / IC diagonal
     const V* idiag = nullptr;  // 1 / diag(A) (Diag preconditioner)
+    const V* Lef = nullptr;    // factor values in the forward / backward level ELL layouts
+    const V* Leb = nullptr;
+    int ico = 0;               // IC ordering: 0 natural, 1 colour-major
     int precon = 0;            // 0 none, 1 diag, 2 ich
     Profiler* prof = nullptr;
     DBuf w[9], part, cs, cnt;
     int* h_cnt = nullptr;
+    GraphCache graphs;
 
-    ~Engine() { if (h_cnt) cudaFreeHost(h_cnt); }
+    ~Engine()
+    {
+        if (h_cnt) cudaFreeHost(h_cnt);
+    }
 
     V* vec(int i, size_t nk) { return (V*)w[i].ensure(nk * sizeof(V)); }
     int ntiles() const { return (int)cdiv_u(mesh->d.n, ROW_TILE); }
@@ -126,8 +184,30 @@ struct Engine {
     {
         const MeshDev& m = mesh->d;
         ProfScope ps(prof, PC_SPMM, st);
+        constexpr int P = W16<V>::P;
+        const int nw = (k / P + 31) / 32;
+        if (k >= 32 && k % P == 0 && nw <= 4) {
+            switch (nw) {
+#define TG_SPMM_VW(J) case J: launch(spmm_vec_kernel<V, J>, ntiles(), 256, 0, st, m.n, m.rowptr, m.colidx, A, k, k, \
+                                     x, y, wv, n2, pt, np, ntiles(), cst); break;
+            TG_SPMM_VW(1) TG_SPMM_VW(2) TG_SPMM_VW(3) TG_SPMM_VW(4)
+#undef TG_SPMM_VW
+            }
+            return;
+        }
+        const int nj = (k + 31) / 32;
+        if (k >= 32 && nj <= 8) {
+            switch (nj) {
+#define TG_SPMM_NJ(J) case J: launch(spmm_wide_kernel<V, J>, ntiles(), 256, 0, st, m.n, m.rowptr, m.colidx, A, k, k, \
+                                     x, y, wv, n2, pt, np, ntiles(), cst); break;
+            TG_SPMM_NJ(1) TG_SPMM_NJ(2) TG_SPMM_NJ(3) TG_SPMM_NJ(4) TG_SPMM_NJ(5) TG_SPMM_NJ(6) TG_SPMM_NJ(7)
+            TG_SPMM_NJ(8)
+#undef TG_SPMM_NJ
+            }
+            return;
+        }
         launch(spmm_dot_kernel<V>, ntiles(), 256, 0, st, m.n, m.rowptr, m.colidx, A, k, k, x, y, wv, n2, pt, np,
-                                                     ntiles(), cst);
+               ntiles(), cst);
     }
     template <int NP>
     void finalize(int k, ColState* cst, int phase, int real_variant = 0, int iter = 0)
@@ -136,26 +216,56 @@ struct Engine {
     }
     static int colw(int k) { return k >= 32 ? 32 : (k >= 16 ? 16 : (k >= 8 ? 8 : (k >= 4 ? 4 : (k >= 2 ? 2 : 1)))); }
 
-    // out = M^-1 in for the IC(0) preconditioner (level-scheduled sweeps)
+    void launch_level_ell(bool fwd, int l, int off, int nr, int k, const V* in, V* out, const ColState* cst)
+    {
+        const MeshDev& m = mesh->d;
+        unsigned g = cdiv_u((size_t)nr * 32, 256);
+        const ICHost& ch = mesh->h.ic[ico];
+        const ICDev& cd_ = m.ic[ico];
+        const int w = fwd ? ch.fwd_ell_w[l] : ch.bwd_ell_w[l];
+        const int eo = fwd ? ch.fwd_ell_off[l] : ch.bwd_ell_off[l];
+        const int* rows = (fwd ? cd_.fwd_lev_rows : cd_.bwd_lev_rows) + off;
+        const int* ec = (fwd ? cd_.fwd_ell_col : cd_.bwd_ell_col) + eo;
+        const V* ev = (fwd ? Lef : Leb) + eo;
+        const V* src = fwd ? in : out;
+        switch ((k + 31) / 32) {
+#define TG_LE(J) case J: if (fwd) launch(ic_level_ell<V, J, true>, g, 256, 0, st, rows, nr, w, ec, ev, k, k, dinv, src, out, cst); \
+                         else launch(ic_level_ell<V, J, false>, g, 256, 0, st, rows, nr, w, ec, ev, k, k, dinv, src, out, cst); break;
+        TG_LE(1) TG_LE(2) TG_LE(3) TG_LE(4) TG_LE(5) TG_LE(6) TG_LE(7) TG_LE(8)
+#undef TG_LE
+        }
+    }
+
+    // out = M^-1 in for the IC(0) preconditioner: the forward and backward
+    // level kernels, captured once per (k, buffers) and replayed as one graph
     void ic_apply(int k, const V* in, V* out, const ColState* cst)
     {
         const MeshDev& m = mesh->d;
+        const ICHost& ch = mesh->h.ic[ico];
+        const ICDev& ic = m.ic[ico];
         ProfScope ps(prof, PC_SWEEP, st);
         int cw = colw(k), ncg = (k + cw - 1) / cw, rpw = 32 / cw;
-        const std::vector<int>& fp = mesh->fwd_lev_ptr_h;
-        for (size_t l = 0; l + 1 < fp.size(); l++) {
-            int nr = fp[l + 1] - fp[l];
-            size_t warps = cdiv_u((size_t)nr * ncg, rpw);
-            launch(ic_fwd_level<V, S>, cdiv_u(warps * 32, 256), 256, 0, st, m, m.fwd_lev_rows + fp[l], nr, k, k, cw, L,
-                                                                       dinv, in, out, cst);
-        }
-        const std::vector<int>& bp = mesh->bwd_lev_ptr_h;
-        for (size_t l = 0; l + 1 < bp.size(); l++) {
-            int nr = bp[l + 1] - bp[l];
-            size_t warps = cdiv_u((size_t)nr * ncg, rpw);
-            launch(ic_bwd_level<V, S>, cdiv_u(warps * 32, 256), 256, 0, st, m, m.bwd_lev_rows + bp[l], nr, k, k, cw, L,
-                                                                       dinv, out, cst);
-        }
+        std::vector<const void*> key = {(const void*)(size_t)k, in, out, cst, L, dinv, Lef, Leb, mesh,
+                                        (const void*)(size_t)ico};
+        const bool wide = k >= 32 && k <= 256;
+        graphs.run(st, key, [&] {
+            const std::vector<int>& fp = ch.fwd_lev_ptr;
+            for (size_t l = 0; l + 1 < fp.size(); l++) {
+                int nr = fp[l + 1] - fp[l];
+                size_t warps = cdiv_u((size_t)nr * ncg, rpw);
+                if (wide) launch_level_ell(true, (int)l, fp[l], nr, k, in, out, cst);
+                else launch(ic_fwd_level<V, S>, cdiv_u(warps * 32, 256), 256, 0, st, ic, ic.fwd_lev_rows + fp[l], nr, k,
+                            k, cw, L, dinv, in, out, cst);
+            }
+            const std::vector<int>& bp = ch.bwd_lev_ptr;
+            for (size_t l = 0; l + 1 < bp.size(); l++) {
+                int nr = bp[l + 1] - bp[l];
+                size_t warps = cdiv_u((size_t)nr * ncg, rpw);
+                if (wide) launch_level_ell(false, (int)l, bp[l], nr, k, out, out, cst);
+                else launch(ic_bwd_level<V, S>, cdiv_u(warps * 32, 256), 256, 0, st, ic, ic.bwd_lev_rows + bp[l], nr, k,
+                            k, cw, L, dinv, out, cst);
+            }
+        });
     }
 
     int count_active(int k, ColState* cst)
@@ -210,8 +320,8 @@ struct Engine {
         finalize<1>(k, cst, PH_BICG_RHO0);
         int pmode = precon == 2 ? 2 : precon;
         const int real_variant = vt<V>::cplx ? 0 : 1;
-        for (int it = 0; it < maxit; it++) {
-            launch(bicg_p_kernel<V, S>, eg, 256, 0, st, m.n, k, k, cst, it == 0, R, P, Vv, PD, idiag, pmode);
+        auto iteration = [&](int first) {
+            launch(bicg_p_kernel<V, S>, eg, 256, 0, st, m.n, k, k, cst, first, R, P, Vv, PD, idiag, pmode);
             if (pmode == 2) ic_apply(k, P, PD, cst);
             spmm(k, PD, Vv, RD, false, cst, pt, 1);
             finalize<1>(k, cst, PH_BICG_ALPHA);
@@ -222,6 +332,9 @@ struct Engine {
             finalize<2>(k, cst, PH_BICG_OMEGA);
             launch(bicg_xr_kernel<V, S>, ntiles(), rowblk(k), 0, st, m.n, k, k, cst, X, R, RD, PD, SD, Sv, T, pt, ntiles());
             finalize<2>(k, cst, PH_BICG_END);
+        };
+        for (int it = 0; it < maxit; it++) {
+            iteration(it == 0);
             if ((it & 3) == 3 || it + 1 == maxit)
                 if (count_active(k, cst) == 0) break;
         }
@@ -239,7 +352,7 @@ struct Engine {
         TG_CUDA(cudaMemcpyAsync(D, Z, nk * sizeof(V), cudaMemcpyDeviceToDevice, st));
         launch(dot_tiles_kernel<V>, ntiles(), rowblk(k), 0, st, m.n, k, k, R, Z, nullptr, nullptr, pt, 1, ntiles(), cst);
         finalize<1>(k, cst, PH_PCG_INIT);
-        for (int it = 0; it < maxit; it++) {
+        auto iteration = [&]() {
             spmm(k, D, Q, D, false, cst, pt, 1);
             finalize<1>(k, cst, PH_PCG_ALPHA);
             launch(pcg_xr_kernel<V, S>, ntiles(), rowblk(k), 0, st, m.n, k, k, cst, X, R, D, Q, Z, idiag, precon, pt, ntiles());
@@ -249,6 +362,9 @@ struct Engine {
             }
             finalize<2>(k, cst, PH_PCG_END);
             launch(pcg_d_kernel<V, S>, eg, 256, 0, st, m.n, k, k, cst, D, Z);
+        };
+        for (int it = 0; it < maxit; it++) {
+            iteration();
             if ((it & 3) == 3 || it + 1 == maxit)
                 if (count_active(k, cst) == 0) break;
         }
@@ -316,9 +432,13 @@ struct tg_solver_s {
     Mesh* mesh = nullptr;
     int cplx = 0, method = 1, precon = 2, precision = 0, maxit = 0;
     double tol = 1e-10;
+    double inner_tol = 1e-4;   // mixed path: relative tolerance of each FP32 inner solve
+    int max_outer = 12;        // mixed path: refinement steps
+    int inner_colour = 1;      // mixed path: IC(0) of the inner solves in the colour-major ordering
     cudaStream_t stream = 0, own = 0;
     bool reset_done = false;
     DBuf val64, val32, L64, L32, dinv64, dinv32, idiag64, idiag32, params;
+    DBuf ef64, eb64, ef32, eb32;  // factor values in the level ELL layouts
     Engine<double> er64;
     Engine<float> er32;
     Engine<cd> ec64;
@@ -327,6 +447,7 @@ struct tg_solver_s {
     DBuf jF, jG, jpair, jyinv, plink_q, plink_m, psup, pnsup, pflag, pMsup, plin, plog;
     DBuf fp_bq, fp_xq, fp_bm, fp_xm, fp_lin, fp_log;
     Profiler prof;
+    GraphCache graphs;
     std::mutex mu;
 };
 
@@ -367,8 +488,16 @@ static void setup_engine(tg_solver s, Engine<V64>& e64)
     e64.mesh = s->mesh; e64.st = s->stream; e64.precon = s->precon == TG_PRECON_DILU ? 0 : s->precon;
     e64.A = s->val64.as<V64>(); e64.L = s->L64.as<V64>(); e64.dinv = s->dinv64.as<V64>();
     e64.idiag = s->idiag64.as<V64>();
+    e64.Lef = s->ef64.as<V64>();
+    e64.Leb = s->eb64.as<V64>();
     e64.prof = &s->prof;
+    e64.ico = 0;
 }
+
+// IC ordering the solver's preconditioner is factored in: the natural
+// (reference) ordering for the FP64 path, the colour-major ordering for the
+// FP32 inner solves of the mixed path (unless the natural one is requested)
+static int ic_order(tg_solver s) { return (s->precision == TG_PREC_MIXED && s->inner_colour) ? 1 : 0; }
 
 template <class V64, class V32>
 static void do_reset(tg_solver s, const double* cmua, const double* ckap, const double* c2a, double omega, int mem)
@@ -383,28 +512,48 @@ static void do_reset(tg_solver s, const double* cmua, const double* ckap, const 
     V64* A = (V64*)s->val64.ensure((size_t)m.nnz * sizeof(V64));
     ProfScope ps(&s->prof, PC_ASM, s->stream);
     launch(assemble_kernel<vt<V64>::cplx>, cdiv_u(m.nnz, 256), 256, 0, s->stream, m, P, P + m.n, P + 2 * m.n, omega,
-                                                                             (double*)A);
+           (double*)A);
     int pre = s->precon == TG_PRECON_DILU ? 0 : s->precon;
     V64* idg = (V64*)s->idiag64.ensure((size_t)m.n * sizeof(V64));
     launch(diag_inv_kernel<V64>, cdiv_u(m.n, 256), 256, 0, s->stream, m.n, m.diagpos, A, idg);
+    const bool mixed = s->precision == TG_PREC_MIXED;
     if (pre == TG_PRECON_ICH) {
-        V64* L = (V64*)s->L64.ensure((size_t)std::max(m.nnzL, 1) * sizeof(V64));
+        const int o = ic_order(s);
+        const ICDev& ic = m.ic[o];
+        const ICHost& ch = s->mesh->h.ic[o];
+        V64* L = (V64*)s->L64.ensure((size_t)std::max(ic.nnzL, 1) * sizeof(V64));
         V64* dinv = (V64*)s->dinv64.ensure((size_t)m.n * sizeof(V64));
-        const std::vector<int>& fp = s->mesh->fwd_lev_ptr_h;
-        for (size_t l = 0; l + 1 < fp.size(); l++) {
-            int nr = fp[l + 1] - fp[l];
-            launch(ic_factor_level<V64>, cdiv_u(nr, 128), 128, 0, s->stream, m, m.fwd_lev_rows + fp[l], nr, A, L, dinv);
+        std::vector<const void*> key = {A, L, dinv, s->mesh, (const void*)(size_t)o};
+        s->graphs.run(s->stream, key, [&] {
+            const std::vector<int>& fp = ch.fwd_lev_ptr;
+            for (size_t l = 0; l + 1 < fp.size(); l++) {
+                int nr = fp[l + 1] - fp[l];
+                launch(ic_factor_level<V64>, cdiv_u(nr, 128), 128, 0, s->stream, m, ic, ic.fwd_lev_rows + fp[l], nr,
+                       A, L, dinv);
+            }
+        });
+        V64* ef = (V64*)s->ef64.ensure((size_t)std::max(ic.nell_fwd, 1) * sizeof(V64));
+        V64* eb = (V64*)s->eb64.ensure((size_t)std::max(ic.nell_bwd, 1) * sizeof(V64));
+        launch(ell_gather_kernel<V64>, cdiv_u(std::max(ic.nell_fwd, 1), 256), 256, 0, s->stream, ic.nell_fwd,
+               ic.fwd_ell_src, L, ef);
+        launch(ell_gather_kernel<V64>, cdiv_u(std::max(ic.nell_bwd, 1), 256), 256, 0, s->stream, ic.nell_bwd,
+               ic.bwd_ell_src, L, eb);
+        if (mixed) {
+            launch(cast_kernel<V32, V64>, cdiv_u(std::max(ic.nell_fwd, 1), 256), 256, 0, s->stream,
+                   (size_t)ic.nell_fwd, ef, (V32*)s->ef32.ensure((size_t)std::max(ic.nell_fwd, 1) * sizeof(V32)));
+            launch(cast_kernel<V32, V64>, cdiv_u(std::max(ic.nell_bwd, 1), 256), 256, 0, s->stream,
+                   (size_t)ic.nell_bwd, eb, (V32*)s->eb32.ensure((size_t)std::max(ic.nell_bwd, 1) * sizeof(V32)));
+            launch(cast_kernel<V32, V64>, cdiv_u(std::max(ic.nnzL, 1), 256), 256, 0, s->stream, (size_t)ic.nnzL, L,
+                   (V32*)s->L32.ensure((size_t)std::max(ic.nnzL, 1) * sizeof(V32)));
+            launch(cast_kernel<V32, V64>, cdiv_u(m.n, 256), 256, 0, s->stream, (size_t)m.n, dinv,
+                   (V32*)s->dinv32.ensure(m.n * sizeof(V32)));
         }
     }
-    if (s->precision == TG_PREC_MIXED) {
-        launch(cast_kernel<V32, V64>, cdiv_u(m.nnz, 256), 256, 0, s->stream, m.nnz, A, (V32*)s->val32.ensure(m.nnz * sizeof(V32)));
-        launch(cast_kernel<V32, V64>, cdiv_u(m.n, 256), 256, 0, s->stream, m.n, idg, (V32*)s->idiag32.ensure(m.n * sizeof(V32)));
-        if (pre == TG_PRECON_ICH) {
-            launch(cast_kernel<V32, V64>, cdiv_u(std::max(m.nnzL, 1), 256), 256, 0, s->stream, 
-                m.nnzL, s->L64.as<V64>(), (V32*)s->L32.ensure((size_t)std::max(m.nnzL, 1) * sizeof(V32)));
-            launch(cast_kernel<V32, V64>, cdiv_u(m.n, 256), 256, 0, s->stream, m.n, s->dinv64.as<V64>(),
-                                                                          (V32*)s->dinv32.ensure(m.n * sizeof(V32)));
-        }
+    if (mixed) {
+        launch(cast_kernel<V32, V64>, cdiv_u(m.nnz, 256), 256, 0, s->stream, (size_t)m.nnz, A,
+               (V32*)s->val32.ensure(m.nnz * sizeof(V32)));
+        launch(cast_kernel<V32, V64>, cdiv_u(m.n, 256), 256, 0, s->stream, (size_t)m.n, idg,
+               (V32*)s->idiag32.ensure(m.n * sizeof(V32)));
     }
     TG_CUDA(cudaGetLastError());
 }
@@ -468,7 +617,10 @@ static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co)
     e32.mesh = s->mesh; e32.st = s->stream; e32.precon = e64.precon;
     e32.A = s->val32.as<V32>(); e32.L = s->L32.as<V32>(); e32.dinv = s->dinv32.as<V32>();
     e32.idiag = s->idiag32.as<V32>();
+    e32.Lef = s->ef32.as<V32>();
+    e32.Leb = s->eb32.as<V32>();
     e32.prof = &s->prof;
+    e32.ico = ic_order(s);
     V64* R = (V64*)s->tmp.ensure(nk * sizeof(V64));
     V32* R32 = (V32*)s->B32.ensure(nk * sizeof(V32));
     V32* E32 = (V32*)s->X32.ensure(nk * sizeof(V32));
@@ -479,8 +631,8 @@ static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co)
     launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, B, B, nullptr, nullptr, pt, 1,
                                                                       e64.ntiles(), nullptr);
     e64.template finalize<1>(k, co, PH_BNORM);
-    const int max_outer = 12;
-    const double inner_tol = 1e-5;
+    const int max_outer = s->max_outer;
+    const double inner_tol = s->inner_tol;
     for (int step = 0; step <= max_outer; step++) {
         launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, R, R, nullptr, nullptr, pt, 1,
                                                                           e64.ntiles(), nullptr);
@@ -529,72 +681,84 @@ static void project_nm(tg_solver s, const V* X, int ldx, int nm, const V* mvec, 
     upload_async(s, s->plink_q, L.q);
     upload_async(s, s->plink_m, L.m);
     ProfScope ps(&s->prof, PC_PROJ, s->stream);
-    launch(project_kernel<V>, cdiv_u((size_t)nqm * 32, 256), 256, 0, s->stream, 
-        nsup, sup, X, ldx, Msup, nm, s->plink_q.as<int>(), s->plink_m.as<int>(), nqm, lg != nullptr, lin, lg);
+    launch(project_kernel<V>, cdiv_u((size_t)nqm * 32, 256), 256, 0, s->stream, nsup, sup, s->mesh->d.perm, X, ldx,
+           Msup, nm, s->plink_q.as<int>(), s->plink_m.as<int>(), nqm, lg != nullptr, lin, lg);
     TG_CUDA(cudaGetLastError());
 }
 
-template <class VC>
-static void launch_jacobian(tg_solver s, int nq, const VC* F, int nm, const VC* G, const LinkHost& L,
-                            const VC* yinv, void* J, int out_fp32)
+template <class VC, int KT>
+static bool try_launch_jacobian(tg_solver s, const JacArgs<VC>& a)
 {
     const MeshDev& m = s->mesh->d;
-    upload_async(s, s->jpair, L.pair);
-    JacArgs<VC> a;
-    a.m = m; a.nq = nq; a.nm = nm; a.nqm = (int)L.q.size();
-    a.F = F; a.ldf = nq; a.G = G; a.ldg = nm;
-    a.pairidx = s->jpair.as<int>(); a.yinv = yinv; a.J = J; a.out_fp32 = out_fp32;
     // the largest CSR row span of a node tile sets the shared-memory size
     const std::vector<int>& rp = s->mesh->h.rowptr;
     int rmax = 0;
-    for (int k0 = 0; k0 < m.n; k0 += JT_NODES) rmax = std::max(rmax, rp[std::min(m.n, k0 + JT_NODES)] - rp[k0]);
-    size_t smem = (size_t)rmax * (3 * JT_M + JT_Q) * sizeof(VC);
-    TG_CHECK(smem <= 220 * 1024, TG_ERR_UNSUPPORTED, "mesh node degree too high for the Jacobian tile");
-    TG_CUDA(cudaFuncSetAttribute(jacobian_kernel<VC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid(cdiv_u(m.n, JT_NODES), cdiv_u(nm, JT_M));
+    for (int k0 = 0; k0 < m.n; k0 += KT) rmax = std::max(rmax, rp[std::min(m.n, k0 + KT)] - rp[k0]);
+    size_t smem = (size_t)rmax * (3 * JM + JQ) * sizeof(VC);
+    if (smem > 200 * 1024) return false;
+    TG_CUDA(cudaFuncSetAttribute(jacobian_kernel<VC, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid(cdiv_u(m.n, KT), cdiv_u(a.nm, JM));
     ProfScope ps(&s->prof, PC_JAC, s->stream);
-    launch(jacobian_kernel<VC>, grid, JT_Q * JT_M, smem, s->stream, a);
-    TG_CUDA(cudaGetLastError());
+    launch(jacobian_kernel<VC, KT>, grid, 256, smem, s->stream, a);
+    return true;
 }
 
-// Jacobian from node-major FP64 fields; the mixed path computes it in FP32
-// from FP32 copies of the (refined) fields.  ylin: device linear projections or null.
+template <class VC>
+static void launch_jacobian(tg_solver s, int nq, const VC* F, int ldf, int nm, const VC* G, int ldg,
+                            const LinkHost& L, const VC* yinv, void* J, int out_fp32)
+{
+    upload_async(s, s->jpair, L.pair);
+    JacArgs<VC> a;
+    a.m = s->mesh->d; a.nq = nq; a.nm = nm; a.nqm = (int)L.q.size();
+    a.F = F; a.ldf = ldf; a.G = G; a.ldg = ldg;
+    a.pairidx = s->jpair.as<int>(); a.yinv = yinv; a.J = J; a.out_fp32 = out_fp32;
+    if (sizeof(VC) <= 8 && try_launch_jacobian<VC, 32>(s, a)) return;
+    if (try_launch_jacobian<VC, 16>(s, a)) return;
+    if (try_launch_jacobian<VC, 8>(s, a)) return;
+    throw Error{TG_ERR_UNSUPPORTED, "mesh node degree too high for the Jacobian tile"};
+}
+
+// Jacobian from node-major FP64 fields (F: nq columns at stride ldf, G: nm
+// columns at stride ldg); the mixed path computes it in FP32 from FP32 copies
+// of the refined fields.  ylin: device linear projections or null.
 template <class V64, class V32>
-static void jacobian_nm(tg_solver s, int nq, const V64* F, int nm, const V64* G, const LinkHost& L,
-                        const V64* ylin, void* J, int out_fp32)
+static void jacobian_nm(tg_solver s, int nq, const V64* F, int ldf, int nm, const V64* G, int ldg,
+                        const LinkHost& L, const V64* ylin, void* J, int out_fp32)
 {
     const MeshDev& m = s->mesh->d;
     int n = m.n, nqm = (int)L.q.size();
     if (s->precision == TG_PREC_MIXED) {
         V32* F32 = (V32*)s->jF.ensure((size_t)n * nq * sizeof(V32));
         V32* G32 = (V32*)s->jG.ensure((size_t)n * nm * sizeof(V32));
-        launch(cast_kernel<V32, V64>, cdiv_u((size_t)n * nq, 256), 256, 0, s->stream, (size_t)n * nq, F, F32);
-        launch(cast_kernel<V32, V64>, cdiv_u((size_t)n * nm, 256), 256, 0, s->stream, (size_t)n * nm, G, G32);
+        launch(strided_cast_kernel<V32, V64>, cdiv_u((size_t)n * nq, 256), 256, 0, s->stream, n, nq, F, ldf, F32);
+        launch(strided_cast_kernel<V32, V64>, cdiv_u((size_t)n * nm, 256), 256, 0, s->stream, n, nm, G, ldg, G32);
         V32* yi = nullptr;
         if (ylin) {
             yi = (V32*)s->jyinv.ensure((size_t)std::max(nqm, 1) * sizeof(V32));
             launch(recip_cast_kernel<V32, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, ylin, yi);
         }
-        launch_jacobian<V32>(s, nq, F32, nm, G32, L, yi, J, out_fp32);
+        launch_jacobian<V32>(s, nq, F32, nq, nm, G32, nm, L, yi, J, out_fp32);
     } else {
         V64* yi = nullptr;
         if (ylin) {
             yi = (V64*)s->jyinv.ensure((size_t)std::max(nqm, 1) * sizeof(V64));
             launch(recip_cast_kernel<V64, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, ylin, yi);
         }
-        launch_jacobian<V64>(s, nq, F, nm, G, L, yi, J, out_fp32);
+        launch_jacobian<V64>(s, nq, F, ldf, nm, G, ldg, L, yi, J, out_fp32);
     }
 }
 
 template <class V>
 static void src_to_nm(tg_solver s, int n, int k, const V* src, V* dst)
 {
-    launch(to_nodemajor_kernel<V, V>, dim3(cdiv_u(n, 32), cdiv_u(k, 32)), dim3(32, 8), 0, s->stream, n, k, k, src, dst);
+    launch(to_nodemajor_kernel<V, V>, dim3(cdiv_u(n, 32), cdiv_u(k, 32)), dim3(32, 8), 0, s->stream, n, k, k, src, dst,
+           s->mesh->d.perm);
 }
 template <class V>
 static void nm_to_src(tg_solver s, int n, int k, const V* nm, V* dst)
 {
-    launch(to_srcmajor_kernel<V, V>, dim3(cdiv_u(n, 32), cdiv_u(k, 32)), dim3(32, 8), 0, s->stream, n, k, k, nm, dst);
+    launch(to_srcmajor_kernel<V, V>, dim3(cdiv_u(n, 32), cdiv_u(k, 32)), dim3(32, 8), 0, s->stream, n, k, k, nm, dst,
+           s->mesh->d.perm);
 }
 
 // ---------------------------------------------------------------------------
@@ -650,7 +814,7 @@ static void api_jacobian(tg_solver s, int nq, const double* dphi, int nm, const 
     const V64* yl = scale == TG_DATA_LOG ? (const V64*)dev_in(s, proj, (size_t)nqm * sizeof(V64), mem, s->plin) : nullptr;
     size_t jbytes = (size_t)2 * nqm * (vt<V64>::cplx ? 2 * n : n) * (out_fp32 ? 4 : 8);
     void* Jd = mem == TG_MEM_DEVICE ? J : s->jout.ensure(jbytes);
-    jacobian_nm<V64, V32>(s, nq, F, nm, G, L, yl, Jd, out_fp32);
+    jacobian_nm<V64, V32>(s, nq, F, nq, nm, G, nm, L, yl, Jd, out_fp32);
     if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(J, Jd, jbytes, cudaMemcpyDeviceToHost, s->stream));
     TG_CUDA(cudaStreamSynchronize(s->stream));
 }
@@ -662,44 +826,43 @@ static void api_forward_path(tg_solver s, const double* cmua, const double* ckap
                              tg_result* res)
 {
     const MeshDev& m = s->mesh->d;
-    int n = m.n, nqm = (int)L.q.size();
+    int n = m.n, nqm = (int)L.q.size(), k = nq + nm;
     do_reset<V64, V32>(s, cmua, ckap, c2a, omega, mem);
     s->reset_done = true;
-    size_t qb = (size_t)nq * n * sizeof(V64), mb = (size_t)nm * n * sizeof(V64);
+    size_t qb = (size_t)nq * n * sizeof(V64), mb = (size_t)nm * n * sizeof(V64), kb = (size_t)k * n * sizeof(V64);
     const V64* Qs = (const V64*)dev_in(s, qvec, qb, mem, s->io_a);
     const V64* Ms = (const V64*)dev_in(s, mvec, mb, mem, s->io_b);
-    V64* Bq = (V64*)s->fp_bq.ensure(qb);
-    V64* Xq = (V64*)s->fp_xq.ensure(qb);
-    V64* Bm = (V64*)s->fp_bm.ensure(mb);
-    V64* Xm = (V64*)s->fp_xm.ensure(mb);
-    src_to_nm(s, n, nq, Qs, Bq);
-    src_to_nm(s, n, nm, Ms, Bm);
-    TG_CUDA(cudaMemsetAsync(Xq, 0, qb, s->stream));
-    TG_CUDA(cudaMemsetAsync(Xm, 0, mb, s->stream));
-    ColState* co = (ColState*)s->cs_outer.ensure(sizeof(ColState) * std::max(nq, nm));
-    solve_nm<V64, V32>(s, nq, Bq, Xq, co);
-    if (res) read_results(s, nq, co, res);
-    // the mvec rows are the adjoint sources (toastmodule.cc:1556-1557)
-    solve_nm<V64, V32>(s, nm, Bm, Xm, co);
-    if (res) read_results(s, nm, co, res + nq);
+    // forward sources (columns 0..nq-1) and adjoint sources, the detector
+    // vectors (toastmodule.cc:1556-1557), in one batch of k right-hand sides
+    V64* B = (V64*)s->fp_bq.ensure(kb);
+    V64* X = (V64*)s->fp_xq.ensure(kb);
+    dim3 tb(32, 8);
+    launch(to_nodemajor_kernel<V64, V64>, dim3(cdiv_u(n, 32), cdiv_u(nq, 32)), tb, 0, s->stream, n, nq, k, Qs, B, m.perm);
+    launch(to_nodemajor_kernel<V64, V64>, dim3(cdiv_u(n, 32), cdiv_u(nm, 32)), tb, 0, s->stream, n, nm, k, Ms, B + nq,
+           m.perm);
+    TG_CUDA(cudaMemsetAsync(X, 0, kb, s->stream));
+    ColState* co = (ColState*)s->cs_outer.ensure(sizeof(ColState) * k);
+    solve_nm<V64, V32>(s, k, B, X, co);
+    if (res) read_results(s, k, co, res);
     V64* ylin = (V64*)s->fp_lin.ensure((size_t)std::max(nqm, 1) * sizeof(V64));
     V64* ylog = (V64*)s->fp_log.ensure((size_t)std::max(nqm, 1) * sizeof(V64));
-    project_nm<V64>(s, Xq, nq, nm, Ms, L, ylin, ylog);
+    project_nm<V64>(s, X, k, nm, Ms, L, ylin, ylog);
     if (J) {
         size_t jbytes = (size_t)2 * nqm * (vt<V64>::cplx ? 2 * n : n) * (j_fp32 ? 4 : 8);
         void* Jd = mem == TG_MEM_DEVICE ? J : s->jout.ensure(jbytes);
-        jacobian_nm<V64, V32>(s, nq, Xq, nm, Xm, L, ylin, Jd, j_fp32);
+        jacobian_nm<V64, V32>(s, nq, X, k, nm, X + nq, k, L, ylin, Jd, j_fp32);
         if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(J, Jd, jbytes, cudaMemcpyDeviceToHost, s->stream));
     }
-    auto out_field = [&](double* dst, const V64* src_nm, int k, DBuf& stage) {
+    auto out_field = [&](double* dst, const V64* src_nm, int kk, DBuf& stage) {
         if (!dst) return;
-        size_t b = (size_t)k * n * sizeof(V64);
+        size_t b = (size_t)kk * n * sizeof(V64);
         V64* o = mem == TG_MEM_DEVICE ? (V64*)dst : (V64*)stage.ensure(b);
-        nm_to_src(s, n, k, src_nm, o);
+        launch(to_srcmajor_kernel<V64, V64>, dim3(cdiv_u(n, 32), cdiv_u(kk, 32)), tb, 0, s->stream, n, kk, k, src_nm, o,
+               m.perm);
         if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(dst, o, b, cudaMemcpyDeviceToHost, s->stream));
     };
-    out_field(dphi, Xq, nq, s->io_a);
-    out_field(aphi, Xm, nm, s->io_b);
+    out_field(dphi, X, nq, s->io_a);
+    out_field(aphi, X + nq, nm, s->io_b);
     auto out_small = [&](double* dst, const V64* src) {
         if (!dst) return;
         TG_CUDA(cudaMemcpyAsync(dst, src, (size_t)nqm * sizeof(V64),
@@ -745,8 +908,8 @@ int tg_mesh_info(tg_mesh mesh, int* n, int* ne, int* nnz, int* nbnd, int* nlev_f
     if (ne) *ne = d.ne;
     if (nnz) *nnz = d.nnz;
     if (nbnd) { int c = 0; for (unsigned char b : mesh->m->h.bndnode) c += b; *nbnd = c; }
-    if (nlev_fwd) *nlev_fwd = d.nlev_fwd;
-    if (nlev_bwd) *nlev_bwd = d.nlev_bwd;
+    if (nlev_fwd) *nlev_fwd = d.ic[0].nlev_fwd;
+    if (nlev_bwd) *nlev_bwd = d.ic[0].nlev_bwd;
     API_END
 }
 
@@ -856,10 +1019,15 @@ int tg_solver_matrix(tg_solver s, double* val, int mem)
     API_BEGIN
     TG_CHECK(s && val, TG_ERR_ARG, "NULL argument");
     TG_CHECK(s->reset_done, TG_ERR_STATE, "tg_solver_reset has not been called");
-    size_t b = (size_t)s->mesh->d.nnz * vsize(s->cplx, false);
-    TG_CUDA(cudaMemcpyAsync(val, s->val64.p, b, mem == TG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                            s->stream));
+    const MeshHost& h = s->mesh->h;
+    size_t nnz = (size_t)s->mesh->d.nnz, w = s->cplx ? 2 : 1;
+    std::vector<double> lay(nnz * w), nat(nnz * w);
+    TG_CUDA(cudaMemcpyAsync(lay.data(), s->val64.p, nnz * w * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     TG_CUDA(cudaStreamSynchronize(s->stream));
+    for (size_t e = 0; e < nnz; e++)  // layout entry -> natural CSR entry
+        for (size_t c = 0; c < w; c++) nat[(size_t)h.lay2nat[e] * w + c] = lay[e * w + c];
+    TG_CUDA(cudaMemcpy(val, nat.data(), nnz * w * sizeof(double),
+                       mem == TG_MEM_DEVICE ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost));
     API_END
 }
 
@@ -923,6 +1091,18 @@ int tg_forward_path(tg_solver s, const double* cmua, const double* ckappa, const
     else
         api_forward_path<double, float>(s, cmua, ckappa, c2a, omega, nq, qvec, nm, mvec, L, dphi, aphi, proj, logproj,
                                         J, j_fp32, mem, res);
+    API_END
+}
+
+int tg_solver_set_refinement(tg_solver s, double inner_tol, int max_outer, int inner_ordering)
+{
+    API_BEGIN
+    TG_CHECK(s && inner_tol > 0 && inner_tol < 1 && max_outer > 0 && (inner_ordering == 0 || inner_ordering == 1),
+             TG_ERR_ARG, "invalid argument");
+    s->inner_tol = inner_tol;
+    s->max_outer = max_outer;
+    s->inner_colour = inner_ordering;
+    s->reset_done = false;  // the factorisation ordering may change
     API_END
 }
 
