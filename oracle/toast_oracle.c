@@ -866,8 +866,9 @@ static int bicgstab_real(const spmat *A, const zd *bz, zd *xz, double *tol, cons
     return niter;
 }
 
-/* gmres (gmres_imp.hpp:39-230), restart 20 (gsmatrix_imp.hpp:539), complex */
-static int gmres_cplx(const spmat *A, const zd *b, zd *x, double *elim, const precon_t *P, int restart, int maxit)
+/* gmres (gmres_imp.hpp:39-230), restart 20 (gsmatrix_imp.hpp:539).  Complex
+   arithmetic throughout; for a real system every imaginary part stays zero. */
+static int gmres_z(const spmat *A, const zd *b, zd *x, double *elim, const precon_t *P, int restart, int maxit)
 {
     int N = A->n, M = restart, MAXC = maxit ? maxit : N + 1;
     int j, k, l, cycle;
@@ -969,7 +970,7 @@ static void *solve_worker(void *arg)
         if (J->method == 0 && !J->A->cplx) it = pcg_real(J->A, b, x, &tol, J->P, J->maxit);
         else if (J->method == 1 && J->A->cplx) it = bicgstab_cplx(J->A, b, x, &tol, J->P, J->maxit, &fail);
         else if (J->method == 1) it = bicgstab_real(J->A, b, x, &tol, J->P, J->maxit);
-        else if (J->method == 2 && J->A->cplx) it = gmres_cplx(J->A, b, x, &tol, J->P, 20, J->maxit);
+        else if (J->method == 2) it = gmres_z(J->A, b, x, &tol, J->P, 20, J->maxit);
         else fail = 2;
         for (int i = 0; i < n; i++) {
             if (J->A->cplx) { J->X[2 * ((size_t)q * n + i)] = creal(x[i]); J->X[2 * ((size_t)q * n + i) + 1] = cimag(x[i]); }
@@ -981,7 +982,7 @@ static void *solve_worker(void *arg)
     return NULL;
 }
 
-/* method: 0 CG (real), 1 BiCGSTAB, 2 GMRES(20) (complex).  precon: 0 none,
+/* method: 0 CG (real), 1 BiCGSTAB, 2 GMRES(20).  precon: 0 none,
    1 diag, 2 IC(0).  B, X: nrhs x n (complex interleaved when cplx); X holds
    the initial guess on entry.  Returns 0, or the number of failed solves. */
 int tor_solve(int n, const int *rowptr, const int *colidx, const double *val, int cplx,

@@ -1,0 +1,101 @@
+"""Generates the golden fixtures of this directory by running the reference
+itself (oracle/_ref/ref_driver, compiled from the reference sources by
+oracle/Makefile.ref) on small seeded problems.
+
+Each fixture <name>.npz holds the problem (mesh, optodes, nodal parameters,
+solver settings) and the reference's outputs: linear and log projections
+(ProjectAll, DATA_LIN / DATA_LOG), the per-call iteration counts and, where
+asked, the nodal Jacobian of GenerateJacobian (toastmodule.cc CalcJacobian /
+CalcJacobianCW call sequence, LOG data).  The GPU parity tests and the oracle
+tests compare against these files, so they need neither the reference tree
+nor the compiled reference at run time.
+
+Usage:  make -f oracle/Makefile.ref REF=<reference tree> -j8
+        python tests/golden/make_golden.py
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from toastpp_gb300 import meshio, workloads  # noqa: E402
+
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+
+def small_cylinder(freq, nopt=4):
+    P = workloads.cylinder(rings=4, layers=6, seed=5, freq_mhz=freq)
+    idx = np.arange(0, 80, 80 // nopt)[:nopt]
+    P.qm = type(P.qm).all_to_all(P.qm.Q[idx] * 1.0, P.qm.M[idx] * 1.0)
+    return P
+
+
+# name -> (problem factory, solver, precon, tol, Jacobian)
+FIXTURES = {
+    "disc_cw_cg_ich": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "ICH", 1e-12, True),
+    "disc_cw_cg_diag": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "DIAG", 1e-12, False),
+    "disc_cw_cg_none": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "NONE", 1e-12, False),
+    "disc_fd_bicgstab_ich": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-12, True),
+    "disc_fd_bicgstab_diag": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "DIAG", 1e-12, False),
+    "disc_fd_bicgstab_none": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "NONE", 1e-12, False),
+    "disc_fd_gmres_ich": (lambda: workloads.disc(8, 3, 100.0, 6), "GMRES", "ICH", 1e-12, False),
+    "disc_fd_gmres_diag": (lambda: workloads.disc(8, 3, 100.0, 6), "GMRES", "DIAG", 1e-12, False),
+    "disc_fd_gmres_none": (lambda: workloads.disc(8, 3, 100.0, 6), "GMRES", "NONE", 1e-12, False),
+    "cyl_cw_cg_ich": (lambda: small_cylinder(0.0), "CG", "ICH", 1e-12, True),
+    "cyl_fd_bicgstab_ich": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-12, True),
+    "cyl_fd_gmres_ich": (lambda: small_cylinder(100.0), "GMRES", "ICH", 1e-12, False),
+}
+
+
+def rd(path, dtype):
+    return np.fromfile(path, dtype=dtype)
+
+
+def run(name, factory, solver, precon, tol, jac):
+    P = factory()
+    cplx = P.complex
+    with tempfile.TemporaryDirectory() as td:
+        msh = os.path.join(td, "m.msh")
+        meshio.write_mesh(msh, P.coords, P.elems)
+        opt = os.path.join(td, "opt.bin")
+        with open(opt, "wb") as f:
+            np.array([P.dim, len(P.qm.Q), len(P.qm.M)], np.int32).tofile(f)
+            np.ascontiguousarray(P.qm.Q, np.float64).tofile(f)
+            np.ascontiguousarray(P.qm.M, np.float64).tofile(f)
+        par = os.path.join(td, "par.bin")
+        np.stack([P.mua, P.mus, P.nref], axis=1).astype(np.float64).tofile(par)
+        out = os.path.join(td, "r")
+        args = [DRIVER, f"mesh={msh}", f"optodes={opt}", f"out={out}", f"params={par}",
+                f"dtype={'complex' if cplx else 'real'}", f"solver={solver}", f"precon={precon}", f"tol={tol}",
+                "maxit=0", f"freq={P.freq_mhz}", f"qwidth={P.qwidth}", f"mwidth={P.mwidth}", f"jac={int(jac)}"]
+        subprocess.run(args, check=True)
+        info = dict(l.split() for l in open(out + "_info.txt") if l.strip())
+        ct = np.complex128 if cplx else np.float64
+        res = dict(proj=rd(out + "_proj.bin", ct), logproj=rd(out + "_logproj.bin", ct),
+                   it_fwd=int(info["it_fwd"]), it_adj=int(info["it_adj"]))
+        if jac:
+            nqm = len(res["proj"])
+            J = rd(out + "_J.bin", np.float64)
+            res["J"] = J.reshape((2 * nqm, 2 * P.n) if cplx else (2 * nqm, P.n))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), coords=P.coords, elems=P.elems, Q=P.qm.Q, M=P.qm.M,
+                        link_ofs=P.qm.link_ofs, link_m=P.qm.link_m, mua=P.mua, mus=P.mus, nref=P.nref,
+                        freq_mhz=P.freq_mhz, qwidth=P.qwidth, mwidth=P.mwidth, solver=solver, precon=precon,
+                        tol=tol, **res)
+    print(name, "n", P.n, "links", len(res["proj"]), "its", res["it_fwd"], res["it_adj"])
+
+
+def main():
+    if not os.path.exists(DRIVER):
+        sys.exit("build the reference driver first: make -f oracle/Makefile.ref REF=<reference tree>")
+    for name, spec in FIXTURES.items():
+        run(name, *spec)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,22 @@
+"""Loading of the golden fixtures in tests/golden (outputs of the reference
+itself; see tests/golden/make_golden.py)."""
+import glob
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d = {k: z[k] for k in z.files}
+    for k in ("solver", "precon"):
+        d[k] = str(d[k])
+    for k in ("freq_mhz", "qwidth", "mwidth", "tol"):
+        d[k] = float(d[k])
+    return d

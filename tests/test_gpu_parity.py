@@ -61,6 +61,62 @@ def test_solve_fp64(case, oracle_mod, precon):
     assert np.all(np.abs(gits - its) <= 2), (gits, its)
 
 
+@pytest.mark.parametrize("precon", ["ICH", "DIAG", "NONE"])
+def test_solve_gmres(case, oracle_mod, precon):
+    """GMRES(20) (gmres_imp.hpp:39-230) per right-hand side against the oracle:
+    same fields and the same number of restart cycles."""
+    P, om, gm = case
+    cm, ck, ca, qvec, mvec = gpu_problem_inputs(P, gm)
+    omega = capi.omega_of(P.freq_mhz)
+    s = capi.FwdSolver(gm, "GMRES", 1e-12, precon, P.complex)
+    s.reset(cm, ck, ca, omega)
+    phi, res = s.calc_fields(qvec)
+    val = om.assemble(cm, ck, ca, omega, P.complex)
+    Xr, its, errs = oracle_mod.solve(om.rowptr, om.colidx, val, qvec.astype(phi.dtype), "GMRES", precon, 1e-12)
+    assert rel2(phi, Xr) < 1e-9
+    assert all(r[1] == 0 for r in res), res
+    gits = np.array([r[0] for r in res])
+    assert np.all(np.abs(gits - its) <= 1), (gits, its)
+    gerr = np.array([r[2] for r in res])
+    assert np.all(gerr <= 1e-12) and np.all(errs <= 1e-12)
+
+
+@pytest.mark.parametrize("freq", [0.0, 100.0])
+@pytest.mark.parametrize("precon", ["ICH", "DIAG", "NONE"])
+def test_solve_gmres_restarts(oracle_mod, freq, precon):
+    """A 1801-node disc on which GMRES(20) needs several restart cycles."""
+    from toastpp_gb300 import workloads
+    P = workloads.disc(24, 7, freq, 8)
+    om = oracle_mod.Mesh(P.coords, P.elems)
+    gm = capi.Mesh(P.coords, P.elems)
+    cm, ck, ca, qvec, mvec = gpu_problem_inputs(P, gm)
+    omega = capi.omega_of(P.freq_mhz)
+    s = capi.FwdSolver(gm, "GMRES", 1e-12, precon, P.complex)
+    s.reset(cm, ck, ca, omega)
+    phi, res = s.calc_fields(qvec)
+    val = om.assemble(cm, ck, ca, omega, P.complex)
+    Xr, its, errs = oracle_mod.solve(om.rowptr, om.colidx, val, qvec.astype(phi.dtype), "GMRES", precon, 1e-12)
+    assert rel2(phi, Xr) < 1e-9
+    gits = np.array([r[0] for r in res])
+    assert np.all(np.abs(gits - its) <= 1), (gits, its)
+    assert np.mean(gits == its) >= 0.75, (gits, its)
+
+
+@pytest.mark.parametrize("method", ["BICGSTAB", "GMRES"])
+def test_calc_fields_mixed(case, oracle_mod, method):
+    """FP32 inner solves inside FP64 refinement reach the FP64 oracle's fields."""
+    P, om, gm = case
+    cm, ck, ca, qvec, mvec = gpu_problem_inputs(P, gm)
+    omega = capi.omega_of(P.freq_mhz)
+    s = capi.FwdSolver(gm, method, 1e-12, "ICH", P.complex, precision="mixed")
+    s.reset(cm, ck, ca, omega)
+    phi, res = s.calc_fields(qvec)
+    val = om.assemble(cm, ck, ca, omega, P.complex)
+    Xr, its, errs = oracle_mod.solve(om.rowptr, om.colidx, val, qvec.astype(phi.dtype), method, "ICH", 1e-13)
+    assert rel2(phi, Xr) < 1e-10
+    assert all(r[1] == 0 for r in res), res
+
+
 def test_project_and_jacobian(case, oracle_mod):
     P, om, gm = case
     cm, ck, ca, qvec, mvec = gpu_problem_inputs(P, gm)

@@ -1,0 +1,28 @@
+"""The oracle against the committed golden fixtures (outputs of the compiled
+reference on small seeded problems, tests/golden/make_golden.py): projections
+and, where stored, the nodal Jacobian -- the Jacobian has no golden vectors in
+the reference's own test data, so these fixtures are what pin it."""
+import numpy as np
+import pytest
+
+from tests.golden_util import load, names
+from tests.gpu_util import rel2, relmax
+
+
+@pytest.mark.parametrize("name", names())
+def test_oracle_matches_reference_fixture(oracle_mod, name):
+    g = load(name)
+    mesh = oracle_mod.Mesh(g["coords"], g["elems"])
+    res = oracle_mod.forward_path(mesh, g["Q"], g["M"], g["link_ofs"], g["link_m"], g["mua"], g["mus"], g["nref"],
+                                  freq_mhz=g["freq_mhz"], qwidth=g["qwidth"], mwidth=g["mwidth"], method=g["solver"],
+                                  precon=g["precon"], tol=g["tol"], jac="J" in g)
+    # both solve to |r|/|b| <= 1e-12 with the same algorithm; the elementwise
+    # bound is the reference's own cmpvec tolerance for these outputs
+    assert relmax(res.proj, g["proj"]) < 1e-8
+    assert rel2(res.proj, g["proj"]) < 1e-10
+    assert relmax(res.logproj.real, g["logproj"].real) < 1e-8
+    if np.iscomplexobj(g["logproj"]):
+        assert relmax(res.logproj.imag, g["logproj"].imag) < 1e-7
+    if "J" in g:
+        J = res.J.reshape(g["J"].shape)
+        assert rel2(J, g["J"]) < 1e-9

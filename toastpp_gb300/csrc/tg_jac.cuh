@@ -96,12 +96,23 @@ __global__ void project_kernel(const int* __restrict__ nsup_p, const int* __rest
 // g = adjoint field, no conjugation).  J = -Re / -Im of PMDF (divided by the
 // linear projection for log data, PMDF_log 76-79).
 //
-// CTA: KT consecutive nodes (one per lane) x JM detectors, looping over the
-// sources in chunks of JQ.  Phase B builds Hm/Hk for the tile in shared
-// memory (thread = node x detector); phase C gives each lane JR_Q sources x
-// JR_M detectors of its node, so a warp writes KT consecutive J columns
-// (coalesced) for each of its pairs.
-constexpr int JM = 8, JQ = 8, JR_Q = 2, JR_M = 4;
+// Layout.  Tile = 32 consecutive (natural) nodes, one per lane.  Each node's
+// neighbours are "slots" (i, t) = i * 32 + t, i < D (the largest node degree):
+// slot (i, t) is the i-th entry of CSR row k0 + t, or padding.  All per-slot
+// arrays in shared memory are column-major [column][slot] with an odd column
+// stride SP, so a warp reading slot i of its 32 nodes touches 32 consecutive
+// words (no bank conflicts), and the writes of J along k are coalesced.
+//
+// The element integrals are gathered per node once per mesh (they depend on
+// the geometry only): Wm_k[i][j] = sum_{e ∋ k} IntFFF_e(k, a_i, a_j) and
+// Wk_k[i][j] = sum_{e ∋ k} IntFDD_e(a_i, a_j), stored tile-interleaved
+// W[((tile * D + i) * D + j) * 32 + t].  Then Hm_k[a_i, m] =
+// sum_j Wm_k[i][j] g_m(a_j) (and Hk likewise) is a small dense product.
+//
+// CTA = one tile x JM detectors; the sources are streamed in chunks of JQ
+// through two cp.async buffers (the next chunk loads while this one is used).
+// Phase C: lane = node, warp = JRQ x JRM (source, detector) pairs.
+constexpr int JKT = 32;
 
 template <class V>
 struct JacArgs {
@@ -113,6 +124,9 @@ struct JacArgs {
     const V* yinv;                // per link 1/y (log data) or null
     void* J;                      // output
     int out_fp32;
+    const typename vt<V>::R* Wm;  // per-node element weights (tile-interleaved)
+    const typename vt<V>::R* Wk;
+    int D, SP, nmc;               // slots per node, column stride, detector chunks
 };
 
 __device__ __forceinline__ double el_intfff(const MeshDev& m, const double* r, int i, int j, int l)
@@ -132,113 +146,173 @@ __device__ __forceinline__ double el_intfdd(const MeshDev& m, const double* r, i
     return r[1 + j * 4 + l];                                  // tet4.cc:380-412
 }
 
-template <class V, class OUT>
-__device__ __forceinline__ void jac_store(OUT* J, size_t idx, typename vt<V>::R v) { J[idx] = (OUT)v; }
+// per-node weights, FP64, into zeroed Wm/Wk; thread = node (its own slots only)
+static __global__ void jac_weights_kernel(MeshDev m, int D, double* __restrict__ Wm, double* __restrict__ Wk)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.n) return;
+    const size_t tb = (size_t)(k / JKT) * D * D * JKT + (k % JKT);
+    for (int p = m.nel_ptr[k]; p < m.nel_ptr[k + 1]; p++) {
+        const int code = m.nel_list[p], e = code >> 2, i = code & 3;
+        const unsigned pk = m.nel_pos[p];
+        const double* r = m.rec + (size_t)e * EL_REC;
+        for (int x = 0; x < m.nn; x++) {
+            const int px = (int)((pk >> (8 * x)) & 255u);
+            for (int y = 0; y < m.nn; y++) {
+                const int py = (int)((pk >> (8 * y)) & 255u);
+                const size_t o = tb + ((size_t)px * D + py) * JKT;
+                Wm[o] += el_intfff(m, r, i, x, y);
+                Wk[o] += el_intfdd(m, r, x, y);
+            }
+        }
+    }
+}
 
-template <class V, int KT>
+// asynchronous global -> shared copy of one value (LDGSTS), B = 4, 8 or 16 bytes
+template <int B>
+__device__ __forceinline__ void cp_async_val(void* dst, const void* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (B == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(src), "n"(B) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <class V, int JQ, int JM, int JRQ, int JRM>
 __global__ void __launch_bounds__(256) jacobian_kernel(JacArgs<V> a)
 {
     using S = typename vt<V>::R;
+    static_assert(JM <= JQ, "the adjoint block shares a source buffer");
     extern __shared__ __align__(16) unsigned char jsm[];
     const MeshDev& m = a.m;
-    const int k0 = blockIdx.x * KT;
-    const int m0 = blockIdx.y * JM;
-    const int kend = min(m.n, k0 + KT);
-    const int base = m.jrowptr[k0];
-    const int R = m.jrowptr[kend] - base;
-    V* Gs = (V*)jsm;                    // R x JM
-    V* Hm = Gs + (size_t)R * JM;        // R x JM
-    V* Hk = Hm + (size_t)R * JM;        // R x JM
-    V* Fs = Hk + (size_t)R * JM;        // R x JQ
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int e = tid; e < R * JM; e += nt) {
-        int rr = e / JM, mm = e % JM, mg = m0 + mm;
-        Gs[e] = mg < a.nm ? a.G[(size_t)m.jcolidx[base + rr] * a.ldg + mg] : vzero<V>();
-        Hm[e] = vzero<V>();
-        Hk[e] = vzero<V>();
+    const int SP = a.SP, D = a.D;
+    const int tile = blockIdx.x / a.nmc, m0 = (blockIdx.x % a.nmc) * JM;
+    const int k0 = tile * JKT;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    V* Hm = (V*)jsm;                          // [JM][SP]
+    V* Hk = Hm + (size_t)JM * SP;             // [JM][SP]
+    V* Fb = Hk + (size_t)JM * SP;             // 2 x [JQ][SP]
+    V* yis = Fb + (size_t)2 * JQ * SP;             // [nq][JM]: 1 / y of the link (log data)
+    int* lidx = (int*)(yis + (size_t)a.nq * JM);   // [nq][JM]: link index or -1
+    int* sidx = lidx + (size_t)a.nq * JM;          // [D * 32]: field row of each slot, -1 padding
+    const int k = k0 + lane;
+    const bool kin = k < m.n;
+    const int deg = kin ? m.jrowptr[k + 1] - m.jrowptr[k] : 0;
+    const int dmax = __reduce_max_sync(0xffffffffu, deg);
+    const int nslot = dmax * JKT;
+    for (int s = tid; s < nslot; s += blockDim.x) {
+        const int i = s / JKT, kk = k0 + s % JKT;
+        int r = -1;
+        if (kk < m.n) {
+            const int b = m.jrowptr[kk];
+            if (i < m.jrowptr[kk + 1] - b) r = m.jcolidx[b + i];
+        }
+        sidx[s] = r;
+    }
+    for (int e = tid; e < a.nq * JM; e += blockDim.x) {
+        const int q = e / JM, mg = m0 + e % JM;
+        const int l = mg < a.nm ? a.pairidx[(size_t)q * a.nm + mg] : -1;
+        lidx[e] = l;
+        if (a.yinv) yis[e] = l >= 0 ? a.yinv[l] : vzero<V>();
     }
     __syncthreads();
-    // Phase B: Hm/Hk rows of every node of the tile; thread = (node, detector).
-    // The IntFFF weights of P1 elements are size/D x {6 all equal, 2 two equal,
-    // 1 distinct} (D = 60 triangles, 120 tetrahedra), so for the element node
-    // i = k:  sum_l IntFFF(i,j,l) g_l = size/D (2 SG + 4 g_i) for j = i and
-    // size/D (SG + g_i + g_j) otherwise, SG = sum of g over the element.
-    for (int w = tid; w < KT * JM; w += nt) {
-        int t = w / JM, mm = w % JM, k = k0 + t;
-        if (k >= kend) continue;
-        const int rk = m.jrowptr[k] - base;
-        const S inv_d = (S)(m.dim == 2 ? 1.0 / 60.0 : 1.0 / 120.0);
-        for (int p = m.nel_ptr[k]; p < m.nel_ptr[k + 1]; p++) {
-            const int code = m.nel_list[p];
-            const int e = code >> 2, i = code & 3;
-            const unsigned pk = m.nel_pos[p];
-            const double* r = m.rec + (size_t)e * EL_REC;
-            int pos[4];
-            V g[4];
-            V sg = vzero<V>();
-            for (int j = 0; j < m.nn; j++) {
-                pos[j] = rk + (int)((pk >> (8 * j)) & 255u);
-                g[j] = Gs[pos[j] * JM + mm];
-                sg = vadd(sg, g[j]);
+    auto load_chunk = [&](int q0, V* Fs) {
+        for (int e = tid; e < JQ * nslot; e += blockDim.x) {
+            const int c = e % JQ, s = e / JQ, r = sidx[s];
+            V* dst = Fs + (size_t)c * SP + s;
+            if (r >= 0 && q0 + c < a.nq) cp_async_val<sizeof(V)>(dst, a.F + (size_t)r * a.ldf + q0 + c);
+            else *dst = vzero<V>();
+        }
+        cp_async_commit();
+    };
+    load_chunk(0, Fb);
+    // adjoint fields of the slots into the second buffer
+    V* Gs = Fb + (size_t)JQ * SP;
+    for (int e = tid; e < JM * nslot; e += blockDim.x) {
+        const int mm = e % JM, s = e / JM, r = sidx[s], mg = m0 + mm;
+        Gs[(size_t)mm * SP + s] = (r >= 0 && mg < a.nm) ? a.G[(size_t)r * a.ldg + mg] : vzero<V>();
+    }
+    __syncthreads();
+    // Phase B: H[mm][slot(i, t)] = sum_j W_t[i][j] Gs[mm][slot(j, t)].  Warp =
+    // rows i; each weight is loaded once (coalesced over the tile's nodes) and
+    // used for every detector of the block.
+    {
+        const size_t tb = (size_t)tile * D * D * JKT + lane;
+        for (int i = warp; i < dmax; i += blockDim.x / 32) {
+            V hm[JM], hk[JM];
+#pragma unroll
+            for (int mm = 0; mm < JM; mm++) { hm[mm] = vzero<V>(); hk[mm] = vzero<V>(); }
+            const S* wm = a.Wm + tb + (size_t)i * D * JKT;
+            const S* wk = a.Wk + tb + (size_t)i * D * JKT;
+#pragma unroll 4
+            for (int j = 0; j < dmax; j++) {
+                const S xm = wm[(size_t)j * JKT], xk = wk[(size_t)j * JKT];
+#pragma unroll
+                for (int mm = 0; mm < JM; mm++) {
+                    const V g = Gs[(size_t)mm * SP + j * JKT + lane];
+                    hm[mm] = vadd(hm[mm], vscale(g, xm));
+                    hk[mm] = vadd(hk[mm], vscale(g, xk));
+                }
             }
-            const S cf = (S)r[0] * inv_d;
-            for (int j = 0; j < m.nn; j++) {
-                V wm = j == i ? vadd(vscale(sg, (S)2), vscale(g[i], (S)4)) : vadd(vadd(sg, g[i]), g[j]);
-                V hk = vzero<V>();
-                for (int l = 0; l < m.nn; l++) hk = vadd(hk, vscale(g[l], (S)el_intfdd(m, r, j, l)));
-                Hm[pos[j] * JM + mm] = vadd(Hm[pos[j] * JM + mm], vscale(wm, cf));
-                Hk[pos[j] * JM + mm] = vadd(Hk[pos[j] * JM + mm], hk);
+#pragma unroll
+            for (int mm = 0; mm < JM; mm++) {
+                Hm[(size_t)mm * SP + i * JKT + lane] = hm[mm];
+                Hk[(size_t)mm * SP + i * JKT + lane] = hk[mm];
             }
         }
     }
     __syncthreads();
-    // Phase C: lane = node of the tile; warp = a group of JR_Q x JR_M pairs
-    const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-    const int t = lane, k = k0 + t;
-    const bool kin = (t < KT) && (k < kend);
-    const int rb = kin ? m.jrowptr[k] - base : 0, re2 = kin ? m.jrowptr[k + 1] - base : 0;
     const int n = m.n;
-    constexpr int GQ = JQ / JR_Q, GM = JM / JR_M;  // pair groups per chunk
-    for (int q0 = 0; q0 < a.nq; q0 += JQ) {
-        for (int e = tid; e < R * JQ; e += nt) {
-            int rr = e / JQ, c = e % JQ;
-            Fs[e] = (q0 + c) < a.nq ? a.F[(size_t)m.jcolidx[base + rr] * a.ldf + q0 + c] : vzero<V>();
+    constexpr int GM = JM / JRM, NG = (JQ / JRQ) * GM;
+    const int nch = (a.nq + JQ - 1) / JQ;
+    for (int ch = 0; ch < nch; ch++) {
+        if (ch + 1 < nch) {
+            load_chunk((ch + 1) * JQ, Fb + (size_t)((ch + 1) & 1) * JQ * SP);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
         __syncthreads();
-        for (int grp = warp; grp < GQ * GM; grp += nwarp) {
-            int qq0 = (grp / GM) * JR_Q, mm0 = (grp % GM) * JR_M;
-            V am[JR_Q][JR_M], ak[JR_Q][JR_M];
+        const V* Fs = Fb + (size_t)(ch & 1) * JQ * SP;
+        const int q0 = ch * JQ;
+        for (int grp = warp; grp < NG; grp += blockDim.x / 32) {
+            const int qq0 = (grp / GM) * JRQ, mm0 = (grp % GM) * JRM;
+            V am[JRQ][JRM], ak[JRQ][JRM];
 #pragma unroll
-            for (int a1 = 0; a1 < JR_Q; a1++)
+            for (int x = 0; x < JRQ; x++)
 #pragma unroll
-                for (int b1 = 0; b1 < JR_M; b1++) { am[a1][b1] = vzero<V>(); ak[a1][b1] = vzero<V>(); }
-            for (int rr = rb; rr < re2; rr++) {
-                V f[JR_Q], hm[JR_M], hk[JR_M];
+                for (int y = 0; y < JRM; y++) { am[x][y] = vzero<V>(); ak[x][y] = vzero<V>(); }
+#pragma unroll 2
+            for (int i = 0; i < dmax; i++) {
+                const int s = i * JKT + lane;
+                V f[JRQ], hm[JRM], hk[JRM];
 #pragma unroll
-                for (int a1 = 0; a1 < JR_Q; a1++) f[a1] = Fs[rr * JQ + qq0 + a1];
+                for (int x = 0; x < JRQ; x++) f[x] = Fs[(size_t)(qq0 + x) * SP + s];
 #pragma unroll
-                for (int b1 = 0; b1 < JR_M; b1++) { hm[b1] = Hm[rr * JM + mm0 + b1]; hk[b1] = Hk[rr * JM + mm0 + b1]; }
+                for (int y = 0; y < JRM; y++) { hm[y] = Hm[(size_t)(mm0 + y) * SP + s]; hk[y] = Hk[(size_t)(mm0 + y) * SP + s]; }
 #pragma unroll
-                for (int a1 = 0; a1 < JR_Q; a1++)
+                for (int x = 0; x < JRQ; x++)
 #pragma unroll
-                    for (int b1 = 0; b1 < JR_M; b1++) {
-                        am[a1][b1] = vfma(am[a1][b1], f[a1], hm[b1]);
-                        ak[a1][b1] = vfma(ak[a1][b1], f[a1], hk[b1]);
+                    for (int y = 0; y < JRM; y++) {
+                        am[x][y] = vfma(am[x][y], f[x], hm[y]);
+                        ak[x][y] = vfma(ak[x][y], f[x], hk[y]);
                     }
             }
             if (!kin) continue;
 #pragma unroll
-            for (int a1 = 0; a1 < JR_Q; a1++)
+            for (int x = 0; x < JRQ; x++)
 #pragma unroll
-                for (int b1 = 0; b1 < JR_M; b1++) {
-                    int q = q0 + qq0 + a1, mg = m0 + mm0 + b1;
+                for (int y = 0; y < JRM; y++) {
+                    const int q = q0 + qq0 + x, mg = m0 + mm0 + y;
                     if (q >= a.nq || mg >= a.nm) continue;
-                    int l = a.pairidx[(size_t)q * a.nm + mg];
+                    const int l = lidx[q * JM + mm0 + y];
                     if (l < 0) continue;
-                    V xm = am[a1][b1], xk = ak[a1][b1];
-                    if (a.yinv) { V yi = a.yinv[l]; xm = vmul(xm, yi); xk = vmul(xk, yi); }
+                    V xm = am[x][y], xk = ak[x][y];
+                    if (a.yinv) { const V yi = yis[q * JM + mm0 + y]; xm = vmul(xm, yi); xk = vmul(xk, yi); }
                     if constexpr (vt<V>::cplx) {
-                        size_t r0 = (size_t)l * 2 * n + k, r1 = (size_t)(l + a.nqm) * 2 * n + k;
+                        const size_t r0 = (size_t)l * 2 * n + k, r1 = (size_t)(l + a.nqm) * 2 * n + k;
                         if (a.out_fp32) {
                             float* J = (float*)a.J;
                             J[r0] = (float)-re(xm); J[r1] = (float)-im(xm);
@@ -249,7 +323,7 @@ __global__ void __launch_bounds__(256) jacobian_kernel(JacArgs<V> a)
                             J[r0 + n] = -re(xk); J[r1 + n] = -im(xk);
                         }
                     } else {
-                        size_t r0 = (size_t)l * n + k, r1 = (size_t)(l + a.nqm) * n + k;
+                        const size_t r0 = (size_t)l * n + k, r1 = (size_t)(l + a.nqm) * n + k;
                         if (a.out_fp32) {
                             float* J = (float*)a.J;
                             J[r0] = (float)-xm; J[r1] = (float)-xk;

@@ -1,6 +1,7 @@
 // tg_solver.cu -- forward solver object, batched Krylov engines and the C ABI.
 #include <algorithm>
 #include <atomic>
+#include <type_traits>
 #include <utility>
 #include <cstdarg>
 #include <cstring>
@@ -10,6 +11,7 @@
 
 #include "../../include/toastgpu.h"
 #include "tg_jac.cuh"
+#include "tg_gmres.cuh"
 
 namespace tg {
 
@@ -139,7 +141,7 @@ struct GraphCache {
         cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
         cudaGraphDestroy(g);
         TG_CUDA(e);
-        if (entries.size() >= 16) {
+        if (entries.size() >= 64) {
             cudaGraphExecDestroy(entries.front().exec);
             entries.erase(entries.begin());
         }
@@ -166,7 +168,7 @@ struct Engine {
     int ico = 0;               // IC ordering: 0 natural, 1 colour-major
     int precon = 0;            // 0 none, 1 diag, 2 ich
     Profiler* prof = nullptr;
-    DBuf w[9], part, cs, cnt;
+    DBuf w[9], part, cs, cnt, gbasis, gcol;
     int* h_cnt = nullptr;
     GraphCache graphs;
 
@@ -281,6 +283,10 @@ struct Engine {
     // B, X: device node-major n x k.  cst: per-column state with tol/maxit set.
     void solve(int method, int k, const V* B, V* X, ColState* cst, bool zero_guess)
     {
+        if (method == TG_SOLVER_GMRES) {
+            gmres(k, B, X, cst, zero_guess);
+            return;
+        }
         const MeshDev& m = mesh->d;
         size_t nk = (size_t)m.n * k;
         unsigned eg = cdiv_u(nk, 256);
@@ -305,6 +311,101 @@ struct Engine {
         if (method == TG_SOLVER_BICGSTAB) bicgstab(k, X, cst, maxit);
         else if (method == TG_SOLVER_CG) pcg(k, X, cst, maxit);
         else throw Error{TG_ERR_UNSUPPORTED, "solver method not implemented on the GPU"};
+    }
+
+    // out = M^-1 in (ICH, Diag or copy), as TPreconditioner::Apply
+    void precon_apply(int k, const V* in, V* out, const ColState* cst)
+    {
+        const MeshDev& m = mesh->d;
+        if (precon == 2) ic_apply(k, in, out, cst);
+        else launch(scale_diag_kernel<V>, cdiv_u((size_t)m.n * k, 256), 256, 0, st, m.n, k, k, in, idiag, out, precon);
+    }
+
+    using W = typename std::conditional<vt<V>::cplx, cd, double>::type;
+
+    int gm_count(int k, const ColState* cst, const GmCol<W>* g)
+    {
+        if (!h_cnt) TG_CUDA(cudaMallocHost(&h_cnt, sizeof(int)));
+        int* dc = (int*)cnt.ensure(sizeof(int));
+        launch(gm_count_kernel<W>, 1, 256, 0, st, k, cst, g, dc);
+        TG_CUDA(cudaMemcpyAsync(h_cnt, dc, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TG_CUDA(cudaStreamSynchronize(st));
+        return *h_cnt;
+    }
+
+    // GMRES(20) per column (src/libmath/gmres_imp.hpp:39-230): the small
+    // Hessenberg systems and rotations live in GmCol (FP64), the basis
+    // vectors in one block of 21 node-major n x k vectors.
+    void gmres(int k, const V* B, V* X, ColState* cst, bool zero_guess)
+    {
+        const MeshDev& m = mesh->d;
+        const size_t nk = (size_t)m.n * k;
+        const unsigned eg = cdiv_u(nk, 256);
+        const int nt = ntiles();
+        V *Mb = vec(0, nk), *T = vec(1, nk), *Z = vec(2, nk);
+        V* basis = (V*)gbasis.ensure(nk * (GM_M + 1) * sizeof(V));
+        auto v = [&](int j) { return basis + (size_t)j * nk; };
+        GmCol<W>* g = (GmCol<W>*)gcol.ensure((size_t)k * sizeof(GmCol<W>));
+        double* pt = parts(k, 2);
+        int maxc = 0;
+        {
+            ColState h;
+            TG_CUDA(cudaMemcpyAsync(&h, cst, sizeof(ColState), cudaMemcpyDeviceToHost, st));
+            TG_CUDA(cudaStreamSynchronize(st));
+            maxc = h.maxit;
+        }
+        auto mgs = [&](int need_inner, int jj, int kprev, V* w, const V* vprev, const V* vk) {
+            launch(gm_mgs_kernel<V, W>, nt, rowblk(k), 0, st, m.n, k, k, cst, g, need_inner, jj, kprev, w, vprev, vk,
+                   pt, nt);
+        };
+        auto reduce = [&](int phase, int jj, int kk) {
+            launch(gm_reduce_kernel<W>, k, 256, 0, st, k, nt, pt, cst, g, phase, jj, kk, (double)m.n);
+        };
+        // r = M b - M A x, or M b where |x| < elim N (gmres_imp.hpp:67-92)
+        auto residual = [&](int first) {
+            spmm(k, X, T, nullptr, false, nullptr, nullptr, 0);
+            precon_apply(k, T, Z, cst);
+            launch(gm_resid_kernel<V, W>, eg, 256, 0, st, m.n, k, k, cst, g, first, Mb, Z, v(0));
+        };
+        launch(gm_init_kernel<W>, cdiv_u(k, 128), 128, 0, st, k, g, maxc);
+        precon_apply(k, B, Mb, cst);
+        mgs(0, 0, 0, Mb, nullptr, nullptr);
+        reduce(GM_NORMB, 0, 0);
+        if (zero_guess) {
+            TG_CUDA(cudaMemcpyAsync(v(0), Mb, nk * sizeof(V), cudaMemcpyDeviceToDevice, st));
+        } else {
+            mgs(0, 0, 0, X, nullptr, nullptr);
+            reduce(GM_NORMX, 0, 0);
+            residual(1);
+        }
+        for (;;) {
+            mgs(0, 0, 0, v(0), nullptr, nullptr);
+            reduce(GM_OUTER, 0, 0);
+            if (count_active(k, cst) == 0) break;
+            launch(gm_scale_kernel<V, W>, eg, 256, 0, st, m.n, k, k, cst, g, 0, 0, v(0));
+            for (int j = 0; j < GM_M; j++) {
+                if ((j & 3) == 0 && gm_count(k, cst, g) == 0) break;
+                V* w = v(j + 1);
+                if (precon) {
+                    spmm(k, v(j), T, nullptr, false, nullptr, nullptr, 0);
+                    precon_apply(k, T, w, cst);
+                } else {
+                    spmm(k, v(j), w, nullptr, false, nullptr, nullptr, 0);
+                }
+                // modified Gram-Schmidt: each pass subtracts the previous
+                // projection and forms the next inner product
+                for (int kk = 0; kk <= j; kk++) {
+                    mgs(1, j, kk - 1, w, kk ? v(kk - 1) : nullptr, v(kk));
+                    reduce(GM_H, j, kk);
+                }
+                mgs(1, j, j, w, v(j), nullptr);
+                reduce(GM_HNORM, j, 0);
+                launch(gm_scale_kernel<V, W>, eg, 256, 0, st, m.n, k, k, cst, g, 1, j, w);
+            }
+            launch(gm_solve_kernel<W>, cdiv_u(k, 64), 64, 0, st, k, cst, g);
+            launch(gm_update_kernel<V, W>, eg, 256, 0, st, m.n, k, k, cst, g, basis, nk, X);
+            residual(0);
+        }
     }
 
     void bicgstab(int k, V* X, ColState* cst, int maxit)
@@ -446,6 +547,8 @@ struct tg_solver_s {
     DBuf B, X, X32, B32, cs_outer, cs_inner, io_a, io_b, tmp, jout;
     DBuf jF, jG, jpair, jyinv, plink_q, plink_m, psup, pnsup, pflag, pMsup, plin, plog;
     DBuf fp_bq, fp_xq, fp_bm, fp_xm, fp_lin, fp_log;
+    DBuf jwm64, jwk64, jwm32, jwk32;  // per-node element weights of the Jacobian (geometry only)
+    int jw_D = 0, jw_ready = 0;       // slots per node; bit 0 FP64 weights built, bit 1 FP32
     Profiler prof;
     GraphCache graphs;
     std::mutex mu;
@@ -686,20 +789,55 @@ static void project_nm(tg_solver s, const V* X, int ldx, int nm, const V* mvec, 
     TG_CUDA(cudaGetLastError());
 }
 
-template <class VC, int KT>
-static bool try_launch_jacobian(tg_solver s, const JacArgs<VC>& a)
+// Per-node element weights for the Jacobian, built on the GPU at the first
+// Jacobian call of the solver (they depend on the mesh geometry only).
+template <class S>
+static const S* jac_weights(tg_solver s, int which)
 {
     const MeshDev& m = s->mesh->d;
-    // the largest CSR row span of a node tile sets the shared-memory size
-    const std::vector<int>& rp = s->mesh->h.rowptr;
-    int rmax = 0;
-    for (int k0 = 0; k0 < m.n; k0 += KT) rmax = std::max(rmax, rp[std::min(m.n, k0 + KT)] - rp[k0]);
-    size_t smem = (size_t)rmax * (3 * JM + JQ) * sizeof(VC);
-    if (smem > 200 * 1024) return false;
-    TG_CUDA(cudaFuncSetAttribute(jacobian_kernel<VC, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid(cdiv_u(m.n, KT), cdiv_u(a.nm, JM));
+    if (!s->jw_D) {
+        const std::vector<int>& rp = s->mesh->h.rowptr;
+        int D = 1;
+        for (int i = 0; i < m.n; i++) D = std::max(D, rp[i + 1] - rp[i]);
+        s->jw_D = D;
+    }
+    const size_t cnt = (size_t)cdiv_u(m.n, JKT) * s->jw_D * s->jw_D * JKT;
+    if (!(s->jw_ready & 1)) {
+        double* wm = (double*)s->jwm64.ensure(cnt * sizeof(double));
+        double* wk = (double*)s->jwk64.ensure(cnt * sizeof(double));
+        TG_CUDA(cudaMemsetAsync(wm, 0, cnt * sizeof(double), s->stream));
+        TG_CUDA(cudaMemsetAsync(wk, 0, cnt * sizeof(double), s->stream));
+        launch(jac_weights_kernel, cdiv_u(m.n, 128), 128, 0, s->stream, m, s->jw_D, wm, wk);
+        s->jw_ready |= 1;
+    }
+    if constexpr (std::is_same<S, float>::value) {
+        if (!(s->jw_ready & 2)) {
+            float* wm = (float*)s->jwm32.ensure(cnt * sizeof(float));
+            float* wk = (float*)s->jwk32.ensure(cnt * sizeof(float));
+            launch(cast_kernel<float, double>, cdiv_u(cnt, 256), 256, 0, s->stream, cnt, s->jwm64.as<double>(), wm);
+            launch(cast_kernel<float, double>, cdiv_u(cnt, 256), 256, 0, s->stream, cnt, s->jwk64.as<double>(), wk);
+            s->jw_ready |= 2;
+        }
+        return (const float*)(which ? s->jwk32.p : s->jwm32.p);
+    } else {
+        return (const double*)(which ? s->jwk64.p : s->jwm64.p);
+    }
+}
+
+template <class VC, int JQ, int JM, int JRQ, int JRM>
+static bool try_launch_jacobian(tg_solver s, JacArgs<VC> a)
+{
+    const MeshDev& m = s->mesh->d;
+    const int D = s->jw_D, SP = D * JKT + 1;
+    const size_t smem = (size_t)(2 * JM + 2 * JQ) * SP * sizeof(VC) + (size_t)a.nq * JM * (sizeof(VC) + sizeof(int)) +
+                        (size_t)D * JKT * sizeof(int);
+    if (smem > 227 * 1024) return false;
+    auto kern = jacobian_kernel<VC, JQ, JM, JRQ, JRM>;
+    TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    a.D = D; a.SP = SP; a.nmc = (int)cdiv_u(a.nm, JM);
+    const size_t nblk = (size_t)cdiv_u(m.n, JKT) * a.nmc;
     ProfScope ps(&s->prof, PC_JAC, s->stream);
-    launch(jacobian_kernel<VC, KT>, grid, 256, smem, s->stream, a);
+    launch(kern, (unsigned)nblk, 256, smem, s->stream, a);
     return true;
 }
 
@@ -707,14 +845,18 @@ template <class VC>
 static void launch_jacobian(tg_solver s, int nq, const VC* F, int ldf, int nm, const VC* G, int ldg,
                             const LinkHost& L, const VC* yinv, void* J, int out_fp32)
 {
+    using S = typename vt<VC>::R;
     upload_async(s, s->jpair, L.pair);
     JacArgs<VC> a;
     a.m = s->mesh->d; a.nq = nq; a.nm = nm; a.nqm = (int)L.q.size();
     a.F = F; a.ldf = ldf; a.G = G; a.ldg = ldg;
     a.pairidx = s->jpair.as<int>(); a.yinv = yinv; a.J = J; a.out_fp32 = out_fp32;
-    if (sizeof(VC) <= 8 && try_launch_jacobian<VC, 32>(s, a)) return;
-    if (try_launch_jacobian<VC, 16>(s, a)) return;
-    if (try_launch_jacobian<VC, 8>(s, a)) return;
+    a.Wm = jac_weights<S>(s, 0);
+    a.Wk = jac_weights<S>(s, 1);
+    if constexpr (sizeof(VC) <= 8)
+        if (try_launch_jacobian<VC, 8, 8, 2, 4>(s, a)) return;
+    if (try_launch_jacobian<VC, 4, 4, 1, 2>(s, a)) return;
+    if (try_launch_jacobian<VC, 2, 2, 1, 1>(s, a)) return;
     throw Error{TG_ERR_UNSUPPORTED, "mesh node degree too high for the Jacobian tile"};
 }
 
@@ -954,7 +1096,6 @@ int tg_solver_create(tg_mesh mesh, int is_complex, int method, int precon, doubl
     TG_CHECK(precision == TG_PREC_FP64 || precision == TG_PREC_MIXED, TG_ERR_ARG, "unknown precision");
     TG_CHECK(tol > 0, TG_ERR_ARG, "tolerance must be positive");
     TG_CHECK(maxit >= 0, TG_ERR_ARG, "maxit must be >= 0");
-    TG_CHECK(method != TG_SOLVER_GMRES, TG_ERR_UNSUPPORTED, "GMRES is not implemented on the GPU yet");
     TG_CHECK(!(method == TG_SOLVER_CG && is_complex), TG_ERR_UNSUPPORTED, "CG is only implemented for real systems");
     auto s = std::make_unique<tg_solver_s>();
     s->mesh = mesh->m.get();
