@@ -167,6 +167,60 @@ int tg_forward_path(tg_solver s, const double *cmua, const double *ckappa, const
 int tg_project_all_noalloc(tg_solver s, int nq, const double *phi, int nm, const double *mvec,
                            const int *link_ofs, const int *link_m, int scale, double *proj);
 
+/* ---- request server (no counterpart in the reference: its CalcFields is not
+   re-entrant, one request per process at a time, fwdsolver.cc:658-731) ------
+   Whole requests -- Reset, CalcFields of sources and detectors, ProjectAll
+   (LIN and LOG) and optionally the Jacobian -- are submitted from any host
+   thread and admitted in arrival order while one of `slots` is free and the
+   estimated device working sets of the requests on the device fit in
+   hbm_budget_gb (a request larger than the budget runs alone).  Admitted
+   requests run concurrently, each on its slot's CUDA stream; each slot keeps
+   its solvers resident per (mesh, settings).  Results do not depend on the
+   other requests on the device (every reduction has a fixed order).
+   All request buffers are host memory owned by the caller until tg_wait
+   returns; outputs as tg_forward_path (proj, logproj: nQM values, complex
+   interleaved for complex requests; J optional; res: nq + nm entries or NULL). */
+typedef struct tg_server_s *tg_server;
+
+typedef struct {
+    tg_mesh mesh;
+    int is_complex;                 /* 1: frequency domain (omega > 0 allowed), 0: CW */
+    int method, precon, precision;  /* TG_SOLVER_*, TG_PRECON_*, TG_PREC_* */
+    double tol;
+    int maxit;
+    const double *cmua, *ckappa, *c2a;   /* nodal, length n */
+    double omega;                   /* rad/ps */
+    int nq;
+    const double *qvec;             /* nq x n, source-major */
+    int nm;
+    const double *mvec;             /* nm x n */
+    const int *link_ofs, *link_m;   /* QMMesh link list */
+    double *proj, *logproj;         /* outputs */
+    void *J;                        /* output or NULL (no Jacobian) */
+    int j_fp32;
+    tg_result *res;
+} tg_request;
+
+#define TG_REQ_QUEUED 0
+#define TG_REQ_RUNNING 1
+#define TG_REQ_DONE 2
+#define TG_REQ_FAILED 3
+
+int tg_server_create(int slots, double hbm_budget_gb, tg_server *out);
+/* waits for every submitted request, then stops the slot threads */
+int tg_server_destroy(tg_server server);
+int tg_submit(tg_server server, const tg_request *req, long long *ticket);
+/* state: TG_REQ_QUEUED / RUNNING / DONE / FAILED */
+int tg_poll(tg_server server, long long ticket, int *state);
+/* blocks until the request has finished; returns its status code; latency =
+   submission to completion.  The ticket is released. */
+int tg_wait(tg_server server, long long ticket, double *latency_ms);
+/* completed / failed requests, source solves (nq + nm per request), p50 / p99
+   latency of the completed requests, seconds since creation or the last reset */
+int tg_server_stats(tg_server server, long long *completed, long long *failed, long long *solves,
+                    double *p50_ms, double *p99_ms, double *elapsed_s);
+int tg_server_reset_stats(tg_server server);
+
 /* ---- measurement (no counterpart in the reference: its timing is
    tic/toc/walltic around calls, src/libmath/timing.h:4-20) ----------------- */
 /* kernel classes for tg_solver_profile's mask (bit = 1 << class) */

@@ -38,18 +38,18 @@ def small_cylinder(freq, nopt=4):
 
 # name -> (problem factory, solver, precon, tol, Jacobian)
 FIXTURES = {
-    "disc_cw_cg_ich": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "ICH", 1e-12, True),
-    "disc_cw_cg_diag": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "DIAG", 1e-12, False),
-    "disc_cw_cg_none": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "NONE", 1e-12, False),
-    "disc_fd_bicgstab_ich": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-12, True),
-    "disc_fd_bicgstab_diag": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "DIAG", 1e-12, False),
-    "disc_fd_bicgstab_none": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "NONE", 1e-12, False),
-    "disc_fd_gmres_ich": (lambda: workloads.disc(8, 3, 100.0, 6), "GMRES", "ICH", 1e-12, False),
-    "disc_fd_gmres_diag": (lambda: workloads.disc(8, 3, 100.0, 6), "GMRES", "DIAG", 1e-12, False),
-    "disc_fd_gmres_none": (lambda: workloads.disc(8, 3, 100.0, 6), "GMRES", "NONE", 1e-12, False),
-    "cyl_cw_cg_ich": (lambda: small_cylinder(0.0), "CG", "ICH", 1e-12, True),
-    "cyl_fd_bicgstab_ich": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-12, True),
-    "cyl_fd_gmres_ich": (lambda: small_cylinder(100.0), "GMRES", "ICH", 1e-12, False),
+    "disc_cw_cg_ich": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "ICH", 1e-15, True),
+    "disc_cw_cg_diag": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "DIAG", 1e-15, False),
+    "disc_cw_cg_none": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "NONE", 1e-15, False),
+    "disc_fd_bicgstab_ich": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, True),
+    "disc_fd_bicgstab_diag": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "DIAG", 1e-15, False),
+    "disc_fd_bicgstab_none": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "NONE", 1e-15, False),
+    "disc_fd_gmres_ich": (lambda: workloads.disc(8, 3, 100.0, 6), "GMRES", "ICH", 1e-15, False),
+    "disc_fd_gmres_diag": (lambda: workloads.disc(8, 3, 100.0, 6), "GMRES", "DIAG", 1e-15, False),
+    "disc_fd_gmres_none": (lambda: workloads.disc(8, 3, 100.0, 6), "GMRES", "NONE", 1e-15, False),
+    "cyl_cw_cg_ich": (lambda: small_cylinder(0.0), "CG", "ICH", 1e-15, True),
+    "cyl_fd_bicgstab_ich": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-15, True),
+    "cyl_fd_gmres_ich": (lambda: small_cylinder(100.0), "GMRES", "ICH", 1e-15, False),
 }
 
 

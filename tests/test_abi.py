@@ -53,3 +53,19 @@ def test_error_path_without_gpu(lib):
     rc = lib.tg_mesh_create(4, 0, None, 0, None, ctypes.byref(h))
     assert rc == 1  # TG_ERR_ARG
     assert lib.tg_last_error()
+
+
+def test_server_create_without_device_fails_cleanly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    lib.tg_server_create.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_void_p)]
+    assert lib.tg_server_create(2, 1.0, ctypes.byref(h)) == 3  # TG_ERR_CUDA
+    assert lib.tg_server_create(0, 1.0, ctypes.byref(h)) == 1  # TG_ERR_ARG
+
+
+def test_cpp_face_compiles_and_links(tmp_path):
+    """include/toastgpu.hpp builds into a caller and links against the library."""
+    from tests.cpp_shim import build
+    assert os.path.exists(build(str(tmp_path)))

@@ -1,0 +1,96 @@
+"""The request server: admission, concurrency on per-slot streams, and the
+invariance of every result to the other requests on the device."""
+import numpy as np
+import pytest
+
+from tests.gpu_util import small_cyl, small_disc
+from toastpp_gb300 import capi
+
+pytestmark = pytest.mark.gpu
+
+
+def make_problems():
+    return [small_disc(0.0), small_disc(100.0), small_cyl(100.0), small_cyl(0.0)]
+
+
+def make_request(P, gm, precision="mixed", solver=None):
+    cm, ck, ca = capi.optical_coefficients(P.mua, P.mus, P.nref)
+    q = gm.qvec_gaussian(P.qm.Q, P.qwidth)
+    m = gm.qvec_gaussian(P.qm.M, P.mwidth) * ca[None, :]
+    L = capi.Links(P.qm.link_ofs, P.qm.link_m)
+    return capi.Request(gm, cm, ck, ca, capi.omega_of(P.freq_mhz), q, m, L, solver=solver, tol=1e-12,
+                        precision=precision, want_jac=True, j_fp32=True)
+
+
+def outputs(r):
+    return r.proj.copy(), r.logproj.copy(), r.J.copy()
+
+
+def test_alone_equals_mix():
+    probs = make_problems()
+    meshes = [capi.Mesh(P.coords, P.elems) for P in probs]
+    # alone: one slot, one request at a time
+    alone = []
+    srv = capi.Server(slots=1, hbm_budget_gb=8.0)
+    for P, gm in zip(probs, meshes):
+        t = srv.submit(make_request(P, gm))
+        alone.append(outputs(srv.wait(t)))
+    srv.close()
+    # mix: every request three times, all submitted at once to four slots
+    srv = capi.Server(slots=4, hbm_budget_gb=8.0)
+    tickets = []
+    for rep in range(3):
+        for i, (P, gm) in enumerate(zip(probs, meshes)):
+            tickets.append((i, srv.submit(make_request(P, gm))))
+    for i, t in tickets:
+        got = outputs(srv.wait(t))
+        for a, b in zip(alone[i], got):
+            assert np.array_equal(a, b), f"request {i} differs in the mix"
+    st = srv.stats()
+    assert st["completed"] == len(tickets) and st["failed"] == 0
+    assert 0 < st["p50_ms"] <= st["p99_ms"]
+    srv.close()
+
+
+def test_server_matches_direct_call():
+    P = small_cyl(100.0)
+    gm = capi.Mesh(P.coords, P.elems)
+    srv = capi.Server(slots=2, hbm_budget_gb=8.0)
+    r = srv.wait(srv.submit(make_request(P, gm, precision="fp64")))
+    srv.close()
+    cm, ck, ca = capi.optical_coefficients(P.mua, P.mus, P.nref)
+    q = gm.qvec_gaussian(P.qm.Q, P.qwidth)
+    m = gm.qvec_gaussian(P.qm.M, P.mwidth) * ca[None, :]
+    s = capi.FwdSolver(gm, "BICGSTAB", 1e-12, "ICH", True, precision="fp64")
+    out = s.forward_path(cm, ck, ca, capi.omega_of(P.freq_mhz), q, m, capi.Links(P.qm.link_ofs, P.qm.link_m),
+                         want_fields=False, want_jac=True, j_fp32=True)
+    assert np.array_equal(out["proj"], r.proj) and np.array_equal(out["logproj"], r.logproj)
+    assert np.array_equal(out["J"], r.J)
+
+
+def test_budget_admission_serialises_but_completes():
+    probs = make_problems()
+    meshes = [capi.Mesh(P.coords, P.elems) for P in probs]
+    # a budget below any request: each runs alone, in arrival order
+    srv = capi.Server(slots=4, hbm_budget_gb=1e-6)
+    ts = [srv.submit(make_request(P, gm)) for P, gm in zip(probs, meshes)]
+    lat = [srv.wait(t).latency_ms for t in ts]
+    assert all(x > 0 for x in lat)
+    # arrival order is kept: each later request finished no earlier
+    assert srv.stats()["completed"] == len(ts)
+    srv.close()
+
+
+def test_failed_request_reports_error():
+    P = small_disc(100.0)
+    gm = capi.Mesh(P.coords, P.elems)
+    srv = capi.Server(slots=2, hbm_budget_gb=8.0)
+    bad = make_request(P, gm, solver="CG")  # CG is not defined for complex systems
+    t = srv.submit(bad)
+    with pytest.raises(capi.ToastGPUError):
+        srv.wait(t)
+    ok = srv.wait(srv.submit(make_request(P, gm)))
+    assert np.all(np.isfinite(ok.proj))
+    st = srv.stats()
+    assert st["failed"] == 1 and st["completed"] == 1
+    srv.close()

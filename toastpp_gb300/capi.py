@@ -27,7 +27,9 @@ EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "
            "tg_qvec_gaussian", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
            "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count",
-           "tg_last_error"]
+           "tg_server_create", "tg_server_destroy", "tg_submit", "tg_poll", "tg_wait", "tg_server_stats",
+           "tg_server_reset_stats", "tg_last_error"]
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
 PROF_SPMM, PROF_SWEEP, PROF_VEC, PROF_JAC, PROF_ASM, PROF_PROJ = range(6)
 
 
@@ -39,6 +41,16 @@ class ToastGPUError(RuntimeError):
 
 class TgResult(C.Structure):
     _fields_ = [("it_count", C.c_int), ("status", C.c_int), ("rel_err", C.c_double)]
+
+
+class TgRequest(C.Structure):
+    """tg_request (include/toastgpu.h)."""
+    _fields_ = [("mesh", C.c_void_p), ("is_complex", C.c_int), ("method", C.c_int), ("precon", C.c_int),
+                ("precision", C.c_int), ("tol", C.c_double), ("maxit", C.c_int), ("cmua", C.c_void_p),
+                ("ckappa", C.c_void_p), ("c2a", C.c_void_p), ("omega", C.c_double), ("nq", C.c_int),
+                ("qvec", C.c_void_p), ("nm", C.c_int), ("mvec", C.c_void_p), ("link_ofs", C.c_void_p),
+                ("link_m", C.c_void_p), ("proj", C.c_void_p), ("logproj", C.c_void_p), ("J", C.c_void_p),
+                ("j_fp32", C.c_int), ("res", C.c_void_p)]
 
 
 _lib = None
@@ -74,6 +86,14 @@ def lib():
             "tg_solver_profile": [vp, i_],
             "tg_solver_profile_read": [vp, i_, C.POINTER(C.c_double), ip],
             "tg_launch_count": [C.POINTER(C.c_longlong)],
+            "tg_server_create": [i_, d_, C.POINTER(C.c_void_p)],
+            "tg_server_destroy": [vp],
+            "tg_submit": [vp, vp, C.POINTER(C.c_longlong)],
+            "tg_poll": [vp, C.c_longlong, ip],
+            "tg_wait": [vp, C.c_longlong, C.POINTER(C.c_double)],
+            "tg_server_stats": [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)],
+            "tg_server_reset_stats": [vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -299,3 +319,96 @@ def optical_coefficients(mua, mus, nref):
 def omega_of(freq_mhz):
     """Modulation frequency [MHz] -> omega [rad/ps] (src/supertoast/fwdfem.cc:116)."""
     return freq_mhz * 2.0 * np.pi * 1e-6
+
+
+class Request:
+    """One whole request for the server: host inputs and the output buffers it
+    fills (proj, logproj, optional J, per-source results)."""
+
+    def __init__(self, mesh: Mesh, cmua, ckap, c2a, omega, qvec, mvec, links: Links, solver=None, precon="ICH",
+                 tol=1e-10, precision="mixed", want_jac=True, j_fp32=True, maxit=0):
+        self.complex = omega != 0.0 or np.iscomplexobj(qvec)
+        self.mesh = mesh
+        cplx = self.complex
+        solver = solver or ("BICGSTAB" if cplx else "CG")
+        self._keep = [np.ascontiguousarray(x, np.float64) for x in (cmua, ckap, c2a)]
+        self.qvec = _f64(qvec, cplx)
+        self.mvec = _f64(mvec, cplx)
+        self.links = links
+        n, nq, nm, nqm = mesh.n, self.qvec.shape[0], self.mvec.shape[0], links.nqm
+        dt = np.complex128 if cplx else np.float64
+        self.proj = np.zeros(nqm, dt)
+        self.logproj = np.zeros(nqm, dt)
+        self.J = (np.zeros((2 * nqm, 2 * n if cplx else n), np.float32 if j_fp32 else np.float64)
+                  if want_jac else None)
+        self.res = (TgResult * (nq + nm))()
+        r = TgRequest()
+        r.mesh = mesh._h.value if hasattr(mesh._h, "value") else mesh._h
+        r.is_complex = int(cplx)
+        r.method, r.precon, r.precision = SOLVERS[solver], PRECONS[precon], PRECISIONS[precision]
+        r.tol, r.maxit = float(tol), int(maxit)
+        r.cmua, r.ckappa, r.c2a = (x.ctypes.data for x in self._keep)
+        r.omega = float(omega)
+        r.nq, r.qvec, r.nm, r.mvec = nq, self.qvec.ctypes.data, nm, self.mvec.ctypes.data
+        r.link_ofs, r.link_m = links.ofs.ctypes.data, links.m.ctypes.data
+        r.proj, r.logproj = self.proj.ctypes.data, self.logproj.ctypes.data
+        r.J = self.J.ctypes.data if self.J is not None else None
+        r.j_fp32 = int(j_fp32)
+        r.res = C.addressof(self.res)
+        self.c = r
+        self.latency_ms = None
+
+    @property
+    def results(self):
+        return [(x.it_count, x.status, x.rel_err) for x in self.res]
+
+
+class Server:
+    """tg_server: whole requests admitted by slot and HBM budget, run
+    concurrently on per-slot streams (include/toastgpu.h)."""
+
+    def __init__(self, slots=4, hbm_budget_gb=64.0):
+        h = C.c_void_p()
+        _check(lib().tg_server_create(int(slots), float(hbm_budget_gb), C.byref(h)))
+        self._h = h
+        self._pending = {}
+
+    def submit(self, req: Request) -> int:
+        t = C.c_longlong()
+        _check(lib().tg_submit(self._h, C.byref(req.c), C.byref(t)))
+        self._pending[t.value] = req
+        return t.value
+
+    def poll(self, ticket) -> int:
+        st = C.c_int()
+        _check(lib().tg_poll(self._h, C.c_longlong(ticket), C.byref(st)))
+        return st.value
+
+    def wait(self, ticket) -> Request:
+        lat = C.c_double()
+        req = self._pending.pop(ticket)
+        _check(lib().tg_wait(self._h, C.c_longlong(ticket), C.byref(lat)))
+        req.latency_ms = lat.value
+        return req
+
+    def stats(self):
+        c, f, sv = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        p50, p99, el = C.c_double(), C.c_double(), C.c_double()
+        _check(lib().tg_server_stats(self._h, C.byref(c), C.byref(f), C.byref(sv), C.byref(p50), C.byref(p99),
+                                     C.byref(el)))
+        return dict(completed=c.value, failed=f.value, solves=sv.value, p50_ms=p50.value, p99_ms=p99.value,
+                    elapsed_s=el.value)
+
+    def reset_stats(self):
+        _check(lib().tg_server_reset_stats(self._h))
+
+    def close(self):
+        if self._h:
+            lib().tg_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
