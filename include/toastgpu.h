@@ -111,6 +111,12 @@ int tg_solver_set(tg_solver s, double tol, int maxit);
    The FP64 path always factors in the natural ordering.  Takes effect at the
    next tg_solver_reset. */
 int tg_solver_set_refinement(tg_solver s, double inner_tol, int max_outer, int inner_ordering);
+/* mixed precision with BiCGSTAB: on (default) keeps ONE FP32 Krylov process
+   per right-hand side and replaces its residual by the FP64 residual
+   b - A x whenever the recursive residual has fallen by inner_tol (reliable
+   updates), instead of restarting an FP32 solve every refinement step (off).
+   At most 4 * max_outer updates. */
+int tg_solver_set_reliable_updates(tg_solver s, int on);
 /* a cudaStream_t; 0 selects the solver's own stream */
 int tg_solver_set_stream(tg_solver s, void *stream);
 int tg_solver_sync(tg_solver s);

@@ -24,7 +24,7 @@ MEM_HOST, MEM_DEVICE = 0, 1
 DATA_LIN, DATA_LOG = 1, 2
 
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
-           "tg_qvec_gaussian", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_stream",
+           "tg_qvec_gaussian", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
            "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count",
            "tg_server_create", "tg_server_destroy", "tg_submit", "tg_poll", "tg_wait", "tg_server_stats",
@@ -74,6 +74,7 @@ def lib():
             "tg_solver_destroy": [vp],
             "tg_solver_set": [vp, d_, i_],
             "tg_solver_set_refinement": [vp, d_, i_, i_],
+            "tg_solver_set_reliable_updates": [vp, i_],
             "tg_solver_set_stream": [vp, vp],
             "tg_solver_sync": [vp],
             "tg_solver_reset": [vp, dp, dp, dp, d_, i_],
@@ -229,6 +230,9 @@ class FwdSolver:
 
     def set_refinement(self, inner_tol, max_outer=12, inner_ordering=1):
         _check(lib().tg_solver_set_refinement(self._h, float(inner_tol), int(max_outer), int(inner_ordering)))
+
+    def set_reliable_updates(self, on=True):
+        _check(lib().tg_solver_set_reliable_updates(self._h, int(bool(on))))
 
     def set_tol(self, tol, maxit=0):
         _check(lib().tg_solver_set(self._h, float(tol), int(maxit)))

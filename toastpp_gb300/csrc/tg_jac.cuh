@@ -1,5 +1,6 @@
 // tg_jac.cuh -- ProjectAll and the nodal-basis Jacobian.
 #pragma once
+#include <type_traits>
 #include "tg_kernels.cuh"
 
 namespace tg {
@@ -168,17 +169,74 @@ static __global__ void jac_weights_kernel(MeshDev m, int D, double* __restrict__
     }
 }
 
-// asynchronous global -> shared copy of one value (LDGSTS), B = 4, 8 or 16 bytes
-template <int B>
-__device__ __forceinline__ void cp_async_val(void* dst, const void* src)
+// packed FP32x2 arithmetic (sm_100+ fma.rn.f32x2): one instruction, two lanes
+__device__ __forceinline__ unsigned long long f2_pack(float a, float b)
 {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    if constexpr (B == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
-    else asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(src), "n"(B) : "memory");
+    unsigned long long d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(a), "f"(b));
+    return d;
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ float2 f2_unpack(unsigned long long a)
+{
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(a));
+    return r;
+}
+
+// Phase C for complex FP32: sum_i f_i h_i kept as four real sums, two per
+// packed register: P = (sum fr hr, sum fr hi), Q = (sum fi hr, sum fi hi);
+// then Re = P.x - Q.y, Im = P.y + Q.x.
+template <int JRQ, int JRM>
+__device__ __forceinline__ void jac_pairs_c32(const cf* __restrict__ Fs, const cf* __restrict__ Hm,
+                                              const cf* __restrict__ Hk, int SP, int qq0, int mm0, int dmax,
+                                              int lane, cf (&am)[JRQ][JRM], cf (&ak)[JRQ][JRM])
+{
+    unsigned long long pm[JRQ][JRM], qm[JRQ][JRM], pk[JRQ][JRM], qk[JRQ][JRM];
+#pragma unroll
+    for (int x = 0; x < JRQ; x++)
+#pragma unroll
+        for (int y = 0; y < JRM; y++) pm[x][y] = qm[x][y] = pk[x][y] = qk[x][y] = 0ull;
+    const unsigned long long* F = reinterpret_cast<const unsigned long long*>(Fs) + (size_t)qq0 * SP + lane;
+    const unsigned long long* M = reinterpret_cast<const unsigned long long*>(Hm) + (size_t)mm0 * SP + lane;
+    const unsigned long long* K = reinterpret_cast<const unsigned long long*>(Hk) + (size_t)mm0 * SP + lane;
+#pragma unroll 2
+    for (int i = 0; i < dmax; i++) {
+        const int s = i * JKT;
+        unsigned long long frr[JRQ], fii[JRQ], hm[JRM], hk[JRM];
+#pragma unroll
+        for (int x = 0; x < JRQ; x++) {
+            const float2 f = f2_unpack(F[(size_t)x * SP + s]);
+            frr[x] = f2_pack(f.x, f.x);
+            fii[x] = f2_pack(f.y, f.y);
+        }
+#pragma unroll
+        for (int y = 0; y < JRM; y++) { hm[y] = M[(size_t)y * SP + s]; hk[y] = K[(size_t)y * SP + s]; }
+#pragma unroll
+        for (int x = 0; x < JRQ; x++)
+#pragma unroll
+            for (int y = 0; y < JRM; y++) {
+                pm[x][y] = f2_fma(frr[x], hm[y], pm[x][y]);
+                qm[x][y] = f2_fma(fii[x], hm[y], qm[x][y]);
+                pk[x][y] = f2_fma(frr[x], hk[y], pk[x][y]);
+                qk[x][y] = f2_fma(fii[x], hk[y], qk[x][y]);
+            }
+    }
+#pragma unroll
+    for (int x = 0; x < JRQ; x++)
+#pragma unroll
+        for (int y = 0; y < JRM; y++) {
+            const float2 p = f2_unpack(pm[x][y]), q = f2_unpack(qm[x][y]);
+            const float2 u = f2_unpack(pk[x][y]), v = f2_unpack(qk[x][y]);
+            am[x][y] = cf{p.x - q.y, p.y + q.x};
+            ak[x][y] = cf{u.x - v.y, u.y + v.x};
+        }
+}
 
 template <class V, int JQ, int JM, int JRQ, int JRM>
 __global__ void __launch_bounds__(256) jacobian_kernel(JacArgs<V> a)
@@ -280,6 +338,9 @@ __global__ void __launch_bounds__(256) jacobian_kernel(JacArgs<V> a)
         for (int grp = warp; grp < NG; grp += blockDim.x / 32) {
             const int qq0 = (grp / GM) * JRQ, mm0 = (grp % GM) * JRM;
             V am[JRQ][JRM], ak[JRQ][JRM];
+            if constexpr (std::is_same<V, cf>::value) {
+                jac_pairs_c32<JRQ, JRM>(Fs, Hm, Hk, SP, qq0, mm0, dmax, lane, am, ak);
+            } else {
 #pragma unroll
             for (int x = 0; x < JRQ; x++)
 #pragma unroll
@@ -299,6 +360,7 @@ __global__ void __launch_bounds__(256) jacobian_kernel(JacArgs<V> a)
                         am[x][y] = vfma(am[x][y], f[x], hm[y]);
                         ak[x][y] = vfma(ak[x][y], f[x], hk[y]);
                     }
+            }
             }
             if (!kin) continue;
 #pragma unroll

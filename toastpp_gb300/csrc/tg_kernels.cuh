@@ -18,6 +18,7 @@ namespace tg {
 struct ColState {
     double rho, rhop, alpha, omega, beta, dnew, dold, bnorm, err, tol;
     int its, active, status, maxit;
+    int rel;  // reliable update of the mixed path: 1 resume the Krylov process, 2 restart it
 };
 
 // ---------------------------------------------------------------------------
@@ -425,6 +426,89 @@ __global__ void __launch_bounds__(256) spmm_vec_kernel(int n, const int* __restr
     tile_dots<V>(r0, r1, k, ld, y, w, want_n2, part, np, ntiles, tile, st);
 }
 
+// asynchronous global -> shared copy of one value (LDGSTS), B = 4, 8 or 16 bytes
+template <int B>
+__device__ __forceinline__ void cp_async_val(void* dst, const void* src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (B == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(src), "n"(B) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// SpMM with the tile's source rows staged in shared memory: the block's
+// ROW_TILE rows reference halo_ptr[t+1] - halo_ptr[t] distinct rows of x
+// (about a third of their entries on a Morton-ordered 3D mesh); each column
+// chunk of those rows is copied once (cp.async, 16-byte words) and every
+// entry then reads shared memory.  Half-warp per row, lane per 16-byte word;
+// the entries of a row are applied in CSR order, as spmm_vec_kernel.
+constexpr int HALO_CW = 16;  // 16-byte words per column chunk
+
+template <class V>
+__global__ void __launch_bounds__(256) spmm_halo_kernel(int n, const int* __restrict__ rowptr,
+                                                        const unsigned short* __restrict__ lcol,
+                                                        const int* __restrict__ halo_ptr,
+                                                        const int* __restrict__ halo_col, const V* __restrict__ A,
+                                                        int k, int ld, const V* __restrict__ x, V* __restrict__ y,
+                                                        const V* __restrict__ w, bool want_n2,
+                                                        double* __restrict__ part, int np, int ntiles,
+                                                        const ColState* __restrict__ st)
+{
+    constexpr int P = W16<V>::P;
+    extern __shared__ __align__(16) unsigned char hsm[];
+    W16<V>* sx = reinterpret_cast<W16<V>*>(hsm);   // [halo rows][HALO_CW]
+    const int tile = blockIdx.x;
+    const int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    const int h0 = halo_ptr[tile], nh = halo_ptr[tile + 1] - h0;
+    const int nwords = k / P, ldw = ld / P;
+    const W16<V>* X = reinterpret_cast<const W16<V>*>(x);
+    W16<V>* Y = reinterpret_cast<W16<V>*>(y);
+    const int hw = threadIdx.x >> 4, l16 = threadIdx.x & 15, nhw = blockDim.x >> 4;
+    for (int w0 = 0; w0 < nwords; w0 += HALO_CW) {
+        const int cw = min(HALO_CW, nwords - w0);
+        for (int e = threadIdx.x; e < nh * cw; e += blockDim.x) {
+            const int h = e / cw, ww = e - h * cw;
+            cp_async_val<16>(&sx[h * HALO_CW + ww], &X[(size_t)halo_col[h0 + h] * ldw + w0 + ww]);
+        }
+        cp_async_commit();
+        cp_async_wait<0>();
+        __syncthreads();
+        if (l16 < cw) {
+            const int wi = w0 + l16;
+            for (int r = r0 + hw; r < r1; r += nhw) {
+                W16<V> acc;
+#pragma unroll
+                for (int p = 0; p < P; p++) acc.v[p] = vzero<V>();
+                const int q1 = rowptr[r + 1];
+#pragma unroll 4
+                for (int q = rowptr[r]; q < q1; q++) {
+                    const V a = A[q];
+                    const W16<V> g = sx[lcol[q] * HALO_CW + l16];
+#pragma unroll
+                    for (int p = 0; p < P; p++) acc.v[p] = vfma(acc.v[p], a, g.v[p]);
+                }
+                if (st) {  // inactive columns keep their values
+                    bool all = true;
+#pragma unroll
+                    for (int p = 0; p < P; p++) all &= st[wi * P + p].active == 1;
+                    if (all) Y[(size_t)r * ldw + wi] = acc;
+                    else
+#pragma unroll
+                        for (int p = 0; p < P; p++)
+                            if (st[wi * P + p].active == 1) y[(size_t)r * ld + wi * P + p] = acc.v[p];
+                } else {
+                    Y[(size_t)r * ldw + wi] = acc;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!w && !want_n2) return;
+    tile_dots<V>(r0, r1, k, ld, y, w, want_n2, part, np, ntiles, tile, st);
+}
+
 // IC(0) level kernel on the level's ELL entries (k >= 32): warp per slot;
 // the slot's entries sit at slot * w, so the row's indices, values, right-hand
 // side and pivot load in one round and the gathers in the next.
@@ -557,6 +641,7 @@ enum Phase : int {
     PH_PCG_ALPHA,        // part0 = d.q -> alpha
     PH_PCG_END,          // part0 = r.q (dnew), part1 = |r|^2 -> beta, err, convergence
     PH_RESID,            // part0 = |r|^2 -> err (refinement residual)
+    PH_REL_RESUME,       // part0 = rd.r after a residual replacement -> rho, beta; reactivate
 };
 
 template <int NP>
@@ -599,7 +684,7 @@ __global__ void reduce_finalize_kernel(int k, int ntiles, const double* __restri
     case PH_BICG_S:
         if (!S.active) break;
         S.err = sqrt(v0);  // real variant only: |s| < tol |b| ends the solve (matrix_imp.hpp:512-517)
-        if (real_variant && S.err < S.tol * S.bnorm) { S.active = -1; }  // -1: finish with x += alpha pd
+        if (real_variant && S.err < S.tol * S.bnorm) { S.active = -1; S.rel = -1; }  // -1: finish with x += alpha pd
         break;
     case PH_BICG_OMEGA:
         if (S.active != 1) break;
@@ -642,6 +727,25 @@ __global__ void reduce_finalize_kernel(int k, int ntiles, const double* __restri
     }
     case PH_RESID:
         S.err = sqrt(v0);
+        break;
+    case PH_REL_RESUME:
+        // the replaced residual continues the same BiCGSTAB process
+        // (rel 1: the END step's rho / beta update with the new r) or
+        // starts a new one from it (rel 2, after a breakdown)
+        if (!S.rel) break;
+        if (S.rel == 1) {
+            S.rhop = S.rho;
+            S.rho = v0;
+            S.beta = (S.rho * S.alpha) / (S.rhop * S.omega);
+        } else {
+            S.rho = v0;
+            S.beta = 0.0;
+            S.omega = 1.0;
+        }
+        S.rel = 0;
+        S.status = 0;
+        S.active = 1;
+        if (v0 == 0.0 || !isfinite(S.beta)) { S.active = 0; S.status = 2; }
         break;
     }
 }
@@ -961,6 +1065,125 @@ static __global__ void count_active_kernel(int k, const ColState* __restrict__ c
     atomicAdd(&s, c);
     __syncthreads();
     if (threadIdx.x == 0) *out = s;
+}
+
+// ---------------------------------------------------------------------------
+// Reliable updates of the mixed-precision BiCGSTAB (residual replacement,
+// Sleijpen & van der Vorst 1996): the FP32 process runs until its recursive
+// residual has fallen by the trigger factor; then the FP32 correction is
+// added to the FP64 solution, the true residual b - A x is formed in FP64 and
+// replaces the FP32 residual, and the same Krylov process continues.
+// ---------------------------------------------------------------------------
+// out[0] outer columns active, out[1] inner columns iterating, out[2] waiting
+// for an update (outer active, inner stopped)
+static __global__ void rel_flags_kernel(int k, const ColState* __restrict__ co, const ColState* __restrict__ ci,
+                                        int* out)
+{
+    __shared__ int s[3];
+    if (threadIdx.x < 3) s[threadIdx.x] = 0;
+    __syncthreads();
+    int a = 0, b = 0, f = 0;
+    for (int c = threadIdx.x; c < k; c += blockDim.x) {
+        const bool oa = co[c].active == 1, ia = ci[c].active == 1;
+        a += oa;
+        b += ia;
+        f += oa && !ia;
+    }
+    atomicAdd(&s[0], a);
+    atomicAdd(&s[1], b);
+    atomicAdd(&s[2], f);
+    __syncthreads();
+    if (threadIdx.x < 3) out[threadIdx.x] = s[threadIdx.x];
+}
+
+// inner columns start from the outer residual: bnorm = |r|, trigger tol
+static __global__ void rel_init_kernel(int k, ColState* __restrict__ co, ColState* __restrict__ ci, double trig,
+                                       int maxit)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    ColState& O = co[c];
+    if (O.active == 1 && O.err <= O.tol * O.bnorm) { O.active = 0; O.status = 0; }
+    ColState s;
+    memset(&s, 0, sizeof(s));
+    s.tol = trig;
+    s.maxit = maxit;
+    s.bnorm = O.err;
+    s.active = O.active;
+    ci[c] = s;
+}
+
+// waiting columns: rel = 1 (the trigger was reached: resume) or 2 (breakdown,
+// omega = 0 or the iteration limit: restart the process)
+static __global__ void rel_mark_kernel(int k, const ColState* __restrict__ co, ColState* __restrict__ ci)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    ColState& I = ci[c];
+    // a half-step exit (rel -1, real variant) leaves no consistent direction: restart
+    I.rel = (co[c].active == 1 && I.active != 1) ? ((I.status == 0 && I.rel != -1) ? 1 : 2) : 0;
+}
+
+// at the iteration limit every active column takes its last update
+static __global__ void rel_mark_all_kernel(int k, const ColState* __restrict__ co, ColState* __restrict__ ci)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    if (co[c].active == 1 && !ci[c].rel) ci[c].rel = 1;
+}
+
+// x += x32 and x32 = 0 on the marked columns
+template <class V64, class V32>
+__global__ void rel_accumulate_kernel(int n, int k, const ColState* __restrict__ ci, V64* __restrict__ x,
+                                      V32* __restrict__ x32)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * k) return;
+    int c = (int)(t % k);
+    const int rel = ci[c].rel;
+    if (!rel) return;
+    if (rel == 1) x[t] = vadd(x[t], vcast<V64, V32>(x32[t]));  // a broken-down process's correction is dropped
+    x32[t] = vzero<V32>();
+}
+
+// after |b - A x| of the marked columns is in co.err: converged columns stop,
+// the others restart their trigger from the new residual; at the update or
+// iteration limit every active column stops with status 1
+static __global__ void rel_outer_kernel(int k, ColState* __restrict__ co, ColState* __restrict__ ci, int limit)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    ColState& O = co[c];
+    ColState& I = ci[c];
+    if (O.active != 1 || !I.rel) return;
+    if (O.err <= O.tol * O.bnorm) { O.active = 0; O.status = 0; I.rel = 0; return; }
+    if (limit) { O.active = 0; O.status = 1; I.rel = 0; return; }
+    I.bnorm = O.err;
+}
+
+// the marked columns take the true residual; restarted columns also reset the
+// shadow residual and the search directions
+template <class V64, class V32>
+__global__ void rel_replace_kernel(int n, int k, const ColState* __restrict__ ci, const V64* __restrict__ r64,
+                                   V32* __restrict__ r, V32* __restrict__ rd, V32* __restrict__ p,
+                                   V32* __restrict__ v)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * k) return;
+    int c = (int)(t % k);
+    const int rel = ci[c].rel;
+    if (!rel) return;
+    const V32 x = vcast<V32, V64>(r64[t]);
+    r[t] = x;
+    if (rel == 2) { rd[t] = x; p[t] = vzero<V32>(); v[t] = vzero<V32>(); }
+}
+
+static __global__ void rel_finish_kernel(int k, ColState* __restrict__ co, const ColState* __restrict__ ci)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    co[c].its = ci[c].its;
+    if (co[c].active == 1) { co[c].active = 0; co[c].status = 1; }
 }
 
 }  // namespace tg

@@ -8,6 +8,7 @@
 // IC(0) pattern = strict lower part of that pattern
 // (CalculateIncompleteCholeskyFillin, crmatrix_imp.hpp:2077-2102).
 #include <algorithm>
+#include <atomic>
 #include <array>
 #include <cstring>
 #include <numeric>
@@ -189,6 +190,31 @@ static int find_col(const std::vector<int>& rowptr, const std::vector<int>& coli
 
 // Morton (Z-order) layout of the nodes: rows that are close in space are
 // close in memory, so the neighbours a row gathers are shared by nearby rows.
+// distinct source rows of every ROW_TILE-row tile of the layout CSR: the
+// SpMM stages them once per tile in shared memory instead of gathering one
+// row per entry
+static void halo_lists(MeshHost& m)
+{
+    const int n = m.n, nt = (n + ROW_TILE - 1) / ROW_TILE;
+    m.halo_ptr.assign(nt + 1, 0);
+    m.halo_col.clear();
+    m.lcol.assign(m.lcolidx.size(), 0);
+    m.halo_max = 0;
+    std::vector<int> cols;
+    for (int t = 0; t < nt; t++) {
+        const int r0 = t * ROW_TILE, r1 = std::min(n, r0 + ROW_TILE);
+        cols.assign(m.lcolidx.begin() + m.lrowptr[r0], m.lcolidx.begin() + m.lrowptr[r1]);
+        std::sort(cols.begin(), cols.end());
+        cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+        if (cols.size() > 65535) throw Error{1, "tile halo too large"};
+        for (int e = m.lrowptr[r0]; e < m.lrowptr[r1]; e++)
+            m.lcol[e] = (unsigned short)(std::lower_bound(cols.begin(), cols.end(), m.lcolidx[e]) - cols.begin());
+        m.halo_col.insert(m.halo_col.end(), cols.begin(), cols.end());
+        m.halo_ptr[t + 1] = (int)m.halo_col.size();
+        m.halo_max = std::max(m.halo_max, (int)cols.size());
+    }
+}
+
 static void layout_order(MeshHost& m)
 {
     int n = m.n, dim = m.dim;
@@ -419,7 +445,7 @@ static T* upload(const std::vector<T>& v)
 Mesh::~Mesh()
 {
     void* ptrs[] = {d.rec, d.el, d.rowptr, d.colidx, d.diagpos, d.perm, d.iperm, d.jrowptr, d.jcolidx, d.asm_ptr,
-                    d.asm_list, d.nel_ptr, d.nel_list, d.nel_pos, d.bndnode};
+                    d.asm_list, d.nel_ptr, d.nel_list, d.nel_pos, d.bndnode, d.halo_ptr, d.halo_col, d.lcol};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto& g : d.ic) {
         void* q[] = {g.key, g.Lrowptr, g.Lcolidx, g.Lapos, g.Lkey, g.Ucolptr, g.Urow, g.Umap, g.fwd_lev_rows,
@@ -446,6 +472,7 @@ Mesh* mesh_build(int dim, int n, const double* coords, int ne, const int* el)
     for (int i = 0; i < n; i++)
         if (m.diagpos[i] < 0) { delete M; throw Error{1, "node not referenced by any element"}; }
     layout_order(m);
+    halo_lists(m);
     {
         std::vector<int> natkey(n);
         for (int i = 0; i < n; i++) natkey[i] = i;
@@ -453,6 +480,8 @@ Mesh* mesh_build(int dim, int n, const double* coords, int ne, const int* el)
         ic_pattern(m, colour_key(m), m.ic[1]);
     }
     gather_maps(m);
+    static std::atomic<long long> next_uid{1};
+    M->uid = next_uid.fetch_add(1);
     cudaGetDevice(&M->device);
     MeshDev& d = M->d;
     d.dim = dim; d.n = n; d.ne = ne; d.nn = m.nn;
@@ -466,6 +495,10 @@ Mesh* mesh_build(int dim, int n, const double* coords, int ne, const int* el)
     d.iperm = upload(m.iperm);
     d.jrowptr = upload(m.rowptr);
     d.jcolidx = upload(m.jcolidx);
+    d.halo_ptr = upload(m.halo_ptr);
+    d.halo_col = upload(m.halo_col);
+    d.lcol = upload(m.lcol);
+    d.halo_max = m.halo_max;
     d.asm_ptr = upload(m.asm_ptr);
     d.asm_list = upload(m.asm_list);
     d.nel_ptr = upload(m.nel_ptr);

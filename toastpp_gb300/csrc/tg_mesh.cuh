@@ -51,6 +51,11 @@ struct MeshHost {
     // rows keep their entries in natural column order, so every row sum is
     // the reference's; lay2nat[e] = natural CSR entry of layout entry e.
     std::vector<int> perm, iperm, lrowptr, lcolidx, ldiagpos, lay2nat, Lkey, jcolidx;
+    // per ROW_TILE-row layout tile: the distinct columns its rows reference
+    // (ascending), and for every layout entry the column's index in that list
+    std::vector<int> halo_ptr, halo_col;
+    std::vector<unsigned short> lcol;
+    int halo_max = 0;
     // IC(0) structures: [0] the natural (reference) ordering, [1] a colour-major
     // ordering (greedy colouring, colour classes are independent sets) used by
     // the FP32 inner preconditioner of the mixed path
@@ -70,6 +75,9 @@ struct MeshDev {
     int *rowptr, *colidx, *diagpos;   // layout CSR (rows and columns in layout positions)
     int *perm, *iperm;         // natural -> layout, layout -> natural
     int *jrowptr, *jcolidx;    // natural-row CSR with layout column ids (Jacobian tiles over natural nodes)
+    int *halo_ptr, *halo_col;  // distinct columns per ROW_TILE-row layout tile
+    unsigned short* lcol;      // per layout entry: index of its column in the tile's halo
+    int halo_max;
     unsigned *nel_pos;         // per node-element slot: positions of the element nodes in the node's CSR row (4 x uint8)
     int *asm_ptr, *asm_list;
     int *nel_ptr, *nel_list;
@@ -81,6 +89,7 @@ struct Mesh {
     MeshHost h;
     MeshDev d{};
     int device = 0;
+    long long uid = 0;  // unique per mesh built in this process
     ~Mesh();
 };
 

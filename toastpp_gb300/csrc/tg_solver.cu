@@ -5,7 +5,9 @@
 #include <utility>
 #include <cstdarg>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <tuple>
 #include <mutex>
 #include <vector>
 
@@ -31,6 +33,9 @@ const char* last_error() { return g_err.c_str(); }
 // launch accounting and opt-in per-class kernel timing
 // ---------------------------------------------------------------------------
 static std::atomic<long long> g_nlaunch{0};
+// SpMM variant chosen per (mesh, value type, k), shared by every solver of the process
+static std::mutex g_tune_mu;
+static std::map<std::tuple<long long, int, int>, int> g_tune;
 
 template <typename... KArgs, typename... Args>
 static inline void launch(void (*k)(KArgs...), dim3 g, dim3 b, size_t sm, cudaStream_t st, Args&&... args)
@@ -169,6 +174,7 @@ struct Engine {
     int precon = 0;            // 0 none, 1 diag, 2 ich
     Profiler* prof = nullptr;
     DBuf w[9], part, cs, cnt, gbasis, gcol;
+    bool halo_attr = false;
     int* h_cnt = nullptr;
     GraphCache graphs;
 
@@ -182,13 +188,38 @@ struct Engine {
     double* parts(int k, int np) { return (double*)part.ensure((size_t)k * np * ntiles() * sizeof(double)); }
     unsigned rowblk(int k) const { return (unsigned)std::min(256, std::max(32, (k + 31) / 32 * 32)); }
 
-    void spmm(int k, const V* x, V* y, const V* wv, bool n2, ColState* cst, double* pt, int np)
+    // SpMM variants: 0 halo-staged, 1 vector words, 2 warp per row, 3 narrow
+    bool spmm_ok(int var, int k) const
+    {
+        constexpr int P = W16<V>::P;
+        const MeshDev& m = mesh->d;
+        switch (var) {
+        case 0: return k % P == 0 && k / P >= 8 && halo_smem() <= 160 * 1024;
+        case 1: return k >= 32 && k % P == 0 && (k / P + 31) / 32 <= 4;
+        case 2: return k >= 32 && (k + 31) / 32 <= 8;
+        default: return true;
+        }
+        (void)m;
+    }
+    size_t halo_smem() const { return (size_t)mesh->d.halo_max * HALO_CW * 16; }
+
+    void spmm_launch(int var, int k, const V* x, V* y, const V* wv, bool n2, ColState* cst, double* pt, int np)
     {
         const MeshDev& m = mesh->d;
-        ProfScope ps(prof, PC_SPMM, st);
         constexpr int P = W16<V>::P;
-        const int nw = (k / P + 31) / 32;
-        if (k >= 32 && k % P == 0 && nw <= 4) {
+        switch (var) {
+        case 0: {
+            if (!halo_attr) {
+                TG_CUDA(cudaFuncSetAttribute(spmm_halo_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)halo_smem()));
+                halo_attr = true;
+            }
+            launch(spmm_halo_kernel<V>, ntiles(), 256, halo_smem(), st, m.n, m.rowptr, m.lcol, m.halo_ptr,
+                   m.halo_col, A, k, k, x, y, wv, n2, pt, np, ntiles(), cst);
+            return;
+        }
+        case 1: {
+            const int nw = (k / P + 31) / 32;
             switch (nw) {
 #define TG_SPMM_VW(J) case J: launch(spmm_vec_kernel<V, J>, ntiles(), 256, 0, st, m.n, m.rowptr, m.colidx, A, k, k, \
                                      x, y, wv, n2, pt, np, ntiles(), cst); break;
@@ -197,8 +228,8 @@ struct Engine {
             }
             return;
         }
-        const int nj = (k + 31) / 32;
-        if (k >= 32 && nj <= 8) {
+        case 2: {
+            const int nj = (k + 31) / 32;
             switch (nj) {
 #define TG_SPMM_NJ(J) case J: launch(spmm_wide_kernel<V, J>, ntiles(), 256, 0, st, m.n, m.rowptr, m.colidx, A, k, k, \
                                      x, y, wv, n2, pt, np, ntiles(), cst); break;
@@ -208,8 +239,57 @@ struct Engine {
             }
             return;
         }
-        launch(spmm_dot_kernel<V>, ntiles(), 256, 0, st, m.n, m.rowptr, m.colidx, A, k, k, x, y, wv, n2, pt, np,
-               ntiles(), cst);
+        default:
+            launch(spmm_dot_kernel<V>, ntiles(), 256, 0, st, m.n, m.rowptr, m.colidx, A, k, k, x, y, wv, n2, pt, np,
+                   ntiles(), cst);
+        }
+    }
+
+    // The autotuner: the first SpMM of a (mesh, value type, k) in the process
+    // times every applicable variant on the call's own operands and keeps the
+    // fastest for the rest of the process (all solvers share the choice, so a
+    // result never depends on which solver ran it).  Under stream capture the
+    // fixed preference order is used instead.
+    int spmm_variant(int k, const V* x, V* y, const V* wv, bool n2, ColState* cst, double* pt, int np)
+    {
+        const auto key = std::make_tuple(mesh->uid, (int)sizeof(V) * 2 + (int)vt<V>::cplx, k);
+        {
+            std::lock_guard<std::mutex> g(g_tune_mu);
+            auto it = g_tune.find(key);
+            if (it != g_tune.end()) return it->second;
+        }
+        std::vector<int> cands;
+        for (int v = 0; v < 4; v++)
+            if (spmm_ok(v, k)) cands.push_back(v);
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        TG_CUDA(cudaStreamIsCapturing(st, &cs));
+        if (cands.size() == 1 || cs != cudaStreamCaptureStatusNone) return cands[0];
+        cudaEvent_t e0, e1;
+        TG_CUDA(cudaEventCreate(&e0));
+        TG_CUDA(cudaEventCreate(&e1));
+        int best = cands[0];
+        float best_ms = 1e30f;
+        for (int v : cands) {
+            spmm_launch(v, k, x, y, wv, n2, cst, pt, np);  // warm-up
+            TG_CUDA(cudaEventRecord(e0, st));
+            for (int r = 0; r < 3; r++) spmm_launch(v, k, x, y, wv, n2, cst, pt, np);
+            TG_CUDA(cudaEventRecord(e1, st));
+            TG_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            TG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best_ms) { best_ms = ms; best = v; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        return g_tune.emplace(key, best).first->second;
+    }
+
+    void spmm(int k, const V* x, V* y, const V* wv, bool n2, ColState* cst, double* pt, int np)
+    {
+        const int var = spmm_variant(k, x, y, wv, n2, cst, pt, np);
+        ProfScope ps(prof, PC_SPMM, st);
+        spmm_launch(var, k, x, y, wv, n2, cst, pt, np);
     }
     template <int NP>
     void finalize(int k, ColState* cst, int phase, int real_variant = 0, int iter = 0)
@@ -408,34 +488,48 @@ struct Engine {
         }
     }
 
-    void bicgstab(int k, V* X, ColState* cst, int maxit)
+    // BiCGSTAB (src/libmath/matrix_imp.hpp:350-413 complex, 479-547 real):
+    // bicg_begin after R = b - A x; bicg_iter once per iteration
+    void bicg_begin(int k, ColState* cst)
+    {
+        const MeshDev& m = mesh->d;
+        size_t nk = (size_t)m.n * k;
+        V *R = vec(0, nk), *RD = vec(1, nk);
+        for (int i = 2; i < 8; i++) vec(i, nk);
+        TG_CUDA(cudaMemcpyAsync(RD, R, nk * sizeof(V), cudaMemcpyDeviceToDevice, st));
+        double* pt = parts(k, 2);
+        launch(dot_tiles_kernel<V>, ntiles(), rowblk(k), 0, st, m.n, k, k, RD, R, nullptr, nullptr, pt, 1, ntiles(), cst);
+        finalize<1>(k, cst, PH_BICG_RHO0);
+    }
+
+    void bicg_iter(int k, V* X, ColState* cst, int first)
     {
         const MeshDev& m = mesh->d;
         size_t nk = (size_t)m.n * k;
         unsigned eg = cdiv_u(nk, 256);
         V *R = vec(0, nk), *RD = vec(1, nk), *P = vec(2, nk), *PD = vec(3, nk), *Vv = vec(4, nk);
         V *Sv = vec(5, nk), *SD = vec(6, nk), *T = vec(7, nk);
-        TG_CUDA(cudaMemcpyAsync(RD, R, nk * sizeof(V), cudaMemcpyDeviceToDevice, st));
         double* pt = parts(k, 2);
-        launch(dot_tiles_kernel<V>, ntiles(), rowblk(k), 0, st, m.n, k, k, RD, R, nullptr, nullptr, pt, 1, ntiles(), cst);
-        finalize<1>(k, cst, PH_BICG_RHO0);
-        int pmode = precon == 2 ? 2 : precon;
+        const int pmode = precon == 2 ? 2 : precon;
         const int real_variant = vt<V>::cplx ? 0 : 1;
-        auto iteration = [&](int first) {
-            launch(bicg_p_kernel<V, S>, eg, 256, 0, st, m.n, k, k, cst, first, R, P, Vv, PD, idiag, pmode);
-            if (pmode == 2) ic_apply(k, P, PD, cst);
-            spmm(k, PD, Vv, RD, false, cst, pt, 1);
-            finalize<1>(k, cst, PH_BICG_ALPHA);
-            launch(bicg_s_kernel<V, S>, ntiles(), rowblk(k), 0, st, m.n, k, k, cst, R, Vv, Sv, SD, idiag, pmode, pt, ntiles());
-            finalize<1>(k, cst, PH_BICG_S, real_variant);
-            if (pmode == 2) ic_apply(k, Sv, SD, cst);
-            spmm(k, SD, T, Sv, true, cst, pt, 2);
-            finalize<2>(k, cst, PH_BICG_OMEGA);
-            launch(bicg_xr_kernel<V, S>, ntiles(), rowblk(k), 0, st, m.n, k, k, cst, X, R, RD, PD, SD, Sv, T, pt, ntiles());
-            finalize<2>(k, cst, PH_BICG_END);
-        };
+        launch(bicg_p_kernel<V, S>, eg, 256, 0, st, m.n, k, k, cst, first, R, P, Vv, PD, idiag, pmode);
+        if (pmode == 2) ic_apply(k, P, PD, cst);
+        spmm(k, PD, Vv, RD, false, cst, pt, 1);
+        finalize<1>(k, cst, PH_BICG_ALPHA);
+        launch(bicg_s_kernel<V, S>, ntiles(), rowblk(k), 0, st, m.n, k, k, cst, R, Vv, Sv, SD, idiag, pmode, pt, ntiles());
+        finalize<1>(k, cst, PH_BICG_S, real_variant);
+        if (pmode == 2) ic_apply(k, Sv, SD, cst);
+        spmm(k, SD, T, Sv, true, cst, pt, 2);
+        finalize<2>(k, cst, PH_BICG_OMEGA);
+        launch(bicg_xr_kernel<V, S>, ntiles(), rowblk(k), 0, st, m.n, k, k, cst, X, R, RD, PD, SD, Sv, T, pt, ntiles());
+        finalize<2>(k, cst, PH_BICG_END);
+    }
+
+    void bicgstab(int k, V* X, ColState* cst, int maxit)
+    {
+        bicg_begin(k, cst);
         for (int it = 0; it < maxit; it++) {
-            iteration(it == 0);
+            bicg_iter(k, X, cst, it == 0);
             if ((it & 3) == 3 || it + 1 == maxit)
                 if (count_active(k, cst) == 0) break;
         }
@@ -536,6 +630,7 @@ struct tg_solver_s {
     double inner_tol = 1e-4;   // mixed path: relative tolerance of each FP32 inner solve
     int max_outer = 12;        // mixed path: refinement steps
     int inner_colour = 1;      // mixed path: IC(0) of the inner solves in the colour-major ordering
+    int reliable = 1;          // mixed BiCGSTAB: reliable updates (1) or restarted refinement (0)
     cudaStream_t stream = 0, own = 0;
     bool reset_done = false;
     DBuf val64, val32, L64, L32, dinv64, dinv32, idiag64, idiag32, params;
@@ -548,6 +643,7 @@ struct tg_solver_s {
     DBuf jF, jG, jpair, jyinv, plink_q, plink_m, psup, pnsup, pflag, pMsup, plin, plog;
     DBuf fp_bq, fp_xq, fp_bm, fp_xm, fp_lin, fp_log;
     DBuf jwm64, jwk64, jwm32, jwk32;  // per-node element weights of the Jacobian (geometry only)
+    DBuf rel_cnt;
     int jw_D = 0, jw_ready = 0;       // slots per node; bit 0 FP64 weights built, bit 1 FP32
     Profiler prof;
     GraphCache graphs;
@@ -699,6 +795,66 @@ static void upload_async(tg_solver s, DBuf& b, const std::vector<T>& v)
 // core steps on device data (node-major n x k blocks)
 // ---------------------------------------------------------------------------
 // Solve F X = B for k right-hand sides; X holds the initial guess.
+// Mixed-precision BiCGSTAB with reliable updates: one FP32 Krylov process per
+// column that is never restarted; whenever its recursive residual has fallen
+// by inner_tol below the last true residual, the FP32 correction goes into the
+// FP64 solution and the FP64 residual b - A x replaces the FP32 one.  The
+// update runs for the waiting columns once half of the active columns wait
+// (or none is iterating); the solve stops per column on the FP64 residual.
+template <class V64, class V32>
+static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* co, V64* R, V32* R32,
+                           V32* X32, ColState* ci, Engine<V64>& e64, Engine<V32>& e32, int maxit)
+{
+    const int n = s->mesh->d.n;
+    const size_t nk = (size_t)n * k;
+    const unsigned eg = cdiv_u(nk, 256), ek = cdiv_u(k, 128);
+    double* pt = e64.parts(k, 1);
+    // co: bnorm (PH_BNORM) was set by the caller; err = |b - A x0|
+    launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, R, R, nullptr, nullptr, pt, 1,
+           e64.ntiles(), nullptr);
+    e64.template finalize<1>(k, co, PH_RESID);
+    launch(rel_init_kernel, ek, 128, 0, s->stream, k, co, ci, s->inner_tol, maxit);
+    V32* Rw = e32.vec(0, nk);
+    launch(cast_kernel<V32, V64>, eg, 256, 0, s->stream, nk, R, Rw);
+    TG_CUDA(cudaMemsetAsync(X32, 0, nk * sizeof(V32), s->stream));
+    e32.bicg_begin(k, ci);
+    V32 *RD = e32.vec(1, nk), *P = e32.vec(2, nk), *Vv = e32.vec(4, nk);
+    int* dcnt = (int*)s->rel_cnt.ensure(4 * sizeof(int));
+    int hc[4] = {0, 0, 0, 0};
+    const int max_upd = 4 * std::max(1, s->max_outer);
+    int it = 0, nupd = 0;
+    for (;;) {
+        e32.bicg_iter(k, X32, ci, it == 0);
+        it++;
+        const bool at_limit = it >= maxit;
+        if ((it & 3) != 0 && !at_limit) continue;
+        launch(rel_flags_kernel, 1, 256, 0, s->stream, k, co, ci, dcnt);
+        TG_CUDA(cudaMemcpyAsync(hc, dcnt, 3 * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+        TG_CUDA(cudaStreamSynchronize(s->stream));
+        const int oa = hc[0], ia = hc[1], fl = hc[2];
+        if (oa == 0) break;
+        if (!at_limit && (fl == 0 || (2 * fl < oa && ia > 0))) continue;
+        // reliable update of the waiting columns (every active one at the limit)
+        launch(rel_mark_kernel, ek, 128, 0, s->stream, k, co, ci);
+        if (at_limit) launch(rel_mark_all_kernel, ek, 128, 0, s->stream, k, co, ci);
+        launch(rel_accumulate_kernel<V64, V32>, eg, 256, 0, s->stream, n, k, ci, X, X32);
+        e64.spmm(k, X, R, nullptr, false, nullptr, nullptr, 0);
+        launch(resid_kernel<V64>, eg, 256, 0, s->stream, n, k, k, B, R, nullptr);
+        launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, R, R, nullptr, nullptr, pt,
+               1, e64.ntiles(), nullptr);
+        e64.template finalize<1>(k, co, PH_RESID);
+        nupd++;
+        launch(rel_outer_kernel, ek, 128, 0, s->stream, k, co, ci, (at_limit || nupd >= max_upd) ? 1 : 0);
+        launch(rel_replace_kernel<V64, V32>, eg, 256, 0, s->stream, n, k, ci, R, Rw, RD, P, Vv);
+        double* pt32 = e32.parts(k, 2);
+        launch(dot_tiles_kernel<V32>, e32.ntiles(), e32.rowblk(k), 0, s->stream, n, k, k, RD, Rw, nullptr, nullptr,
+               pt32, 1, e32.ntiles(), nullptr);
+        e32.template finalize<1>(k, ci, PH_REL_RESUME);
+        if (at_limit || nupd >= max_upd) break;
+    }
+    launch(rel_finish_kernel, ek, 128, 0, s->stream, k, co, ci);
+}
+
 template <class V64, class V32>
 static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co)
 {
@@ -736,6 +892,10 @@ static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co)
     e64.template finalize<1>(k, co, PH_BNORM);
     const int max_outer = s->max_outer;
     const double inner_tol = s->inner_tol;
+    if (s->method == TG_SOLVER_BICGSTAB && s->reliable) {
+        solve_reliable<V64, V32>(s, k, B, X, co, R, R32, E32, ci, e64, e32, maxit);
+        return;
+    }
     for (int step = 0; step <= max_outer; step++) {
         launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, R, R, nullptr, nullptr, pt, 1,
                                                                           e64.ntiles(), nullptr);
@@ -1244,6 +1404,14 @@ int tg_solver_set_refinement(tg_solver s, double inner_tol, int max_outer, int i
     s->max_outer = max_outer;
     s->inner_colour = inner_ordering;
     s->reset_done = false;  // the factorisation ordering may change
+    API_END
+}
+
+int tg_solver_set_reliable_updates(tg_solver s, int on)
+{
+    API_BEGIN
+    TG_CHECK(s, TG_ERR_ARG, "solver is NULL");
+    s->reliable = on != 0;
     API_END
 }
 
