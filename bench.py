@@ -29,8 +29,25 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "source-solves/s (fwd+adj, whole requests incl. assembly, ProjectAll, Jacobian), 3D 30k-node cylinder 100 MHz"
 UNIT = "source-solves/s"
+LABELS = {"c0_disc3k_cw": "2D 3.3k-node disc CW", "c1_disc13k_fd": "2D 13k-node disc 100 MHz",
+          "c2_cyl30k_fd": "3D 30k-node cylinder 100 MHz", "c3_box250k_fd": "3D 250k-node box 100 MHz"}
+
+
+def metric_of(cfg):
+    return ("source-solves/s (fwd+adj, whole requests incl. assembly, ProjectAll, Jacobian), " + LABELS[cfg])
+
+
+def method_of(P):
+    return "BICGSTAB" if P.complex else "CG"
+
+
+def workload_of(P, cfg, n_el, tol, precision, extra=""):
+    nq, nm, nqm = P.qm.nQ, P.qm.nM, P.qm.nQM
+    kind = "tets" if P.dim == 3 else "triangles"
+    cols = 2 * P.n if P.complex else P.n
+    return (f"{cfg}: {P.n} nodes, {n_el} {kind}, {'%g MHz' % P.freq_mhz if P.complex else 'CW'}, {nq}+{nm} optodes, "
+            f"{method_of(P)}+ICH tol {tol}, {precision}{extra}, nodal Jacobian {2 * nqm}x{cols}")
 
 
 def parse():
@@ -39,6 +56,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c2_cyl30k_fd",
+                    choices=["c0_disc3k_cw", "c1_disc13k_fd", "c2_cyl30k_fd", "c3_box250k_fd"])
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--tol", type=float, default=1e-12)
     ap.add_argument("--inner-tol", type=float, default=1e-4, help="mixed path: inner FP32 solve tolerance")
@@ -55,9 +75,9 @@ def parse():
     return ap.parse_args()
 
 
-def problem():
+def problem(cfg="c2_cyl30k_fd"):
     from toastpp_gb300 import workloads
-    return workloads.cylinder(seed=0, freq_mhz=100.0)
+    return workloads.CONFIGS[cfg]()
 
 
 def dist_env():
@@ -124,18 +144,20 @@ def cpu_request_time(P, nsrc_sample=16, nq_jac_sample=8, threads=None, tol=1e-12
     cm, ck, ca = O.optical_coefficients(P.mua, P.mus, P.nref)
     omega = P.freq_mhz * 2 * np.pi * 1e-6
     nq, nm = P.qm.nQ, P.qm.nM
+    meth = method_of(P)
+    dt = np.complex128 if P.complex else np.float64
     t0 = time.perf_counter()
-    val = m.assemble(cm, ck, ca, omega, True)
+    val = m.assemble(cm, ck, ca, omega, P.complex)
     O.ic_factor(m.rowptr, m.colidx, val)
     t_reset = time.perf_counter() - t0
     rng = np.random.default_rng(7)
     qs = rng.choice(nq, size=min(nsrc_sample, nq), replace=False)
     ms = rng.choice(nm, size=min(nsrc_sample, nm), replace=False)
-    qvec = np.stack([m.qvec_gaussian(P.qm.Q[i], P.qwidth) for i in range(nq)]).astype(np.complex128)
-    mvec = np.stack([m.qvec_gaussian(P.qm.M[i], P.mwidth) * ca for i in range(nm)]).astype(np.complex128)
+    qvec = np.stack([m.qvec_gaussian(P.qm.Q[i], P.qwidth) for i in range(nq)]).astype(dt)
+    mvec = np.stack([m.qvec_gaussian(P.qm.M[i], P.mwidth) * ca for i in range(nm)]).astype(dt)
     t0 = time.perf_counter()
-    dphi_s, itq, _ = O.solve(m.rowptr, m.colidx, val, qvec[qs], "BICGSTAB", "ICH", tol, 0, threads)
-    aphi_s, itm, _ = O.solve(m.rowptr, m.colidx, val, mvec[ms], "BICGSTAB", "ICH", tol, 0, threads)
+    dphi_s, itq, _ = O.solve(m.rowptr, m.colidx, val, qvec[qs], meth, "ICH", tol, 0, threads)
+    aphi_s, itm, _ = O.solve(m.rowptr, m.colidx, val, mvec[ms], meth, "ICH", tol, 0, threads)
     t_solve = time.perf_counter() - t0
     nsolved = len(qs) + len(ms)
     # Jacobian sample: nq_jac_sample sources x all detectors (one thread per source)
@@ -148,7 +170,7 @@ def cpu_request_time(P, nsrc_sample=16, nq_jac_sample=8, threads=None, tol=1e-12
     t_jac = time.perf_counter() - t0
     pairs_sample = jq * len(ms)
     t_full = t_reset + t_solve * (nq + nm) / nsolved + t_jac * (nq * nm) / pairs_sample
-    sample = (f"full assembly+IC(0) factor, {len(qs)}+{len(ms)} of {nq}+{nm} BiCGSTAB+ICH solves, "
+    sample = (f"full assembly+IC(0) factor, {len(qs)}+{len(ms)} of {nq}+{nm} {meth}+ICH solves, "
               f"Jacobian rows of {pairs_sample} of {nq * nm} links; extrapolated linearly to one request")
     return dict(t_request=t_full, t_reset=t_reset, t_solve_sample=t_solve, t_jac_sample=t_jac,
                 its_per_src=float(np.mean(np.concatenate([itq, itm]))), threads=threads, sample=sample)
@@ -158,7 +180,7 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    P = problem()
+    P = problem(args.config)
     nsolves = P.qm.nQ + P.qm.nM
     times = []
     info = None
@@ -169,11 +191,11 @@ def run_reference(args):
             times.append(info["t_request"])
     t = float(np.mean(times))
     val = nsolves / t
-    line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+    line = {"metric": metric_of(args.config), "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "complex-f64", "data": "synthetic (seeded mesh, optodes, inclusions)",
-            "config": {"workload": "3D cylinder R25 H50, 30810 nodes, 169128 tets, 100 MHz, 80+80 optodes, "
-                                   f"BiCGSTAB+ICH tol {args.tol}, nodal Jacobian 12800x61620",
+            "vs_baseline": None, "dtype": "complex-f64" if P.complex else "f64",
+            "data": "synthetic (seeded mesh, optodes, inclusions)",
+            "config": {"workload": workload_of(P, args.config, len(P.elems), args.tol, "fp64"),
                        "parallelism": "threads over sources (host)"},
             "impl": "reference",
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": info["threads"], "kind": "port",
@@ -197,14 +219,19 @@ def run_gpu(args):
     B.build()
     from toastpp_gb300 import capi
 
-    P = problem()
+    P = problem(args.config)
     n, nq, nm = P.n, P.qm.nQ, P.qm.nM
     nqm = P.qm.nQM
+    cplx = P.complex
+    meth = method_of(P)
+    cdt = np.complex128 if cplx else np.float64
     gm = capi.Mesh(P.coords, P.elems)
     cm, ck, ca = capi.optical_coefficients(P.mua, P.mus, P.nref)
     omega = capi.omega_of(P.freq_mhz)
-    qvec = gm.qvec_gaussian(P.qm.Q, P.qwidth).astype(np.complex128)
-    mvec = (gm.qvec_gaussian(P.qm.M, P.mwidth) * ca[None, :]).astype(np.complex128)
+    qvec = gm.qvec_gaussian(P.qm.Q, P.qwidth).astype(cdt)
+    mvec = (gm.qvec_gaussian(P.qm.M, P.mwidth) * ca[None, :]).astype(cdt)
+    vmul = 2 if cplx else 1
+    jcols = 2 * n if cplx else n
     links = capi.Links(P.qm.link_ofs, P.qm.link_m)
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)   # the library launches on this stream
@@ -219,12 +246,12 @@ def run_gpu(args):
 
     d_cm, d_ck, d_ca = dtensor(cm), dtensor(ck), dtensor(ca)
     d_q, d_m = dtensor(qvec), dtensor(mvec)
-    d_proj = torch.empty(2 * nqm, dtype=torch.float64, device=dev)
-    d_lproj = torch.empty(2 * nqm, dtype=torch.float64, device=dev)
-    d_J = torch.empty((2 * nqm, 2 * n), dtype=torch.float32 if j_fp32 else torch.float64, device=dev)
+    d_proj = torch.empty(vmul * nqm, dtype=torch.float64, device=dev)
+    d_lproj = torch.empty(vmul * nqm, dtype=torch.float64, device=dev)
+    d_J = torch.empty((2 * nqm, jcols), dtype=torch.float32 if j_fp32 else torch.float64, device=dev)
     torch.cuda.synchronize()
 
-    s = capi.FwdSolver(gm, "BICGSTAB", args.tol, "ICH", True, precision=args.precision)
+    s = capi.FwdSolver(gm, meth, args.tol, "ICH", cplx, precision=args.precision)
     s.set_stream(stream.cuda_stream)
     if args.precision == "mixed":
         s.set_refinement(args.inner_tol, 12, args.inner_order)
@@ -240,9 +267,8 @@ def run_gpu(args):
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
-    # timed region: device-resident inputs; J (>= 3 GB per step) flushes L2 every step
-    s.profile((1 << capi.PROF_SPMM) | (1 << capi.PROF_SWEEP) | (1 << capi.PROF_JAC) | (1 << capi.PROF_ASM)
-              | (1 << capi.PROF_PROJ))
+    # timed region: device-resident inputs, no profiling events inside; the
+    # Jacobian written every step (3 GB at the default size) flushes L2
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     l0 = capi.launch_count()
     with ClockSampler(local) as clk:
@@ -261,10 +287,18 @@ def run_gpu(args):
         t = torch.tensor([total_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
+    its = [r.it_count for r in res]
+    # per-class device time from separate profiled steps (CUDA events around
+    # each launch class, on the library's stream), outside the timed region
+    psteps = max(1, min(2, args.steps))
+    s.profile((1 << capi.PROF_SPMM) | (1 << capi.PROF_SWEEP) | (1 << capi.PROF_JAC) | (1 << capi.PROF_ASM)
+              | (1 << capi.PROF_PROJ))
+    for _ in range(psteps):
+        step()
+    torch.cuda.synchronize()
     prof = {c: s.profile_read(c) for c in (capi.PROF_SPMM, capi.PROF_SWEEP, capi.PROF_JAC, capi.PROF_ASM,
                                            capi.PROF_PROJ)}
     s.profile(0)
-    its = [r.it_count for r in res]
     nsolves = nq + nm
     value = ws * nsolves * args.steps / (total_ms / 1e3)
 
@@ -272,16 +306,16 @@ def run_gpu(args):
     nnz = gm.nnz
     k_f = nq + nm          # forward and adjoint sources share one batch
     nnz_l = (nnz - n) // 2
-    names = {capi.PROF_SPMM: f"spmm_dot_kernel (complex SpMM, k={nq + nm})",
-             capi.PROF_SWEEP: f"IC(0) apply: {gm.nlev_fwd}+{gm.nlev_bwd} level kernels (ic_fwd_level/ic_bwd_level) in one graph",
+    names = {capi.PROF_SPMM: f"SpMM (autotuned spmm_halo/vec/wide kernel, k={nq + nm})",
+             capi.PROF_SWEEP: "IC(0) apply: the level kernels of both sweeps (ic_level_ell) in one graph",
              capi.PROF_JAC: "jacobian_kernel", capi.PROF_ASM: "assembly + IC(0) factor",
              capi.PROF_PROJ: "project_kernel"}
     dom = max(prof, key=lambda c: prof[c][0])
-    vb = 8 if args.precision == "mixed" else 16
+    vb = (8 if args.precision == "mixed" else 16) // (1 if cplx else 2)
     jb = 4 if j_fp32 else 8
     if dom == capi.PROF_JAC:
         # J write + fields read once + CSR pattern (per launch)
-        alg_bytes = 2 * nqm * 2 * n * jb + (nq + nm) * n * vb + (n + 1 + nnz) * 4
+        alg_bytes = 2 * nqm * jcols * jb + (nq + nm) * n * vb + (n + 1 + nnz) * 4
     elif dom == capi.PROF_SPMM:
         alg_bytes = nnz * (vb + 4) + 4 * (n + 1) + 2 * n * k_f * vb
     elif dom == capi.PROF_SWEEP:
@@ -302,18 +336,19 @@ def run_gpu(args):
                 "frac": ach / peak, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "traffic": None, "algorithmic_bytes_per_launch": alg_bytes,
                 "launch_ms": dom_ms / dom_cnt}
-    shares = {names[c]: {"ms_per_step": prof[c][0] / args.steps, "launches_or_scopes": prof[c][1]}
+    shares = {names[c]: {"ms_per_step": prof[c][0] / psteps, "launches_or_scopes": prof[c][1] // psteps}
               for c in prof}
 
     # ---- e2e through the C ABI with host buffers (pinned), copies inside the timed region
     e2e = None
-    if rank == 0 or ws > 1:
+    j_bytes = 2 * nqm * jcols * (4 if j_fp32 else 8)
+    if (rank == 0 or ws > 1) and not args.no_e2e and j_bytes <= 16e9:
         h_cm, h_ck, h_ca = (torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for x in (cm, ck, ca))
-        h_q = torch.from_numpy(qvec.view(np.float64).copy()).pin_memory()
-        h_m = torch.from_numpy(mvec.view(np.float64).copy()).pin_memory()
-        h_proj = torch.empty(2 * nqm, dtype=torch.float64).pin_memory()
-        h_lproj = torch.empty(2 * nqm, dtype=torch.float64).pin_memory()
-        h_J = torch.empty((2 * nqm, 2 * n), dtype=torch.float32 if j_fp32 else torch.float64).pin_memory()
+        h_q = torch.from_numpy(np.ascontiguousarray(qvec).view(np.float64).copy()).pin_memory()
+        h_m = torch.from_numpy(np.ascontiguousarray(mvec).view(np.float64).copy()).pin_memory()
+        h_proj = torch.empty(vmul * nqm, dtype=torch.float64).pin_memory()
+        h_lproj = torch.empty(vmul * nqm, dtype=torch.float64).pin_memory()
+        h_J = torch.empty((2 * nqm, jcols), dtype=torch.float32 if j_fp32 else torch.float64).pin_memory()
         ksteps = max(1, min(args.steps, 3))
         s.forward_path_raw(h_cm, h_ck, h_ca, omega, nq, h_q, nm, h_m, links, None, None, h_proj, h_lproj, h_J,
                            j_fp32, capi.MEM_HOST)
@@ -324,8 +359,8 @@ def run_gpu(args):
                                j_fp32, capi.MEM_HOST)
         torch.cuda.synchronize()
         te = time.perf_counter() - t0
-        h2d = 3 * n * 8 + (nq + nm) * n * 16 + (nq + 1 + nqm) * 4
-        d2h = 2 * nqm * 16 + h_J.numel() * h_J.element_size()
+        h2d = 3 * n * 8 + (nq + nm) * n * 8 * vmul + (nq + 1 + nqm) * 4
+        d2h = 2 * nqm * 8 * vmul + h_J.numel() * h_J.element_size()
         e2e = {"value": ws * nsolves * ksteps / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "steps": ksteps}
 
@@ -334,9 +369,9 @@ def run_gpu(args):
         # ---- FP64 comparison legs (same request, plain FP64)
         compare = {}
         if not args.no_compare:
-            s64 = capi.FwdSolver(gm, "BICGSTAB", args.tol, "ICH", True, precision="fp64")
+            s64 = capi.FwdSolver(gm, meth, args.tol, "ICH", cplx, precision="fp64")
             s64.set_stream(stream.cuda_stream)
-            d_J64 = torch.empty((2 * nqm, 2 * n), dtype=torch.float64, device=dev)
+            d_J64 = torch.empty((2 * nqm, jcols), dtype=torch.float64, device=dev)
             p64 = torch.empty_like(d_proj)
             lp64 = torch.empty_like(d_lproj)
             s64.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, p64, lp64, d_J64, 0,
@@ -351,9 +386,10 @@ def run_gpu(args):
             t64 = a.elapsed_time(b) / 1e3
             compare["fp64_batched"] = {"value": nsolves / t64, "unit": UNIT, "ms_per_request": t64 * 1e3}
             # boundary-data agreement of the measured path with plain FP64 (same tolerance)
-            lp = d_lproj.cpu().numpy().view(np.complex128)
-            lr = lp64.cpu().numpy().view(np.complex128)
-            cm_err = float(np.max(np.abs(lp - lr) / np.maximum(np.abs(lp), np.abs(lr))))
+            lp = d_lproj.cpu().numpy().view(cdt)
+            lr = lp64.cpu().numpy().view(cdt)
+            ok = np.isfinite(lp) & np.isfinite(lr)   # log of a negative CW projection is NaN (as the reference)
+            cm_err = float(np.max(np.abs(lp - lr)[ok] / np.maximum(np.abs(lp), np.abs(lr))[ok]))
             l2_err = float(np.linalg.norm(d_proj.cpu().numpy() - p64.cpu().numpy()) / np.linalg.norm(p64.cpu().numpy()))
             compare["boundary_data_err_vs_fp64"] = {"cmpvec_max_rel_log": cm_err, "l2_rel_linear": l2_err}
             Jm = d_J.float().cpu()
@@ -362,7 +398,7 @@ def run_gpu(args):
                                                        torch.linalg.norm(J64.flatten()))
             del d_J64, Jm, J64
             # plain per-source FP64 (one right-hand side per solve), sampled
-            s1 = capi.FwdSolver(gm, "BICGSTAB", args.tol, "ICH", True, precision="fp64")
+            s1 = capi.FwdSolver(gm, meth, args.tol, "ICH", cplx, precision="fp64")
             s1.reset(cm, ck, ca, omega)
             ns = 4
             t0 = time.perf_counter()
@@ -379,23 +415,25 @@ def run_gpu(args):
                    "sample": info["sample"], "its_per_src": info["its_per_src"]}
         clocks = clk.summary()
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "metric": metric_of(args.config), "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "complex-f32 inner / complex-f64 refinement" if args.precision == "mixed" else "complex-f64",
+            "dtype": ((("complex-f32" if cplx else "f32") + " inner / " + ("complex-f64" if cplx else "f64") +
+                       " refinement") if args.precision == "mixed" else ("complex-f64" if cplx else "f64")),
             "data": "synthetic (seeded mesh, optodes, inclusions)",
-            "config": {"workload": f"3D cylinder R25 H50, {n} nodes, {gm.ne} tets, 100 MHz, {nq}+{nm} optodes, "
-                                   f"BiCGSTAB+ICH tol {args.tol}, {args.precision}"
-                                   f"{f' (inner FP32 tol {args.inner_tol})' if args.precision == 'mixed' else ''}, nodal Jacobian "
-                                   f"{2 * nqm}x{2 * n} ({'fp32' if j_fp32 else 'fp64'})",
+            "config": {"workload": workload_of(P, args.config, gm.ne, args.tol, args.precision,
+                                               f" (inner FP32 tol {args.inner_tol}, J {'fp32' if j_fp32 else 'fp64'})"
+                                               if args.precision == "mixed" else ""),
                        "parallelism": f"replicas x{ws} (one request per GPU)",
-                       "l2": "each step writes the >=3 GB Jacobian, larger than L2"},
+                       "l2": f"each step writes the {j_bytes / 1e9:.2f} GB Jacobian"
+                             + (", larger than L2" if j_bytes > 130e6 else ", smaller than L2: L2-resident case")},
             "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
             "jacobians_per_s": ws * args.steps / (total_ms / 1e3),
             "iterations_per_source": float(np.mean(its)),
             "roofline": roof, "kernel_time_per_step": shares,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
             "clocks": clocks, "wall_s": wall, "compare": compare,
+            "spmm_autotuner": capi.tuner_log().strip().splitlines(),
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -242,6 +242,9 @@ int tg_solver_profile(tg_solver s, int mask);
 int tg_solver_profile_read(tg_solver s, int cls, double *total_ms, int *count);
 /* number of kernels this library has launched in this process */
 int tg_launch_count(long long *count);
+/* the SpMM autotuner's decisions so far: one text line per (mesh, value type,
+   columns) with every candidate kernel's best launch time and the choice */
+int tg_tuner_log(char *buf, int len);
 
 const char *tg_last_error(void);
 

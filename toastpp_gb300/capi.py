@@ -26,7 +26,7 @@ DATA_LIN, DATA_LOG = 1, 2
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
            "tg_qvec_gaussian", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
-           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count",
+           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log",
            "tg_server_create", "tg_server_destroy", "tg_submit", "tg_poll", "tg_wait", "tg_server_stats",
            "tg_server_reset_stats", "tg_last_error"]
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
@@ -87,6 +87,7 @@ def lib():
             "tg_solver_profile": [vp, i_],
             "tg_solver_profile_read": [vp, i_, C.POINTER(C.c_double), ip],
             "tg_launch_count": [C.POINTER(C.c_longlong)],
+            "tg_tuner_log": [C.c_char_p, i_],
             "tg_server_create": [i_, d_, C.POINTER(C.c_void_p)],
             "tg_server_destroy": [vp],
             "tg_submit": [vp, vp, C.POINTER(C.c_longlong)],
@@ -298,6 +299,12 @@ class FwdSolver:
                                      _ptr(J), int(j_fp32), MEM_HOST, res))
         its = [(r.it_count, r.status, r.rel_err) for r in res]
         return dict(dphi=dphi, aphi=aphi, proj=proj, logproj=lproj, J=J, results=its)
+
+
+def tuner_log():
+    buf = C.create_string_buffer(1 << 16)
+    _check(lib().tg_tuner_log(buf, len(buf)))
+    return buf.value.decode()
 
 
 def launch_count():

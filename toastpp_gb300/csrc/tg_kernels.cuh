@@ -19,7 +19,16 @@ struct ColState {
     double rho, rhop, alpha, omega, beta, dnew, dold, bnorm, err, tol;
     int its, active, status, maxit;
     int rel;  // reliable update of the mixed path: 1 resume the Krylov process, 2 restart it
+    // mixed path: the FP32 process works on (true residual) / scale, a power
+    // of two of the last true residual norm, so its values stay O(1)
+    double scale, scale_prev;
 };
+
+// 2^floor(log2 x) for x > 0 finite, else 1: scaling by it is exact
+__host__ __device__ __forceinline__ double pow2_floor(double x)
+{
+    return (x > 0.0 && isfinite(x)) ? ldexp(1.0, ilogb(x)) : 1.0;
+}
 
 // ---------------------------------------------------------------------------
 // Assembly: one thread per CSR entry gathers its element contributions in
@@ -227,11 +236,13 @@ struct TileAcc {
 template <class V>
 __device__ __forceinline__ void tile_dots(int r0, int r1, int k, int ld, const V* __restrict__ y,
                                           const V* __restrict__ w, bool want_n2, double* __restrict__ part, int np,
-                                          int ntiles, int tile, const ColState* __restrict__ st)
+                                          int ntiles, int tile, const ColState* __restrict__ st, int cbeg = 0)
 {
+    // columns [cbeg, k) of the tile (a block that owns a column range passes
+    // its range; the per-column order is the same)
     __shared__ double sh[2 * TILE_RG * TILE_CK];
     TileAcc T{sh};
-    for (int c0 = 0; c0 < k; c0 += TILE_CK) {
+    for (int c0 = cbeg; c0 < k; c0 += TILE_CK) {
         const int ck = min(TILE_CK, k - c0);
         for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
             const int cc = it % ck, g = it / ck, c = c0 + cc;
@@ -438,13 +449,17 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// SpMM with the tile's source rows staged in shared memory: the block's
-// ROW_TILE rows reference halo_ptr[t+1] - halo_ptr[t] distinct rows of x
-// (about a third of their entries on a Morton-ordered 3D mesh); each column
-// chunk of those rows is copied once (cp.async, 16-byte words) and every
-// entry then reads shared memory.  Half-warp per row, lane per 16-byte word;
-// the entries of a row are applied in CSR order, as spmm_vec_kernel.
-constexpr int HALO_CW = 16;  // 16-byte words per column chunk
+// SpMM with the tile's source rows staged in shared memory.  The ROW_TILE
+// rows of a tile reference halo_ptr[t+1] - halo_ptr[t] distinct rows of x
+// (about a third of their entries on a Morton-ordered 3D mesh).  Block =
+// (tile, chunk of HALO_CW 16-byte words): it copies that chunk of the
+// distinct rows once (cp.async) and the tile's values and local indices,
+// then HALO_CW lanes per row apply the entries in CSR order (as
+// spmm_vec_kernel) from shared memory, and the block forms the dot partials
+// of its own columns.  Small blocks and no chunk loop: many blocks per SM
+// hide the gather latency.
+constexpr int HALO_CW = 8;       // 16-byte words per block = lanes per row
+constexpr int HALO_MAXE = 1024;  // entries of a tile held in shared memory
 
 template <class V>
 __global__ void __launch_bounds__(256) spmm_halo_kernel(int n, const int* __restrict__ rowptr,
@@ -454,59 +469,75 @@ __global__ void __launch_bounds__(256) spmm_halo_kernel(int n, const int* __rest
                                                         int k, int ld, const V* __restrict__ x, V* __restrict__ y,
                                                         const V* __restrict__ w, bool want_n2,
                                                         double* __restrict__ part, int np, int ntiles,
-                                                        const ColState* __restrict__ st)
+                                                        const ColState* __restrict__ st, int hmax)
 {
     constexpr int P = W16<V>::P;
     extern __shared__ __align__(16) unsigned char hsm[];
-    W16<V>* sx = reinterpret_cast<W16<V>*>(hsm);   // [halo rows][HALO_CW]
-    const int tile = blockIdx.x;
+    W16<V>* sx = reinterpret_cast<W16<V>*>(hsm);                       // [hmax][HALO_CW]
+    V* sa = reinterpret_cast<V*>(sx + (size_t)hmax * HALO_CW);          // [HALO_MAXE]
+    unsigned short* sl = reinterpret_cast<unsigned short*>(sa + HALO_MAXE);  // [HALO_MAXE]
+    __shared__ int srp[ROW_TILE + 1];
+    const int tile = blockIdx.x, w0 = blockIdx.y * HALO_CW;
     const int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
     const int h0 = halo_ptr[tile], nh = halo_ptr[tile + 1] - h0;
     const int nwords = k / P, ldw = ld / P;
+    const int cw = min(HALO_CW, nwords - w0);
     const W16<V>* X = reinterpret_cast<const W16<V>*>(x);
     W16<V>* Y = reinterpret_cast<W16<V>*>(y);
-    const int hw = threadIdx.x >> 4, l16 = threadIdx.x & 15, nhw = blockDim.x >> 4;
-    for (int w0 = 0; w0 < nwords; w0 += HALO_CW) {
-        const int cw = min(HALO_CW, nwords - w0);
-        for (int e = threadIdx.x; e < nh * cw; e += blockDim.x) {
-            const int h = e / cw, ww = e - h * cw;
-            cp_async_val<16>(&sx[h * HALO_CW + ww], &X[(size_t)halo_col[h0 + h] * ldw + w0 + ww]);
-        }
-        cp_async_commit();
-        cp_async_wait<0>();
-        __syncthreads();
-        if (l16 < cw) {
-            const int wi = w0 + l16;
-            for (int r = r0 + hw; r < r1; r += nhw) {
-                W16<V> acc;
+    for (int e = threadIdx.x; e < nh * cw; e += blockDim.x) {
+        const int h = e / cw, ww = e - h * cw;
+        cp_async_val<16>(&sx[h * HALO_CW + ww], &X[(size_t)halo_col[h0 + h] * ldw + w0 + ww]);
+    }
+    cp_async_commit();
+    const int e0 = rowptr[r0], ne = rowptr[r1] - e0;
+    const bool sm_entries = ne <= HALO_MAXE;
+    for (int t = threadIdx.x; t <= r1 - r0; t += blockDim.x) srp[t] = rowptr[r0 + t] - e0;
+    if (sm_entries)
+        for (int t = threadIdx.x; t < ne; t += blockDim.x) { sa[t] = A[e0 + t]; sl[t] = lcol[e0 + t]; }
+    cp_async_wait<0>();
+    __syncthreads();
+    const int grp = threadIdx.x / HALO_CW, l = threadIdx.x % HALO_CW, ngrp = blockDim.x / HALO_CW;
+    if (l < cw) {
+        const int wi = w0 + l;
+        for (int r = r0 + grp; r < r1; r += ngrp) {
+            W16<V> acc;
 #pragma unroll
-                for (int p = 0; p < P; p++) acc.v[p] = vzero<V>();
-                const int q1 = rowptr[r + 1];
+            for (int p = 0; p < P; p++) acc.v[p] = vzero<V>();
+            const int q0 = srp[r - r0], q1 = srp[r - r0 + 1];
+            if (sm_entries) {
 #pragma unroll 4
-                for (int q = rowptr[r]; q < q1; q++) {
-                    const V a = A[q];
-                    const W16<V> g = sx[lcol[q] * HALO_CW + l16];
+                for (int q = q0; q < q1; q++) {
+                    const V a = sa[q];
+                    const W16<V> g = sx[sl[q] * HALO_CW + l];
 #pragma unroll
                     for (int p = 0; p < P; p++) acc.v[p] = vfma(acc.v[p], a, g.v[p]);
                 }
-                if (st) {  // inactive columns keep their values
-                    bool all = true;
+            } else {
+#pragma unroll 4
+                for (int q = q0; q < q1; q++) {
+                    const V a = A[e0 + q];
+                    const W16<V> g = sx[lcol[e0 + q] * HALO_CW + l];
 #pragma unroll
-                    for (int p = 0; p < P; p++) all &= st[wi * P + p].active == 1;
-                    if (all) Y[(size_t)r * ldw + wi] = acc;
-                    else
-#pragma unroll
-                        for (int p = 0; p < P; p++)
-                            if (st[wi * P + p].active == 1) y[(size_t)r * ld + wi * P + p] = acc.v[p];
-                } else {
-                    Y[(size_t)r * ldw + wi] = acc;
+                    for (int p = 0; p < P; p++) acc.v[p] = vfma(acc.v[p], a, g.v[p]);
                 }
             }
+            if (st) {  // inactive columns keep their values
+                bool all = true;
+#pragma unroll
+                for (int p = 0; p < P; p++) all &= st[wi * P + p].active == 1;
+                if (all) Y[(size_t)r * ldw + wi] = acc;
+                else
+#pragma unroll
+                    for (int p = 0; p < P; p++)
+                        if (st[wi * P + p].active == 1) y[(size_t)r * ld + wi * P + p] = acc.v[p];
+            } else {
+                Y[(size_t)r * ldw + wi] = acc;
+            }
         }
-        __syncthreads();
     }
     if (!w && !want_n2) return;
-    tile_dots<V>(r0, r1, k, ld, y, w, want_n2, part, np, ntiles, tile, st);
+    __syncthreads();
+    tile_dots<V>(r0, r1, (w0 + cw) * P, ld, y, w, want_n2, part, np, ntiles, tile, st, w0 * P);
 }
 
 // IC(0) level kernel on the level's ELL entries (k >= 32): warp per slot;
@@ -528,7 +559,7 @@ __global__ void __launch_bounds__(256) ic_level_ell(const int* __restrict__ rows
         int c = lane + 32 * j;
         acc[j] = c < k ? (FWD ? b[(size_t)i * ld + c] : y[(size_t)i * ld + c]) : vzero<V>();
     }
-    constexpr int UNR = 4;
+    constexpr int UNR = 4;  // entries whose gathers are in flight together
     for (int base = 0; base < w; base += 32) {
         const int cnt = min(32, w - base);
         int my_c = -1;
@@ -680,6 +711,7 @@ __global__ void reduce_finalize_kernel(int k, int ntiles, const double* __restri
     case PH_BICG_ALPHA:
         if (!S.active) break;
         S.alpha = S.rho / v0;
+        if (!isfinite(S.alpha)) { S.active = 0; S.status = 2; S.its = S.its; }  // rd.v = 0: breakdown
         break;
     case PH_BICG_S:
         if (!S.active) break;
@@ -1096,7 +1128,8 @@ static __global__ void rel_flags_kernel(int k, const ColState* __restrict__ co, 
     if (threadIdx.x < 3) out[threadIdx.x] = s[threadIdx.x];
 }
 
-// inner columns start from the outer residual: bnorm = |r|, trigger tol
+// inner columns start from the outer residual, scaled to O(1): scale =
+// pow2_floor(|r|), bnorm = |r| / scale, trigger tol
 static __global__ void rel_init_kernel(int k, ColState* __restrict__ co, ColState* __restrict__ ci, double trig,
                                        int maxit)
 {
@@ -1108,9 +1141,21 @@ static __global__ void rel_init_kernel(int k, ColState* __restrict__ co, ColStat
     memset(&s, 0, sizeof(s));
     s.tol = trig;
     s.maxit = maxit;
-    s.bnorm = O.err;
+    s.scale = s.scale_prev = pow2_floor(O.err);
+    s.bnorm = O.err / s.scale;
     s.active = O.active;
     ci[c] = s;
+}
+
+// r32 = r / scale for every column (the start of the process)
+template <class V64, class V32>
+__global__ void rel_scaled_cast_kernel(int n, int k, const ColState* __restrict__ ci, const V64* __restrict__ r64,
+                                       V32* __restrict__ r)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * k) return;
+    int c = (int)(t % k);
+    r[t] = vcast<V32, V64>(vscale(r64[t], 1.0 / ci[c].scale));
 }
 
 // waiting columns: rel = 1 (the trigger was reached: resume) or 2 (breakdown,
@@ -1132,7 +1177,7 @@ static __global__ void rel_mark_all_kernel(int k, const ColState* __restrict__ c
     if (co[c].active == 1 && !ci[c].rel) ci[c].rel = 1;
 }
 
-// x += x32 and x32 = 0 on the marked columns
+// x += scale * x32 and x32 = 0 on the marked columns
 template <class V64, class V32>
 __global__ void rel_accumulate_kernel(int n, int k, const ColState* __restrict__ ci, V64* __restrict__ x,
                                       V32* __restrict__ x32)
@@ -1140,9 +1185,8 @@ __global__ void rel_accumulate_kernel(int n, int k, const ColState* __restrict__
     size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (size_t)n * k) return;
     int c = (int)(t % k);
-    const int rel = ci[c].rel;
-    if (!rel) return;
-    if (rel == 1) x[t] = vadd(x[t], vcast<V64, V32>(x32[t]));  // a broken-down process's correction is dropped
+    if (!ci[c].rel) return;
+    x[t] = vadd(x[t], vscale(vcast<V64, V32>(x32[t]), ci[c].scale));
     x32[t] = vzero<V32>();
 }
 
@@ -1158,7 +1202,11 @@ static __global__ void rel_outer_kernel(int k, ColState* __restrict__ co, ColSta
     if (O.active != 1 || !I.rel) return;
     if (O.err <= O.tol * O.bnorm) { O.active = 0; O.status = 0; I.rel = 0; return; }
     if (limit) { O.active = 0; O.status = 1; I.rel = 0; return; }
-    I.bnorm = O.err;
+    // rescale the process to the new residual (exact: powers of two)
+    I.scale_prev = I.scale;
+    I.scale = pow2_floor(O.err);
+    I.bnorm = O.err / I.scale;
+    I.rho *= I.scale_prev / I.scale;
 }
 
 // the marked columns take the true residual; restarted columns also reset the
@@ -1173,9 +1221,15 @@ __global__ void rel_replace_kernel(int n, int k, const ColState* __restrict__ ci
     int c = (int)(t % k);
     const int rel = ci[c].rel;
     if (!rel) return;
-    const V32 x = vcast<V32, V64>(r64[t]);
+    const V32 x = vcast<V32, V64>(vscale(r64[t], 1.0 / ci[c].scale));
     r[t] = x;
     if (rel == 2) { rd[t] = x; p[t] = vzero<V32>(); v[t] = vzero<V32>(); }
+    else {
+        using S32 = typename vt<V32>::R;
+        const S32 f = (S32)(ci[c].scale_prev / ci[c].scale);
+        p[t] = vscale(p[t], f);
+        v[t] = vscale(v[t], f);
+    }
 }
 
 static __global__ void rel_finish_kernel(int k, ColState* __restrict__ co, const ColState* __restrict__ ci)

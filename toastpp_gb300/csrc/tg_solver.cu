@@ -36,6 +36,17 @@ static std::atomic<long long> g_nlaunch{0};
 // SpMM variant chosen per (mesh, value type, k), shared by every solver of the process
 static std::mutex g_tune_mu;
 static std::map<std::tuple<long long, int, int>, int> g_tune;
+static std::string g_tune_log;  // one line per decision: candidates with their best launch time
+static const char* spmm_name(int v)
+{
+    static const char* nm[] = {"spmm_halo", "spmm_vec", "spmm_wide", "spmm_dot"};
+    return nm[v];
+}
+template <class V> static const char* vt_name();
+template <> const char* vt_name<double>() { return "f64"; }
+template <> const char* vt_name<float>() { return "f32"; }
+template <> const char* vt_name<cd>() { return "c64"; }
+template <> const char* vt_name<cf>() { return "c32"; }
 
 template <typename... KArgs, typename... Args>
 static inline void launch(void (*k)(KArgs...), dim3 g, dim3 b, size_t sm, cudaStream_t st, Args&&... args)
@@ -194,14 +205,17 @@ struct Engine {
         constexpr int P = W16<V>::P;
         const MeshDev& m = mesh->d;
         switch (var) {
-        case 0: return k % P == 0 && k / P >= 8 && halo_smem() <= 160 * 1024;
+        case 0: return k % P == 0 && k / P >= HALO_CW && halo_smem() <= 160 * 1024;
         case 1: return k >= 32 && k % P == 0 && (k / P + 31) / 32 <= 4;
         case 2: return k >= 32 && (k + 31) / 32 <= 8;
         default: return true;
         }
         (void)m;
     }
-    size_t halo_smem() const { return (size_t)mesh->d.halo_max * HALO_CW * 16; }
+    size_t halo_smem() const
+    {
+        return (size_t)mesh->d.halo_max * HALO_CW * 16 + (size_t)HALO_MAXE * (sizeof(V) + sizeof(unsigned short));
+    }
 
     void spmm_launch(int var, int k, const V* x, V* y, const V* wv, bool n2, ColState* cst, double* pt, int np)
     {
@@ -214,8 +228,9 @@ struct Engine {
                                              (int)halo_smem()));
                 halo_attr = true;
             }
-            launch(spmm_halo_kernel<V>, ntiles(), 256, halo_smem(), st, m.n, m.rowptr, m.lcol, m.halo_ptr,
-                   m.halo_col, A, k, k, x, y, wv, n2, pt, np, ntiles(), cst);
+            const unsigned nch = cdiv_u(k / P, HALO_CW);
+            launch(spmm_halo_kernel<V>, dim3(ntiles(), nch), 256, halo_smem(), st, m.n, m.rowptr, m.lcol, m.halo_ptr,
+                   m.halo_col, A, k, k, x, y, wv, n2, pt, np, ntiles(), cst, m.halo_max);
             return;
         }
         case 1: {
@@ -264,25 +279,40 @@ struct Engine {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         TG_CUDA(cudaStreamIsCapturing(st, &cs));
         if (cands.size() == 1 || cs != cudaStreamCaptureStatusNone) return cands[0];
-        cudaEvent_t e0, e1;
-        TG_CUDA(cudaEventCreate(&e0));
-        TG_CUDA(cudaEventCreate(&e1));
-        int best = cands[0];
-        float best_ms = 1e30f;
-        for (int v : cands) {
-            spmm_launch(v, k, x, y, wv, n2, cst, pt, np);  // warm-up
-            TG_CUDA(cudaEventRecord(e0, st));
-            for (int r = 0; r < 3; r++) spmm_launch(v, k, x, y, wv, n2, cst, pt, np);
-            TG_CUDA(cudaEventRecord(e1, st));
-            TG_CUDA(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            TG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            if (ms < best_ms) { best_ms = ms; best = v; }
-        }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        // every candidate: one warm-up launch, then the best of three timed
+        // launches, in two rounds of alternating order
+        std::vector<cudaEvent_t> ev(2);
+        for (auto& e : ev) TG_CUDA(cudaEventCreate(&e));
+        std::vector<float> best_ms(cands.size(), 1e30f);
+        for (size_t i = 0; i < cands.size(); i++) spmm_launch(cands[i], k, x, y, wv, n2, cst, pt, np);
+        for (int round = 0; round < 2; round++)
+            for (size_t j = 0; j < cands.size(); j++) {
+                const size_t i = round ? cands.size() - 1 - j : j;
+                for (int r = 0; r < 3; r++) {
+                    TG_CUDA(cudaEventRecord(ev[0], st));
+                    spmm_launch(cands[i], k, x, y, wv, n2, cst, pt, np);
+                    TG_CUDA(cudaEventRecord(ev[1], st));
+                    TG_CUDA(cudaEventSynchronize(ev[1]));
+                    float ms = 0.f;
+                    TG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+                    best_ms[i] = std::min(best_ms[i], ms);
+                }
+            }
+        for (auto& e : ev) cudaEventDestroy(e);
+        size_t bi = 0;
+        for (size_t i = 1; i < cands.size(); i++)
+            if (best_ms[i] < best_ms[bi]) bi = i;
         std::lock_guard<std::mutex> g(g_tune_mu);
-        return g_tune.emplace(key, best).first->second;
+        auto res = g_tune.emplace(key, cands[bi]);
+        if (res.second) {
+            char line[256];
+            int o = snprintf(line, sizeof line, "mesh %lld %s k=%d:", std::get<0>(key), vt_name<V>(), k);
+            for (size_t i = 0; i < cands.size(); i++)
+                o += snprintf(line + o, sizeof line - o, " %s %.1fus", spmm_name(cands[i]), best_ms[i] * 1e3f);
+            snprintf(line + o, sizeof line - o, " -> %s\n", spmm_name(cands[bi]));
+            g_tune_log += line;
+        }
+        return res.first->second;
     }
 
     void spmm(int k, const V* x, V* y, const V* wv, bool n2, ColState* cst, double* pt, int np)
@@ -815,7 +845,7 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
     e64.template finalize<1>(k, co, PH_RESID);
     launch(rel_init_kernel, ek, 128, 0, s->stream, k, co, ci, s->inner_tol, maxit);
     V32* Rw = e32.vec(0, nk);
-    launch(cast_kernel<V32, V64>, eg, 256, 0, s->stream, nk, R, Rw);
+    launch(rel_scaled_cast_kernel<V64, V32>, eg, 256, 0, s->stream, n, k, ci, R, Rw);
     TG_CUDA(cudaMemsetAsync(X32, 0, nk * sizeof(V32), s->stream));
     e32.bicg_begin(k, ci);
     V32 *RD = e32.vec(1, nk), *P = e32.vec(2, nk), *Vv = e32.vec(4, nk);
@@ -856,7 +886,7 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
 }
 
 template <class V64, class V32>
-static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co)
+static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co, bool zero_guess = false)
 {
     const MeshDev& m = s->mesh->d;
     int n = m.n;
@@ -866,7 +896,7 @@ static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co)
     Engine<V64>& e64 = engine<V64>(s);
     setup_engine(s, e64);
     if (s->precision == TG_PREC_FP64) {
-        e64.solve(s->method, k, B, X, co, false);
+        e64.solve(s->method, k, B, X, co, zero_guess);
         return;
     }
     // FP64 iterative refinement around FP32 / complex-FP32 inner solves:
@@ -885,8 +915,12 @@ static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co)
     V32* E32 = (V32*)s->X32.ensure(nk * sizeof(V32));
     ColState* ci = (ColState*)s->cs_inner.ensure(sizeof(ColState) * k);
     double* pt = e64.parts(k, 1);
-    e64.spmm(k, X, R, nullptr, false, nullptr, nullptr, 0);
-    launch(resid_kernel<V64>, cdiv_u(nk, 256), 256, 0, s->stream, n, k, k, B, R, nullptr);
+    if (zero_guess) {  // r = b: the FP64 product with x = 0 is skipped
+        TG_CUDA(cudaMemcpyAsync(R, B, nk * sizeof(V64), cudaMemcpyDeviceToDevice, s->stream));
+    } else {
+        e64.spmm(k, X, R, nullptr, false, nullptr, nullptr, 0);
+        launch(resid_kernel<V64>, cdiv_u(nk, 256), 256, 0, s->stream, n, k, k, B, R, nullptr);
+    }
     launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, B, B, nullptr, nullptr, pt, 1,
                                                                       e64.ntiles(), nullptr);
     e64.template finalize<1>(k, co, PH_BNORM);
@@ -1144,7 +1178,7 @@ static void api_forward_path(tg_solver s, const double* cmua, const double* ckap
            m.perm);
     TG_CUDA(cudaMemsetAsync(X, 0, kb, s->stream));
     ColState* co = (ColState*)s->cs_outer.ensure(sizeof(ColState) * k);
-    solve_nm<V64, V32>(s, k, B, X, co);
+    solve_nm<V64, V32>(s, k, B, X, co, true);
     if (res) read_results(s, k, co, res);
     V64* ylin = (V64*)s->fp_lin.ensure((size_t)std::max(nqm, 1) * sizeof(V64));
     V64* ylog = (V64*)s->fp_log.ensure((size_t)std::max(nqm, 1) * sizeof(V64));
@@ -1439,6 +1473,15 @@ int tg_solver_profile_read(tg_solver s, int cls, double* total_ms, int* count)
     }
     if (total_ms) *total_ms = t;
     if (count) *count = (int)s->prof.ev[cls].size();
+    API_END
+}
+
+int tg_tuner_log(char* buf, int len)
+{
+    API_BEGIN
+    TG_CHECK(buf && len > 0, TG_ERR_ARG, "invalid argument");
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    snprintf(buf, (size_t)len, "%s", g_tune_log.c_str());
     API_END
 }
 
