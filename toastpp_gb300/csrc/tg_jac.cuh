@@ -238,8 +238,8 @@ __device__ __forceinline__ void jac_pairs_c32(const cf* __restrict__ Fs, const c
         }
 }
 
-template <class V, int JQ, int JM, int JRQ, int JRM>
-__global__ void __launch_bounds__(256) jacobian_kernel(JacArgs<V> a)
+template <class V, int JQ, int JM, int JRQ, int JRM, int NT>
+__global__ void __launch_bounds__(NT) jacobian_kernel(JacArgs<V> a)
 {
     using S = typename vt<V>::R;
     static_assert(JM <= JQ, "the adjoint block shares a source buffer");

@@ -1240,4 +1240,58 @@ static __global__ void rel_finish_kernel(int k, ColState* __restrict__ co, const
     if (co[c].active == 1) { co[c].active = 0; co[c].status = 1; }
 }
 
+// the marked columns (rel != 0) as a list, in column order (one block)
+static __global__ void rel_compact_kernel(int k, const ColState* __restrict__ ci, int* __restrict__ idx,
+                                          int* __restrict__ cnt)
+{
+    __shared__ int base;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    for (int c0 = 0; c0 < k; c0 += blockDim.x) {
+        const int c = c0 + threadIdx.x;
+        const int f = (c < k && ci[c].rel) ? 1 : 0;
+        // ordered compaction of this chunk: warp ballots, then warp offsets
+        const unsigned b = __ballot_sync(0xffffffffu, f);
+        __shared__ int wcnt[32];
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        if (lane == 0) wcnt[wid] = __popc(b);
+        __syncthreads();
+        int off = base;
+        for (int w = 0; w < wid; w++) off += wcnt[w];
+        if (f) idx[off + __popc(b & ((1u << lane) - 1))] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int t = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += wcnt[w];
+            base += t;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *cnt = base;
+}
+
+// dst (n x kf) = src columns idx (n x k)
+template <class V>
+__global__ void gather_cols_kernel(int n, int k, int kf, const int* __restrict__ idx, const V* __restrict__ src,
+                                   V* __restrict__ dst)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * kf) return;
+    const size_t i = t / kf;
+    const int j = (int)(t % kf);
+    dst[t] = src[i * k + idx[j]];
+}
+
+// r[:, idx] = b[:, idx] - ax (ax: n x kf)
+template <class V>
+__global__ void scatter_resid_kernel(int n, int k, int kf, const int* __restrict__ idx, const V* __restrict__ b,
+                                     const V* __restrict__ ax, V* __restrict__ r)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * kf) return;
+    const size_t i = t / kf;
+    const int c = idx[t % kf];
+    r[i * k + c] = vsub(b[i * k + c], ax[t]);
+}
+
 }  // namespace tg

@@ -55,6 +55,28 @@ static inline void launch(void (*k)(KArgs...), dim3 g, dim3 b, size_t sm, cudaSt
     g_nlaunch.fetch_add(1, std::memory_order_relaxed);
 }
 
+// Raise a kernel's dynamic shared-memory limit to the device's opt-in
+// maximum, once per (kernel, device).  Setting it per launch to the launch's
+// own size would race between solvers (another solver's smaller setting
+// makes this launch invalid); a high limit costs no occupancy, which follows
+// the launch's actual size.
+static void allow_smem(const void* kern)
+{
+    static std::mutex mu;
+    static std::vector<std::pair<const void*, int>> done;
+    int dev = 0;
+    TG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(mu);
+    for (auto& d : done)
+        if (d.first == kern && d.second == dev) return;
+    int optin = 0;
+    TG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    TG_CUDA(cudaFuncGetAttributes(&fa, kern));
+    TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+    done.emplace_back(kern, dev);
+}
+
 enum ProfClass { PC_SPMM = 0, PC_SWEEP, PC_VEC, PC_JAC, PC_ASM, PC_PROJ, PC_N };
 
 struct Profiler {
@@ -185,7 +207,6 @@ struct Engine {
     int precon = 0;            // 0 none, 1 diag, 2 ich
     Profiler* prof = nullptr;
     DBuf w[9], part, cs, cnt, gbasis, gcol;
-    bool halo_attr = false;
     int* h_cnt = nullptr;
     GraphCache graphs;
 
@@ -223,11 +244,7 @@ struct Engine {
         constexpr int P = W16<V>::P;
         switch (var) {
         case 0: {
-            if (!halo_attr) {
-                TG_CUDA(cudaFuncSetAttribute(spmm_halo_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)halo_smem()));
-                halo_attr = true;
-            }
+            allow_smem((const void*)spmm_halo_kernel<V>);
             const unsigned nch = cdiv_u(k / P, HALO_CW);
             launch(spmm_halo_kernel<V>, dim3(ntiles(), nch), 256, halo_smem(), st, m.n, m.rowptr, m.lcol, m.halo_ptr,
                    m.halo_col, A, k, k, x, y, wv, n2, pt, np, ntiles(), cst, m.halo_max);
@@ -276,6 +293,10 @@ struct Engine {
         std::vector<int> cands;
         for (int v = 0; v < 4; v++)
             if (spmm_ok(v, k)) cands.push_back(v);
+        // FP64 products are bound by the FP64 FMA rate whatever the layout:
+        // no timing, the fixed preference (each new column count would cost
+        // the tuner seconds of FP64 work)
+        if (sizeof(typename vt<V>::R) == 8) return cands[0];
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         TG_CUDA(cudaStreamIsCapturing(st, &cs));
         if (cands.size() == 1 || cs != cudaStreamCaptureStatusNone) return cands[0];
@@ -673,7 +694,7 @@ struct tg_solver_s {
     DBuf jF, jG, jpair, jyinv, plink_q, plink_m, psup, pnsup, pflag, pMsup, plin, plog;
     DBuf fp_bq, fp_xq, fp_bm, fp_xm, fp_lin, fp_log;
     DBuf jwm64, jwk64, jwm32, jwk32;  // per-node element weights of the Jacobian (geometry only)
-    DBuf rel_cnt;
+    DBuf rel_cnt, rel_idx, rel_xc, rel_ac;
     int jw_D = 0, jw_ready = 0;       // slots per node; bit 0 FP64 weights built, bit 1 FP32
     Profiler prof;
     GraphCache graphs;
@@ -868,8 +889,23 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
         launch(rel_mark_kernel, ek, 128, 0, s->stream, k, co, ci);
         if (at_limit) launch(rel_mark_all_kernel, ek, 128, 0, s->stream, k, co, ci);
         launch(rel_accumulate_kernel<V64, V32>, eg, 256, 0, s->stream, n, k, ci, X, X32);
-        e64.spmm(k, X, R, nullptr, false, nullptr, nullptr, 0);
-        launch(resid_kernel<V64>, eg, 256, 0, s->stream, n, k, k, B, R, nullptr);
+        // the FP64 product (FP64-FMA bound on this part) only for the marked columns
+        int* idx = (int*)s->rel_idx.ensure((size_t)(k + 1) * sizeof(int));
+        launch(rel_compact_kernel, 1, 256, 0, s->stream, k, ci, idx, dcnt + 3);
+        TG_CUDA(cudaMemcpyAsync(hc + 3, dcnt + 3, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+        TG_CUDA(cudaStreamSynchronize(s->stream));
+        const int kf = hc[3];
+        if (kf == k) {
+            e64.spmm(k, X, R, nullptr, false, nullptr, nullptr, 0);
+            launch(resid_kernel<V64>, eg, 256, 0, s->stream, n, k, k, B, R, nullptr);
+        } else if (kf > 0) {
+            const size_t nkf = (size_t)n * kf;
+            V64* Xc = (V64*)s->rel_xc.ensure(nkf * sizeof(V64));
+            V64* Ac = (V64*)s->rel_ac.ensure(nkf * sizeof(V64));
+            launch(gather_cols_kernel<V64>, cdiv_u(nkf, 256), 256, 0, s->stream, n, k, kf, idx, X, Xc);
+            e64.spmm(kf, Xc, Ac, nullptr, false, nullptr, nullptr, 0);
+            launch(scatter_resid_kernel<V64>, cdiv_u(nkf, 256), 256, 0, s->stream, n, k, kf, idx, B, Ac, R);
+        }
         launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, R, R, nullptr, nullptr, pt,
                1, e64.ntiles(), nullptr);
         e64.template finalize<1>(k, co, PH_RESID);
@@ -1018,7 +1054,7 @@ static const S* jac_weights(tg_solver s, int which)
     }
 }
 
-template <class VC, int JQ, int JM, int JRQ, int JRM>
+template <class VC, int JQ, int JM, int JRQ, int JRM, int NT = 256>
 static bool try_launch_jacobian(tg_solver s, JacArgs<VC> a)
 {
     const MeshDev& m = s->mesh->d;
@@ -1026,12 +1062,12 @@ static bool try_launch_jacobian(tg_solver s, JacArgs<VC> a)
     const size_t smem = (size_t)(2 * JM + 2 * JQ) * SP * sizeof(VC) + (size_t)a.nq * JM * (sizeof(VC) + sizeof(int)) +
                         (size_t)D * JKT * sizeof(int);
     if (smem > 227 * 1024) return false;
-    auto kern = jacobian_kernel<VC, JQ, JM, JRQ, JRM>;
-    TG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    auto kern = jacobian_kernel<VC, JQ, JM, JRQ, JRM, NT>;
+    allow_smem((const void*)kern);
     a.D = D; a.SP = SP; a.nmc = (int)cdiv_u(a.nm, JM);
     const size_t nblk = (size_t)cdiv_u(m.n, JKT) * a.nmc;
     ProfScope ps(&s->prof, PC_JAC, s->stream);
-    launch(kern, (unsigned)nblk, 256, smem, s->stream, a);
+    launch(kern, (unsigned)nblk, NT, smem, s->stream, a);
     return true;
 }
 
@@ -1047,6 +1083,9 @@ static void launch_jacobian(tg_solver s, int nq, const VC* F, int ldf, int nm, c
     a.pairidx = s->jpair.as<int>(); a.yinv = yinv; a.J = J; a.out_fp32 = out_fp32;
     a.Wm = jac_weights<S>(s, 0);
     a.Wk = jac_weights<S>(s, 1);
+    // complex FP32: 16 warps of 2 x 2 (source, detector) pairs each
+    if constexpr (std::is_same<VC, cf>::value)
+        if (try_launch_jacobian<VC, 8, 8, 2, 2, 512>(s, a)) return;
     if constexpr (sizeof(VC) <= 8)
         if (try_launch_jacobian<VC, 8, 8, 2, 4>(s, a)) return;
     if (try_launch_jacobian<VC, 4, 4, 1, 2>(s, a)) return;

@@ -75,7 +75,8 @@ def make_requests(ms: MeshSet, spec: StreamSpec):
         k = int(rng.choice(keys, p=w))
         name, P, gm, bnd = ms.items[k]
         smax = spec.src_max_large if name.startswith("c3") else spec.src_max
-        ns = int(rng.integers(spec.src_min, smax + 1))
+        # sources and detectors at distinct boundary nodes (a small mesh caps the count)
+        ns = min(int(rng.integers(spec.src_min, smax + 1)), len(bnd) // 2)
         freq = 100.0 if rng.uniform() < 0.5 else 0.0
         mua, mus, nref = fresh_params(P, rng)
         cm, ck, ca = capi.optical_coefficients(mua, mus, nref)
