@@ -64,8 +64,8 @@ def parse():
     ap.add_argument("--inner-tol", type=float, default=1e-4, help="mixed path: inner FP32 solve tolerance")
     ap.add_argument("--inner-order", type=int, default=1, help="mixed path: inner IC(0) ordering, 1 colour, 0 natural")
     ap.add_argument("--no-compare", action="store_true", help="skip the FP64 comparison legs")
-    ap.add_argument("--no-reliable", action="store_true",
-                    help="mixed path: restarted refinement instead of reliable updates")
+    ap.add_argument("--inner", default="cocg", choices=["cocg", "bicgstab", "restart"],
+                    help="mixed path: FP32 inner process (reliable updates of COCG or BiCGSTAB, or restarts)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--serving", action="store_true",
                     help="run the mixed-mesh request stream through the request server instead")
@@ -255,7 +255,7 @@ def run_gpu(args):
     s.set_stream(stream.cuda_stream)
     if args.precision == "mixed":
         s.set_refinement(args.inner_tol, 12, args.inner_order)
-        s.set_reliable_updates(not args.no_reliable)
+        s.set_reliable_updates({"restart": 0, "bicgstab": 1, "cocg": 2}[args.inner])
     res = (capi.TgResult * (nq + nm))()
 
     def step():
@@ -430,6 +430,7 @@ def run_gpu(args):
             "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
             "jacobians_per_s": ws * args.steps / (total_ms / 1e3),
             "iterations_per_source": float(np.mean(its)),
+            "ic_applies_per_request": prof[capi.PROF_SWEEP][1] / psteps,
             "roofline": roof, "kernel_time_per_step": shares,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
             "clocks": clocks, "wall_s": wall, "compare": compare,
@@ -463,6 +464,12 @@ def run_serving(args):
         done, st, wall = serving.run_stream(reqs, slots=args.slots)
         out[prec] = serving.summarize(done, st, wall)
         del reqs, done
+        # the same requests all arriving at once: the server's capacity
+        sat = serving.make_requests(ms, serving.StreamSpec(requests=args.requests, rate_hz=1e6, seed=1,
+                                                           precision=prec, tol=1e-10))
+        done, st, wall = serving.run_stream(sat, slots=args.slots)
+        out[prec + "_saturated"] = serving.summarize(done, st, wall)
+        del sat, done
     m = out["mixed"]
     line = {"metric": "serving stream: source-solves/s with p50/p99 request latency", "value": m["solves_per_s"],
             "unit": "source-solves/s", "n_gpus": 1, "steps": args.requests, "warmup": 8, "higher_is_better": True,
@@ -472,7 +479,8 @@ def run_serving(args):
                                    "(0.4/0.3/0.2/0.1), 8-128 sources (<=32 on the 250k box), CW or 100 MHz, "
                                    "forward + projections + nodal Jacobian per request, tol 1e-10",
                        "slots": args.slots},
-            "latency_ms": {"p50": m["p50_ms"], "p99": m["p99_ms"]}, "mixed": m, "fp64": out["fp64"]}
+            "latency_ms": {"p50": m["p50_ms"], "p99": m["p99_ms"]}, "mixed": m, "fp64": out["fp64"],
+            "saturated": {"mixed": out["mixed_saturated"], "fp64": out["fp64_saturated"]}}
     print(json.dumps(line), flush=True)
     return 0
 

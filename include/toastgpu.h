@@ -111,12 +111,19 @@ int tg_solver_set(tg_solver s, double tol, int maxit);
    The FP64 path always factors in the natural ordering.  Takes effect at the
    next tg_solver_reset. */
 int tg_solver_set_refinement(tg_solver s, double inner_tol, int max_outer, int inner_ordering);
-/* mixed precision with BiCGSTAB: on (default) keeps ONE FP32 Krylov process
-   per right-hand side and replaces its residual by the FP64 residual
-   b - A x whenever the recursive residual has fallen by inner_tol (reliable
-   updates), instead of restarting an FP32 solve every refinement step (off).
-   At most 4 * max_outer updates. */
-int tg_solver_set_reliable_updates(tg_solver s, int on);
+/* mixed precision with BiCGSTAB requested: how the FP32 inner work runs.
+   0: restarted refinement (a new FP32 BiCGSTAB solve per FP64 step);
+   1: ONE FP32 BiCGSTAB process per right-hand side whose residual is replaced
+      by the FP64 residual b - A x whenever it has fallen by inner_tol
+      (reliable updates);
+   2 (default): as 1 with an FP32 COCG process for complex systems (the
+      conjugate-orthogonal CG of the complex symmetric F: one SpMM and one
+      IC(0) apply per iteration); real systems use 1.
+   The FP64 result meets tol in every mode.  At most 4 * max_outer updates. */
+#define TG_MIXED_RESTART 0
+#define TG_MIXED_RELIABLE_BICGSTAB 1
+#define TG_MIXED_RELIABLE_COCG 2
+int tg_solver_set_reliable_updates(tg_solver s, int mode);
 /* a cudaStream_t; 0 selects the solver's own stream */
 int tg_solver_set_stream(tg_solver s, void *stream);
 int tg_solver_sync(tg_solver s);

@@ -117,6 +117,25 @@ def test_calc_fields_mixed(case, oracle_mod, method):
     assert all(r[1] == 0 for r in res), res
 
 
+@pytest.mark.parametrize("mode", [0, 1, 2], ids=["restart", "reliable_bicgstab", "reliable_cocg"])
+def test_mixed_inner_modes(case, oracle_mod, mode):
+    """Every FP32 inner scheme of the mixed path (restarted refinement, reliable
+    updates of BiCGSTAB or of COCG) reaches the FP64 oracle's fields."""
+    P, om, gm = case
+    cm, ck, ca, qvec, mvec = gpu_problem_inputs(P, gm)
+    omega = capi.omega_of(P.freq_mhz)
+    s = capi.FwdSolver(gm, "BICGSTAB", 1e-12, "ICH", P.complex, precision="mixed")
+    s.set_reliable_updates(mode)
+    s.reset(cm, ck, ca, omega)
+    B = np.concatenate([qvec, mvec])
+    phi, res = s.calc_fields(B)
+    val = om.assemble(cm, ck, ca, omega, P.complex)
+    Xr, its, errs = oracle_mod.solve(om.rowptr, om.colidx, val, B.astype(phi.dtype), "BICGSTAB", "ICH", 1e-13)
+    assert rel2(phi, Xr) < 1e-10
+    assert all(r[1] == 0 for r in res), res
+    assert all(r[2] <= 1e-12 for r in res), res
+
+
 def test_project_and_jacobian(case, oracle_mod):
     P, om, gm = case
     cm, ck, ca, qvec, mvec = gpu_problem_inputs(P, gm)

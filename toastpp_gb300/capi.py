@@ -232,8 +232,9 @@ class FwdSolver:
     def set_refinement(self, inner_tol, max_outer=12, inner_ordering=1):
         _check(lib().tg_solver_set_refinement(self._h, float(inner_tol), int(max_outer), int(inner_ordering)))
 
-    def set_reliable_updates(self, on=True):
-        _check(lib().tg_solver_set_reliable_updates(self._h, int(bool(on))))
+    def set_reliable_updates(self, mode=2):
+        """0 restarted refinement, 1 reliable-update BiCGSTAB, 2 reliable-update COCG (complex)."""
+        _check(lib().tg_solver_set_reliable_updates(self._h, int(mode)))
 
     def set_tol(self, tol, maxit=0):
         _check(lib().tg_solver_set(self._h, float(tol), int(maxit)))

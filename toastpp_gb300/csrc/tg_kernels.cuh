@@ -22,6 +22,8 @@ struct ColState {
     // mixed path: the FP32 process works on (true residual) / scale, a power
     // of two of the last true residual norm, so its values stay O(1)
     double scale, scale_prev;
+    // COCG (complex symmetric CG) scalars, complex: rho = r.z, alpha, beta
+    double zr, zi, ar, ai, br, bi;
 };
 
 // 2^floor(log2 x) for x > 0 finite, else 1: scaling by it is exact
@@ -235,9 +237,11 @@ struct TileAcc {
 // y-dots of a tile: part0 = sum Re(conj(w) y) (w != null), part1 = sum |y|^2
 template <class V>
 __device__ __forceinline__ void tile_dots(int r0, int r1, int k, int ld, const V* __restrict__ y,
-                                          const V* __restrict__ w, bool want_n2, double* __restrict__ part, int np,
+                                          const V* __restrict__ w, int want_n2, double* __restrict__ part, int np,
                                           int ntiles, int tile, const ColState* __restrict__ st, int cbeg = 0)
 {
+    // want_n2: 0 -> [Re(conj(w) y)], 1 -> [Re(conj(w) y)], |y|^2 (the first
+    // only with w), 2 -> the bilinear w.y as [Re, Im] (COCG)
     // columns [cbeg, k) of the tile (a block that owns a column range passes
     // its range; the per-column order is the same)
     __shared__ double sh[2 * TILE_RG * TILE_CK];
@@ -251,6 +255,12 @@ __device__ __forceinline__ void tile_dots(int r0, int r1, int k, int ld, const V
 #pragma unroll 4
                 for (int r = r0 + g; r < r1; r += TILE_RG) {
                     V yv = y[(size_t)r * ld + c];
+                    if (want_n2 == 2) {
+                        const V pr = vmul(w[(size_t)r * ld + c], yv);
+                        d0 += (double)re(pr);
+                        d1 += (double)im(pr);
+                        continue;
+                    }
                     if (w) d0 += (double)redot(w[(size_t)r * ld + c], yv);
                     if (want_n2) d1 += (double)nrm2(yv);
                 }
@@ -261,6 +271,11 @@ __device__ __forceinline__ void tile_dots(int r0, int r1, int k, int ld, const V
         for (int cc = threadIdx.x; cc < ck; cc += blockDim.x) {
             const int c = c0 + cc;
             if (st && st[c].active != 1) continue;
+            if (want_n2 == 2) {
+                part[((size_t)c * np) * ntiles + tile] = T.sum(0, cc);
+                part[((size_t)c * np + 1) * ntiles + tile] = T.sum(1, cc);
+                continue;
+            }
             int p = 0;
             if (w) part[((size_t)c * np + p++) * ntiles + tile] = T.sum(0, cc);
             if (want_n2) part[((size_t)c * np + p) * ntiles + tile] = T.sum(1, cc);
@@ -325,7 +340,7 @@ template <class V, int NJ>
 __global__ void __launch_bounds__(256) spmm_wide_kernel(int n, const int* __restrict__ rowptr,
                                                         const int* __restrict__ colidx, const V* __restrict__ A, int k,
                                                         int ld, const V* __restrict__ x, V* __restrict__ y,
-                                                        const V* __restrict__ w, bool want_n2, double* __restrict__ part,
+                                                        const V* __restrict__ w, int want_n2, double* __restrict__ part,
                                                         int np, int ntiles, const ColState* __restrict__ st)
 {
     const int tile = blockIdx.x;
@@ -362,7 +377,7 @@ template <class V, int NW>
 __global__ void __launch_bounds__(256) spmm_vec_kernel(int n, const int* __restrict__ rowptr,
                                                        const int* __restrict__ colidx, const V* __restrict__ A, int k,
                                                        int ld, const V* __restrict__ x, V* __restrict__ y,
-                                                       const V* __restrict__ w, bool want_n2,
+                                                       const V* __restrict__ w, int want_n2,
                                                        double* __restrict__ part, int np, int ntiles,
                                                        const ColState* __restrict__ st)
 {
@@ -467,7 +482,7 @@ __global__ void __launch_bounds__(256) spmm_halo_kernel(int n, const int* __rest
                                                         const int* __restrict__ halo_ptr,
                                                         const int* __restrict__ halo_col, const V* __restrict__ A,
                                                         int k, int ld, const V* __restrict__ x, V* __restrict__ y,
-                                                        const V* __restrict__ w, bool want_n2,
+                                                        const V* __restrict__ w, int want_n2,
                                                         double* __restrict__ part, int np, int ntiles,
                                                         const ColState* __restrict__ st, int hmax)
 {
@@ -618,7 +633,7 @@ __global__ void ell_gather_kernel(int cnt, const int* __restrict__ src, const V*
 template <class V>
 __global__ void spmm_dot_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ colidx,
                                 const V* __restrict__ A, int k, int ld, const V* __restrict__ x,
-                                V* __restrict__ y, const V* __restrict__ w, bool want_n2,
+                                V* __restrict__ y, const V* __restrict__ w, int want_n2,
                                 double* __restrict__ part, int np, int ntiles, const ColState* __restrict__ st)
 {
     int tile = blockIdx.x;
@@ -661,6 +676,13 @@ __global__ void spmv1_kernel(int n, const int* __restrict__ rowptr, const int* _
 // ---------------------------------------------------------------------------
 
 
+// a value from (re, im) (the imaginary part is dropped for real types)
+template <class V> __device__ __forceinline__ V vmake(double re_, double im_);
+template <> __device__ __forceinline__ double vmake<double>(double re_, double) { return re_; }
+template <> __device__ __forceinline__ float vmake<float>(double re_, double) { return (float)re_; }
+template <> __device__ __forceinline__ cd vmake<cd>(double re_, double im_) { return cd{re_, im_}; }
+template <> __device__ __forceinline__ cf vmake<cf>(double re_, double im_) { return cf{(float)re_, (float)im_}; }
+
 enum Phase : int {
     PH_BNORM = 0,        // part0 = |b|^2 -> bnorm; (re)activate
     PH_BICG_RHO0,        // part0 = rd.r  -> rho (iteration 0)
@@ -673,6 +695,10 @@ enum Phase : int {
     PH_PCG_END,          // part0 = r.q (dnew), part1 = |r|^2 -> beta, err, convergence
     PH_RESID,            // part0 = |r|^2 -> err (refinement residual)
     PH_REL_RESUME,       // part0 = rd.r after a residual replacement -> rho, beta; reactivate
+    PH_COCG_RHO0,        // part0 + i part1 = r.z (bilinear) -> rho
+    PH_COCG_ALPHA,       // part0 + i part1 = p.q -> alpha = rho / (p.q)
+    PH_COCG_RES,         // part0 = |r|^2 -> err, convergence
+    PH_COCG_BETA,        // part0 + i part1 = r.z -> beta = rho' / rho, rho = rho'
 };
 
 template <int NP>
@@ -760,6 +786,38 @@ __global__ void reduce_finalize_kernel(int k, int ntiles, const double* __restri
     case PH_RESID:
         S.err = sqrt(v0);
         break;
+    case PH_COCG_RHO0:
+        if (S.active != 1) break;
+        S.zr = v0; S.zi = v1;
+        if (v0 == 0.0 && v1 == 0.0) { S.active = 0; S.status = 2; }
+        break;
+    case PH_COCG_ALPHA: {
+        if (S.active != 1) break;
+        const cd a = cdiv(cd{S.zr, S.zi}, cd{v0, v1});
+        S.ar = a.x; S.ai = a.y;
+        if (!isfinite(a.x) || !isfinite(a.y)) { S.active = 0; S.status = 2; }
+        break;
+    }
+    case PH_COCG_RES:
+        if (S.active != 1) break;
+        S.err = sqrt(v0);
+        S.its++;
+        if (S.err <= S.tol * S.bnorm) { S.active = 0; S.status = 0; break; }
+        if (S.its >= S.maxit) { S.active = 0; S.status = 1; }
+        break;
+    case PH_COCG_BETA: {
+        if (S.active != 1) break;
+        if (S.rel == 2) {  // restarted process: p = z
+            S.br = 0.0; S.bi = 0.0;
+        } else {
+            const cd b = cdiv(cd{v0, v1}, cd{S.zr, S.zi});
+            S.br = b.x; S.bi = b.y;
+        }
+        S.rel = 0;
+        S.zr = v0; S.zi = v1;
+        if ((v0 == 0.0 && v1 == 0.0) || !isfinite(S.br) || !isfinite(S.bi)) { S.active = 0; S.status = 2; }
+        break;
+    }
     case PH_REL_RESUME:
         // the replaced residual continues the same BiCGSTAB process
         // (rel 1: the END step's rho / beta update with the new r) or
@@ -1193,7 +1251,8 @@ __global__ void rel_accumulate_kernel(int n, int k, const ColState* __restrict__
 // after |b - A x| of the marked columns is in co.err: converged columns stop,
 // the others restart their trigger from the new residual; at the update or
 // iteration limit every active column stops with status 1
-static __global__ void rel_outer_kernel(int k, ColState* __restrict__ co, ColState* __restrict__ ci, int limit)
+static __global__ void rel_outer_kernel(int k, ColState* __restrict__ co, ColState* __restrict__ ci, int limit,
+                                        int cocg)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= k) return;
@@ -1206,7 +1265,9 @@ static __global__ void rel_outer_kernel(int k, ColState* __restrict__ co, ColSta
     I.scale_prev = I.scale;
     I.scale = pow2_floor(O.err);
     I.bnorm = O.err / I.scale;
-    I.rho *= I.scale_prev / I.scale;
+    const double f = I.scale_prev / I.scale;
+    if (cocg) { I.zr *= f * f; I.zi *= f * f; }  // r.z: both factors rescale
+    else I.rho *= f;                             // rd.r: rd stays
 }
 
 // the marked columns take the true residual; restarted columns also reset the
@@ -1223,12 +1284,15 @@ __global__ void rel_replace_kernel(int n, int k, const ColState* __restrict__ ci
     if (!rel) return;
     const V32 x = vcast<V32, V64>(vscale(r64[t], 1.0 / ci[c].scale));
     r[t] = x;
-    if (rel == 2) { rd[t] = x; p[t] = vzero<V32>(); v[t] = vzero<V32>(); }
-    else {
+    if (rel == 2) {
+        if (rd) rd[t] = x;
+        p[t] = vzero<V32>();
+        if (v) v[t] = vzero<V32>();
+    } else {
         using S32 = typename vt<V32>::R;
         const S32 f = (S32)(ci[c].scale_prev / ci[c].scale);
         p[t] = vscale(p[t], f);
-        v[t] = vscale(v[t], f);
+        if (v) v[t] = vscale(v[t], f);
     }
 }
 
@@ -1292,6 +1356,81 @@ __global__ void scatter_resid_kernel(int n, int k, int kf, const int* __restrict
     const size_t i = t / kf;
     const int c = idx[t % kf];
     r[i * k + c] = vsub(b[i * k + c], ax[t]);
+}
+
+// ---------------------------------------------------------------------------
+// COCG, the conjugate-orthogonal CG for complex symmetric A = A^T with a
+// complex symmetric preconditioner (IC(0): M = L~ L~^T): CG with the bilinear
+// product x.y = sum x_i y_i in place of the inner product, one SpMM and one
+// preconditioner apply per iteration.  Used as the FP32 inner process of the
+// mixed path for complex systems.
+// ---------------------------------------------------------------------------
+// x += alpha p, r -= alpha q on the active columns, |r|^2 partials
+template <class V>
+__global__ void cocg_xr_kernel(int n, int k, int ld, const ColState* __restrict__ st, V* __restrict__ x,
+                               V* __restrict__ r, const V* __restrict__ p, const V* __restrict__ q,
+                               double* __restrict__ part, int ntiles)
+{
+    __shared__ double sh[2 * TILE_RG * TILE_CK];
+    TileAcc T{sh};
+    const int tile = blockIdx.x;
+    const int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    for (int c0 = 0; c0 < k; c0 += TILE_CK) {
+        const int ck = min(TILE_CK, k - c0);
+        for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
+            const int cc = it % ck, g = it / ck, c = c0 + cc;
+            double acc = 0.0;
+            if (st[c].active == 1) {
+                const V a = vmake<V>(st[c].ar, st[c].ai);
+#pragma unroll 4
+                for (int i = r0 + g; i < r1; i += TILE_RG) {
+                    const size_t o = (size_t)i * ld + c;
+                    x[o] = vfma(x[o], a, p[o]);
+                    const V rv = vfms(r[o], a, q[o]);
+                    r[o] = rv;
+                    acc += (double)nrm2(rv);
+                }
+            }
+            T.put(0, g, cc, acc);
+        }
+        __syncthreads();
+        for (int cc = threadIdx.x; cc < ck; cc += blockDim.x)
+            if (st[c0 + cc].active == 1) part[(size_t)(c0 + cc) * ntiles + tile] = T.sum(0, cc);
+        __syncthreads();
+    }
+}
+
+// p = z (first) or p = z + beta p on the active columns
+template <class V>
+__global__ void cocg_p_kernel(int n, int k, int ld, const ColState* __restrict__ st, int first,
+                              const V* __restrict__ z, V* __restrict__ p)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * k) return;
+    const int c = (int)(t % k);
+    if (st[c].active != 1) return;
+    const size_t o = (t / k) * ld + c;
+    p[o] = first ? z[o] : vfma(z[o], vmake<V>(st[c].br, st[c].bi), p[o]);
+}
+
+// reactivate the columns that took a residual replacement (COCG continues
+// with z = M r, beta and p; a restart keeps rel = 2 until the beta step)
+static __global__ void rel_reactivate_kernel(int k, ColState* __restrict__ ci)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k || !ci[c].rel) return;
+    ci[c].active = 1;
+    ci[c].status = 0;
+}
+
+// bilinear column products sum a_i b_i (no conjugation) as [Re, Im] tile partials
+template <class V>
+__global__ void bdot_tiles_kernel(int n, int k, int ld, const V* __restrict__ a, const V* __restrict__ b,
+                                  double* __restrict__ part, int ntiles, const ColState* __restrict__ st)
+{
+    const int tile = blockIdx.x;
+    const int r0 = tile * ROW_TILE, r1 = min(n, r0 + ROW_TILE);
+    tile_dots<V>(r0, r1, k, ld, b, a, 2, part, 2, ntiles, tile, st);
 }
 
 }  // namespace tg

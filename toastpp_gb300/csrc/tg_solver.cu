@@ -238,7 +238,7 @@ struct Engine {
         return (size_t)mesh->d.halo_max * HALO_CW * 16 + (size_t)HALO_MAXE * (sizeof(V) + sizeof(unsigned short));
     }
 
-    void spmm_launch(int var, int k, const V* x, V* y, const V* wv, bool n2, ColState* cst, double* pt, int np)
+    void spmm_launch(int var, int k, const V* x, V* y, const V* wv, int n2, ColState* cst, double* pt, int np)
     {
         const MeshDev& m = mesh->d;
         constexpr int P = W16<V>::P;
@@ -282,7 +282,7 @@ struct Engine {
     // fastest for the rest of the process (all solvers share the choice, so a
     // result never depends on which solver ran it).  Under stream capture the
     // fixed preference order is used instead.
-    int spmm_variant(int k, const V* x, V* y, const V* wv, bool n2, ColState* cst, double* pt, int np)
+    int spmm_variant(int k, const V* x, V* y, const V* wv, int n2, ColState* cst, double* pt, int np)
     {
         const auto key = std::make_tuple(mesh->uid, (int)sizeof(V) * 2 + (int)vt<V>::cplx, k);
         {
@@ -336,7 +336,7 @@ struct Engine {
         return res.first->second;
     }
 
-    void spmm(int k, const V* x, V* y, const V* wv, bool n2, ColState* cst, double* pt, int np)
+    void spmm(int k, const V* x, V* y, const V* wv, int n2, ColState* cst, double* pt, int np)
     {
         const int var = spmm_variant(k, x, y, wv, n2, cst, pt, np);
         ProfScope ps(prof, PC_SPMM, st);
@@ -539,6 +539,45 @@ struct Engine {
         }
     }
 
+    // COCG (the FP32 inner process of the mixed path for complex systems):
+    // R = vec(0) filled by the caller, Z = vec(1), P = vec(2), Q = vec(3)
+    void cocg_begin(int k, ColState* cst)
+    {
+        const MeshDev& m = mesh->d;
+        size_t nk = (size_t)m.n * k;
+        V *R = vec(0, nk), *Z = vec(1, nk), *P = vec(2, nk);
+        vec(3, nk);
+        double* pt = parts(k, 2);
+        precon_apply(k, R, Z, cst);
+        launch(bdot_tiles_kernel<V>, ntiles(), rowblk(k), 0, st, m.n, k, k, R, Z, pt, ntiles(), cst);
+        finalize<2>(k, cst, PH_COCG_RHO0);
+        launch(cocg_p_kernel<V>, cdiv_u(nk, 256), 256, 0, st, m.n, k, k, cst, 1, Z, P);
+    }
+    // q = A p, alpha, x += alpha p, r -= alpha q, |r|
+    void cocg_step1(int k, V* X, ColState* cst)
+    {
+        const MeshDev& m = mesh->d;
+        size_t nk = (size_t)m.n * k;
+        V *R = vec(0, nk), *P = vec(2, nk), *Q = vec(3, nk);
+        double* pt = parts(k, 2);
+        spmm(k, P, Q, P, 2, cst, pt, 2);
+        finalize<2>(k, cst, PH_COCG_ALPHA);
+        launch(cocg_xr_kernel<V>, ntiles(), rowblk(k), 0, st, m.n, k, k, cst, X, R, P, Q, pt, ntiles());
+        finalize<1>(k, cst, PH_COCG_RES);
+    }
+    // z = M r, beta = r.z / rho, p = z + beta p
+    void cocg_step2(int k, ColState* cst)
+    {
+        const MeshDev& m = mesh->d;
+        size_t nk = (size_t)m.n * k;
+        V *R = vec(0, nk), *Z = vec(1, nk), *P = vec(2, nk);
+        double* pt = parts(k, 2);
+        precon_apply(k, R, Z, cst);
+        launch(bdot_tiles_kernel<V>, ntiles(), rowblk(k), 0, st, m.n, k, k, R, Z, pt, ntiles(), cst);
+        finalize<2>(k, cst, PH_COCG_BETA);
+        launch(cocg_p_kernel<V>, cdiv_u(nk, 256), 256, 0, st, m.n, k, k, cst, 0, Z, P);
+    }
+
     // BiCGSTAB (src/libmath/matrix_imp.hpp:350-413 complex, 479-547 real):
     // bicg_begin after R = b - A x; bicg_iter once per iteration
     void bicg_begin(int k, ColState* cst)
@@ -681,7 +720,8 @@ struct tg_solver_s {
     double inner_tol = 1e-4;   // mixed path: relative tolerance of each FP32 inner solve
     int max_outer = 12;        // mixed path: refinement steps
     int inner_colour = 1;      // mixed path: IC(0) of the inner solves in the colour-major ordering
-    int reliable = 1;          // mixed BiCGSTAB: reliable updates (1) or restarted refinement (0)
+    int reliable = 2;          // mixed BiCGSTAB: 0 restarted refinement, 1 reliable updates of an FP32
+                               // BiCGSTAB, 2 reliable updates of an FP32 COCG (complex; real: BiCGSTAB)
     cudaStream_t stream = 0, own = 0;
     bool reset_done = false;
     DBuf val64, val32, L64, L32, dinv64, dinv32, idiag64, idiag32, params;
@@ -846,15 +886,17 @@ static void upload_async(tg_solver s, DBuf& b, const std::vector<T>& v)
 // core steps on device data (node-major n x k blocks)
 // ---------------------------------------------------------------------------
 // Solve F X = B for k right-hand sides; X holds the initial guess.
-// Mixed-precision BiCGSTAB with reliable updates: one FP32 Krylov process per
-// column that is never restarted; whenever its recursive residual has fallen
-// by inner_tol below the last true residual, the FP32 correction goes into the
-// FP64 solution and the FP64 residual b - A x replaces the FP32 one.  The
-// update runs for the waiting columns once half of the active columns wait
-// (or none is iterating); the solve stops per column on the FP64 residual.
+// Mixed precision with reliable updates: one FP32 Krylov process per column
+// (BiCGSTAB, or COCG for complex systems) that is never restarted; whenever
+// its recursive residual has fallen by inner_tol below the last true
+// residual, the FP32 correction goes into the FP64 solution and the FP64
+// residual b - A x replaces the FP32 one.  The update runs at every check
+// (each 4 iterations) for the columns waiting then, with the FP64 product
+// over those columns only, so no column idles behind the others; the solve
+// stops per column on the FP64 residual.
 template <class V64, class V32>
 static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* co, V64* R, V32* R32,
-                           V32* X32, ColState* ci, Engine<V64>& e64, Engine<V32>& e32, int maxit)
+                           V32* X32, ColState* ci, Engine<V64>& e64, Engine<V32>& e32, int maxit, bool cocg)
 {
     const int n = s->mesh->d.n;
     const size_t nk = (size_t)n * k;
@@ -868,55 +910,65 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
     V32* Rw = e32.vec(0, nk);
     launch(rel_scaled_cast_kernel<V64, V32>, eg, 256, 0, s->stream, n, k, ci, R, Rw);
     TG_CUDA(cudaMemsetAsync(X32, 0, nk * sizeof(V32), s->stream));
-    e32.bicg_begin(k, ci);
-    V32 *RD = e32.vec(1, nk), *P = e32.vec(2, nk), *Vv = e32.vec(4, nk);
+    if (cocg) e32.cocg_begin(k, ci);
+    else e32.bicg_begin(k, ci);
+    V32 *RD = cocg ? nullptr : e32.vec(1, nk), *P = e32.vec(2, nk), *Vv = cocg ? nullptr : e32.vec(4, nk);
     int* dcnt = (int*)s->rel_cnt.ensure(4 * sizeof(int));
     int hc[4] = {0, 0, 0, 0};
     const int max_upd = 4 * std::max(1, s->max_outer);
     int it = 0, nupd = 0;
     for (;;) {
-        e32.bicg_iter(k, X32, ci, it == 0);
+        if (cocg) e32.cocg_step1(k, X32, ci);
+        else e32.bicg_iter(k, X32, ci, it == 0);
         it++;
         const bool at_limit = it >= maxit;
-        if ((it & 3) != 0 && !at_limit) continue;
-        launch(rel_flags_kernel, 1, 256, 0, s->stream, k, co, ci, dcnt);
-        TG_CUDA(cudaMemcpyAsync(hc, dcnt, 3 * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-        TG_CUDA(cudaStreamSynchronize(s->stream));
-        const int oa = hc[0], ia = hc[1], fl = hc[2];
-        if (oa == 0) break;
-        if (!at_limit && (fl == 0 || (2 * fl < oa && ia > 0))) continue;
-        // reliable update of the waiting columns (every active one at the limit)
-        launch(rel_mark_kernel, ek, 128, 0, s->stream, k, co, ci);
-        if (at_limit) launch(rel_mark_all_kernel, ek, 128, 0, s->stream, k, co, ci);
-        launch(rel_accumulate_kernel<V64, V32>, eg, 256, 0, s->stream, n, k, ci, X, X32);
-        // the FP64 product (FP64-FMA bound on this part) only for the marked columns
-        int* idx = (int*)s->rel_idx.ensure((size_t)(k + 1) * sizeof(int));
-        launch(rel_compact_kernel, 1, 256, 0, s->stream, k, ci, idx, dcnt + 3);
-        TG_CUDA(cudaMemcpyAsync(hc + 3, dcnt + 3, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-        TG_CUDA(cudaStreamSynchronize(s->stream));
-        const int kf = hc[3];
-        if (kf == k) {
-            e64.spmm(k, X, R, nullptr, false, nullptr, nullptr, 0);
-            launch(resid_kernel<V64>, eg, 256, 0, s->stream, n, k, k, B, R, nullptr);
-        } else if (kf > 0) {
-            const size_t nkf = (size_t)n * kf;
-            V64* Xc = (V64*)s->rel_xc.ensure(nkf * sizeof(V64));
-            V64* Ac = (V64*)s->rel_ac.ensure(nkf * sizeof(V64));
-            launch(gather_cols_kernel<V64>, cdiv_u(nkf, 256), 256, 0, s->stream, n, k, kf, idx, X, Xc);
-            e64.spmm(kf, Xc, Ac, nullptr, false, nullptr, nullptr, 0);
-            launch(scatter_resid_kernel<V64>, cdiv_u(nkf, 256), 256, 0, s->stream, n, k, kf, idx, B, Ac, R);
+        if ((it & 3) == 0 || at_limit) {
+            launch(rel_flags_kernel, 1, 256, 0, s->stream, k, co, ci, dcnt);
+            TG_CUDA(cudaMemcpyAsync(hc, dcnt, 3 * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+            TG_CUDA(cudaStreamSynchronize(s->stream));
+            const int oa = hc[0], fl = hc[2];
+            if (oa == 0) break;
+            if (fl > 0 || at_limit) {
+                // reliable update of the waiting columns (every active one at the limit)
+                launch(rel_mark_kernel, ek, 128, 0, s->stream, k, co, ci);
+                if (at_limit) launch(rel_mark_all_kernel, ek, 128, 0, s->stream, k, co, ci);
+                launch(rel_accumulate_kernel<V64, V32>, eg, 256, 0, s->stream, n, k, ci, X, X32);
+                // the FP64 product (FP64-FMA bound on this part) only for the marked columns
+                int* idx = (int*)s->rel_idx.ensure((size_t)(k + 1) * sizeof(int));
+                launch(rel_compact_kernel, 1, 256, 0, s->stream, k, ci, idx, dcnt + 3);
+                TG_CUDA(cudaMemcpyAsync(hc + 3, dcnt + 3, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+                TG_CUDA(cudaStreamSynchronize(s->stream));
+                const int kf = hc[3];
+                if (kf == k) {
+                    e64.spmm(k, X, R, nullptr, 0, nullptr, nullptr, 0);
+                    launch(resid_kernel<V64>, eg, 256, 0, s->stream, n, k, k, B, R, nullptr);
+                } else if (kf > 0) {
+                    const size_t nkf = (size_t)n * kf;
+                    V64* Xc = (V64*)s->rel_xc.ensure(nkf * sizeof(V64));
+                    V64* Ac = (V64*)s->rel_ac.ensure(nkf * sizeof(V64));
+                    launch(gather_cols_kernel<V64>, cdiv_u(nkf, 256), 256, 0, s->stream, n, k, kf, idx, X, Xc);
+                    e64.spmm(kf, Xc, Ac, nullptr, 0, nullptr, nullptr, 0);
+                    launch(scatter_resid_kernel<V64>, cdiv_u(nkf, 256), 256, 0, s->stream, n, k, kf, idx, B, Ac, R);
+                }
+                launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, R, R, nullptr,
+                       nullptr, pt, 1, e64.ntiles(), nullptr);
+                e64.template finalize<1>(k, co, PH_RESID);
+                nupd++;
+                const int limit = (at_limit || nupd >= max_upd) ? 1 : 0;
+                launch(rel_outer_kernel, ek, 128, 0, s->stream, k, co, ci, limit, cocg ? 1 : 0);
+                launch(rel_replace_kernel<V64, V32>, eg, 256, 0, s->stream, n, k, ci, R, Rw, RD, P, Vv);
+                if (cocg) {
+                    launch(rel_reactivate_kernel, ek, 128, 0, s->stream, k, ci);
+                } else {
+                    double* pt32 = e32.parts(k, 2);
+                    launch(dot_tiles_kernel<V32>, e32.ntiles(), e32.rowblk(k), 0, s->stream, n, k, k, RD, Rw,
+                           nullptr, nullptr, pt32, 1, e32.ntiles(), nullptr);
+                    e32.template finalize<1>(k, ci, PH_REL_RESUME);
+                }
+                if (limit) break;
+            }
         }
-        launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, R, R, nullptr, nullptr, pt,
-               1, e64.ntiles(), nullptr);
-        e64.template finalize<1>(k, co, PH_RESID);
-        nupd++;
-        launch(rel_outer_kernel, ek, 128, 0, s->stream, k, co, ci, (at_limit || nupd >= max_upd) ? 1 : 0);
-        launch(rel_replace_kernel<V64, V32>, eg, 256, 0, s->stream, n, k, ci, R, Rw, RD, P, Vv);
-        double* pt32 = e32.parts(k, 2);
-        launch(dot_tiles_kernel<V32>, e32.ntiles(), e32.rowblk(k), 0, s->stream, n, k, k, RD, Rw, nullptr, nullptr,
-               pt32, 1, e32.ntiles(), nullptr);
-        e32.template finalize<1>(k, ci, PH_REL_RESUME);
-        if (at_limit || nupd >= max_upd) break;
+        if (cocg) e32.cocg_step2(k, ci);
     }
     launch(rel_finish_kernel, ek, 128, 0, s->stream, k, co, ci);
 }
@@ -963,7 +1015,10 @@ static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co, boo
     const int max_outer = s->max_outer;
     const double inner_tol = s->inner_tol;
     if (s->method == TG_SOLVER_BICGSTAB && s->reliable) {
-        solve_reliable<V64, V32>(s, k, B, X, co, R, R32, E32, ci, e64, e32, maxit);
+        // complex systems: COCG inner process (one SpMM and one IC(0) apply
+        // per iteration) unless BiCGSTAB was asked for (reliable mode 1)
+        const bool cocg = vt<V32>::cplx && s->reliable == 2;
+        solve_reliable<V64, V32>(s, k, B, X, co, R, R32, E32, ci, e64, e32, maxit, cocg);
         return;
     }
     for (int step = 0; step <= max_outer; step++) {
@@ -1480,11 +1535,11 @@ int tg_solver_set_refinement(tg_solver s, double inner_tol, int max_outer, int i
     API_END
 }
 
-int tg_solver_set_reliable_updates(tg_solver s, int on)
+int tg_solver_set_reliable_updates(tg_solver s, int mode)
 {
     API_BEGIN
-    TG_CHECK(s, TG_ERR_ARG, "solver is NULL");
-    s->reliable = on != 0;
+    TG_CHECK(s && mode >= 0 && mode <= 2, TG_ERR_ARG, "invalid argument");
+    s->reliable = mode;
     API_END
 }
 
