@@ -372,7 +372,10 @@ def run_gpu(args):
         if not args.no_compare:
             s64 = capi.FwdSolver(gm, meth, args.tol, "ICH", cplx, precision="fp64")
             s64.set_stream(stream.cuda_stream)
-            d_J64 = torch.empty((2 * nqm, jcols), dtype=torch.float64, device=dev)
+            # the FP64 Jacobian only where it is modest (16 GB); its error is
+            # formed on the device in row blocks, never copied to the host
+            d_J64 = (torch.empty((2 * nqm, jcols), dtype=torch.float64, device=dev)
+                     if 2 * nqm * jcols * 8 <= 16e9 else None)
             p64 = torch.empty_like(d_proj)
             lp64 = torch.empty_like(d_lproj)
             s64.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, p64, lp64, d_J64, 0,
@@ -393,11 +396,18 @@ def run_gpu(args):
             cm_err = float(np.max(np.abs(lp - lr)[ok] / np.maximum(np.abs(lp), np.abs(lr))[ok]))
             l2_err = float(np.linalg.norm(d_proj.cpu().numpy() - p64.cpu().numpy()) / np.linalg.norm(p64.cpu().numpy()))
             compare["boundary_data_err_vs_fp64"] = {"cmpvec_max_rel_log": cm_err, "l2_rel_linear": l2_err}
-            Jm = d_J.float().cpu()
-            J64 = d_J64.cpu()
-            compare["jacobian_err_vs_fp64_l2"] = float(torch.linalg.norm((Jm.double() - J64).flatten()) /
-                                                       torch.linalg.norm(J64.flatten()))
-            del d_J64, Jm, J64
+            if d_J64 is not None:
+                e2, r2 = 0.0, 0.0
+                for r0 in range(0, 2 * nqm, 256):
+                    a_ = d_J[r0:r0 + 256].double()
+                    b_ = d_J64[r0:r0 + 256]
+                    e2 += float(torch.sum((a_ - b_) ** 2))
+                    r2 += float(torch.sum(b_ ** 2))
+                compare["jacobian_err_vs_fp64_l2"] = (e2 / r2) ** 0.5
+                del d_J64
+            else:
+                compare["jacobian_err_vs_fp64_l2"] = None
+                compare["jacobian_err_note"] = "FP64 Jacobian above 16 GB: not formed"
             # plain per-source FP64 (one right-hand side per solve), sampled
             s1 = capi.FwdSolver(gm, meth, args.tol, "ICH", cplx, precision="fp64")
             s1.reset(cm, ck, ca, omega)
