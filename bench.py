@@ -441,6 +441,7 @@ def run_gpu(args):
             "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
             "jacobians_per_s": ws * args.steps / (total_ms / 1e3),
             "iterations_per_source": float(np.mean(its)),
+            "unconverged_sources": int(sum(1 for r in res if r.status != 0)),
             "ic_applies_per_request": prof[capi.PROF_SWEEP][1] / psteps,
             "roofline": roof, "kernel_time_per_step": shares,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),

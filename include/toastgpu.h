@@ -119,7 +119,8 @@ int tg_solver_set_refinement(tg_solver s, double inner_tol, int max_outer, int i
    2 (default): as 1 with an FP32 COCG process for complex systems (the
       conjugate-orthogonal CG of the complex symmetric F: one SpMM and one
       IC(0) apply per iteration); real systems use 1.
-   The FP64 result meets tol in every mode.  At most 4 * max_outer updates. */
+   The FP64 result meets tol in every mode.  At most 4 * max_outer residual
+   replacements per right-hand side. */
 #define TG_MIXED_RESTART 0
 #define TG_MIXED_RELIABLE_BICGSTAB 1
 #define TG_MIXED_RELIABLE_COCG 2

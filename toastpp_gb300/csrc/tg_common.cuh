@@ -53,20 +53,24 @@ template <class R> TGHD cpx<R> operator*(cpx<R> a, R s) { return {a.x * s, a.y *
 template <class R> TGHD cpx<R>& operator+=(cpx<R>& a, cpx<R> b) { a.x += b.x; a.y += b.y; return a; }
 template <class R> TGHD cpx<R>& operator-=(cpx<R>& a, cpx<R> b) { a.x -= b.x; a.y -= b.y; return a; }
 
-// a*b for mixed real/complex scalar
+// a*b for mixed real/complex scalar (complex: explicit fused multiply-adds,
+// so kernels round alike)
 TGHD double vmul(double a, double b) { return a * b; }
 TGHD float vmul(float a, float b) { return a * b; }
-TGHD cd vmul(cd a, cd b) { return a * b; }
-TGHD cf vmul(cf a, cf b) { return a * b; }
-// acc - a*b (the forward/back substitution and residual kernels)
-TGHD double vfms(double acc, double a, double b) { return acc - a * b; }
-TGHD float vfms(float acc, float a, float b) { return acc - a * b; }
-TGHD cd vfms(cd acc, cd a, cd b) { return acc - a * b; }
-TGHD cf vfms(cf acc, cf a, cf b) { return acc - a * b; }
-TGHD double vfma(double acc, double a, double b) { return acc + a * b; }
-TGHD float vfma(float acc, float a, float b) { return acc + a * b; }
-TGHD cd vfma(cd acc, cd a, cd b) { return acc + a * b; }
-TGHD cf vfma(cf acc, cf a, cf b) { return acc + a * b; }
+TGHD cd vmul(cd a, cd b) { return {fma(a.x, b.x, -(a.y * b.y)), fma(a.x, b.y, a.y * b.x)}; }
+TGHD cf vmul(cf a, cf b) { return {fmaf(a.x, b.x, -(a.y * b.y)), fmaf(a.x, b.y, a.y * b.x)}; }
+// acc - a*b (the forward/back substitution and residual kernels) and
+// acc + a*b.  The complex forms are written as explicit chains of fused
+// multiply-adds, so every kernel that uses them rounds alike whatever the
+// compiler would contract.
+TGHD double vfms(double acc, double a, double b) { return fma(-a, b, acc); }
+TGHD float vfms(float acc, float a, float b) { return fmaf(-a, b, acc); }
+TGHD cd vfms(cd acc, cd a, cd b) { return {fma(a.y, b.y, fma(-a.x, b.x, acc.x)), fma(-a.y, b.x, fma(-a.x, b.y, acc.y))}; }
+TGHD cf vfms(cf acc, cf a, cf b) { return {fmaf(a.y, b.y, fmaf(-a.x, b.x, acc.x)), fmaf(-a.y, b.x, fmaf(-a.x, b.y, acc.y))}; }
+TGHD double vfma(double acc, double a, double b) { return fma(a, b, acc); }
+TGHD float vfma(float acc, float a, float b) { return fmaf(a, b, acc); }
+TGHD cd vfma(cd acc, cd a, cd b) { return {fma(-a.y, b.y, fma(a.x, b.x, acc.x)), fma(a.y, b.x, fma(a.x, b.y, acc.y))}; }
+TGHD cf vfma(cf acc, cf a, cf b) { return {fmaf(-a.y, b.y, fmaf(a.x, b.x, acc.x)), fmaf(a.y, b.x, fmaf(a.x, b.y, acc.y))}; }
 // scale by a real scalar
 TGHD double vscale(double a, double s) { return a * s; }
 TGHD float vscale(float a, float s) { return a * s; }

@@ -24,6 +24,7 @@ struct ColState {
     double scale, scale_prev;
     // COCG (complex symmetric CG) scalars, complex: rho = r.z, alpha, beta
     double zr, zi, ar, ai, br, bi;
+    int nupd;  // residual replacements this column has taken
 };
 
 // 2^floor(log2 x) for x > 0 finite, else 1: scaling by it is exact
@@ -1251,8 +1252,9 @@ __global__ void rel_accumulate_kernel(int n, int k, const ColState* __restrict__
 // after |b - A x| of the marked columns is in co.err: converged columns stop,
 // the others restart their trigger from the new residual; at the update or
 // iteration limit every active column stops with status 1
+// limit: the iteration limit was reached; max_upd: replacements per column
 static __global__ void rel_outer_kernel(int k, ColState* __restrict__ co, ColState* __restrict__ ci, int limit,
-                                        int cocg)
+                                        int cocg, int max_upd)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= k) return;
@@ -1260,7 +1262,7 @@ static __global__ void rel_outer_kernel(int k, ColState* __restrict__ co, ColSta
     ColState& I = ci[c];
     if (O.active != 1 || !I.rel) return;
     if (O.err <= O.tol * O.bnorm) { O.active = 0; O.status = 0; I.rel = 0; return; }
-    if (limit) { O.active = 0; O.status = 1; I.rel = 0; return; }
+    if (limit || ++I.nupd >= max_upd) { O.active = 0; O.status = 1; I.rel = 0; return; }
     // rescale the process to the new residual (exact: powers of two)
     I.scale_prev = I.scale;
     I.scale = pow2_floor(O.err);

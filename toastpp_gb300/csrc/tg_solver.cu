@@ -915,8 +915,8 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
     V32 *RD = cocg ? nullptr : e32.vec(1, nk), *P = e32.vec(2, nk), *Vv = cocg ? nullptr : e32.vec(4, nk);
     int* dcnt = (int*)s->rel_cnt.ensure(4 * sizeof(int));
     int hc[4] = {0, 0, 0, 0};
-    const int max_upd = 4 * std::max(1, s->max_outer);
-    int it = 0, nupd = 0;
+    const int max_upd = 4 * std::max(1, s->max_outer);  // residual replacements per column
+    int it = 0;
     for (;;) {
         if (cocg) e32.cocg_step1(k, X32, ci);
         else e32.bicg_iter(k, X32, ci, it == 0);
@@ -953,9 +953,8 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
                 launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, R, R, nullptr,
                        nullptr, pt, 1, e64.ntiles(), nullptr);
                 e64.template finalize<1>(k, co, PH_RESID);
-                nupd++;
-                const int limit = (at_limit || nupd >= max_upd) ? 1 : 0;
-                launch(rel_outer_kernel, ek, 128, 0, s->stream, k, co, ci, limit, cocg ? 1 : 0);
+                const int limit = at_limit ? 1 : 0;
+                launch(rel_outer_kernel, ek, 128, 0, s->stream, k, co, ci, limit, cocg ? 1 : 0, max_upd);
                 launch(rel_replace_kernel<V64, V32>, eg, 256, 0, s->stream, n, k, ci, R, Rw, RD, P, Vv);
                 if (cocg) {
                     launch(rel_reactivate_kernel, ek, 128, 0, s->stream, k, ci);
