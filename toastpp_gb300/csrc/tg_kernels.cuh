@@ -245,28 +245,29 @@ __device__ __forceinline__ void tile_dots(int r0, int r1, int k, int ld, const V
     // only with w), 2 -> the bilinear w.y as [Re, Im] (COCG)
     // columns [cbeg, k) of the tile (a block that owns a column range passes
     // its range; the per-column order is the same)
+    using S = typename vt<V>::R;  // a thread's few rows sum in the value's own precision
     __shared__ double sh[2 * TILE_RG * TILE_CK];
     TileAcc T{sh};
     for (int c0 = cbeg; c0 < k; c0 += TILE_CK) {
         const int ck = min(TILE_CK, k - c0);
         for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
             const int cc = it % ck, g = it / ck, c = c0 + cc;
-            double d0 = 0.0, d1 = 0.0;
+            S d0 = 0, d1 = 0;
             if (!(st && st[c].active != 1))
 #pragma unroll 4
                 for (int r = r0 + g; r < r1; r += TILE_RG) {
                     V yv = y[(size_t)r * ld + c];
                     if (want_n2 == 2) {
                         const V pr = vmul(w[(size_t)r * ld + c], yv);
-                        d0 += (double)re(pr);
-                        d1 += (double)im(pr);
+                        d0 += re(pr);
+                        d1 += im(pr);
                         continue;
                     }
-                    if (w) d0 += (double)redot(w[(size_t)r * ld + c], yv);
-                    if (want_n2) d1 += (double)nrm2(yv);
+                    if (w) d0 += redot(w[(size_t)r * ld + c], yv);
+                    if (want_n2) d1 += nrm2(yv);
                 }
-            T.put(0, g, cc, d0);
-            T.put(1, g, cc, d1);
+            T.put(0, g, cc, (double)d0);
+            T.put(1, g, cc, (double)d1);
         }
         __syncthreads();
         for (int cc = threadIdx.x; cc < ck; cc += blockDim.x) {
@@ -856,15 +857,15 @@ __global__ void dot_tiles_kernel(int n, int k, int ld, const V* __restrict__ a, 
         const int ck = min(TILE_CK, k - c0);
         for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
             const int cc = it % ck, g = it / ck, c = c0 + cc;
-            double d0 = 0.0, d1 = 0.0;
+            typename vt<V>::R d0 = 0, d1 = 0;
             if (!(st && st[c].active != 1))
                 for (int r = r0 + g; r < r1; r += TILE_RG) {
                     size_t o = (size_t)r * ld + c;
-                    d0 += (double)redot(a[o], b[o]);
-                    if (c2) d1 += (double)redot(c2[o], d2[o]);
+                    d0 += redot(a[o], b[o]);
+                    if (c2) d1 += redot(c2[o], d2[o]);
                 }
-            T.put(0, g, cc, d0);
-            T.put(1, g, cc, d1);
+            T.put(0, g, cc, (double)d0);
+            T.put(1, g, cc, (double)d1);
         }
         __syncthreads();
         for (int cc = threadIdx.x; cc < ck; cc += blockDim.x) {
@@ -920,7 +921,7 @@ __global__ void bicg_s_kernel(int n, int k, int ld, const ColState* st, const V*
         const int ck = min(TILE_CK, k - c0);
         for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
             const int cc = it % ck, g = it / ck, c = c0 + cc;
-            double acc = 0.0;
+            S acc = 0;
             if (col_on(st, c)) {
                 const S alpha = (S)st[c].alpha;
 #pragma unroll 4
@@ -930,10 +931,10 @@ __global__ void bicg_s_kernel(int n, int k, int ld, const ColState* st, const V*
                     s[o] = sv;
                     if (precon == 1) sd[o] = vmul(sv, idiag[i]);
                     else if (precon == 0) sd[o] = sv;
-                    acc += (double)nrm2(sv);
+                    acc += nrm2(sv);
                 }
             }
-            T.put(0, g, cc, acc);
+            T.put(0, g, cc, (double)acc);
         }
         __syncthreads();
         for (int cc = threadIdx.x; cc < ck; cc += blockDim.x)
@@ -958,7 +959,7 @@ __global__ void bicg_xr_kernel(int n, int k, int ld, const ColState* st, V* __re
         for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
             const int cc = it % ck, g = it / ck, c = c0 + cc;
             const int a = st[c].active;
-            double n2 = 0.0, rr = 0.0;
+            S n2 = 0, rr = 0;
             if (a != 0) {
                 const S alpha = (S)st[c].alpha, omega = (S)st[c].omega;
 #pragma unroll 4
@@ -968,12 +969,12 @@ __global__ void bicg_xr_kernel(int n, int k, int ld, const ColState* st, V* __re
                     x[o] = vadd(x[o], vadd(vscale(pd[o], alpha), vscale(sd[o], omega)));
                     V rv = vsub(s[o], vscale(t[o], omega));
                     r[o] = rv;
-                    n2 += (double)nrm2(rv);
-                    rr += (double)redot(rd[o], rv);
+                    n2 += nrm2(rv);
+                    rr += redot(rd[o], rv);
                 }
             }
-            T.put(0, g, cc, n2);
-            T.put(1, g, cc, rr);
+            T.put(0, g, cc, (double)n2);
+            T.put(1, g, cc, (double)rr);
         }
         __syncthreads();
         for (int cc = threadIdx.x; cc < ck; cc += blockDim.x) {
@@ -1003,7 +1004,7 @@ __global__ void pcg_xr_kernel(int n, int k, int ld, const ColState* st, V* __res
         const int ck = min(TILE_CK, k - c0);
         for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
             const int cc = it % ck, g = it / ck, c = c0 + cc;
-            double rz = 0.0, n2 = 0.0;
+            S rz = 0, n2 = 0;
             if (col_on(st, c)) {
                 const S alpha = (S)st[c].alpha;
                 for (int i = r0 + g; i < r1; i += TILE_RG) {
@@ -1014,13 +1015,13 @@ __global__ void pcg_xr_kernel(int n, int k, int ld, const ColState* st, V* __res
                     if (precon != 2) {
                         V zv = precon == 1 ? vmul(rv, idiag[i]) : rv;
                         z[o] = zv;
-                        rz += (double)redot(rv, zv);
-                        n2 += (double)nrm2(rv);
+                        rz += redot(rv, zv);
+                        n2 += nrm2(rv);
                     }
                 }
             }
-            T.put(0, g, cc, rz);
-            T.put(1, g, cc, n2);
+            T.put(0, g, cc, (double)rz);
+            T.put(1, g, cc, (double)n2);
         }
         __syncthreads();
         if (precon != 2)
@@ -1381,7 +1382,7 @@ __global__ void cocg_xr_kernel(int n, int k, int ld, const ColState* __restrict_
         const int ck = min(TILE_CK, k - c0);
         for (int it = threadIdx.x; it < ck * TILE_RG; it += blockDim.x) {
             const int cc = it % ck, g = it / ck, c = c0 + cc;
-            double acc = 0.0;
+            typename vt<V>::R acc = 0;  // a thread's few rows in the value's precision
             if (st[c].active == 1) {
                 const V a = vmake<V>(st[c].ar, st[c].ai);
 #pragma unroll 4
@@ -1390,10 +1391,10 @@ __global__ void cocg_xr_kernel(int n, int k, int ld, const ColState* __restrict_
                     x[o] = vfma(x[o], a, p[o]);
                     const V rv = vfms(r[o], a, q[o]);
                     r[o] = rv;
-                    acc += (double)nrm2(rv);
+                    acc += nrm2(rv);
                 }
             }
-            T.put(0, g, cc, acc);
+            T.put(0, g, cc, (double)acc);
         }
         __syncthreads();
         for (int cc = threadIdx.x; cc < ck; cc += blockDim.x)
