@@ -560,6 +560,11 @@ __global__ void __launch_bounds__(256) spmm_halo_kernel(int n, const int* __rest
 // IC(0) level kernel on the level's ELL entries (k >= 32): warp per slot;
 // the slot's entries sit at slot * w, so the row's indices, values, right-hand
 // side and pivot load in one round and the gathers in the next.
+// Launched as a programmatic dependent of the previous level: it lets the
+// next level start at once (griddepcontrol.launch_dependents), loads what no
+// kernel of the sweep writes (the level's rows, ELL indices and values,
+// pivots), and only then waits for the previous level's completion
+// (griddepcontrol.wait, a no-op after an ordinary launch).
 template <class V, int NJ, bool FWD>
 __global__ void __launch_bounds__(256) ic_level_ell(const int* __restrict__ rows, int nrows, int w,
                                                     const int* __restrict__ ecol, const V* __restrict__ eval, int k,
@@ -567,9 +572,20 @@ __global__ void __launch_bounds__(256) ic_level_ell(const int* __restrict__ rows
                                                     V* __restrict__ y, const ColState* __restrict__ st)
 {
     const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (slot >= nrows) return;
-    const int i = rows[slot];
-    const V di = dinv[i];
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const bool live = slot < nrows;
+    int i = 0, my_c0 = -1;
+    V di = vzero<V>(), my_v0 = vzero<V>();
+    if (live) {
+        i = rows[slot];
+        di = dinv[i];
+        if (lane < min(32, w)) {
+            my_c0 = ecol[(size_t)slot * w + lane];
+            my_v0 = eval[(size_t)slot * w + lane];
+        }
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (!live) return;
     V acc[NJ];
 #pragma unroll
     for (int j = 0; j < NJ; j++) {
@@ -579,11 +595,15 @@ __global__ void __launch_bounds__(256) ic_level_ell(const int* __restrict__ rows
     constexpr int UNR = 4;  // entries whose gathers are in flight together
     for (int base = 0; base < w; base += 32) {
         const int cnt = min(32, w - base);
-        int my_c = -1;
-        V my_v = vzero<V>();
-        if (lane < cnt) {
-            my_c = ecol[(size_t)slot * w + base + lane];
-            my_v = eval[(size_t)slot * w + base + lane];
+        int my_c = my_c0;
+        V my_v = my_v0;
+        if (base > 0) {
+            my_c = -1;
+            my_v = vzero<V>();
+            if (lane < cnt) {
+                my_c = ecol[(size_t)slot * w + base + lane];
+                my_v = eval[(size_t)slot * w + base + lane];
+            }
         }
         for (int e = 0; e < cnt; e += UNR) {
             int cc[UNR];

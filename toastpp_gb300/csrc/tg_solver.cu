@@ -55,6 +55,26 @@ static inline void launch(void (*k)(KArgs...), dim3 g, dim3 b, size_t sm, cudaSt
     g_nlaunch.fetch_add(1, std::memory_order_relaxed);
 }
 
+// Launch as a programmatic dependent of the previous kernel in the stream
+// (it may start while that one finishes; the kernel itself waits with
+// griddepcontrol.wait before it reads anything the previous kernel writes).
+template <class... KArgs, class... Args>
+static inline void launch_pdl(void (*k)(KArgs...), dim3 g, dim3 b, size_t sm, cudaStream_t st, Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = g;
+    cfg.blockDim = b;
+    cfg.dynamicSmemBytes = sm;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    TG_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...));
+    g_nlaunch.fetch_add(1, std::memory_order_relaxed);
+}
+
 // Raise a kernel's dynamic shared-memory limit to the device's opt-in
 // maximum, once per (kernel, device).  Setting it per launch to the launch's
 // own size would race between solvers (another solver's smaller setting
@@ -349,7 +369,8 @@ struct Engine {
     }
     static int colw(int k) { return k >= 32 ? 32 : (k >= 16 ? 16 : (k >= 8 ? 8 : (k >= 4 ? 4 : (k >= 2 ? 2 : 1)))); }
 
-    void launch_level_ell(bool fwd, int l, int off, int nr, int k, const V* in, V* out, const ColState* cst)
+    // pdl: a programmatic dependent of the previous level
+    void launch_level_ell(bool fwd, int l, int off, int nr, int k, const V* in, V* out, const ColState* cst, bool pdl)
     {
         const MeshDev& m = mesh->d;
         unsigned g = cdiv_u((size_t)nr * 32, 256);
@@ -362,8 +383,15 @@ struct Engine {
         const V* ev = (fwd ? Lef : Leb) + eo;
         const V* src = fwd ? in : out;
         switch ((k + 31) / 32) {
-#define TG_LE(J) case J: if (fwd) launch(ic_level_ell<V, J, true>, g, 256, 0, st, rows, nr, w, ec, ev, k, k, dinv, src, out, cst); \
-                         else launch(ic_level_ell<V, J, false>, g, 256, 0, st, rows, nr, w, ec, ev, k, k, dinv, src, out, cst); break;
+#define TG_LE(J) case J: \
+            if (fwd) { \
+                if (pdl) launch_pdl(ic_level_ell<V, J, true>, g, 256, 0, st, rows, nr, w, ec, ev, k, k, dinv, src, out, cst); \
+                else launch(ic_level_ell<V, J, true>, g, 256, 0, st, rows, nr, w, ec, ev, k, k, dinv, src, out, cst); \
+            } else { \
+                if (pdl) launch_pdl(ic_level_ell<V, J, false>, g, 256, 0, st, rows, nr, w, ec, ev, k, k, dinv, src, out, cst); \
+                else launch(ic_level_ell<V, J, false>, g, 256, 0, st, rows, nr, w, ec, ev, k, k, dinv, src, out, cst); \
+            } \
+            break;
         TG_LE(1) TG_LE(2) TG_LE(3) TG_LE(4) TG_LE(5) TG_LE(6) TG_LE(7) TG_LE(8)
 #undef TG_LE
         }
@@ -386,7 +414,7 @@ struct Engine {
             for (size_t l = 0; l + 1 < fp.size(); l++) {
                 int nr = fp[l + 1] - fp[l];
                 size_t warps = cdiv_u((size_t)nr * ncg, rpw);
-                if (wide) launch_level_ell(true, (int)l, fp[l], nr, k, in, out, cst);
+                if (wide) launch_level_ell(true, (int)l, fp[l], nr, k, in, out, cst, l > 0);
                 else launch(ic_fwd_level<V, S>, cdiv_u(warps * 32, 256), 256, 0, st, ic, ic.fwd_lev_rows + fp[l], nr, k,
                             k, cw, L, dinv, in, out, cst);
             }
@@ -394,7 +422,7 @@ struct Engine {
             for (size_t l = 0; l + 1 < bp.size(); l++) {
                 int nr = bp[l + 1] - bp[l];
                 size_t warps = cdiv_u((size_t)nr * ncg, rpw);
-                if (wide) launch_level_ell(false, (int)l, bp[l], nr, k, out, out, cst);
+                if (wide) launch_level_ell(false, (int)l, bp[l], nr, k, out, out, cst, true);
                 else launch(ic_bwd_level<V, S>, cdiv_u(warps * 32, 256), 256, 0, st, ic, ic.bwd_lev_rows + bp[l], nr, k,
                             k, cw, L, dinv, out, cst);
             }
