@@ -251,7 +251,9 @@ int tg_solver_profile_read(tg_solver s, int cls, double *total_ms, int *count);
 /* number of kernels this library has launched in this process */
 int tg_launch_count(long long *count);
 /* the SpMM autotuner's decisions so far: one text line per (mesh, value type,
-   columns) with every candidate kernel's best launch time and the choice */
+   columns) with every candidate kernel's best launch time and the choice.
+   The environment variable TOASTGPU_SPMM_VARIANT (spmm_halo, spmm_vec,
+   spmm_wide or spmm_dot) fixes the variant wherever it applies. */
 int tg_tuner_log(char *buf, int len);
 
 const char *tg_last_error(void);

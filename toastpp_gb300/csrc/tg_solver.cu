@@ -4,6 +4,7 @@
 #include <type_traits>
 #include <utility>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -313,6 +314,11 @@ struct Engine {
         std::vector<int> cands;
         for (int v = 0; v < 4; v++)
             if (spmm_ok(v, k)) cands.push_back(v);
+        // TOASTGPU_SPMM_VARIANT=<name> fixes the choice where that variant
+        // applies (profiling runs, whose timings would mislead the tuner)
+        if (const char* fv = getenv("TOASTGPU_SPMM_VARIANT"))
+            for (int v : cands)
+                if (!strcmp(fv, spmm_name(v))) return v;
         // FP64 products are bound by the FP64 FMA rate whatever the layout:
         // no timing, the fixed preference (each new column count would cost
         // the tuner seconds of FP64 work)
