@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--config", default="c2_cyl30k_fd",
                     choices=["c0_disc3k_cw", "c1_disc13k_fd", "c2_cyl30k_fd", "c3_box250k_fd"])
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
+    ap.add_argument("--e2e-slots", type=int, default=1, help="e2e leg: request-server slots")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--tol", type=float, default=1e-12)
     ap.add_argument("--inner-tol", type=float, default=1e-4, help="mixed path: inner FP32 solve tolerance")
@@ -362,8 +363,40 @@ def run_gpu(args):
         te = time.perf_counter() - t0
         h2d = 3 * n * 8 + (nq + nm) * n * 8 * vmul + (nq + 1 + nqm) * 4
         d2h = 2 * nqm * 8 * vmul + h_J.numel() * h_J.element_size()
-        e2e = {"value": ws * nsolves * ksteps / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "steps": ksteps}
+        serial = ws * nsolves * ksteps / te
+        e2e = {"value": serial, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "steps": ksteps, "api": "tg_forward_path, one request at a time, page-locked host buffers"}
+    # the server's solvers take the library's default refinement settings
+    defaults = args.precision == "fp64" or (args.inner_tol == 1e-4 and args.inner_order == 1 and args.inner == "cocg")
+    if e2e is not None and defaults:
+        # the same requests through the request server: request i + 1 solves
+        # while request i's Jacobian streams to host memory (deferred output)
+        pdt = np.complex128 if cplx else np.float64
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+        p_cm, p_ck, p_ca, p_q, p_m = pin(cm), pin(ck), pin(ca), pin(qvec.astype(pdt)), pin(mvec.astype(pdt))
+        outs = [(pin(np.zeros(nqm, pdt)), pin(np.zeros(nqm, pdt)), h_J.numpy() if b == 0 else
+                 torch.empty(tuple(h_J.shape), dtype=h_J.dtype).pin_memory().numpy()) for b in range(2)]
+        srv = capi.Server(slots=args.e2e_slots, hbm_budget_gb=200.0)
+
+        def request(b):
+            return capi.Request(gm, p_cm, p_ck, p_ca, omega, p_q, p_m, links, solver=meth, precon="ICH",
+                                tol=args.tol, precision=args.precision, want_jac=True, j_fp32=j_fp32, outputs=outs[b])
+
+        for t in [srv.submit(request(b)) for b in range(2)]:
+            srv.wait(t)
+        psteps_e2e = max(10, 2 * ksteps)
+        t0 = time.perf_counter()
+        tickets = [srv.submit(request(i % 2)) for i in range(psteps_e2e)]
+        done = [srv.wait(t) for t in tickets]
+        tp = time.perf_counter() - t0
+        srv.close()
+        bad = sum(1 for rq in done for r in rq.results if r[1] != 0)
+        e2e = {"value": ws * nsolves * psteps_e2e / tp, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "steps": psteps_e2e,
+               "api": f"tg_submit / tg_wait, request server with {args.e2e_slots} slot(s), page-locked host buffers",
+               "unconverged_sources": bad,
+               "serial": {"value": serial, "steps": ksteps,
+                          "api": "tg_forward_path, one request at a time, page-locked host buffers"}}
 
     line = None
     if rank == 0:

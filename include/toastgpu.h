@@ -128,6 +128,14 @@ int tg_solver_set_reliable_updates(tg_solver s, int mode);
 /* a cudaStream_t; 0 selects the solver's own stream */
 int tg_solver_set_stream(tg_solver s, void *stream);
 int tg_solver_sync(tg_solver s);
+/* Deferred Jacobian output, for pipelining requests: with a copy stream set
+   (a cudaStream_t), tg_forward_path queues the device-to-host copy of a host
+   J on that stream and returns without waiting for it.  J is complete once
+   the work queued on that stream so far has finished (an event recorded on
+   it after the call, or tg_solver_sync).  The solver alternates two device J
+   buffers and never overwrites one whose copy is still in flight.  NULL
+   (default) turns it off: J is in place when tg_forward_path returns. */
+int tg_solver_set_output_stream(tg_solver s, void *stream);
 /* Reset(sol, omega): nodal cmua, ckappa, c2a (length n); omega in rad/ps
    (0 for real systems).  Assembles F and factors the preconditioner on the GPU. */
 int tg_solver_reset(tg_solver s, const double *cmua, const double *ckappa, const double *c2a,

@@ -24,7 +24,7 @@ MEM_HOST, MEM_DEVICE = 0, 1
 DATA_LIN, DATA_LOG = 1, 2
 
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
-           "tg_qvec_gaussian", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream",
+           "tg_qvec_gaussian", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream", "tg_solver_set_output_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
            "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log",
            "tg_server_create", "tg_server_destroy", "tg_submit", "tg_poll", "tg_wait", "tg_server_stats",
@@ -76,6 +76,7 @@ def lib():
             "tg_solver_set_refinement": [vp, d_, i_, i_],
             "tg_solver_set_reliable_updates": [vp, i_],
             "tg_solver_set_stream": [vp, vp],
+            "tg_solver_set_output_stream": [vp, vp],
             "tg_solver_sync": [vp],
             "tg_solver_reset": [vp, dp, dp, dp, d_, i_],
             "tg_solver_matrix": [vp, dp, i_],
@@ -236,6 +237,14 @@ class FwdSolver:
         """0 restarted refinement, 1 reliable-update BiCGSTAB, 2 reliable-update COCG (complex)."""
         _check(lib().tg_solver_set_reliable_updates(self._h, int(mode)))
 
+    def sync(self):
+        """Wait for the solver's stream and its deferred-output stream."""
+        _check(lib().tg_solver_sync(self._h))
+
+    def set_output_stream(self, stream=None):
+        """Deferred Jacobian output on a copy stream (cudaStream_t handle), or None."""
+        _check(lib().tg_solver_set_output_stream(self._h, C.c_void_p(stream) if stream else None))
+
     def set_tol(self, tol, maxit=0):
         _check(lib().tg_solver_set(self._h, float(tol), int(maxit)))
 
@@ -338,7 +347,10 @@ class Request:
     fills (proj, logproj, optional J, per-source results)."""
 
     def __init__(self, mesh: Mesh, cmua, ckap, c2a, omega, qvec, mvec, links: Links, solver=None, precon="ICH",
-                 tol=1e-10, precision="mixed", want_jac=True, j_fp32=True, maxit=0):
+                 tol=1e-10, precision="mixed", want_jac=True, j_fp32=True, maxit=0, outputs=None):
+        """outputs: optional caller-owned (proj, logproj, J) arrays (e.g. views of
+        page-locked memory), C-contiguous with the shapes and types the
+        request fills; J is None without want_jac."""
         self.complex = omega != 0.0 or np.iscomplexobj(qvec)
         self.mesh = mesh
         cplx = self.complex
@@ -349,10 +361,19 @@ class Request:
         self.links = links
         n, nq, nm, nqm = mesh.n, self.qvec.shape[0], self.mvec.shape[0], links.nqm
         dt = np.complex128 if cplx else np.float64
-        self.proj = np.zeros(nqm, dt)
-        self.logproj = np.zeros(nqm, dt)
-        self.J = (np.zeros((2 * nqm, 2 * n if cplx else n), np.float32 if j_fp32 else np.float64)
-                  if want_jac else None)
+        jshape, jdt = (2 * nqm, 2 * n if cplx else n), np.float32 if j_fp32 else np.float64
+        if outputs is None:
+            self.proj = np.zeros(nqm, dt)
+            self.logproj = np.zeros(nqm, dt)
+            self.J = np.zeros(jshape, jdt) if want_jac else None
+        else:
+            self.proj, self.logproj, self.J = outputs
+            for a, shp, t in ((self.proj, (nqm,), dt), (self.logproj, (nqm,), dt)) + \
+                    (((self.J, jshape, jdt),) if want_jac else ()):
+                if a.shape != shp or a.dtype != t or not a.flags.c_contiguous:
+                    raise ValueError(f"output buffer must be a C-contiguous {np.dtype(t).name} array of shape {shp}")
+            if not want_jac:
+                self.J = None
         self.res = (TgResult * (nq + nm))()
         r = TgRequest()
         r.mesh = mesh._h.value if hasattr(mesh._h, "value") else mesh._h

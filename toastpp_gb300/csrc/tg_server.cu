@@ -54,9 +54,17 @@ struct SolverKey {
 
 struct Slot {
     cudaStream_t stream = nullptr;
+    cudaStream_t copy = nullptr;              // the Jacobians' device-to-host copies
     std::map<SolverKey, tg_solver> solvers;   // resident per mesh and settings
     std::vector<SolverKey> lru;
     std::thread th;
+    // requests whose compute is done and whose Jacobian copy is in flight,
+    // completed in order by the slot's completion thread
+    std::mutex pmu;
+    std::condition_variable pcv;
+    std::deque<std::pair<std::shared_ptr<Ticket>, cudaEvent_t>> pend;
+    bool pstop = false;
+    std::thread done_th;
 };
 
 }  // namespace
@@ -72,6 +80,7 @@ struct tg_server_s {
     std::vector<std::shared_ptr<Ticket>> ready;          // admitted, waiting for a slot thread
     size_t inflight_bytes = 0;
     int inflight = 0, nslots = 0;
+    int running = 0;          // requests computing in a slot (the rest of inflight: copies)
     long long next_id = 1;
     bool stop = false;
     std::vector<double> lat_ms;                          // completed requests
@@ -113,15 +122,16 @@ size_t estimate_bytes(const tg_request& r)
     return b;
 }
 
-// admission: strictly in arrival order, while a slot is free and the working
-// set fits the budget (a request larger than the whole budget runs alone)
+// admission: strictly in arrival order, while a slot is free (not computing)
+// and the working set of the requests in flight (computing, or copying their
+// Jacobian out) fits the budget (a request larger than the budget runs alone)
 void dispatch_loop(tg_server_s* S)
 {
     std::unique_lock<std::mutex> g(S->mu);
     for (;;) {
         S->cv_work.wait(g, [&] {
             if (S->stop) return true;
-            if (S->queue.empty() || S->inflight >= S->nslots) return false;
+            if (S->queue.empty() || S->running >= S->nslots) return false;
             const auto& h = S->queue.front();
             return S->inflight == 0 || S->inflight_bytes + h->bytes <= S->budget;
         });
@@ -129,6 +139,7 @@ void dispatch_loop(tg_server_s* S)
         auto t = S->queue.front();
         S->queue.pop_front();
         S->inflight++;
+        S->running++;
         S->inflight_bytes += t->bytes;
         t->state = TG_REQ_RUNNING;
         S->ready.push_back(t);
@@ -159,11 +170,40 @@ tg_solver get_solver(tg_server_s* S, Slot& sl, const tg_request& r)
     int rc = tg_solver_create(r.mesh, r.is_complex, r.method, r.precon, r.tol, r.maxit, r.precision, &s);
     if (rc != TG_OK) throw std::runtime_error(tg_last_error());
     tg_solver_set_stream(s, sl.stream);
+    tg_solver_set_output_stream(s, sl.copy);
     sl.solvers[key] = s;
     sl.lru.push_back(key);
     return s;
 }
 
+// the bookkeeping of a finished request (its latency ends here)
+void finish(tg_server_s* S, const std::shared_ptr<Ticket>& t, int rc, const std::string& msg)
+{
+    t->t_done = clk::now();
+    const tg_request& r = t->req;
+    {
+        std::lock_guard<std::mutex> g(S->mu);
+        t->status = rc;
+        t->err = msg;
+        t->state = rc == TG_OK ? TG_REQ_DONE : TG_REQ_FAILED;
+        S->inflight--;
+        S->inflight_bytes -= t->bytes;
+        if (rc == TG_OK) {
+            S->completed++;
+            S->solves += (long long)r.nq + r.nm;
+            S->lat_ms.push_back(std::chrono::duration<double, std::milli>(t->t_done - t->t_submit).count());
+        } else {
+            S->failed++;
+        }
+    }
+    S->cv_work.notify_all();
+    S->cv_done.notify_all();
+}
+
+// A slot runs one request at a time on its stream.  tg_forward_path returns
+// once the compute is done and the Jacobian's copy is queued on the slot's
+// copy stream, so the next request starts while that copy runs; the
+// completion thread waits for each copy (an event) and completes the request.
 void slot_loop(tg_server_s* S, Slot* sl)
 {
     cudaSetDevice(S->device);
@@ -180,33 +220,55 @@ void slot_loop(tg_server_s* S, Slot* sl)
         const tg_request& r = t->req;
         int rc = TG_OK;
         std::string msg;
+        cudaEvent_t ev = nullptr;
         try {
             tg_solver s = get_solver(S, *sl, r);
             rc = tg_forward_path(s, r.cmua, r.ckappa, r.c2a, r.omega, r.nq, r.qvec, r.nm, r.mvec, r.link_ofs,
                                  r.link_m, nullptr, nullptr, r.proj, r.logproj, r.J, r.j_fp32, TG_MEM_HOST, r.res);
             if (rc != TG_OK) msg = tg_last_error();
+            else if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess ||
+                     cudaEventRecord(ev, sl->copy) != cudaSuccess) {
+                rc = TG_ERR_CUDA;
+                msg = "event record on the copy stream failed";
+            }
         } catch (const std::exception& e) {
             rc = TG_ERR_ARG;
             msg = e.what();
         }
-        t->t_done = clk::now();
         {
             std::lock_guard<std::mutex> g(S->mu);
-            t->status = rc;
-            t->err = msg;
-            t->state = rc == TG_OK ? TG_REQ_DONE : TG_REQ_FAILED;
-            S->inflight--;
-            S->inflight_bytes -= t->bytes;
-            if (rc == TG_OK) {
-                S->completed++;
-                S->solves += (long long)r.nq + r.nm;
-                S->lat_ms.push_back(std::chrono::duration<double, std::milli>(t->t_done - t->t_submit).count());
-            } else {
-                S->failed++;
-            }
+            S->running--;
         }
         S->cv_work.notify_all();
-        S->cv_done.notify_all();
+        if (rc != TG_OK) {
+            if (ev) cudaEventDestroy(ev);
+            finish(S, t, rc, msg);
+            continue;
+        }
+        {
+            std::lock_guard<std::mutex> g(sl->pmu);
+            sl->pend.emplace_back(t, ev);
+        }
+        sl->pcv.notify_all();
+    }
+}
+
+void done_loop(tg_server_s* S, Slot* sl)
+{
+    cudaSetDevice(S->device);
+    for (;;) {
+        std::pair<std::shared_ptr<Ticket>, cudaEvent_t> p;
+        {
+            std::unique_lock<std::mutex> g(sl->pmu);
+            sl->pcv.wait(g, [&] { return sl->pstop || !sl->pend.empty(); });
+            if (sl->pend.empty()) return;
+            p = sl->pend.front();
+            sl->pend.pop_front();
+        }
+        const cudaError_t e = cudaEventSynchronize(p.second);
+        cudaEventDestroy(p.second);
+        finish(S, p.first, e == cudaSuccess ? TG_OK : TG_ERR_CUDA,
+               e == cudaSuccess ? std::string() : std::string("Jacobian copy failed: ") + cudaGetErrorString(e));
     }
 }
 
@@ -234,12 +296,16 @@ int tg_server_create(int slots, double hbm_budget_gb, tg_server* out)
     S->nslots = slots;
     for (int i = 0; i < slots; i++) {
         auto sl = std::make_unique<Slot>();
-        if (cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking) != cudaSuccess)
+        if (cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&sl->copy, cudaStreamNonBlocking) != cudaSuccess)
             return fail(TG_ERR_CUDA, "stream creation failed");
         S->slots.push_back(std::move(sl));
     }
     tg_server_s* raw = S.get();
-    for (auto& sl : S->slots) sl->th = std::thread(slot_loop, raw, sl.get());
+    for (auto& sl : S->slots) {
+        sl->th = std::thread(slot_loop, raw, sl.get());
+        sl->done_th = std::thread(done_loop, raw, sl.get());
+    }
     S->dispatcher = std::thread(dispatch_loop, raw);
     *out = S.release();
     return TG_OK;
@@ -258,8 +324,17 @@ int tg_server_destroy(tg_server S)
     S->dispatcher.join();
     for (auto& sl : S->slots) sl->th.join();
     for (auto& sl : S->slots) {
+        {
+            std::lock_guard<std::mutex> g(sl->pmu);
+            sl->pstop = true;
+        }
+        sl->pcv.notify_all();
+        sl->done_th.join();
+    }
+    for (auto& sl : S->slots) {
         for (auto& kv : sl->solvers) tg_solver_destroy(kv.second);
         cudaStreamDestroy(sl->stream);
+        cudaStreamDestroy(sl->copy);
     }
     delete S;
     return TG_OK;

@@ -159,6 +159,45 @@ struct DBuf {
 
 static inline unsigned cdiv_u(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 
+// Small device-to-host reads (counts, column states) written by a kernel into
+// mapped page-locked memory instead of going through the copy engines: a
+// large copy in flight on another stream (a Jacobian going out while the
+// next request solves) would hold a copy-engine read up behind it.
+static __global__ void bounce_kernel(const unsigned* __restrict__ src, unsigned* __restrict__ dst, int nw)
+{
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) dst[i] = src[i];
+}
+
+struct Bounce {
+    unsigned* h = nullptr;
+    unsigned* d = nullptr;  // device view of h
+    size_t bytes = 0;
+    Bounce() = default;
+    Bounce(const Bounce&) = delete;
+    Bounce& operator=(const Bounce&) = delete;
+    ~Bounce() { if (h) cudaFreeHost(h); }
+    // dst <- bytes (a multiple of 4) at device address src, ordered on st
+    void fetch(void* dst, const void* src, size_t b, cudaStream_t st)
+    {
+        if (b % 4) throw Error{TG_ERR_ARG, "bounce read of a size that is not a multiple of 4 bytes"};
+        if (b > bytes) {
+            if (h) cudaFreeHost(h);
+            h = d = nullptr;
+            bytes = 0;
+            const size_t nb = std::max<size_t>(b, 256);
+            if (cudaHostAlloc((void**)&h, nb, cudaHostAllocMapped) != cudaSuccess) {
+                cudaGetLastError();
+                throw Error{TG_ERR_NOMEM, "page-locked host allocation failed"};
+            }
+            TG_CUDA(cudaHostGetDevicePointer((void**)&d, h, 0));
+            bytes = nb;
+        }
+        launch(bounce_kernel, 1, 256, 0, st, (const unsigned*)src, d, (int)(b / 4));
+        TG_CUDA(cudaStreamSynchronize(st));
+        std::memcpy(dst, h, b);
+    }
+};
+
 
 // Captured launch sequences (the level kernels of an IC(0) apply or
 // factorisation), keyed by their sizes and buffer pointers and replayed with
@@ -228,13 +267,8 @@ struct Engine {
     int precon = 0;            // 0 none, 1 diag, 2 ich
     Profiler* prof = nullptr;
     DBuf w[9], part, cs, cnt, gbasis, gcol;
-    int* h_cnt = nullptr;
+    Bounce bnc;
     GraphCache graphs;
-
-    ~Engine()
-    {
-        if (h_cnt) cudaFreeHost(h_cnt);
-    }
 
     V* vec(int i, size_t nk) { return (V*)w[i].ensure(nk * sizeof(V)); }
     int ntiles() const { return (int)cdiv_u(mesh->d.n, ROW_TILE); }
@@ -437,12 +471,11 @@ struct Engine {
 
     int count_active(int k, ColState* cst)
     {
-        if (!h_cnt) TG_CUDA(cudaMallocHost(&h_cnt, sizeof(int)));
         int* dc = (int*)cnt.ensure(sizeof(int));
         launch(count_active_kernel, 1, 256, 0, st, k, cst, dc);
-        TG_CUDA(cudaMemcpyAsync(h_cnt, dc, sizeof(int), cudaMemcpyDeviceToHost, st));
-        TG_CUDA(cudaStreamSynchronize(st));
-        return *h_cnt;
+        int h = 0;
+        bnc.fetch(&h, dc, sizeof(int), st);
+        return h;
     }
 
     // B, X: device node-major n x k.  cst: per-column state with tol/maxit set.
@@ -469,8 +502,7 @@ struct Engine {
         {
             // maxit is per column but identical within one call; read it back from the first column
             ColState h;
-            TG_CUDA(cudaMemcpyAsync(&h, cst, sizeof(ColState), cudaMemcpyDeviceToHost, st));
-            TG_CUDA(cudaStreamSynchronize(st));
+            bnc.fetch(&h, cst, sizeof(ColState), st);
             maxit = h.maxit;
         }
         if (method == TG_SOLVER_BICGSTAB) bicgstab(k, X, cst, maxit);
@@ -490,12 +522,11 @@ struct Engine {
 
     int gm_count(int k, const ColState* cst, const GmCol<W>* g)
     {
-        if (!h_cnt) TG_CUDA(cudaMallocHost(&h_cnt, sizeof(int)));
         int* dc = (int*)cnt.ensure(sizeof(int));
         launch(gm_count_kernel<W>, 1, 256, 0, st, k, cst, g, dc);
-        TG_CUDA(cudaMemcpyAsync(h_cnt, dc, sizeof(int), cudaMemcpyDeviceToHost, st));
-        TG_CUDA(cudaStreamSynchronize(st));
-        return *h_cnt;
+        int h = 0;
+        bnc.fetch(&h, dc, sizeof(int), st);
+        return h;
     }
 
     // GMRES(20) per column (src/libmath/gmres_imp.hpp:39-230): the small
@@ -515,8 +546,7 @@ struct Engine {
         int maxc = 0;
         {
             ColState h;
-            TG_CUDA(cudaMemcpyAsync(&h, cst, sizeof(ColState), cudaMemcpyDeviceToHost, st));
-            TG_CUDA(cudaStreamSynchronize(st));
+            bnc.fetch(&h, cst, sizeof(ColState), st);
             maxc = h.maxit;
         }
         auto mgs = [&](int need_inner, int jj, int kprev, V* w, const V* vprev, const V* vk) {
@@ -757,6 +787,13 @@ struct tg_solver_s {
     int reliable = 2;          // mixed BiCGSTAB: 0 restarted refinement, 1 reliable updates of an FP32
                                // BiCGSTAB, 2 reliable updates of an FP32 COCG (complex; real: BiCGSTAB)
     cudaStream_t stream = 0, own = 0;
+    // deferred Jacobian output: the device-to-host copy of a host J goes on
+    // out_stream and tg_forward_path returns without waiting for it; two
+    // device J buffers alternate, jev[b] marks the end of buffer b's copy
+    cudaStream_t out_stream = nullptr;
+    DBuf jdev[2];
+    cudaEvent_t jev[2] = {nullptr, nullptr}, jready = nullptr;
+    int jflip = 0;
     bool reset_done = false;
     DBuf val64, val32, L64, L32, dinv64, dinv32, idiag64, idiag32, params;
     DBuf ef64, eb64, ef32, eb32;  // factor values in the level ELL layouts
@@ -769,10 +806,18 @@ struct tg_solver_s {
     DBuf fp_bq, fp_xq, fp_bm, fp_xm, fp_lin, fp_log;
     DBuf jwm64, jwk64, jwm32, jwk32;  // per-node element weights of the Jacobian (geometry only)
     DBuf rel_cnt, rel_idx, rel_xc, rel_ac;
+    Bounce bnc;                       // small device-to-host reads
     int jw_D = 0, jw_ready = 0;       // slots per node; bit 0 FP64 weights built, bit 1 FP32
     Profiler prof;
     GraphCache graphs;
     std::mutex mu;
+    ~tg_solver_s()
+    {
+        if (out_stream) cudaStreamSynchronize(out_stream);
+        for (cudaEvent_t e : jev)
+            if (e) cudaEventDestroy(e);
+        if (jready) cudaEventDestroy(jready);
+    }
 };
 
 static int fail(const Error& e)
@@ -958,8 +1003,7 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
         const bool at_limit = it >= maxit;
         if ((it & 3) == 0 || at_limit) {
             launch(rel_flags_kernel, 1, 256, 0, s->stream, k, co, ci, dcnt);
-            TG_CUDA(cudaMemcpyAsync(hc, dcnt, 3 * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-            TG_CUDA(cudaStreamSynchronize(s->stream));
+            s->bnc.fetch(hc, dcnt, 3 * sizeof(int), s->stream);
             const int oa = hc[0], fl = hc[2];
             if (oa == 0) break;
             if (fl > 0 || at_limit) {
@@ -970,8 +1014,7 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
                 // the FP64 product (FP64-FMA bound on this part) only for the marked columns
                 int* idx = (int*)s->rel_idx.ensure((size_t)(k + 1) * sizeof(int));
                 launch(rel_compact_kernel, 1, 256, 0, s->stream, k, ci, idx, dcnt + 3);
-                TG_CUDA(cudaMemcpyAsync(hc + 3, dcnt + 3, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-                TG_CUDA(cudaStreamSynchronize(s->stream));
+                s->bnc.fetch(hc + 3, dcnt + 3, sizeof(int), s->stream);
                 const int kf = hc[3];
                 if (kf == k) {
                     e64.spmm(k, X, R, nullptr, 0, nullptr, nullptr, 0);
@@ -1074,8 +1117,7 @@ static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co, boo
 static void read_results(tg_solver s, int k, const ColState* co, tg_result* res)
 {
     std::vector<ColState> h(k);
-    TG_CUDA(cudaMemcpyAsync(h.data(), co, sizeof(ColState) * k, cudaMemcpyDeviceToHost, s->stream));
-    TG_CUDA(cudaStreamSynchronize(s->stream));
+    s->bnc.fetch(h.data(), co, sizeof(ColState) * k, s->stream);
     for (int c = 0; c < k; c++) {
         res[c].it_count = h[c].its;
         res[c].status = h[c].status;
@@ -1312,9 +1354,28 @@ static void api_forward_path(tg_solver s, const double* cmua, const double* ckap
     project_nm<V64>(s, X, k, nm, Ms, L, ylin, ylog);
     if (J) {
         size_t jbytes = (size_t)2 * nqm * (vt<V64>::cplx ? 2 * n : n) * (j_fp32 ? 4 : 8);
-        void* Jd = mem == TG_MEM_DEVICE ? J : s->jout.ensure(jbytes);
-        jacobian_nm<V64, V32>(s, nq, X, k, nm, X + nq, k, L, ylin, Jd, j_fp32);
-        if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(J, Jd, jbytes, cudaMemcpyDeviceToHost, s->stream));
+        if (mem != TG_MEM_DEVICE && s->out_stream) {
+            // deferred: this request's J buffer was last copied out two
+            // requests ago; the copy of this one overlaps the next request
+            const int b = s->jflip;
+            s->jflip ^= 1;
+            if (!s->jready) {
+                for (auto& e : s->jev) TG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+                TG_CUDA(cudaEventCreateWithFlags(&s->jready, cudaEventDisableTiming));
+                for (auto& e : s->jev) TG_CUDA(cudaEventRecord(e, s->out_stream));
+            }
+            void* Jd = s->jdev[b].ensure(jbytes);
+            TG_CUDA(cudaStreamWaitEvent(s->stream, s->jev[b], 0));
+            jacobian_nm<V64, V32>(s, nq, X, k, nm, X + nq, k, L, ylin, Jd, j_fp32);
+            TG_CUDA(cudaEventRecord(s->jready, s->stream));
+            TG_CUDA(cudaStreamWaitEvent(s->out_stream, s->jready, 0));
+            TG_CUDA(cudaMemcpyAsync(J, Jd, jbytes, cudaMemcpyDeviceToHost, s->out_stream));
+            TG_CUDA(cudaEventRecord(s->jev[b], s->out_stream));
+        } else {
+            void* Jd = mem == TG_MEM_DEVICE ? J : s->jout.ensure(jbytes);
+            jacobian_nm<V64, V32>(s, nq, X, k, nm, X + nq, k, L, ylin, Jd, j_fp32);
+            if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(J, Jd, jbytes, cudaMemcpyDeviceToHost, s->stream));
+        }
     }
     auto out_field = [&](double* dst, const V64* src_nm, int kk, DBuf& stage) {
         if (!dst) return;
@@ -1460,6 +1521,17 @@ int tg_solver_sync(tg_solver s)
     API_BEGIN
     TG_CHECK(s, TG_ERR_ARG, "solver is NULL");
     TG_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->out_stream) TG_CUDA(cudaStreamSynchronize(s->out_stream));
+    API_END
+}
+
+int tg_solver_set_output_stream(tg_solver s, void* stream)
+{
+    API_BEGIN
+    TG_CHECK(s, TG_ERR_ARG, "solver is NULL");
+    std::lock_guard<std::mutex> g(s->mu);
+    if (s->out_stream) TG_CUDA(cudaStreamSynchronize(s->out_stream));
+    s->out_stream = (cudaStream_t)stream;
     API_END
 }
 
