@@ -129,8 +129,9 @@ int tg_solver_set_reliable_updates(tg_solver s, int mode);
 int tg_solver_set_stream(tg_solver s, void *stream);
 int tg_solver_sync(tg_solver s);
 /* Deferred Jacobian output, for pipelining requests: with a copy stream set
-   (a cudaStream_t), tg_forward_path queues the device-to-host copy of a host
-   J on that stream and returns without waiting for it.  J is complete once
+   (a cudaStream_t), tg_forward_path queues the device-to-host copy of a
+   page-locked host J on that stream and returns without waiting for it (a
+   pageable J is copied before the call returns, as without the stream).  J is complete once
    the work queued on that stream so far has finished (an event recorded on
    it after the call, or tg_solver_sync).  The solver alternates two device J
    buffers and never overwrites one whose copy is still in flight.  NULL

@@ -96,10 +96,30 @@ def test_failed_request_reports_error():
     srv.close()
 
 
+def pinned_outputs(P, gm):
+    """(proj, logproj, J) in page-locked memory (deferred Jacobian copies)."""
+    torch = pytest.importorskip("torch")
+    nqm, n = len(P.qm.link_m), gm.n
+    dt = torch.complex128 if P.complex else torch.float64
+    cols = 2 * n if P.complex else n
+    return (torch.zeros(nqm, dtype=dt).pin_memory().numpy(), torch.zeros(nqm, dtype=dt).pin_memory().numpy(),
+            torch.zeros((2 * nqm, cols), dtype=torch.float32).pin_memory().numpy())
+
+
+def make_pinned_request(P, gm):
+    cm, ck, ca = capi.optical_coefficients(P.mua, P.mus, P.nref)
+    q = gm.qvec_gaussian(P.qm.Q, P.qwidth)
+    m = gm.qvec_gaussian(P.qm.M, P.mwidth) * ca[None, :]
+    L = capi.Links(P.qm.link_ofs, P.qm.link_m)
+    return capi.Request(gm, cm, ck, ca, capi.omega_of(P.freq_mhz), q, m, L, tol=1e-12, precision="mixed",
+                        want_jac=True, j_fp32=True, outputs=pinned_outputs(P, gm))
+
+
 def test_pipelined_requests_keep_their_jacobians():
-    """One slot, requests back to back: each Jacobian's device-to-host copy
-    overlaps the next request's compute (two device J buffers per solver), and
-    every request still receives its own complete J."""
+    """One slot, requests back to back with page-locked outputs: each
+    Jacobian's device-to-host copy overlaps the next request's compute (two
+    device J buffers per solver), and every request still receives its own
+    complete J, equal to the one of a request run alone."""
     probs = [small_cyl(100.0), small_cyl(100.0, seed=9)]
     meshes = [capi.Mesh(P.coords, P.elems) for P in probs]
     ref = []
@@ -110,7 +130,7 @@ def test_pipelined_requests_keep_their_jacobians():
     assert not np.array_equal(ref[0][2], ref[1][2])
     srv = capi.Server(slots=1, hbm_budget_gb=8.0)
     order = [0, 1, 0, 0, 1, 1, 0, 1]
-    ts = [srv.submit(make_request(probs[i], meshes[i])) for i in order]
+    ts = [srv.submit(make_pinned_request(probs[i], meshes[i])) for i in order]
     got = [outputs(srv.wait(t)) for t in ts]
     srv.close()
     for i, g in zip(order, got):
@@ -119,8 +139,9 @@ def test_pipelined_requests_keep_their_jacobians():
 
 
 def test_deferred_output_stream_on_the_solver():
-    """tg_solver_set_output_stream: the Jacobian lands in host memory once the
-    copy stream's work is done (tg_solver_sync), equal to the direct result."""
+    """tg_solver_set_output_stream: a page-locked Jacobian lands in host memory
+    once the copy stream's work is done (tg_solver_sync), equal to the direct
+    result, also when calls follow one another without a sync."""
     torch = pytest.importorskip("torch")
     P = small_cyl(100.0)
     gm = capi.Mesh(P.coords, P.elems)
@@ -129,11 +150,17 @@ def test_deferred_output_stream_on_the_solver():
     m = gm.qvec_gaussian(P.qm.M, P.mwidth) * ca[None, :]
     L = capi.Links(P.qm.link_ofs, P.qm.link_m)
     s = capi.FwdSolver(gm, "BICGSTAB", 1e-12, "ICH", True, precision="mixed")
-    direct = s.forward_path(cm, ck, ca, capi.omega_of(P.freq_mhz), q, m, L, want_fields=False, j_fp32=True)
+    om = capi.omega_of(P.freq_mhz)
+    direct = s.forward_path(cm, ck, ca, om, q, m, L, want_fields=False, j_fp32=True)
     cs = torch.cuda.Stream()
     s.set_output_stream(cs.cuda_stream)
-    for _ in range(3):
-        out = s.forward_path(cm, ck, ca, capi.omega_of(P.freq_mhz), q, m, L, want_fields=False, j_fp32=True)
-        s.sync()
-        assert np.array_equal(out["J"], direct["J"])
+    outs = [pinned_outputs(P, gm) for _ in range(3)]
+    qc, mc = np.ascontiguousarray(q, np.complex128), np.ascontiguousarray(m, np.complex128)
+    for o in outs:
+        s.forward_path_raw(np.ascontiguousarray(cm), np.ascontiguousarray(ck), np.ascontiguousarray(ca), om,
+                           q.shape[0], qc, m.shape[0], mc, L, None, None, o[0], o[1], o[2], 1, capi.MEM_HOST)
+    s.sync()
+    for o in outs:
+        assert np.array_equal(o[2], direct["J"])
+        assert np.array_equal(o[0], direct["proj"])
     s.set_output_stream(None)

@@ -1354,9 +1354,14 @@ static void api_forward_path(tg_solver s, const double* cmua, const double* ckap
     project_nm<V64>(s, X, k, nm, Ms, L, ylin, ylog);
     if (J) {
         size_t jbytes = (size_t)2 * nqm * (vt<V64>::cplx ? 2 * n : n) * (j_fp32 ? 4 : 8);
-        if (mem != TG_MEM_DEVICE && s->out_stream) {
-            // deferred: this request's J buffer was last copied out two
-            // requests ago; the copy of this one overlaps the next request
+        cudaPointerAttributes pa = {};
+        const bool locked = mem != TG_MEM_DEVICE && cudaPointerGetAttributes(&pa, J) == cudaSuccess &&
+                            pa.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+        if (locked && s->out_stream) {
+            // deferred (page-locked J only: a copy to pageable memory blocks
+            // the host anyway): this request's J buffer was last copied out
+            // two requests ago; the copy of this one overlaps the next request
             const int b = s->jflip;
             s->jflip ^= 1;
             if (!s->jready) {
