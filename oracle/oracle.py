@@ -36,7 +36,7 @@ def build(force: bool = False) -> str:
     """Compile the oracle shared library in place (gcc, a second or two)."""
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
         tmp = LIB + f".tmp{os.getpid()}"
-        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-o", tmp, SRC, "-lm", "-lpthread"])
+        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", tmp, SRC, "-lm", "-lpthread"])
         os.replace(tmp, LIB)
     return LIB
 
@@ -68,6 +68,11 @@ def lib():
                                    _dp, C.c_int]
         L.tor_a_keijzer.restype = C.c_double
         L.tor_a_keijzer.argtypes = [C.c_double]
+        L.tor_raster_pixel.restype = C.c_int
+        L.tor_raster_pixel.argtypes = [C.c_void_p, _ip, _dp, _dp, _ip, _ip, _ip, _dp]
+        L.tor_jacobian_grid.restype = C.c_int
+        L.tor_jacobian_grid.argtypes = [C.c_void_p, _ip, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int,
+                                        C.c_int, _dp]
         _lib = L
     return _lib
 
@@ -202,6 +207,54 @@ def jacobian(mesh: Mesh, dphi, aphi, proj_lin, link_ofs, link_m, logscale=True, 
                        _cview(proj_lin).ravel() if cplx else np.ascontiguousarray(proj_lin, np.float64).ravel(),
                        np.ascontiguousarray(link_ofs, np.int32), np.ascontiguousarray(link_m, np.int32),
                        int(cplx), int(logscale), J.reshape(-1), int(nthreads))
+    return J
+
+
+@dataclass
+class RasterPixel:
+    """Raster_Pixel with grid == basis: bounding box, element per grid point
+    (-1 outside), the grid map matrix B (CSR, natural node numbering) and the
+    solution points (grid points inside the mesh, in grid order)."""
+    bdim: np.ndarray
+    bbmin: np.ndarray
+    bbmax: np.ndarray
+    elref: np.ndarray
+    browptr: np.ndarray
+    bcol: np.ndarray
+    bval: np.ndarray
+
+    @property
+    def sol(self):
+        return np.nonzero(self.elref >= 0)[0].astype(np.int32)
+
+
+def raster_pixel(mesh: Mesh, bdim) -> RasterPixel:
+    bdim = np.ascontiguousarray(bdim, np.int32)
+    glen = int(np.prod(bdim))
+    nn = mesh.elems.shape[1]
+    bbmin, bbmax = np.zeros(mesh.dim), np.zeros(mesh.dim)
+    elref = np.zeros(glen, np.int32)
+    rp = np.zeros(glen + 1, np.int32)
+    col = np.zeros(glen * nn, np.int32)
+    val = np.zeros(glen * nn)
+    lib().tor_raster_pixel(mesh._h, bdim, bbmin, bbmax, elref, rp, col, val)
+    return RasterPixel(bdim, bbmin, bbmax, elref, rp, col[:rp[-1]].copy(), val[:rp[-1]].copy())
+
+
+def jacobian_grid(mesh: Mesh, bdim, dphi, aphi, proj_lin, link_ofs, link_m, logscale=True):
+    """Grid-basis Jacobian for Raster_Pixel(bdim, bdim): complex (2 nQM) x
+    (2 slen), real (2 nQM) x slen."""
+    cplx = np.iscomplexobj(dphi)
+    bdim = np.ascontiguousarray(bdim, np.int32)
+    nq, n = dphi.shape
+    nm = aphi.shape[0]
+    nqm = int(link_ofs[-1])
+    slen = int((raster_pixel(mesh, bdim).elref >= 0).sum())
+    J = np.zeros((2 * nqm, 2 * slen) if cplx else (2 * nqm, slen))
+    f = (lambda a: _cview(a).ravel()) if cplx else (lambda a: np.ascontiguousarray(a, np.float64).ravel())
+    lib().tor_jacobian_grid(mesh._h, bdim, nq, nm, f(dphi), f(aphi), f(proj_lin),
+                            np.ascontiguousarray(link_ofs, np.int32), np.ascontiguousarray(link_m, np.int32),
+                            int(cplx), int(logscale), J.reshape(-1))
     return J
 
 

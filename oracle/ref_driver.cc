@@ -14,11 +14,15 @@
 //              dtype=real|complex solver=CG|BICGSTAB|GMRES precon=NONE|DIAG|ICH
 //              tol=1e-10 maxit=0 freq=100 qwidth=2 mwidth=2 nth=1
 //              (params=P.bin | mua=0.025 mus=2 nref=1.4) jac=0|1 fields=0|1
-//              sysmat=0|1 qsub=0 msub=0
+//              sysmat=0|1 qsub=0 msub=0 grid=NX,NY[,NZ]
 // optodes.bin: int32 dim,nQ,nM ; nQ*dim doubles ; nM*dim doubles (all-to-all links)
 // params.bin : n*3 doubles, node-major (mua, mus', nref)
 // qsub/msub  : if >0, only the first qsub sources / msub detectors are solved
 //              (bounded CPU baseline samples); the Jacobian is then skipped.
+// grid       : also the grid-basis Jacobian for Raster_Pixel(bdim = gdim =
+//              grid) (src/python/toastmodule.cc:696, raster_px.cc:10-48),
+//              LOG data, written with the raster's element reference per grid
+//              point (PREFIX_Jgrid.bin, PREFIX_elref.bin).
 #include "stoastlib.h"
 #include <fstream>
 #include <iostream>
@@ -103,6 +107,16 @@ int main(int argc, char** argv) {
     bool want_fields = atoi(arg("fields", "0").c_str()) != 0;
     bool want_sys = atoi(arg("sysmat", "0").c_str()) != 0;
     int qsub = atoi(arg("qsub", "0").c_str());
+    std::vector<int> grid;
+    {
+        string g = arg("grid", "");
+        for (size_t a = 0; a < g.size();) {
+            size_t b = g.find(',', a);
+            if (b == string::npos) b = g.size();
+            grid.push_back(atoi(g.substr(a, b - a).c_str()));
+            a = b + 1;
+        }
+    }
     int msub = atoi(arg("msub", "0").c_str());
 
     Task_Init(nth);
@@ -213,6 +227,16 @@ int main(int argc, char** argv) {
                 fprintf(info, "t_jac %.9g\n", walltoc(t0));
                 wbin(out + "_J.bin", J.ValPtr(), (size_t)2 * nQM * 2 * n * sizeof(double));
             }
+            if ((int)grid.size() == dim) {
+                IVector bdim(dim, grid.data());
+                Raster_Pixel raster(bdim, bdim, &mesh);
+                int slen = raster.SLen(), glen = raster.GLen();
+                RDenseMatrix Jg(2 * nQM, 2 * slen);
+                GenerateJacobian(&raster, &mesh, dphi, aphi, &proj, DATA_LOG, Jg);
+                wbin(out + "_Jgrid.bin", Jg.ValPtr(), (size_t)2 * nQM * 2 * slen * sizeof(double));
+                wbin(out + "_elref.bin", raster.Elref(), (size_t)glen * sizeof(int));
+                fprintf(info, "slen %d\nglen %d\n", slen, glen);
+            }
         }
         if (want_fields) {
             FILE* f = fopen((out + "_dphi.bin").c_str(), "wb");
@@ -272,6 +296,19 @@ int main(int argc, char** argv) {
                 fwrite(Jmua.ValPtr(), sizeof(double), (size_t)nQM * n, f);
                 fwrite(Jkap.ValPtr(), sizeof(double), (size_t)nQM * n, f);
                 fclose(f);
+            }
+            if ((int)grid.size() == dim) {
+                IVector bdim(dim, grid.data());
+                Raster_Pixel raster(bdim, bdim, &mesh);
+                int slen = raster.SLen(), glen = raster.GLen();
+                RDenseMatrix Jmua, Jkap;
+                GenerateJacobian_cw(&raster, &mesh, dphi, aphi, &proj, DATA_LOG, &Jmua, &Jkap);
+                FILE* f = fopen((out + "_Jgrid.bin").c_str(), "wb");
+                fwrite(Jmua.ValPtr(), sizeof(double), (size_t)nQM * slen, f);
+                fwrite(Jkap.ValPtr(), sizeof(double), (size_t)nQM * slen, f);
+                fclose(f);
+                wbin(out + "_elref.bin", raster.Elref(), (size_t)glen * sizeof(int));
+                fprintf(info, "slen %d\nglen %d\n", slen, glen);
             }
         }
         if (want_fields) {

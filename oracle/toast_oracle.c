@@ -1194,6 +1194,261 @@ void tor_jacobian(const tor_mesh *m, int nq, int nm, const double *dphi, const d
     free(jobs); free(th);
 }
 
+/* ------------------------------------------------------------------------ */
+/* Pixel raster and the grid-basis Jacobian                                  */
+/* ------------------------------------------------------------------------ */
+
+/* Element_Unstructured::GContains (element.cc:553-563): the element's
+   bounding box widened by 1e-8, then Element::GContains (element.cc:178-182):
+   LContains(Local(p)) with the padded test (pad = true, tri3.cc:191-200,
+   tet4.cc:268-279); Local per tri3.cc:134-144, tet4.cc:186-196. */
+static int el_gcontains(const tor_mesh *m, int e, const double *p)
+{
+    const int dim = m->dim, nn = m->nn;
+    const int *nd = m->el + (size_t)e * nn;
+    for (int d = 0; d < dim; d++) {  /* Element_Unstructured::Initialise (element.cc:528-536) */
+        double lo = 1e10, hi = -1e10;
+        for (int i = 0; i < nn; i++) {
+            double v = m->x[(size_t)nd[i] * dim + d];
+            if (v < lo) lo = v;
+            if (v > hi) hi = v;
+        }
+        if (p[d] < lo - 1e-8 || p[d] > hi + 1e-8) return 0;
+    }
+    const double *g = m->geo + (size_t)e * 16;
+    const double EPS = 1e-8;
+    if (dim == 2) {
+        double scale = 1.0 / (g[0] + g[1] + g[2]);
+        double l0 = (g[1] + g[4] * p[0] + g[7] * p[1]) * scale;
+        double l1 = (g[2] + g[5] * p[0] + g[8] * p[1]) * scale;
+        return l0 + EPS >= 0.0 && l1 + EPS >= 0.0 && l0 + l1 - EPS <= 1.0;
+    }
+    const double *a = g, *b = g + 4, *c = g + 8, *dd = g + 12;
+    double scale = 1.0 / (a[0] + a[1] + a[2] + a[3]);
+    double l[3];
+    for (int r = 0; r < 3; r++) l[r] = (a[r + 1] + b[r + 1] * p[0] + c[r + 1] * p[1] + dd[r + 1] * p[2]) * scale;
+    return l[0] + EPS >= 0.0 && l[1] + EPS >= 0.0 && l[2] + EPS >= 0.0 && l[0] + l[1] + l[2] - EPS <= 1.0;
+}
+
+/* Raster_Pixel with the grid equal to the basis (raster.cc:18-83,
+   raster_px.cc:10-48, the case bdim == gdim):
+   - bounding box: Mesh::BoundingBox (mesh.cc:1341-1360), no padding;
+   - elref: GenerateElementPixelRef (mesh.cc:2944-3014), the first element
+     (in element order) containing each grid point, -1 outside;
+   - B: GridMapMatrix (mesh.cc:2486-2554), row g = the containing element's
+     global shape functions at the grid point (tri3.cc:231-240,
+     tet4.cc:302-313), in the element's node order.
+   Returns glen.  browptr: glen+1, bcol / bval: glen*nn (room for every row). */
+int tor_raster_pixel(const tor_mesh *m, const int *bdim, double *bbmin, double *bbmax, int *elref,
+                     int *browptr, int *bcol, double *bval)
+{
+    const int dim = m->dim, nn = m->nn;
+    for (int d = 0; d < dim; d++) { bbmin[d] = 1e6; bbmax[d] = -1e6; }
+    for (int k = 0; k < m->n; k++)
+        for (int d = 0; d < dim; d++) {
+            double v = m->x[(size_t)k * dim + d];
+            if (v < bbmin[d]) bbmin[d] = v;
+            if (v > bbmax[d]) bbmax[d] = v;
+        }
+    const int nx = bdim[0], ny = bdim[1], nz = dim > 2 ? bdim[2] : 1;
+    const int glen = nx * ny * nz;
+    double dW[3];
+    for (int d = 0; d < dim; d++) dW[d] = (bbmax[d] - bbmin[d]) / (double)(bdim[d] - 1);
+    for (int i = 0; i < glen; i++) elref[i] = -1;
+    for (int e = 0; e < m->ne; e++) {
+        const int *nd = m->el + (size_t)e * nn;
+        double lo[3], hi[3];
+        for (int d = 0; d < dim; d++) { lo[d] = 1e10; hi[d] = -1e10; }
+        for (int i = 0; i < nn; i++)
+            for (int d = 0; d < dim; d++) {
+                double v = m->x[(size_t)nd[i] * dim + d];
+                if (v < lo[d]) lo[d] = v;
+                if (v > hi[d]) hi[d] = v;
+            }
+        int rmin[3] = {0, 0, 0}, rmax[3] = {1, 1, 1}, skip = 0;
+        for (int d = 0; d < dim; d++) {
+            lo[d] -= 1e-6;
+            hi[d] += 1e-6;
+            if (lo[d] > bbmax[d] || hi[d] < bbmin[d]) { skip = 1; break; }
+            int a = (int)ceil((lo[d] - bbmin[d]) / dW[d]);
+            int b = (int)floor((hi[d] - bbmin[d]) / dW[d]) + 1;
+            rmin[d] = a > 0 ? a : 0;
+            rmax[d] = b < bdim[d] ? b : bdim[d];
+        }
+        if (skip) continue;
+        double p[3] = {0.0, 0.0, 0.0};
+        for (int iz = rmin[2]; iz < rmax[2]; iz++) {
+            if (dim > 2) p[2] = iz * dW[2] + bbmin[2];
+            for (int iy = rmin[1]; iy < rmax[1]; iy++) {
+                p[1] = iy * dW[1] + bbmin[1];
+                for (int ix = rmin[0]; ix < rmax[0]; ix++) {
+                    int idx = ix + nx * (iy + ny * iz);
+                    if (elref[idx] >= 0) continue;
+                    p[0] = ix * dW[0] + bbmin[0];
+                    if (el_gcontains(m, e, p)) elref[idx] = e;
+                }
+            }
+        }
+    }
+    int k = 0;
+    browptr[0] = 0;
+    for (int iz = 0, i = 0; iz < nz; iz++) {
+        double p[3] = {0.0, 0.0, 0.0};
+        if (dim > 2) p[2] = iz * dW[2] + bbmin[2];
+        for (int iy = 0; iy < ny; iy++) {
+            p[1] = iy * dW[1] + bbmin[1];
+            for (int ix = 0; ix < nx; ix++, i++) {
+                int e = elref[i];
+                if (e >= 0) {
+                    p[0] = ix * dW[0] + bbmin[0];
+                    const int *nd = m->el + (size_t)e * nn;
+                    const double *g = m->geo + (size_t)e * 16;
+                    if (dim == 2) {
+                        double scale = 1.0 / (2.0 * m->size[e]);
+                        for (int j = 0; j < 3; j++) {
+                            bcol[k] = nd[j];
+                            bval[k++] = scale * (g[j] + g[3 + j] * p[0] + g[6 + j] * p[1]);
+                        }
+                    } else {
+                        double scale = 1.0 / (6.0 * m->size[e]);
+                        for (int j = 0; j < 4; j++) {
+                            bcol[k] = nd[j];
+                            bval[k++] = scale * (g[j] + g[4 + j] * p[0] + g[8 + j] * p[1] + g[12 + j] * p[2]);
+                        }
+                    }
+                }
+                browptr[i + 1] = k;
+            }
+        }
+    }
+    return glen;
+}
+
+/* ImageGradient (jacobian.cc:944-1060): central differences where both
+   neighbours are in the mask, one-sided where one is, 0 outside the mask;
+   spacing gsize/n (sic: n, not n-1).  mask NULL: every point counts as
+   inside.  grad: dim planes of glen values. */
+static void image_gradient(int dim, const int *gdim, const double *gsize, const zd *im, zd *grad, const int *mask)
+{
+    const int nx = gdim[0], ny = gdim[1], nz = dim >= 3 ? gdim[2] : 1, n = nx * ny * nz;
+    const int stride[3] = {1, nx, nx * ny}, len[3] = {nx, ny, nz};
+    for (int d = 0; d < dim; d++) {
+        double h = gsize[d] / len[d], ih = 1.0 / h, i2h = 0.5 * ih;
+        zd *gr = grad + (size_t)d * n;
+        for (int z = 0, idx = 0; z < nz; z++)
+            for (int y = 0; y < ny; y++)
+                for (int x = 0; x < nx; x++, idx++) {
+                    int c = d == 0 ? x : (d == 1 ? y : z);
+                    int st = stride[d];
+                    int bcnt = !mask || mask[idx] >= 0;
+                    int blo = c > 0 && (!mask || mask[idx - st] >= 0);
+                    int bhi = c < len[d] - 1 && (!mask || mask[idx + st] >= 0);
+                    zd v;
+                    if (blo && bhi) v = (im[idx + st] - im[idx - st]) * i2h;
+                    else if (!bcnt) v = 0.0;
+                    else if (blo) v = (im[idx] - im[idx - st]) * ih;
+                    else if (bhi) v = (im[idx + st] - im[idx]) * ih;
+                    else v = 0.0;
+                    gr[idx] = v;
+                }
+    }
+}
+
+/* Map_MeshToGrid (raster.cc:188-199; RCompRowMatrix::Ax_cplx,
+   crmatrix_imp.hpp:1302-1327): g = B f, row by row in entry order */
+static void grid_map(int glen, const int *browptr, const int *bcol, const double *bval, const zd *f, zd *g)
+{
+    for (int r = 0; r < glen; r++) {
+        double re = 0.0, im = 0.0;
+        for (int j = browptr[r]; j < browptr[r + 1]; j++) {
+            re += creal(f[bcol[j]]) * bval[j];
+            im += cimag(f[bcol[j]]) * bval[j];
+        }
+        g[r] = re + I * im;
+    }
+}
+
+/* Grid-basis Jacobian for Raster_Pixel with bdim == gdim.
+   Complex (GenerateJacobian_grid with projections, jacobian.cc:289-373):
+   PMDF_mua = -(f a), PMDF_kap = -sum_d grad_d f grad_d a (jacobian.cc:58-72),
+   both gradients masked by elref; LOG divides by y (PMDF_log, 76-79); the
+   solution points are the grid points with elref >= 0 in grid order
+   (raster.cc:66-77, Map_BasisToSol 305-315); J(l, s) = Re, J(l+nQM, s) = Im,
+   kappa at column slen + s; then J *= prod gsize/(bdim-1).
+   Real (GenerateJacobian_cw_grid, jacobian.cc:516-712, the threaded engine):
+   the adjoint gradient is NOT masked; Jmua = PMDF_mua, Jkap = PMDF_kap (rows
+   nQM + l), times the voxel scale, then, for LOG data, each row times 1/y
+   (GenerateJacobian_cw, 178-193).
+   J: complex (2 nQM) x (2 slen), real (2 nQM) x slen.  Returns slen. */
+int tor_jacobian_grid(const tor_mesh *m, const int *bdim, int nq, int nm, const double *dphi, const double *aphi,
+                      const double *proj, const int *link_ofs, const int *link_m, int cplx, int logscale,
+                      double *J)
+{
+    const int dim = m->dim, nn = m->nn, n = m->n;
+    int glen = 1;
+    for (int d = 0; d < dim; d++) glen *= bdim[d];
+    double bbmin[3], bbmax[3], gsize[3];
+    int *elref = malloc(sizeof(int) * glen), *browptr = malloc(sizeof(int) * (glen + 1));
+    int *bcol = malloc(sizeof(int) * (size_t)glen * nn);
+    double *bval = malloc(sizeof(double) * (size_t)glen * nn);
+    tor_raster_pixel(m, bdim, bbmin, bbmax, elref, browptr, bcol, bval);
+    for (int d = 0; d < dim; d++) gsize[d] = bbmax[d] - bbmin[d];
+    int slen = 0;
+    int *sol = malloc(sizeof(int) * glen);
+    for (int i = 0; i < glen; i++) if (elref[i] >= 0) sol[slen++] = i;
+    const int nqm = link_ofs[nq];
+    zd *fin = malloc(sizeof(zd) * n);
+    zd *ag = malloc(sizeof(zd) * (size_t)nm * glen), *agr = malloc(sizeof(zd) * (size_t)nm * dim * glen);
+    zd *dg = malloc(sizeof(zd) * glen), *dgr = malloc(sizeof(zd) * (size_t)dim * glen);
+    zd *pm = malloc(sizeof(zd) * glen), *pk = malloc(sizeof(zd) * glen);
+    for (int j = 0; j < nm; j++) {
+        for (int i = 0; i < n; i++)
+            fin[i] = cplx ? aphi[2 * ((size_t)j * n + i)] + I * aphi[2 * ((size_t)j * n + i) + 1] : aphi[(size_t)j * n + i];
+        grid_map(glen, browptr, bcol, bval, fin, ag + (size_t)j * glen);
+        image_gradient(dim, bdim, gsize, ag + (size_t)j * glen, agr + (size_t)j * dim * glen, cplx ? elref : NULL);
+    }
+    double sz = 1.0;
+    for (int d = 0; d < dim; d++) sz *= gsize[d] / (bdim[d] - 1.0);
+    const size_t cols = cplx ? 2 * (size_t)slen : (size_t)slen;
+    for (int q = 0; q < nq; q++) {
+        for (int i = 0; i < n; i++)
+            fin[i] = cplx ? dphi[2 * ((size_t)q * n + i)] + I * dphi[2 * ((size_t)q * n + i) + 1] : dphi[(size_t)q * n + i];
+        grid_map(glen, browptr, bcol, bval, fin, dg);
+        image_gradient(dim, bdim, gsize, dg, dgr, elref);
+        for (int l = link_ofs[q]; l < link_ofs[q + 1]; l++) {
+            const int j = link_m[l];
+            const zd *a = ag + (size_t)j * glen, *agj = agr + (size_t)j * dim * glen;
+            for (int g = 0; g < glen; g++) {
+                pm[g] = -(dg[g] * a[g]);
+                zd kk = 0.0;
+                for (int d = 0; d < dim; d++) kk -= dgr[(size_t)d * glen + g] * agj[(size_t)d * glen + g];
+                pk[g] = kk;
+            }
+            if (cplx) {
+                zd y = proj[2 * l] + I * proj[2 * l + 1];
+                double *r0 = J + (size_t)l * cols, *r1 = J + (size_t)(l + nqm) * cols;
+                for (int s = 0; s < slen; s++) {
+                    zd vm = pm[sol[s]], vk = pk[sol[s]];
+                    if (logscale) { vm = vm / y; vk = vk / y; }
+                    r0[s] = creal(vm) * sz; r1[s] = cimag(vm) * sz;
+                    r0[slen + s] = creal(vk) * sz; r1[slen + s] = cimag(vk) * sz;
+                }
+            } else {
+                double iy = 1.0 / proj[l];
+                double *r0 = J + (size_t)l * cols, *r1 = J + (size_t)(l + nqm) * cols;
+                for (int s = 0; s < slen; s++) {
+                    double vm = creal(pm[sol[s]]) * sz, vk = creal(pk[sol[s]]) * sz;
+                    r0[s] = logscale ? vm * iy : vm;
+                    r1[s] = logscale ? vk * iy : vk;
+                }
+            }
+        }
+    }
+    free(elref); free(browptr); free(bcol); free(bval); free(sol); free(fin);
+    free(ag); free(agr); free(dg); free(dgr); free(pm); free(pk);
+    return slen;
+}
+
 /* A_Keijzer (param.cc:24-32) */
 double tor_a_keijzer(double n)
 {

@@ -10,8 +10,14 @@ CalcJacobianCW call sequence, LOG data).  The GPU parity tests and the oracle
 tests compare against these files, so they need neither the reference tree
 nor the compiled reference at run time.
 
+The *_grid fixtures add the grid-basis Jacobian of Raster_Pixel with the
+basis equal to the grid (what toast.Raster(mesh, grd) builds,
+src/python/toastmodule.cc:696), the raster's element reference per grid
+point and the reference's own fields, so the oracle's raster and grid
+Jacobian are checked on exactly the reference's inputs.
+
 Usage:  make -f oracle/Makefile.ref REF=<reference tree> -j8
-        python tests/golden/make_golden.py
+        python tests/golden/make_golden.py [fixture names]
 """
 import os
 import subprocess
@@ -50,6 +56,11 @@ FIXTURES = {
     "cyl_cw_cg_ich": (lambda: small_cylinder(0.0), "CG", "ICH", 1e-15, True),
     "cyl_fd_bicgstab_ich": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-15, True),
     "cyl_fd_gmres_ich": (lambda: small_cylinder(100.0), "GMRES", "ICH", 1e-15, False),
+    # grid-basis Jacobians (Raster_Pixel, basis = grid)
+    "disc_cw_grid": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "ICH", 1e-15, False, (24, 24)),
+    "disc_fd_grid": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (24, 20)),
+    "cyl_cw_grid": (lambda: small_cylinder(0.0), "CG", "ICH", 1e-15, False, (9, 10, 12)),
+    "cyl_fd_grid": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-15, False, (10, 9, 11)),
 }
 
 
@@ -57,7 +68,7 @@ def rd(path, dtype):
     return np.fromfile(path, dtype=dtype)
 
 
-def run(name, factory, solver, precon, tol, jac):
+def run(name, factory, solver, precon, tol, jac, grid=None):
     P = factory()
     cplx = P.complex
     with tempfile.TemporaryDirectory() as td:
@@ -74,6 +85,8 @@ def run(name, factory, solver, precon, tol, jac):
         args = [DRIVER, f"mesh={msh}", f"optodes={opt}", f"out={out}", f"params={par}",
                 f"dtype={'complex' if cplx else 'real'}", f"solver={solver}", f"precon={precon}", f"tol={tol}",
                 "maxit=0", f"freq={P.freq_mhz}", f"qwidth={P.qwidth}", f"mwidth={P.mwidth}", f"jac={int(jac)}"]
+        if grid:
+            args += ["grid=" + ",".join(str(g) for g in grid), "fields=1"]
         subprocess.run(args, check=True)
         info = dict(l.split() for l in open(out + "_info.txt") if l.strip())
         ct = np.complex128 if cplx else np.float64
@@ -83,6 +96,15 @@ def run(name, factory, solver, precon, tol, jac):
             nqm = len(res["proj"])
             J = rd(out + "_J.bin", np.float64)
             res["J"] = J.reshape((2 * nqm, 2 * P.n) if cplx else (2 * nqm, P.n))
+        if grid:
+            nqm = len(res["proj"])
+            slen = int(info["slen"])
+            Jg = rd(out + "_Jgrid.bin", np.float64)
+            res["Jgrid"] = Jg.reshape((2 * nqm, 2 * slen) if cplx else (2 * nqm, slen))
+            res["elref"] = rd(out + "_elref.bin", np.int32)
+            res["bdim"] = np.array(grid, np.int32)
+            res["dphi"] = rd(out + "_dphi.bin", ct).reshape(len(P.qm.Q), P.n)
+            res["aphi"] = rd(out + "_aphi.bin", ct).reshape(len(P.qm.M), P.n)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), coords=P.coords, elems=P.elems, Q=P.qm.Q, M=P.qm.M,
                         link_ofs=P.qm.link_ofs, link_m=P.qm.link_m, mua=P.mua, mus=P.mus, nref=P.nref,
                         freq_mhz=P.freq_mhz, qwidth=P.qwidth, mwidth=P.mwidth, solver=solver, precon=precon,
@@ -93,8 +115,9 @@ def run(name, factory, solver, precon, tol, jac):
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("build the reference driver first: make -f oracle/Makefile.ref REF=<reference tree>")
-    for name, spec in FIXTURES.items():
-        run(name, *spec)
+    names = sys.argv[1:] or list(FIXTURES)
+    for name in names:
+        run(name, *FIXTURES[name])
 
 
 if __name__ == "__main__":

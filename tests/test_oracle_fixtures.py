@@ -26,3 +26,20 @@ def test_oracle_matches_reference_fixture(oracle_mod, name):
     if "J" in g:
         J = res.J.reshape(g["J"].shape)
         assert rel2(J, g["J"]) < 1e-9
+
+
+GRID = [n for n in names() if n.endswith("_grid")]
+
+
+@pytest.mark.parametrize("name", GRID)
+def test_oracle_grid_jacobian_matches_reference(oracle_mod, name):
+    """Raster_Pixel (basis = grid) and the grid-basis Jacobian on the
+    reference's own fields: the element reference per grid point and every
+    Jacobian entry equal the reference's bit for bit."""
+    g = load(name)
+    mesh = oracle_mod.Mesh(g["coords"], g["elems"])
+    r = oracle_mod.raster_pixel(mesh, g["bdim"])
+    assert np.array_equal(r.elref, g["elref"])
+    J = oracle_mod.jacobian_grid(mesh, g["bdim"], g["dphi"], g["aphi"], g["proj"], g["link_ofs"], g["link_m"])
+    assert J.shape == g["Jgrid"].shape
+    assert np.array_equal(J, g["Jgrid"])
