@@ -259,6 +259,31 @@ int tg_solver_profile(tg_solver s, int mask);
 int tg_solver_profile_read(tg_solver s, int cls, double *total_ms, int *count);
 /* number of kernels this library has launched in this process */
 int tg_launch_count(long long *count);
+/* ---- grid basis (pixel raster) ----
+   Raster_Pixel with the basis equal to the grid, as toast.Raster(mesh, grd)
+   builds it (src/python/toastmodule.cc:696; raster.cc:18-83,
+   raster_px.cc:10-48): a regular grid of bdim[0] x bdim[1] (x bdim[2])
+   points over the mesh's bounding box; the solution points are the grid
+   points inside the mesh, in grid order (x fastest).  A raster built on a
+   different intermediate grid (gdim != bdim) is not supported. */
+typedef struct tg_raster_s *tg_raster;
+int tg_raster_create(tg_mesh mesh, const int *bdim, tg_raster *out);
+int tg_raster_destroy(tg_raster r);
+/* glen grid points, slen solution points, bounding box (dim values each) */
+int tg_raster_info(tg_raster r, int *glen, int *slen, double *bbmin, double *bbmax);
+/* element containing each grid point, -1 outside (Raster::Elref) */
+int tg_raster_elref(tg_raster r, int *elref);
+/* Grid-basis Jacobian (GenerateJacobian with a raster, jacobian.cc:105-123
+   -> GenerateJacobian_grid 289-373; real systems GenerateJacobian_cw with a
+   raster, 178-193 -> GenerateJacobian_cw_grid 610-712).  Inputs as
+   tg_jacobian (source-major natural fields, projections for LOG data).
+   J row-major: complex (2 nQM) x (2 slen) = [Re mua | Re kappa ; Im mua |
+   Im kappa]; real (2 nQM) x slen = [mua ; kappa].  out_fp32 selects an FP32
+   J computed in FP32, else FP64 throughout. */
+int tg_jacobian_grid(tg_solver s, tg_raster r, int nq, const double *dphi, int nm, const double *aphi,
+                     const double *proj, const int *link_ofs, const int *link_m, int scale, void *J,
+                     int out_fp32, int mem);
+
 /* the SpMM autotuner's decisions so far: one text line per (mesh, value type,
    columns) with every candidate kernel's best launch time and the choice.
    The environment variable TOASTGPU_SPMM_VARIANT (spmm_halo, spmm_vec,

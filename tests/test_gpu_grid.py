@@ -1,0 +1,80 @@
+"""Grid-basis Jacobian (pixel raster, basis = grid) on the GPU against the
+reference's own outputs (tests/golden/*_grid.npz, made by the compiled
+reference) and the oracle."""
+import numpy as np
+import pytest
+
+from tests.golden_util import load, names
+from tests.gpu_util import rel2
+from toastpp_gb300 import capi
+
+pytestmark = pytest.mark.gpu
+
+GRID = [n for n in names() if n.endswith("_grid")]
+
+
+def setup(name):
+    g = load(name)
+    gm = capi.Mesh(g["coords"], g["elems"])
+    r = capi.Raster(gm, g["bdim"])
+    cplx = np.iscomplexobj(g["proj"])
+    s = capi.FwdSolver(gm, g["solver"], 1e-15, g["precon"], cplx, precision="fp64")
+    return g, gm, r, s, capi.Links(g["link_ofs"], g["link_m"])
+
+
+@pytest.mark.parametrize("name", GRID)
+def test_raster_matches_reference(name):
+    g, gm, r, s, L = setup(name)
+    assert r.glen == int(np.prod(g["bdim"]))
+    assert np.array_equal(r.elref(), g["elref"])
+    assert r.slen == int((g["elref"] >= 0).sum())
+
+
+@pytest.mark.parametrize("name", GRID)
+def test_grid_jacobian_on_reference_fields(name):
+    """Same fields as the reference: FP64 agrees to round-off, FP32 to FP32
+    accuracy."""
+    g, gm, r, s, L = setup(name)
+    J = s.jacobian_grid(r, g["dphi"], g["aphi"], g["proj"], L)
+    ref = g["Jgrid"]
+    assert J.shape == ref.shape
+    assert rel2(J, ref) < 1e-13
+    assert np.abs(J - ref).max() <= 1e-12 * np.abs(ref).max()
+    J32 = s.jacobian_grid(r, g["dphi"], g["aphi"], g["proj"], L, fp32=True)
+    assert J32.dtype == np.float32
+    assert rel2(J32.astype(np.float64), ref) < 1e-5
+
+
+@pytest.mark.parametrize("name", GRID)
+def test_grid_jacobian_linear_data_against_oracle(name, oracle_mod):
+    g, gm, r, s, L = setup(name)
+    J = s.jacobian_grid(r, g["dphi"], g["aphi"], None, L, scale=capi.DATA_LIN)
+    om = oracle_mod.Mesh(g["coords"], g["elems"])
+    ref = oracle_mod.jacobian_grid(om, g["bdim"], g["dphi"], g["aphi"], g["proj"], g["link_ofs"], g["link_m"],
+                                   logscale=False)
+    assert rel2(J, ref) < 1e-13
+
+
+@pytest.mark.parametrize("name", GRID)
+def test_grid_jacobian_end_to_end(name):
+    """GPU fields (FP64 path) -> projections -> grid Jacobian, against the
+    reference's Jacobian from its own fields."""
+    g, gm, r, s, L = setup(name)
+    cm, ck, ca = capi.optical_coefficients(g["mua"], g["mus"], g["nref"])
+    s.reset(cm, ck, ca, capi.omega_of(g["freq_mhz"]))
+    q = gm.qvec_gaussian(g["Q"], g["qwidth"])
+    m = gm.qvec_gaussian(g["M"], g["mwidth"]) * ca[None, :]
+    dphi, _ = s.calc_fields(q)
+    aphi, _ = s.calc_fields(m)
+    proj = s.project_all(m, dphi, L, capi.DATA_LIN)
+    J = s.jacobian_grid(r, dphi, aphi, proj, L)
+    assert rel2(J, g["Jgrid"]) < 1e-9
+
+
+def test_raster_of_another_mesh_is_rejected():
+    g, gm, r, s, L = setup(GRID[0])
+    g2 = load(GRID[-1])
+    other = capi.Mesh(g2["coords"], g2["elems"])
+    r2 = capi.Raster(other, g2["bdim"])
+    with pytest.raises(capi.ToastGPUError):
+        s.jacobian_grid(r2, g["dphi"], g["aphi"], g["proj"], L)

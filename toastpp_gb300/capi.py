@@ -26,7 +26,7 @@ DATA_LIN, DATA_LOG = 1, 2
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
            "tg_qvec_gaussian", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream", "tg_solver_set_output_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
-           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log",
+           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_raster_create", "tg_raster_destroy", "tg_raster_info", "tg_raster_elref", "tg_jacobian_grid",
            "tg_server_create", "tg_server_destroy", "tg_submit", "tg_poll", "tg_wait", "tg_server_stats",
            "tg_server_reset_stats", "tg_last_error"]
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
@@ -89,6 +89,11 @@ def lib():
             "tg_solver_profile_read": [vp, i_, C.POINTER(C.c_double), ip],
             "tg_launch_count": [C.POINTER(C.c_longlong)],
             "tg_tuner_log": [C.c_char_p, i_],
+            "tg_raster_create": [vp, ip, C.POINTER(C.c_void_p)],
+            "tg_raster_destroy": [vp],
+            "tg_raster_info": [vp, ip, ip, dp, dp],
+            "tg_raster_elref": [vp, ip],
+            "tg_jacobian_grid": [vp, vp, i_, dp, i_, dp, dp, vp, vp, i_, vp, i_, i_],
             "tg_server_create": [i_, d_, C.POINTER(C.c_void_p)],
             "tg_server_destroy": [vp],
             "tg_submit": [vp, vp, C.POINTER(C.c_longlong)],
@@ -280,6 +285,18 @@ class FwdSolver:
         _check(lib().tg_project_all_noalloc(self._h, int(nq), _ptr(d_phi), int(nm), _ptr(d_mvec), _ptr(links.ofs),
                                             _ptr(links.m), int(scale), _ptr(d_proj)))
 
+    def jacobian_grid(self, raster: "Raster", dphi, aphi, proj, links: Links, scale=DATA_LOG, fp32=False):
+        """Grid-basis Jacobian (tg_jacobian_grid): complex (2 nQM) x (2 slen),
+        real (2 nQM) x slen."""
+        dphi = _f64(dphi, self.complex)
+        aphi = _f64(aphi, self.complex)
+        nqm, slen = links.nqm, raster.slen
+        J = np.zeros((2 * nqm, 2 * slen if self.complex else slen), np.float32 if fp32 else np.float64)
+        pr = None if proj is None else _f64(proj, self.complex)
+        _check(lib().tg_jacobian_grid(self._h, raster._h, dphi.shape[0], _ptr(dphi), aphi.shape[0], _ptr(aphi),
+                                      _ptr(pr), _ptr(links.ofs), _ptr(links.m), scale, _ptr(J), int(fp32), MEM_HOST))
+        return J
+
     def jacobian(self, dphi, aphi, proj, links: Links, scale=DATA_LOG, fp32=False):
         dphi = _f64(dphi, self.complex)
         aphi = _f64(aphi, self.complex)
@@ -340,6 +357,38 @@ def optical_coefficients(mua, mus, nref):
 def omega_of(freq_mhz):
     """Modulation frequency [MHz] -> omega [rad/ps] (src/supertoast/fwdfem.cc:116)."""
     return freq_mhz * 2.0 * np.pi * 1e-6
+
+
+class Raster:
+    """tg_raster: the pixel raster with basis = grid (toast.Raster(mesh, grd))."""
+
+    def __init__(self, mesh: Mesh, bdim):
+        self.mesh = mesh
+        self.bdim = np.ascontiguousarray(bdim, np.int32)
+        h = C.c_void_p()
+        _check(lib().tg_raster_create(mesh._h, self.bdim.ctypes.data_as(C.POINTER(C.c_int)), C.byref(h)))
+        self._h = h
+        gl, sl = C.c_int(), C.c_int()
+        self.bbmin, self.bbmax = np.zeros(len(self.bdim)), np.zeros(len(self.bdim))
+        _check(lib().tg_raster_info(self._h, C.byref(gl), C.byref(sl), self.bbmin.ctypes.data_as(C.POINTER(C.c_double)),
+                                    self.bbmax.ctypes.data_as(C.POINTER(C.c_double))))
+        self.glen, self.slen = gl.value, sl.value
+
+    def elref(self):
+        out = np.zeros(self.glen, np.int32)
+        _check(lib().tg_raster_elref(self._h, out.ctypes.data_as(C.POINTER(C.c_int))))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tg_raster_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Request:

@@ -15,6 +15,7 @@
 #include "../../include/toastgpu.h"
 #include "tg_jac.cuh"
 #include "tg_gmres.cuh"
+#include "tg_grid.cuh"
 
 namespace tg {
 
@@ -777,6 +778,169 @@ struct tg_mesh_s {
     std::unique_ptr<Mesh> m;
 };
 
+// Raster_Pixel with the basis equal to the grid (src/libstoast/raster.cc:18-83,
+// raster_px.cc:10-48; what toast.Raster(mesh, grd) builds,
+// src/python/toastmodule.cc:696).  Built on the host once per raster: the
+// bounding box, the element containing each grid point and the grid map
+// matrix B, then kept on the device.
+struct tg_raster_s {
+    Mesh* mesh = nullptr;
+    int dim = 0, bdim[3] = {1, 1, 1}, glen = 0, slen = 0;
+    double bbmin[3] = {0, 0, 0}, bbmax[3] = {0, 0, 0};
+    std::vector<int> elref, sol, rowptr, col;  // col: natural node numbers
+    std::vector<double> val;
+    DBuf d_elref, d_sol, d_rowptr, d_col, d_val;
+    GridDev dev() const
+    {
+        GridDev G;
+        G.dim = dim; G.nx = bdim[0]; G.ny = bdim[1]; G.nz = dim > 2 ? bdim[2] : 1;
+        G.glen = glen; G.slen = slen;
+        for (int d = 0; d < 3; d++) G.ih[d] = d < dim ? 1.0 / ((bbmax[d] - bbmin[d]) / bdim[d]) : 0.0;
+        G.elref = d_elref.as<int>(); G.sol = d_sol.as<int>(); G.rowptr = d_rowptr.as<int>();
+        G.col = d_col.as<int>(); G.val = d_val.as<double>();
+        return G;
+    }
+    // prod gsize / (bdim - 1): the voxel scale of the grid Jacobian (jacobian.cc:365-370)
+    double voxel() const
+    {
+        double sz = 1.0;
+        for (int d = 0; d < dim; d++) sz *= (bbmax[d] - bbmin[d]) / (bdim[d] - 1.0);
+        return sz;
+    }
+};
+
+namespace {
+
+// Element_Unstructured::GContains (element.cc:553-563): the element's bounding
+// box widened by 1e-8, then LContains(Local(p)) with the padded test
+// (tri3.cc:134-144 / 191-200, tet4.cc:186-196 / 268-279)
+bool el_gcontains(const MeshHost& m, int e, const double* p)
+{
+    const int dim = m.dim, nn = m.nn;
+    const int* nd = &m.el[(size_t)e * nn];
+    for (int d = 0; d < dim; d++) {
+        double lo = 1e10, hi = -1e10;
+        for (int i = 0; i < nn; i++) {
+            const double v = m.coords[(size_t)nd[i] * dim + d];
+            lo = std::min(lo, v);
+            hi = std::max(hi, v);
+        }
+        if (p[d] < lo - 1e-8 || p[d] > hi + 1e-8) return false;
+    }
+    const double* g = &m.geo[(size_t)e * 16];
+    const double EPS = 1e-8;
+    if (dim == 2) {
+        const double scale = 1.0 / (g[0] + g[1] + g[2]);
+        const double l0 = (g[1] + g[4] * p[0] + g[7] * p[1]) * scale;
+        const double l1 = (g[2] + g[5] * p[0] + g[8] * p[1]) * scale;
+        return l0 + EPS >= 0.0 && l1 + EPS >= 0.0 && l0 + l1 - EPS <= 1.0;
+    }
+    const double *a = g, *b = g + 4, *c = g + 8, *dd = g + 12;
+    const double scale = 1.0 / (a[0] + a[1] + a[2] + a[3]);
+    double l[3];
+    for (int r = 0; r < 3; r++) l[r] = (a[r + 1] + b[r + 1] * p[0] + c[r + 1] * p[1] + dd[r + 1] * p[2]) * scale;
+    return l[0] + EPS >= 0.0 && l[1] + EPS >= 0.0 && l[2] + EPS >= 0.0 && l[0] + l[1] + l[2] - EPS <= 1.0;
+}
+
+// bounding box (Mesh::BoundingBox, mesh.cc:1341-1360), element per grid
+// point (GenerateElementPixelRef, mesh.cc:2944-3014: elements in order, each
+// claims the unclaimed grid points of its widened box that it contains) and
+// the grid map matrix (GridMapMatrix, mesh.cc:2486-2554: the element's global
+// shape functions at the point, tri3.cc:231-240, tet4.cc:302-313)
+void raster_build(const MeshHost& m, tg_raster_s& r)
+{
+    const int dim = m.dim, nn = m.nn;
+    for (int d = 0; d < dim; d++) { r.bbmin[d] = 1e6; r.bbmax[d] = -1e6; }
+    for (int k = 0; k < m.n; k++)
+        for (int d = 0; d < dim; d++) {
+            const double v = m.coords[(size_t)k * dim + d];
+            r.bbmin[d] = std::min(r.bbmin[d], v);
+            r.bbmax[d] = std::max(r.bbmax[d], v);
+        }
+    const int nx = r.bdim[0], ny = r.bdim[1], nz = dim > 2 ? r.bdim[2] : 1;
+    double dW[3] = {0, 0, 0};
+    for (int d = 0; d < dim; d++) dW[d] = (r.bbmax[d] - r.bbmin[d]) / (double)(r.bdim[d] - 1);
+    r.elref.assign(r.glen, -1);
+    for (int e = 0; e < m.ne; e++) {
+        const int* nd = &m.el[(size_t)e * nn];
+        double lo[3], hi[3];
+        for (int d = 0; d < dim; d++) { lo[d] = 1e10; hi[d] = -1e10; }
+        for (int i = 0; i < nn; i++)
+            for (int d = 0; d < dim; d++) {
+                const double v = m.coords[(size_t)nd[i] * dim + d];
+                lo[d] = std::min(lo[d], v);
+                hi[d] = std::max(hi[d], v);
+            }
+        int rmin[3] = {0, 0, 0}, rmax[3] = {1, 1, 1};
+        bool skip = false;
+        for (int d = 0; d < dim && !skip; d++) {
+            lo[d] -= 1e-6;
+            hi[d] += 1e-6;
+            if (lo[d] > r.bbmax[d] || hi[d] < r.bbmin[d]) { skip = true; break; }
+            rmin[d] = std::max(0, (int)std::ceil((lo[d] - r.bbmin[d]) / dW[d]));
+            rmax[d] = std::min(r.bdim[d], (int)std::floor((hi[d] - r.bbmin[d]) / dW[d]) + 1);
+        }
+        if (skip) continue;
+        double p[3] = {0.0, 0.0, 0.0};
+        for (int iz = rmin[2]; iz < rmax[2]; iz++) {
+            if (dim > 2) p[2] = iz * dW[2] + r.bbmin[2];
+            for (int iy = rmin[1]; iy < rmax[1]; iy++) {
+                p[1] = iy * dW[1] + r.bbmin[1];
+                for (int ix = rmin[0]; ix < rmax[0]; ix++) {
+                    const int idx = ix + nx * (iy + ny * iz);
+                    if (r.elref[idx] >= 0) continue;
+                    p[0] = ix * dW[0] + r.bbmin[0];
+                    if (el_gcontains(m, e, p)) r.elref[idx] = e;
+                }
+            }
+        }
+    }
+    r.rowptr.assign(r.glen + 1, 0);
+    r.col.clear();
+    r.val.clear();
+    r.sol.clear();
+    for (int iz = 0, i = 0; iz < nz; iz++) {
+        double p[3] = {0.0, 0.0, 0.0};
+        if (dim > 2) p[2] = iz * dW[2] + r.bbmin[2];
+        for (int iy = 0; iy < ny; iy++) {
+            p[1] = iy * dW[1] + r.bbmin[1];
+            for (int ix = 0; ix < nx; ix++, i++) {
+                const int e = r.elref[i];
+                if (e >= 0) {
+                    r.sol.push_back(i);
+                    p[0] = ix * dW[0] + r.bbmin[0];
+                    const int* nd = &m.el[(size_t)e * nn];
+                    const double* g = &m.geo[(size_t)e * 16];
+                    if (dim == 2) {
+                        const double scale = 1.0 / (2.0 * (0.5 * (g[0] + g[1] + g[2])));
+                        for (int j = 0; j < 3; j++) {
+                            r.col.push_back(nd[j]);
+                            r.val.push_back(scale * (g[j] + g[3 + j] * p[0] + g[6 + j] * p[1]));
+                        }
+                    } else {
+                        const double scale = 1.0 / (6.0 * ((1.0 / 6.0) * (g[0] + g[1] + g[2] + g[3])));
+                        for (int j = 0; j < 4; j++) {
+                            r.col.push_back(nd[j]);
+                            r.val.push_back(scale * (g[j] + g[4 + j] * p[0] + g[8 + j] * p[1] + g[12 + j] * p[2]));
+                        }
+                    }
+                }
+                r.rowptr[i + 1] = (int)r.col.size();
+            }
+        }
+    }
+    r.slen = (int)r.sol.size();
+}
+
+template <class T>
+void upload_sync(DBuf& b, const std::vector<T>& v)
+{
+    void* p = b.ensure(std::max<size_t>(1, v.size()) * sizeof(T));
+    if (!v.empty()) TG_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+}  // namespace
+
 struct tg_solver_s {
     Mesh* mesh = nullptr;
     int cplx = 0, method = 1, precon = 2, precision = 0, maxit = 0;
@@ -803,6 +967,7 @@ struct tg_solver_s {
     Engine<cf> ec32;
     DBuf B, X, X32, B32, cs_outer, cs_inner, io_a, io_b, tmp, jout;
     DBuf jF, jG, jpair, jyinv, plink_q, plink_m, psup, pnsup, pflag, pMsup, plin, plog;
+    DBuf gplanes_q, gplanes_m, gy;    // grid-basis Jacobian: field planes, projections
     DBuf fp_bq, fp_xq, fp_bm, fp_xm, fp_lin, fp_log;
     DBuf jwm64, jwk64, jwm32, jwk32;  // per-node element weights of the Jacobian (geometry only)
     DBuf rel_cnt, rel_idx, rel_xc, rel_ac;
@@ -1324,6 +1489,61 @@ static void api_jacobian(tg_solver s, int nq, const double* dphi, int nm, const 
     TG_CUDA(cudaStreamSynchronize(s->stream));
 }
 
+// Grid-basis Jacobian (GenerateJacobian_grid, jacobian.cc:289-373; real:
+// GenerateJacobian_cw_grid, 516-712, and the LOG scaling of
+// GenerateJacobian_cw, 178-193).  Fields are source-major in the natural
+// numbering; FP64 arithmetic for an FP64 J, FP32 for an FP32 J.
+template <class V64, class C>
+static void grid_jac_run(tg_solver s, const tg_raster_s& r, int nq, const V64* F, int nm, const V64* A,
+                         const V64* yl, const LinkHost& L, int logscale, void* Jd)
+{
+    const int n = s->mesh->d.n, nqm = (int)L.q.size(), np = 1 + r.dim;
+    const GridDev G = r.dev();
+    C* Pq = (C*)s->gplanes_q.ensure((size_t)nq * np * r.slen * sizeof(C));
+    C* Pm = (C*)s->gplanes_m.ensure((size_t)nm * np * r.slen * sizeof(C));
+    const unsigned gx = cdiv_u(std::max(r.slen, 1), 256);
+    launch(grid_fields_kernel<V64, C>, dim3(gx, nq), 256, 0, s->stream, G, nq, F, n, 1, Pq);
+    // the reference masks the adjoint gradient for complex data only
+    // (jacobian.cc:348-350 against 557)
+    launch(grid_fields_kernel<V64, C>, dim3(gx, nm), 256, 0, s->stream, G, nm, A, n, vt<V64>::cplx ? 1 : 0, Pm);
+    const C* y = nullptr;
+    if (logscale) {
+        C* yc = (C*)s->gy.ensure((size_t)nqm * sizeof(C));
+        launch(cast_kernel<C, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, (size_t)nqm, yl, yc);
+        y = yc;
+    }
+    int *lo = (int*)s->plink_q.ensure((size_t)(nq + 1) * sizeof(int)), *lm = (int*)s->plink_m.ensure(
+        (size_t)std::max(nqm, 1) * sizeof(int));
+    std::vector<int> ofs(nq + 1, 0);
+    for (int l = 0; l < nqm; l++) ofs[L.q[l] + 1]++;
+    for (int q = 0; q < nq; q++) ofs[q + 1] += ofs[q];
+    // pageable sources: the copies complete before these calls return
+    TG_CUDA(cudaMemcpyAsync(lo, ofs.data(), (size_t)(nq + 1) * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    TG_CUDA(cudaMemcpyAsync(lm, L.m.data(), (size_t)nqm * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    using JT = typename vt<C>::R;
+    launch(grid_jacobian_kernel<C, JT>, dim3(gx, nq), 256, 0, s->stream, r.dim, r.slen, nq, nqm, Pq, Pm, lo, lm, y,
+           logscale, r.voxel(), (JT*)Jd);
+}
+
+template <class V64, class V32>
+static void api_jacobian_grid(tg_solver s, const tg_raster_s& r, int nq, const double* dphi, int nm,
+                              const double* aphi, const double* proj, const LinkHost& L, int scale, void* J,
+                              int out_fp32, int mem)
+{
+    const int n = s->mesh->d.n, nqm = (int)L.q.size();
+    const V64* F = (const V64*)dev_in(s, dphi, (size_t)nq * n * sizeof(V64), mem, s->io_a);
+    const V64* A = (const V64*)dev_in(s, aphi, (size_t)nm * n * sizeof(V64), mem, s->io_b);
+    const V64* yl = scale == TG_DATA_LOG ? (const V64*)dev_in(s, proj, (size_t)nqm * sizeof(V64), mem, s->plin)
+                                         : nullptr;
+    const size_t jbytes = (size_t)2 * nqm * (vt<V64>::cplx ? 2 : 1) * r.slen * (out_fp32 ? 4 : 8);
+    void* Jd = mem == TG_MEM_DEVICE ? J : s->jout.ensure(jbytes);
+    if (out_fp32) grid_jac_run<V64, V32>(s, r, nq, F, nm, A, yl, L, scale == TG_DATA_LOG, Jd);
+    else grid_jac_run<V64, V64>(s, r, nq, F, nm, A, yl, L, scale == TG_DATA_LOG, Jd);
+    if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(J, Jd, jbytes, cudaMemcpyDeviceToHost, s->stream));
+    TG_CUDA(cudaGetLastError());
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+}
+
 template <class V64, class V32>
 static void api_forward_path(tg_solver s, const double* cmua, const double* ckap, const double* c2a, double omega,
                              int nq, const double* qvec, int nm, const double* mvec, const LinkHost& L,
@@ -1610,6 +1830,79 @@ int tg_jacobian(tg_solver s, int nq, const double* dphi, int nm, const double* a
     if (L.q.empty()) return TG_OK;
     if (s->cplx) api_jacobian<cd, cf>(s, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
     else api_jacobian<double, float>(s, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
+    API_END
+}
+
+int tg_raster_create(tg_mesh mesh, const int* bdim, tg_raster* out)
+{
+    API_BEGIN
+    TG_CHECK(mesh && bdim && out, TG_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    const MeshHost& m = mesh->m->h;
+    auto r = std::make_unique<tg_raster_s>();
+    r->mesh = mesh->m.get();
+    r->dim = m.dim;
+    long long glen = 1;
+    for (int d = 0; d < m.dim; d++) {
+        TG_CHECK(bdim[d] >= 2, TG_ERR_ARG, "every grid dimension needs at least 2 points");
+        r->bdim[d] = bdim[d];
+        glen *= bdim[d];
+    }
+    TG_CHECK(glen < (1LL << 30), TG_ERR_ARG, "grid too large");
+    r->glen = (int)glen;
+    raster_build(m, *r);
+    TG_CUDA(cudaSetDevice(mesh->m->device));
+    upload_sync(r->d_elref, r->elref);
+    upload_sync(r->d_sol, r->sol);
+    upload_sync(r->d_rowptr, r->rowptr);
+    upload_sync(r->d_col, r->col);
+    upload_sync(r->d_val, r->val);
+    *out = r.release();
+    API_END
+}
+
+int tg_raster_destroy(tg_raster r)
+{
+    API_BEGIN
+    delete r;
+    API_END
+}
+
+int tg_raster_info(tg_raster r, int* glen, int* slen, double* bbmin, double* bbmax)
+{
+    API_BEGIN
+    TG_CHECK(r, TG_ERR_ARG, "raster is NULL");
+    if (glen) *glen = r->glen;
+    if (slen) *slen = r->slen;
+    for (int d = 0; d < r->dim; d++) {
+        if (bbmin) bbmin[d] = r->bbmin[d];
+        if (bbmax) bbmax[d] = r->bbmax[d];
+    }
+    API_END
+}
+
+int tg_raster_elref(tg_raster r, int* elref)
+{
+    API_BEGIN
+    TG_CHECK(r && elref, TG_ERR_ARG, "NULL argument");
+    std::memcpy(elref, r->elref.data(), r->elref.size() * sizeof(int));
+    API_END
+}
+
+int tg_jacobian_grid(tg_solver s, tg_raster r, int nq, const double* dphi, int nm, const double* aphi,
+                     const double* proj, const int* link_ofs, const int* link_m, int scale, void* J, int out_fp32,
+                     int mem)
+{
+    API_BEGIN
+    TG_CHECK(s && r && dphi && aphi && link_ofs && J, TG_ERR_ARG, "NULL argument");
+    TG_CHECK(r->mesh == s->mesh, TG_ERR_ARG, "the raster was built on another mesh");
+    TG_CHECK(nq > 0 && nm > 0 && nq <= 65535 && nm <= 65535, TG_ERR_ARG, "source / detector count out of range");
+    TG_CHECK(scale == TG_DATA_LIN || (scale == TG_DATA_LOG && proj), TG_ERR_ARG, "log data needs the projections");
+    std::lock_guard<std::mutex> g(s->mu);
+    LinkHost L = make_links(nq, nm, link_ofs, link_m);
+    if (L.q.empty() || r->slen == 0) return TG_OK;
+    if (s->cplx) api_jacobian_grid<cd, cf>(s, *r, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
+    else api_jacobian_grid<double, float>(s, *r, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
     API_END
 }
 
