@@ -60,6 +60,8 @@ def parse():
                     choices=["c0_disc3k_cw", "c1_disc13k_fd", "c2_cyl30k_fd", "c3_box250k_fd"])
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--e2e-slots", type=int, default=1, help="e2e leg: request-server slots")
+    ap.add_argument("--grid", type=int, default=32,
+                    help="grid-basis Jacobian leg: raster points per axis (0: skip)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--tol", type=float, default=1e-12)
     ap.add_argument("--inner-tol", type=float, default=1e-4, help="mixed path: inner FP32 solve tolerance")
@@ -341,6 +343,45 @@ def run_gpu(args):
     shares = {names[c]: {"ms_per_step": prof[c][0] / psteps, "launches_or_scopes": prof[c][1] // psteps}
               for c in prof}
 
+    # ---- grid-basis Jacobian (pixel raster, basis = grid) on this request's
+    # fields, device-resident, timed alone with CUDA events
+    grid = None
+    if args.grid > 0:
+        d_dphi = torch.empty((nq, n * vmul), dtype=torch.float64, device=dev)
+        d_aphi = torch.empty((nm, n * vmul), dtype=torch.float64, device=dev)
+        s.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, d_dphi, d_aphi, d_proj, d_lproj, d_J,
+                           j_fp32, capi.MEM_DEVICE, res)
+        rast = capi.Raster(gm, [args.grid] * P.dim)
+        gcols = (2 if cplx else 1) * rast.slen
+        d_Jg = torch.empty((2 * nqm, gcols), dtype=torch.float32 if j_fp32 else torch.float64, device=dev)
+
+        def gstep():
+            s.jacobian_grid_raw(rast, nq, d_dphi, nm, d_aphi, d_proj, links, capi.DATA_LOG, d_Jg, j_fp32,
+                                capi.MEM_DEVICE)
+
+        for _ in range(3):
+            gstep()
+        torch.cuda.synchronize()
+        ge = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
+        for a, b in ge:
+            a.record(stream)
+            gstep()
+            b.record(stream)
+        torch.cuda.synchronize()
+        g_ms = float(np.mean([a.elapsed_time(b) for a, b in ge]))
+        jb = d_Jg.numel() * d_Jg.element_size()
+        # field planes read once per source / detector (value + dim gradients)
+        pb = (nq + nm) * (1 + P.dim) * rast.slen * (8 if j_fp32 else 16) // (1 if cplx else 2)
+        peak = peaks.get("hbm_gbs", 6800.0)
+        grid = {"raster": [args.grid] * P.dim, "solution_points": rast.slen, "ms_per_jacobian": g_ms,
+                "jacobians_per_s": 1e3 / g_ms, "J_bytes": jb,
+                "roofline": {"bound": "hbm", "achieved": (jb + pb) / (g_ms / 1e3) / 1e9, "peak": peak,
+                             "unit": "GB/s", "frac": (jb + pb) / (g_ms / 1e3) / 1e9 / peak,
+                             "algorithmic_bytes_per_launch": jb + pb},
+                "note": "includes the field resampling and gradient launches; inputs on the device"}
+        rast.close()
+        del d_Jg, d_dphi, d_aphi
+
     # ---- e2e through the C ABI with host buffers (pinned), copies inside the timed region
     e2e = None
     j_bytes = 2 * nqm * jcols * (4 if j_fp32 else 8)
@@ -477,7 +518,7 @@ def run_gpu(args):
             "unconverged_sources": int(sum(1 for r in res if r.status != 0)),
             "ic_applies_per_request": prof[capi.PROF_SWEEP][1] / psteps,
             "roofline": roof, "kernel_time_per_step": shares,
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "grid_jacobian": grid,
             "clocks": clocks, "wall_s": wall, "compare": compare,
             "spmm_autotuner": capi.tuner_log().strip().splitlines(),
         }

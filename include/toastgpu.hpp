@@ -8,6 +8,9 @@
 //   toastgpu::GenerateJacobian    GenerateJacobian(raster = 0, ...) nodal basis
 //                                 (src/libstoast/jacobian.h:62-82) and
 //                                 GenerateJacobian_cw (jacobian.h:101-147)
+//   toastgpu::Raster_Pixel        Raster_Pixel(bdim, bdim, mesh) (raster_px.cc:10-48), the
+//                                 raster toast.Raster(mesh, grd) builds
+//   toastgpu::GenerateJacobian    GenerateJacobian(raster, ...) grid basis (jacobian.cc:105-123)
 //   toastgpu::QVec_Gaussian       QVec_Gaussian, Neumann mode (src/libstoast/source.cc:19-56)
 //
 // Differences a caller sees:
@@ -217,6 +220,46 @@ void GenerateJacobian(const TFwdSolver<T>& fws, int nq, const T* dphi, int nm, c
 {
     check(tg_jacobian(fws.handle(), nq, (const double*)dphi, nm, (const double*)aphi, (const double*)proj,
                       L.ofs.data(), L.m.data(), dscale == DATA_LOG ? TG_DATA_LOG : TG_DATA_LIN, J, 0, TG_MEM_HOST));
+}
+
+// Raster_Pixel(bdim, bdim, mesh): a grid of bdim points per axis over the
+// mesh's bounding box; SLen() solution points (grid points inside the mesh)
+class Raster_Pixel {
+public:
+    Raster_Pixel(const int* bdim, const Mesh& mesh)
+    {
+        check(tg_raster_create(mesh.handle(), bdim, &h_));
+        check(tg_raster_info(h_, &glen_, &slen_, nullptr, nullptr));
+    }
+    ~Raster_Pixel() { tg_raster_destroy(h_); }
+    Raster_Pixel(const Raster_Pixel&) = delete;
+    Raster_Pixel& operator=(const Raster_Pixel&) = delete;
+    int GLen() const { return glen_; }
+    int SLen() const { return slen_; }
+    std::vector<int> Elref() const
+    {
+        std::vector<int> e(glen_);
+        check(tg_raster_elref(h_, e.data()));
+        return e;
+    }
+    tg_raster handle() const { return h_; }
+
+private:
+    tg_raster h_ = nullptr;
+    int glen_ = 0, slen_ = 0;
+};
+
+// GenerateJacobian(raster, mesh, dphi, aphi, proj, dscale, J) grid basis:
+// complex J (2 nQM) x (2 SLen) row-major [Re mua | Re kappa ; Im mua | Im
+// kappa] (jacobian.cc:289-373); real J (2 nQM) x SLen [mua ; kappa]
+// (GenerateJacobian_cw with a raster, jacobian.cc:178-193, 610-712)
+template <class T>
+void GenerateJacobian(const Raster_Pixel& raster, const TFwdSolver<T>& fws, int nq, const T* dphi, int nm,
+                      const T* aphi, const T* proj, const Links& L, DataScale dscale, double* J)
+{
+    check(tg_jacobian_grid(fws.handle(), raster.handle(), nq, (const double*)dphi, nm, (const double*)aphi,
+                           (const double*)proj, L.ofs.data(), L.m.data(),
+                           dscale == DATA_LOG ? TG_DATA_LOG : TG_DATA_LIN, J, 0, TG_MEM_HOST));
 }
 
 }  // namespace toastgpu

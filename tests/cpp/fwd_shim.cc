@@ -8,7 +8,8 @@
 //   IN : int32 dim, n, ne, nq, nm, cplx ; double freq_mhz, width ;
 //        n*dim coords ; ne*(dim+1) int32 elements ; n cmua ; n ckappa ; n c2a ;
 //        nq*dim source positions ; nm*dim detector positions
-//   OUT: nQM logproj values, then the Jacobian (doubles; complex interleaved)
+//   OUT: nQM logproj values, then the Jacobian (doubles; complex interleaved),
+//        then the grid-basis Jacobian of Raster_Pixel(12 points per axis)
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -51,8 +52,14 @@ static int run(int dim, int n, int nq, int nm, double omega, double width, const
     const int cols = std::is_same<T, double>::value ? n : 2 * n;
     std::vector<double> J((size_t)2 * L.nQM() * cols);
     GenerateJacobian(FWS, nq, dphi.data(), nm, aphi.data(), proj.data(), L, DATA_LOG, J.data());
+    const int bdim[3] = {12, 12, 12};
+    Raster_Pixel raster(bdim, mesh);
+    const int gcols = std::is_same<T, double>::value ? raster.SLen() : 2 * raster.SLen();
+    std::vector<double> Jg((size_t)2 * L.nQM() * gcols);
+    GenerateJacobian(raster, FWS, nq, dphi.data(), nm, aphi.data(), proj.data(), L, DATA_LOG, Jg.data());
     fwrite(lproj.data(), sizeof(T), lproj.size(), out);
     fwrite(J.data(), sizeof(double), J.size(), out);
+    fwrite(Jg.data(), sizeof(double), Jg.size(), out);
     return 0;
 }
 

@@ -30,6 +30,10 @@ def test_cpp_caller_matches_c_abi(tmp_path, make):
     nqm = P.qm.nQM
     nl = 2 * nqm if P.complex else nqm
     lp = raw[:nl].view(np.complex128) if P.complex else raw[:nl]
-    J = raw[nl:].reshape(r["J"].shape)
+    J = raw[nl:nl + r["J"].size].reshape(r["J"].shape)
     assert np.array_equal(lp, r["logproj"])
     assert np.array_equal(J, r["J"])
+    # grid basis: Raster_Pixel of 12 points per axis
+    rast = capi.Raster(gm, [12] * P.dim)
+    Jg = s.jacobian_grid(rast, r["dphi"], r["aphi"], r["proj"], capi.Links(P.qm.link_ofs, P.qm.link_m))
+    assert np.array_equal(raw[nl + r["J"].size:].reshape(Jg.shape), Jg)

@@ -297,6 +297,11 @@ class FwdSolver:
                                       _ptr(pr), _ptr(links.ofs), _ptr(links.m), scale, _ptr(J), int(fp32), MEM_HOST))
         return J
 
+    def jacobian_grid_raw(self, raster: "Raster", nq, dphi, nm, aphi, proj, links: Links, scale, J, fp32, mem):
+        """tg_jacobian_grid with caller-owned buffers (numpy or device tensors)."""
+        _check(lib().tg_jacobian_grid(self._h, raster._h, int(nq), _ptr(dphi), int(nm), _ptr(aphi), _ptr(proj),
+                                      _ptr(links.ofs), _ptr(links.m), int(scale), _ptr(J), int(fp32), int(mem)))
+
     def jacobian(self, dphi, aphi, proj, links: Links, scale=DATA_LOG, fp32=False):
         dphi = _f64(dphi, self.complex)
         aphi = _f64(aphi, self.complex)

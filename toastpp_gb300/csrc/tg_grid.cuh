@@ -4,13 +4,14 @@
 // complex, projections given) and GenerateJacobian_cw_grid (516-712, real)
 // with Raster_Pixel (raster_px.cc:10-48) whose basis equals its grid.
 //
-// Per request the fields are resampled at the solution points (the grid
-// points inside the mesh) and at their grid neighbours, with central or
-// one-sided differences as ImageGradient (jacobian.cc:944-1060) takes them,
-// into planes P[(c * (1 + dim) + comp) * slen + s] (comp 0 the value, 1..dim
-// the gradient), so that a thread per solution point reads every plane of a
-// source or detector coalesced.  Then one thread per solution point and
-// source walks the source's links and writes its column of every link row.
+// Per request the fields (node-major, natural numbering) are resampled on
+// the grid, then the values and the central or one-sided differences of
+// ImageGradient (jacobian.cc:944-1060) at the solution points (the grid
+// points inside the mesh) go to planes P[(c * (1 + dim) + comp) * slen + s]
+// (comp 0 the value, 1..dim the gradient), so that a thread per solution
+// point reads every plane of a source or detector coalesced.  Then one thread
+// per solution point and source walks the source's links and writes its
+// column of every link row.
 #pragma once
 #include "tg_kernels.cuh"
 
@@ -26,50 +27,72 @@ struct GridDev {
     const double* val;
 };
 
-// f(g) = sum_j B(g, j) x[col j] (Map_MeshToGrid, raster.cc:188-199; complex:
-// Ax_cplx, crmatrix_imp.hpp:1302-1327), x source-major natural
+// Map_MeshToGrid (raster.cc:188-199; complex: Ax_cplx, crmatrix_imp.hpp:
+// 1302-1327): gm[g * k + c] = sum_j B(g, j) x[col_j * k + c], x node-major
+// in the natural numbering; a warp per grid point, lanes over columns
 template <class V>
-__device__ __forceinline__ V grid_value(const GridDev& G, const V* __restrict__ x, int g)
+__global__ void grid_map_kernel(GridDev G, int k, const V* __restrict__ x, V* __restrict__ gm)
 {
-    V acc = vzero<V>();
-    for (int j = G.rowptr[g]; j < G.rowptr[g + 1]; j++) acc = vadd(acc, vscale(x[G.col[j]], G.val[j]));
-    return acc;
-}
-
-// one thread per (solution point, column); masked: the one-sided rules of
-// ImageGradient with the element mask, else every grid point counts
-template <class V, class OUT>
-__global__ void grid_fields_kernel(GridDev G, int k, const V* __restrict__ src, int ld, int masked,
-                                   OUT* __restrict__ planes)
-{
-    const int s = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
-    if (s >= G.slen || c >= k) return;
-    const V* x = src + (size_t)c * ld;
-    const int g = G.sol[s];
-    const V v0 = grid_value(G, x, g);
-    const int np = 1 + G.dim;
-    OUT* out = planes + (size_t)c * np * G.slen + s;
-    out[0] = vcast<OUT, V>(v0);
-    const int x0 = g % G.nx, y0 = (g / G.nx) % G.ny, z0 = g / (G.nx * G.ny);
-    const int co[3] = {x0, y0, z0}, len[3] = {G.nx, G.ny, G.nz}, st[3] = {1, G.nx, G.nx * G.ny};
-    for (int d = 0; d < G.dim; d++) {
-        const bool blo = co[d] > 0 && (!masked || G.elref[g - st[d]] >= 0);
-        const bool bhi = co[d] < len[d] - 1 && (!masked || G.elref[g + st[d]] >= 0);
-        // the point itself is a solution point, so inside the mask
-        V gr = vzero<V>();
-        using R = typename vt<V>::R;
-        if (blo && bhi)
-            gr = vscale(vsub(grid_value(G, x, g + st[d]), grid_value(G, x, g - st[d])), (R)(0.5 * G.ih[d]));
-        else if (blo)
-            gr = vscale(vsub(v0, grid_value(G, x, g - st[d])), (R)G.ih[d]);
-        else if (bhi)
-            gr = vscale(vsub(grid_value(G, x, g + st[d]), v0), (R)G.ih[d]);
-        out[(size_t)(1 + d) * G.slen] = vcast<OUT, V>(gr);
+    const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (g >= G.glen) return;
+    const int j0 = G.rowptr[g], j1 = G.rowptr[g + 1];
+    for (int c = lane; c < k; c += 32) {
+        V acc = vzero<V>();
+        for (int j = j0; j < j1; j++) acc = vadd(acc, vscale(x[(size_t)G.col[j] * k + c], G.val[j]));
+        gm[(size_t)g * k + c] = acc;
     }
 }
 
-// Smith's complex division (Smith 1962), as the reference's complex
-// division of the PMDF by the projection does
+// value (comp 0) or ImageGradient component comp - 1 of column c at grid
+// point g: central or one-sided differences as jacobian.cc:944-1060 takes
+// them; masked: neighbours outside the element mask do not count, else every
+// grid point does
+template <class V>
+__device__ __forceinline__ V grid_component(const GridDev& G, int k, const V* __restrict__ gm, int g, int c,
+                                            int comp, int masked)
+{
+    const V v0 = gm[(size_t)g * k + c];
+    if (comp == 0) return v0;
+    const int d = comp - 1;
+    const int co = d == 0 ? g % G.nx : (d == 1 ? (g / G.nx) % G.ny : g / (G.nx * G.ny));
+    const int len = d == 0 ? G.nx : (d == 1 ? G.ny : G.nz), st = d == 0 ? 1 : (d == 1 ? G.nx : G.nx * G.ny);
+    const bool blo = co > 0 && (!masked || G.elref[g - st] >= 0);
+    const bool bhi = co < len - 1 && (!masked || G.elref[g + st] >= 0);
+    using R = typename vt<V>::R;
+    // the point itself is a solution point, so inside the mask
+    if (blo && bhi) return vscale(vsub(gm[(size_t)(g + st) * k + c], gm[(size_t)(g - st) * k + c]), (R)(0.5 * G.ih[d]));
+    if (blo) return vscale(vsub(v0, gm[(size_t)(g - st) * k + c]), (R)G.ih[d]);
+    if (bhi) return vscale(vsub(gm[(size_t)(g + st) * k + c], v0), (R)G.ih[d]);
+    return vzero<V>();
+}
+
+// Field planes P[(c * (1 + dim) + comp) * slen + s] from the grid fields:
+// block = 32 solution points x 32 columns; each component is formed with
+// lanes over columns (coalesced reads of gm) into a shared tile, then
+// written with lanes over solution points (coalesced planes)
+template <class V, class OUT>
+__global__ void __launch_bounds__(256) grid_planes_kernel(GridDev G, int k, const V* __restrict__ gm, int masked,
+                                                          OUT* __restrict__ planes)
+{
+    __shared__ OUT tile[32][33];
+    const int s0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+    const int np = 1 + G.dim;
+    for (int comp = 0; comp < np; comp++) {
+        for (int r = ty; r < 32; r += 8) {
+            const int s = s0 + r, c = c0 + tx;
+            if (s < G.slen && c < k) tile[r][tx] = vcast<OUT, V>(grid_component(G, k, gm, G.sol[s], c, comp, masked));
+        }
+        __syncthreads();
+        for (int r = ty; r < 32; r += 8) {
+            const int c = c0 + r, s = s0 + tx;
+            if (s < G.slen && c < k) planes[((size_t)c * np + comp) * G.slen + s] = tile[tx][r];
+        }
+        __syncthreads();
+    }
+}
+
+// Smith's complex division (Smith 1962)
 __device__ __forceinline__ cd cdiv_smith(cd a, cd b)
 {
     if (fabs(b.x) >= fabs(b.y)) {
@@ -79,22 +102,29 @@ __device__ __forceinline__ cd cdiv_smith(cd a, cd b)
     const double r = b.x / b.y, den = b.x * r + b.y;
     return cd{(a.x * r + a.y) / den, (a.y * r - a.x) / den};
 }
-__device__ __forceinline__ cf cdiv_smith(cf a, cf b)
+
+// 1 / y per link, in FP64 (Smith's division for complex y), then cast to the
+// Jacobian's arithmetic type
+template <class C, class V64>
+__global__ void grid_yinv_kernel(int nqm, const V64* __restrict__ y, C* __restrict__ yinv)
 {
-    const cd q = cdiv_smith(cd{a.x, a.y}, cd{b.x, b.y});
-    return cf{(float)q.x, (float)q.y};
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= nqm) return;
+    if constexpr (vt<V64>::cplx) yinv[l] = vcast<C, V64>(cdiv_smith(cd{1.0, 0.0}, y[l]));
+    else yinv[l] = vcast<C, V64>(1.0 / y[l]);
 }
 
 // One thread per (solution point, source): PMDF_mua = -(f a), PMDF_kap =
-// -sum_d (grad_d f)(grad_d a) (jacobian.cc:58-72); complex LOG data divide
-// by y (PMDF_log, 76-79) before the voxel scale; real LOG rows are scaled by
-// 1/y after it (GenerateJacobian_cw, 178-193).  J rows: complex
-// [Re mua | Re kap] at l and [Im mua | Im kap] at nQM + l (2 slen columns);
-// real mua at l and kap at nQM + l (slen columns).
+// -sum_d (grad_d f)(grad_d a) (jacobian.cc:58-72); complex LOG data are
+// divided by y (PMDF_log, 76-79) before the voxel scale, real LOG rows are
+// scaled by 1/y after it (GenerateJacobian_cw, 178-193).  Both multiply by
+// the link's 1/y (yinv): a division per entry would run on the FP64 pipe.
+// J rows: complex [Re mua | Re kap] at l and [Im mua | Im kap] at nQM + l
+// (2 slen columns); real mua at l and kap at nQM + l (slen columns).
 template <class V, class JT>
 __global__ void grid_jacobian_kernel(int dim, int slen, int nq, int nqm, const V* __restrict__ Fp,
                                      const V* __restrict__ Ap, const int* __restrict__ link_ofs,
-                                     const int* __restrict__ link_m, const V* __restrict__ y, int logscale, double sz,
+                                     const int* __restrict__ link_m, const V* __restrict__ yinv, double sz,
                                      JT* __restrict__ J)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x, q = blockIdx.y;
@@ -106,6 +136,8 @@ __global__ void grid_jacobian_kernel(int dim, int slen, int nq, int nqm, const V
     for (int d = 0; d < 4; d++) f[d] = d < np ? Fp[((size_t)q * np + d) * slen + s] : vzero<V>();
     constexpr bool CPLX = vt<V>::cplx;
     const size_t cols = CPLX ? 2 * (size_t)slen : (size_t)slen;
+    // several links in flight per thread: their plane loads are independent
+#pragma unroll 4
     for (int l = link_ofs[q]; l < link_ofs[q + 1]; l++) {
         const int m = link_m[l];
         V a[4];
@@ -119,9 +151,9 @@ __global__ void grid_jacobian_kernel(int dim, int slen, int nq, int nqm, const V
         JT* r0 = J + (size_t)l * cols;
         JT* r1 = J + (size_t)(l + nqm) * cols;
         if constexpr (CPLX) {
-            if (logscale) {
-                pm = cdiv_smith(pm, y[l]);
-                pk = cdiv_smith(pk, y[l]);
+            if (yinv) {
+                pm = vmul(pm, yinv[l]);
+                pk = vmul(pk, yinv[l]);
             }
             r0[s] = (JT)(re(pm) * (R)sz);
             r1[s] = (JT)(im(pm) * (R)sz);
@@ -129,10 +161,9 @@ __global__ void grid_jacobian_kernel(int dim, int slen, int nq, int nqm, const V
             r1[slen + s] = (JT)(im(pk) * (R)sz);
         } else {
             R vm = re(pm) * (R)sz, vk = re(pk) * (R)sz;
-            if (logscale) {
-                const R iy = (R)(1.0 / (double)re(y[l]));
-                vm *= iy;
-                vk *= iy;
+            if (yinv) {
+                vm *= yinv[l];
+                vk *= yinv[l];
             }
             r0[s] = (JT)vm;
             r1[s] = (JT)vk;

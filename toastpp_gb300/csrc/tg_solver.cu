@@ -967,7 +967,7 @@ struct tg_solver_s {
     Engine<cf> ec32;
     DBuf B, X, X32, B32, cs_outer, cs_inner, io_a, io_b, tmp, jout;
     DBuf jF, jG, jpair, jyinv, plink_q, plink_m, psup, pnsup, pflag, pMsup, plin, plog;
-    DBuf gplanes_q, gplanes_m, gy;    // grid-basis Jacobian: field planes, projections
+    DBuf gplanes_q, gplanes_m, gy, io_c;  // grid-basis Jacobian: field planes, 1/y, grid fields
     DBuf fp_bq, fp_xq, fp_bm, fp_xm, fp_lin, fp_log;
     DBuf jwm64, jwk64, jwm32, jwk32;  // per-node element weights of the Jacobian (geometry only)
     DBuf rel_cnt, rel_idx, rel_xc, rel_ac;
@@ -1502,15 +1502,25 @@ static void grid_jac_run(tg_solver s, const tg_raster_s& r, int nq, const V64* F
     C* Pq = (C*)s->gplanes_q.ensure((size_t)nq * np * r.slen * sizeof(C));
     C* Pm = (C*)s->gplanes_m.ensure((size_t)nm * np * r.slen * sizeof(C));
     const unsigned gx = cdiv_u(std::max(r.slen, 1), 256);
-    launch(grid_fields_kernel<V64, C>, dim3(gx, nq), 256, 0, s->stream, G, nq, F, n, 1, Pq);
+    // fields node-major (natural numbering), resampled on the grid, planes;
     // the reference masks the adjoint gradient for complex data only
     // (jacobian.cc:348-350 against 557)
-    launch(grid_fields_kernel<V64, C>, dim3(gx, nm), 256, 0, s->stream, G, nm, A, n, vt<V64>::cplx ? 1 : 0, Pm);
-    const C* y = nullptr;
+    auto planes = [&](int k, const V64* src, int masked, C* P) {
+        V64* xn = (V64*)s->tmp.ensure((size_t)k * n * sizeof(V64));
+        launch(to_nodemajor_kernel<V64, V64>, dim3(cdiv_u(n, 32), cdiv_u(k, 32)), dim3(32, 8), 0, s->stream, n, k, k,
+               src, xn, (const int*)nullptr);
+        V64* gm = (V64*)s->io_c.ensure((size_t)r.glen * k * sizeof(V64));
+        launch(grid_map_kernel<V64>, cdiv_u((size_t)r.glen * 32, 256), 256, 0, s->stream, G, k, (const V64*)xn, gm);
+        launch(grid_planes_kernel<V64, C>, dim3(cdiv_u(r.slen, 32), cdiv_u(k, 32)), dim3(32, 8), 0, s->stream, G, k,
+               (const V64*)gm, masked, P);
+    };
+    planes(nq, F, 1, Pq);
+    planes(nm, A, vt<V64>::cplx ? 1 : 0, Pm);
+    const C* yinv = nullptr;
     if (logscale) {
         C* yc = (C*)s->gy.ensure((size_t)nqm * sizeof(C));
-        launch(cast_kernel<C, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, (size_t)nqm, yl, yc);
-        y = yc;
+        launch(grid_yinv_kernel<C, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, yl, yc);
+        yinv = yc;
     }
     int *lo = (int*)s->plink_q.ensure((size_t)(nq + 1) * sizeof(int)), *lm = (int*)s->plink_m.ensure(
         (size_t)std::max(nqm, 1) * sizeof(int));
@@ -1521,8 +1531,8 @@ static void grid_jac_run(tg_solver s, const tg_raster_s& r, int nq, const V64* F
     TG_CUDA(cudaMemcpyAsync(lo, ofs.data(), (size_t)(nq + 1) * sizeof(int), cudaMemcpyHostToDevice, s->stream));
     TG_CUDA(cudaMemcpyAsync(lm, L.m.data(), (size_t)nqm * sizeof(int), cudaMemcpyHostToDevice, s->stream));
     using JT = typename vt<C>::R;
-    launch(grid_jacobian_kernel<C, JT>, dim3(gx, nq), 256, 0, s->stream, r.dim, r.slen, nq, nqm, Pq, Pm, lo, lm, y,
-           logscale, r.voxel(), (JT*)Jd);
+    launch(grid_jacobian_kernel<C, JT>, dim3(gx, nq), 256, 0, s->stream, r.dim, r.slen, nq, nqm, Pq, Pm, lo, lm, yinv,
+           r.voxel(), (JT*)Jd);
 }
 
 template <class V64, class V32>
