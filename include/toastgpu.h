@@ -97,6 +97,12 @@ int tg_mesh_boundary(tg_mesh mesh, unsigned char *bndnode);
 /* QVec_Gaussian for npos centres (pos: npos x dim); Neumann mode reproduces the
    boundary source of source.cc:19-56.  out: npos x n, host memory. */
 int tg_qvec_gaussian(tg_mesh mesh, int npos, const double *pos, double width, int neumann, double *out);
+/* The same on the device (a thread per node and position; the reference's
+   summation order): positions on the host, scale (n values, optional, e.g.
+   c2a for detector vectors) and out (npos x n) on the host or the device as
+   mem says. */
+int tg_qvec_gaussian_ex(tg_mesh mesh, int npos, const double *pos, double width, int neumann,
+                        const double *scale, double *out, int mem);
 
 /* ---- forward solver ------------------------------------------------------ */
 int tg_solver_create(tg_mesh mesh, int is_complex, int method, int precon, double tol, int maxit,

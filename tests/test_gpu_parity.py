@@ -184,3 +184,26 @@ def test_mixed_precision_boundary_data(case, oracle_mod):
     assert rel2(out["proj"], ref.proj) < 1e-10
     # Jacobian from FP32 arithmetic: report-level agreement
     assert rel2(out["J"], ref.J) < 1e-5
+
+
+@pytest.mark.parametrize("neumann", [True, False], ids=["neumann", "isotropic"])
+def test_source_vectors_on_device(case, neumann):
+    """tg_qvec_gaussian_ex (device) against the host QVec_Gaussian: the same
+    sums in the same order; the device's rounding of exp(-d^2 / 2w^2) and of
+    its argument shows in the far tail (values near e^-300, where one unit of
+    the argument's last place is 3e-14 of the value), so the elementwise
+    bound is 1e-12 and the L2 one 1e-15; detector vectors times c2a."""
+    P, om, gm = case
+    q_host = gm.qvec_gaussian(P.qm.Q, P.qwidth, neumann)
+    q_dev = gm.qvec_gaussian_device(P.qm.Q, P.qwidth, neumann)
+    assert relmax(q_dev, q_host) < 1e-12
+    assert rel2(q_dev, q_host) < 1e-15
+    cm, ck, ca = capi.optical_coefficients(P.mua, P.mus, P.nref)
+    m_dev = gm.qvec_gaussian_device(P.qm.M, P.mwidth, neumann, scale=ca)
+    m_host = gm.qvec_gaussian(P.qm.M, P.mwidth, neumann) * ca[None, :]
+    assert relmax(m_dev, m_host) < 1e-12
+    assert rel2(m_dev, m_host) < 1e-15
+    torch = pytest.importorskip("torch")
+    d_out = torch.zeros((len(P.qm.Q), gm.n), dtype=torch.float64, device="cuda")
+    gm.qvec_gaussian_device(P.qm.Q, P.qwidth, neumann, out=d_out)
+    assert relmax(d_out.cpu().numpy(), q_host) < 1e-12

@@ -17,8 +17,11 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libtoastgpu.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code (mesh geometry, rasters, host source vectors) without contracted
+# multiply-adds, so that it rounds as the reference's x86 build does on every
+# host architecture; device code keeps nvcc's fused multiply-adds
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-              "--expt-relaxed-constexpr", f"-I{INCLUDE}"]
+              "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", f"-I{INCLUDE}"]
 
 
 def _nvcc() -> str:
@@ -33,7 +36,8 @@ def sources():
 
 
 def deps():
-    return sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    return (sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+            + [os.path.abspath(__file__)])
 
 
 def build(force: bool = False, verbose: bool = False) -> str:

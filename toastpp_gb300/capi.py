@@ -24,7 +24,7 @@ MEM_HOST, MEM_DEVICE = 0, 1
 DATA_LIN, DATA_LOG = 1, 2
 
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
-           "tg_qvec_gaussian", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream", "tg_solver_set_output_stream",
+           "tg_qvec_gaussian", "tg_qvec_gaussian_ex", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream", "tg_solver_set_output_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
            "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_raster_create", "tg_raster_destroy", "tg_raster_info", "tg_raster_elref", "tg_jacobian_grid",
            "tg_server_create", "tg_server_destroy", "tg_submit", "tg_poll", "tg_wait", "tg_server_stats",
@@ -70,6 +70,7 @@ def lib():
             "tg_mesh_csr": [vp, vp, vp],
             "tg_mesh_boundary": [vp, vp],
             "tg_qvec_gaussian": [vp, i_, vp, d_, i_, vp],
+            "tg_qvec_gaussian_ex": [vp, i_, vp, d_, i_, vp, vp, i_],
             "tg_solver_create": [vp, i_, i_, i_, d_, i_, i_, C.POINTER(C.c_void_p)],
             "tg_solver_destroy": [vp],
             "tg_solver_set": [vp, d_, i_],
@@ -172,6 +173,22 @@ class Mesh:
         pos = np.ascontiguousarray(np.atleast_2d(pos), np.float64)
         out = np.zeros((pos.shape[0], self.n))
         _check(lib().tg_qvec_gaussian(self._h, pos.shape[0], _ptr(pos), float(width), int(neumann), _ptr(out)))
+        return out
+
+    def qvec_gaussian_device(self, pos, width, neumann=True, scale=None, out=None):
+        """tg_qvec_gaussian_ex: the source (or, with scale = c2a, detector)
+        vectors formed on the device.  out: a device tensor (npos x n float64)
+        for MEM_DEVICE (scale then a device tensor too), else None for a
+        host array."""
+        pos = np.ascontiguousarray(np.atleast_2d(pos), np.float64)
+        if out is None:
+            res = np.zeros((pos.shape[0], self.n))
+            sc = None if scale is None else np.ascontiguousarray(scale, np.float64)
+            _check(lib().tg_qvec_gaussian_ex(self._h, pos.shape[0], _ptr(pos), float(width), int(neumann), _ptr(sc),
+                                             _ptr(res), MEM_HOST))
+            return res
+        _check(lib().tg_qvec_gaussian_ex(self._h, pos.shape[0], _ptr(pos), float(width), int(neumann), _ptr(scale),
+                                         _ptr(out), MEM_DEVICE))
         return out
 
 

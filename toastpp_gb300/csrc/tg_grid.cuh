@@ -171,4 +171,44 @@ __global__ void grid_jacobian_kernel(int dim, int slen, int nq, int nqm, const V
     }
 }
 
+// QVec_Gaussian (src/libstoast/source.cc:19-56) for npos positions on the
+// device: a thread per (node, position) gathers the contributions the
+// reference scatters, in the reference's order (elements ascending, then the
+// element's source nodes i ascending): q[js] += s_i BndIntFF(i, j) (Neumann:
+// boundary source and receiving nodes only) or s_i IntFF(i, j), with
+// s_i = exp(-d_i^2 / 2w^2) fac1.  scale (optional, n values) multiplies the
+// result (detector vectors times c2a, toastmodule.cc:1189-1220).
+__global__ void qvec_gaussian_kernel(int n, int dim, int nn, const double* __restrict__ coords,
+                                     const int* __restrict__ el, const int* __restrict__ nel_ptr,
+                                     const int* __restrict__ nel_list, const unsigned char* __restrict__ bnd,
+                                     const double* __restrict__ intbff, const double* __restrict__ rec, int rec_len,
+                                     int npos, const double* __restrict__ pos, double fac1, double fac2, int neumann,
+                                     const double* __restrict__ scale, double* __restrict__ q)
+{
+    const int js = blockIdx.x * blockDim.x + threadIdx.x, p = blockIdx.y;
+    if (js >= n || p >= npos) return;
+    double acc = 0.0;
+    if (!neumann || bnd[js]) {
+        const double* c = pos + (size_t)p * dim;
+        for (int t = nel_ptr[js]; t < nel_ptr[js + 1]; t++) {
+            const int e = nel_list[t] >> 2, j = nel_list[t] & 3;
+            const int* nd = el + (size_t)e * nn;
+            for (int i = 0; i < nn; i++) {
+                const int is = nd[i];
+                if (neumann && !bnd[is]) continue;
+                double d2 = 0.0;
+                for (int k = 0; k < dim; k++) {
+                    const double dk = c[k] - coords[(size_t)is * dim + k];
+                    d2 += dk * dk;
+                }
+                const double d = sqrt(d2);
+                const double sv = exp(d * d * fac2) * fac1;
+                if (neumann) acc += sv * intbff[((size_t)e * nn + i) * nn + j];
+                else acc += sv * ((i == j ? 2.0 : 1.0) * (dim == 2 ? 1.0 / 12.0 : 1.0 / 20.0) * rec[(size_t)e * rec_len]);
+            }
+        }
+    }
+    q[(size_t)p * n + js] = scale ? acc * scale[js] : acc;
+}
+
 }  // namespace tg

@@ -776,6 +776,9 @@ using namespace tg;
 // ---------------------------------------------------------------------------
 struct tg_mesh_s {
     std::unique_ptr<Mesh> m;
+    // source-vector data on the device, made on first use
+    std::mutex mu;
+    DBuf d_coords, d_intbff, d_pos, d_scale, d_out;
 };
 
 // Raster_Pixel with the basis equal to the grid (src/libstoast/raster.cc:18-83,
@@ -1698,6 +1701,49 @@ int tg_qvec_gaussian(tg_mesh mesh, int npos, const double* pos, double width, in
     const MeshHost& h = mesh->m->h;
     for (int p = 0; p < npos; p++)
         qvec_gaussian_host(h, pos + (size_t)p * h.dim, width, neumann != 0, out + (size_t)p * h.n);
+    API_END
+}
+
+int tg_qvec_gaussian_ex(tg_mesh mesh, int npos, const double* pos, double width, int neumann, const double* scale,
+                        double* out, int mem)
+{
+    API_BEGIN
+    TG_CHECK(mesh && (npos == 0 || (pos && out)), TG_ERR_ARG, "NULL argument");
+    TG_CHECK(width > 0, TG_ERR_ARG, "width must be positive");
+    TG_CHECK(npos <= 65535, TG_ERR_ARG, "too many positions in one call");
+    if (npos == 0) return TG_OK;
+    std::lock_guard<std::mutex> g(mesh->mu);
+    const MeshHost& h = mesh->m->h;
+    const MeshDev& d = mesh->m->d;
+    TG_CUDA(cudaSetDevice(mesh->m->device));
+    if (!mesh->d_coords.p) {
+        upload_sync(mesh->d_coords, h.coords);
+        upload_sync(mesh->d_intbff, h.intbff);
+    }
+    // the reference's factors (source.cc:24-31)
+    const double PI = 3.14159265358979323846;
+    double fac1 = 1.0 / (std::sqrt(2.0 * PI) * width);
+    if (h.dim == 3) fac1 /= (std::sqrt(2.0 * PI) * width);
+    if (!neumann) fac1 /= (std::sqrt(2.0 * PI) * width);
+    const double fac2 = -0.5 / (width * width);
+    const size_t pb = (size_t)npos * h.dim * sizeof(double), ob = (size_t)npos * h.n * sizeof(double);
+    double* dpos = (double*)mesh->d_pos.ensure(pb);
+    TG_CUDA(cudaMemcpy(dpos, pos, pb, cudaMemcpyHostToDevice));
+    const double* dsc = nullptr;
+    if (scale) {
+        if (mem == TG_MEM_DEVICE) dsc = scale;
+        else {
+            dsc = (const double*)mesh->d_scale.ensure((size_t)h.n * sizeof(double));
+            TG_CUDA(cudaMemcpy((void*)dsc, scale, (size_t)h.n * sizeof(double), cudaMemcpyHostToDevice));
+        }
+    }
+    double* dout = mem == TG_MEM_DEVICE ? out : (double*)mesh->d_out.ensure(ob);
+    launch(qvec_gaussian_kernel, dim3(cdiv_u(h.n, 128), npos), 128, 0, (cudaStream_t)0, h.n, h.dim, h.nn,
+           mesh->d_coords.as<double>(), d.el, d.nel_ptr, d.nel_list, d.bndnode, mesh->d_intbff.as<double>(), d.rec,
+           EL_REC, npos, (const double*)dpos, fac1, fac2, neumann, dsc, dout);
+    TG_CUDA(cudaGetLastError());
+    if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpy(out, dout, ob, cudaMemcpyDeviceToHost));
+    else TG_CUDA(cudaStreamSynchronize(0));
     API_END
 }
 
