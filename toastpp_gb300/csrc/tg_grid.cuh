@@ -114,59 +114,78 @@ __global__ void grid_yinv_kernel(int nqm, const V64* __restrict__ y, C* __restri
     else yinv[l] = vcast<C, V64>(1.0 / y[l]);
 }
 
-// One thread per (solution point, source): PMDF_mua = -(f a), PMDF_kap =
-// -sum_d (grad_d f)(grad_d a) (jacobian.cc:58-72); complex LOG data are
-// divided by y (PMDF_log, 76-79) before the voxel scale, real LOG rows are
-// scaled by 1/y after it (GenerateJacobian_cw, 178-193).  Both multiply by
-// the link's 1/y (yinv): a division per entry would run on the FP64 pipe.
-// J rows: complex [Re mua | Re kap] at l and [Im mua | Im kap] at nQM + l
-// (2 slen columns); real mua at l and kap at nQM + l (slen columns).
-template <class V, class JT>
-__global__ void grid_jacobian_kernel(int dim, int slen, int nq, int nqm, const V* __restrict__ Fp,
-                                     const V* __restrict__ Ap, const int* __restrict__ link_ofs,
-                                     const int* __restrict__ link_m, const V* __restrict__ yinv, double sz,
-                                     JT* __restrict__ J)
+// J stores bypass L2 retention (evict-first), so the 2.4 GB stream of rows
+// does not push the field planes out of L2
+__device__ __forceinline__ void st_stream(float* p, float v) { __stcs(p, v); }
+__device__ __forceinline__ void st_stream(double* p, double v) { __stcs(p, v); }
+
+// One thread per (solution point, group of GQ sources): the sources' planes
+// stay in registers while the detectors' planes stream past, each loaded
+// once per group.  PMDF_mua = -(f a), PMDF_kap = -sum_d (grad_d f)(grad_d a)
+// (jacobian.cc:58-72); complex LOG data are divided by y (PMDF_log, 76-79)
+// before the voxel scale, real LOG rows are scaled by 1/y after it
+// (GenerateJacobian_cw, 178-193).  Both multiply by the link's 1/y (yinv): a
+// division per entry would run on the FP64 pipe.  pair[q * nm + m]: link
+// index or -1.  J rows: complex [Re mua | Re kap] at l and [Im mua | Im kap]
+// at nQM + l (2 slen columns); real mua at l and kap at nQM + l (slen).
+template <class V, class JT, int GQ>
+__global__ void grid_jacobian_kernel(int dim, int slen, int nq, int nm, int nqm, const V* __restrict__ Fp,
+                                     const V* __restrict__ Ap, const int* __restrict__ pair,
+                                     const V* __restrict__ yinv, double sz, JT* __restrict__ J)
 {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x, q = blockIdx.y;
-    if (s >= slen || q >= nq) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x, q0 = blockIdx.y * GQ;
+    if (s >= slen) return;
     using R = typename vt<V>::R;
     const int np = 1 + dim;
-    V f[4];
+    V f[GQ][4];
 #pragma unroll
-    for (int d = 0; d < 4; d++) f[d] = d < np ? Fp[((size_t)q * np + d) * slen + s] : vzero<V>();
+    for (int g = 0; g < GQ; g++)
+#pragma unroll
+        for (int d = 0; d < 4; d++)
+            f[g][d] = (q0 + g < nq && d < np) ? Fp[((size_t)(q0 + g) * np + d) * slen + s] : vzero<V>();
     constexpr bool CPLX = vt<V>::cplx;
     const size_t cols = CPLX ? 2 * (size_t)slen : (size_t)slen;
-    // several links in flight per thread: their plane loads are independent
-#pragma unroll 4
-    for (int l = link_ofs[q]; l < link_ofs[q + 1]; l++) {
-        const int m = link_m[l];
+    for (int m = 0; m < nm; m++) {
+        int lk[GQ];
+        bool any = false;
+#pragma unroll
+        for (int g = 0; g < GQ; g++) {
+            lk[g] = q0 + g < nq ? pair[(size_t)(q0 + g) * nm + m] : -1;
+            any |= lk[g] >= 0;
+        }
+        if (!any) continue;
         V a[4];
 #pragma unroll
         for (int d = 0; d < 4; d++) a[d] = d < np ? Ap[((size_t)m * np + d) * slen + s] : vzero<V>();
-        V pm = vsub(vzero<V>(), vmul(f[0], a[0]));
-        V pk = vzero<V>();
 #pragma unroll
-        for (int d = 1; d < 4; d++)
-            if (d < np) pk = vsub(pk, vmul(f[d], a[d]));
-        JT* r0 = J + (size_t)l * cols;
-        JT* r1 = J + (size_t)(l + nqm) * cols;
-        if constexpr (CPLX) {
-            if (yinv) {
-                pm = vmul(pm, yinv[l]);
-                pk = vmul(pk, yinv[l]);
+        for (int g = 0; g < GQ; g++) {
+            const int l = lk[g];
+            if (l < 0) continue;
+            V pm = vsub(vzero<V>(), vmul(f[g][0], a[0]));
+            V pk = vzero<V>();
+#pragma unroll
+            for (int d = 1; d < 4; d++)
+                if (d < np) pk = vsub(pk, vmul(f[g][d], a[d]));
+            JT* r0 = J + (size_t)l * cols;
+            JT* r1 = J + (size_t)(l + nqm) * cols;
+            if constexpr (CPLX) {
+                if (yinv) {
+                    pm = vmul(pm, yinv[l]);
+                    pk = vmul(pk, yinv[l]);
+                }
+                st_stream(r0 + s, (JT)(re(pm) * (R)sz));
+                st_stream(r1 + s, (JT)(im(pm) * (R)sz));
+                st_stream(r0 + slen + s, (JT)(re(pk) * (R)sz));
+                st_stream(r1 + slen + s, (JT)(im(pk) * (R)sz));
+            } else {
+                R vm = re(pm) * (R)sz, vk = re(pk) * (R)sz;
+                if (yinv) {
+                    vm *= yinv[l];
+                    vk *= yinv[l];
+                }
+                st_stream(r0 + s, (JT)vm);
+                st_stream(r1 + s, (JT)vk);
             }
-            r0[s] = (JT)(re(pm) * (R)sz);
-            r1[s] = (JT)(im(pm) * (R)sz);
-            r0[slen + s] = (JT)(re(pk) * (R)sz);
-            r1[slen + s] = (JT)(im(pk) * (R)sz);
-        } else {
-            R vm = re(pm) * (R)sz, vk = re(pk) * (R)sz;
-            if (yinv) {
-                vm *= yinv[l];
-                vk *= yinv[l];
-            }
-            r0[s] = (JT)vm;
-            r1[s] = (JT)vk;
         }
     }
 }

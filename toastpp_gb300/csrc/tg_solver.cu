@@ -1525,17 +1525,14 @@ static void grid_jac_run(tg_solver s, const tg_raster_s& r, int nq, const V64* F
         launch(grid_yinv_kernel<C, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, yl, yc);
         yinv = yc;
     }
-    int *lo = (int*)s->plink_q.ensure((size_t)(nq + 1) * sizeof(int)), *lm = (int*)s->plink_m.ensure(
-        (size_t)std::max(nqm, 1) * sizeof(int));
-    std::vector<int> ofs(nq + 1, 0);
-    for (int l = 0; l < nqm; l++) ofs[L.q[l] + 1]++;
-    for (int q = 0; q < nq; q++) ofs[q + 1] += ofs[q];
-    // pageable sources: the copies complete before these calls return
-    TG_CUDA(cudaMemcpyAsync(lo, ofs.data(), (size_t)(nq + 1) * sizeof(int), cudaMemcpyHostToDevice, s->stream));
-    TG_CUDA(cudaMemcpyAsync(lm, L.m.data(), (size_t)nqm * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    // link index per (source, detector); a pageable source: the copy
+    // completes before the call returns
+    int* pr = (int*)s->jpair.ensure(L.pair.size() * sizeof(int));
+    TG_CUDA(cudaMemcpyAsync(pr, L.pair.data(), L.pair.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
     using JT = typename vt<C>::R;
-    launch(grid_jacobian_kernel<C, JT>, dim3(gx, nq), 256, 0, s->stream, r.dim, r.slen, nq, nqm, Pq, Pm, lo, lm, yinv,
-           r.voxel(), (JT*)Jd);
+    constexpr int GQ = 4;
+    launch(grid_jacobian_kernel<C, JT, GQ>, dim3(gx, cdiv_u(nq, GQ)), 256, 0, s->stream, r.dim, r.slen, nq, nm, nqm,
+           Pq, Pm, (const int*)pr, yinv, r.voxel(), (JT*)Jd);
 }
 
 template <class V64, class V32>
