@@ -147,6 +147,12 @@ int tg_solver_set_output_stream(tg_solver s, void *stream);
    (0 for real systems).  Assembles F and factors the preconditioner on the GPU. */
 int tg_solver_reset(tg_solver s, const double *cmua, const double *ckappa, const double *c2a,
                     double omega, int mem);
+/* Reset(sol, omega, elbasis) (fwdsolver.cc:467-505): elbasis = 1 takes one
+   cmua / ckappa / c2a value per element (ne each) and assembles with the
+   element-basis modes ASSEMBLE_PFF_EL / PDD_EL / BNDPFF_EL
+   (src/libfe/mesh.cc:1985-1993); elbasis = 0 is tg_solver_reset. */
+int tg_solver_reset_basis(tg_solver s, const double *cmua, const double *ckappa, const double *c2a, double omega,
+                          int mem, int elbasis);
 /* copy of the assembled system matrix values in CSR order (nnz reals or
    nnz complex) */
 int tg_solver_matrix(tg_solver s, double *val, int mem);

@@ -68,6 +68,8 @@ def lib():
                                    _dp, C.c_int]
         L.tor_a_keijzer.restype = C.c_double
         L.tor_a_keijzer.argtypes = [C.c_double]
+        L.tor_assemble_el.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, C.c_int, _dp]
+        L.tor_jacobian_el.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int, C.c_int, _dp]
         L.tor_raster_pixel.restype = C.c_int
         L.tor_raster_pixel.argtypes = [C.c_void_p, _ip, _dp, _dp, _ip, _ip, _ip, _dp]
         L.tor_jacobian_grid.restype = C.c_int
@@ -207,6 +209,27 @@ def jacobian(mesh: Mesh, dphi, aphi, proj_lin, link_ofs, link_m, logscale=True, 
                        _cview(proj_lin).ravel() if cplx else np.ascontiguousarray(proj_lin, np.float64).ravel(),
                        np.ascontiguousarray(link_ofs, np.int32), np.ascontiguousarray(link_m, np.int32),
                        int(cplx), int(logscale), J.reshape(-1), int(nthreads))
+    return J
+
+
+def assemble_el(mesh: Mesh, cmua_el, ckap_el, c2a_el, omega, cplx):
+    """System matrix values (mesh CSR) from one coefficient per element."""
+    val = np.zeros(mesh.nnz * (2 if cplx else 1))
+    lib().tor_assemble_el(mesh._h, np.ascontiguousarray(cmua_el, np.float64), np.ascontiguousarray(ckap_el, np.float64),
+                          np.ascontiguousarray(c2a_el, np.float64), float(omega), int(cplx), val)
+    return val.view(np.complex128) if cplx else val
+
+
+def jacobian_el(mesh: Mesh, dphi, aphi, proj_lin, link_ofs, link_m, logscale=True):
+    """Element-basis Jacobian: complex (2 nQM) x (2 ne), real (2 nQM) x ne."""
+    cplx = np.iscomplexobj(dphi)
+    nq, n = dphi.shape
+    nm = aphi.shape[0]
+    nqm = int(link_ofs[-1])
+    J = np.zeros((2 * nqm, 2 * mesh.ne) if cplx else (2 * nqm, mesh.ne))
+    f = (lambda a: _cview(a).ravel()) if cplx else (lambda a: np.ascontiguousarray(a, np.float64).ravel())
+    lib().tor_jacobian_el(mesh._h, nq, nm, f(dphi), f(aphi), f(proj_lin), np.ascontiguousarray(link_ofs, np.int32),
+                          np.ascontiguousarray(link_m, np.int32), int(cplx), int(logscale), J.reshape(-1))
     return J
 
 

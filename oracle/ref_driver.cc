@@ -19,6 +19,11 @@
 // params.bin : n*3 doubles, node-major (mua, mus', nref)
 // qsub/msub  : if >0, only the first qsub sources / msub detectors are solved
 //              (bounded CPU baseline samples); the Jacobian is then skipped.
+// elparams   : E.bin, ne*3 doubles (mua, mus', nref per element): Reset in
+//              the element basis (Reset(sol, omega, true), fwdsolver.cc:467-505)
+//              and the element-basis Jacobian (GenerateJacobian(RASTER_ELBASIS,
+//              ...), jacobian.cc:441-497; CW 738-802), PREFIX_Jel.bin; the
+//              nodal params still give c2a for the detector vectors
 // grid       : also the grid-basis Jacobian for Raster_Pixel(bdim = gdim =
 //              grid) (src/python/toastmodule.cc:696, raster_px.cc:10-48),
 //              LOG data, written with the raster's element reference per grid
@@ -155,6 +160,20 @@ int main(int argc, char** argv) {
     for (int i = 0; i < n; i++) c2a[i] = c0 / (2.0 * ref[i] * A_Keijzer(ref[i]));
     msol.SetParam(OT_C2A, c2a);
     double omega = freq * 2.0 * Pi * 1e-6;
+    const bool elbasis = g_args.count("elparams") > 0;
+    const int ne = mesh.elen();
+    Solution msol_el(OT_NPARAM, elbasis ? ne : 1);
+    if (elbasis) {
+        std::vector<char> b = rbin(arg("elparams", ""));
+        const double* p = (const double*)b.data();
+        RVector emua(ne), emus(ne), eref(ne), ec2a(ne);
+        for (int e = 0; e < ne; e++) { emua[e] = p[3 * e]; emus[e] = p[3 * e + 1]; eref[e] = p[3 * e + 2]; }
+        for (int e = 0; e < ne; e++) ec2a[e] = c0 / (2.0 * eref[e] * A_Keijzer(eref[e]));
+        msol_el.SetParam(OT_CMUA, emua * c0 / eref);
+        msol_el.SetParam(OT_CKAPPA, c0 / (3.0 * eref * (emua + emus)));
+        msol_el.SetParam(OT_N, eref);
+        msol_el.SetParam(OT_C2A, ec2a);
+    }
 
     // detector positions as used (after LoadQM/InitM pulled them to the boundary)
     {
@@ -191,7 +210,8 @@ int main(int argc, char** argv) {
         FWS.SetDataScaling(DATA_LOG);
         FWS.Allocate();
         double t0 = walltic();
-        FWS.Reset(msol, omega);
+        if (elbasis) FWS.Reset(msol_el, omega, true);
+        else FWS.Reset(msol, omega);
         fprintf(info, "t_reset %.9g\n", walltoc(t0));
         if (want_sys) {
             const CCompRowMatrix& F = *FWS.F;
@@ -227,6 +247,11 @@ int main(int argc, char** argv) {
                 fprintf(info, "t_jac %.9g\n", walltoc(t0));
                 wbin(out + "_J.bin", J.ValPtr(), (size_t)2 * nQM * 2 * n * sizeof(double));
             }
+            if (elbasis) {
+                RDenseMatrix Je(2 * nQM, 2 * ne);
+                GenerateJacobian(RASTER_ELBASIS, &mesh, dphi, aphi, &proj, DATA_LOG, Je);
+                wbin(out + "_Jel.bin", Je.ValPtr(), (size_t)2 * nQM * 2 * ne * sizeof(double));
+            }
             if ((int)grid.size() == dim) {
                 IVector bdim(dim, grid.data());
                 Raster_Pixel raster(bdim, bdim, &mesh);
@@ -258,7 +283,8 @@ int main(int argc, char** argv) {
         FWS.SetDataScaling(DATA_LOG);
         FWS.Allocate();
         double t0 = walltic();
-        FWS.Reset(msol, 0);
+        if (elbasis) FWS.Reset(msol_el, 0, true);
+        else FWS.Reset(msol, 0);
         fprintf(info, "t_reset %.9g\n", walltoc(t0));
         if (want_sys) {
             const RCompRowMatrix& F = *FWS.F;
@@ -295,6 +321,14 @@ int main(int argc, char** argv) {
                 FILE* f = fopen((out + "_J.bin").c_str(), "wb");
                 fwrite(Jmua.ValPtr(), sizeof(double), (size_t)nQM * n, f);
                 fwrite(Jkap.ValPtr(), sizeof(double), (size_t)nQM * n, f);
+                fclose(f);
+            }
+            if (elbasis) {
+                RDenseMatrix Jmua, Jkap;
+                GenerateJacobian_cw(RASTER_ELBASIS, &mesh, dphi, aphi, &proj, DATA_LOG, &Jmua, &Jkap);
+                FILE* f = fopen((out + "_Jel.bin").c_str(), "wb");
+                fwrite(Jmua.ValPtr(), sizeof(double), (size_t)nQM * ne, f);
+                fwrite(Jkap.ValPtr(), sizeof(double), (size_t)nQM * ne, f);
                 fclose(f);
             }
             if ((int)grid.size() == dim) {

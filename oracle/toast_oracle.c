@@ -439,6 +439,43 @@ void tor_assemble(const tor_mesh *m, const double *cmua, const double *ckap, con
     free(tmp);
 }
 
+/* Element-basis assembly (TFwdSolver::Reset with elbasis, fwdsolver.cc:
+   337-357 / 404-424; AddToElMatrix modes ASSEMBLE_PFF_EL / PDD_EL /
+   BNDPFF_EL, mesh.cc:1985-1993): entry IntFF(i,j) P[e], IntDD(i,j) P[e],
+   BndIntFF(i,j) P[e], each mode accumulated as tor_assemble does. */
+void tor_assemble_el(const tor_mesh *m, const double *cmua, const double *ckap, const double *c2a,
+                     double omega, int cplx, double *val)
+{
+    int nnz = m->nnz, nn = m->nn;
+    double *tmp = malloc(sizeof(double) * nnz);
+    memset(val, 0, sizeof(double) * nnz * (cplx ? 2 : 1));
+    for (int mode = 0; mode < 3; mode++) {
+        const double *P = mode == 0 ? cmua : mode == 1 ? ckap : c2a;
+        memset(tmp, 0, sizeof(double) * nnz);
+        for (int e = 0; e < m->ne; e++) {
+            const int *nd = m->el + (size_t)e * nn;
+            for (int i = 0; i < nn; i++)
+                for (int j = 0; j < nn; j++) {
+                    double v;
+                    if (mode == 0) v = el_intff(m, e, i, j) * P[e];
+                    else if (mode == 1) v = m->intdd[((size_t)e * nn + i) * nn + j] * P[e];
+                    else v = m->intbff[((size_t)e * nn + i) * nn + j] * P[e];
+                    tmp[csr_find(m->rowptr, m->colidx, nd[i], nd[j])] += v;
+                }
+        }
+        for (int k = 0; k < nnz; k++) val[cplx ? 2 * k : k] += tmp[k];
+    }
+    if (cplx) {
+        for (int e = 0; e < m->ne; e++) {
+            const int *nd = m->el + (size_t)e * nn;
+            for (int i = 0; i < nn; i++)
+                for (int j = 0; j < nn; j++)
+                    val[2 * csr_find(m->rowptr, m->colidx, nd[i], nd[j]) + 1] += el_intff(m, e, i, j) * omega;
+        }
+    }
+    free(tmp);
+}
+
 /* ------------------------------------------------------------------------ */
 /* Source and measurement vectors: QVec_Gaussian (source.cc:19-56)           */
 /* ------------------------------------------------------------------------ */
@@ -1447,6 +1484,62 @@ int tor_jacobian_grid(const tor_mesh *m, const int *bdim, int nq, int nm, const 
     free(elref); free(browptr); free(bcol); free(bval); free(sol); free(fin);
     free(ag); free(agr); free(dg); free(dgr); free(pm); free(pk);
     return slen;
+}
+
+/* Element-basis Jacobian (GenerateJacobian_mesh with elbasis, jacobian.cc:
+   441-497, complex, projections given; GenerateJacobian_cw_mesh 738-802 and
+   the LOG row scaling of GenerateJacobian_cw 178-193, real), with IntFG_el /
+   IntGradFGradG_el (jacobian.cc:884-939): per element sum_ij (f_i g_j)
+   IntFF(i,j) and (f_i g_j) IntDD(i,j).  J: complex (2 nQM) x (2 ne) rows
+   -Re / -Im, kappa at column ne + e; real (2 nQM) x ne [mua ; kappa]. */
+void tor_jacobian_el(const tor_mesh *m, int nq, int nm, const double *dphi, const double *aphi,
+                     const double *proj, const int *link_ofs, const int *link_m, int cplx, int logscale, double *J)
+{
+    const int n = m->n, ne = m->ne, nn = m->nn, nqm = link_ofs[nq];
+    (void)nm;
+    const size_t cols = cplx ? 2 * (size_t)ne : (size_t)ne;
+    for (int q = 0; q < nq; q++)
+        for (int l = link_ofs[q]; l < link_ofs[q + 1]; l++) {
+            const int j = link_m[l];
+            double *r0 = J + (size_t)l * cols, *r1 = J + (size_t)(l + nqm) * cols;
+            for (int e = 0; e < ne; e++) {
+                const int *nd = m->el + (size_t)e * nn;
+                if (cplx) {
+                    zd sm = 0.0, sk = 0.0;
+                    for (int a = 0; a < nn; a++)
+                        for (int b = 0; b < nn; b++) {
+                            zd f = dphi[2 * ((size_t)q * n + nd[a])] + I * dphi[2 * ((size_t)q * n + nd[a]) + 1];
+                            zd g = aphi[2 * ((size_t)j * n + nd[b])] + I * aphi[2 * ((size_t)j * n + nd[b]) + 1];
+                            sm += (f * g) * el_intff(m, e, a, b);
+                            sk += (f * g) * m->intdd[((size_t)e * nn + a) * nn + b];
+                        }
+                    zd pm = 0.0 + sm, pk = 0.0 + sk;
+                    if (logscale) {
+                        zd y = proj[2 * l] + I * proj[2 * l + 1];
+                        pm = pm / y;
+                        pk = pk / y;
+                    }
+                    r0[e] = -creal(pm); r1[e] = -cimag(pm);
+                    r0[ne + e] = -creal(pk); r1[ne + e] = -cimag(pk);
+                } else {
+                    double sm = 0.0, sk = 0.0;
+                    for (int a = 0; a < nn; a++)
+                        for (int b = 0; b < nn; b++) {
+                            double fg = dphi[(size_t)q * n + nd[a]] * aphi[(size_t)j * n + nd[b]];
+                            sm += fg * el_intff(m, e, a, b);
+                            sk += fg * m->intdd[((size_t)e * nn + a) * nn + b];
+                        }
+                    double vm = -(0.0 + sm), vk = -(0.0 + sk);
+                    if (logscale) {
+                        double iy = 1.0 / proj[l];
+                        vm *= iy;
+                        vk *= iy;
+                    }
+                    r0[e] = vm;
+                    r1[e] = vk;
+                }
+            }
+        }
 }
 
 /* A_Keijzer (param.cc:24-32) */

@@ -16,6 +16,10 @@ src/python/toastmodule.cc:696), the raster's element reference per grid
 point and the reference's own fields, so the oracle's raster and grid
 Jacobian are checked on exactly the reference's inputs.
 
+The *_el fixtures reset the solver in the element basis (one mua, mus',
+nref per element, seeded) and hold the reference's system matrix, fields,
+projections and element-basis Jacobian.
+
 Usage:  make -f oracle/Makefile.ref REF=<reference tree> -j8
         python tests/golden/make_golden.py [fixture names]
 """
@@ -61,14 +65,31 @@ FIXTURES = {
     "disc_fd_grid": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (24, 20)),
     "cyl_cw_grid": (lambda: small_cylinder(0.0), "CG", "ICH", 1e-15, False, (9, 10, 12)),
     "cyl_fd_grid": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-15, False, (10, 9, 11)),
+    # element basis (Reset(sol, omega, true), GenerateJacobian(RASTER_ELBASIS, ...))
+    "disc_cw_el": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "ICH", 1e-15, False, None, True),
+    "disc_fd_el": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, None, True),
+    "cyl_cw_el": (lambda: small_cylinder(0.0), "CG", "ICH", 1e-15, False, None, True),
+    "cyl_fd_el": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-15, False, None, True),
 }
+
+
+def element_params(P, seed=11):
+    """Seeded per-element parameters: the element mean of the nodal mua and
+    mus' times 1 + 0.3 u (u uniform in [-1, 1]); the nodal refractive index's
+    element mean."""
+    rng = np.random.default_rng(seed)
+    ne = len(P.elems)
+    mua = P.mua[P.elems].mean(1) * (1 + 0.3 * rng.uniform(-1, 1, ne))
+    mus = P.mus[P.elems].mean(1) * (1 + 0.3 * rng.uniform(-1, 1, ne))
+    nref = P.nref[P.elems].mean(1)
+    return mua, mus, nref
 
 
 def rd(path, dtype):
     return np.fromfile(path, dtype=dtype)
 
 
-def run(name, factory, solver, precon, tol, jac, grid=None):
+def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False):
     P = factory()
     cplx = P.complex
     with tempfile.TemporaryDirectory() as td:
@@ -87,6 +108,11 @@ def run(name, factory, solver, precon, tol, jac, grid=None):
                 "maxit=0", f"freq={P.freq_mhz}", f"qwidth={P.qwidth}", f"mwidth={P.mwidth}", f"jac={int(jac)}"]
         if grid:
             args += ["grid=" + ",".join(str(g) for g in grid), "fields=1"]
+        if elbasis:
+            emua, emus, eref = element_params(P)
+            epar = os.path.join(td, "elpar.bin")
+            np.stack([emua, emus, eref], axis=1).astype(np.float64).tofile(epar)
+            args += [f"elparams={epar}", "fields=1", "sysmat=1"]
         subprocess.run(args, check=True)
         info = dict(l.split() for l in open(out + "_info.txt") if l.strip())
         ct = np.complex128 if cplx else np.float64
@@ -96,6 +122,15 @@ def run(name, factory, solver, precon, tol, jac, grid=None):
             nqm = len(res["proj"])
             J = rd(out + "_J.bin", np.float64)
             res["J"] = J.reshape((2 * nqm, 2 * P.n) if cplx else (2 * nqm, P.n))
+        if elbasis:
+            nqm = len(res["proj"])
+            ne = len(P.elems)
+            Je = rd(out + "_Jel.bin", np.float64)
+            res["Jel"] = Je.reshape((2 * nqm, 2 * ne) if cplx else (2 * nqm, ne))
+            res["elmua"], res["elmus"], res["elnref"] = element_params(P)
+            res["sysval"] = rd(out + "_sysval.bin", ct)
+            res["dphi"] = rd(out + "_dphi.bin", ct).reshape(len(P.qm.Q), P.n)
+            res["aphi"] = rd(out + "_aphi.bin", ct).reshape(len(P.qm.M), P.n)
         if grid:
             nqm = len(res["proj"])
             slen = int(info["slen"])

@@ -117,6 +117,39 @@ __global__ void assemble_kernel(MeshDev m, const double* __restrict__ cmua, cons
     else val[k] = v;
 }
 
+// Element-basis assembly (AddToElMatrix modes ASSEMBLE_PFF_EL, PDD_EL,
+// BNDPFF_EL, src/libfe/mesh.cc:1985-1993, for TFwdSolver::Reset with
+// elbasis, fwdsolver.cc:337-357 / 404-424): one coefficient per element,
+// entry = IntFF(i,j) c_e (tri3.cc:285-292, tet4.cc:348-355), IntDD(i,j) k_e,
+// BndIntFF(i,j) a_e; the three passes summed in the reference's order
+template <bool CPLX>
+__global__ void assemble_el_kernel(MeshDev m, const double* __restrict__ cmua, const double* __restrict__ ckap,
+                                   const double* __restrict__ c2a, double omega, double* __restrict__ val)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.nnz) return;
+    double pff = 0.0, pdd = 0.0, bnd = 0.0, iff = 0.0;
+    const int nn = m.nn;
+    const double ffd = m.dim == 2 ? 1.0 / 12.0 : 1.0 / 20.0;
+    for (int c = m.asm_ptr[k]; c < m.asm_ptr[k + 1]; c++) {
+        int code = m.asm_list[c];
+        int e = code >> 4, i = (code >> 2) & 3, j = code & 3;
+        const double* r = m.rec + (size_t)e * EL_REC;
+        const double sz = r[0];
+        const double intff = ((i == j ? 2.0 : 1.0) * ffd) * sz;
+        pff += intff * cmua[e];
+        pdd += r[1 + i * nn + j] * ckap[e];
+        bnd += m.intbff[((size_t)e * nn + i) * nn + j] * c2a[e];
+        if (CPLX) iff += intff * omega;
+    }
+    double v = 0.0;
+    v += pff;
+    v += pdd;
+    v += bnd;
+    if (CPLX) { val[2 * k] = v; val[2 * k + 1] = iff; }
+    else val[k] = v;
+}
+
 // ---------------------------------------------------------------------------
 // IC(0) (IncompleteCholeskyFactorize, src/libmath/crmatrix_imp.hpp:2166-2203,
 // recover = true; complex pivots compared by squared magnitude,

@@ -445,7 +445,8 @@ static T* upload(const std::vector<T>& v)
 Mesh::~Mesh()
 {
     void* ptrs[] = {d.rec, d.el, d.rowptr, d.colidx, d.diagpos, d.perm, d.iperm, d.jrowptr, d.jcolidx, d.asm_ptr,
-                    d.asm_list, d.nel_ptr, d.nel_list, d.nel_pos, d.bndnode, d.halo_ptr, d.halo_col, d.lcol};
+                    d.asm_list, d.nel_ptr, d.nel_list, d.nel_pos, d.bndnode, d.halo_ptr, d.halo_col, d.lcol,
+                    d.intbff};
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto& g : d.ic) {
         void* q[] = {g.key, g.Lrowptr, g.Lcolidx, g.Lapos, g.Lkey, g.Ucolptr, g.Urow, g.Umap, g.fwd_lev_rows,
@@ -487,6 +488,7 @@ Mesh* mesh_build(int dim, int n, const double* coords, int ne, const int* el)
     d.dim = dim; d.n = n; d.ne = ne; d.nn = m.nn;
     d.nnz = m.rowptr[n];
     d.rec = upload(m.rec);
+    d.intbff = upload(m.intbff);
     d.el = upload(m.el);
     d.rowptr = upload(m.lrowptr);
     d.colidx = upload(m.lcolidx);

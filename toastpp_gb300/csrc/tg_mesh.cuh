@@ -82,6 +82,7 @@ struct MeshDev {
     int *asm_ptr, *asm_list;
     int *nel_ptr, *nel_list;
     unsigned char* bndnode;
+    double* intbff;            // ne*nn*nn boundary integrals BndIntFF (element basis, source vectors)
     ICDev ic[2];
 };
 

@@ -1037,19 +1037,26 @@ static void setup_engine(tg_solver s, Engine<V64>& e64)
 static int ic_order(tg_solver s) { return (s->precision == TG_PREC_MIXED && s->inner_colour) ? 1 : 0; }
 
 template <class V64, class V32>
-static void do_reset(tg_solver s, const double* cmua, const double* ckap, const double* c2a, double omega, int mem)
+static void do_reset(tg_solver s, const double* cmua, const double* ckap, const double* c2a, double omega, int mem,
+                     int elbasis = 0)
 {
     const MeshDev& m = s->mesh->d;
-    size_t nb = (size_t)m.n * sizeof(double);
+    // nodal coefficients, or one per element (element basis)
+    const int np = elbasis ? m.ne : m.n;
+    size_t nb = (size_t)np * sizeof(double);
     double* P = (double*)s->params.ensure(3 * nb);
     cudaMemcpyKind kind = mem == TG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     TG_CUDA(cudaMemcpyAsync(P, cmua, nb, kind, s->stream));
-    TG_CUDA(cudaMemcpyAsync(P + m.n, ckap, nb, kind, s->stream));
-    TG_CUDA(cudaMemcpyAsync(P + 2 * m.n, c2a, nb, kind, s->stream));
+    TG_CUDA(cudaMemcpyAsync(P + np, ckap, nb, kind, s->stream));
+    TG_CUDA(cudaMemcpyAsync(P + 2 * np, c2a, nb, kind, s->stream));
     V64* A = (V64*)s->val64.ensure((size_t)m.nnz * sizeof(V64));
     ProfScope ps(&s->prof, PC_ASM, s->stream);
-    launch(assemble_kernel<vt<V64>::cplx>, cdiv_u(m.nnz, 256), 256, 0, s->stream, m, P, P + m.n, P + 2 * m.n, omega,
-           (double*)A);
+    if (elbasis)
+        launch(assemble_el_kernel<vt<V64>::cplx>, cdiv_u(m.nnz, 256), 256, 0, s->stream, m, P, P + np, P + 2 * np,
+               omega, (double*)A);
+    else
+        launch(assemble_kernel<vt<V64>::cplx>, cdiv_u(m.nnz, 256), 256, 0, s->stream, m, P, P + np, P + 2 * np, omega,
+               (double*)A);
     int pre = s->precon == TG_PRECON_DILU ? 0 : s->precon;
     V64* idg = (V64*)s->idiag64.ensure((size_t)m.n * sizeof(V64));
     launch(diag_inv_kernel<V64>, cdiv_u(m.n, 256), 256, 0, s->stream, m.n, m.diagpos, A, idg);
@@ -1821,6 +1828,21 @@ int tg_solver_reset(tg_solver s, const double* cmua, const double* ckappa, const
     std::lock_guard<std::mutex> g(s->mu);
     if (s->cplx) do_reset<cd, cf>(s, cmua, ckappa, c2a, omega, mem);
     else do_reset<double, float>(s, cmua, ckappa, c2a, omega, mem);
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+    s->reset_done = true;
+    API_END
+}
+
+int tg_solver_reset_basis(tg_solver s, const double* cmua, const double* ckappa, const double* c2a, double omega,
+                          int mem, int elbasis)
+{
+    API_BEGIN
+    TG_CHECK(s && cmua && ckappa && c2a, TG_ERR_ARG, "NULL argument");
+    TG_CHECK(s->cplx || omega == 0.0, TG_ERR_ARG, "nonzero omega for a real system");
+    TG_CHECK(elbasis == 0 || elbasis == 1, TG_ERR_ARG, "elbasis must be 0 or 1");
+    std::lock_guard<std::mutex> g(s->mu);
+    if (s->cplx) do_reset<cd, cf>(s, cmua, ckappa, c2a, omega, mem, elbasis);
+    else do_reset<double, float>(s, cmua, ckappa, c2a, omega, mem, elbasis);
     TG_CUDA(cudaStreamSynchronize(s->stream));
     s->reset_done = true;
     API_END
