@@ -8,8 +8,11 @@ import numpy as np
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def names():
-    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+def names(nodal_only=False):
+    """Fixture names; nodal_only drops the element-basis fixtures (*_el), whose
+    solves use one coefficient per element."""
+    out = sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    return [n for n in out if not n.endswith("_el")] if nodal_only else out
 
 
 def load(name):

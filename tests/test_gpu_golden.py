@@ -26,7 +26,7 @@ def run(g, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("name", names())
+@pytest.mark.parametrize("name", names(nodal_only=True))
 def test_gpu_matches_reference_fixture(name, precision):
     g = load(name)
     out = run(g, precision)

@@ -9,7 +9,7 @@ from tests.golden_util import load, names
 from tests.gpu_util import rel2, relmax
 
 
-@pytest.mark.parametrize("name", names())
+@pytest.mark.parametrize("name", names(nodal_only=True))
 def test_oracle_matches_reference_fixture(oracle_mod, name):
     g = load(name)
     mesh = oracle_mod.Mesh(g["coords"], g["elems"])
