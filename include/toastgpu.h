@@ -271,6 +271,14 @@ int tg_solver_profile(tg_solver s, int mask);
 int tg_solver_profile_read(tg_solver s, int cls, double *total_ms, int *count);
 /* number of kernels this library has launched in this process */
 int tg_launch_count(long long *count);
+/* Element-basis Jacobian (GenerateJacobian(RASTER_ELBASIS, ...),
+   jacobian.cc:441-497 with IntFG_el / IntGradFGradG_el, 884-939; real:
+   GenerateJacobian_cw(RASTER_ELBASIS, ...), 178-193 / 738-802).  Inputs as
+   tg_jacobian.  J row-major: complex (2 nQM) x (2 ne) = [-Re mua | -Re kappa ;
+   -Im mua | -Im kappa]; real (2 nQM) x ne = [mua ; kappa]. */
+int tg_jacobian_el(tg_solver s, int nq, const double *dphi, int nm, const double *aphi, const double *proj,
+                   const int *link_ofs, const int *link_m, int scale, void *J, int out_fp32, int mem);
+
 /* ---- grid basis (pixel raster) ----
    Raster_Pixel with the basis equal to the grid, as toast.Raster(mesh, grd)
    builds it (src/python/toastmodule.cc:696; raster.cc:18-83,

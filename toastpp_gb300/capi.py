@@ -26,7 +26,7 @@ DATA_LIN, DATA_LOG = 1, 2
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
            "tg_qvec_gaussian", "tg_qvec_gaussian_ex", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream", "tg_solver_set_output_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
-           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_raster_create", "tg_raster_destroy", "tg_raster_info", "tg_raster_elref", "tg_jacobian_grid",
+           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_solver_reset_basis", "tg_jacobian_el", "tg_raster_create", "tg_raster_destroy", "tg_raster_info", "tg_raster_elref", "tg_jacobian_grid",
            "tg_server_create", "tg_server_destroy", "tg_submit", "tg_poll", "tg_wait", "tg_server_stats",
            "tg_server_reset_stats", "tg_last_error"]
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
@@ -90,6 +90,8 @@ def lib():
             "tg_solver_profile_read": [vp, i_, C.POINTER(C.c_double), ip],
             "tg_launch_count": [C.POINTER(C.c_longlong)],
             "tg_tuner_log": [C.c_char_p, i_],
+            "tg_solver_reset_basis": [vp, dp, dp, dp, d_, i_, i_],
+            "tg_jacobian_el": [vp, i_, dp, i_, dp, dp, vp, vp, i_, vp, i_, i_],
             "tg_raster_create": [vp, ip, C.POINTER(C.c_void_p)],
             "tg_raster_destroy": [vp],
             "tg_raster_info": [vp, ip, ip, dp, dp],
@@ -274,6 +276,23 @@ class FwdSolver:
         if mem == MEM_HOST:
             cmua, ckap, c2a = (np.ascontiguousarray(x, np.float64) for x in (cmua, ckap, c2a))
         _check(lib().tg_solver_reset(self._h, _ptr(cmua), _ptr(ckap), _ptr(c2a), float(omega), mem))
+
+    def reset_elbasis(self, cmua_el, ckap_el, c2a_el, omega=0.0):
+        """Reset(sol, omega, elbasis = true): one coefficient per element."""
+        a = [np.ascontiguousarray(x, np.float64) for x in (cmua_el, ckap_el, c2a_el)]
+        _check(lib().tg_solver_reset_basis(self._h, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), float(omega), MEM_HOST, 1))
+
+    def jacobian_el(self, dphi, aphi, proj, links: Links, scale=DATA_LOG, fp32=False):
+        """Element-basis Jacobian (tg_jacobian_el): complex (2 nQM) x (2 ne),
+        real (2 nQM) x ne."""
+        dphi = _f64(dphi, self.complex)
+        aphi = _f64(aphi, self.complex)
+        nqm, ne = links.nqm, self.mesh.ne
+        J = np.zeros((2 * nqm, 2 * ne if self.complex else ne), np.float32 if fp32 else np.float64)
+        pr = None if proj is None else _f64(proj, self.complex)
+        _check(lib().tg_jacobian_el(self._h, dphi.shape[0], _ptr(dphi), aphi.shape[0], _ptr(aphi), _ptr(pr),
+                                    _ptr(links.ofs), _ptr(links.m), scale, _ptr(J), int(fp32), MEM_HOST))
+        return J
 
     def system_matrix(self):
         out = np.zeros(self.mesh.nnz, np.complex128 if self.complex else np.float64)

@@ -190,6 +190,97 @@ __global__ void grid_jacobian_kernel(int dim, int slen, int nq, int nm, int nqm,
     }
 }
 
+// Element-basis Jacobian (GenerateJacobian_mesh with elbasis, jacobian.cc:
+// 441-497; CW 738-802 and the LOG scaling 178-193), with IntFG_el /
+// IntGradFGradG_el (884-939): per element e and link (q, m),
+// sum_ij f_i g_j IntFF(i,j) and sum_ij f_i g_j IntDD(i,j), formed as
+// sum_i f_i h_i with h = W g once per (element, detector) and shared by the
+// group's GQ sources.  Fields source-major in the natural numbering.
+// J: complex (2 nQM) x (2 ne) rows -Re / -Im, kappa at column ne + e; real
+// (2 nQM) x ne [mua ; kappa].
+template <class V, class JT, int GQ>
+__global__ void element_jacobian_kernel(MeshDev m, int nq, int nm, int nqm, const V* __restrict__ F,
+                                        const V* __restrict__ A, const int* __restrict__ pair,
+                                        const V* __restrict__ yinv, JT* __restrict__ J)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x, q0 = blockIdx.y * GQ;
+    if (e >= m.ne) return;
+    using R = typename vt<V>::R;
+    const int nn = m.nn, n = m.n;
+    const int* nd = m.el + (size_t)e * nn;
+    const double* r = m.rec + (size_t)e * EL_REC;
+    const double ffd = m.dim == 2 ? 1.0 / 12.0 : 1.0 / 20.0;
+    R wff[4][4], wdd[4][4];
+    int node[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        node[i] = i < nn ? nd[i] : 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            wff[i][j] = (i < nn && j < nn) ? (R)(((i == j ? 2.0 : 1.0) * ffd) * r[0]) : (R)0;
+            // IntDD: the record's value for triangles, 4 x it for tetrahedra
+            wdd[i][j] = (i < nn && j < nn) ? (R)((m.dim == 3 ? 4.0 : 1.0) * r[1 + i * nn + j]) : (R)0;
+        }
+    }
+    V f[GQ][4];
+#pragma unroll
+    for (int g = 0; g < GQ; g++)
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+            f[g][i] = (q0 + g < nq && i < nn) ? F[(size_t)(q0 + g) * n + node[i]] : vzero<V>();
+    constexpr bool CPLX = vt<V>::cplx;
+    const size_t cols = CPLX ? 2 * (size_t)m.ne : (size_t)m.ne;
+    for (int mm = 0; mm < nm; mm++) {
+        int lk[GQ];
+        bool any = false;
+#pragma unroll
+        for (int g = 0; g < GQ; g++) {
+            lk[g] = q0 + g < nq ? pair[(size_t)(q0 + g) * nm + mm] : -1;
+            any |= lk[g] >= 0;
+        }
+        if (!any) continue;
+        V a[4], hm[4], hk[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) a[j] = j < nn ? A[(size_t)mm * n + node[j]] : vzero<V>();
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            hm[i] = vzero<V>();
+            hk[i] = vzero<V>();
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                hm[i] = vadd(hm[i], vscale(a[j], wff[i][j]));
+                hk[i] = vadd(hk[i], vscale(a[j], wdd[i][j]));
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < GQ; g++) {
+            const int l = lk[g];
+            if (l < 0) continue;
+            V pm = vzero<V>(), pk = vzero<V>();
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                pm = vfma(pm, f[g][i], hm[i]);
+                pk = vfma(pk, f[g][i], hk[i]);
+            }
+            if (yinv) {
+                pm = vmul(pm, yinv[l]);
+                pk = vmul(pk, yinv[l]);
+            }
+            JT* r0 = J + (size_t)l * cols;
+            JT* r1 = J + (size_t)(l + nqm) * cols;
+            if constexpr (CPLX) {
+                st_stream(r0 + e, (JT)-re(pm));
+                st_stream(r1 + e, (JT)-im(pm));
+                st_stream(r0 + m.ne + e, (JT)-re(pk));
+                st_stream(r1 + m.ne + e, (JT)-im(pk));
+            } else {
+                st_stream(r0 + e, (JT)-pm);
+                st_stream(r1 + e, (JT)-pk);
+            }
+        }
+    }
+}
+
 // QVec_Gaussian (src/libstoast/source.cc:19-56) for npos positions on the
 // device: a thread per (node, position) gathers the contributions the
 // reference scatters, in the reference's order (elements ascending, then the

@@ -138,7 +138,9 @@ __global__ void assemble_el_kernel(MeshDev m, const double* __restrict__ cmua, c
         const double sz = r[0];
         const double intff = ((i == j ? 2.0 : 1.0) * ffd) * sz;
         pff += intff * cmua[e];
-        pdd += r[1 + i * nn + j] * ckap[e];
+        // the record holds IntDD for triangles and IntDD / 4 (the IntFDD
+        // factor, exact) for tetrahedra (Tetrahedron4::ComputeIntDD, tet4.cc:1016-1031)
+        pdd += (m.dim == 3 ? 4.0 * r[1 + i * nn + j] : r[1 + i * nn + j]) * ckap[e];
         bnd += m.intbff[((size_t)e * nn + i) * nn + j] * c2a[e];
         if (CPLX) iff += intff * omega;
     }

@@ -1561,6 +1561,55 @@ static void api_jacobian_grid(tg_solver s, const tg_raster_s& r, int nq, const d
     TG_CUDA(cudaStreamSynchronize(s->stream));
 }
 
+// Element-basis Jacobian: fields source-major natural, FP32 arithmetic for an
+// FP32 J, FP64 for an FP64 J
+template <class V64, class C>
+static void element_jac_run(tg_solver s, int nq, const V64* F, int nm, const V64* A, const V64* yl,
+                            const LinkHost& L, int logscale, void* Jd)
+{
+    const MeshDev& m = s->mesh->d;
+    const int n = m.n, nqm = (int)L.q.size();
+    const C *Fc = (const C*)F, *Ac = (const C*)A;
+    if (!std::is_same<C, V64>::value) {
+        C* f = (C*)s->gplanes_q.ensure((size_t)nq * n * sizeof(C));
+        C* a = (C*)s->gplanes_m.ensure((size_t)nm * n * sizeof(C));
+        launch(cast_kernel<C, V64>, cdiv_u((size_t)nq * n, 256), 256, 0, s->stream, (size_t)nq * n, F, f);
+        launch(cast_kernel<C, V64>, cdiv_u((size_t)nm * n, 256), 256, 0, s->stream, (size_t)nm * n, A, a);
+        Fc = f;
+        Ac = a;
+    }
+    const C* yinv = nullptr;
+    if (logscale) {
+        C* yc = (C*)s->gy.ensure((size_t)nqm * sizeof(C));
+        launch(grid_yinv_kernel<C, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, yl, yc);
+        yinv = yc;
+    }
+    int* pr = (int*)s->jpair.ensure(L.pair.size() * sizeof(int));
+    TG_CUDA(cudaMemcpyAsync(pr, L.pair.data(), L.pair.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    using JT = typename vt<C>::R;
+    constexpr int GQ = 4;
+    launch(element_jacobian_kernel<C, JT, GQ>, dim3(cdiv_u(m.ne, 128), cdiv_u(nq, GQ)), 128, 0, s->stream, m, nq, nm,
+           nqm, Fc, Ac, (const int*)pr, yinv, (JT*)Jd);
+}
+
+template <class V64, class V32>
+static void api_jacobian_el(tg_solver s, int nq, const double* dphi, int nm, const double* aphi, const double* proj,
+                            const LinkHost& L, int scale, void* J, int out_fp32, int mem)
+{
+    const int n = s->mesh->d.n, ne = s->mesh->d.ne, nqm = (int)L.q.size();
+    const V64* F = (const V64*)dev_in(s, dphi, (size_t)nq * n * sizeof(V64), mem, s->io_a);
+    const V64* A = (const V64*)dev_in(s, aphi, (size_t)nm * n * sizeof(V64), mem, s->io_b);
+    const V64* yl = scale == TG_DATA_LOG ? (const V64*)dev_in(s, proj, (size_t)nqm * sizeof(V64), mem, s->plin)
+                                         : nullptr;
+    const size_t jbytes = (size_t)2 * nqm * (vt<V64>::cplx ? 2 : 1) * ne * (out_fp32 ? 4 : 8);
+    void* Jd = mem == TG_MEM_DEVICE ? J : s->jout.ensure(jbytes);
+    if (out_fp32) element_jac_run<V64, V32>(s, nq, F, nm, A, yl, L, scale == TG_DATA_LOG, Jd);
+    else element_jac_run<V64, V64>(s, nq, F, nm, A, yl, L, scale == TG_DATA_LOG, Jd);
+    if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(J, Jd, jbytes, cudaMemcpyDeviceToHost, s->stream));
+    TG_CUDA(cudaGetLastError());
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+}
+
 template <class V64, class V32>
 static void api_forward_path(tg_solver s, const double* cmua, const double* ckap, const double* c2a, double omega,
                              int nq, const double* qvec, int nm, const double* mvec, const LinkHost& L,
@@ -1978,6 +2027,21 @@ int tg_jacobian_grid(tg_solver s, tg_raster r, int nq, const double* dphi, int n
     if (L.q.empty() || r->slen == 0) return TG_OK;
     if (s->cplx) api_jacobian_grid<cd, cf>(s, *r, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
     else api_jacobian_grid<double, float>(s, *r, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
+    API_END
+}
+
+int tg_jacobian_el(tg_solver s, int nq, const double* dphi, int nm, const double* aphi, const double* proj,
+                   const int* link_ofs, const int* link_m, int scale, void* J, int out_fp32, int mem)
+{
+    API_BEGIN
+    TG_CHECK(s && dphi && aphi && link_ofs && J, TG_ERR_ARG, "NULL argument");
+    TG_CHECK(nq > 0 && nm > 0 && nq <= 65535 * 4, TG_ERR_ARG, "source / detector count out of range");
+    TG_CHECK(scale == TG_DATA_LIN || (scale == TG_DATA_LOG && proj), TG_ERR_ARG, "log data needs the projections");
+    std::lock_guard<std::mutex> g(s->mu);
+    LinkHost L = make_links(nq, nm, link_ofs, link_m);
+    if (L.q.empty()) return TG_OK;
+    if (s->cplx) api_jacobian_el<cd, cf>(s, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
+    else api_jacobian_el<double, float>(s, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
     API_END
 }
 
