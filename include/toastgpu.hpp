@@ -11,6 +11,7 @@
 //   toastgpu::Raster_Pixel        Raster_Pixel(bdim, bdim, mesh) (raster_px.cc:10-48), the
 //                                 raster toast.Raster(mesh, grd) builds
 //   toastgpu::GenerateJacobian    GenerateJacobian(raster, ...) grid basis (jacobian.cc:105-123)
+//   toastgpu::GenerateJacobian_el GenerateJacobian(RASTER_ELBASIS, ...) element basis
 //   toastgpu::QVec_Gaussian       QVec_Gaussian, Neumann mode (src/libstoast/source.cc:19-56)
 //
 // Differences a caller sees:
@@ -156,10 +157,12 @@ public:
         }
     }
     // Reset(sol, omega) (fwdsolver.cc:467-505): assembly and preconditioner
-    void Reset(const double* cmua, const double* ckappa, const double* c2a, double omega = 0)
+    // Reset(sol, omega, elbasis) (fwdsolver.cc:467-505): elbasis = true takes
+    // one coefficient per element (mesh.elen() values each)
+    void Reset(const double* cmua, const double* ckappa, const double* c2a, double omega = 0, bool elbasis = false)
     {
         Allocate();
-        check(tg_solver_reset(s_, cmua, ckappa, c2a, omega, TG_MEM_HOST));
+        check(tg_solver_reset_basis(s_, cmua, ckappa, c2a, omega, TG_MEM_HOST, elbasis ? 1 : 0));
     }
     // CalcFields(qvec, phi, res) (fwdsolver.cc:653-750): phi holds the
     // initial guess; res gets the summed iterations and the largest error
@@ -220,6 +223,18 @@ void GenerateJacobian(const TFwdSolver<T>& fws, int nq, const T* dphi, int nm, c
 {
     check(tg_jacobian(fws.handle(), nq, (const double*)dphi, nm, (const double*)aphi, (const double*)proj,
                       L.ofs.data(), L.m.data(), dscale == DATA_LOG ? TG_DATA_LOG : TG_DATA_LIN, J, 0, TG_MEM_HOST));
+}
+
+// GenerateJacobian(RASTER_ELBASIS, mesh, dphi, aphi, proj, dscale, J) element
+// basis: complex J (2 nQM) x (2 ne) row-major [-Re mua | -Re kappa ; -Im mua |
+// -Im kappa] (jacobian.cc:441-497); real J (2 nQM) x ne [mua ; kappa]
+// (GenerateJacobian_cw(RASTER_ELBASIS, ...), jacobian.cc:178-193, 738-802)
+template <class T>
+void GenerateJacobian_el(const TFwdSolver<T>& fws, int nq, const T* dphi, int nm, const T* aphi, const T* proj,
+                         const Links& L, DataScale dscale, double* J)
+{
+    check(tg_jacobian_el(fws.handle(), nq, (const double*)dphi, nm, (const double*)aphi, (const double*)proj,
+                         L.ofs.data(), L.m.data(), dscale == DATA_LOG ? TG_DATA_LOG : TG_DATA_LIN, J, 0, TG_MEM_HOST));
 }
 
 // Raster_Pixel(bdim, bdim, mesh): a grid of bdim points per axis over the
