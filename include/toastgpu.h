@@ -88,6 +88,13 @@ typedef struct {
 
 /* ---- mesh ---------------------------------------------------------------- */
 int tg_mesh_create(int dim, int n, const double *coords, int ne, const int *elnodes, tg_mesh *out);
+/* a mesh file in the reference's MeshData 5.0 text format (operator>> for
+   Mesh, src/libfe/mesh.cc:1787-1836): NodeList and an ElementList of 3-noded
+   triangles ('o') or 4-noded tetrahedra ('c'); later sections are ignored */
+int tg_mesh_load(const char *path, tg_mesh *out);
+/* the mesh's dimension, nodes per element and, where the pointers are not
+   NULL, its node coordinates (n x dim) and 0-based element nodes (ne x nn) */
+int tg_mesh_geometry(tg_mesh mesh, int *dim, int *nn, double *coords, int *elnodes);
 int tg_mesh_destroy(tg_mesh mesh);
 /* n, ne, nnz of the CSR pattern, number of boundary nodes, IC(0) levels
    (forward and backward sweep depth) */

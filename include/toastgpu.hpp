@@ -80,6 +80,13 @@ public:
         check(tg_mesh_info(h_, &n_, &ne_, &nnz_, nullptr, nullptr, nullptr));
         dim_ = dim;
     }
+    // operator>> for Mesh (src/libfe/mesh.cc:1787-1836) + Setup: a MeshData 5.0 file
+    explicit Mesh(const char* path)
+    {
+        check(tg_mesh_load(path, &h_));
+        check(tg_mesh_info(h_, &n_, &ne_, &nnz_, nullptr, nullptr, nullptr));
+        check(tg_mesh_geometry(h_, &dim_, nullptr, nullptr, nullptr));
+    }
     ~Mesh() { tg_mesh_destroy(h_); }
     Mesh(const Mesh&) = delete;
     Mesh& operator=(const Mesh&) = delete;

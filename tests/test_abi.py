@@ -69,3 +69,21 @@ def test_cpp_face_compiles_and_links(tmp_path):
     """include/toastgpu.hpp builds into a caller and links against the library."""
     from tests.cpp_shim import build
     assert os.path.exists(build(str(tmp_path)))
+
+
+@pytest.mark.parametrize("text,code", [
+    ("not a mesh\n", 1),                                                      # no MeshData 5.0 header
+    ("MeshData 5.0\n\nNodeList 3 1\nN[0 0]R0\nN[1 0]R0\n", 1),                # truncated node list
+    ("MeshData 5.0\n\nNodeList 3 1\nN[0 0]R0\nN[1 0]R0\nN[0 1]R0\n\nElementList 1\nq 1 2 3 4\n", 5),  # 4-noded quad
+    ("MeshData 5.0\n\nNodeList 3 1\nN[0 0]R0\nN[1 0]R0\nN[0 1]R0\n\nElementList 1\no 1 2 9\n", 1),    # index out of range
+])
+def test_mesh_file_errors_without_gpu(lib, tmp_path, text, code):
+    """tg_mesh_load parses on the host and rejects bad files before any
+    device call: missing header, truncated lists, element types other than
+    P1 triangles / tetrahedra, out-of-range node indices."""
+    p = tmp_path / "m.msh"
+    p.write_text(text)
+    h = ctypes.c_void_p()
+    lib.tg_mesh_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]
+    assert lib.tg_mesh_load(str(p).encode(), ctypes.byref(h)) == code
+    assert not h.value

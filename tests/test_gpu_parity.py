@@ -207,3 +207,21 @@ def test_source_vectors_on_device(case, neumann):
     d_out = torch.zeros((len(P.qm.Q), gm.n), dtype=torch.float64, device="cuda")
     gm.qvec_gaussian_device(P.qm.Q, P.qwidth, neumann, out=d_out)
     assert relmax(d_out.cpu().numpy(), q_host) < 1e-12
+
+
+def test_mesh_file_load(case, tmp_path):
+    """tg_mesh_load on a file in the reference's format equals the mesh built
+    from the arrays (geometry, CSR, boundary), trailing sections ignored."""
+    from toastpp_gb300 import meshio
+    P, om, gm = case
+    path = str(tmp_path / "m.msh")
+    meshio.write_mesh(path, P.coords, P.elems)
+    with open(path, "a") as f:
+        f.write("\n[ParameterList]\nSize 1\nParam1 MUA\n")
+    lm = capi.Mesh.load(path)
+    coords, el = lm.geometry()
+    assert np.array_equal(el, P.elems) and np.allclose(coords, P.coords, rtol=0, atol=1e-15 * np.abs(P.coords).max())
+    rp, ci = lm.csr()
+    rp0, ci0 = gm.csr()
+    assert np.array_equal(rp, rp0) and np.array_equal(ci, ci0)
+    assert np.array_equal(lm.boundary(), gm.boundary())

@@ -26,7 +26,7 @@ DATA_LIN, DATA_LOG = 1, 2
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
            "tg_qvec_gaussian", "tg_qvec_gaussian_ex", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream", "tg_solver_set_output_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
-           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_solver_reset_basis", "tg_jacobian_el", "tg_raster_create", "tg_raster_destroy", "tg_raster_info", "tg_raster_elref", "tg_jacobian_grid",
+           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_solver_reset_basis", "tg_jacobian_el", "tg_mesh_load", "tg_mesh_geometry", "tg_raster_create", "tg_raster_destroy", "tg_raster_info", "tg_raster_elref", "tg_jacobian_grid",
            "tg_server_create", "tg_server_destroy", "tg_submit", "tg_poll", "tg_wait", "tg_server_stats",
            "tg_server_reset_stats", "tg_last_error"]
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
@@ -91,6 +91,8 @@ def lib():
             "tg_launch_count": [C.POINTER(C.c_longlong)],
             "tg_tuner_log": [C.c_char_p, i_],
             "tg_solver_reset_basis": [vp, dp, dp, dp, d_, i_, i_],
+            "tg_mesh_load": [C.c_char_p, C.POINTER(C.c_void_p)],
+            "tg_mesh_geometry": [vp, ip, ip, vp, vp],
             "tg_jacobian_el": [vp, i_, dp, i_, dp, dp, vp, vp, i_, vp, i_, i_],
             "tg_raster_create": [vp, ip, C.POINTER(C.c_void_p)],
             "tg_raster_destroy": [vp],
@@ -152,6 +154,31 @@ class Mesh:
         v = [C.c_int() for _ in range(6)]
         _check(lib().tg_mesh_info(self._h, *[C.byref(x) for x in v]))
         self.nnz, self.nbnd, self.nlev_fwd, self.nlev_bwd = v[2].value, v[3].value, v[4].value, v[5].value
+
+    @classmethod
+    def load(cls, path):
+        """A mesh file in the reference's MeshData 5.0 format, read by the
+        library (tg_mesh_load)."""
+        h = C.c_void_p()
+        _check(lib().tg_mesh_load(os.fsencode(path), C.byref(h)))
+        self = cls.__new__(cls)
+        self._h = h
+        d, nn = C.c_int(), C.c_int()
+        _check(lib().tg_mesh_geometry(h, C.byref(d), C.byref(nn), None, None))
+        v = [C.c_int() for _ in range(6)]
+        _check(lib().tg_mesh_info(h, *[C.byref(x) for x in v]))
+        self.dim, self.n, self.ne = d.value, v[0].value, v[1].value
+        self.nnz, self.nbnd, self.nlev_fwd, self.nlev_bwd = v[2].value, v[3].value, v[4].value, v[5].value
+        return self
+
+    def geometry(self):
+        """(coords n x dim, 0-based elements ne x nn)."""
+        d, nn = C.c_int(), C.c_int()
+        _check(lib().tg_mesh_geometry(self._h, C.byref(d), C.byref(nn), None, None))
+        coords = np.zeros((self.n, d.value))
+        el = np.zeros((self.ne, nn.value), np.int32)
+        _check(lib().tg_mesh_geometry(self._h, None, None, _ptr(coords), _ptr(el)))
+        return coords, el
 
     def close(self):
         if getattr(self, "_h", None):

@@ -1707,6 +1707,94 @@ int tg_mesh_create(int dim, int n, const double* coords, int ne, const int* elno
     API_END
 }
 
+// Mesh file in the reference's text format (operator>> for Mesh,
+// src/libfe/mesh.cc:1787-1836; NodeList src/libfe/ndlist.cc:146 with nodes
+// "N[x y (z)]R0" or "B[...]..."; ElementList src/libfe/ellist.cc:154-195 with
+// lines "o i j k" (3-noded triangle) or "c i j k l" (4-noded tetrahedron),
+// 1-based).  Later sections (ParameterList, Surface) are not read.
+int tg_mesh_load(const char* path, tg_mesh* out)
+{
+    API_BEGIN
+    TG_CHECK(path && out, TG_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    FILE* f = fopen(path, "r");
+    TG_CHECK(f, TG_ERR_ARG, std::string("cannot open mesh file ") + path);
+    std::vector<char> buf;
+    {
+        char tmp[1 << 16];
+        size_t r;
+        while ((r = fread(tmp, 1, sizeof tmp, f)) > 0) buf.insert(buf.end(), tmp, tmp + r);
+        fclose(f);
+    }
+    buf.push_back('\0');
+    const char* t = buf.data();
+    const char* p = strstr(t, "MeshData 5.0");
+    TG_CHECK(p, TG_ERR_ARG, "not a MeshData 5.0 mesh file");
+    const char* nl = strstr(p, "NodeList");
+    TG_CHECK(nl, TG_ERR_ARG, "mesh file without a NodeList");
+    char* end = nullptr;
+    const long n = strtol(nl + 8, &end, 10);
+    TG_CHECK(n > 0 && n < (1L << 30), TG_ERR_ARG, "bad node count");
+    std::vector<double> coords;
+    int dim = 0;
+    const char* q = end;
+    for (long i = 0; i < n; i++) {
+        const char* lb = strchr(q, '[');
+        const char* rb = lb ? strchr(lb, ']') : nullptr;
+        TG_CHECK(lb && rb, TG_ERR_ARG, "truncated NodeList");
+        int d = 0;
+        for (const char* c = lb + 1; c < rb; d++) {
+            char* e2 = nullptr;
+            const double v = strtod(c, &e2);
+            if (e2 == c || e2 > rb) break;
+            coords.push_back(v);
+            c = e2;
+            while (c < rb && (*c == ' ' || *c == '\t')) c++;
+        }
+        if (i == 0) dim = d;
+        TG_CHECK(d == dim && (dim == 2 || dim == 3), TG_ERR_ARG, "node coordinates must be 2D or 3D throughout");
+        q = rb + 1;
+    }
+    const char* el = strstr(q, "ElementList");
+    TG_CHECK(el, TG_ERR_ARG, "mesh file without an ElementList");
+    const long ne = strtol(el + 11, &end, 10);
+    TG_CHECK(ne > 0 && ne < (1L << 30), TG_ERR_ARG, "bad element count");
+    const int nn = dim + 1;
+    std::vector<int> elems((size_t)ne * nn);
+    q = end;
+    for (long e = 0; e < ne; e++) {
+        while (*q == ' ' || *q == '\t' || *q == '\n' || *q == '\r') q++;
+        TG_CHECK(*q, TG_ERR_ARG, "truncated ElementList");
+        const char type = *q++;
+        TG_CHECK((dim == 2 && type == 'o') || (dim == 3 && type == 'c'), TG_ERR_UNSUPPORTED,
+                 "only 3-noded triangles ('o') in 2D and 4-noded tetrahedra ('c') in 3D are supported");
+        for (int k = 0; k < nn; k++) {
+            const long v = strtol(q, &end, 10);
+            TG_CHECK(end != q && v >= 1 && v <= n, TG_ERR_ARG, "element node index out of range");
+            elems[(size_t)e * nn + k] = (int)(v - 1);
+            q = end;
+        }
+        const char* eol = strchr(q, '\n');
+        q = eol ? eol + 1 : q + strlen(q);
+    }
+    auto h = std::make_unique<tg_mesh_s>();
+    h->m.reset(mesh_build(dim, (int)n, coords.data(), (int)ne, elems.data()));
+    *out = h.release();
+    API_END
+}
+
+int tg_mesh_geometry(tg_mesh mesh, int* dim, int* nn, double* coords, int* elnodes)
+{
+    API_BEGIN
+    TG_CHECK(mesh, TG_ERR_ARG, "mesh is NULL");
+    const MeshHost& h = mesh->m->h;
+    if (dim) *dim = h.dim;
+    if (nn) *nn = h.nn;
+    if (coords) std::memcpy(coords, h.coords.data(), h.coords.size() * sizeof(double));
+    if (elnodes) std::memcpy(elnodes, h.el.data(), h.el.size() * sizeof(int));
+    API_END
+}
+
 int tg_mesh_destroy(tg_mesh mesh)
 {
     API_BEGIN
