@@ -70,6 +70,8 @@ def lib():
         L.tor_a_keijzer.argtypes = [C.c_double]
         L.tor_assemble_el.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, C.c_int, _dp]
         L.tor_jacobian_el.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int, C.c_int, _dp]
+        L.tor_gradient_weights.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp]
+        L.tor_gradient_grid.argtypes = [C.c_void_p, _ip, C.c_int, _dp, _dp, _dp]
         L.tor_raster_pixel.restype = C.c_int
         L.tor_raster_pixel.argtypes = [C.c_void_p, _ip, _dp, _dp, _ip, _ip, _ip, _dp]
         L.tor_jacobian_grid.restype = C.c_int
@@ -231,6 +233,25 @@ def jacobian_el(mesh: Mesh, dphi, aphi, proj_lin, link_ofs, link_m, logscale=Tru
     lib().tor_jacobian_el(mesh._h, nq, nm, f(dphi), f(aphi), f(proj_lin), np.ascontiguousarray(link_ofs, np.int32),
                           np.ascontiguousarray(link_m, np.int32), int(cplx), int(logscale), J.reshape(-1))
     return J
+
+
+def data_gradient(mesh: Mesh, bdim, sysval, dphi, mvec, proj_lin, proj_log, link_ofs, link_m, data, sd,
+                  method="BICGSTAB", precon="ICH", tol=1e-15):
+    """toast's Gradient on Raster_Pixel(bdim, bdim) given the fields: weights,
+    one adjoint solve per source with the weighted detector vectors, then the
+    grid products (src/python/toastmodule.cc:1745-1843).  Returns 2 slen."""
+    bdim = np.ascontiguousarray(bdim, np.int32)
+    nq, n = dphi.shape
+    W = np.zeros((nq, n), np.complex128)
+    lib().tor_gradient_weights(nq, n, _cview(np.asarray(mvec, np.complex128)).ravel(), _cview(proj_lin).ravel(),
+                               _cview(proj_log).ravel(), np.ascontiguousarray(data, np.float64),
+                               np.ascontiguousarray(sd, np.float64), np.ascontiguousarray(link_ofs, np.int32),
+                               np.ascontiguousarray(link_m, np.int32), W.view(np.float64).reshape(-1))
+    wphi, _, _ = solve(mesh.rowptr, mesh.colidx, sysval, W, method, precon, tol)
+    slen = int((raster_pixel(mesh, bdim).elref >= 0).sum())
+    grad = np.zeros(2 * slen)
+    lib().tor_gradient_grid(mesh._h, bdim, nq, _cview(dphi).ravel(), _cview(wphi).ravel(), grad)
+    return grad
 
 
 @dataclass

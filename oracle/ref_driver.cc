@@ -24,6 +24,11 @@
 //              and the element-basis Jacobian (GenerateJacobian(RASTER_ELBASIS,
 //              ...), jacobian.cc:441-497; CW 738-802), PREFIX_Jel.bin; the
 //              nodal params still give c2a for the detector vectors
+// gradient   : with grid, data=D.bin and sd=S.bin (2 nQM doubles each: log
+//              amplitude then phase), also the data gradient of toast's
+//              Gradient (GetGradient / AddDataGradient,
+//              src/python/toastmodule.cc:1745-1887) on the raster, run as that
+//              code runs it with this library's calls: PREFIX_grad.bin
 // grid       : also the grid-basis Jacobian for Raster_Pixel(bdim = gdim =
 //              grid) (src/python/toastmodule.cc:696, raster_px.cc:10-48),
 //              LOG data, written with the raster's element reference per grid
@@ -89,6 +94,60 @@ static void setup_optodes(QMMesh& mesh, const string& fn) {
 
 template <class T> static const double* rawd(const TVector<T>& v) {
     return (const double*)v.data_buffer();
+}
+
+// The data gradient on a raster, in the sequence of toast's GetGradient /
+// AddDataGradient (src/python/toastmodule.cc:1745-1843), with the model data
+// from ProjectAll_real (LOG: log amplitude, phase) of the fields already
+// solved: per source, weights from the data residuals, one adjoint solve of
+// the weighted detector vectors, then the products of the two fields and of
+// their image gradients on the grid, subtracted into the gradient.
+static void ref_data_gradient(QMMesh& mesh, Raster& raster, CFwdSolver& FWS, const RVector& data, const RVector& sd,
+                              CVector* dphi, const CCompRowMatrix& mvec, RVector& grad)
+{
+    const int glen = raster.GLen(), slen = raster.SLen(), dim = raster.Dim(), nQM = mesh.nQM;
+    RVector proj = FWS.ProjectAll_real(mvec, dphi, DATA_LOG);
+    RVector gmua(grad, 0, slen), gkap(grad, slen, slen);
+    int omod = 0, oarg = nQM;
+    for (int q = 0; q < mesh.nQ; q++) {
+        CVector df(glen);
+        CVector* dg = new CVector[dim];
+        raster.Map_MeshToGrid(dphi[q], df);
+        ImageGradient(raster.GDim(), raster.GSize(), df, dg, raster.Elref());
+        const int nl = mesh.nQMref[q];
+        CVector cp = ProjectSingle(&mesh, q, mvec, dphi[q]);
+        CVector w(mesh.nlen());
+        for (int m = 0, k = 0; m < mesh.nM; m++) {
+            if (!mesh.Connected(q, m)) continue;
+            const CVector row = mvec.Row(m);
+            const double rp = cp[k].real(), ip = cp[k].imag(), dn = 1.0 / (rp * rp + ip * ip);
+            const double bm = (data[omod + k] - proj[omod + k]) / sd[omod + k];
+            const double ba = (data[oarg + k] - proj[oarg + k]) / sd[oarg + k];
+            double t = -2.0 * bm / (1.0 * sd[omod + k]);
+            w += row * std::complex<double>(t * rp * dn, -t * ip * dn);
+            t = -2.0 * ba / (1.0 * sd[oarg + k]);
+            w += row * std::complex<double>(-t * ip * dn, -t * rp * dn);
+            k++;
+        }
+        CVector wa(mesh.nlen());
+        FWS.CalcField(w, wa);
+        CVector af(glen);
+        CVector* ag = new CVector[dim];
+        raster.Map_MeshToGrid(wa, af);
+        ImageGradient(raster.GDim(), raster.GSize(), af, ag, raster.Elref());
+        CVector dgr(slen);
+        raster.Map_GridToSol(df * af, dgr);
+        gmua -= Re(dgr);
+        CVector gk(glen);
+        for (int i = 0; i < glen; i++)
+            for (int d = 0; d < dim; d++) gk[i] += dg[d][i] * ag[d][i];
+        raster.Map_GridToSol(gk, dgr);
+        gkap -= Re(dgr);
+        delete[] dg;
+        delete[] ag;
+        omod += nl;
+        oarg += nl;
+    }
 }
 
 int main(int argc, char** argv) {
@@ -261,6 +320,13 @@ int main(int argc, char** argv) {
                 wbin(out + "_Jgrid.bin", Jg.ValPtr(), (size_t)2 * nQM * 2 * slen * sizeof(double));
                 wbin(out + "_elref.bin", raster.Elref(), (size_t)glen * sizeof(int));
                 fprintf(info, "slen %d\nglen %d\n", slen, glen);
+                if (g_args.count("data")) {
+                    std::vector<char> db = rbin(arg("data", "")), sb = rbin(arg("sd", ""));
+                    RVector data(2 * nQM, (double*)db.data()), sd(2 * nQM, (double*)sb.data());
+                    RVector grad(2 * slen);
+                    ref_data_gradient(mesh, raster, FWS, data, sd, dphi, mvec, grad);
+                    wbin(out + "_grad.bin", grad.data_buffer(), (size_t)2 * slen * sizeof(double));
+                }
             }
         }
         if (want_fields) {

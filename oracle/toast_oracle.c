@@ -1542,6 +1542,75 @@ void tor_jacobian_el(const tor_mesh *m, int nq, int nm, const double *dphi, cons
         }
 }
 
+/* The data gradient of toast's Gradient (GetGradient / AddDataGradient,
+   src/python/toastmodule.cc:1745-1887), in two parts around the adjoint
+   solves.  Weights: for source q, w_q = sum over its links (in order) of
+   mvec_m * (a r dn, -a i dn) and then mvec_m * (-p i dn, -p r dn), with
+   y = r + i i the linear projection, dn = 1/|y|^2, a = -2 b_mod / sd_mod,
+   p = -2 b_arg / sd_arg, b = (data - model) / sd, model = (ln|y|, arg y).
+   data, sd: 2 nQM (log amplitude block, then phase block).  W: nq x n. */
+void tor_gradient_weights(int nq, int n, const double *mvec, const double *ylin, const double *ylog,
+                          const double *data, const double *sd, const int *link_ofs, const int *link_m, double *W)
+{
+    const int nqm = link_ofs[nq];
+    for (int q = 0; q < nq; q++) {
+        zd *w = (zd *)(W + 2 * (size_t)q * n);
+        for (int i = 0; i < n; i++) w[i] = 0.0;
+        for (int l = link_ofs[q]; l < link_ofs[q + 1]; l++) {
+            const zd *row = (const zd *)(mvec + 2 * (size_t)link_m[l] * n);
+            const double rp = ylin[2 * l], ip = ylin[2 * l + 1], dn = 1.0 / (rp * rp + ip * ip);
+            const double bm = (data[l] - ylog[2 * l]) / sd[l];
+            const double ba = (data[nqm + l] - ylog[2 * l + 1]) / sd[nqm + l];
+            double t = -2.0 * bm / (1.0 * sd[l]);
+            const zd c1 = t * rp * dn + I * (-t * ip * dn);
+            for (int i = 0; i < n; i++) w[i] += row[i] * c1;
+            t = -2.0 * ba / (1.0 * sd[nqm + l]);
+            const zd c2 = -t * ip * dn + I * (-t * rp * dn);
+            for (int i = 0; i < n; i++) w[i] += row[i] * c2;
+        }
+    }
+}
+
+/* Grid part: per source, both fields resampled on the Raster_Pixel grid
+   (basis = grid), their masked image gradients, then at the solution points
+   grad_mua -= Re(f a) and grad_kappa -= Re(sum_d grad_d f grad_d a)
+   (no voxel scaling).  dphi, wphi: nq x n complex; grad: 2 slen, in/out. */
+void tor_gradient_grid(const tor_mesh *m, const int *bdim, int nq, const double *dphi, const double *wphi,
+                       double *grad)
+{
+    const int dim = m->dim, nn = m->nn, n = m->n;
+    int glen = 1;
+    for (int d = 0; d < dim; d++) glen *= bdim[d];
+    double bbmin[3], bbmax[3], gsize[3];
+    int *elref = malloc(sizeof(int) * glen), *browptr = malloc(sizeof(int) * (glen + 1));
+    int *bcol = malloc(sizeof(int) * (size_t)glen * nn);
+    double *bval = malloc(sizeof(double) * (size_t)glen * nn);
+    tor_raster_pixel(m, bdim, bbmin, bbmax, elref, browptr, bcol, bval);
+    for (int d = 0; d < dim; d++) gsize[d] = bbmax[d] - bbmin[d];
+    int slen = 0;
+    int *sol = malloc(sizeof(int) * glen);
+    for (int i = 0; i < glen; i++) if (elref[i] >= 0) sol[slen++] = i;
+    zd *df = malloc(sizeof(zd) * glen), *af = malloc(sizeof(zd) * glen);
+    zd *dg = malloc(sizeof(zd) * (size_t)dim * glen), *ag = malloc(sizeof(zd) * (size_t)dim * glen);
+    for (int q = 0; q < nq; q++) {
+        grid_map(glen, browptr, bcol, bval, (const zd *)(dphi + 2 * (size_t)q * n), df);
+        image_gradient(dim, bdim, gsize, df, dg, elref);
+        grid_map(glen, browptr, bcol, bval, (const zd *)(wphi + 2 * (size_t)q * n), af);
+        image_gradient(dim, bdim, gsize, af, ag, elref);
+        for (int s = 0; s < slen; s++) {
+            const int g = sol[s];
+            grad[s] -= creal(df[g] * af[g]);
+        }
+        for (int s = 0; s < slen; s++) {
+            const int g = sol[s];
+            zd gk = 0.0;
+            for (int d = 0; d < dim; d++) gk += dg[(size_t)d * glen + g] * ag[(size_t)d * glen + g];
+            grad[slen + s] -= creal(gk);
+        }
+    }
+    free(elref); free(browptr); free(bcol); free(bval); free(sol); free(df); free(af); free(dg); free(ag);
+}
+
 /* A_Keijzer (param.cc:24-32) */
 double tor_a_keijzer(double n)
 {

@@ -70,6 +70,10 @@ FIXTURES = {
     "disc_fd_el": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, None, True),
     "cyl_cw_el": (lambda: small_cylinder(0.0), "CG", "ICH", 1e-15, False, None, True),
     "cyl_fd_el": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-15, False, None, True),
+    # data gradient on a raster (toast Gradient: GetGradient / AddDataGradient)
+    "disc_fd_grad": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (20, 20), False,
+                     True),
+    "cyl_fd_grad": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-15, False, (9, 9, 10), False, True),
 }
 
 
@@ -89,7 +93,17 @@ def rd(path, dtype):
     return np.fromfile(path, dtype=dtype)
 
 
-def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False):
+def synthetic_data(logproj, seed=17):
+    """Measured data for the gradient fixtures: the model's log amplitude and
+    phase perturbed by seeded noise, and their standard deviations."""
+    rng = np.random.default_rng(seed)
+    mod, arg = logproj.real, logproj.imag
+    data = np.concatenate([mod + 0.02 * rng.standard_normal(mod.size), arg + 0.01 * rng.standard_normal(arg.size)])
+    sd = np.concatenate([0.05 * np.abs(mod) + 0.01, 0.05 * np.abs(arg) + 0.01])
+    return data, sd
+
+
+def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradient=False):
     P = factory()
     cplx = P.complex
     with tempfile.TemporaryDirectory() as td:
@@ -113,6 +127,15 @@ def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False):
             epar = os.path.join(td, "elpar.bin")
             np.stack([emua, emus, eref], axis=1).astype(np.float64).tofile(epar)
             args += [f"elparams={epar}", "fields=1", "sysmat=1"]
+        if gradient:
+            # the model data first, then the run with the perturbed data
+            subprocess.run(args, check=True)
+            lp = rd(out + "_logproj.bin", np.complex128)
+            gdata, gsd = synthetic_data(lp)
+            dfile, sfile = os.path.join(td, "data.bin"), os.path.join(td, "sd.bin")
+            gdata.tofile(dfile)
+            gsd.tofile(sfile)
+            args += [f"data={dfile}", f"sd={sfile}"]
         subprocess.run(args, check=True)
         info = dict(l.split() for l in open(out + "_info.txt") if l.strip())
         ct = np.complex128 if cplx else np.float64
@@ -131,6 +154,9 @@ def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False):
             res["sysval"] = rd(out + "_sysval.bin", ct)
             res["dphi"] = rd(out + "_dphi.bin", ct).reshape(len(P.qm.Q), P.n)
             res["aphi"] = rd(out + "_aphi.bin", ct).reshape(len(P.qm.M), P.n)
+        if gradient:
+            res["data"], res["sd"] = gdata, gsd
+            res["grad"] = rd(out + "_grad.bin", np.float64)
         if grid:
             nqm = len(res["proj"])
             slen = int(info["slen"])

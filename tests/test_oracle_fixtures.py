@@ -61,3 +61,21 @@ def test_oracle_element_basis_matches_reference(oracle_mod, name):
     assert np.array_equal(val, g["sysval"])
     J = oracle_mod.jacobian_el(mesh, g["dphi"], g["aphi"], g["proj"], g["link_ofs"], g["link_m"])
     assert np.array_equal(J, g["Jel"])
+
+
+GRAD = [n for n in names() if n.endswith("_grad")]
+
+
+@pytest.mark.parametrize("name", GRAD)
+def test_oracle_data_gradient_matches_reference(oracle_mod, name):
+    """toast's Gradient (weights from the data residuals, one adjoint solve per
+    source, grid products) on the reference's fields: equal to the
+    reference's bit for bit, adjoint solves included."""
+    g = load(name)
+    m = oracle_mod.Mesh(g["coords"], g["elems"])
+    cm, ck, ca = oracle_mod.optical_coefficients(g["mua"], g["mus"], g["nref"])
+    val = m.assemble(cm, ck, ca, g["freq_mhz"] * 2 * np.pi * 1e-6, True)
+    mvec = np.stack([m.qvec_gaussian(x, g["mwidth"]) * ca for x in g["M"]]).astype(np.complex128)
+    grad = oracle_mod.data_gradient(m, g["bdim"], val, g["dphi"], mvec, g["proj"], g["logproj"], g["link_ofs"],
+                                    g["link_m"], g["data"], g["sd"], g["solver"], g["precon"], g["tol"])
+    assert np.array_equal(grad, g["grad"])
