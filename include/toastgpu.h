@@ -311,6 +311,18 @@ int tg_jacobian_grid(tg_solver s, tg_raster r, int nq, const double *dphi, int n
                      const double *proj, const int *link_ofs, const int *link_m, int scale, void *J,
                      int out_fp32, int mem);
 
+/* toast's Gradient on a raster (GetGradient / AddDataGradient,
+   src/python/toastmodule.cc:1745-1887), after tg_solver_reset of a complex
+   solver: solves the nq sources, projects (model data = ln|y|, arg y), forms
+   one adjoint source per source from the data residuals, solves those, and
+   subtracts the grid products of the two fields (and of their image
+   gradients) from grad.  data, sd: 2 nQM (log amplitude block, then phase
+   block); grad: 2 slen [mua | kappa], in/out.  res (optional): 2 nq results,
+   the forward solves then the adjoint ones. */
+int tg_gradient(tg_solver s, tg_raster r, int nq, const double *qvec, int nm, const double *mvec,
+                const int *link_ofs, const int *link_m, const double *data, const double *sd, double *grad, int mem,
+                tg_result *res);
+
 /* the SpMM autotuner's decisions so far: one text line per (mesh, value type,
    columns) with every candidate kernel's best launch time and the choice.
    The environment variable TOASTGPU_SPMM_VARIANT (spmm_halo, spmm_vec,

@@ -78,3 +78,30 @@ def test_raster_of_another_mesh_is_rejected():
     r2 = capi.Raster(other, g2["bdim"])
     with pytest.raises(capi.ToastGPUError):
         s.jacobian_grid(r2, g["dphi"], g["aphi"], g["proj"], L)
+
+
+GRAD = [n for n in names() if n.endswith("_grad")]
+
+
+@pytest.mark.parametrize("name", GRAD)
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-6)])
+def test_data_gradient_against_reference(name, precision, tol):
+    """toast's Gradient on the GPU (forward solves, projections, weighted
+    adjoint solves, grid products) against the compiled reference's.  The
+    adjoint sources weight each detector by 1/|y|^2, so the far detectors'
+    fields (|y| ~ e^-20 of the near ones) set the accuracy: the mixed path,
+    stopped at the same 1e-15 relative residual, agrees to 4e-7 on the disc."""
+    g = load(name)
+    gm = capi.Mesh(g["coords"], g["elems"])
+    r = capi.Raster(gm, g["bdim"])
+    s = capi.FwdSolver(gm, g["solver"], 1e-15, g["precon"], True, precision=precision)
+    cm, ck, ca = capi.optical_coefficients(g["mua"], g["mus"], g["nref"])
+    s.reset(cm, ck, ca, capi.omega_of(g["freq_mhz"]))
+    q = gm.qvec_gaussian(g["Q"], g["qwidth"])
+    m = gm.qvec_gaussian(g["M"], g["mwidth"]) * ca[None, :]
+    grad, res = s.gradient(r, q, m, capi.Links(g["link_ofs"], g["link_m"]), g["data"], g["sd"])
+    assert all(x[1] == 0 for x in res), res
+    assert rel2(grad, g["grad"]) < tol
+    # grad is accumulated into: a second call from the first result doubles the sum
+    grad2, _ = s.gradient(r, q, m, capi.Links(g["link_ofs"], g["link_m"]), g["data"], g["sd"], grad=grad)
+    assert rel2(grad2, 2 * grad) < 1e-12

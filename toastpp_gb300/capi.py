@@ -26,7 +26,7 @@ DATA_LIN, DATA_LOG = 1, 2
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
            "tg_qvec_gaussian", "tg_qvec_gaussian_ex", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream", "tg_solver_set_output_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
-           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_solver_reset_basis", "tg_jacobian_el", "tg_mesh_load", "tg_mesh_geometry", "tg_raster_create", "tg_raster_destroy", "tg_raster_info", "tg_raster_elref", "tg_jacobian_grid",
+           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_solver_reset_basis", "tg_jacobian_el", "tg_mesh_load", "tg_mesh_geometry", "tg_gradient", "tg_raster_create", "tg_raster_destroy", "tg_raster_info", "tg_raster_elref", "tg_jacobian_grid",
            "tg_server_create", "tg_server_destroy", "tg_submit", "tg_poll", "tg_wait", "tg_server_stats",
            "tg_server_reset_stats", "tg_last_error"]
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
@@ -92,6 +92,7 @@ def lib():
             "tg_tuner_log": [C.c_char_p, i_],
             "tg_solver_reset_basis": [vp, dp, dp, dp, d_, i_, i_],
             "tg_mesh_load": [C.c_char_p, C.POINTER(C.c_void_p)],
+            "tg_gradient": [vp, vp, i_, dp, i_, dp, vp, vp, dp, dp, dp, i_, vp],
             "tg_mesh_geometry": [vp, ip, ip, vp, vp],
             "tg_jacobian_el": [vp, i_, dp, i_, dp, dp, vp, vp, i_, vp, i_, i_],
             "tg_raster_create": [vp, ip, C.POINTER(C.c_void_p)],
@@ -308,6 +309,18 @@ class FwdSolver:
         """Reset(sol, omega, elbasis = true): one coefficient per element."""
         a = [np.ascontiguousarray(x, np.float64) for x in (cmua_el, ckap_el, c2a_el)]
         _check(lib().tg_solver_reset_basis(self._h, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), float(omega), MEM_HOST, 1))
+
+    def gradient(self, raster: "Raster", qvec, mvec, links: Links, data, sd, grad=None):
+        """toast's Gradient after reset (tg_gradient): returns (grad 2 slen,
+        per-solve results: forward then adjoint)."""
+        q = _f64(qvec, True)
+        mv = _f64(mvec, True)
+        g = np.zeros(2 * raster.slen) if grad is None else np.ascontiguousarray(grad, np.float64).copy()
+        res = (TgResult * (2 * q.shape[0]))()
+        _check(lib().tg_gradient(self._h, raster._h, q.shape[0], _ptr(q), mv.shape[0], _ptr(mv), _ptr(links.ofs),
+                                 _ptr(links.m), _ptr(np.ascontiguousarray(data, np.float64)),
+                                 _ptr(np.ascontiguousarray(sd, np.float64)), _ptr(g), MEM_HOST, res))
+        return g, [(x.it_count, x.status, x.rel_err) for x in res]
 
     def jacobian_el(self, dphi, aphi, proj, links: Links, scale=DATA_LOG, fp32=False):
         """Element-basis Jacobian (tg_jacobian_el): complex (2 nQM) x (2 ne),

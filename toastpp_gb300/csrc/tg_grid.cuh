@@ -28,17 +28,22 @@ struct GridDev {
 };
 
 // Map_MeshToGrid (raster.cc:188-199; complex: Ax_cplx, crmatrix_imp.hpp:
-// 1302-1327): gm[g * k + c] = sum_j B(g, j) x[col_j * k + c], x node-major
-// in the natural numbering; a warp per grid point, lanes over columns
+// 1302-1327): gm[g * k + c] = sum_j B(g, j) x[row(col_j) * ld + c], x
+// node-major, rows in the natural numbering (perm null) or in a layout
+// (row = perm[natural]); a warp per grid point, lanes over columns
 template <class V>
-__global__ void grid_map_kernel(GridDev G, int k, const V* __restrict__ x, V* __restrict__ gm)
+__global__ void grid_map_kernel(GridDev G, int k, const V* __restrict__ x, int ld, const int* __restrict__ perm,
+                                V* __restrict__ gm)
 {
     const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (g >= G.glen) return;
     const int j0 = G.rowptr[g], j1 = G.rowptr[g + 1];
     for (int c = lane; c < k; c += 32) {
         V acc = vzero<V>();
-        for (int j = j0; j < j1; j++) acc = vadd(acc, vscale(x[(size_t)G.col[j] * k + c], G.val[j]));
+        for (int j = j0; j < j1; j++) {
+            const int r = perm ? perm[G.col[j]] : G.col[j];
+            acc = vadd(acc, vscale(x[(size_t)r * ld + c], G.val[j]));
+        }
         gm[(size_t)g * k + c] = acc;
     }
 }
@@ -279,6 +284,65 @@ __global__ void element_jacobian_kernel(MeshDev m, int nq, int nm, int nqm, cons
             }
         }
     }
+}
+
+// The data gradient of toast's Gradient (GetGradient / AddDataGradient,
+// src/python/toastmodule.cc:1745-1887).  Per link: with y = r + i i the
+// linear projection, dn = 1/|y|^2, b = (data - model) / sd for the log
+// amplitude and the phase (model = ln|y|, arg y), a = -2 b_mod / sd_mod and
+// p = -2 b_arg / sd_arg, the detector vector enters the source's adjoint
+// right-hand side twice: times (a r dn, -a i dn), then times (-p i dn, -p r dn).
+__global__ void gradient_coef_kernel(int nqm, const cd* __restrict__ ylin, const cd* __restrict__ ylog,
+                                     const double* __restrict__ data, const double* __restrict__ sd,
+                                     cd* __restrict__ coef)
+{
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= nqm) return;
+    const double rp = ylin[l].x, ip = ylin[l].y, dn = 1.0 / (rp * rp + ip * ip);
+    const double bm = (data[l] - ylog[l].x) / sd[l];
+    const double ba = (data[nqm + l] - ylog[l].y) / sd[nqm + l];
+    double t = -2.0 * bm / (1.0 * sd[l]);
+    coef[2 * l] = cd{t * rp * dn, -t * ip * dn};
+    t = -2.0 * ba / (1.0 * sd[nqm + l]);
+    coef[2 * l + 1] = cd{-t * ip * dn, -t * rp * dn};
+}
+
+// adjoint right-hand sides w_q = sum over q's links (in order) of
+// mvec_m coef1 + mvec_m coef2, written node-major in the solver's layout
+__global__ void gradient_weights_kernel(int n, int nq, const cd* __restrict__ mvec, const int* __restrict__ link_ofs,
+                                        const int* __restrict__ link_m, const cd* __restrict__ coef,
+                                        const int* __restrict__ perm, cd* __restrict__ W)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, q = blockIdx.y;
+    if (i >= n || q >= nq) return;
+    cd w = cd{0.0, 0.0};
+    for (int l = link_ofs[q]; l < link_ofs[q + 1]; l++) {
+        const cd r = mvec[(size_t)link_m[l] * n + i];
+        w = vadd(w, vmul(r, coef[2 * l]));
+        w = vadd(w, vmul(r, coef[2 * l + 1]));
+    }
+    W[(size_t)perm[i] * nq + q] = w;
+}
+
+// grad_mua[s] -= Re(f a), grad_kappa[s] -= Re(sum_d grad_d f grad_d a),
+// summed over the sources in order (no voxel scaling); grad in/out
+__global__ void gradient_accum_kernel(int dim, int slen, int nq, const cd* __restrict__ Pf, const cd* __restrict__ Pa,
+                                      double* __restrict__ grad)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= slen) return;
+    const int np = 1 + dim;
+    double gm = grad[s], gk = grad[slen + s];
+    for (int q = 0; q < nq; q++) {
+        const cd* f = Pf + (size_t)q * np * slen + s;
+        const cd* a = Pa + (size_t)q * np * slen + s;
+        gm -= re(vmul(f[0], a[0]));
+        cd k = cd{0.0, 0.0};
+        for (int d = 1; d < np; d++) k = vadd(k, vmul(f[(size_t)d * slen], a[(size_t)d * slen]));
+        gk -= re(k);
+    }
+    grad[s] = gm;
+    grad[slen + s] = gk;
 }
 
 // QVec_Gaussian (src/libstoast/source.cc:19-56) for npos positions on the

@@ -971,6 +971,7 @@ struct tg_solver_s {
     DBuf B, X, X32, B32, cs_outer, cs_inner, io_a, io_b, tmp, jout;
     DBuf jF, jG, jpair, jyinv, plink_q, plink_m, psup, pnsup, pflag, pMsup, plin, plog;
     DBuf gplanes_q, gplanes_m, gy, io_c;  // grid-basis Jacobian: field planes, 1/y, grid fields
+    DBuf gdata, gsd, ggrad, gofs, glm;    // data gradient: data, sd, gradient, link lists
     DBuf fp_bq, fp_xq, fp_bm, fp_xm, fp_lin, fp_log;
     DBuf jwm64, jwk64, jwm32, jwk32;  // per-node element weights of the Jacobian (geometry only)
     DBuf rel_cnt, rel_idx, rel_xc, rel_ac;
@@ -1520,7 +1521,8 @@ static void grid_jac_run(tg_solver s, const tg_raster_s& r, int nq, const V64* F
         launch(to_nodemajor_kernel<V64, V64>, dim3(cdiv_u(n, 32), cdiv_u(k, 32)), dim3(32, 8), 0, s->stream, n, k, k,
                src, xn, (const int*)nullptr);
         V64* gm = (V64*)s->io_c.ensure((size_t)r.glen * k * sizeof(V64));
-        launch(grid_map_kernel<V64>, cdiv_u((size_t)r.glen * 32, 256), 256, 0, s->stream, G, k, (const V64*)xn, gm);
+        launch(grid_map_kernel<V64>, cdiv_u((size_t)r.glen * 32, 256), 256, 0, s->stream, G, k, (const V64*)xn, k,
+               (const int*)nullptr, gm);
         launch(grid_planes_kernel<V64, C>, dim3(cdiv_u(r.slen, 32), cdiv_u(k, 32)), dim3(32, 8), 0, s->stream, G, k,
                (const V64*)gm, masked, P);
     };
@@ -1606,6 +1608,72 @@ static void api_jacobian_el(tg_solver s, int nq, const double* dphi, int nm, con
     if (out_fp32) element_jac_run<V64, V32>(s, nq, F, nm, A, yl, L, scale == TG_DATA_LOG, Jd);
     else element_jac_run<V64, V64>(s, nq, F, nm, A, yl, L, scale == TG_DATA_LOG, Jd);
     if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(J, Jd, jbytes, cudaMemcpyDeviceToHost, s->stream));
+    TG_CUDA(cudaGetLastError());
+    TG_CUDA(cudaStreamSynchronize(s->stream));
+}
+
+// toast's Gradient on a raster (GetGradient / AddDataGradient,
+// src/python/toastmodule.cc:1745-1887) after Reset: forward solves of the
+// sources, projections, the adjoint right-hand sides weighted by the data
+// residuals, their solves, then the grid products summed over the sources
+static void api_gradient(tg_solver s, const tg_raster_s& r, int nq, const double* qvec, int nm, const double* mvec,
+                         const LinkHost& L, const double* data, const double* sd, double* grad, int mem,
+                         tg_result* res)
+{
+    const MeshDev& m = s->mesh->d;
+    const int n = m.n, nqm = (int)L.q.size(), np = 1 + r.dim;
+    const size_t kb = (size_t)nq * n * sizeof(cd);
+    const cd* Qs = (const cd*)dev_in(s, qvec, kb, mem, s->io_a);
+    const cd* Mv = (const cd*)dev_in(s, mvec, (size_t)nm * n * sizeof(cd), mem, s->io_b);
+    const double* dd = (const double*)dev_in(s, data, (size_t)2 * nqm * sizeof(double), mem, s->gdata);
+    const double* ds = (const double*)dev_in(s, sd, (size_t)2 * nqm * sizeof(double), mem, s->gsd);
+    double* dg = (double*)dev_in(s, grad, (size_t)2 * r.slen * sizeof(double), mem, s->ggrad);
+    // forward fields
+    cd* B = (cd*)s->fp_bq.ensure(kb);
+    cd* X = (cd*)s->fp_xq.ensure(kb);
+    src_to_nm(s, n, nq, Qs, B);
+    TG_CUDA(cudaMemsetAsync(X, 0, kb, s->stream));
+    ColState* co = (ColState*)s->cs_outer.ensure(sizeof(ColState) * nq);
+    solve_nm<cd, cf>(s, nq, B, X, co, true);
+    if (res) read_results(s, nq, co, res);
+    // linear and log projections of the model
+    cd* yl = (cd*)s->fp_lin.ensure((size_t)std::max(nqm, 1) * sizeof(cd));
+    cd* yg = (cd*)s->fp_log.ensure((size_t)std::max(nqm, 1) * sizeof(cd));
+    project_nm<cd>(s, X, nq, nm, Mv, L, yl, yg);
+    // weighted adjoint sources and their solves
+    cd* coef = (cd*)s->gy.ensure((size_t)2 * std::max(nqm, 1) * sizeof(cd));
+    launch(gradient_coef_kernel, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, (const cd*)yl, (const cd*)yg, dd, ds, coef);
+    std::vector<int> ofs(nq + 1, 0);
+    for (int l = 0; l < nqm; l++) ofs[L.q[l] + 1]++;
+    for (int q = 0; q < nq; q++) ofs[q + 1] += ofs[q];
+    int* lo = (int*)s->gofs.ensure((size_t)(nq + 1) * sizeof(int));
+    int* lm = (int*)s->glm.ensure((size_t)std::max(nqm, 1) * sizeof(int));
+    TG_CUDA(cudaMemcpyAsync(lo, ofs.data(), (size_t)(nq + 1) * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    TG_CUDA(cudaMemcpyAsync(lm, L.m.data(), (size_t)nqm * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    cd* W = (cd*)s->fp_bm.ensure(kb);
+    cd* Y = (cd*)s->fp_xm.ensure(kb);
+    launch(gradient_weights_kernel, dim3(cdiv_u(n, 128), nq), 128, 0, s->stream, n, nq, Mv, (const int*)lo,
+           (const int*)lm, (const cd*)coef, m.perm, W);
+    TG_CUDA(cudaMemsetAsync(Y, 0, kb, s->stream));
+    solve_nm<cd, cf>(s, nq, W, Y, co, true);
+    if (res) read_results(s, nq, co, res + nq);
+    // both fields on the grid with their gradients, then the sums
+    const GridDev G = r.dev();
+    cd* Pf = (cd*)s->gplanes_q.ensure((size_t)nq * np * r.slen * sizeof(cd));
+    cd* Pa = (cd*)s->gplanes_m.ensure((size_t)nq * np * r.slen * sizeof(cd));
+    auto planes = [&](const cd* x, cd* P) {
+        cd* gm = (cd*)s->io_c.ensure((size_t)r.glen * nq * sizeof(cd));
+        launch(grid_map_kernel<cd>, cdiv_u((size_t)r.glen * 32, 256), 256, 0, s->stream, G, nq, x, nq,
+               (const int*)m.perm, gm);
+        launch(grid_planes_kernel<cd, cd>, dim3(cdiv_u(r.slen, 32), cdiv_u(nq, 32)), dim3(32, 8), 0, s->stream, G, nq,
+               (const cd*)gm, 1, P);
+    };
+    planes(X, Pf);
+    planes(Y, Pa);
+    launch(gradient_accum_kernel, cdiv_u(r.slen, 256), 256, 0, s->stream, r.dim, r.slen, nq, (const cd*)Pf,
+           (const cd*)Pa, dg);
+    if (mem != TG_MEM_DEVICE)
+        TG_CUDA(cudaMemcpyAsync(grad, dg, (size_t)2 * r.slen * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     TG_CUDA(cudaGetLastError());
     TG_CUDA(cudaStreamSynchronize(s->stream));
 }
@@ -2115,6 +2183,23 @@ int tg_jacobian_grid(tg_solver s, tg_raster r, int nq, const double* dphi, int n
     if (L.q.empty() || r->slen == 0) return TG_OK;
     if (s->cplx) api_jacobian_grid<cd, cf>(s, *r, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
     else api_jacobian_grid<double, float>(s, *r, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
+    API_END
+}
+
+int tg_gradient(tg_solver s, tg_raster r, int nq, const double* qvec, int nm, const double* mvec,
+                const int* link_ofs, const int* link_m, const double* data, const double* sd, double* grad, int mem,
+                tg_result* res)
+{
+    API_BEGIN
+    TG_CHECK(s && r && qvec && mvec && link_ofs && data && sd && grad, TG_ERR_ARG, "NULL argument");
+    TG_CHECK(s->cplx, TG_ERR_UNSUPPORTED, "the data gradient is defined for frequency-domain (complex) solvers");
+    TG_CHECK(s->reset_done, TG_ERR_STATE, "tg_gradient before tg_solver_reset");
+    TG_CHECK(r->mesh == s->mesh, TG_ERR_ARG, "the raster was built on another mesh");
+    TG_CHECK(nq > 0 && nm > 0 && nq <= 65535, TG_ERR_ARG, "source / detector count out of range");
+    std::lock_guard<std::mutex> g(s->mu);
+    LinkHost L = make_links(nq, nm, link_ofs, link_m);
+    if (L.q.empty() || r->slen == 0) return TG_OK;
+    api_gradient(s, *r, nq, qvec, nm, mvec, L, data, sd, grad, mem, res);
     API_END
 }
 
