@@ -117,7 +117,9 @@ int tg_solver_create(tg_mesh mesh, int is_complex, int method, int precon, doubl
 int tg_solver_destroy(tg_solver s);
 int tg_solver_set(tg_solver s, double tol, int maxit);
 /* mixed precision only: relative tolerance of each FP32 inner solve (default
-   1e-4), the maximum number of FP64 refinement steps (default 12) and the
+   1e-4, at least 1e-5: an FP32 recursion does not hold more digits between
+   residual replacements), the maximum number of FP64 refinement steps
+   (default 12) and the
    elimination ordering of the inner IC(0) preconditioner: 1 (default) a
    colour-major ordering of a greedy colouring, whose colour classes are the
    levels of the triangular sweeps, or 0 the natural ordering of the reference.

@@ -87,3 +87,4 @@ def test_mesh_file_errors_without_gpu(lib, tmp_path, text, code):
     lib.tg_mesh_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]
     assert lib.tg_mesh_load(str(p).encode(), ctypes.byref(h)) == code
     assert not h.value
+

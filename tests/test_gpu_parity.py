@@ -225,3 +225,13 @@ def test_mesh_file_load(case, tmp_path):
     rp0, ci0 = gm.csr()
     assert np.array_equal(rp, rp0) and np.array_equal(ci, ci0)
     assert np.array_equal(lm.boundary(), gm.boundary())
+
+
+def test_inner_tolerance_bound(case):
+    """The mixed path refuses inner tolerances below 1e-5, where its FP32
+    process stagnates or diverges, and accepts the bound itself."""
+    P, om, gm = case
+    s = capi.FwdSolver(gm, "BICGSTAB" if P.complex else "CG", 1e-12, "ICH", P.complex, precision="mixed")
+    with pytest.raises(capi.ToastGPUError):
+        s.set_refinement(1e-6)
+    s.set_refinement(1e-5)

@@ -2241,8 +2241,11 @@ int tg_forward_path(tg_solver s, const double* cmua, const double* ckappa, const
 int tg_solver_set_refinement(tg_solver s, double inner_tol, int max_outer, int inner_ordering)
 {
     API_BEGIN
-    TG_CHECK(s && inner_tol > 0 && inner_tol < 1 && max_outer > 0 && (inner_ordering == 0 || inner_ordering == 1),
-             TG_ERR_ARG, "invalid argument");
+    TG_CHECK(s && inner_tol < 1 && max_outer > 0 && (inner_ordering == 0 || inner_ordering == 1), TG_ERR_ARG,
+             "invalid argument");
+    // an FP32 recursion cannot be trusted for more than about five digits
+    // between residual replacements: at 1e-6 it stagnates or diverges
+    TG_CHECK(inner_tol >= 1e-5, TG_ERR_ARG, "inner_tol below 1e-5 asks more of the FP32 process than it holds");
     s->inner_tol = inner_tol;
     s->max_outer = max_outer;
     s->inner_colour = inner_ordering;
