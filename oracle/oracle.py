@@ -72,6 +72,7 @@ def lib():
         L.tor_jacobian_el.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int, C.c_int, _dp]
         L.tor_gradient_weights.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp]
         L.tor_gradient_grid.argtypes = [C.c_void_p, _ip, C.c_int, _dp, _dp, _dp]
+        L.tor_node_map.argtypes = [C.c_void_p, _ip, _dp, _dp, _ip, _ip, _ip, _dp]
         L.tor_raster_pixel.restype = C.c_int
         L.tor_raster_pixel.argtypes = [C.c_void_p, _ip, _dp, _dp, _ip, _ip, _ip, _dp]
         L.tor_jacobian_grid.restype = C.c_int
@@ -283,6 +284,38 @@ def raster_pixel(mesh: Mesh, bdim) -> RasterPixel:
     val = np.zeros(glen * nn)
     lib().tor_raster_pixel(mesh._h, bdim, bbmin, bbmax, elref, rp, col, val)
     return RasterPixel(bdim, bbmin, bbmax, elref, rp, col[:rp[-1]].copy(), val[:rp[-1]].copy())
+
+
+def _csr_apply(rp, col, val, x):
+    """y = A x row by row in entry order from 0 (RCompRowMatrix::Ax)."""
+    y = np.zeros(len(rp) - 1)
+    for r in range(len(rp) - 1):
+        acc = 0.0
+        for j in range(rp[r], rp[r + 1]):
+            acc += float(val[j]) * float(x[col[j]])
+        y[r] = acc
+    return y
+
+
+def raster_maps(mesh: Mesh, bdim, f_mesh, s_sol):
+    """The pixel raster's basis maps (toast.Raster.Map): mesh -> grid (B),
+    mesh -> solution (B then the support), solution -> mesh (scatter to the
+    grid, then NodeMapMatrix BI), grid -> mesh (BI) of the grid image of
+    f_mesh.  Returns (m2g, m2s, s2m, g2m)."""
+    r = raster_pixel(mesh, bdim)
+    glen = len(r.elref)
+    nn = 1 << mesh.dim
+    rp = np.zeros(mesh.n + 1, np.int32)
+    col = np.zeros(mesh.n * nn, np.int32)
+    val = np.zeros(mesh.n * nn)
+    lib().tor_node_map(mesh._h, np.ascontiguousarray(bdim, np.int32), r.bbmin, r.bbmax, r.elref, rp, col, val)
+    m2g = _csr_apply(r.browptr, r.bcol, r.bval, f_mesh)
+    m2s = m2g[r.sol]
+    g = np.zeros(glen)
+    g[r.sol] = s_sol
+    s2m = _csr_apply(rp, col, val, g)
+    g2m = _csr_apply(rp, col, val, m2g)
+    return m2g, m2s, s2m, g2m
 
 
 def jacobian_grid(mesh: Mesh, bdim, dphi, aphi, proj_lin, link_ofs, link_m, logscale=True):

@@ -96,6 +96,26 @@ template <class T> static const double* rawd(const TVector<T>& v) {
     return (const double*)v.data_buffer();
 }
 
+// The raster's basis maps (toast.Raster.Map, src/python/toastmodule.cc:
+// 718-790) of a nodal field (mua) and of a solution-basis vector (s + 1 at
+// solution point s): PREFIX_m2g.bin (mesh -> grid), _m2s.bin (mesh ->
+// solution), _s2m.bin (solution -> mesh), _g2m.bin (grid -> mesh, the grid
+// vector being the mesh -> grid map of mua)
+static void write_maps(Raster& raster, const RVector& mua, const string& out)
+{
+    const int glen = raster.GLen(), slen = raster.SLen(), n = mua.Dim();
+    RVector g(glen), sv(slen), m(n), sin(slen);
+    raster.Map_MeshToGrid(mua, g);
+    wbin(out + "_m2g.bin", g.data_buffer(), glen * sizeof(double));
+    raster.Map_MeshToSol(mua, sv);
+    wbin(out + "_m2s.bin", sv.data_buffer(), slen * sizeof(double));
+    for (int i = 0; i < slen; i++) sin[i] = i + 1.0;
+    raster.Map_SolToMesh(sin, m);
+    wbin(out + "_s2m.bin", m.data_buffer(), n * sizeof(double));
+    raster.Map_GridToMesh(g, m);
+    wbin(out + "_g2m.bin", m.data_buffer(), n * sizeof(double));
+}
+
 // The data gradient on a raster, in the sequence of toast's GetGradient /
 // AddDataGradient (src/python/toastmodule.cc:1745-1843), with the model data
 // from ProjectAll_real (LOG: log amplitude, phase) of the fields already
@@ -320,6 +340,7 @@ int main(int argc, char** argv) {
                 wbin(out + "_Jgrid.bin", Jg.ValPtr(), (size_t)2 * nQM * 2 * slen * sizeof(double));
                 wbin(out + "_elref.bin", raster.Elref(), (size_t)glen * sizeof(int));
                 fprintf(info, "slen %d\nglen %d\n", slen, glen);
+                write_maps(raster, mua, out);
                 if (g_args.count("data")) {
                     std::vector<char> db = rbin(arg("data", "")), sb = rbin(arg("sd", ""));
                     RVector data(2 * nQM, (double*)db.data()), sd(2 * nQM, (double*)sb.data());
@@ -409,6 +430,7 @@ int main(int argc, char** argv) {
                 fclose(f);
                 wbin(out + "_elref.bin", raster.Elref(), (size_t)glen * sizeof(int));
                 fprintf(info, "slen %d\nglen %d\n", slen, glen);
+                write_maps(raster, mua, out);
             }
         }
         if (want_fields) {

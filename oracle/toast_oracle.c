@@ -1361,6 +1361,61 @@ int tor_raster_pixel(const tor_mesh *m, const int *bdim, double *bbmin, double *
     return glen;
 }
 
+/* NodeMapMatrix (mesh.cc:2695-2852): per mesh node, the bilinear /
+   trilinear weights of the grid points around it, only those inside the
+   mesh (elref >= 0), renormalised when some are missing (equal weights when
+   their sum is below 1e-8); a node outside the box has no entries.  Zero
+   weights are dropped (Shrink).  browptr: n+1, bcol / bval: n*2^dim. */
+void tor_node_map(const tor_mesh *m, const int *bdim, const double *bbmin, const double *bbmax, const int *elref,
+                  int *browptr, int *bcol, double *bval)
+{
+    const int dim = m->dim, nx = bdim[0], ny = bdim[1];
+    double dW[3];
+    for (int d = 0; d < dim; d++) dW[d] = (bbmax[d] - bbmin[d]) / (double)(bdim[d] - 1);
+    int idx = 0;
+    browptr[0] = 0;
+    for (int k = 0; k < m->n; k++) {
+        const double *p = m->x + (size_t)k * dim;
+        int i0[3] = {0, 0, 0}, inside = 1;
+        double d0[3] = {0, 0, 0};
+        for (int d = 0; d < dim; d++) {
+            if (!(p[d] >= bbmin[d] && p[d] <= bbmax[d])) { inside = 0; break; }
+            i0[d] = (int)((p[d] - bbmin[d]) / dW[d]);
+            if (i0[d] < 0) i0[d] = 0;
+            else if (i0[d] >= bdim[d] - 1) i0[d] = bdim[d] - 2;
+            d0[d] = (p[d] - (i0[d] * dW[d] + bbmin[d])) / dW[d];
+            if (d0[d] < 0.0) d0[d] = 0.0;
+            else if (d0[d] > 1.0) d0[d] = 1.0;
+        }
+        if (inside) {
+            const int idx0 = idx, ncorner = dim == 2 ? 4 : 8;
+            for (int c = 0; c < ncorner; c++) {
+                const int cx = c & 1, cy = (c >> 1) & 1, cz = (c >> 2) & 1;
+                const int pix = (i0[0] + cx) + nx * ((i0[1] + cy) + ny * (dim > 2 ? i0[2] + cz : 0));
+                if (elref[pix] < 0) continue;
+                double w = (cx ? d0[0] : 1.0 - d0[0]) * (cy ? d0[1] : 1.0 - d0[1]);
+                if (dim > 2) w *= cz ? d0[2] : 1.0 - d0[2];
+                bcol[idx] = pix;
+                bval[idx++] = w;
+            }
+            if (idx > idx0 && idx - idx0 < ncorner) {
+                double wsum = 0.0;
+                for (int i = idx0; i < idx; i++) wsum += bval[i];
+                if (wsum > 1e-8)
+                    for (int i = idx0; i < idx; i++) bval[i] /= wsum;
+                else
+                    for (int i = idx0; i < idx; i++) bval[i] = 1.0 / (double)(idx - idx0);
+            }
+            /* Shrink: drop zero weights, keeping the order */
+            int o = idx0;
+            for (int i = idx0; i < idx; i++)
+                if (bval[i] != 0.0) { bcol[o] = bcol[i]; bval[o++] = bval[i]; }
+            idx = o;
+        }
+        browptr[k + 1] = idx;
+    }
+}
+
 /* ImageGradient (jacobian.cc:944-1060): central differences where both
    neighbours are in the mask, one-sided where one is, 0 outside the mask;
    spacing gsize/n (sic: n, not n-1).  mask NULL: every point counts as

@@ -162,6 +162,8 @@ def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradi
             slen = int(info["slen"])
             Jg = rd(out + "_Jgrid.bin", np.float64)
             res["Jgrid"] = Jg.reshape((2 * nqm, 2 * slen) if cplx else (2 * nqm, slen))
+            for key in ("m2g", "m2s", "s2m", "g2m"):
+                res["map_" + key] = rd(out + f"_{key}.bin", np.float64)
             res["elref"] = rd(out + "_elref.bin", np.int32)
             res["bdim"] = np.array(grid, np.int32)
             res["dphi"] = rd(out + "_dphi.bin", ct).reshape(len(P.qm.Q), P.n)

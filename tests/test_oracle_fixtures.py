@@ -79,3 +79,16 @@ def test_oracle_data_gradient_matches_reference(oracle_mod, name):
     grad = oracle_mod.data_gradient(m, g["bdim"], val, g["dphi"], mvec, g["proj"], g["logproj"], g["link_ofs"],
                                     g["link_m"], g["data"], g["sd"], g["solver"], g["precon"], g["tol"])
     assert np.array_equal(grad, g["grad"])
+
+
+@pytest.mark.parametrize("name", GRID)
+def test_oracle_raster_maps_match_reference(oracle_mod, name):
+    """The pixel raster's basis maps (mesh -> grid, mesh -> solution,
+    solution -> mesh through NodeMapMatrix, grid -> mesh) equal the
+    reference's bit for bit."""
+    g = load(name)
+    mesh = oracle_mod.Mesh(g["coords"], g["elems"])
+    slen = int((g["elref"] >= 0).sum())
+    maps = oracle_mod.raster_maps(mesh, g["bdim"], g["mua"], np.arange(1, slen + 1, dtype=float))
+    for a, key in zip(maps, ("m2g", "m2s", "s2m", "g2m")):
+        assert np.array_equal(a, g["map_" + key]), key
