@@ -302,6 +302,12 @@ int tg_raster_destroy(tg_raster r);
 int tg_raster_info(tg_raster r, int *glen, int *slen, double *bbmin, double *bbmax);
 /* element containing each grid point, -1 outside (Raster::Elref) */
 int tg_raster_elref(tg_raster r, int *elref);
+/* toast.Raster.Map (MapBasis, src/python/toastmodule.cc:718-790): map is
+   "X->Y" with X, Y among M (mesh nodes), G (grid), B (basis, = G here), S
+   (solution points); nvec vectors back to back, width doubles per point
+   (1 real, 2 complex interleaved); src, dst in host or device memory.  Sums
+   in the reference's order without fused multiply-adds (bit-identical). */
+int tg_raster_map(tg_raster r, const char *map, int nvec, const double *src, double *dst, int width, int mem);
 /* Grid-basis Jacobian (GenerateJacobian with a raster, jacobian.cc:105-123
    -> GenerateJacobian_grid 289-373; real systems GenerateJacobian_cw with a
    raster, 178-193 -> GenerateJacobian_cw_grid 610-712).  Inputs as

@@ -105,3 +105,23 @@ def test_data_gradient_against_reference(name, precision, tol):
     # grad is accumulated into: a second call from the first result doubles the sum
     grad2, _ = s.gradient(r, q, m, capi.Links(g["link_ofs"], g["link_m"]), g["data"], g["sd"], grad=grad)
     assert rel2(grad2, 2 * grad) < 1e-12
+
+
+@pytest.mark.parametrize("name", GRID)
+def test_raster_maps_match_reference(name):
+    """tg_raster_map: mesh -> grid, mesh -> solution, solution -> mesh and
+    grid -> mesh equal the reference's maps bit for bit; complex vectors map
+    component by component; stacks map row by row."""
+    g, gm, r, s, L = setup(name)
+    sin = np.arange(1, r.slen + 1, dtype=float)
+    m2g = r.map("M->G", g["mua"])
+    assert np.array_equal(m2g, g["map_m2g"])
+    assert np.array_equal(r.map("M->S", g["mua"]), g["map_m2s"])
+    assert np.array_equal(r.map("S->M", sin), g["map_s2m"])
+    assert np.array_equal(r.map("G->M", m2g), g["map_g2m"])
+    assert np.array_equal(r.map("G->S", m2g), g["map_m2s"])
+    assert np.array_equal(r.map("S->G", r.map("G->S", m2g))[g["elref"] >= 0], m2g[g["elref"] >= 0])
+    z = r.map("M->S", g["mua"] + 2j * g["mua"])
+    assert np.array_equal(z.real, g["map_m2s"]) and np.array_equal(z.imag, 2 * g["map_m2s"])
+    st = r.map("S->M", np.stack([sin, 3 * sin]))
+    assert np.array_equal(st[0], g["map_s2m"]) and np.array_equal(st[1], r.map("S->M", 3 * sin))

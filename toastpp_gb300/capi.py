@@ -26,7 +26,7 @@ DATA_LIN, DATA_LOG = 1, 2
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
            "tg_qvec_gaussian", "tg_qvec_gaussian_ex", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream", "tg_solver_set_output_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
-           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_solver_reset_basis", "tg_jacobian_el", "tg_mesh_load", "tg_mesh_geometry", "tg_gradient", "tg_raster_create", "tg_raster_destroy", "tg_raster_info", "tg_raster_elref", "tg_jacobian_grid",
+           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_solver_reset_basis", "tg_jacobian_el", "tg_mesh_load", "tg_mesh_geometry", "tg_gradient", "tg_raster_create", "tg_raster_destroy", "tg_raster_map", "tg_raster_info", "tg_raster_elref", "tg_jacobian_grid",
            "tg_server_create", "tg_server_destroy", "tg_submit", "tg_poll", "tg_wait", "tg_server_stats",
            "tg_server_reset_stats", "tg_last_error"]
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
@@ -99,6 +99,7 @@ def lib():
             "tg_raster_destroy": [vp],
             "tg_raster_info": [vp, ip, ip, dp, dp],
             "tg_raster_elref": [vp, ip],
+            "tg_raster_map": [vp, C.c_char_p, i_, vp, vp, i_, i_],
             "tg_jacobian_grid": [vp, vp, i_, dp, i_, dp, dp, vp, vp, i_, vp, i_, i_],
             "tg_server_create": [i_, d_, C.POINTER(C.c_void_p)],
             "tg_server_destroy": [vp],
@@ -454,6 +455,18 @@ class Raster:
         _check(lib().tg_raster_info(self._h, C.byref(gl), C.byref(sl), self.bbmin.ctypes.data_as(C.POINTER(C.c_double)),
                                     self.bbmax.ctypes.data_as(C.POINTER(C.c_double))))
         self.glen, self.slen = gl.value, sl.value
+
+    def map(self, kind, x):
+        """toast.Raster.Map: kind "M->S", "S->M", "M->G", "G->M", "G->S", "S->G"
+        (B = G); x one vector or a stack (rows), real or complex."""
+        x = np.asarray(x)
+        cplx = np.iscomplexobj(x)
+        xs = np.ascontiguousarray(np.atleast_2d(x), np.complex128 if cplx else np.float64)
+        sizes = {"M": self.mesh.n, "G": self.glen, "B": self.glen, "S": self.slen}
+        out = np.zeros((xs.shape[0], sizes[kind[3]]), xs.dtype)
+        _check(lib().tg_raster_map(self._h, kind.encode(), xs.shape[0], _ptr(xs), _ptr(out), 2 if cplx else 1,
+                                   MEM_HOST))
+        return out[0] if x.ndim == 1 else out
 
     def elref(self):
         out = np.zeros(self.glen, np.int32)

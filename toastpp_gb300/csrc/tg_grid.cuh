@@ -345,6 +345,43 @@ __global__ void gradient_accum_kernel(int dim, int slen, int nq, const cd* __res
     grad[slen + s] = gk;
 }
 
+// Raster basis maps: y = A x row by row in entry order (RCompRowMatrix::Ax,
+// crmatrix_imp.hpp:1168-1189; complex vectors component by component,
+// Ax_cplx 1302-1327), one thread per (row, vector), `width` doubles per point
+__global__ void csr_apply_kernel(int rows, int cols, int width, const int* __restrict__ rp,
+                                 const int* __restrict__ col, const double* __restrict__ val,
+                                 const double* __restrict__ x, double* __restrict__ y)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y;
+    if (r >= rows) return;
+    const double* xv = x + (size_t)v * cols * width;
+    for (int c = 0; c < width; c++) {
+        double acc = 0.0;
+        for (int j = rp[r]; j < rp[r + 1]; j++) acc = __dadd_rn(acc, __dmul_rn(val[j], xv[(size_t)col[j] * width + c]));
+        y[((size_t)v * rows + r) * width + c] = acc;
+    }
+}
+
+// grid -> solution points (Map_BasisToSol, raster.cc:292-315)
+__global__ void gather_points_kernel(int slen, int glen, int width, const int* __restrict__ sol,
+                                     const double* __restrict__ g, double* __restrict__ s)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y;
+    if (i >= slen) return;
+    for (int c = 0; c < width; c++)
+        s[((size_t)v * slen + i) * width + c] = g[((size_t)v * glen + sol[i]) * width + c];
+}
+
+// solution points -> grid, zeros elsewhere (Map_SolToBasis, raster.cc:318-345)
+__global__ void scatter_points_kernel(int slen, int glen, int width, const int* __restrict__ sol,
+                                      const double* __restrict__ s, double* __restrict__ g)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y;
+    if (i >= slen) return;
+    for (int c = 0; c < width; c++)
+        g[((size_t)v * glen + sol[i]) * width + c] = s[((size_t)v * slen + i) * width + c];
+}
+
 // QVec_Gaussian (src/libstoast/source.cc:19-56) for npos positions on the
 // device: a thread per (node, position) gathers the contributions the
 // reference scatters, in the reference's order (elements ascending, then the

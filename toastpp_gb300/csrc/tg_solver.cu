@@ -792,7 +792,9 @@ struct tg_raster_s {
     double bbmin[3] = {0, 0, 0}, bbmax[3] = {0, 0, 0};
     std::vector<int> elref, sol, rowptr, col;  // col: natural node numbers
     std::vector<double> val;
-    DBuf d_elref, d_sol, d_rowptr, d_col, d_val;
+    std::vector<int> nrowptr, ncol;              // NodeMapMatrix: grid -> mesh nodes
+    std::vector<double> nval;
+    DBuf d_elref, d_sol, d_rowptr, d_col, d_val, d_nrowptr, d_ncol, d_nval, d_src, d_dst, d_tmp;
     GridDev dev() const
     {
         GridDev G;
@@ -933,6 +935,54 @@ void raster_build(const MeshHost& m, tg_raster_s& r)
         }
     }
     r.slen = (int)r.sol.size();
+    // NodeMapMatrix (mesh.cc:2695-2852): per node the bilinear / trilinear
+    // weights of the grid points around it that lie in the mesh,
+    // renormalised when some are missing (equal weights below 1e-8); zero
+    // weights dropped (Shrink); no entries for a node outside the box
+    r.nrowptr.assign(m.n + 1, 0);
+    r.ncol.clear();
+    r.nval.clear();
+    for (int k = 0; k < m.n; k++) {
+        const double* p = &m.coords[(size_t)k * dim];
+        int i0[3] = {0, 0, 0};
+        double d0[3] = {0, 0, 0};
+        bool inside = true;
+        for (int d = 0; d < dim; d++) {
+            if (!(p[d] >= r.bbmin[d] && p[d] <= r.bbmax[d])) { inside = false; break; }
+            i0[d] = (int)((p[d] - r.bbmin[d]) / dW[d]);
+            if (i0[d] < 0) i0[d] = 0;
+            else if (i0[d] >= r.bdim[d] - 1) i0[d] = r.bdim[d] - 2;
+            d0[d] = (p[d] - (i0[d] * dW[d] + r.bbmin[d])) / dW[d];
+            if (d0[d] < 0.0) d0[d] = 0.0;
+            else if (d0[d] > 1.0) d0[d] = 1.0;
+        }
+        if (inside) {
+            const size_t i0n = r.ncol.size();
+            const int ncorner = dim == 2 ? 4 : 8;
+            for (int c = 0; c < ncorner; c++) {
+                const int cx = c & 1, cy = (c >> 1) & 1, cz = (c >> 2) & 1;
+                const int pix = (i0[0] + cx) + nx * ((i0[1] + cy) + ny * (dim > 2 ? i0[2] + cz : 0));
+                if (r.elref[pix] < 0) continue;
+                double w = (cx ? d0[0] : 1.0 - d0[0]) * (cy ? d0[1] : 1.0 - d0[1]);
+                if (dim > 2) w *= cz ? d0[2] : 1.0 - d0[2];
+                r.ncol.push_back(pix);
+                r.nval.push_back(w);
+            }
+            const size_t cnt = r.ncol.size() - i0n;
+            if (cnt > 0 && (int)cnt < ncorner) {
+                double wsum = 0.0;
+                for (size_t i = i0n; i < r.ncol.size(); i++) wsum += r.nval[i];
+                for (size_t i = i0n; i < r.ncol.size(); i++)
+                    r.nval[i] = wsum > 1e-8 ? r.nval[i] / wsum : 1.0 / (double)cnt;
+            }
+            size_t o = i0n;
+            for (size_t i = i0n; i < r.ncol.size(); i++)
+                if (r.nval[i] != 0.0) { r.ncol[o] = r.ncol[i]; r.nval[o++] = r.nval[i]; }
+            r.ncol.resize(o);
+            r.nval.resize(o);
+        }
+        r.nrowptr[k + 1] = (int)r.ncol.size();
+    }
 }
 
 template <class T>
@@ -2137,6 +2187,9 @@ int tg_raster_create(tg_mesh mesh, const int* bdim, tg_raster* out)
     upload_sync(r->d_rowptr, r->rowptr);
     upload_sync(r->d_col, r->col);
     upload_sync(r->d_val, r->val);
+    upload_sync(r->d_nrowptr, r->nrowptr);
+    upload_sync(r->d_ncol, r->ncol);
+    upload_sync(r->d_nval, r->nval);
     *out = r.release();
     API_END
 }
@@ -2166,6 +2219,53 @@ int tg_raster_elref(tg_raster r, int* elref)
     API_BEGIN
     TG_CHECK(r && elref, TG_ERR_ARG, "NULL argument");
     std::memcpy(elref, r->elref.data(), r->elref.size() * sizeof(int));
+    API_END
+}
+
+// toast.Raster.Map (MapBasis, src/python/toastmodule.cc:718-790) for the
+// pixel raster whose basis is its grid: mesh (M), grid / basis (G, B),
+// solution (S).  M -> G: B; G -> S: the support; S -> G: scatter with zeros;
+// G -> M: NodeMapMatrix; the rest compose these.  Each vector is `width`
+// doubles per point (1 real, 2 complex).
+int tg_raster_map(tg_raster r, const char* map, int nvec, const double* src, double* dst, int width, int mem)
+{
+    API_BEGIN
+    TG_CHECK(r && map && src && dst && nvec > 0 && nvec <= 65535 && (width == 1 || width == 2), TG_ERR_ARG,
+             "invalid argument");
+    TG_CHECK(strlen(map) == 4 && map[1] == '-' && map[2] == '>', TG_ERR_ARG, "map must read \"X->Y\"");
+    auto kind = [](char c) { return c == 'B' ? 'G' : c; };
+    const char a = kind(map[0]), b = kind(map[3]);
+    auto len = [&](char c) { return c == 'M' ? r->mesh->d.n : c == 'G' ? r->glen : c == 'S' ? r->slen : -1; };
+    TG_CHECK(len(a) > 0 && len(b) > 0 && a != b, TG_ERR_ARG, "map ids are M, G, B or S, source and target different");
+    TG_CUDA(cudaSetDevice(r->mesh->device));
+    const size_t sb = (size_t)nvec * len(a) * width * sizeof(double), db = (size_t)nvec * len(b) * width * sizeof(double);
+    const double* x = mem == TG_MEM_DEVICE ? src : (const double*)r->d_src.ensure(sb);
+    if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpy((void*)x, src, sb, cudaMemcpyHostToDevice));
+    double* y = mem == TG_MEM_DEVICE ? dst : (double*)r->d_dst.ensure(db);
+    const int glen = r->glen, slen = r->slen, n = r->mesh->d.n;
+    auto apply = [&](const DBuf& rp, const DBuf& cl, const DBuf& vl, int rows, int cols, const double* in, double* out) {
+        launch(csr_apply_kernel, dim3(cdiv_u(rows, 128), nvec), 128, 0, (cudaStream_t)0, rows, cols, width,
+               rp.as<int>(), cl.as<int>(), vl.as<double>(), in, out);
+    };
+    auto select = [&](const double* in, double* out) {
+        launch(gather_points_kernel, dim3(cdiv_u(slen, 128), nvec), 128, 0, (cudaStream_t)0, slen, glen, width,
+               r->d_sol.as<int>(), in, out);
+    };
+    auto scatter = [&](const double* in, double* out) {
+        TG_CUDA(cudaMemsetAsync(out, 0, (size_t)nvec * glen * width * sizeof(double), (cudaStream_t)0));
+        launch(scatter_points_kernel, dim3(cdiv_u(slen, 128), nvec), 128, 0, (cudaStream_t)0, slen, glen, width,
+               r->d_sol.as<int>(), in, out);
+    };
+    double* t = (double*)r->d_tmp.ensure((size_t)nvec * glen * width * sizeof(double));
+    if (a == 'M' && b == 'G') apply(r->d_rowptr, r->d_col, r->d_val, glen, n, x, y);
+    else if (a == 'M' && b == 'S') { apply(r->d_rowptr, r->d_col, r->d_val, glen, n, x, t); select(t, y); }
+    else if (a == 'G' && b == 'S') select(x, y);
+    else if (a == 'S' && b == 'G') scatter(x, y);
+    else if (a == 'G' && b == 'M') apply(r->d_nrowptr, r->d_ncol, r->d_nval, n, glen, x, y);
+    else if (a == 'S' && b == 'M') { scatter(x, t); apply(r->d_nrowptr, r->d_ncol, r->d_nval, n, glen, t, y); }
+    TG_CUDA(cudaGetLastError());
+    if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpy(dst, y, db, cudaMemcpyDeviceToHost));
+    else TG_CUDA(cudaStreamSynchronize(0));
     API_END
 }
 
