@@ -1053,8 +1053,6 @@ static int fail(const Error& e)
     catch (...) { set_error("unknown error"); return TG_ERR_ARG; }                              \
     return TG_OK;
 
-static size_t vsize(int cplx, bool fp32) { return (cplx ? 2 : 1) * (fp32 ? 4 : 8); }
-
 template <class V> static Engine<V>& engine(tg_solver s);
 template <> Engine<double>& engine<double>(tg_solver s) { return s->er64; }
 template <> Engine<float>& engine<float>(tg_solver s) { return s->er32; }
