@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--e2e-slots", type=int, default=1, help="e2e leg: request-server slots")
     ap.add_argument("--grid", type=int, default=32,
                     help="grid-basis Jacobian leg: raster points per axis (0: skip)")
+    ap.add_argument("--element", action="store_true",
+                    help="also time the element-basis Jacobian on the same fields")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--tol", type=float, default=1e-12)
     ap.add_argument("--inner-tol", type=float, default=1e-4, help="mixed path: inner FP32 solve tolerance")
@@ -345,12 +347,25 @@ def run_gpu(args):
 
     # ---- grid-basis Jacobian (pixel raster, basis = grid) on this request's
     # fields, device-resident, timed alone with CUDA events
-    grid = None
-    if args.grid > 0:
+    def event_ms(fn, reps=5):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for a, b in ev:
+            a.record(stream)
+            fn()
+            b.record(stream)
+        torch.cuda.synchronize()
+        return float(np.mean([a.elapsed_time(b) for a, b in ev]))
+
+    grid = element = None
+    if args.grid > 0 or args.element:
         d_dphi = torch.empty((nq, n * vmul), dtype=torch.float64, device=dev)
         d_aphi = torch.empty((nm, n * vmul), dtype=torch.float64, device=dev)
         s.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, d_dphi, d_aphi, d_proj, d_lproj, d_J,
                            j_fp32, capi.MEM_DEVICE, res)
+    if args.grid > 0:
         rast = capi.Raster(gm, [args.grid] * P.dim)
         gcols = (2 if cplx else 1) * rast.slen
         d_Jg = torch.empty((2 * nqm, gcols), dtype=torch.float32 if j_fp32 else torch.float64, device=dev)
@@ -359,16 +374,7 @@ def run_gpu(args):
             s.jacobian_grid_raw(rast, nq, d_dphi, nm, d_aphi, d_proj, links, capi.DATA_LOG, d_Jg, j_fp32,
                                 capi.MEM_DEVICE)
 
-        for _ in range(3):
-            gstep()
-        torch.cuda.synchronize()
-        ge = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(5)]
-        for a, b in ge:
-            a.record(stream)
-            gstep()
-            b.record(stream)
-        torch.cuda.synchronize()
-        g_ms = float(np.mean([a.elapsed_time(b) for a, b in ge]))
+        g_ms = event_ms(gstep)
         jb = d_Jg.numel() * d_Jg.element_size()
         # field planes read once per source / detector (value + dim gradients)
         pb = (nq + nm) * (1 + P.dim) * rast.slen * (8 if j_fp32 else 16) // (1 if cplx else 2)
@@ -380,7 +386,23 @@ def run_gpu(args):
                              "algorithmic_bytes_per_launch": jb + pb},
                 "note": "includes the field resampling and gradient launches; inputs on the device"}
         rast.close()
-        del d_Jg, d_dphi, d_aphi
+        del d_Jg
+    if args.element:
+        # element-basis Jacobian (one column per element and component) on the same fields
+        ecols = (2 if cplx else 1) * gm.ne
+        d_Je = torch.empty((2 * nqm, ecols), dtype=torch.float32 if j_fp32 else torch.float64, device=dev)
+        e_ms = event_ms(lambda: s.jacobian_el_raw(nq, d_dphi, nm, d_aphi, d_proj, links, capi.DATA_LOG, d_Je,
+                                                  j_fp32, capi.MEM_DEVICE))
+        jb = d_Je.numel() * d_Je.element_size()
+        fb = (nq + nm) * n * vmul * 8  # the FP64 fields, read once
+        element = {"elements": gm.ne, "ms_per_jacobian": e_ms, "jacobians_per_s": 1e3 / e_ms, "J_bytes": jb,
+                   "roofline": {"bound": "hbm", "achieved": (jb + fb) / (e_ms / 1e3) / 1e9, "peak": peak,
+                                "unit": "GB/s", "frac": (jb + fb) / (e_ms / 1e3) / 1e9 / peak,
+                                "algorithmic_bytes_per_launch": jb + fb},
+                   "note": "includes the FP32 casts of the fields; inputs on the device"}
+        del d_Je
+    if args.grid > 0 or args.element:
+        del d_dphi, d_aphi
 
     # ---- e2e through the C ABI with host buffers (pinned), copies inside the timed region
     e2e = None
@@ -519,6 +541,7 @@ def run_gpu(args):
             "ic_applies_per_request": prof[capi.PROF_SWEEP][1] / psteps,
             "roofline": roof, "kernel_time_per_step": shares,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "grid_jacobian": grid,
+            "element_jacobian": element,
             "clocks": clocks, "wall_s": wall, "compare": compare,
             "spmm_autotuner": capi.tuner_log().strip().splitlines(),
         }

@@ -23,3 +23,18 @@ def load(name):
     for k in ("freq_mhz", "qwidth", "mwidth", "tol"):
         d[k] = float(d[k])
     return d
+
+
+def sparse_links(g):
+    """A subset of the fixture's links: source 1 keeps none, source 0 keeps
+    all, the others every second detector.  Returns (link_ofs, link_m,
+    indices of the kept links)."""
+    ofs, lm = g["link_ofs"], g["link_m"]
+    new_ofs, new_m, keep = [0], [], []
+    for q in range(len(ofs) - 1):
+        for i in range(ofs[q], ofs[q + 1]):
+            if q != 1 and (q == 0 or (q + int(lm[i])) % 2 == 0):
+                new_m.append(int(lm[i]))
+                keep.append(i)
+        new_ofs.append(len(new_m))
+    return np.array(new_ofs, np.int32), np.array(new_m, np.int32), np.array(keep)

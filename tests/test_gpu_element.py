@@ -4,7 +4,7 @@ element-basis Jacobian, against the compiled reference's own outputs
 import numpy as np
 import pytest
 
-from tests.golden_util import load, names
+from tests.golden_util import load, names, sparse_links
 from tests.gpu_util import rel2, relmax
 from toastpp_gb300 import capi
 
@@ -50,6 +50,19 @@ def test_element_jacobian_linear_data_against_oracle(name, oracle_mod):
     J = s.jacobian_el(g["dphi"], g["aphi"], None, L, scale=capi.DATA_LIN)
     om = oracle_mod.Mesh(g["coords"], g["elems"])
     ref = oracle_mod.jacobian_el(om, g["dphi"], g["aphi"], g["proj"], g["link_ofs"], g["link_m"], logscale=False)
+    assert rel2(J, ref) < 1e-13
+
+
+@pytest.mark.parametrize("name", ELEM)
+def test_element_jacobian_sparse_links_against_oracle(name, oracle_mod):
+    """Links missing for some (source, detector) pairs and a source without
+    any, with a source count that leaves a partial group of sources."""
+    g, gm, s, L = setup(name)
+    ofs, lm, keep = sparse_links(g)
+    J = s.jacobian_el(g["dphi"], g["aphi"], g["proj"][keep], capi.Links(ofs, lm))
+    om = oracle_mod.Mesh(g["coords"], g["elems"])
+    ref = oracle_mod.jacobian_el(om, g["dphi"], g["aphi"], g["proj"][keep], ofs, lm)
+    assert J.shape == ref.shape == (2 * len(keep), g["Jel"].shape[1])
     assert rel2(J, ref) < 1e-13
 
 

@@ -4,7 +4,7 @@ reference) and the oracle."""
 import numpy as np
 import pytest
 
-from tests.golden_util import load, names
+from tests.golden_util import load, names, sparse_links
 from tests.gpu_util import rel2
 from toastpp_gb300 import capi
 
@@ -69,6 +69,19 @@ def test_grid_jacobian_end_to_end(name):
     proj = s.project_all(m, dphi, L, capi.DATA_LIN)
     J = s.jacobian_grid(r, dphi, aphi, proj, L)
     assert rel2(J, g["Jgrid"]) < 1e-9
+
+
+@pytest.mark.parametrize("name", GRID)
+def test_grid_jacobian_sparse_links_against_oracle(name, oracle_mod):
+    """Links missing for some (source, detector) pairs and a source without
+    any, with a source count that leaves a partial group of sources."""
+    g, gm, r, s, L = setup(name)
+    ofs, lm, keep = sparse_links(g)
+    J = s.jacobian_grid(r, g["dphi"], g["aphi"], g["proj"][keep], capi.Links(ofs, lm))
+    om = oracle_mod.Mesh(g["coords"], g["elems"])
+    ref = oracle_mod.jacobian_grid(om, g["bdim"], g["dphi"], g["aphi"], g["proj"][keep], ofs, lm)
+    assert J.shape == ref.shape == (2 * len(keep), g["Jgrid"].shape[1])
+    assert rel2(J, ref) < 1e-13
 
 
 def test_raster_of_another_mesh_is_rejected():

@@ -335,6 +335,11 @@ class FwdSolver:
                                     _ptr(links.ofs), _ptr(links.m), scale, _ptr(J), int(fp32), MEM_HOST))
         return J
 
+    def jacobian_el_raw(self, nq, dphi, nm, aphi, proj, links: Links, scale, J, fp32, mem):
+        """tg_jacobian_el with caller-owned buffers (numpy or device tensors)."""
+        _check(lib().tg_jacobian_el(self._h, int(nq), _ptr(dphi), int(nm), _ptr(aphi), _ptr(proj), _ptr(links.ofs),
+                                    _ptr(links.m), int(scale), _ptr(J), int(fp32), int(mem)))
+
     def system_matrix(self):
         out = np.zeros(self.mesh.nnz, np.complex128 if self.complex else np.float64)
         _check(lib().tg_solver_matrix(self._h, _ptr(out), MEM_HOST))

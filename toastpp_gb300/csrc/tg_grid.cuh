@@ -4,14 +4,15 @@
 // complex, projections given) and GenerateJacobian_cw_grid (516-712, real)
 // with Raster_Pixel (raster_px.cc:10-48) whose basis equals its grid.
 //
-// Per request the fields (node-major, natural numbering) are resampled on
-// the grid, then the values and the central or one-sided differences of
-// ImageGradient (jacobian.cc:944-1060) at the solution points (the grid
-// points inside the mesh) go to planes P[(c * (1 + dim) + comp) * slen + s]
-// (comp 0 the value, 1..dim the gradient), so that a thread per solution
-// point reads every plane of a source or detector coalesced.  Then one thread
-// per solution point and source walks the source's links and writes its
-// column of every link row.
+// Per request the fields (source-major, natural numbering) are resampled on
+// the grid column by column (gm[c * glen + g]), then the values and the
+// central or one-sided differences of ImageGradient (jacobian.cc:944-1060) at
+// the solution points (the grid points inside the mesh) go to planes
+// P[(c * (1 + dim) + comp) * slen + s] (comp 0 the value, 1..dim the
+// gradient), so that a thread per solution point reads every plane of a
+// source or detector coalesced.  Then one thread per solution point and
+// group of sources walks the sources' links and writes its column of every
+// link row.
 #pragma once
 #include "tg_kernels.cuh"
 
@@ -97,6 +98,84 @@ __global__ void __launch_bounds__(256) grid_planes_kernel(GridDev G, int k, cons
     }
 }
 
+// Map_MeshToGrid of source-major columns, column-major result:
+// gm[c * glen + g] = sum_j B(g, j) x[c * n + col_j] in the arithmetic type A;
+// columns c < k0 from x0, the others from x1.  A thread per grid point keeps
+// its row of B (at most four entries for linear elements) in registers for
+// MAPC columns; neighbouring grid points gather from neighbouring nodes.
+constexpr int MAPC = 8;
+template <class A, class V>
+__global__ void __launch_bounds__(256) grid_map_cm_kernel(GridDev G, int n, int k, int k0, const V* __restrict__ x0,
+                                                          const V* __restrict__ x1, A* __restrict__ gm)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= G.glen) return;
+    using R = typename vt<A>::R;
+    const int j0 = G.rowptr[g], nj = G.rowptr[g + 1] - j0;
+    int col[4];
+    R w[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        col[j] = j < nj ? G.col[j0 + j] : 0;
+        w[j] = j < nj ? (R)G.val[j0 + j] : (R)0;
+    }
+    const int c1 = min(k, (int)(blockIdx.y + 1) * MAPC);
+    for (int c = blockIdx.y * MAPC; c < c1; c++) {
+        const V* x = c < k0 ? x0 + (size_t)c * n : x1 + (size_t)(c - k0) * n;
+        A acc = vzero<A>();
+        if (nj <= 4) {
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if (j < nj) acc = vadd(acc, vscale(vcast<A, V>(x[col[j]]), w[j]));
+        } else {
+            for (int j = j0; j < j0 + nj; j++) acc = vadd(acc, vscale(vcast<A, V>(x[G.col[j]]), (R)G.val[j]));
+        }
+        gm[(size_t)c * G.glen + g] = acc;
+    }
+}
+
+// Field planes P[(c * (1 + dim) + comp) * slen + s] from the column-major grid
+// fields: a thread per solution point finds, once, the neighbours and weight
+// of each axis's difference under the masked and the unmasked rule of
+// grid_component, then forms MAPC columns; columns c < kmask are masked, the
+// others when mask_rest is set.  Reads and writes run along s.
+template <class A>
+__global__ void __launch_bounds__(256) grid_planes_cm_kernel(GridDev G, int k, int kmask, int mask_rest,
+                                                             const A* __restrict__ gm, A* __restrict__ planes)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= G.slen) return;
+    using R = typename vt<A>::R;
+    const int g = G.sol[s], np = 1 + G.dim;
+    const int co[3] = {g % G.nx, (g / G.nx) % G.ny, g / (G.nx * G.ny)};
+    const int len[3] = {G.nx, G.ny, G.nz}, st[3] = {1, G.nx, G.nx * G.ny};
+    int lo[2][3], hi[2][3];
+    R w[2][3];
+#pragma unroll
+    for (int mk = 0; mk < 2; mk++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            lo[mk][d] = hi[mk][d] = g;
+            w[mk][d] = (R)0;
+            if (d >= G.dim) continue;
+            const bool blo = co[d] > 0 && (!mk || G.elref[g - st[d]] >= 0);
+            const bool bhi = co[d] < len[d] - 1 && (!mk || G.elref[g + st[d]] >= 0);
+            if (blo) lo[mk][d] = g - st[d];
+            if (bhi) hi[mk][d] = g + st[d];
+            if (blo || bhi) w[mk][d] = (R)((blo && bhi ? 0.5 : 1.0) * G.ih[d]);
+        }
+    const int c1 = min(k, (int)(blockIdx.y + 1) * MAPC);
+    for (int c = blockIdx.y * MAPC; c < c1; c++) {
+        const A* x = gm + (size_t)c * G.glen;
+        const int mk = (c < kmask || mask_rest) ? 1 : 0;
+        A* P = planes + (size_t)c * np * G.slen + s;
+        P[0] = x[g];
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+            if (d < G.dim) P[(size_t)(d + 1) * G.slen] = vscale(vsub(x[hi[mk][d]], x[lo[mk][d]]), w[mk][d]);
+    }
+}
+
 // Smith's complex division (Smith 1962)
 __device__ __forceinline__ cd cdiv_smith(cd a, cd b)
 {
@@ -108,15 +187,20 @@ __device__ __forceinline__ cd cdiv_smith(cd a, cd b)
     return cd{(a.x * r + a.y) / den, (a.y * r - a.x) / den};
 }
 
-// 1 / y per link, in FP64 (Smith's division for complex y), then cast to the
+// The factor of each link's row: sc / y for log data (Smith's division for
+// complex y), sc for linear data (y null), in FP64, then cast to the
 // Jacobian's arithmetic type
 template <class C, class V64>
-__global__ void grid_yinv_kernel(int nqm, const V64* __restrict__ y, C* __restrict__ yinv)
+__global__ void grid_yscale_kernel(int nqm, const V64* __restrict__ y, double sc, C* __restrict__ ysc)
 {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= nqm) return;
-    if constexpr (vt<V64>::cplx) yinv[l] = vcast<C, V64>(cdiv_smith(cd{1.0, 0.0}, y[l]));
-    else yinv[l] = vcast<C, V64>(1.0 / y[l]);
+    if constexpr (vt<V64>::cplx) {
+        const cd r = y ? cdiv_smith(cd{1.0, 0.0}, y[l]) : cd{1.0, 0.0};
+        ysc[l] = vcast<C, cd>(cd{r.x * sc, r.y * sc});
+    } else {
+        ysc[l] = vcast<C, double>(y ? sc / y[l] : sc);
+    }
 }
 
 // J stores bypass L2 retention (evict-first), so the 2.4 GB stream of rows
@@ -125,32 +209,41 @@ __device__ __forceinline__ void st_stream(float* p, float v) { __stcs(p, v); }
 __device__ __forceinline__ void st_stream(double* p, double v) { __stcs(p, v); }
 
 // One thread per (solution point, group of GQ sources): the sources' planes
-// stay in registers while the detectors' planes stream past, each loaded
-// once per group.  PMDF_mua = -(f a), PMDF_kap = -sum_d (grad_d f)(grad_d a)
-// (jacobian.cc:58-72); complex LOG data are divided by y (PMDF_log, 76-79)
-// before the voxel scale, real LOG rows are scaled by 1/y after it
-// (GenerateJacobian_cw, 178-193).  Both multiply by the link's 1/y (yinv): a
-// division per entry would run on the FP64 pipe.  pair[q * nm + m]: link
-// index or -1.  J rows: complex [Re mua | Re kap] at l and [Im mua | Im kap]
-// at nQM + l (2 slen columns); real mua at l and kap at nQM + l (slen).
-template <class V, class JT, int GQ>
-__global__ void grid_jacobian_kernel(int dim, int slen, int nq, int nm, int nqm, const V* __restrict__ Fp,
-                                     const V* __restrict__ Ap, const int* __restrict__ pair,
-                                     const V* __restrict__ yinv, double sz, JT* __restrict__ J)
+// stay in registers while the detectors' planes stream past, each loaded once
+// per group, the next detector's while this one's entries form.  PMDF_mua =
+// -(f a), PMDF_kap = -sum_d (grad_d f)(grad_d a) (jacobian.cc:58-72); LOG
+// data are divided by y (complex: PMDF_log, 76-79; real:
+// GenerateJacobian_cw, 178-193) and every entry is multiplied by the voxel
+// scale (365-370).  ysc[l] carries -scale / y of the link (-scale for LINEAR
+// data), so an entry costs one complex product more than its PMDF: a
+// division per entry would run on the FP64 pipe.  NP = 1 + dim planes.
+// pair[q * nm + m]: link index or -1.  J rows: complex [Re mua | Re kap] at l
+// and [Im mua | Im kap] at nQM + l (2 slen columns); real mua at l and kap at
+// nQM + l (slen).
+template <class V, class JT, int GQ, int NP>
+__global__ void __launch_bounds__(256) grid_jacobian_kernel(int slen, int nq, int nm, int nqm, const V* __restrict__ Fp,
+                                                            const V* __restrict__ Ap, const int* __restrict__ pair,
+                                                            const V* __restrict__ ysc, JT* __restrict__ J)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x, q0 = blockIdx.y * GQ;
     if (s >= slen) return;
-    using R = typename vt<V>::R;
-    const int np = 1 + dim;
-    V f[GQ][4];
+    V f[GQ][NP];
 #pragma unroll
     for (int g = 0; g < GQ; g++)
 #pragma unroll
-        for (int d = 0; d < 4; d++)
-            f[g][d] = (q0 + g < nq && d < np) ? Fp[((size_t)(q0 + g) * np + d) * slen + s] : vzero<V>();
+        for (int d = 0; d < NP; d++) f[g][d] = Fp[((size_t)min(q0 + g, nq - 1) * NP + d) * slen + s];
     constexpr bool CPLX = vt<V>::cplx;
     const size_t cols = CPLX ? 2 * (size_t)slen : (size_t)slen;
+    V an[NP];
+#pragma unroll
+    for (int d = 0; d < NP; d++) an[d] = Ap[(size_t)d * slen + s];
     for (int m = 0; m < nm; m++) {
+        V a[NP];
+#pragma unroll
+        for (int d = 0; d < NP; d++) {
+            a[d] = an[d];
+            if (m + 1 < nm) an[d] = Ap[((size_t)(m + 1) * NP + d) * slen + s];
+        }
         int lk[GQ];
         bool any = false;
 #pragma unroll
@@ -159,37 +252,25 @@ __global__ void grid_jacobian_kernel(int dim, int slen, int nq, int nm, int nqm,
             any |= lk[g] >= 0;
         }
         if (!any) continue;
-        V a[4];
-#pragma unroll
-        for (int d = 0; d < 4; d++) a[d] = d < np ? Ap[((size_t)m * np + d) * slen + s] : vzero<V>();
 #pragma unroll
         for (int g = 0; g < GQ; g++) {
             const int l = lk[g];
             if (l < 0) continue;
-            V pm = vsub(vzero<V>(), vmul(f[g][0], a[0]));
-            V pk = vzero<V>();
+            const V y = ysc[l];
+            V t = vmul(f[g][1], a[1]);
 #pragma unroll
-            for (int d = 1; d < 4; d++)
-                if (d < np) pk = vsub(pk, vmul(f[g][d], a[d]));
-            JT* r0 = J + (size_t)l * cols;
-            JT* r1 = J + (size_t)(l + nqm) * cols;
+            for (int d = 2; d < NP; d++) t = vfma(t, f[g][d], a[d]);
+            const V pm = vmul(vmul(f[g][0], a[0]), y), pk = vmul(t, y);
+            JT* r0 = J + (size_t)l * cols + s;
+            JT* r1 = J + (size_t)(l + nqm) * cols + s;
             if constexpr (CPLX) {
-                if (yinv) {
-                    pm = vmul(pm, yinv[l]);
-                    pk = vmul(pk, yinv[l]);
-                }
-                st_stream(r0 + s, (JT)(re(pm) * (R)sz));
-                st_stream(r1 + s, (JT)(im(pm) * (R)sz));
-                st_stream(r0 + slen + s, (JT)(re(pk) * (R)sz));
-                st_stream(r1 + slen + s, (JT)(im(pk) * (R)sz));
+                st_stream(r0, (JT)re(pm));
+                st_stream(r1, (JT)im(pm));
+                st_stream(r0 + slen, (JT)re(pk));
+                st_stream(r1 + slen, (JT)im(pk));
             } else {
-                R vm = re(pm) * (R)sz, vk = re(pk) * (R)sz;
-                if (yinv) {
-                    vm *= yinv[l];
-                    vk *= yinv[l];
-                }
-                st_stream(r0 + s, (JT)vm);
-                st_stream(r1 + s, (JT)vk);
+                st_stream(r0, (JT)pm);
+                st_stream(r1, (JT)pk);
             }
         }
     }
@@ -200,42 +281,52 @@ __global__ void grid_jacobian_kernel(int dim, int slen, int nq, int nm, int nqm,
 // IntGradFGradG_el (884-939): per element e and link (q, m),
 // sum_ij f_i g_j IntFF(i,j) and sum_ij f_i g_j IntDD(i,j), formed as
 // sum_i f_i h_i with h = W g once per (element, detector) and shared by the
-// group's GQ sources.  Fields source-major in the natural numbering.
-// J: complex (2 nQM) x (2 ne) rows -Re / -Im, kappa at column ne + e; real
-// (2 nQM) x ne [mua ; kappa].
-template <class V, class JT, int GQ>
-__global__ void element_jacobian_kernel(MeshDev m, int nq, int nm, int nqm, const V* __restrict__ F,
-                                        const V* __restrict__ A, const int* __restrict__ pair,
-                                        const V* __restrict__ yinv, JT* __restrict__ J)
+// group's GQ sources.  IntFF(i,j) = size (1 + [i = j]) / 12 (triangles) or
+// / 20 (tetrahedra), so h_i = size / 12 (or 20) (a_i + sum_j a_j).  NN nodes
+// per element (3 or 4).  Fields source-major in the natural numbering.
+// ysc[l] = -1 / y for LOG data, -1 for LINEAR.  J: complex (2 nQM) x (2 ne)
+// rows -Re / -Im, kappa at column ne + e; real (2 nQM) x ne [mua ; kappa].
+template <class V, class JT, int GQ, int NN>
+__global__ void __launch_bounds__(256) element_jacobian_kernel(MeshDev m, int nq, int nm, int nqm,
+                                                               const V* __restrict__ F, const V* __restrict__ A,
+                                                               const int* __restrict__ pair,
+                                                               const V* __restrict__ ysc, JT* __restrict__ J)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x, q0 = blockIdx.y * GQ;
     if (e >= m.ne) return;
     using R = typename vt<V>::R;
-    const int nn = m.nn, n = m.n;
-    const int* nd = m.el + (size_t)e * nn;
+    const int n = m.n;
+    const int* nd = m.el + (size_t)e * NN;
     const double* r = m.rec + (size_t)e * EL_REC;
-    const double ffd = m.dim == 2 ? 1.0 / 12.0 : 1.0 / 20.0;
-    R wff[4][4], wdd[4][4];
-    int node[4];
+    const R cff = (R)((NN == 3 ? 1.0 / 12.0 : 1.0 / 20.0) * r[0]);
+    R wdd[NN][NN];
+    int node[NN];
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        node[i] = i < nn ? nd[i] : 0;
+    for (int i = 0; i < NN; i++) {
+        node[i] = nd[i];
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            wff[i][j] = (i < nn && j < nn) ? (R)(((i == j ? 2.0 : 1.0) * ffd) * r[0]) : (R)0;
+        for (int j = 0; j < NN; j++)
             // IntDD: the record's value for triangles, 4 x it for tetrahedra
-            wdd[i][j] = (i < nn && j < nn) ? (R)((m.dim == 3 ? 4.0 : 1.0) * r[1 + i * nn + j]) : (R)0;
-        }
+            wdd[i][j] = (R)((NN == 4 ? 4.0 : 1.0) * r[1 + i * NN + j]);
     }
-    V f[GQ][4];
+    V f[GQ][NN];
 #pragma unroll
     for (int g = 0; g < GQ; g++)
 #pragma unroll
-        for (int i = 0; i < 4; i++)
-            f[g][i] = (q0 + g < nq && i < nn) ? F[(size_t)(q0 + g) * n + node[i]] : vzero<V>();
+        for (int i = 0; i < NN; i++) f[g][i] = F[(size_t)min(q0 + g, nq - 1) * n + node[i]];
     constexpr bool CPLX = vt<V>::cplx;
     const size_t cols = CPLX ? 2 * (size_t)m.ne : (size_t)m.ne;
+    // the next detector's nodal values load while this one's entries form
+    V an[NN];
+#pragma unroll
+    for (int j = 0; j < NN; j++) an[j] = A[node[j]];
     for (int mm = 0; mm < nm; mm++) {
+        V a[NN];
+#pragma unroll
+        for (int j = 0; j < NN; j++) {
+            a[j] = an[j];
+            if (mm + 1 < nm) an[j] = A[(size_t)(mm + 1) * n + node[j]];
+        }
         int lk[GQ];
         bool any = false;
 #pragma unroll
@@ -244,43 +335,40 @@ __global__ void element_jacobian_kernel(MeshDev m, int nq, int nm, int nqm, cons
             any |= lk[g] >= 0;
         }
         if (!any) continue;
-        V a[4], hm[4], hk[4];
+        V hm[NN], hk[NN];
+        V sa = vzero<V>();
 #pragma unroll
-        for (int j = 0; j < 4; j++) a[j] = j < nn ? A[(size_t)mm * n + node[j]] : vzero<V>();
+        for (int j = 0; j < NN; j++) sa = vadd(sa, a[j]);
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            hm[i] = vzero<V>();
-            hk[i] = vzero<V>();
+        for (int i = 0; i < NN; i++) {
+            hm[i] = vscale(vadd(sa, a[i]), cff);
+            hk[i] = vscale(a[0], wdd[i][0]);
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                hm[i] = vadd(hm[i], vscale(a[j], wff[i][j]));
-                hk[i] = vadd(hk[i], vscale(a[j], wdd[i][j]));
-            }
+            for (int j = 1; j < NN; j++) hk[i] = vadd(hk[i], vscale(a[j], wdd[i][j]));
         }
 #pragma unroll
         for (int g = 0; g < GQ; g++) {
             const int l = lk[g];
             if (l < 0) continue;
-            V pm = vzero<V>(), pk = vzero<V>();
+            V pm = vmul(f[g][0], hm[0]), pk = vmul(f[g][0], hk[0]);
 #pragma unroll
-            for (int i = 0; i < 4; i++) {
+            for (int i = 1; i < NN; i++) {
                 pm = vfma(pm, f[g][i], hm[i]);
                 pk = vfma(pk, f[g][i], hk[i]);
             }
-            if (yinv) {
-                pm = vmul(pm, yinv[l]);
-                pk = vmul(pk, yinv[l]);
-            }
+            const V y = ysc[l];
+            pm = vmul(pm, y);
+            pk = vmul(pk, y);
             JT* r0 = J + (size_t)l * cols;
             JT* r1 = J + (size_t)(l + nqm) * cols;
             if constexpr (CPLX) {
-                st_stream(r0 + e, (JT)-re(pm));
-                st_stream(r1 + e, (JT)-im(pm));
-                st_stream(r0 + m.ne + e, (JT)-re(pk));
-                st_stream(r1 + m.ne + e, (JT)-im(pk));
+                st_stream(r0 + e, (JT)re(pm));
+                st_stream(r1 + e, (JT)im(pm));
+                st_stream(r0 + m.ne + e, (JT)re(pk));
+                st_stream(r1 + m.ne + e, (JT)im(pk));
             } else {
-                st_stream(r0 + e, (JT)-pm);
-                st_stream(r1 + e, (JT)-pk);
+                st_stream(r0 + e, (JT)pm);
+                st_stream(r1 + e, (JT)pk);
             }
         }
     }

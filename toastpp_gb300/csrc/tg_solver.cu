@@ -1556,40 +1556,44 @@ template <class V64, class C>
 static void grid_jac_run(tg_solver s, const tg_raster_s& r, int nq, const V64* F, int nm, const V64* A,
                          const V64* yl, const LinkHost& L, int logscale, void* Jd)
 {
-    const int n = s->mesh->d.n, nqm = (int)L.q.size(), np = 1 + r.dim;
+    const int n = s->mesh->d.n, nqm = (int)L.q.size(), np = 1 + r.dim, k = nq + nm;
     const GridDev G = r.dev();
-    C* Pq = (C*)s->gplanes_q.ensure((size_t)nq * np * r.slen * sizeof(C));
-    C* Pm = (C*)s->gplanes_m.ensure((size_t)nm * np * r.slen * sizeof(C));
-    const unsigned gx = cdiv_u(std::max(r.slen, 1), 256);
-    // fields node-major (natural numbering), resampled on the grid, planes;
-    // the reference masks the adjoint gradient for complex data only
-    // (jacobian.cc:348-350 against 557)
-    auto planes = [&](int k, const V64* src, int masked, C* P) {
-        V64* xn = (V64*)s->tmp.ensure((size_t)k * n * sizeof(V64));
-        launch(to_nodemajor_kernel<V64, V64>, dim3(cdiv_u(n, 32), cdiv_u(k, 32)), dim3(32, 8), 0, s->stream, n, k, k,
-               src, xn, (const int*)nullptr);
-        V64* gm = (V64*)s->io_c.ensure((size_t)r.glen * k * sizeof(V64));
-        launch(grid_map_kernel<V64>, cdiv_u((size_t)r.glen * 32, 256), 256, 0, s->stream, G, k, (const V64*)xn, k,
-               (const int*)nullptr, gm);
-        launch(grid_planes_kernel<V64, C>, dim3(cdiv_u(r.slen, 32), cdiv_u(k, 32)), dim3(32, 8), 0, s->stream, G, k,
-               (const V64*)gm, masked, P);
-    };
-    planes(nq, F, 1, Pq);
-    planes(nm, A, vt<V64>::cplx ? 1 : 0, Pm);
-    const C* yinv = nullptr;
-    if (logscale) {
-        C* yc = (C*)s->gy.ensure((size_t)nqm * sizeof(C));
-        launch(grid_yinv_kernel<C, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, yl, yc);
-        yinv = yc;
-    }
-    // link index per (source, detector); a pageable source: the copy
-    // completes before the call returns
+    // link index per (source, detector), from pageable memory: issued before
+    // the launches, so a staging wait finds the stream idle
     int* pr = (int*)s->jpair.ensure(L.pair.size() * sizeof(int));
     TG_CUDA(cudaMemcpyAsync(pr, L.pair.data(), L.pair.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    // fields resampled on the grid column by column in the Jacobian's
+    // arithmetic type (an FP32 Jacobian casts the fields first), then the
+    // planes of sources and detectors in one buffer; the reference masks the
+    // adjoint gradient for complex data only (jacobian.cc:348-350 against 557)
+    C* gm = (C*)s->io_c.ensure((size_t)r.glen * k * sizeof(C));
+    C* P = (C*)s->gplanes_q.ensure((size_t)k * np * r.slen * sizeof(C));
+    const dim3 mg(cdiv_u(r.glen, 256), cdiv_u(k, MAPC));
+    if constexpr (std::is_same<C, V64>::value) {
+        launch(grid_map_cm_kernel<C, V64>, mg, 256, 0, s->stream, G, n, k, nq, F, A, gm);
+    } else {
+        C* X = (C*)s->tmp.ensure((size_t)k * n * sizeof(C));
+        launch(cast_kernel<C, V64>, cdiv_u((size_t)nq * n, 256), 256, 0, s->stream, (size_t)nq * n, F, X);
+        launch(cast_kernel<C, V64>, cdiv_u((size_t)nm * n, 256), 256, 0, s->stream, (size_t)nm * n, A,
+               X + (size_t)nq * n);
+        launch(grid_map_cm_kernel<C, C>, mg, 256, 0, s->stream, G, n, k, nq, (const C*)X,
+               (const C*)(X + (size_t)nq * n), gm);
+    }
+    launch(grid_planes_cm_kernel<C>, dim3(cdiv_u(r.slen, 256), cdiv_u(k, MAPC)), 256, 0, s->stream, G, k, nq,
+           vt<V64>::cplx ? 1 : 0, (const C*)gm, P);
+    C* ysc = (C*)s->gy.ensure((size_t)nqm * sizeof(C));
+    launch(grid_yscale_kernel<C, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, logscale ? yl : nullptr, -r.voxel(),
+           ysc);
     using JT = typename vt<C>::R;
-    constexpr int GQ = 4;
-    launch(grid_jacobian_kernel<C, JT, GQ>, dim3(gx, cdiv_u(nq, GQ)), 256, 0, s->stream, r.dim, r.slen, nq, nm, nqm,
-           Pq, Pm, (const int*)pr, yinv, r.voxel(), (JT*)Jd);
+    constexpr int GQ = 4, TB = 256;
+    const dim3 jg(cdiv_u(r.slen, TB), cdiv_u(nq, GQ));
+    const C* Pm = P + (size_t)nq * np * r.slen;
+    if (r.dim == 3)
+        launch(grid_jacobian_kernel<C, JT, GQ, 4>, jg, TB, 0, s->stream, r.slen, nq, nm, nqm, (const C*)P, Pm,
+               (const int*)pr, (const C*)ysc, (JT*)Jd);
+    else
+        launch(grid_jacobian_kernel<C, JT, GQ, 3>, jg, TB, 0, s->stream, r.slen, nq, nm, nqm, (const C*)P, Pm,
+               (const int*)pr, (const C*)ysc, (JT*)Jd);
 }
 
 template <class V64, class V32>
@@ -1619,8 +1623,10 @@ static void element_jac_run(tg_solver s, int nq, const V64* F, int nm, const V64
 {
     const MeshDev& m = s->mesh->d;
     const int n = m.n, nqm = (int)L.q.size();
+    int* pr = (int*)s->jpair.ensure(L.pair.size() * sizeof(int));
+    TG_CUDA(cudaMemcpyAsync(pr, L.pair.data(), L.pair.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
     const C *Fc = (const C*)F, *Ac = (const C*)A;
-    if (!std::is_same<C, V64>::value) {
+    if constexpr (!std::is_same<C, V64>::value) {
         C* f = (C*)s->gplanes_q.ensure((size_t)nq * n * sizeof(C));
         C* a = (C*)s->gplanes_m.ensure((size_t)nm * n * sizeof(C));
         launch(cast_kernel<C, V64>, cdiv_u((size_t)nq * n, 256), 256, 0, s->stream, (size_t)nq * n, F, f);
@@ -1628,18 +1634,17 @@ static void element_jac_run(tg_solver s, int nq, const V64* F, int nm, const V64
         Fc = f;
         Ac = a;
     }
-    const C* yinv = nullptr;
-    if (logscale) {
-        C* yc = (C*)s->gy.ensure((size_t)nqm * sizeof(C));
-        launch(grid_yinv_kernel<C, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, yl, yc);
-        yinv = yc;
-    }
-    int* pr = (int*)s->jpair.ensure(L.pair.size() * sizeof(int));
-    TG_CUDA(cudaMemcpyAsync(pr, L.pair.data(), L.pair.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    C* ysc = (C*)s->gy.ensure((size_t)nqm * sizeof(C));
+    launch(grid_yscale_kernel<C, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, logscale ? yl : nullptr, -1.0, ysc);
     using JT = typename vt<C>::R;
-    constexpr int GQ = 4;
-    launch(element_jacobian_kernel<C, JT, GQ>, dim3(cdiv_u(m.ne, 128), cdiv_u(nq, GQ)), 128, 0, s->stream, m, nq, nm,
-           nqm, Fc, Ac, (const int*)pr, yinv, (JT*)Jd);
+    constexpr int GQ = 6, TB = 128;
+    const dim3 eg(cdiv_u(m.ne, TB), cdiv_u(nq, GQ));
+    if (m.dim == 3)
+        launch(element_jacobian_kernel<C, JT, GQ, 4>, eg, TB, 0, s->stream, m, nq, nm, nqm, Fc, Ac, (const int*)pr,
+               (const C*)ysc, (JT*)Jd);
+    else
+        launch(element_jacobian_kernel<C, JT, GQ, 3>, eg, TB, 0, s->stream, m, nq, nm, nqm, Fc, Ac, (const int*)pr,
+               (const C*)ysc, (JT*)Jd);
 }
 
 template <class V64, class V32>
