@@ -96,6 +96,23 @@ int tg_mesh_load(const char *path, tg_mesh *out);
    NULL, its node coordinates (n x dim) and 0-based element nodes (ne x nn) */
 int tg_mesh_geometry(tg_mesh mesh, int *dim, int *nn, double *coords, int *elnodes);
 int tg_mesh_destroy(tg_mesh mesh);
+/* A QM file (QMMesh::LoadQM, src/libfe/qmmesh.cc:319-460): source and
+   detector positions and the link list.  Detector positions of a list not
+   flagged "fixed" are pulled to the mesh boundary as QMMesh::InitM does
+   (Mesh::PullToBoundary, src/libfe/mesh.cc:1052-1111; where no boundary side
+   takes the projection the reference keeps the position, and so does this);
+   fixed positions outside every element are nudged by 1e-4 along an axis
+   (qmmesh.cc:112-127).  "external" lists give TG_ERR_UNSUPPORTED; a dimension
+   other than the mesh's, a missing section or a detector index out of range
+   give TG_ERR_ARG. */
+typedef struct tg_qm_s *tg_qm;
+int tg_qm_load(tg_mesh mesh, const char *path, tg_qm *out);
+int tg_qm_info(tg_qm qm, int *dim, int *nq, int *nm, int *nqm);
+/* Q: nq x dim, M: nm x dim (either may be NULL) */
+int tg_qm_positions(tg_qm qm, double *Q, double *M);
+/* link_ofs: nq + 1 offsets (Qofs), link_m: nqm detector indices (QMref) */
+int tg_qm_links(tg_qm qm, int *link_ofs, int *link_m);
+int tg_qm_destroy(tg_qm qm);
 /* n, ne, nnz of the CSR pattern, number of boundary nodes, IC(0) levels
    (forward and backward sweep depth) */
 int tg_mesh_info(tg_mesh mesh, int *n, int *ne, int *nnz, int *nbnd, int *nlev_fwd, int *nlev_bwd);

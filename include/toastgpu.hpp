@@ -100,6 +100,33 @@ private:
     int n_ = 0, ne_ = 0, nnz_ = 0, dim_ = 0;
 };
 
+// QMMesh::LoadQM (src/libfe/qmmesh.cc:319-460) with InitM's detector
+// placement, against a mesh: positions Q, M (row-major, dim per point) and
+// the link list (nQMref / QMref as offsets and detector indices)
+struct QMData {
+    int dim = 0, nQ = 0, nM = 0, nQM = 0;
+    std::vector<double> Q, M;
+    Links links;
+};
+inline QMData LoadQM(const Mesh& mesh, const char* path)
+{
+    tg_qm h = nullptr;
+    check(tg_qm_load(mesh.handle(), path, &h));
+    QMData d;
+    int rc = tg_qm_info(h, &d.dim, &d.nQ, &d.nM, &d.nQM);
+    if (rc == TG_OK) {
+        d.Q.resize((size_t)d.nQ * d.dim);
+        d.M.resize((size_t)d.nM * d.dim);
+        d.links.ofs.resize(d.nQ + 1);
+        d.links.m.resize(d.nQM);
+        rc = tg_qm_positions(h, d.Q.data(), d.M.data());
+        if (rc == TG_OK) rc = tg_qm_links(h, d.links.ofs.data(), d.links.m.data());
+    }
+    tg_qm_destroy(h);
+    check(rc);
+    return d;
+}
+
 // QVec_Gaussian(mesh, cnt, w, SRCMODE_NEUMANN) for one position: n values
 inline std::vector<double> QVec_Gaussian(const Mesh& mesh, const double* cnt, double w)
 {

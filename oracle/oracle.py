@@ -56,6 +56,8 @@ def lib():
         L.tor_mesh_elsize.argtypes = [C.c_void_p, _dp]
         L.tor_pull_to_boundary.restype = C.c_int
         L.tor_pull_to_boundary.argtypes = [C.c_void_p, _dp, _dp]
+        L.tor_el_found.restype = C.c_int
+        L.tor_el_found.argtypes = [C.c_void_p, _dp]
         L.tor_qvec_gaussian.argtypes = [C.c_void_p, _dp, C.c_double, C.c_int, _dp]
         L.tor_assemble.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, C.c_int, _dp]
         L.tor_solve.restype = C.c_int
@@ -121,6 +123,41 @@ class Mesh:
         if rc:
             raise RuntimeError("PullToBoundary: no boundary side found")
         return out
+
+    def el_found(self, p) -> bool:
+        return bool(lib().tor_el_found(self._h, np.ascontiguousarray(p, np.float64)))
+
+    def place_detectors(self, M, fixed: bool) -> np.ndarray:
+        """QMMesh::InitM's detector positions (qmmesh.cc:105-147): fixed
+        positions outside every element are moved by -1e-4, 0, +1e-4 along
+        each axis in turn until one is inside; the others are pulled to the
+        boundary (Mesh::PullToBoundary, mesh.cc:1052-1111).  When no boundary
+        side takes the projection the reference's fallback writes its result
+        to a local point (mesh.cc:1110), so the position stays as read."""
+        out = []
+        for p in np.asarray(M, np.float64):
+            if fixed:
+                q = p.copy()
+                if not self.el_found(q):
+                    found = False
+                    for d in range(self.dim):
+                        for s in (-1, 0, 1):
+                            q = p.copy()
+                            q[d] += s * 1e-4
+                            if self.el_found(q):
+                                found = True
+                                break
+                        if found:
+                            break
+                    if not found:
+                        raise RuntimeError("no element found to place measurement")
+                out.append(q)
+            else:
+                try:
+                    out.append(self.pull_to_boundary(p))
+                except RuntimeError:
+                    out.append(p.copy())
+        return np.array(out).reshape(-1, self.dim)
 
     def qvec_gaussian(self, cnt, w, neumann=True) -> np.ndarray:
         out = np.zeros(self.n)

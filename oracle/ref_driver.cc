@@ -33,6 +33,10 @@
 //              grid) (src/python/toastmodule.cc:696, raster_px.cc:10-48),
 //              LOG data, written with the raster's element reference per grid
 //              point (PREFIX_Jgrid.bin, PREFIX_elref.bin).
+// qmdump     : with qm, write what QMMesh::LoadQM (qmmesh.cc:319-460, with
+//              InitM's detector placement) made of the file and stop:
+//              PREFIX_qpos.bin, PREFIX_mpos.bin (nQ / nM x dim doubles),
+//              PREFIX_nqmref.bin (nQ int32), PREFIX_qmref.bin (nQM int32)
 #include "stoastlib.h"
 #include <fstream>
 #include <iostream>
@@ -215,6 +219,20 @@ int main(int argc, char** argv) {
     if (g_args.count("qm")) {
         ifstream ifs(arg("qm", "").c_str());
         mesh.LoadQM(ifs);
+        if (atoi(arg("qmdump", "0").c_str())) {
+            const int d = mesh.Dimension();
+            std::vector<double> qp, mp;
+            for (int i = 0; i < mesh.nQ; i++) for (int k = 0; k < d; k++) qp.push_back(mesh.Q[i][k]);
+            for (int i = 0; i < mesh.nM; i++) for (int k = 0; k < d; k++) mp.push_back(mesh.M[i][k]);
+            std::vector<int> nref(mesh.nQMref, mesh.nQMref + mesh.nQ), ref;
+            for (int i = 0; i < mesh.nQ; i++) for (int j = 0; j < mesh.nQMref[i]; j++) ref.push_back(mesh.QMref[i][j]);
+            string out = arg("out", "ref");
+            wbin(out + "_qpos.bin", qp.data(), qp.size() * sizeof(double));
+            wbin(out + "_mpos.bin", mp.data(), mp.size() * sizeof(double));
+            wbin(out + "_nqmref.bin", nref.data(), nref.size() * sizeof(int));
+            wbin(out + "_qmref.bin", ref.data(), ref.size() * sizeof(int));
+            return 0;
+        }
     } else {
         setup_optodes(mesh, arg("optodes", ""));
     }

@@ -1267,6 +1267,16 @@ static int el_gcontains(const tor_mesh *m, int e, const double *p)
     return l[0] + EPS >= 0.0 && l[1] + EPS >= 0.0 && l[2] + EPS >= 0.0 && l[0] + l[1] + l[2] - EPS <= 1.0;
 }
 
+/* Whether any element contains p (Mesh::ElFind, mesh.cc:248-290, searches
+   from the last element found; whether one is found does not depend on the
+   search order) */
+int tor_el_found(const tor_mesh *m, const double *p)
+{
+    for (int e = 0; e < m->ne; e++)
+        if (el_gcontains(m, e, p)) return 1;
+    return 0;
+}
+
 /* Raster_Pixel with the grid equal to the basis (raster.cc:18-83,
    raster_px.cc:10-48, the case bdim == gdim):
    - bounding box: Mesh::BoundingBox (mesh.cc:1341-1360), no padding;

@@ -20,6 +20,12 @@ The *_el fixtures reset the solver in the element basis (one mua, mus',
 nref per element, seeded) and hold the reference's system matrix, fields,
 projections and element-basis Jacobian.
 
+The qm_* fixtures hold a QM file written here (seeded positions off the
+boundary, sparse link lists, normals on some lines), its mesh, and what the
+reference's QMMesh::LoadQM made of them: source positions, detector
+positions after InitM's placement (pulled to the boundary, or fixed and
+nudged into an element) and the link list.
+
 Usage:  make -f oracle/Makefile.ref REF=<reference tree> -j8
         python tests/golden/make_golden.py [fixture names]
 """
@@ -175,12 +181,101 @@ def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradi
     print(name, "n", P.n, "links", len(res["proj"]), "its", res["it_fwd"], res["it_adj"])
 
 
+def qm_text(P, Q, M, links, mflag, seed):
+    """A QM file as QMMesh::LoadQM reads it (qmmesh.cc:319-460): every other
+    position line also carries a normal, which the reader parses and drops
+    for non-external lists."""
+    rng = np.random.default_rng(seed)
+    dim = P.dim
+    out = [f"QM file {dim}D", f"Dimension {dim}", "", f"SourceList {len(Q)}"]
+    for i, p in enumerate(Q):
+        vals = list(p) + (list(rng.standard_normal(dim)) if i % 2 else [])
+        out.append(" ".join(repr(float(v)) for v in vals))
+    out += ["", f"MeasurementList {len(M)}" + (" " + mflag if mflag else "")]
+    for i, p in enumerate(M):
+        vals = list(p) + (list(rng.standard_normal(dim)) if i % 2 == 0 else [])
+        out.append(" ".join(repr(float(v)) for v in vals))
+    out += ["", "LinkList"]
+    for ms in links:
+        out.append(f"{len(ms)}: " + " ".join(str(m) for m in ms))
+    return "\n".join(out) + "\n"
+
+
+def _radial(P, pts, dr):
+    """Points moved by dr along their radius in the cross-section."""
+    pts = np.array(pts, float)
+    r = np.linalg.norm(pts[:, :2], axis=1, keepdims=True)
+    pts[:, :2] *= (r + dr[:, None]) / r
+    return pts
+
+
+def qm_case(kind):
+    """Problem and QM text of a QM fixture: detectors pulled to the boundary
+    (2D and 3D) or at fixed positions just inside (or, one of them, 5e-5
+    outside) the boundary; sparse link lists with a source without links."""
+    rng = np.random.default_rng({"qm_disc_pull": 31, "qm_cyl_pull": 32, "qm_disc_fixed": 33}[kind])
+    P = workloads.disc(8, 3, 0.0, 6) if kind.startswith("qm_disc") else small_cylinder(0.0, nopt=6)
+    nq, nm = len(P.qm.Q), len(P.qm.M)
+    Q = _radial(P, P.qm.Q, rng.uniform(-0.3, 0.3, nq))
+    if kind == "qm_disc_fixed":
+        # midpoints of boundary edges (edges of one triangle only), moved
+        # inward 1e-3 (the last 5e-5 outward)
+        cnt = {}
+        for t in P.elems:
+            for a, b in ((t[0], t[1]), (t[1], t[2]), (t[2], t[0])):
+                k = (min(a, b), max(a, b))
+                cnt[k] = cnt.get(k, 0) + 1
+        edges = [k for k, c in cnt.items() if c == 1]
+        mids = np.array([0.5 * (P.coords[a] + P.coords[b]) for a, b in edges])
+        order = np.argsort(np.arctan2(mids[:, 1], mids[:, 0]))
+        M = mids[order[np.linspace(0, len(order) - 1, nm, endpoint=False).astype(int)]]
+        M = _radial(P, np.array(M), np.array([-1e-3] * (nm - 1) + [5e-5]))
+        flag = "fixed"
+    else:
+        M = _radial(P, P.qm.M, rng.uniform(-0.4, 0.4, nm))
+        flag = ""
+    links = []
+    for q in range(nq):
+        if q == 1:
+            links.append([])
+        else:
+            ms = [m for m in range(nm) if q == 0 or rng.uniform() < 0.7]
+            links.append(ms)
+    return P, qm_text(P, Q, M, links, flag, rng.integers(1 << 30))
+
+
+def run_qm(name):
+    P, text = qm_case(name)
+    with tempfile.TemporaryDirectory() as td:
+        msh = os.path.join(td, "m.msh")
+        meshio.write_mesh(msh, P.coords, P.elems)
+        qmf = os.path.join(td, "f.qm")
+        with open(qmf, "w") as f:
+            f.write(text)
+        out = os.path.join(td, "r")
+        subprocess.run([DRIVER, f"mesh={msh}", f"qm={qmf}", f"out={out}", "qmdump=1"], check=True)
+        qpos = rd(out + "_qpos.bin", np.float64).reshape(-1, P.dim)
+        mpos = rd(out + "_mpos.bin", np.float64).reshape(-1, P.dim)
+        nref = rd(out + "_nqmref.bin", np.int32)
+        qmref = rd(out + "_qmref.bin", np.int32)
+    ofs = np.concatenate([[0], np.cumsum(nref)]).astype(np.int32)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), coords=P.coords, elems=P.elems, qm_text=text,
+                        qpos=qpos, mpos=mpos, link_ofs=ofs, link_m=qmref)
+    print(name, "nQ", len(qpos), "nM", len(mpos), "nQM", len(qmref))
+
+
+QM_FIXTURES = ("qm_disc_pull", "qm_cyl_pull", "qm_disc_fixed")
+
+
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("build the reference driver first: make -f oracle/Makefile.ref REF=<reference tree>")
-    names = sys.argv[1:] or list(FIXTURES)
+    names = sys.argv[1:] or list(FIXTURES) + list(QM_FIXTURES)
     for name in names:
-        run(name, *FIXTURES[name])
+        if name in QM_FIXTURES:
+            run_qm(name)
+        else:
+            run(name, *FIXTURES[name])
 
 
 if __name__ == "__main__":

@@ -9,10 +9,29 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def names(nodal_only=False):
-    """Fixture names; nodal_only drops the element-basis fixtures (*_el), whose
-    solves use one coefficient per element."""
+    """Forward-path fixture names (not the QM-file ones); nodal_only drops the
+    element-basis fixtures (*_el), whose solves use one coefficient per
+    element."""
     out = sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    out = [n for n in out if not n.startswith("qm_")]
     return [n for n in out if not n.endswith("_el")] if nodal_only else out
+
+
+def qm_names():
+    """The QM-file fixtures: a QM text, its mesh and what the reference's
+    LoadQM made of them (positions after InitM, link list)."""
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "qm_*.npz")))
+
+
+def load_qm(name, tmp_path):
+    """(fixture dict, path of its QM text written under tmp_path)."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d = {k: z[k] for k in z.files}
+    d["qm_text"] = str(d["qm_text"])
+    path = os.path.join(str(tmp_path), name + ".qm")
+    with open(path, "w") as f:
+        f.write(d["qm_text"])
+    return d, path
 
 
 def load(name):

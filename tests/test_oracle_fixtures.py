@@ -5,7 +5,7 @@ the reference's own test data, so these fixtures are what pin it."""
 import numpy as np
 import pytest
 
-from tests.golden_util import load, names
+from tests.golden_util import load, load_qm, names, qm_names
 from tests.gpu_util import rel2, relmax
 
 
@@ -92,3 +92,19 @@ def test_oracle_raster_maps_match_reference(oracle_mod, name):
     maps = oracle_mod.raster_maps(mesh, g["bdim"], g["mua"], np.arange(1, slen + 1, dtype=float))
     for a, key in zip(maps, ("m2g", "m2s", "s2m", "g2m")):
         assert np.array_equal(a, g["map_" + key]), key
+
+
+@pytest.mark.parametrize("name", qm_names())
+def test_oracle_qm_placement_matches_reference(oracle_mod, name, tmp_path):
+    """The QM file parsed (meshio.read_qm) and the detectors placed as InitM
+    places them (pulled to the boundary, or fixed and nudged into an
+    element) equal what the compiled reference's LoadQM made, bit for bit.
+    qm_disc_pull has two detectors whose projection no boundary side takes:
+    the reference keeps them where they were read."""
+    from toastpp_gb300 import meshio
+    g, path = load_qm(name, tmp_path)
+    qm = meshio.read_qm(path)
+    mesh = oracle_mod.Mesh(g["coords"], g["elems"])
+    assert np.array_equal(qm.Q, g["qpos"])
+    assert np.array_equal(mesh.place_detectors(qm.M, qm.m_fixed), g["mpos"])
+    assert np.array_equal(qm.link_ofs, g["link_ofs"]) and np.array_equal(qm.link_m, g["link_m"])

@@ -63,7 +63,7 @@ def problem(dim, oracle_mod):
         coords, els = meshio.read_mesh(os.path.join(T, f"{dim}D", "meshes", msh))
         qm = meshio.read_qm(os.path.join(T, f"{dim}D", "meshes", qmf))
         mesh = oracle_mod.Mesh(coords, els)
-        M = qm.M if qm.m_fixed else np.stack([mesh.pull_to_boundary(p) for p in qm.M])
+        M = mesh.place_detectors(qm.M, qm.m_fixed)
         _problems[dim] = (mesh, qm, M)
     return _problems[dim]
 

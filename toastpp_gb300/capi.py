@@ -22,11 +22,14 @@ PRECONS = {"NONE": 0, "DIAG": 1, "ICH": 2, "DILU": 3}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 MEM_HOST, MEM_DEVICE = 0, 1
 DATA_LIN, DATA_LOG = 1, 2
+# status codes (toastgpu.h)
+ERR_ARG, ERR_STATE, ERR_CUDA, ERR_NOMEM, ERR_UNSUPPORTED, ERR_BREAKDOWN = 1, 2, 3, 4, 5, 6
 
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
            "tg_qvec_gaussian", "tg_qvec_gaussian_ex", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream", "tg_solver_set_output_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
            "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_solver_reset_basis", "tg_jacobian_el", "tg_mesh_load", "tg_mesh_geometry", "tg_gradient", "tg_raster_create", "tg_raster_destroy", "tg_raster_map", "tg_raster_info", "tg_raster_elref", "tg_jacobian_grid",
+           "tg_qm_load", "tg_qm_info", "tg_qm_positions", "tg_qm_links", "tg_qm_destroy",
            "tg_server_create", "tg_server_destroy", "tg_submit", "tg_poll", "tg_wait", "tg_server_stats",
            "tg_server_reset_stats", "tg_last_error"]
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = range(4)
@@ -97,6 +100,11 @@ def lib():
             "tg_jacobian_el": [vp, i_, dp, i_, dp, dp, vp, vp, i_, vp, i_, i_],
             "tg_raster_create": [vp, ip, C.POINTER(C.c_void_p)],
             "tg_raster_destroy": [vp],
+            "tg_qm_load": [vp, C.c_char_p, C.POINTER(C.c_void_p)],
+            "tg_qm_info": [vp, ip, ip, ip, ip],
+            "tg_qm_positions": [vp, vp, vp],
+            "tg_qm_links": [vp, vp, vp],
+            "tg_qm_destroy": [vp],
             "tg_raster_info": [vp, ip, ip, dp, dp],
             "tg_raster_elref": [vp, ip],
             "tg_raster_map": [vp, C.c_char_p, i_, vp, vp, i_, i_],
@@ -444,6 +452,26 @@ def optical_coefficients(mua, mus, nref):
 def omega_of(freq_mhz):
     """Modulation frequency [MHz] -> omega [rad/ps] (src/supertoast/fwdfem.cc:116)."""
     return freq_mhz * 2.0 * np.pi * 1e-6
+
+
+class QM:
+    """tg_qm_load: a QM file read against a mesh (QMMesh::LoadQM with
+    InitM's detector placement).  Q, M: positions; links: the link list."""
+
+    def __init__(self, mesh: Mesh, path: str):
+        h = C.c_void_p()
+        _check(lib().tg_qm_load(mesh._h, os.fsencode(path), C.byref(h)))
+        try:
+            d, nq, nm, nqm = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+            _check(lib().tg_qm_info(h, C.byref(d), C.byref(nq), C.byref(nm), C.byref(nqm)))
+            self.Q = np.zeros((nq.value, d.value))
+            self.M = np.zeros((nm.value, d.value))
+            _check(lib().tg_qm_positions(h, _ptr(self.Q), _ptr(self.M)))
+            ofs, lm = np.zeros(nq.value + 1, np.int32), np.zeros(nqm.value, np.int32)
+            _check(lib().tg_qm_links(h, _ptr(ofs), _ptr(lm)))
+            self.links = Links(ofs, lm)
+        finally:
+            lib().tg_qm_destroy(h)
 
 
 class Raster:

@@ -563,4 +563,146 @@ void qvec_gaussian_host(const MeshHost& m, const double* cnt, double w, bool neu
     }
 }
 
+// Element_Unstructured::GContains (element.cc:553-563): the element's bounding
+// box widened by 1e-8, then LContains(Local(p)) with the padded test
+// (tri3.cc:134-144 / 191-200, tet4.cc:186-196 / 268-279)
+bool el_gcontains(const MeshHost& m, int e, const double* p)
+{
+    const int dim = m.dim, nn = m.nn;
+    const int* nd = &m.el[(size_t)e * nn];
+    for (int d = 0; d < dim; d++) {
+        double lo = 1e10, hi = -1e10;
+        for (int i = 0; i < nn; i++) {
+            const double v = m.coords[(size_t)nd[i] * dim + d];
+            lo = std::min(lo, v);
+            hi = std::max(hi, v);
+        }
+        if (p[d] < lo - 1e-8 || p[d] > hi + 1e-8) return false;
+    }
+    const double* g = &m.geo[(size_t)e * 16];
+    const double EPS = 1e-8;
+    if (dim == 2) {
+        const double scale = 1.0 / (g[0] + g[1] + g[2]);
+        const double l0 = (g[1] + g[4] * p[0] + g[7] * p[1]) * scale;
+        const double l1 = (g[2] + g[5] * p[0] + g[8] * p[1]) * scale;
+        return l0 + EPS >= 0.0 && l1 + EPS >= 0.0 && l0 + l1 - EPS <= 1.0;
+    }
+    const double *a = g, *b = g + 4, *c = g + 8, *dd = g + 12;
+    const double scale = 1.0 / (a[0] + a[1] + a[2] + a[3]);
+    double l[3];
+    for (int r = 0; r < 3; r++) l[r] = (a[r + 1] + b[r + 1] * p[0] + c[r + 1] * p[1] + dd[r + 1] * p[2]) * scale;
+    return l[0] + EPS >= 0.0 && l[1] + EPS >= 0.0 && l[2] + EPS >= 0.0 && l[0] + l[1] + l[2] - EPS <= 1.0;
+}
+
+
+// Mesh::PullToBoundary (mesh.cc:1052-1111) with sub = 0 for P1 elements: the
+// boundary node nearest p (the first of equal distance), then the elements
+// around it in order; in each, the sides whose nodes are all boundary nodes
+// (Element::BndSideList, element.cc:338-348) in side order: p in the
+// element's local coordinates (Triangle3::Local, tri3.cc:134-144;
+// Tetrahedron4::Local, tet4.cc:186-196) is projected along the side's local
+// normal (LNormal, tri3.cc:172-182, tet4.cc:254-266, the reference's
+// truncated constants) and the first projection inside the element
+// (LContains with padding, tri3.cc:191-200, tet4.cc:268-279) is mapped back
+// (Element::Global, element.cc:164-176).  Returns false when none is.
+static bool pull_to_boundary(const MeshHost& m, const double* p, double* out)
+{
+    const int dim = m.dim, nn = m.nn;
+    int nmin = -1;
+    double dmin = 1e10;
+    for (int k = 0; k < m.n; k++) {
+        if (!m.bndnode[k]) continue;
+        const double d = dist(p, &m.coords[(size_t)k * dim], dim);
+        if (d < dmin) {
+            dmin = d;
+            nmin = k;
+        }
+    }
+    static const double LN2[3][2] = {{0, -1}, {0.7071067814, 0.7071067814}, {-1, 0}};
+    static const double LN3[4][3] = {{0, 0, -1}, {0, -1, 0}, {-1, 0, 0}, {0.577350269, 0.577350269, 0.577350269}};
+    const int nside = dim == 2 ? 3 : 4, nsn = dim == 2 ? 2 : 3;
+    for (int e = 0; e < m.ne && nmin >= 0; e++) {
+        const int* nd = &m.el[(size_t)e * nn];
+        bool has = false;
+        for (int i = 0; i < nn; i++) has |= nd[i] == nmin;
+        if (!has) continue;
+        const double* g = &m.geo[(size_t)e * 16];
+        // local coordinates of a global point
+        auto local = [&](const double* x, double* l) {
+            if (dim == 2) {
+                const double scale = 1.0 / (g[0] + g[1] + g[2]);
+                l[0] = (g[1] + g[4] * x[0] + g[7] * x[1]) * scale;
+                l[1] = (g[2] + g[5] * x[0] + g[8] * x[1]) * scale;
+            } else {
+                const double *a = g, *b = g + 4, *c = g + 8, *d = g + 12;
+                const double scale = 1.0 / (a[0] + a[1] + a[2] + a[3]);
+                for (int r = 0; r < 3; r++) l[r] = (a[r + 1] + b[r + 1] * x[0] + c[r + 1] * x[1] + d[r + 1] * x[2]) * scale;
+            }
+        };
+        for (int sd = 0; sd < nside; sd++) {
+            bool bnd = true;
+            for (int k = 0; k < nsn && bnd; k++)
+                if (!m.bndnode[nd[dim == 2 ? TRI_SIDE[sd][k] : TET_SIDE[sd][k]]]) bnd = false;
+            if (!bnd) continue;
+            const double* ln = dim == 2 ? LN2[sd] : LN3[sd];
+            double ploc[3], nloc[3], l[3];
+            local(p, ploc);
+            local(&m.coords[(size_t)nd[dim == 2 ? TRI_SIDE[sd][0] : TET_SIDE[sd][0]] * dim], nloc);
+            double pd = 0.0;
+            for (int r = 0; r < dim; r++) pd += (ploc[r] - nloc[r]) * ln[r];
+            for (int r = 0; r < dim; r++) l[r] = ploc[r] - ln[r] * pd;
+            const double EPS = 1e-8;
+            bool in = true;
+            double sum = 0.0;
+            for (int r = 0; r < dim; r++) {
+                in = in && l[r] + EPS >= 0.0;
+                sum = r ? sum + l[r] : l[r];
+            }
+            if (!in || sum - EPS > 1.0) continue;
+            double u[4];
+            u[0] = dim == 2 ? 1.0 - l[0] - l[1] : 1.0 - l[0] - l[1] - l[2];
+            for (int r = 0; r < dim; r++) u[r + 1] = l[r];
+            for (int c = 0; c < dim; c++) {
+                double v = 0.0;
+                for (int j = 0; j < nn; j++) v += u[j] * m.coords[(size_t)nd[j] * dim + c];
+                out[c] = v;
+            }
+            return true;
+        }
+    }
+    return false;
+}
+
+bool el_found(const MeshHost& m, const double* p)
+{
+    for (int e = 0; e < m.ne; e++)
+        if (el_gcontains(m, e, p)) return true;
+    return false;
+}
+
+bool qm_place_detector(const MeshHost& m, bool fixed, double* p)
+{
+    if (!fixed) {
+        // when no side takes the projection, the reference's fallback
+        // (PullToBoundary_old) writes to a local point (mesh.cc:1110): the
+        // position stays as read
+        double q[3];
+        if (pull_to_boundary(m, p, q))
+            for (int c = 0; c < m.dim; c++) p[c] = q[c];
+        return true;
+    }
+    // a fixed position outside every element moves by -1e-4, 0, +1e-4 along
+    // each axis in turn until an element contains it (qmmesh.cc:112-127)
+    if (el_found(m, p)) return true;
+    double p0[3] = {p[0], p[1], m.dim > 2 ? p[2] : 0.0};
+    const double eps = 1e-4;
+    for (int d = 0; d < m.dim; d++)
+        for (int s = -1; s <= 1; s++) {
+            for (int c = 0; c < m.dim; c++) p[c] = p0[c];
+            p[d] += s * eps;
+            if (el_found(m, p)) return true;
+        }
+    return false;
+}
+
 }  // namespace tg

@@ -96,5 +96,12 @@ struct Mesh {
 
 Mesh* mesh_build(int dim, int n, const double* coords, int ne, const int* el);
 void qvec_gaussian_host(const MeshHost& m, const double* cnt, double w, bool neumann, double* q);
+// Element_Unstructured::GContains for element e (padded bounding box, then
+// the padded local test)
+bool el_gcontains(const MeshHost& m, int e, const double* p);
+// QMMesh::InitM's placement of a detector read from a QM file (fixed: kept,
+// or nudged into an element; else pulled to the boundary); false if a fixed
+// position lies in no element
+bool qm_place_detector(const MeshHost& m, bool fixed, double* p);
 
 }  // namespace tg

@@ -9,7 +9,9 @@
 #include <map>
 #include <memory>
 #include <tuple>
+#include <fstream>
 #include <mutex>
+#include <sstream>
 #include <vector>
 
 #include "../../include/toastgpu.h"
@@ -815,37 +817,6 @@ struct tg_raster_s {
 };
 
 namespace {
-
-// Element_Unstructured::GContains (element.cc:553-563): the element's bounding
-// box widened by 1e-8, then LContains(Local(p)) with the padded test
-// (tri3.cc:134-144 / 191-200, tet4.cc:186-196 / 268-279)
-bool el_gcontains(const MeshHost& m, int e, const double* p)
-{
-    const int dim = m.dim, nn = m.nn;
-    const int* nd = &m.el[(size_t)e * nn];
-    for (int d = 0; d < dim; d++) {
-        double lo = 1e10, hi = -1e10;
-        for (int i = 0; i < nn; i++) {
-            const double v = m.coords[(size_t)nd[i] * dim + d];
-            lo = std::min(lo, v);
-            hi = std::max(hi, v);
-        }
-        if (p[d] < lo - 1e-8 || p[d] > hi + 1e-8) return false;
-    }
-    const double* g = &m.geo[(size_t)e * 16];
-    const double EPS = 1e-8;
-    if (dim == 2) {
-        const double scale = 1.0 / (g[0] + g[1] + g[2]);
-        const double l0 = (g[1] + g[4] * p[0] + g[7] * p[1]) * scale;
-        const double l1 = (g[2] + g[5] * p[0] + g[8] * p[1]) * scale;
-        return l0 + EPS >= 0.0 && l1 + EPS >= 0.0 && l0 + l1 - EPS <= 1.0;
-    }
-    const double *a = g, *b = g + 4, *c = g + 8, *dd = g + 12;
-    const double scale = 1.0 / (a[0] + a[1] + a[2] + a[3]);
-    double l[3];
-    for (int r = 0; r < 3; r++) l[r] = (a[r + 1] + b[r + 1] * p[0] + c[r + 1] * p[1] + dd[r + 1] * p[2]) * scale;
-    return l[0] + EPS >= 0.0 && l[1] + EPS >= 0.0 && l[2] + EPS >= 0.0 && l[0] + l[1] + l[2] - EPS <= 1.0;
-}
 
 // bounding box (Mesh::BoundingBox, mesh.cc:1341-1360), element per grid
 // point (GenerateElementPixelRef, mesh.cc:2944-3014: elements in order, each
@@ -1920,6 +1891,146 @@ int tg_mesh_destroy(tg_mesh mesh)
 {
     API_BEGIN
     delete mesh;
+    API_END
+}
+
+// QMMesh::LoadQM (src/libfe/qmmesh.cc:319-460) with InitM's detector
+// placement (105-147): the header "QM file", "Dimension d" (the mesh's), a
+// SourceList and a MeasurementList (count, optional "fixed" / "external" and
+// normal flags, then one line per position, normals parsed and dropped) and a
+// LinkList ("count: detector ..." per source).  Detector positions of a
+// non-fixed list are pulled to the boundary.
+struct tg_qm_s {
+    int dim = 0, nq = 0, nm = 0;
+    std::vector<double> Q, M;
+    std::vector<int> ofs, lm;
+};
+
+namespace {
+
+// the section header line starting with tag, its count and flags
+void qm_section(std::istream& is, const char* tag, int& count, bool& fixed)
+{
+    std::string line;
+    const size_t tl = strlen(tag);
+    bool ok = false;
+    while (std::getline(is, line))
+        if (line.compare(0, tl, tag) == 0) {
+            ok = true;
+            break;
+        }
+    TG_CHECK(ok, TG_ERR_ARG, std::string("QM file: ") + tag + " not found");
+    std::istringstream h(line.substr(tl));
+    TG_CHECK(bool(h >> count) && count >= 0, TG_ERR_ARG, std::string("QM file: no count after ") + tag);
+    std::string flag;
+    fixed = false;
+    if (h >> flag) {
+        std::string f = flag;
+        for (auto& c : f) c = (char)tolower((unsigned char)c);
+        TG_CHECK(f != "external", TG_ERR_UNSUPPORTED, "QM file: external positions are not supported");
+        fixed = f == "fixed";
+    }
+}
+
+void qm_positions(std::istream& is, int count, int dim, std::vector<double>& out, const char* what)
+{
+    std::string line;
+    for (int i = 0; i < count; i++) {
+        TG_CHECK(bool(std::getline(is, line)), TG_ERR_ARG, std::string("QM file: truncated ") + what);
+        double v[6];
+        const int k = dim == 2 ? sscanf(line.c_str(), "%lf%lf%lf%lf", v, v + 1, v + 2, v + 3)
+                               : sscanf(line.c_str(), "%lf%lf%lf%lf%lf%lf", v, v + 1, v + 2, v + 3, v + 4, v + 5);
+        TG_CHECK(k >= dim, TG_ERR_ARG, std::string("QM file: parse error in the ") + what);
+        out.insert(out.end(), v, v + dim);
+    }
+}
+
+}  // namespace
+
+int tg_qm_load(tg_mesh mesh, const char* path, tg_qm* out)
+{
+    API_BEGIN
+    TG_CHECK(mesh && path && out, TG_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    std::ifstream is(path);
+    TG_CHECK(is.good(), TG_ERR_ARG, std::string("cannot open QM file ") + path);
+    const MeshHost& m = mesh->m->h;
+    std::string line;
+    TG_CHECK(std::getline(is, line) && line.compare(0, 7, "QM file") == 0, TG_ERR_ARG,
+             "QM file not found or invalid format");
+    int dim = 0;
+    TG_CHECK(std::getline(is, line) && line.compare(0, 9, "Dimension") == 0 &&
+                 sscanf(line.c_str() + 9, "%d", &dim) == 1,
+             TG_ERR_ARG, "QM file: no Dimension line");
+    TG_CHECK(dim == m.dim, TG_ERR_ARG, "QM dimension does not match mesh");
+    std::unique_ptr<tg_qm_s> q(new tg_qm_s);
+    q->dim = dim;
+    bool qfixed = false, mfixed = false;
+    qm_section(is, "SourceList", q->nq, qfixed);
+    qm_positions(is, q->nq, dim, q->Q, "source list");
+    qm_section(is, "MeasurementList", q->nm, mfixed);
+    qm_positions(is, q->nm, dim, q->M, "measurement list");
+    bool ok = false;
+    while (std::getline(is, line))
+        if (line.compare(0, 8, "LinkList") == 0) {
+            ok = true;
+            break;
+        }
+    TG_CHECK(ok, TG_ERR_ARG, "QM file: LinkList not found");
+    q->ofs.assign(1, 0);
+    for (int i = 0; i < q->nq; i++) {
+        int cnt = -1;
+        TG_CHECK(bool(is >> cnt) && cnt >= 0, TG_ERR_ARG, "QM file: bad link count");
+        char c = 0;
+        while (is.get(c) && c != ':') {}
+        TG_CHECK(c == ':', TG_ERR_ARG, "QM file: truncated LinkList");
+        for (int j = 0; j < cnt; j++) {
+            int md = -1;
+            TG_CHECK(bool(is >> md) && md >= 0 && md < q->nm, TG_ERR_ARG, "QM file: bad detector index in LinkList");
+            q->lm.push_back(md);
+        }
+        q->ofs.push_back((int)q->lm.size());
+    }
+    for (int i = 0; i < q->nm; i++)
+        TG_CHECK(qm_place_detector(m, mfixed, &q->M[(size_t)i * dim]), TG_ERR_ARG,
+                 "QM file: no element found to place measurement " + std::to_string(i));
+    *out = q.release();
+    API_END
+}
+
+int tg_qm_info(tg_qm qm, int* dim, int* nq, int* nm, int* nqm)
+{
+    API_BEGIN
+    TG_CHECK(qm, TG_ERR_ARG, "qm is NULL");
+    if (dim) *dim = qm->dim;
+    if (nq) *nq = qm->nq;
+    if (nm) *nm = qm->nm;
+    if (nqm) *nqm = (int)qm->lm.size();
+    API_END
+}
+
+int tg_qm_positions(tg_qm qm, double* Q, double* M)
+{
+    API_BEGIN
+    TG_CHECK(qm, TG_ERR_ARG, "qm is NULL");
+    if (Q) std::copy(qm->Q.begin(), qm->Q.end(), Q);
+    if (M) std::copy(qm->M.begin(), qm->M.end(), M);
+    API_END
+}
+
+int tg_qm_links(tg_qm qm, int* link_ofs, int* link_m)
+{
+    API_BEGIN
+    TG_CHECK(qm, TG_ERR_ARG, "qm is NULL");
+    if (link_ofs) std::copy(qm->ofs.begin(), qm->ofs.end(), link_ofs);
+    if (link_m) std::copy(qm->lm.begin(), qm->lm.end(), link_m);
+    API_END
+}
+
+int tg_qm_destroy(tg_qm qm)
+{
+    API_BEGIN
+    delete qm;
     API_END
 }
 
