@@ -345,8 +345,10 @@ def run_gpu(args):
     shares = {names[c]: {"ms_per_step": prof[c][0] / psteps, "launches_or_scopes": prof[c][1] // psteps}
               for c in prof}
 
-    # ---- grid-basis Jacobian (pixel raster, basis = grid) on this request's
-    # fields, device-resident, timed alone with CUDA events
+    # ---- grid-basis Jacobian (pixel raster, basis = grid) and, with
+    # --element, the element-basis Jacobian on this request's fields,
+    # device-resident, each timed alone with CUDA events (mean of reps calls
+    # after 3 untimed ones)
     def event_ms(fn, reps=5):
         for _ in range(3):
             fn()
