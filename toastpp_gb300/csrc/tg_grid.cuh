@@ -208,6 +208,30 @@ __global__ void grid_yscale_kernel(int nqm, const V64* __restrict__ y, double sc
 __device__ __forceinline__ void st_stream(float* p, float v) { __stcs(p, v); }
 __device__ __forceinline__ void st_stream(double* p, double v) { __stcs(p, v); }
 
+// The links of a block's GQ sources for LT detectors at a time, in shared
+// memory: the link index (or -1) and its factor, read by every thread of the
+// block from there instead of from the pair table and the factor array
+// (element_jacobian_kernel: 4.10 -> 3.76 ms on the 3D cylinder; the grid
+// kernel, at 80 registers with it, lost as much at 48^3 as it gained at 32^3).
+constexpr int LT = 64;
+template <class V, int GQ>
+struct LinkTile {
+    int l[GQ][LT];
+    V y[GQ][LT];
+    // detectors m0 .. m0 + LT - 1 of sources q0 .. q0 + GQ - 1; the caller
+    // syncs the block before (the previous tile's readers) and after
+    __device__ __forceinline__ void fill(int m0, int q0, int nq, int nm, const int* __restrict__ pair,
+                                         const V* __restrict__ ysc)
+    {
+        for (int i = threadIdx.x; i < GQ * LT; i += blockDim.x) {
+            const int g = i / LT, j = i % LT, m = m0 + j;
+            const int k = (m < nm && q0 + g < nq) ? pair[(size_t)(q0 + g) * nm + m] : -1;
+            l[g][j] = k;
+            y[g][j] = k >= 0 ? ysc[k] : vzero<V>();
+        }
+    }
+};
+
 // One thread per (solution point, group of GQ sources): the sources' planes
 // stay in registers while the detectors' planes stream past, each loaded once
 // per group, the next detector's while this one's entries form.  PMDF_mua =
@@ -292,8 +316,11 @@ __global__ void __launch_bounds__(256) element_jacobian_kernel(MeshDev m, int nq
                                                                const int* __restrict__ pair,
                                                                const V* __restrict__ ysc, JT* __restrict__ J)
 {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x, q0 = blockIdx.y * GQ;
-    if (e >= m.ne) return;
+    __shared__ LinkTile<V, GQ> tile;
+    const int q0 = blockIdx.y * GQ;
+    // threads past ne take part in the tile fills only
+    const bool act = blockIdx.x * blockDim.x + threadIdx.x < m.ne;
+    const int e = min((int)(blockIdx.x * blockDim.x + threadIdx.x), m.ne - 1);
     using R = typename vt<V>::R;
     const int n = m.n;
     const int* nd = m.el + (size_t)e * NN;
@@ -321,20 +348,22 @@ __global__ void __launch_bounds__(256) element_jacobian_kernel(MeshDev m, int nq
 #pragma unroll
     for (int j = 0; j < NN; j++) an[j] = A[node[j]];
     for (int mm = 0; mm < nm; mm++) {
+        const int jt = mm % LT;
+        if (jt == 0) {
+            __syncthreads();
+            tile.fill(mm, q0, nq, nm, pair, ysc);
+            __syncthreads();
+        }
         V a[NN];
 #pragma unroll
         for (int j = 0; j < NN; j++) {
             a[j] = an[j];
             if (mm + 1 < nm) an[j] = A[(size_t)(mm + 1) * n + node[j]];
         }
-        int lk[GQ];
         bool any = false;
 #pragma unroll
-        for (int g = 0; g < GQ; g++) {
-            lk[g] = q0 + g < nq ? pair[(size_t)(q0 + g) * nm + mm] : -1;
-            any |= lk[g] >= 0;
-        }
-        if (!any) continue;
+        for (int g = 0; g < GQ; g++) any |= tile.l[g][jt] >= 0;
+        if (!any || !act) continue;
         V hm[NN], hk[NN];
         V sa = vzero<V>();
 #pragma unroll
@@ -348,7 +377,7 @@ __global__ void __launch_bounds__(256) element_jacobian_kernel(MeshDev m, int nq
         }
 #pragma unroll
         for (int g = 0; g < GQ; g++) {
-            const int l = lk[g];
+            const int l = tile.l[g][jt];
             if (l < 0) continue;
             V pm = vmul(f[g][0], hm[0]), pk = vmul(f[g][0], hk[0]);
 #pragma unroll
@@ -356,7 +385,7 @@ __global__ void __launch_bounds__(256) element_jacobian_kernel(MeshDev m, int nq
                 pm = vfma(pm, f[g][i], hm[i]);
                 pk = vfma(pk, f[g][i], hk[i]);
             }
-            const V y = ysc[l];
+            const V y = tile.y[g][jt];
             pm = vmul(pm, y);
             pk = vmul(pk, y);
             JT* r0 = J + (size_t)l * cols;
