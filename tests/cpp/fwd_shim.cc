@@ -10,9 +10,14 @@
 //        nq*dim source positions ; nm*dim detector positions
 //   OUT: nQM logproj values, then the Jacobian (doubles; complex interleaved),
 //        then the grid-basis Jacobian of Raster_Pixel(12 points per axis)
+//
+//   fwd_shim qm MESH QMFILE OUT
+//   reads a mesh file and a QM file through the face (Mesh(path), LoadQM) and
+//   writes int32 dim, nQ, nM, nQM ; Q ; M (doubles) ; link offsets ; detectors
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <string>
 #include <vector>
 
 #include "toastgpu.hpp"
@@ -63,9 +68,26 @@ static int run(int dim, int n, int nq, int nm, double omega, double width, const
     return 0;
 }
 
+static int qm_main(const char* meshf, const char* qmf, const char* outf)
+{
+    Mesh mesh(meshf);
+    QMData qm = LoadQM(mesh, qmf);
+    FILE* o = fopen(outf, "wb");
+    if (!o) return 2;
+    const int hdr[4] = {qm.dim, qm.nQ, qm.nM, qm.nQM};
+    fwrite(hdr, sizeof(int), 4, o);
+    fwrite(qm.Q.data(), sizeof(double), qm.Q.size(), o);
+    fwrite(qm.M.data(), sizeof(double), qm.M.size(), o);
+    fwrite(qm.links.ofs.data(), sizeof(int), qm.links.ofs.size(), o);
+    fwrite(qm.links.m.data(), sizeof(int), qm.links.m.size(), o);
+    fclose(o);
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
-    if (argc != 3) { fprintf(stderr, "usage: fwd_shim IN OUT\n"); return 2; }
+    if (argc == 5 && std::string(argv[1]) == "qm") return qm_main(argv[2], argv[3], argv[4]);
+    if (argc != 3) { fprintf(stderr, "usage: fwd_shim IN OUT | fwd_shim qm MESH QMFILE OUT\n"); return 2; }
     FILE* f = fopen(argv[1], "rb");
     if (!f) return 2;
     int hdr[6];

@@ -37,3 +37,27 @@ def test_cpp_caller_matches_c_abi(tmp_path, make):
     rast = capi.Raster(gm, [12] * P.dim)
     Jg = s.jacobian_grid(rast, r["dphi"], r["aphi"], r["proj"], capi.Links(P.qm.link_ofs, P.qm.link_m))
     assert np.array_equal(raw[nl + r["J"].size:].reshape(Jg.shape), Jg)
+
+
+def test_cpp_load_qm(tmp_path):
+    """Mesh(path) and LoadQM through the C++ face give the reference's QM
+    positions and links (tests/golden/qm_cyl_pull.npz) bit for bit."""
+    from tests.golden_util import load_qm
+    from toastpp_gb300 import meshio
+    g, qpath = load_qm("qm_cyl_pull", tmp_path)
+    mpath, out = str(tmp_path / "m.msh"), str(tmp_path / "qm.bin")
+    meshio.write_mesh(mpath, g["coords"], g["elems"])
+    exe = build(str(tmp_path))
+    subprocess.run([exe, "qm", mpath, qpath, out], check=True)
+    raw = open(out, "rb").read()
+    dim, nq, nm, nqm = np.frombuffer(raw[:16], np.int32)
+    o = 16
+    Q = np.frombuffer(raw[o:o + 8 * nq * dim], np.float64).reshape(nq, dim)
+    o += 8 * nq * dim
+    M = np.frombuffer(raw[o:o + 8 * nm * dim], np.float64).reshape(nm, dim)
+    o += 8 * nm * dim
+    ofs = np.frombuffer(raw[o:o + 4 * (nq + 1)], np.int32)
+    o += 4 * (nq + 1)
+    lm = np.frombuffer(raw[o:o + 4 * nqm], np.int32)
+    assert np.array_equal(Q, g["qpos"]) and np.array_equal(M, g["mpos"])
+    assert np.array_equal(ofs, g["link_ofs"]) and np.array_equal(lm, g["link_m"])
