@@ -45,6 +45,13 @@ static __constant__ int c_tet_fff[4][4][4] = {  // Tet4 IntFFF planes x120 (tet4
     {{2,2,1,1},{2,6,2,2},{1,2,2,1},{1,2,1,2}},
     {{2,1,2,1},{1,2,2,1},{2,2,6,2},{1,1,2,2}},
     {{2,1,1,2},{1,2,1,2},{1,1,2,2},{2,2,2,6}}};
+// the same divided by 120, as the reference divides each entry (folded here:
+// the quotient is the correctly rounded one either way)
+static __constant__ double c_tet_fff120[4][4][4] = {
+    {{6.0 / 120.0, 2.0 / 120.0, 2.0 / 120.0, 2.0 / 120.0}, {2.0 / 120.0, 2.0 / 120.0, 1.0 / 120.0, 1.0 / 120.0}, {2.0 / 120.0, 1.0 / 120.0, 2.0 / 120.0, 1.0 / 120.0}, {2.0 / 120.0, 1.0 / 120.0, 1.0 / 120.0, 2.0 / 120.0}},
+    {{2.0 / 120.0, 2.0 / 120.0, 1.0 / 120.0, 1.0 / 120.0}, {2.0 / 120.0, 6.0 / 120.0, 2.0 / 120.0, 2.0 / 120.0}, {1.0 / 120.0, 2.0 / 120.0, 2.0 / 120.0, 1.0 / 120.0}, {1.0 / 120.0, 2.0 / 120.0, 1.0 / 120.0, 2.0 / 120.0}},
+    {{2.0 / 120.0, 1.0 / 120.0, 2.0 / 120.0, 1.0 / 120.0}, {1.0 / 120.0, 2.0 / 120.0, 2.0 / 120.0, 1.0 / 120.0}, {2.0 / 120.0, 2.0 / 120.0, 6.0 / 120.0, 2.0 / 120.0}, {1.0 / 120.0, 1.0 / 120.0, 2.0 / 120.0, 2.0 / 120.0}},
+    {{2.0 / 120.0, 1.0 / 120.0, 1.0 / 120.0, 2.0 / 120.0}, {1.0 / 120.0, 2.0 / 120.0, 1.0 / 120.0, 2.0 / 120.0}, {1.0 / 120.0, 1.0 / 120.0, 2.0 / 120.0, 2.0 / 120.0}, {2.0 / 120.0, 2.0 / 120.0, 2.0 / 120.0, 6.0 / 120.0}}};
 static __constant__ int c_tet_bfff[4][4][4][4] = {  // Tet4 face IntFFF tables x60 (tet4.cc:724-817)
     { {{6,2,2,0},{2,2,1,0},{2,1,2,0},{0,0,0,0}}, {{2,2,1,0},{2,6,2,0},{1,2,2,0},{0,0,0,0}},
       {{2,1,2,0},{1,2,2,0},{2,2,6,0},{0,0,0,0}}, {{0,0,0,0},{0,0,0,0},{0,0,0,0},{0,0,0,0}} },
@@ -90,8 +97,8 @@ __global__ void assemble_kernel(MeshDev m, const double* __restrict__ cmua, cons
             if (CPLX) iff += (((i == j ? 2.0 : 1.0) * (1.0 / 12.0)) * sz) * omega;
         } else {
             double p0 = cmua[nd[0]], p1 = cmua[nd[1]], p2 = cmua[nd[2]], p3 = cmua[nd[3]];
-            pff += (c_tet_fff[0][i][j] / 120.0 * p0 + c_tet_fff[1][i][j] / 120.0 * p1 +
-                    c_tet_fff[2][i][j] / 120.0 * p2 + c_tet_fff[3][i][j] / 120.0 * p3) * sz;
+            pff += (c_tet_fff120[0][i][j] * p0 + c_tet_fff120[1][i][j] * p1 + c_tet_fff120[2][i][j] * p2 +
+                    c_tet_fff120[3][i][j] * p3) * sz;
             double res = 0.0;
             for (int q = 0; q < 4; q++) res += ckap[nd[q]];
             pdd += res * r[1 + i * 4 + j];
