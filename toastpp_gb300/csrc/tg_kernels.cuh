@@ -178,7 +178,10 @@ template <class V>
 __global__ void ic_factor_level(MeshDev m, ICDev ic, const int* __restrict__ rows, int nrows, const V* __restrict__ A,
                                 V* __restrict__ L, V* __restrict__ dinv)
 {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    // a warp per row: every lane forms the pivot (the same sums in the same
+    // order), then the lanes share the column's entries L(j, i), each of
+    // which depends only on rows of earlier levels
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (t >= nrows) return;
     int i = rows[t];
     const int ikey = ic.key[i];
@@ -195,7 +198,7 @@ __global__ void ic_factor_level(MeshDev m, ICDev ic, const int* __restrict__ row
         if constexpr (vt<V>::cplx) di = V{1e-10, 0.0};
         else di = 1e-10;
     }
-    for (int u = ic.Ucolptr[i]; u < ic.Ucolptr[i + 1]; u++) {
+    for (int u = ic.Ucolptr[i] + lane; u < ic.Ucolptr[i + 1]; u += 32) {
         int j = ic.Urow[u];
         // row_mult (crmatrix_imp.hpp:1971-2009): sum over columns ranked before i of L(i,c) L(j,c)
         V s = vzero<V>();
@@ -210,7 +213,7 @@ __global__ void ic_factor_level(MeshDev m, ICDev ic, const int* __restrict__ row
         V aij = A[ic.Lapos[ic.Umap[u]]];  // a_ji = a_ij (symmetric pattern and values)
         L[ic.Umap[u]] = vdiv(vsub(aij, s), di);
     }
-    dinv[i] = vrecip(di);
+    if (lane == 0) dinv[i] = vrecip(di);
 }
 
 // Level-scheduled sweeps of the IC(0) apply: one kernel per level, spread

@@ -1092,8 +1092,8 @@ static void do_reset(tg_solver s, const double* cmua, const double* ckap, const 
             const std::vector<int>& fp = ch.fwd_lev_ptr;
             for (size_t l = 0; l + 1 < fp.size(); l++) {
                 int nr = fp[l + 1] - fp[l];
-                launch(ic_factor_level<V64>, cdiv_u(nr, 128), 128, 0, s->stream, m, ic, ic.fwd_lev_rows + fp[l], nr,
-                       A, L, dinv);
+                launch(ic_factor_level<V64>, cdiv_u((size_t)nr * 32, 256), 256, 0, s->stream, m, ic,
+                       ic.fwd_lev_rows + fp[l], nr, A, L, dinv);
             }
         });
         V64* ef = (V64*)s->ef64.ensure((size_t)std::max(ic.nell_fwd, 1) * sizeof(V64));
