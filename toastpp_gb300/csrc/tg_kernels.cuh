@@ -32,13 +32,6 @@ __host__ __device__ __forceinline__ double pow2_floor(double x)
 {
     return (x > 0.0 && isfinite(x)) ? ldexp(1.0, ilogb(x)) : 1.0;
 }
-// a / b for powers of two a, b (the column scales above), exactly the
-// quotient, formed from the exponents: a division per element would run on
-// the FP64 pipe
-__host__ __device__ __forceinline__ double pow2_div(double a, double b)
-{
-    return ldexp(1.0, ilogb(a) - ilogb(b));
-}
 
 // ---------------------------------------------------------------------------
 // Assembly: one thread per CSR entry gathers its element contributions in
@@ -1287,7 +1280,7 @@ __global__ void rel_scaled_cast_kernel(int n, int k, const ColState* __restrict_
     size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (size_t)n * k) return;
     int c = (int)(t % k);
-    r[t] = vcast<V32, V64>(vscale(r64[t], pow2_div(1.0, ci[c].scale)));
+    r[t] = vcast<V32, V64>(vscale(r64[t], 1.0 / ci[c].scale));
 }
 
 // waiting columns: rel = 1 (the trigger was reached: resume) or 2 (breakdown,
@@ -1357,7 +1350,7 @@ __global__ void rel_replace_kernel(int n, int k, const ColState* __restrict__ ci
     int c = (int)(t % k);
     const int rel = ci[c].rel;
     if (!rel) return;
-    const V32 x = vcast<V32, V64>(vscale(r64[t], pow2_div(1.0, ci[c].scale)));
+    const V32 x = vcast<V32, V64>(vscale(r64[t], 1.0 / ci[c].scale));
     r[t] = x;
     if (rel == 2) {
         if (rd) rd[t] = x;
@@ -1365,7 +1358,7 @@ __global__ void rel_replace_kernel(int n, int k, const ColState* __restrict__ ci
         if (v) v[t] = vzero<V32>();
     } else {
         using S32 = typename vt<V32>::R;
-        const S32 f = (S32)pow2_div(ci[c].scale_prev, ci[c].scale);
+        const S32 f = (S32)(ci[c].scale_prev / ci[c].scale);
         p[t] = vscale(p[t], f);
         if (v) v[t] = vscale(v[t], f);
     }
