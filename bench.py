@@ -65,6 +65,10 @@ def parse():
     ap.add_argument("--element", action="store_true",
                     help="also time the element-basis Jacobian on the same fields")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--jac", default="fp64", choices=["fp64", "fp32"],
+                    help="Jacobian output (fp64: FP64 arithmetic from the FP64 fields; fp32: FP32)")
+    ap.add_argument("--cw-tol", type=float, default=1e-10,
+                    help="mixed path: componentwise backward-error bound of every solution (0: off)")
     ap.add_argument("--tol", type=float, default=1e-12)
     ap.add_argument("--inner-tol", type=float, default=1e-4, help="mixed path: inner FP32 solve tolerance")
     ap.add_argument("--inner-order", type=int, default=1, help="mixed path: inner IC(0) ordering, 1 colour, 0 natural")
@@ -140,9 +144,14 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU legs (oracle port; test infrastructure used here only as the baseline)
 # ---------------------------------------------------------------------------
-def cpu_request_time(P, nsrc_sample=16, nq_jac_sample=8, threads=None, tol=1e-12):
+def cpu_request_time(P, nsrc_sample=None, nq_jac_sample=2, threads=None, tol=1e-12):
     """Time one request on the host cores: full assembly + IC factor, a sample of
-    the source solves and of the Jacobian rows; extrapolate to the whole request."""
+    the source solves (one per host thread, forward and adjoint) and of the
+    Jacobian rows (nq_jac_sample sources x all sampled detectors, the links
+    shared by all threads); extrapolate linearly to the whole request.  The
+    reference arm and the GPU line's cpu_baseline call this with the same
+    arguments."""
+    nsrc_sample = nsrc_sample or max(8, os.cpu_count() or 1)
     from oracle import oracle as O
     threads = threads or os.cpu_count() or 1
     m = O.Mesh(P.coords, P.elems)
@@ -165,7 +174,7 @@ def cpu_request_time(P, nsrc_sample=16, nq_jac_sample=8, threads=None, tol=1e-12
     aphi_s, itm, _ = O.solve(m.rowptr, m.colidx, val, mvec[ms], meth, "ICH", tol, 0, threads)
     t_solve = time.perf_counter() - t0
     nsolved = len(qs) + len(ms)
-    # Jacobian sample: nq_jac_sample sources x all detectors (one thread per source)
+    # Jacobian sample: nq_jac_sample sources x the sampled detectors (threads share the links)
     jq = min(nq_jac_sample, len(qs))
     links_ofs = np.arange(jq + 1, dtype=np.int32) * len(ms)
     links_m = np.tile(np.arange(len(ms), dtype=np.int32), jq)
@@ -192,7 +201,7 @@ def run_reference(args):
     for s in range(args.warmup + args.steps):
         t0 = time.perf_counter()
         # one solve per host thread in each leg, so the sample keeps every core busy
-        info = cpu_request_time(P, nsrc_sample=max(8, os.cpu_count() or 1), nq_jac_sample=4, tol=args.tol)
+        info = cpu_request_time(P, tol=args.tol)
         if s >= args.warmup:
             times.append(info["t_request"])
     t = float(np.mean(times))
@@ -242,7 +251,7 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)   # the library launches on this stream
     torch.cuda.set_stream(stream)
-    j_fp32 = args.precision == "mixed"
+    j_fp32 = args.jac == "fp32"
 
     def dtensor(a):
         a = np.ascontiguousarray(a)
@@ -262,6 +271,7 @@ def run_gpu(args):
     if args.precision == "mixed":
         s.set_refinement(args.inner_tol, 12, args.inner_order)
         s.set_reliable_updates({"restart": 0, "bicgstab": 1, "cocg": 2}[args.inner])
+        s.set_backward_error(args.cw_tol)
     res = (capi.TgResult * (nq + nm))()
 
     def step():
@@ -362,39 +372,43 @@ def run_gpu(args):
         return float(np.mean([a.elapsed_time(b) for a, b in ev]))
 
     grid = element = None
-    if args.grid > 0 or args.element:
-        d_dphi = torch.empty((nq, n * vmul), dtype=torch.float64, device=dev)
-        d_aphi = torch.empty((nm, n * vmul), dtype=torch.float64, device=dev)
-        s.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, d_dphi, d_aphi, d_proj, d_lproj, d_J,
-                           j_fp32, capi.MEM_DEVICE, res)
+    # one more request with its fields kept: the inputs of the grid / element
+    # Jacobian legs and of the comparison with the oracle
+    d_dphi = torch.empty((nq, n * vmul), dtype=torch.float64, device=dev)
+    d_aphi = torch.empty((nm, n * vmul), dtype=torch.float64, device=dev)
+    s.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, d_dphi, d_aphi, d_proj, d_lproj, d_J,
+                       j_fp32, capi.MEM_DEVICE, res)
+    torch.cuda.synchronize()
+    fields = {"dphi": d_dphi, "aphi": d_aphi, "proj": d_proj.clone(), "lproj": d_lproj.clone(), "J": d_J}
     if args.grid > 0:
         rast = capi.Raster(gm, [args.grid] * P.dim)
         gcols = (2 if cplx else 1) * rast.slen
-        d_Jg = torch.empty((2 * nqm, gcols), dtype=torch.float32 if j_fp32 else torch.float64, device=dev)
+        # the grid and element legs time FP32 Jacobians (their own bases' kernels)
+        d_Jg = torch.empty((2 * nqm, gcols), dtype=torch.float32, device=dev)
 
         def gstep():
-            s.jacobian_grid_raw(rast, nq, d_dphi, nm, d_aphi, d_proj, links, capi.DATA_LOG, d_Jg, j_fp32,
+            s.jacobian_grid_raw(rast, nq, d_dphi, nm, d_aphi, d_proj, links, capi.DATA_LOG, d_Jg, True,
                                 capi.MEM_DEVICE)
 
         g_ms = event_ms(gstep)
         jb = d_Jg.numel() * d_Jg.element_size()
         # field planes read once per source / detector (value + dim gradients)
-        pb = (nq + nm) * (1 + P.dim) * rast.slen * (8 if j_fp32 else 16) // (1 if cplx else 2)
+        pb = (nq + nm) * (1 + P.dim) * rast.slen * 8 // (1 if cplx else 2)
         peak = peaks.get("hbm_gbs", 6800.0)
         grid = {"raster": [args.grid] * P.dim, "solution_points": rast.slen, "ms_per_jacobian": g_ms,
                 "jacobians_per_s": 1e3 / g_ms, "J_bytes": jb,
                 "roofline": {"bound": "hbm", "achieved": (jb + pb) / (g_ms / 1e3) / 1e9, "peak": peak,
                              "unit": "GB/s", "frac": (jb + pb) / (g_ms / 1e3) / 1e9 / peak,
                              "algorithmic_bytes_per_launch": jb + pb},
-                "note": "includes the field resampling and gradient launches; inputs on the device"}
+                "note": "FP32 J; includes the field resampling and gradient launches; inputs on the device"}
         rast.close()
         del d_Jg
     if args.element:
         # element-basis Jacobian (one column per element and component) on the same fields
         ecols = (2 if cplx else 1) * gm.ne
-        d_Je = torch.empty((2 * nqm, ecols), dtype=torch.float32 if j_fp32 else torch.float64, device=dev)
+        d_Je = torch.empty((2 * nqm, ecols), dtype=torch.float32, device=dev)
         e_ms = event_ms(lambda: s.jacobian_el_raw(nq, d_dphi, nm, d_aphi, d_proj, links, capi.DATA_LOG, d_Je,
-                                                  j_fp32, capi.MEM_DEVICE))
+                                                  True, capi.MEM_DEVICE))
         jb = d_Je.numel() * d_Je.element_size()
         fb = (nq + nm) * n * vmul * 8  # the FP64 fields, read once
         element = {"elements": gm.ne, "ms_per_jacobian": e_ms, "jacobians_per_s": 1e3 / e_ms, "J_bytes": jb,
@@ -403,8 +417,6 @@ def run_gpu(args):
                                 "algorithmic_bytes_per_launch": jb + fb},
                    "note": "includes the FP32 casts of the fields; inputs on the device"}
         del d_Je
-    if args.grid > 0 or args.element:
-        del d_dphi, d_aphi
 
     # ---- e2e through the C ABI with host buffers (pinned), copies inside the timed region
     e2e = None
@@ -432,7 +444,8 @@ def run_gpu(args):
         e2e = {"value": serial, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "steps": ksteps, "api": "tg_forward_path, one request at a time, page-locked host buffers"}
     # the server's solvers take the library's default refinement settings
-    defaults = args.precision == "fp64" or (args.inner_tol == 1e-4 and args.inner_order == 1 and args.inner == "cocg")
+    defaults = args.precision == "fp64" or (args.inner_tol == 1e-4 and args.inner_order == 1 and args.inner == "cocg"
+                                            and args.cw_tol == 1e-10)
     if e2e is not None and defaults:
         # the same requests through the request server: request i + 1 solves
         # while request i's Jacobian streams to host memory (deferred output)
@@ -468,55 +481,8 @@ def run_gpu(args):
         # ---- FP64 comparison legs (same request, plain FP64)
         compare = {}
         if not args.no_compare:
-            s64 = capi.FwdSolver(gm, meth, args.tol, "ICH", cplx, precision="fp64")
-            s64.set_stream(stream.cuda_stream)
-            # the FP64 Jacobian only where it is modest (16 GB); its error is
-            # formed on the device in row blocks, never copied to the host
-            d_J64 = (torch.empty((2 * nqm, jcols), dtype=torch.float64, device=dev)
-                     if 2 * nqm * jcols * 8 <= 16e9 else None)
-            p64 = torch.empty_like(d_proj)
-            lp64 = torch.empty_like(d_lproj)
-            s64.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, p64, lp64, d_J64, 0,
-                                 capi.MEM_DEVICE)
-            torch.cuda.synchronize()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            s64.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, p64, lp64, d_J64, 0,
-                                 capi.MEM_DEVICE)
-            b.record(stream)
-            torch.cuda.synchronize()
-            t64 = a.elapsed_time(b) / 1e3
-            compare["fp64_batched"] = {"value": nsolves / t64, "unit": UNIT, "ms_per_request": t64 * 1e3}
-            # boundary-data agreement of the measured path with plain FP64 (same tolerance)
-            lp = d_lproj.cpu().numpy().view(cdt)
-            lr = lp64.cpu().numpy().view(cdt)
-            ok = np.isfinite(lp) & np.isfinite(lr)   # log of a negative CW projection is NaN (as the reference)
-            cm_err = float(np.max(np.abs(lp - lr)[ok] / np.maximum(np.abs(lp), np.abs(lr))[ok]))
-            l2_err = float(np.linalg.norm(d_proj.cpu().numpy() - p64.cpu().numpy()) / np.linalg.norm(p64.cpu().numpy()))
-            compare["boundary_data_err_vs_fp64"] = {"cmpvec_max_rel_log": cm_err, "l2_rel_linear": l2_err}
-            if d_J64 is not None:
-                e2, r2 = 0.0, 0.0
-                for r0 in range(0, 2 * nqm, 256):
-                    a_ = d_J[r0:r0 + 256].double()
-                    b_ = d_J64[r0:r0 + 256]
-                    e2 += float(torch.sum((a_ - b_) ** 2))
-                    r2 += float(torch.sum(b_ ** 2))
-                compare["jacobian_err_vs_fp64_l2"] = (e2 / r2) ** 0.5
-                del d_J64
-            else:
-                compare["jacobian_err_vs_fp64_l2"] = None
-                compare["jacobian_err_note"] = "FP64 Jacobian above 16 GB: not formed"
-            # plain per-source FP64 (one right-hand side per solve), sampled
-            s1 = capi.FwdSolver(gm, meth, args.tol, "ICH", cplx, precision="fp64")
-            s1.reset(cm, ck, ca, omega)
-            ns = 4
-            t0 = time.perf_counter()
-            for i in range(ns):
-                s1.calc_fields(qvec[i:i + 1])
-            tps = (time.perf_counter() - t0) / ns
-            compare["fp64_per_source_solve"] = {"value": 1.0 / tps, "unit": "source-solves/s (solve only)",
-                                                "sample": f"{ns} single-RHS solves"}
-            compare["speedup_vs_fp64_per_source_solve_only"] = None
+            compare = compare_legs(args, P, gm, s, stream, dev, links, (d_cm, d_ck, d_ca), omega, (d_q, d_m),
+                                   (cm, ck, ca, qvec, mvec), fields, value, res_kind=meth)
         cpu = None
         if not args.no_cpu:
             info = cpu_request_time(P, tol=args.tol)
@@ -531,7 +497,8 @@ def run_gpu(args):
                        " refinement") if args.precision == "mixed" else ("complex-f64" if cplx else "f64")),
             "data": "synthetic (seeded mesh, optodes, inclusions)",
             "config": {"workload": workload_of(P, args.config, gm.ne, args.tol, args.precision,
-                                               f" (inner FP32 tol {args.inner_tol}, J {'fp32' if j_fp32 else 'fp64'})"
+                                               f" (inner FP32 tol {args.inner_tol}, componentwise backward error "
+                                               f"<= {args.cw_tol}, J {'fp32' if j_fp32 else 'fp64'})"
                                                if args.precision == "mixed" else ""),
                        "parallelism": f"replicas x{ws} (one request per GPU)",
                        "l2": f"each step writes the {j_bytes / 1e9:.2f} GB Jacobian"
@@ -552,6 +519,146 @@ def run_gpu(args):
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     return 0
+
+
+def compare_legs(args, P, gm, s, stream, dev, links, d_par, omega, d_src, h_src, fields, value, res_kind):
+    """Error of the measured request against the FP64 oracle, and the GPU
+    baselines the benchmark spec names, all outside the timed region:
+
+    - vs_oracle: the oracle's exact FP64 solve of the same request (the
+      direct factorisation in a nested-dissection ordering, every source and
+      detector), its projections, and its Jacobian rows for a sample of links;
+    - fp64_batched: the same request through the plain FP64 path (the
+      reference's recursion, all right-hand sides in one block) and that
+      path's own error against the oracle;
+    - fp64_per_source_solve: the plain FP64 solve one right-hand side per
+      call, device-resident, timed with CUDA events over 16 sources;
+    - jacobian_fp32_variant: the same request with an FP32 Jacobian.
+    """
+    import torch
+    from toastpp_gb300 import capi
+    from oracle import oracle as O
+    cm, ck, ca, qvec, mvec = h_src
+    d_cm, d_ck, d_ca = d_par
+    d_q, d_m = d_src
+    n, nq, nm, nqm = P.n, P.qm.nQ, P.qm.nM, P.qm.nQM
+    cplx = P.complex
+    cdt = np.complex128 if cplx else np.float64
+    nsolves = nq + nm
+    out = {}
+    # ---- the oracle's exact FP64 solve
+    t0 = time.perf_counter()
+    om = O.Mesh(P.coords, P.elems)
+    ocm, ock, oca = O.optical_coefficients(P.mua, P.mus, P.nref)
+    val = om.assemble(ocm, ock, oca, P.freq_mhz * 2 * np.pi * 1e-6, cplx)
+    oq = np.stack([om.qvec_gaussian(q, P.qwidth) for q in P.qm.Q]).astype(cdt)
+    omv = np.stack([om.qvec_gaussian(m, P.mwidth) * oca for m in P.qm.M]).astype(cdt)
+    D = O.Direct(om.rowptr, om.colidx, val, "nd", om.coords)
+    th = os.cpu_count() or 1
+    Xq = D.solve(oq, th)
+    Xm = D.solve(omv, th)
+    pref = O.project(Xq, omv, P.qm.link_ofs, P.qm.link_m, logscale=False)
+    lref = O.project(Xq, omv, P.qm.link_ofs, P.qm.link_m, logscale=True)
+    jq = min(4, nq)
+    lofs = np.asarray(P.qm.link_ofs, np.int32)[:jq + 1]
+    lm = np.asarray(P.qm.link_m, np.int32)[:lofs[-1]]
+    Jref = O.jacobian(om, Xq[:jq], Xm, pref[:lofs[-1]], lofs, lm, True, th)
+    t_oracle = time.perf_counter() - t0
+
+    def errors(dphi, aphi, proj, lproj, J):
+        e = {}
+        fq = dphi.cpu().numpy().view(cdt) if dphi is not None else None
+        if fq is not None:
+            fm = aphi.cpu().numpy().view(cdt)
+            e["fields_l2"] = float(np.sqrt((np.linalg.norm(fq - Xq) ** 2 + np.linalg.norm(fm - Xm) ** 2) /
+                                           (np.linalg.norm(Xq) ** 2 + np.linalg.norm(Xm) ** 2)))
+        pg = proj.cpu().numpy().view(cdt)
+        lg = lproj.cpu().numpy().view(cdt)
+        e["boundary_data_max_rel_linear"] = float(np.max(np.abs(pg - pref) / np.abs(pref)))
+        e["boundary_data_l2_rel_linear"] = float(np.linalg.norm(pg - pref) / np.linalg.norm(pref))
+        ok = np.isfinite(lg) & np.isfinite(lref)
+        e["boundary_data_max_abs_log"] = float(np.max(np.abs(lg - lref)[ok]))
+        if J is not None:
+            nl = int(lofs[-1])
+            rows = np.concatenate([np.arange(nl), nqm + np.arange(nl)])
+            Jg = J[torch.as_tensor(rows, device=J.device)].double().cpu().numpy()
+            Jr = Jref.reshape(2 * nl, -1)
+            e["jacobian_l2_rel_sampled_rows"] = float(np.linalg.norm(Jg - Jr) / np.linalg.norm(Jr))
+        return e
+
+    f = fields
+    out["vs_oracle"] = {"oracle": "exact FP64 solve of the same request (direct factorisation, nested-dissection "
+                                  "order), projections, and Jacobian rows of the first %d sources' %d links" %
+                                  (jq, int(lofs[-1])),
+                        "oracle_s": t_oracle, **errors(f["dphi"], f["aphi"], f["proj"], f["lproj"], f["J"])}
+    # ---- plain FP64 path, batched (the reference's recursion)
+    s64 = capi.FwdSolver(gm, res_kind, args.tol, "ICH", cplx, precision="fp64")
+    s64.set_stream(stream.cuda_stream)
+    jcols = 2 * n if cplx else n
+    d_J64 = torch.empty((2 * nqm, jcols), dtype=torch.float64, device=dev)
+    p64 = torch.empty_like(f["proj"])
+    lp64 = torch.empty_like(f["lproj"])
+    s64.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, p64, lp64, d_J64, 0,
+                         capi.MEM_DEVICE)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    s64.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, p64, lp64, d_J64, 0,
+                         capi.MEM_DEVICE)
+    b.record(stream)
+    torch.cuda.synchronize()
+    t64 = a.elapsed_time(b) / 1e3
+    out["fp64_batched"] = {"value": nsolves / t64, "unit": UNIT, "ms_per_request": t64 * 1e3,
+                           "tol": args.tol, "vs_oracle": errors(None, None, p64, lp64, d_J64)}
+    del d_J64, s64
+    # ---- plain FP64, one right-hand side per call, device-resident
+    s1 = capi.FwdSolver(gm, res_kind, args.tol, "ICH", cplx, precision="fp64")
+    s1.set_stream(stream.cuda_stream)
+    s1.reset(d_cm, d_ck, d_ca, omega, capi.MEM_DEVICE)
+    ns = min(16, nq)
+    vm = 2 if cplx else 1
+    d_phi1 = torch.zeros((ns, n * vm), dtype=torch.float64, device=dev)
+    r1 = (capi.TgResult * 1)()
+    s1.calc_fields_raw(1, d_q[0], d_phi1[0], capi.MEM_DEVICE, r1)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(ns)]
+    its1 = []
+    for i in range(ns):
+        ev[i][0].record(stream)
+        s1.calc_fields_raw(1, d_q[i], d_phi1[i], capi.MEM_DEVICE, r1)
+        ev[i][1].record(stream)
+        its1.append(r1[0].it_count)
+    torch.cuda.synchronize()
+    tps = float(np.mean([x.elapsed_time(y) for x, y in ev])) / 1e3
+    out["fp64_per_source_solve"] = {"value": 1.0 / tps, "unit": "source-solves/s (solve only)",
+                                    "ms_per_solve": tps * 1e3, "iterations_per_source": float(np.mean(its1)),
+                                    "sample": f"{ns} single-RHS solves, device-resident, CUDA events"}
+    out["speedup_vs_fp64_per_source_solve"] = value / (1.0 / tps)
+    del s1, d_phi1
+    # ---- the same request with an FP32 Jacobian (FP32 products of the refined fields)
+    if args.precision == "mixed" and args.jac == "fp64":
+        d_J32 = torch.empty((2 * nqm, jcols), dtype=torch.float32, device=dev)
+        p32 = torch.empty_like(f["proj"])
+        lp32 = torch.empty_like(f["lproj"])
+        r32 = (capi.TgResult * nsolves)()
+        for _ in range(2):
+            s.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, p32, lp32, d_J32, 1,
+                               capi.MEM_DEVICE, r32)
+        torch.cuda.synchronize()
+        k32 = 3
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k32)]
+        for x, y in ev:
+            x.record(stream)
+            s.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, p32, lp32, d_J32, 1,
+                               capi.MEM_DEVICE, r32)
+            y.record(stream)
+        torch.cuda.synchronize()
+        t32 = float(np.mean([x.elapsed_time(y) for x, y in ev])) / 1e3
+        e32 = errors(None, None, p32, lp32, d_J32)
+        out["jacobian_fp32_variant"] = {"value": nsolves / t32, "unit": UNIT, "ms_per_request": t32 * 1e3,
+                                        "jacobian_l2_rel_sampled_rows": e32["jacobian_l2_rel_sampled_rows"]}
+        del d_J32
+    return out
 
 
 def run_serving(args):

@@ -56,6 +56,15 @@ extern "C" {
 #define TG_SOLVER_CG 0
 #define TG_SOLVER_BICGSTAB 1
 #define TG_SOLVER_GMRES 2
+/* LSOLVER_DIRECT (fwdsolver.cc:89-123, 467-505: Cholesky for real systems,
+   SuperLU for complex ones): a complete F = L L^T factorisation in FP64 at
+   each reset (complex systems: complex-symmetric L L^T), in a nested-dissection
+   ordering of the nodes; each solve is the two triangular sweeps.  The
+   preconditioner and precision settings do not apply.  Per right-hand side
+   the result reports 0 iterations and the true relative residual.  A mesh
+   whose factor would exceed 2^28 entries gives TG_ERR_UNSUPPORTED at
+   tg_solver_create. */
+#define TG_SOLVER_DIRECT 3
 
 /* PreconType (src/libmath/precon.h:23-32).  DILU is accepted and, as in
    TFwdSolver::Allocate (fwdsolver.cc:149-153), solved without a preconditioner. */
@@ -153,6 +162,18 @@ int tg_solver_set_refinement(tg_solver s, double inner_tol, int max_outer, int i
       IC(0) apply per iteration); real systems use 1.
    The FP64 result meets tol in every mode.  At most 4 * max_outer residual
    replacements per right-hand side. */
+/* mixed precision only: the componentwise backward-error bound of every
+   solution (default 1e-10; 0 turns the test off).  Besides |b - A x| <= tol |b|
+   the FP64 refinement then continues until
+       max_i |b - A x|_i / (|A| |x| + |b|)_i <= cw_tol,  |z| = |Re z| + |Im z|,
+   the Oettli-Prager measure that iterative refinement stops on.  The normwise
+   test alone bounds the error of the large entries of a field; the far
+   entries, e^-20 of the peak at the far detectors, keep an error of the order
+   tol times that dynamic range, which the reference's own solvers carry too.
+   With the componentwise bound every entry is as accurate as the bound.  No
+   counterpart in the reference (its iterative solvers stop on the normwise
+   test, src/libmath/matrix_imp.hpp:93-154, 350-547). */
+int tg_solver_set_backward_error(tg_solver s, double cw_tol);
 #define TG_MIXED_RESTART 0
 #define TG_MIXED_RELIABLE_BICGSTAB 1
 #define TG_MIXED_RELIABLE_COCG 2

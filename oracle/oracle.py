@@ -56,6 +56,14 @@ def lib():
         L.tor_mesh_elsize.argtypes = [C.c_void_p, _dp]
         L.tor_pull_to_boundary.restype = C.c_int
         L.tor_pull_to_boundary.argtypes = [C.c_void_p, _dp, _dp]
+        L.tor_rcm.argtypes = [C.c_int, _ip, _ip, _ip]
+        L.tor_nd_order.argtypes = [C.c_int, _ip, _ip, _dp, C.c_int, _ip]
+        L.tor_direct_factor.restype = C.c_void_p
+        L.tor_direct_factor.argtypes = [C.c_int, _ip, _ip, _dp, C.c_int, C.c_void_p]
+        L.tor_direct_nnz.restype = C.c_int
+        L.tor_direct_nnz.argtypes = [C.c_void_p]
+        L.tor_direct_free.argtypes = [C.c_void_p]
+        L.tor_direct_solve.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, C.c_int]
         L.tor_el_found.restype = C.c_int
         L.tor_el_found.argtypes = [C.c_void_p, _dp]
         L.tor_qvec_gaussian.argtypes = [C.c_void_p, _dp, C.c_double, C.c_int, _dp]
@@ -206,6 +214,71 @@ def solve(rowptr, colidx, val, B, method="BICGSTAB", precon="ICH", tol=1e-10, ma
     if nf:
         raise RuntimeError(f"oracle solve: {nf} right-hand sides failed (breakdown)")
     return X, its, errs
+
+
+def rcm(rowptr, colidx):
+    """Reverse Cuthill-McKee ordering, perm[new] = old."""
+    n = len(rowptr) - 1
+    perm = np.zeros(n, np.int32)
+    lib().tor_rcm(n, np.ascontiguousarray(rowptr, np.int32), np.ascontiguousarray(colidx, np.int32), perm)
+    return perm
+
+
+def nd_order(rowptr, colidx, coords):
+    """Nested dissection by node coordinates, perm[new] = old."""
+    n = len(rowptr) - 1
+    coords = np.ascontiguousarray(coords, np.float64)
+    perm = np.zeros(n, np.int32)
+    lib().tor_nd_order(n, np.ascontiguousarray(rowptr, np.int32), np.ascontiguousarray(colidx, np.int32),
+                       coords.ravel(), coords.shape[1], perm)
+    return perm
+
+
+class Direct:
+    """The reference's LSOLVER_DIRECT path restated: symbolic Cholesky fill,
+    left-looking numeric factor and substitution (real; complex systems by the
+    same code in complex-symmetric arithmetic).  order: "natural" (the
+    reference's: the mesh's own node order), "rcm", or "nd" (nested dissection
+    by the node coordinates `coords`); the reorderings only reduce the fill."""
+
+    def __init__(self, rowptr, colidx, val, order="rcm", coords=None):
+        self.cplx = np.iscomplexobj(val)
+        self.n = len(rowptr) - 1
+        rp = np.ascontiguousarray(rowptr, np.int32)
+        ci = np.ascontiguousarray(colidx, np.int32)
+        if order == "nd":
+            perm = nd_order(rp, ci, coords)
+        elif order == "rcm":
+            perm = rcm(rp, ci)
+        else:
+            perm = None
+        v = _cview(val) if self.cplx else np.ascontiguousarray(val, np.float64)
+        self._h = lib().tor_direct_factor(self.n, rp, ci, v, int(self.cplx),
+                                          perm.ctypes.data_as(C.c_void_p) if perm is not None else None)
+        if not self._h:
+            raise MemoryError("oracle direct factor")
+
+    @property
+    def nnz_factor(self):
+        return lib().tor_direct_nnz(self._h)
+
+    def solve(self, B, nthreads=1):
+        B = np.atleast_2d(np.asarray(B, np.complex128 if self.cplx else np.float64))
+        X = np.zeros_like(B)
+        lib().tor_direct_solve(self._h, int(self.cplx), B.shape[0],
+                               _cview(B).ravel() if self.cplx else np.ascontiguousarray(B).ravel(),
+                               _cview(X).reshape(-1) if self.cplx else X.reshape(-1), int(nthreads))
+        return X
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().tor_direct_free(self._h)
+            self._h = None
+
+
+def solve_direct(rowptr, colidx, val, B, order="rcm", coords=None, nthreads=1):
+    """Direct FP64 solve of every row of B (nrhs x n)."""
+    return Direct(rowptr, colidx, val, order, coords).solve(B, nthreads)
 
 
 def ic_factor(rowptr, colidx, val):
@@ -389,7 +462,9 @@ class PathResult:
 
 def forward_path(mesh: Mesh, Q, M, link_ofs, link_m, mua, mus, nref, freq_mhz=0.0, qwidth=2.0, mwidth=2.0,
                  method=None, precon="ICH", tol=1e-10, maxit=0, jac=True, nthreads=1) -> PathResult:
-    """The whole forward path on the CPU, as the reference's callers run it."""
+    """The whole forward path on the CPU, as the reference's callers run it.
+    method "DIRECT" solves with the direct factorisation (an exact FP64 solve
+    up to round-off, the accuracy reference of the mixed path)."""
     cplx = freq_mhz != 0.0
     method = method or ("BICGSTAB" if cplx else "CG")
     cmua, ckap, c2a = optical_coefficients(mua, mus, nref)
@@ -401,12 +476,24 @@ def forward_path(mesh: Mesh, Q, M, link_ofs, link_m, mua, mus, nref, freq_mhz=0.
     val = mesh.assemble(cmua, ckap, c2a, omega, cplx)
     t["assemble"] = time.perf_counter() - t0
     dt = np.complex128 if cplx else np.float64
-    t0 = time.perf_counter()
-    dphi, itf, _ = solve(mesh.rowptr, mesh.colidx, val, qvec.astype(dt), method, precon, tol, maxit, nthreads)
-    t["fwd"] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    aphi, ita, _ = solve(mesh.rowptr, mesh.colidx, val, mvec.astype(dt), method, precon, tol, maxit, nthreads)
-    t["adj"] = time.perf_counter() - t0
+    if method == "DIRECT":
+        # LSOLVER_DIRECT (fwdsolver.cc:467-505): one factorisation, substitutions per source
+        t0 = time.perf_counter()
+        D = Direct(mesh.rowptr, mesh.colidx, val, "nd", mesh.coords)
+        dphi = D.solve(qvec.astype(dt), nthreads)
+        t["fwd"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        aphi = D.solve(mvec.astype(dt), nthreads)
+        t["adj"] = time.perf_counter() - t0
+        itf = np.zeros(len(qvec), np.int32)
+        ita = np.zeros(len(mvec), np.int32)
+    else:
+        t0 = time.perf_counter()
+        dphi, itf, _ = solve(mesh.rowptr, mesh.colidx, val, qvec.astype(dt), method, precon, tol, maxit, nthreads)
+        t["fwd"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        aphi, ita, _ = solve(mesh.rowptr, mesh.colidx, val, mvec.astype(dt), method, precon, tol, maxit, nthreads)
+        t["adj"] = time.perf_counter() - t0
     t0 = time.perf_counter()
     proj = project(dphi, mvec.astype(dt), link_ofs, link_m, logscale=False)
     lproj = project(dphi, mvec.astype(dt), link_ofs, link_m, logscale=True)

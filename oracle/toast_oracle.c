@@ -1154,10 +1154,25 @@ static void intfg_pair_real(const tor_mesh *m, const double *f, const double *g,
 }
 
 typedef struct {
-    const tor_mesh *m; int nq, nm, cplx, logscale, q0, q1;
+    const tor_mesh *m; int nq, nm, cplx, logscale, l0, l1;
     const double *dphi, *aphi, *proj; const int *link_ofs, *link_m; double *J; int nqm;
 } jac_job;
 
+/* the source of link l (link_ofs ascending) */
+static int link_source(const int *link_ofs, int nq, int l)
+{
+    int a = 0, b = nq;  /* link_ofs[a] <= l < link_ofs[b] */
+    while (b - a > 1) {
+        int c = (a + b) / 2;
+        if (link_ofs[c] <= l) a = c;
+        else b = c;
+    }
+    return a;
+}
+
+/* a range of links [l0, l1): the same per-link sums as jacobian.cc:441-497
+   (complex) and 738-802 (CW) whatever the split, so the result does not
+   depend on the thread count */
 static void *jac_worker(void *arg)
 {
     jac_job *jb = arg;
@@ -1166,40 +1181,42 @@ static void *jac_worker(void *arg)
     if (jb->cplx) {
         zd *f = malloc(sizeof(zd) * n), *g = malloc(sizeof(zd) * n);
         zd *pm = malloc(sizeof(zd) * n), *pk = malloc(sizeof(zd) * n);
-        for (int q = jb->q0; q < jb->q1; q++) {
-            for (int i = 0; i < n; i++) f[i] = jb->dphi[2 * ((size_t)q * n + i)] + I * jb->dphi[2 * ((size_t)q * n + i) + 1];
-            for (int l = jb->link_ofs[q]; l < jb->link_ofs[q + 1]; l++) {
-                int mm = jb->link_m[l];
-                for (int i = 0; i < n; i++) g[i] = jb->aphi[2 * ((size_t)mm * n + i)] + I * jb->aphi[2 * ((size_t)mm * n + i) + 1];
-                intfg_pair(m, f, g, 0, pm);
-                intfg_pair(m, f, g, 1, pk);
-                if (jb->logscale) {
-                    zd y = jb->proj[2 * l] + I * jb->proj[2 * l + 1];
-                    for (int k = 0; k < n; k++) { pm[k] = pm[k] / y; pk[k] = pk[k] / y; }
-                }
-                double *r0 = jb->J + (size_t)l * 2 * n, *r1 = jb->J + (size_t)(l + nqm) * 2 * n;
-                for (int k = 0; k < n; k++) {
-                    r0[k] = -creal(pm[k]); r1[k] = -cimag(pm[k]);
-                    r0[k + n] = -creal(pk[k]); r1[k + n] = -cimag(pk[k]);
-                }
+        int qf = -1;
+        for (int l = jb->l0; l < jb->l1; l++) {
+            int q = link_source(jb->link_ofs, jb->nq, l);
+            if (q != qf) {
+                for (int i = 0; i < n; i++) f[i] = jb->dphi[2 * ((size_t)q * n + i)] + I * jb->dphi[2 * ((size_t)q * n + i) + 1];
+                qf = q;
+            }
+            int mm = jb->link_m[l];
+            for (int i = 0; i < n; i++) g[i] = jb->aphi[2 * ((size_t)mm * n + i)] + I * jb->aphi[2 * ((size_t)mm * n + i) + 1];
+            intfg_pair(m, f, g, 0, pm);
+            intfg_pair(m, f, g, 1, pk);
+            if (jb->logscale) {
+                zd y = jb->proj[2 * l] + I * jb->proj[2 * l + 1];
+                for (int k = 0; k < n; k++) { pm[k] = pm[k] / y; pk[k] = pk[k] / y; }
+            }
+            double *r0 = jb->J + (size_t)l * 2 * n, *r1 = jb->J + (size_t)(l + nqm) * 2 * n;
+            for (int k = 0; k < n; k++) {
+                r0[k] = -creal(pm[k]); r1[k] = -cimag(pm[k]);
+                r0[k + n] = -creal(pk[k]); r1[k + n] = -cimag(pk[k]);
             }
         }
         free(f); free(g); free(pm); free(pk);
     } else {
         double *pm = malloc(sizeof(double) * n), *pk = malloc(sizeof(double) * n);
-        for (int q = jb->q0; q < jb->q1; q++) {
+        for (int l = jb->l0; l < jb->l1; l++) {
+            int q = link_source(jb->link_ofs, jb->nq, l);
             const double *f = jb->dphi + (size_t)q * n;
-            for (int l = jb->link_ofs[q]; l < jb->link_ofs[q + 1]; l++) {
-                const double *g = jb->aphi + (size_t)jb->link_m[l] * n;
-                intfg_pair_real(m, f, g, 0, pm);
-                intfg_pair_real(m, f, g, 1, pk);
-                double sc = jb->logscale ? 1.0 / jb->proj[l] : 1.0;
-                double *rm = jb->J + (size_t)l * n, *rk = jb->J + (size_t)(nqm + l) * n;
-                for (int k = 0; k < n; k++) {
-                    rm[k] = -pm[k];
-                    rk[k] = -pk[k];
-                    if (jb->logscale) { rm[k] *= sc; rk[k] *= sc; }
-                }
+            const double *g = jb->aphi + (size_t)jb->link_m[l] * n;
+            intfg_pair_real(m, f, g, 0, pm);
+            intfg_pair_real(m, f, g, 1, pk);
+            double sc = jb->logscale ? 1.0 / jb->proj[l] : 1.0;
+            double *rm = jb->J + (size_t)l * n, *rk = jb->J + (size_t)(nqm + l) * n;
+            for (int k = 0; k < n; k++) {
+                rm[k] = -pm[k];
+                rk[k] = -pk[k];
+                if (jb->logscale) { rm[k] *= sc; rk[k] *= sc; }
             }
         }
         free(pm); free(pk);
@@ -1209,7 +1226,9 @@ static void *jac_worker(void *arg)
 
 /* Complex: J is (2 nQM) x (2 n) row-major, rows [Re; Im], columns [mua | kappa].
    Real (CW): J holds Jmua (nQM x n) followed by Jkap (nQM x n).
-   proj: the linear projections (complex interleaved or real) used for LOG. */
+   proj: the linear projections (complex interleaved or real) used for LOG.
+   nthreads host threads share the links (the reference forms J serially,
+   jacobian.cc:380-497; every link's row is the same sum either way). */
 void tor_jacobian(const tor_mesh *m, int nq, int nm, const double *dphi, const double *aphi,
                   const double *proj, const int *link_ofs, const int *link_m, int cplx, int logscale,
                   double *J, int nthreads)
@@ -1217,12 +1236,12 @@ void tor_jacobian(const tor_mesh *m, int nq, int nm, const double *dphi, const d
     int nqm = link_ofs[nq];
     (void)nm;
     if (nthreads < 1) nthreads = 1;
-    if (nthreads > nq) nthreads = nq > 0 ? nq : 1;
+    if (nthreads > nqm) nthreads = nqm > 0 ? nqm : 1;
     jac_job *jobs = malloc(sizeof(jac_job) * nthreads);
     pthread_t *th = malloc(sizeof(pthread_t) * nthreads);
     for (int t = 0; t < nthreads; t++) {
-        jac_job jb = {m, nq, nm, cplx, logscale, (t * nq) / nthreads, ((t + 1) * nq) / nthreads,
-                      dphi, aphi, proj, link_ofs, link_m, J, nqm};
+        jac_job jb = {m, nq, nm, cplx, logscale, (int)(((long long)t * nqm) / nthreads),
+                      (int)(((long long)(t + 1) * nqm) / nthreads), dphi, aphi, proj, link_ofs, link_m, J, nqm};
         jobs[t] = jb;
         if (nthreads > 1) pthread_create(&th[t], NULL, jac_worker, &jobs[t]);
         else jac_worker(&jobs[t]);
@@ -1683,4 +1702,303 @@ double tor_a_keijzer(double n)
     double costh = fabs(cos(th));
     double R0 = ((n - 1.0) * (n - 1.0)) / ((n + 1.0) * (n + 1.0));
     return (2.0 / (1.0 - R0) - 1.0 + costh * costh * costh) / (1.0 - costh * costh);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Direct solver (LSOLVER_DIRECT)                                            */
+/* ------------------------------------------------------------------------ */
+/* The reference's direct path for real systems: SymbolicCholeskyFactorize
+   (src/libmath/crmatrix_imp.hpp:2067-2073 -> symbolic_cholesky_factor,
+   src/libmath/cr_cholesky.cc:76-233: the row set of each column merged into
+   its elimination-tree parent), CholeskyFactorize (crmatrix_imp.hpp:2104-2164:
+   left-looking columns, d_c = sqrt of the pivot, recover mode sets 1e-10) and
+   CholeskySubst (crmatrix_imp.hpp:2267-2295).  Complex systems go through
+   SuperLU in the reference (src/libstoast/fwdsolver_zslu.cc: zgssvx, natural
+   column order, no equilibration, no refinement); here they take the same
+   Cholesky code in complex-symmetric arithmetic (F = L L^T, principal square
+   roots, no pivoting), which solves the same system to round-off for these
+   matrices (a dominant positive definite real part), and the tests check it
+   against SuperLU itself.
+   The reference factors in the mesh's own node order; perm (optional,
+   perm[new] = old) applies a symmetric reordering first, which changes the
+   fill and the rounding but not the solution. */
+typedef struct {
+    int n;
+    int *cptr, *crow;   /* strictly lower factor by columns, rows ascending */
+    zd *cval, *d;
+    int *perm;          /* perm[new] = old */
+} tor_direct;
+
+static int int_cmp(const void *a, const void *b)
+{
+    int x = *(const int *)a, y = *(const int *)b;
+    return (x > y) - (x < y);
+}
+
+/* Reverse Cuthill-McKee: breadth-first from a low-degree node of each
+   component, neighbours by ascending degree, the order reversed. */
+void tor_rcm(int n, const int *rowptr, const int *colidx, int *perm)
+{
+    int *deg = malloc(sizeof(int) * (n ? n : 1)), *seen = calloc(n ? n : 1, sizeof(int));
+    int *q = malloc(sizeof(int) * (n ? n : 1)), *nb = malloc(sizeof(int) * (n ? n : 1));
+    for (int i = 0; i < n; i++) deg[i] = rowptr[i + 1] - rowptr[i];
+    int head = 0, tail = 0;
+    for (;;) {
+        int s = -1;
+        for (int i = 0; i < n; i++)
+            if (!seen[i] && (s < 0 || deg[i] < deg[s])) s = i;
+        if (s < 0) break;
+        seen[s] = 1;
+        q[tail++] = s;
+        while (head < tail) {
+            int v = q[head++], cnt = 0;
+            for (int e = rowptr[v]; e < rowptr[v + 1]; e++) {
+                int w = colidx[e];
+                if (!seen[w]) { seen[w] = 1; nb[cnt++] = w; }
+            }
+            /* insertion sort by degree, then index */
+            for (int a = 1; a < cnt; a++) {
+                int w = nb[a], b = a - 1;
+                while (b >= 0 && (deg[nb[b]] > deg[w] || (deg[nb[b]] == deg[w] && nb[b] > w))) { nb[b + 1] = nb[b]; b--; }
+                nb[b + 1] = w;
+            }
+            for (int a = 0; a < cnt; a++) q[tail++] = nb[a];
+        }
+    }
+    for (int i = 0; i < n; i++) perm[i] = q[n - 1 - i];
+    free(deg); free(seen); free(q); free(nb);
+}
+
+/* Factor F (CSR, sorted columns) after the reordering perm (NULL: natural).
+   Returns NULL on allocation failure. */
+tor_direct *tor_direct_factor(int n, const int *rowptr, const int *colidx, const double *val, int cplx,
+                              const int *perm)
+{
+    tor_direct *D = calloc(1, sizeof(tor_direct));
+    D->n = n;
+    D->perm = malloc(sizeof(int) * (n ? n : 1));
+    int *iperm = malloc(sizeof(int) * (n ? n : 1));
+    for (int i = 0; i < n; i++) D->perm[i] = perm ? perm[i] : i;
+    for (int i = 0; i < n; i++) iperm[D->perm[i]] = i;
+    /* the permuted lower pattern by columns: column j holds rows i > j */
+    int *cnt = calloc((size_t)(n > 0 ? n : 0) + 1, sizeof(int));
+    for (int i = 0; i < n; i++) {
+        int oi = D->perm[i];
+        for (int e = rowptr[oi]; e < rowptr[oi + 1]; e++) {
+            int j = iperm[colidx[e]];
+            if (j < i) cnt[j]++;
+        }
+    }
+    int **col = malloc(sizeof(int *) * (size_t)(n > 0 ? n : 1));
+    int *len = calloc(n ? n : 1, sizeof(int)), *cap = malloc(sizeof(int) * (n ? n : 1));
+    for (int j = 0; j < n; j++) { cap[j] = cnt[j] + 4; col[j] = malloc(sizeof(int) * cap[j]); }
+    for (int i = 0; i < n; i++) {
+        int oi = D->perm[i];
+        for (int e = rowptr[oi]; e < rowptr[oi + 1]; e++) {
+            int j = iperm[colidx[e]];
+            if (j < i) col[j][len[j]++] = i;
+        }
+    }
+    /* symbolic factorisation: ascending columns, each sorted column's rows
+       (minus its parent, the smallest) merged into the parent's */
+    int *buf = NULL, bcap = 0;
+    for (int j = 0; j < n; j++) {
+        qsort(col[j], len[j], sizeof(int), int_cmp);
+        if (len[j] == 0) continue;
+        int p = col[j][0];
+        int need = len[j] - 1 + len[p];
+        if (need > bcap) { bcap = need * 2; buf = realloc(buf, sizeof(int) * bcap); }
+        int a = 1, b = 0, m = 0;
+        qsort(col[p], len[p], sizeof(int), int_cmp);
+        while (a < len[j] && b < len[p]) {
+            if (col[j][a] < col[p][b]) buf[m++] = col[j][a++];
+            else if (col[j][a] > col[p][b]) buf[m++] = col[p][b++];
+            else { buf[m++] = col[j][a++]; b++; }
+        }
+        while (a < len[j]) buf[m++] = col[j][a++];
+        while (b < len[p]) buf[m++] = col[p][b++];
+        if (m > cap[p]) { cap[p] = m; col[p] = realloc(col[p], sizeof(int) * m); }
+        memcpy(col[p], buf, sizeof(int) * m);
+        len[p] = m;
+    }
+    free(buf);
+    D->cptr = malloc(sizeof(int) * (n + 1));
+    D->cptr[0] = 0;
+    for (int j = 0; j < n; j++) D->cptr[j + 1] = D->cptr[j] + len[j];
+    size_t nl = (size_t)D->cptr[n];
+    D->crow = malloc(sizeof(int) * (nl ? nl : 1));
+    D->cval = calloc(nl ? nl : 1, sizeof(zd));
+    D->d = malloc(sizeof(zd) * (n ? n : 1));
+    for (int j = 0; j < n; j++) { memcpy(D->crow + D->cptr[j], col[j], sizeof(int) * len[j]); free(col[j]); }
+    free(col); free(len); free(cap); free(cnt);
+    /* row view of L (the columns cc < c with L(c, cc) != 0, ascending) */
+    int *rptr = calloc(n + 1, sizeof(int)), *rcol = malloc(sizeof(int) * (nl ? nl : 1));
+    for (size_t q = 0; q < nl; q++) rptr[D->crow[q] + 1]++;
+    for (int i = 0; i < n; i++) rptr[i + 1] += rptr[i];
+    int *fillp = malloc(sizeof(int) * (n ? n : 1));
+    for (int i = 0; i < n; i++) fillp[i] = rptr[i];
+    for (int j = 0; j < n; j++)
+        for (int q = D->cptr[j]; q < D->cptr[j + 1]; q++) rcol[fillp[D->crow[q]]++] = j;
+    /* numeric factorisation (CholeskyFactorize): column c gathers A(c:n, c),
+       subtracts L(r, cc) L(c, cc) for every left column cc of row c, takes the
+       pivot's square root (recover: 1e-10) and scales the column */
+    zd *full = calloc(n ? n : 1, sizeof(zd));
+    int *next = malloc(sizeof(int) * (n ? n : 1));  /* per column: first entry with row >= current c */
+    for (int j = 0; j < n; j++) next[j] = D->cptr[j];
+    const double EPS = 1e-10;
+    for (int c = 0; c < n; c++) {
+        int oc = D->perm[c];
+        for (int e = rowptr[oc]; e < rowptr[oc + 1]; e++) {
+            int r = iperm[colidx[e]];
+            if (r >= c) full[r] = cplx ? val[2 * e] + I * val[2 * e + 1] : val[e];
+        }
+        for (int t = rptr[c]; t < rptr[c + 1]; t++) {
+            int cc = rcol[t];
+            int q = next[cc];  /* the entry (c, cc) */
+            zd ajk = D->cval[q];
+            for (; q < D->cptr[cc + 1]; q++) full[D->crow[q]] -= ajk * D->cval[q];
+            next[cc]++;
+        }
+        zd piv = full[c];
+        int ok = cplx ? cabs(piv) > 0.0 : creal(piv) > 0.0;
+        D->d[c] = ok ? csqrt(piv) : EPS;
+        zd idiag = 1.0 / D->d[c];
+        full[c] = 0.0;
+        for (int q = D->cptr[c]; q < D->cptr[c + 1]; q++) {
+            int r = D->crow[q];
+            D->cval[q] = full[r] * idiag;
+            full[r] = 0.0;
+        }
+    }
+    free(full); free(next); free(rptr); free(rcol); free(fillp); free(iperm);
+    return D;
+}
+
+int tor_direct_nnz(const tor_direct *D) { return D->cptr[D->n]; }
+
+void tor_direct_free(tor_direct *D)
+{
+    if (!D) return;
+    free(D->cptr); free(D->crow); free(D->cval); free(D->d); free(D->perm);
+    free(D);
+}
+
+/* CholeskySubst on nrhs right-hand sides (nrhs x n, complex interleaved when
+   cplx): forward sweep over rows of L, backward sweep over its columns; host
+   threads share the right-hand sides. */
+typedef struct { const tor_direct *D; int cplx, q0, q1; const double *B; double *X; } dsolve_job;
+
+static void *dsolve_worker(void *arg)
+{
+    dsolve_job *jb = arg;
+    const tor_direct *D = jb->D;
+    int n = D->n, cplx = jb->cplx;
+    zd *y = malloc(sizeof(zd) * (size_t)(n > 0 ? n : 1));
+    for (int q = jb->q0; q < jb->q1; q++) {
+        const double *b = jb->B + (size_t)q * n * (cplx ? 2 : 1);
+        for (int i = 0; i < n; i++) {
+            int o = D->perm[i];
+            y[i] = cplx ? b[2 * o] + I * b[2 * o + 1] : b[o];
+        }
+        /* forward: L y = b by columns (same sums as the row form) */
+        for (int j = 0; j < n; j++) {
+            y[j] /= D->d[j];
+            for (int t = D->cptr[j]; t < D->cptr[j + 1]; t++) y[D->crow[t]] -= D->cval[t] * y[j];
+        }
+        /* backward: L^T x = y */
+        for (int j = n - 1; j >= 0; j--) {
+            zd s = y[j];
+            for (int t = D->cptr[j + 1] - 1; t >= D->cptr[j]; t--) s -= D->cval[t] * y[D->crow[t]];
+            y[j] = s / D->d[j];
+        }
+        double *x = jb->X + (size_t)q * n * (cplx ? 2 : 1);
+        for (int i = 0; i < n; i++) {
+            int o = D->perm[i];
+            if (cplx) { x[2 * o] = creal(y[i]); x[2 * o + 1] = cimag(y[i]); }
+            else x[o] = creal(y[i]);
+        }
+    }
+    free(y);
+    return NULL;
+}
+
+void tor_direct_solve(const tor_direct *D, int cplx, int nrhs, const double *B, double *X, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > nrhs) nthreads = nrhs > 0 ? nrhs : 1;
+    dsolve_job *jobs = malloc(sizeof(dsolve_job) * nthreads);
+    pthread_t *th = malloc(sizeof(pthread_t) * nthreads);
+    for (int t = 0; t < nthreads; t++) {
+        dsolve_job jb = {D, cplx, (t * nrhs) / nthreads, ((t + 1) * nrhs) / nthreads, B, X};
+        jobs[t] = jb;
+        if (nthreads > 1) pthread_create(&th[t], NULL, dsolve_worker, &jobs[t]);
+        else dsolve_worker(&jobs[t]);
+    }
+    if (nthreads > 1) for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    free(jobs); free(th);
+}
+
+/* Nested dissection by coordinates (an ordering for the direct factor that
+   only reduces its fill): a node set is split at the median of its longest
+   bounding-box axis, the nodes of the upper half adjacent to the lower half
+   form the separator, and the order is lower half, upper half, separator,
+   recursively down to sets of 64 nodes. */
+static const double *nd_x;
+static int nd_dim, nd_axis;
+static int nd_cmp(const void *a, const void *b)
+{
+    double u = nd_x[(size_t)(*(const int *)a) * nd_dim + nd_axis], v = nd_x[(size_t)(*(const int *)b) * nd_dim + nd_axis];
+    if (u != v) return (u > v) - (u < v);
+    return (*(const int *)a > *(const int *)b) - (*(const int *)a < *(const int *)b);
+}
+
+static void nd_rec(const int *rowptr, const int *colidx, int *idx, int m, int *mark, int *stamp, int *out, int *pos,
+                   int *tmp)
+{
+    if (m <= 64) {
+        for (int i = 0; i < m; i++) out[(*pos)++] = idx[i];
+        return;
+    }
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < m; i++)
+        for (int d = 0; d < nd_dim; d++) {
+            double v = nd_x[(size_t)idx[i] * nd_dim + d];
+            if (v < lo[d]) lo[d] = v;
+            if (v > hi[d]) hi[d] = v;
+        }
+    nd_axis = 0;
+    for (int d = 1; d < nd_dim; d++)
+        if (hi[d] - lo[d] > hi[nd_axis] - lo[nd_axis]) nd_axis = d;
+    qsort(idx, m, sizeof(int), nd_cmp);
+    int half = m / 2;
+    int lid = ++(*stamp);
+    for (int i = 0; i < half; i++) mark[idx[i]] = lid;
+    /* upper half: separator nodes (adjacent to the lower half) go last */
+    int nu = 0, ns = 0;
+    for (int i = half; i < m; i++) {
+        int v = idx[i], sep = 0;
+        for (int e = rowptr[v]; e < rowptr[v + 1]; e++)
+            if (mark[colidx[e]] == lid) { sep = 1; break; }
+        if (sep) tmp[ns++] = v;
+        else idx[half + nu++] = v;
+    }
+    memcpy(idx + half + nu, tmp, sizeof(int) * ns);
+    int *sepcopy = malloc(sizeof(int) * (ns ? ns : 1));
+    memcpy(sepcopy, tmp, sizeof(int) * ns);
+    nd_rec(rowptr, colidx, idx, half, mark, stamp, out, pos, tmp);
+    nd_rec(rowptr, colidx, idx + half, nu, mark, stamp, out, pos, tmp);
+    for (int i = 0; i < ns; i++) out[(*pos)++] = sepcopy[i];
+    free(sepcopy);
+}
+
+void tor_nd_order(int n, const int *rowptr, const int *colidx, const double *coords, int dim, int *perm)
+{
+    int *idx = malloc(sizeof(int) * (size_t)(n > 0 ? n : 1)), *mark = calloc((size_t)(n > 0 ? n : 1), sizeof(int));
+    int *tmp = malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int i = 0; i < n; i++) idx[i] = i;
+    nd_x = coords;
+    nd_dim = dim;
+    int stamp = 0, pos = 0;
+    nd_rec(rowptr, colidx, idx, n, mark, &stamp, perm, &pos, tmp);
+    free(idx); free(mark); free(tmp);
 }

@@ -66,6 +66,12 @@ FIXTURES = {
     "cyl_cw_cg_ich": (lambda: small_cylinder(0.0), "CG", "ICH", 1e-15, True),
     "cyl_fd_bicgstab_ich": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-15, True),
     "cyl_fd_gmres_ich": (lambda: small_cylinder(100.0), "GMRES", "ICH", 1e-15, False),
+    # LSOLVER_DIRECT: Cholesky (real) and SuperLU (complex), exact FP64 solves
+    # up to round-off: the accuracy reference of the mixed path
+    "disc_cw_direct": (lambda: workloads.disc(8, 3, 0.0, 6), "DIRECT", "NONE", 1e-15, True),
+    "disc_fd_direct": (lambda: workloads.disc(8, 3, 100.0, 6), "DIRECT", "NONE", 1e-15, True),
+    "cyl_cw_direct": (lambda: small_cylinder(0.0), "DIRECT", "NONE", 1e-15, True),
+    "cyl_fd_direct": (lambda: small_cylinder(100.0), "DIRECT", "NONE", 1e-15, True),
     # grid-basis Jacobians (Raster_Pixel, basis = grid)
     "disc_cw_grid": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "ICH", 1e-15, False, (24, 24)),
     "disc_fd_grid": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (24, 20)),

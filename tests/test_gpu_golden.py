@@ -1,7 +1,16 @@
 """The GPU path against the reference's own outputs (tests/golden: fixtures
 written by the compiled reference, tests/golden/make_golden.py), through the
-C ABI: projections (ProjectAll LIN and LOG) and the nodal Jacobian, FP64 and
-mixed precision, for every solver / preconditioner the fixtures hold."""
+C ABI: projections (ProjectAll LIN and LOG) and the nodal Jacobian.
+
+- The FP64 path runs the reference's own recursion (same solver,
+  preconditioner and tolerance) and is held to the reference's iterative
+  fixtures.
+- The mixed path (FP32 inner process, FP64 refinement to the componentwise
+  backward-error bound) is held to 1e-8 against the reference's DIRECT
+  fixtures (Cholesky / SuperLU: exact FP64 solves up to round-off).  The
+  reference's iterative runs themselves sit up to ~3e-7 from those on the far
+  detectors of these discs, which is why an iterative fixture cannot be the
+  1e-8 yardstick."""
 import numpy as np
 import pytest
 
@@ -11,43 +20,54 @@ from toastpp_gb300 import capi
 
 pytestmark = pytest.mark.gpu
 
+ITERATIVE = [n for n in names(nodal_only=True) if not n.endswith("_direct")]
+DIRECT = [n for n in names(nodal_only=True) if n.endswith("_direct")]
 
-def run(g, precision):
+
+def run(g, precision, solver=None):
     gm = capi.Mesh(g["coords"], g["elems"])
     cplx = g["freq_mhz"] != 0.0
     cm, ck, ca = capi.optical_coefficients(g["mua"], g["mus"], g["nref"])
     qvec = gm.qvec_gaussian(g["Q"], g["qwidth"])
     mvec = gm.qvec_gaussian(g["M"], g["mwidth"]) * ca[None, :]
-    # same solver, preconditioner and tolerance as the reference run
-    s = capi.FwdSolver(gm, g["solver"], g["tol"], g["precon"], cplx, precision=precision)
+    solver = solver or g["solver"]
+    precon = g["precon"] if solver == g["solver"] else "ICH"
+    tol = g["tol"] if solver == g["solver"] else 1e-12
+    s = capi.FwdSolver(gm, solver, tol, precon, cplx, precision=precision)
     L = capi.Links(g["link_ofs"], g["link_m"])
     return s.forward_path(cm, ck, ca, capi.omega_of(g["freq_mhz"]), qvec, mvec, L, want_fields=False,
                           want_jac="J" in g)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("name", names(nodal_only=True))
-def test_gpu_matches_reference_fixture(name, precision):
+def logdiff(a, b):
+    """max |a - b| over entries finite in both; NaNs (log of a negative CW
+    projection, as in the reference) must sit at the same places"""
+    a, b = np.asarray(a), np.asarray(b)
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    ok = np.isfinite(a) & np.isfinite(b)
+    return float(np.max(np.abs(a - b)[ok])) if ok.any() else 0.0
+
+
+@pytest.mark.parametrize("name", ITERATIVE)
+def test_fp64_matches_reference_fixture(name):
+    """The reference's recursion at tol 1e-15 on both sides: differences are
+    round-off carried through the Krylov process."""
     g = load(name)
-    out = run(g, precision)
-    # Elementwise bounds on ln|y| and arg y.  The FP64 path runs the
-    # reference's recursion and must agree to 1e-8 / 1e-7.  The mixed path
-    # converges the true residual by refinement instead; the far detectors
-    # (|y| ~ e^-25 of the near ones) then see the reference's own solve error:
-    # the reference's BiCGSTAB+DIAG, BiCGSTAB+NONE and GMRES runs at tol 1e-15
-    # differ from its BiCGSTAB+ICH run by up to 2.5e-8 (ln|y|) and 4.8e-7
-    # (arg y) on this disc, so the mixed bound is the reference's own 2D
-    # complex golden tolerance (test/2D/fwdfem/Makefile: cmpvec -r=1e-7 / 1e-6).
-    tol_mod, tol_arg = (1e-8, 1e-7) if precision == "fp64" else (1e-7, 1e-6)
-    assert relmax(out["logproj"].real, g["logproj"].real) < tol_mod
-    if np.iscomplexobj(g["logproj"]):
-        assert relmax(out["logproj"].imag, g["logproj"].imag) < tol_arg
-    assert rel2(out["proj"], g["proj"]) < 1e-10
+    out = run(g, "fp64")
+    assert relmax(out["proj"], g["proj"]) < 1e-9
+    assert logdiff(out["logproj"], g["logproj"]) < 1e-9
     if "J" in g:
-        # The log-data Jacobian amplifies field differences far from the
-        # optodes: the reference itself run at tol 1e-16 instead of 1e-15
-        # moves J by up to 6e-8 (L2) on these meshes, so that is the scale of
-        # agreement two correct solvers can reach.
-        J = out["J"].reshape(g["J"].shape)
-        err = rel2(J, g["J"])
-        assert err < (1e-7 if precision == "fp64" else 1e-6), err
+        assert rel2(out["J"].reshape(g["J"].shape), g["J"]) < 1e-10
+
+
+@pytest.mark.parametrize("name", DIRECT)
+def test_mixed_matches_reference_direct(name):
+    """Mixed precision against the reference's exact FP64 solve: boundary data
+    within 1e-8 entry by entry (linear, ln|y| and arg y) and the FP64 Jacobian
+    within 1e-8 (L2)."""
+    g = load(name)
+    cplx = g["freq_mhz"] != 0.0
+    out = run(g, "mixed", "BICGSTAB" if cplx else "CG")
+    assert relmax(out["proj"], g["proj"]) < 1e-8
+    assert logdiff(out["logproj"], g["logproj"]) < 1e-8
+    assert rel2(out["J"].reshape(g["J"].shape), g["J"]) < 1e-8

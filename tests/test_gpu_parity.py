@@ -159,31 +159,49 @@ def test_project_and_jacobian(case, oracle_mod):
 
 
 def test_mixed_precision_boundary_data(case, oracle_mod):
+    """The mixed path (FP32 inner process, FP64 refinement until the
+    componentwise backward error is 1e-10) against the oracle's exact FP64
+    solve (the direct factorisation): fields, boundary data entry by entry,
+    and the Jacobian, each within 1e-8; the FP32 Jacobian of the same fields
+    within 1e-6 (FP32 products and storage)."""
     P, om, gm = case
     cm, ck, ca, qvec, mvec = gpu_problem_inputs(P, gm)
     omega = capi.omega_of(P.freq_mhz)
     method = "BICGSTAB" if P.complex else "CG"
     L = capi.Links(P.qm.link_ofs, P.qm.link_m)
-    # far-detector data are ~1e-7 of the near ones, so an elementwise 1e-8
-    # bound needs both solves converged to round-off (the reference's own
-    # golden tests use tol 1e-15 for the same reason)
-    s = capi.FwdSolver(gm, method, 1e-15, "ICH", P.complex, precision="mixed")
+    s = capi.FwdSolver(gm, method, 1e-12, "ICH", P.complex, precision="mixed")
     out = s.forward_path(cm, ck, ca, omega, qvec, mvec, L)
     ref = oracle_mod.forward_path(om, P.qm.Q, P.qm.M, P.qm.link_ofs, P.qm.link_m, P.mua, P.mus, P.nref,
-                                  P.freq_mhz, P.qwidth, P.mwidth, method, "ICH", 1e-15, jac=True)
-    # boundary data: log amplitude within 1e-7 and phase within 1e-6
-    # elementwise, the cmpvec bounds of the reference's own 2D complex golden
-    # tests (test/2D/fwdfem/Makefile:60-174).  Far detectors sit ~1e-7 below
-    # the near ones, at the FP64 rounding floor: the reference's own BiCGSTAB
-    # runs with different preconditioners disagree there by up to 4.8e-7 in
-    # phase.  Linear data within 1e-10 (L2), far below the 1e-8 target.
+                                  P.freq_mhz, P.qwidth, P.mwidth, "DIRECT", jac=True)
+    assert rel2(out["dphi"], ref.dphi) < 1e-10 and rel2(out["aphi"], ref.aphi) < 1e-10
+    assert relmax(out["proj"], ref.proj) < 1e-8
     lp, lr = np.asarray(out["logproj"]), np.asarray(ref.logproj)
-    assert relmax(lp.real, lr.real) < 1e-7
-    if P.complex:
-        assert relmax(lp.imag, lr.imag) < 1e-6
-    assert rel2(out["proj"], ref.proj) < 1e-10
-    # Jacobian from FP32 arithmetic: report-level agreement
-    assert rel2(out["J"], ref.J) < 1e-5
+    assert np.array_equal(np.isnan(lp), np.isnan(lr))
+    ok = np.isfinite(lp) & np.isfinite(lr)
+    assert np.max(np.abs(lp - lr)[ok]) < 1e-8
+    assert rel2(out["J"], ref.J) < 1e-8
+    J32 = s.jacobian(out["dphi"], out["aphi"], out["proj"], L, fp32=True)
+    assert rel2(J32, ref.J) < 1e-6
+
+
+def test_componentwise_bound_off_is_normwise(case):
+    """With the componentwise bound off the mixed path stops on the normwise
+    test alone (fewer iterations); both results meet the normwise tolerance."""
+    P, om, gm = case
+    cm, ck, ca, qvec, mvec = gpu_problem_inputs(P, gm)
+    omega = capi.omega_of(P.freq_mhz)
+    method = "BICGSTAB" if P.complex else "CG"
+    its = {}
+    for cw in (0.0, 1e-10):
+        s = capi.FwdSolver(gm, method, 1e-12, "ICH", P.complex, precision="mixed")
+        s.set_backward_error(cw)
+        s.reset(cm, ck, ca, omega)
+        phi, res = s.calc_fields(np.concatenate([qvec, mvec]))
+        assert all(r[1] == 0 and r[2] <= 1e-12 for r in res), res
+        its[cw] = sum(r[0] for r in res)
+    assert its[0.0] <= its[1e-10]
+    with pytest.raises(capi.ToastGPUError):
+        s.set_backward_error(-1.0)
 
 
 @pytest.mark.parametrize("neumann", [True, False], ids=["neumann", "isotropic"])

@@ -17,7 +17,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libtoastgpu.so")
 
-SOLVERS = {"CG": 0, "BICGSTAB": 1, "GMRES": 2}
+SOLVERS = {"CG": 0, "BICGSTAB": 1, "GMRES": 2, "DIRECT": 3}
 PRECONS = {"NONE": 0, "DIAG": 1, "ICH": 2, "DILU": 3}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 MEM_HOST, MEM_DEVICE = 0, 1
@@ -26,7 +26,7 @@ DATA_LIN, DATA_LOG = 1, 2
 ERR_ARG, ERR_STATE, ERR_CUDA, ERR_NOMEM, ERR_UNSUPPORTED, ERR_BREAKDOWN = 1, 2, 3, 4, 5, 6
 
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
-           "tg_qvec_gaussian", "tg_qvec_gaussian_ex", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_reliable_updates", "tg_solver_set_stream", "tg_solver_set_output_stream",
+           "tg_qvec_gaussian", "tg_qvec_gaussian_ex", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_backward_error", "tg_solver_set_reliable_updates", "tg_solver_set_stream", "tg_solver_set_output_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
            "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_solver_reset_basis", "tg_jacobian_el", "tg_mesh_load", "tg_mesh_geometry", "tg_gradient", "tg_raster_create", "tg_raster_destroy", "tg_raster_map", "tg_raster_info", "tg_raster_elref", "tg_jacobian_grid",
            "tg_qm_load", "tg_qm_info", "tg_qm_positions", "tg_qm_links", "tg_qm_destroy",
@@ -79,6 +79,7 @@ def lib():
             "tg_solver_set": [vp, d_, i_],
             "tg_solver_set_refinement": [vp, d_, i_, i_],
             "tg_solver_set_reliable_updates": [vp, i_],
+            "tg_solver_set_backward_error": [vp, d_],
             "tg_solver_set_stream": [vp, vp],
             "tg_solver_set_output_stream": [vp, vp],
             "tg_solver_sync": [vp],
@@ -294,6 +295,10 @@ class FwdSolver:
     def set_refinement(self, inner_tol, max_outer=12, inner_ordering=1):
         _check(lib().tg_solver_set_refinement(self._h, float(inner_tol), int(max_outer), int(inner_ordering)))
 
+    def set_backward_error(self, cw_tol=1e-10):
+        """Mixed path: refine until max_i |b - A x|_i / (|A||x| + |b|)_i <= cw_tol (0: off)."""
+        _check(lib().tg_solver_set_backward_error(self._h, float(cw_tol)))
+
     def set_reliable_updates(self, mode=2):
         """0 restarted refinement, 1 reliable-update BiCGSTAB, 2 reliable-update COCG (complex)."""
         _check(lib().tg_solver_set_reliable_updates(self._h, int(mode)))
@@ -360,6 +365,11 @@ class FwdSolver:
         res = (TgResult * q.shape[0])()
         _check(lib().tg_calc_fields(self._h, q.shape[0], _ptr(q), _ptr(phi), MEM_HOST, res))
         return phi, [(r.it_count, r.status, r.rel_err) for r in res]
+
+    def calc_fields_raw(self, k, qvec, phi, mem, res=None):
+        """tg_calc_fields with caller-owned buffers (numpy arrays or device
+        tensors of k x n values; phi holds the initial guess)."""
+        _check(lib().tg_calc_fields(self._h, int(k), _ptr(qvec), _ptr(phi), int(mem), res))
 
     def project_all(self, mvec, phi, links: Links, scale=DATA_LOG):
         phi = _f64(phi, self.complex)

@@ -95,6 +95,10 @@ TGHD double nrm2(double a) { return a * a; }
 TGHD float nrm2(float a) { return a * a; }
 TGHD double nrm2(cd a) { return a.x * a.x + a.y * a.y; }
 TGHD float nrm2(cf a) { return a.x * a.x + a.y * a.y; }
+// |Re a| + |Im a| rounded to FP32: the magnitude the componentwise
+// backward-error test works with (within a factor sqrt 2 of |a|)
+TGHD float mag1f(double a) { return (float)fabs(a); }
+TGHD float mag1f(cd a) { return (float)(fabs(a.x) + fabs(a.y)); }
 
 // value conversion between precisions
 template <class To, class From> TGHD To vcast(From a);

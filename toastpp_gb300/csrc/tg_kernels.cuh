@@ -25,6 +25,9 @@ struct ColState {
     // COCG (complex symmetric CG) scalars, complex: rho = r.z, alpha, beta
     double zr, zi, ar, ai, br, bi;
     int nupd;  // residual replacements this column has taken
+    // mixed path: componentwise backward error of the FP64 solution at its
+    // last true residual (max_i |r_i| / (|A| |x| + |b|)_i)
+    double berr;
 };
 
 // 2^floor(log2 x) for x > 0 finite, else 1: scaling by it is exact
@@ -210,7 +213,10 @@ __global__ void ic_factor_level(MeshDev m, ICDev ic, const int* __restrict__ row
             else if (ca > cb) b++;
             else { s = vfma(s, L[a], L[b]); a++; b++; }
         }
-        V aij = A[ic.Lapos[ic.Umap[u]]];  // a_ji = a_ij (symmetric pattern and values)
+        // a_ji = a_ij (symmetric pattern and values); a fill entry of a
+        // complete factor has no entry in A (Lapos -1)
+        const int ap = ic.Lapos[ic.Umap[u]];
+        V aij = ap >= 0 ? A[ap] : vzero<V>();
         L[ic.Umap[u]] = vdiv(vsub(aij, s), di);
     }
     if (lane == 0) dinv[i] = vrecip(di);
@@ -1199,6 +1205,28 @@ __global__ void add_correction_kernel(size_t cnt, V* __restrict__ x, const E* __
     if (t < cnt) x[t] = vadd(x[t], vcast<V, E>(e[t]));
 }
 
+// restarted refinement: the inner solve of column c works on r / scale_c
+// (scale_c a power of two of |r|, so the FP32 values stay O(1) down to the
+// rounding floor); its correction is added back times scale_c.  A column
+// whose inner solve broke down (status 2) adds nothing.
+static __global__ void refine_scale_kernel(int k, const ColState* __restrict__ outer, ColState* __restrict__ inner)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    inner[c].scale = pow2_floor(outer[c].err);
+}
+
+template <class V64, class V32>
+__global__ void add_scaled_correction_kernel(int n, int k, const ColState* __restrict__ inner, V64* __restrict__ x,
+                                             const V32* __restrict__ e)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * k) return;
+    const int c = (int)(t % k);
+    if (inner[c].status == 2) return;
+    x[t] = vadd(x[t], vscale(vcast<V64, V32>(e[t]), inner[c].scale));
+}
+
 // 1/diag(A) for the Diag preconditioner (TPrecon_Diag::Reset,
 // src/libmath/precon_imp.hpp:56-64): 1 where the diagonal is zero.
 template <class V>
@@ -1253,15 +1281,81 @@ static __global__ void rel_flags_kernel(int k, const ColState* __restrict__ co, 
     if (threadIdx.x < 3) out[threadIdx.x] = s[threadIdx.x];
 }
 
+// ---------------------------------------------------------------------------
+// Componentwise backward error of an FP64 solution (the Oettli-Prager
+// measure that iterative refinement stops on): for each listed column c,
+//   berr_c = max_i |r_ic| / (|A| |x_c| + |b_c|)_i,   r = b - A x,
+// with |z| = |Re z| + |Im z| and the sums in FP32 (the test needs the
+// magnitude of the denominator, not its digits).  A solution whose berr is at
+// the FP64 rounding level is exact for a matrix and right-hand side perturbed
+// by that relative amount entry by entry, so its small entries (far from the
+// source, where the fields are e^-20 of their peak) are as accurate as its
+// large ones, which a normwise residual test does not give.
+// A block handles BERR_ROWS rows of the kf listed columns (idx, or all k
+// columns when idx is null) and folds its maxima into cmax[c] as the bits of
+// a non-negative float: an integer maximum of those bits is the float
+// maximum, exact and independent of the order (NaN bits sort above inf, so a
+// NaN never passes the test).  cmax must be zeroed before the launch.
+// ---------------------------------------------------------------------------
+constexpr int BERR_ROWS = 32;
+
+template <class V64>
+__global__ void berr_kernel(int n, int k, int kf, const int* __restrict__ idx, const int* __restrict__ rowptr,
+                            const int* __restrict__ colidx, const float* __restrict__ absA,
+                            const V64* __restrict__ x, const V64* __restrict__ b, const V64* __restrict__ r,
+                            unsigned* __restrict__ cmax)
+{
+    extern __shared__ unsigned sm_berr[];  // kf entries
+    for (int j = threadIdx.x; j < kf; j += blockDim.x) sm_berr[j] = 0u;
+    __syncthreads();
+    const int r0 = blockIdx.x * BERR_ROWS, r1 = min(n, r0 + BERR_ROWS);
+    const int cnt = (r1 - r0) * kf;
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+        const int i = r0 + t / kf, j = t % kf;
+        const int c = idx ? idx[j] : j;
+        float d = 0.f;
+        for (int e = rowptr[i]; e < rowptr[i + 1]; e++) d = fmaf(absA[e], mag1f(x[(size_t)colidx[e] * k + c]), d);
+        const size_t o = (size_t)i * k + c;
+        d += mag1f(b[o]);
+        const float rr = mag1f(r[o]);
+        const float q = rr == 0.f ? 0.f : (d > 0.f ? rr / d : INFINITY);
+        atomicMax(&sm_berr[j], __float_as_uint(q));
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < kf; j += blockDim.x)
+        if (sm_berr[j]) atomicMax(&cmax[idx ? idx[j] : j], sm_berr[j]);
+}
+
+// |Re a| + |Im a| of each system-matrix entry, in FP32, for berr_kernel
+template <class V64>
+__global__ void abs_values_kernel(int nnz, const V64* __restrict__ a, float* __restrict__ out)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nnz) out[t] = mag1f(a[t]);
+}
+
+// the column passes both tests: normwise |r| <= tol |b| and, when cwtol > 0,
+// the componentwise backward error from cmax (berr_kernel) <= cwtol
+__device__ __forceinline__ bool col_converged(ColState& O, int c, double cwtol, const unsigned* cmax)
+{
+    if (cwtol > 0.0 && cmax) O.berr = (double)__uint_as_float(cmax[c]);
+    if (!(O.err <= O.tol * O.bnorm)) return false;
+    if (cwtol <= 0.0) return true;
+    if (!cmax) return O.err == 0.0;
+    return O.berr <= cwtol;  // false for NaN
+}
+
 // inner columns start from the outer residual, scaled to O(1): scale =
-// pow2_floor(|r|), bnorm = |r| / scale, trigger tol
+// pow2_floor(|r|), bnorm = |r| / scale, trigger tol.  With a componentwise
+// test (cwtol > 0) only an exact initial guess (r = 0) stops here.
 static __global__ void rel_init_kernel(int k, ColState* __restrict__ co, ColState* __restrict__ ci, double trig,
-                                       int maxit)
+                                       int maxit, double cwtol)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= k) return;
     ColState& O = co[c];
-    if (O.active == 1 && O.err <= O.tol * O.bnorm) { O.active = 0; O.status = 0; }
+    O.berr = 1.0;
+    if (O.active == 1 && col_converged(O, c, cwtol, nullptr)) { O.active = 0; O.status = 0; O.berr = 0.0; }
     ColState s;
     memset(&s, 0, sizeof(s));
     s.tol = trig;
@@ -1320,15 +1414,20 @@ __global__ void rel_accumulate_kernel(int n, int k, const ColState* __restrict__
 // iteration limit every active column stops with status 1
 // limit: the iteration limit was reached; max_upd: replacements per column
 static __global__ void rel_outer_kernel(int k, ColState* __restrict__ co, ColState* __restrict__ ci, int limit,
-                                        int cocg, int max_upd)
+                                        int cocg, int max_upd, double cwtol, const unsigned* __restrict__ cmax)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= k) return;
     ColState& O = co[c];
     ColState& I = ci[c];
     if (O.active != 1 || !I.rel) return;
-    if (O.err <= O.tol * O.bnorm) { O.active = 0; O.status = 0; I.rel = 0; return; }
+    if (col_converged(O, c, cwtol, cmax)) { O.active = 0; O.status = 0; I.rel = 0; return; }
     if (limit || ++I.nupd >= max_upd) { O.active = 0; O.status = 1; I.rel = 0; return; }
+    // a true residual far above the recursive one means the process no longer
+    // follows the FP64 system (at the rounding floor of the FP64 residual the
+    // true residual stops falling while the recursion goes on): resuming it
+    // with the old directions stagnates, so it restarts from the true residual
+    if (O.err > 8.0 * I.err * I.scale) I.rel = 2;
     // rescale the process to the new residual (exact: powers of two)
     I.scale_prev = I.scale;
     I.scale = pow2_floor(O.err);

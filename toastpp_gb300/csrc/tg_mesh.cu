@@ -13,6 +13,7 @@
 #include <cstring>
 #include <numeric>
 #include "tg_mesh.cuh"
+#include "../../include/toastgpu.h"
 
 namespace tg {
 
@@ -259,6 +260,8 @@ static void layout_order(MeshHost& m)
     for (size_t q = 0; q < m.colidx.size(); q++) m.jcolidx[q] = m.perm[m.colidx[q]];
 }
 
+static void ic_finish(const MeshHost& m, ICHost& c);
+
 // IC(0) structure for the ordering given by key[natural node] (a rank): see ICHost.
 static void ic_pattern(MeshHost& m, const std::vector<int>& keynat, ICHost& c)
 {
@@ -284,6 +287,14 @@ static void ic_pattern(MeshHost& m, const std::vector<int>& keynat, ICHost& c)
         }
         c.Lrowptr[p + 1] = (int)c.Lcolidx.size();
     }
+    ic_finish(m, c);
+}
+
+// The column view, the level schedules and the level ELL layouts of an L
+// pattern whose rows (Lrowptr, Lcolidx, Lkey, Lapos) and ranks (key) are set.
+static void ic_finish(const MeshHost& m, ICHost& c)
+{
+    const int n = m.n;
     int nl = c.Lrowptr[n];
     std::vector<int> byrank(n);  // layout rows in ascending rank
     for (int p = 0; p < n; p++) byrank[p] = p;
@@ -357,6 +368,135 @@ static void ic_pattern(MeshHost& m, const std::vector<int>& keynat, ICHost& c)
     };
     ell(true, c.fwd_lev_ptr, c.fwd_lev_rows, c.fwd_ell_w, c.fwd_ell_off, c.fwd_ell_col, c.fwd_ell_src);
     ell(false, c.bwd_lev_ptr, c.bwd_lev_rows, c.bwd_ell_w, c.bwd_ell_off, c.bwd_ell_col, c.bwd_ell_src);
+}
+
+// ---------------------------------------------------------------------------
+// Complete factor for the direct solver (LSOLVER_DIRECT): a fill-reducing
+// nested-dissection ordering and the symbolic Cholesky pattern, in the same
+// ICHost form as the IC(0) patterns so the same factor and sweep kernels run
+// on it (IC on a pattern closed under fill is the exact factorisation).
+// ---------------------------------------------------------------------------
+namespace {
+struct NDState {
+    const MeshHost* m;
+    std::vector<int> mark, sep;
+    int stamp = 0;
+    double coord(int p, int d) const { return m->coords[(size_t)m->iperm[p] * m->dim + d]; }
+};
+
+// orders idx[lo, hi) into out: lower half, upper half (both recursively),
+// then the separator (upper-half nodes adjacent to the lower half); the
+// halves split at the median of the longest extent; sets of at most 32
+// nodes keep their layout (spatial) order
+void nd_order(NDState& S, std::vector<int>& idx, int lo, int hi, std::vector<int>& out)
+{
+    const MeshHost& m = *S.m;
+    const int cnt = hi - lo;
+    if (cnt <= 32) {
+        std::sort(idx.begin() + lo, idx.begin() + hi);
+        out.insert(out.end(), idx.begin() + lo, idx.begin() + hi);
+        return;
+    }
+    double ext = -1.0;
+    int ax = 0;
+    for (int d = 0; d < m.dim; d++) {
+        double a = 1e300, b = -1e300;
+        for (int t = lo; t < hi; t++) {
+            const double v = S.coord(idx[t], d);
+            a = std::min(a, v);
+            b = std::max(b, v);
+        }
+        if (b - a > ext) { ext = b - a; ax = d; }
+    }
+    const int mid = lo + cnt / 2;
+    std::nth_element(idx.begin() + lo, idx.begin() + mid, idx.begin() + hi, [&](int a, int b) {
+        const double u = S.coord(a, ax), v = S.coord(b, ax);
+        return u < v || (u == v && a < b);
+    });
+    const int tag = ++S.stamp;
+    for (int t = lo; t < mid; t++) S.mark[idx[t]] = tag;
+    const size_t s0 = S.sep.size();
+    int w = mid;
+    for (int t = mid; t < hi; t++) {
+        const int p = idx[t];
+        bool adj = false;
+        for (int e = m.lrowptr[p]; e < m.lrowptr[p + 1] && !adj; e++) adj = S.mark[m.lcolidx[e]] == tag;
+        if (adj) S.sep.push_back(p);
+        else idx[w++] = p;
+    }
+    std::vector<int> sep(S.sep.begin() + s0, S.sep.end());
+    S.sep.resize(s0);
+    nd_order(S, idx, lo, mid, out);
+    nd_order(S, idx, mid, w, out);
+    std::sort(sep.begin(), sep.end());
+    out.insert(out.end(), sep.begin(), sep.end());
+}
+}  // namespace
+
+void direct_pattern(const MeshHost& m, ICHost& c, long long max_nnz)
+{
+    const int n = m.n;
+    NDState S;
+    S.m = &m;
+    S.mark.assign(n, 0);
+    std::vector<int> idx(n), order;
+    for (int p = 0; p < n; p++) idx[p] = p;
+    order.reserve(n);
+    nd_order(S, idx, 0, n, order);
+    c.key.assign(n, 0);
+    for (int r = 0; r < n; r++) c.key[order[r]] = r;
+    // symbolic factorisation in rank space: column j holds the ranks i > j of
+    // its neighbours and of its elimination-tree children's columns
+    std::vector<std::vector<int>> col(n);
+    std::vector<std::vector<int>> kids(n);
+    std::vector<int> seen(n, -1);
+    long long total = 0;
+    for (int j = 0; j < n; j++) {
+        const int p = order[j];
+        std::vector<int>& cj = col[j];
+        seen[j] = j;
+        for (int e = m.lrowptr[p]; e < m.lrowptr[p + 1]; e++) {
+            const int i = c.key[m.lcolidx[e]];
+            if (i > j && seen[i] != j) { seen[i] = j; cj.push_back(i); }
+        }
+        for (int ch : kids[j]) {
+            for (int i : col[ch])
+                if (i > j && seen[i] != j) { seen[i] = j; cj.push_back(i); }
+        }
+        std::sort(cj.begin(), cj.end());
+        if (!cj.empty()) kids[cj[0]].push_back(j);
+        total += (long long)cj.size();
+        TG_CHECK(total <= max_nnz, TG_ERR_UNSUPPORTED, "direct solver: the factor's fill exceeds its limit");
+    }
+    // rows of L by layout row, entries in ascending rank (the transpose of
+    // the columns, which come in ascending rank)
+    std::vector<int> rcnt(n + 1, 0);
+    for (int j = 0; j < n; j++)
+        for (int i : col[j]) rcnt[order[i] + 1]++;
+    c.Lrowptr.assign(n + 1, 0);
+    for (int p = 0; p < n; p++) c.Lrowptr[p + 1] = c.Lrowptr[p] + rcnt[p + 1];
+    const size_t nl = (size_t)c.Lrowptr[n];
+    c.Lcolidx.assign(nl, 0);
+    c.Lkey.assign(nl, 0);
+    c.Lapos.assign(nl, -1);
+    std::vector<int> fill(c.Lrowptr.begin(), c.Lrowptr.end() - 1);
+    for (int j = 0; j < n; j++) {
+        for (int i : col[j]) {
+            const int pr = order[i];
+            const int q = fill[pr]++;
+            c.Lcolidx[q] = order[j];
+            c.Lkey[q] = j;
+        }
+        std::vector<int>().swap(col[j]);
+    }
+    // Lapos: the entry of A at (row, column), or -1 for a fill entry
+    std::vector<int> where(n, -1);
+    for (int p = 0; p < n; p++) {
+        for (int e = m.lrowptr[p]; e < m.lrowptr[p + 1]; e++) where[m.lcolidx[e]] = e;
+        for (int q = c.Lrowptr[p]; q < c.Lrowptr[p + 1]; q++) c.Lapos[q] = where[c.Lcolidx[q]];
+        for (int e = m.lrowptr[p]; e < m.lrowptr[p + 1]; e++) where[m.lcolidx[e]] = -1;
+    }
+    ic_finish(m, c);
 }
 
 // greedy colouring in natural order; key = colour-major rank (colour, natural index)

@@ -95,6 +95,12 @@ struct Mesh {
 };
 
 Mesh* mesh_build(int dim, int n, const double* coords, int ne, const int* el);
+// The complete Cholesky pattern of F for the direct solver: a nested-
+// dissection ordering of the nodes by their coordinates and the symbolic
+// factor (fill included, Lapos -1 where A has no entry), with the column
+// view, levels and ELL layouts of ICHost.  Throws TG_ERR_UNSUPPORTED past
+// max_nnz factor entries.
+void direct_pattern(const MeshHost& m, ICHost& c, long long max_nnz);
 void qvec_gaussian_host(const MeshHost& m, const double* cnt, double w, bool neumann, double* q);
 // Element_Unstructured::GContains for element e (padded bounding box, then
 // the padded local test)

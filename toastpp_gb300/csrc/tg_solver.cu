@@ -252,6 +252,16 @@ struct GraphCache {
     }
 };
 
+// the direct solver's per-column result: done, no iterations
+static __global__ void direct_done_kernel(int k, ColState* cst)
+{
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    cst[c].active = 0;
+    cst[c].status = 0;
+    cst[c].its = 0;
+}
+
 // ---------------------------------------------------------------------------
 // Krylov engine for one value type.  Vectors are node-major n x k (ld = k).
 // ---------------------------------------------------------------------------
@@ -267,6 +277,12 @@ struct Engine {
     const V* Lef = nullptr;    // factor values in the forward / backward level ELL layouts
     const V* Leb = nullptr;
     int ico = 0;               // IC ordering: 0 natural, 1 colour-major
+    // a factor pattern of the solver's own (the direct solver's complete
+    // factor) in place of the mesh's IC(0) pattern ico, when set
+    const ICHost* ich = nullptr;
+    const ICDev* icd = nullptr;
+    const ICHost& ic_host() const { return ich ? *ich : mesh->h.ic[ico]; }
+    const ICDev& ic_dev() const { return icd ? *icd : mesh->d.ic[ico]; }
     int precon = 0;            // 0 none, 1 diag, 2 ich
     Profiler* prof = nullptr;
     DBuf w[9], part, cs, cnt, gbasis, gcol;
@@ -417,8 +433,8 @@ struct Engine {
     {
         const MeshDev& m = mesh->d;
         unsigned g = cdiv_u((size_t)nr * 32, 256);
-        const ICHost& ch = mesh->h.ic[ico];
-        const ICDev& cd_ = m.ic[ico];
+        const ICHost& ch = ic_host();
+        const ICDev& cd_ = ic_dev();
         const int w = fwd ? ch.fwd_ell_w[l] : ch.bwd_ell_w[l];
         const int eo = fwd ? ch.fwd_ell_off[l] : ch.bwd_ell_off[l];
         const int* rows = (fwd ? cd_.fwd_lev_rows : cd_.bwd_lev_rows) + off;
@@ -445,12 +461,12 @@ struct Engine {
     void ic_apply(int k, const V* in, V* out, const ColState* cst)
     {
         const MeshDev& m = mesh->d;
-        const ICHost& ch = mesh->h.ic[ico];
-        const ICDev& ic = m.ic[ico];
+        const ICHost& ch = ic_host();
+        const ICDev& ic = ic_dev();
         ProfScope ps(prof, PC_SWEEP, st);
         int cw = colw(k), ncg = (k + cw - 1) / cw, rpw = 32 / cw;
         std::vector<const void*> key = {(const void*)(size_t)k, in, out, cst, L, dinv, Lef, Leb, mesh,
-                                        (const void*)(size_t)ico};
+                                        (const void*)(size_t)ico, (const void*)icd};
         const bool wide = k >= 32 && k <= 256;
         graphs.run(st, key, [&] {
             const std::vector<int>& fp = ch.fwd_lev_ptr;
@@ -511,6 +527,25 @@ struct Engine {
         if (method == TG_SOLVER_BICGSTAB) bicgstab(k, X, cst, maxit);
         else if (method == TG_SOLVER_CG) pcg(k, X, cst, maxit);
         else throw Error{TG_ERR_UNSUPPORTED, "solver method not implemented on the GPU"};
+    }
+
+    // LSOLVER_DIRECT: X = F^-1 B by the two sweeps of the complete factor
+    // (CholeskySolve, crmatrix_imp.hpp:2297-2306), then the true residual
+    // b - A x for the per-column result (0 iterations, status 0)
+    void direct_solve(int k, const V* B, V* X, ColState* cst)
+    {
+        const MeshDev& m = mesh->d;
+        const size_t nk = (size_t)m.n * k;
+        double* pt = parts(k, 1);
+        launch(dot_tiles_kernel<V>, ntiles(), rowblk(k), 0, st, m.n, k, k, B, B, nullptr, nullptr, pt, 1, ntiles(), nullptr);
+        finalize<1>(k, cst, PH_BNORM);
+        ic_apply(k, B, X, nullptr);
+        V* R = vec(0, nk);
+        spmm(k, X, R, nullptr, false, nullptr, nullptr, 0);
+        launch(resid_kernel<V>, cdiv_u(nk, 256), 256, 0, st, m.n, k, k, B, R, nullptr);
+        launch(dot_tiles_kernel<V>, ntiles(), rowblk(k), 0, st, m.n, k, k, R, R, nullptr, nullptr, pt, 1, ntiles(), nullptr);
+        finalize<1>(k, cst, PH_RESID);
+        launch(direct_done_kernel, cdiv_u(k, 128), 128, 0, st, k, cst);
     }
 
     // out = M^-1 in (ICH, Diag or copy), as TPreconditioner::Apply
@@ -749,14 +784,16 @@ __global__ void init_inner_kernel(int k, const ColState* outer, ColState* inner,
 }
 
 // outer refinement bookkeeping: err = |r| from PH_RESID, converge test
-__global__ void refine_check_kernel(int k, ColState* outer, const ColState* inner, int step, int maxsteps)
+// (normwise, and componentwise from cmax when cwtol > 0)
+__global__ void refine_check_kernel(int k, ColState* outer, const ColState* inner, int step, int maxsteps,
+                                    double cwtol, const unsigned* cmax)
 {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= k) return;
     ColState& o = outer[c];
     if (inner) o.its += inner[c].its + (inner[c].status == 0 ? 1 : 0);
     if (!o.active) return;
-    if (o.err <= o.tol * o.bnorm) { o.active = 0; o.status = 0; return; }
+    if (col_converged(o, c, cwtol, cmax)) { o.active = 0; o.status = 0; return; }
     if (step >= maxsteps) { o.active = 0; o.status = 1; }
 }
 
@@ -974,6 +1011,7 @@ struct tg_solver_s {
     int inner_colour = 1;      // mixed path: IC(0) of the inner solves in the colour-major ordering
     int reliable = 2;          // mixed BiCGSTAB: 0 restarted refinement, 1 reliable updates of an FP32
                                // BiCGSTAB, 2 reliable updates of an FP32 COCG (complex; real: BiCGSTAB)
+    double cw_tol = 1e-10;     // mixed path: componentwise backward-error bound of each solution (0: off)
     cudaStream_t stream = 0, own = 0;
     // deferred Jacobian output: the device-to-host copy of a host J goes on
     // out_stream and tg_forward_path returns without waiting for it; two
@@ -996,6 +1034,11 @@ struct tg_solver_s {
     DBuf fp_bq, fp_xq, fp_bm, fp_xm, fp_lin, fp_log;
     DBuf jwm64, jwk64, jwm32, jwk32;  // per-node element weights of the Jacobian (geometry only)
     DBuf rel_cnt, rel_idx, rel_xc, rel_ac;
+    DBuf absA, berr_max;              // |entries| of F in FP32, per-column backward-error maxima
+    // direct solver: the complete factor's pattern (host and device)
+    std::unique_ptr<ICHost> dh;
+    ICDev dd{};
+    DBuf dbuf[14];
     Bounce bnc;                       // small device-to-host reads
     int jw_D = 0, jw_ready = 0;       // slots per node; bit 0 FP64 weights built, bit 1 FP32
     Profiler prof;
@@ -1014,6 +1057,31 @@ static int fail(const Error& e)
 {
     set_error("%s", e.msg.c_str());
     return e.code;
+}
+
+// the direct solver's factor pattern, built on the host once per solver and
+// uploaded (TG_SOLVER_DIRECT)
+static void direct_setup(tg_solver s)
+{
+    s->dh = std::make_unique<ICHost>();
+    ICHost& c = *s->dh;
+    direct_pattern(s->mesh->h, c, 1LL << 28);
+    ICDev& g = s->dd;
+    const int n = s->mesh->h.n;
+    g.nnzL = c.Lrowptr[n];
+    g.nlev_fwd = (int)c.fwd_lev_ptr.size() - 1;
+    g.nlev_bwd = (int)c.bwd_lev_ptr.size() - 1;
+    g.nell_fwd = (int)c.fwd_ell_col.size();
+    g.nell_bwd = (int)c.bwd_ell_col.size();
+    int** dst[14] = {&g.key, &g.Lrowptr, &g.Lcolidx, &g.Lapos, &g.Lkey, &g.Ucolptr, &g.Urow, &g.Umap,
+                     &g.fwd_lev_rows, &g.bwd_lev_rows, &g.fwd_ell_col, &g.fwd_ell_src, &g.bwd_ell_col, &g.bwd_ell_src};
+    const std::vector<int>* src[14] = {&c.key, &c.Lrowptr, &c.Lcolidx, &c.Lapos, &c.Lkey, &c.Ucolptr, &c.Urow, &c.Umap,
+                                       &c.fwd_lev_rows, &c.bwd_lev_rows, &c.fwd_ell_col, &c.fwd_ell_src,
+                                       &c.bwd_ell_col, &c.bwd_ell_src};
+    for (int t = 0; t < 14; t++) {
+        upload_sync(s->dbuf[t], *src[t]);
+        *dst[t] = s->dbuf[t].as<int>();
+    }
 }
 
 #define API_BEGIN try {
@@ -1049,6 +1117,13 @@ static void setup_engine(tg_solver s, Engine<V64>& e64)
     e64.Leb = s->eb64.as<V64>();
     e64.prof = &s->prof;
     e64.ico = 0;
+    e64.ich = nullptr;
+    e64.icd = nullptr;
+    if (s->method == TG_SOLVER_DIRECT) {  // the complete factor as the "preconditioner"
+        e64.precon = TG_PRECON_ICH;
+        e64.ich = s->dh.get();
+        e64.icd = &s->dd;
+    }
 }
 
 // IC ordering the solver's preconditioner is factored in: the natural
@@ -1080,14 +1155,17 @@ static void do_reset(tg_solver s, const double* cmua, const double* ckap, const 
     int pre = s->precon == TG_PRECON_DILU ? 0 : s->precon;
     V64* idg = (V64*)s->idiag64.ensure((size_t)m.n * sizeof(V64));
     launch(diag_inv_kernel<V64>, cdiv_u(m.n, 256), 256, 0, s->stream, m.n, m.diagpos, A, idg);
-    const bool mixed = s->precision == TG_PREC_MIXED;
-    if (pre == TG_PRECON_ICH) {
-        const int o = ic_order(s);
-        const ICDev& ic = m.ic[o];
-        const ICHost& ch = s->mesh->h.ic[o];
+    const bool direct = s->method == TG_SOLVER_DIRECT;
+    const bool mixed = s->precision == TG_PREC_MIXED && !direct;
+    if (pre == TG_PRECON_ICH || direct) {
+        // IC(0) in the mesh's ordering o, or the direct solver's complete
+        // factor: the same level-scheduled factorisation on either pattern
+        const int o = direct ? -1 : ic_order(s);
+        const ICDev& ic = direct ? s->dd : m.ic[o];
+        const ICHost& ch = direct ? *s->dh : s->mesh->h.ic[o];
         V64* L = (V64*)s->L64.ensure((size_t)std::max(ic.nnzL, 1) * sizeof(V64));
         V64* dinv = (V64*)s->dinv64.ensure((size_t)m.n * sizeof(V64));
-        std::vector<const void*> key = {A, L, dinv, s->mesh, (const void*)(size_t)o};
+        std::vector<const void*> key = {A, L, dinv, s->mesh, (const void*)(size_t)(o + 1), (const void*)&ic};
         s->graphs.run(s->stream, key, [&] {
             const std::vector<int>& fp = ch.fwd_lev_ptr;
             for (size_t l = 0; l + 1 < fp.size(); l++) {
@@ -1114,6 +1192,8 @@ static void do_reset(tg_solver s, const double* cmua, const double* ckap, const 
         }
     }
     if (mixed) {
+        launch(abs_values_kernel<V64>, cdiv_u(m.nnz, 256), 256, 0, s->stream, m.nnz, A,
+               (float*)s->absA.ensure((size_t)m.nnz * sizeof(float)));
         launch(cast_kernel<V32, V64>, cdiv_u(m.nnz, 256), 256, 0, s->stream, (size_t)m.nnz, A,
                (V32*)s->val32.ensure(m.nnz * sizeof(V32)));
         launch(cast_kernel<V32, V64>, cdiv_u(m.n, 256), 256, 0, s->stream, (size_t)m.n, idg,
@@ -1159,6 +1239,25 @@ static void upload_async(tg_solver s, DBuf& b, const std::vector<T>& v)
 // ---------------------------------------------------------------------------
 // core steps on device data (node-major n x k blocks)
 // ---------------------------------------------------------------------------
+// Componentwise backward error of the kf columns listed in idx (all k when
+// idx is null) of the FP64 solution X with residual R = B - A X; returns the
+// per-column maxima for the convergence kernels, or null when the solver has
+// no componentwise bound (cw_tol 0) or no column is listed.
+template <class V64>
+static const unsigned* backward_error(tg_solver s, int k, int kf, const int* idx, const V64* X, const V64* B,
+                                      const V64* R)
+{
+    if (s->cw_tol <= 0.0 || kf <= 0) return nullptr;
+    const MeshDev& m = s->mesh->d;
+    unsigned* cmax = (unsigned*)s->berr_max.ensure((size_t)k * sizeof(unsigned));
+    TG_CUDA(cudaMemsetAsync(cmax, 0, (size_t)k * sizeof(unsigned), s->stream));
+    const size_t sm = (size_t)kf * sizeof(unsigned);
+    if (sm > 48 * 1024) allow_smem((const void*)berr_kernel<V64>);
+    launch(berr_kernel<V64>, cdiv_u(m.n, BERR_ROWS), 256, sm, s->stream, m.n, k, kf, idx, m.rowptr, m.colidx,
+           s->absA.as<float>(), X, B, R, cmax);
+    return cmax;
+}
+
 // Solve F X = B for k right-hand sides; X holds the initial guess.
 // Mixed precision with reliable updates: one FP32 Krylov process per column
 // (BiCGSTAB, or COCG for complex systems) that is never restarted; whenever
@@ -1180,7 +1279,7 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
     launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, R, R, nullptr, nullptr, pt, 1,
            e64.ntiles(), nullptr);
     e64.template finalize<1>(k, co, PH_RESID);
-    launch(rel_init_kernel, ek, 128, 0, s->stream, k, co, ci, s->inner_tol, maxit);
+    launch(rel_init_kernel, ek, 128, 0, s->stream, k, co, ci, s->inner_tol, maxit, s->cw_tol);
     V32* Rw = e32.vec(0, nk);
     launch(rel_scaled_cast_kernel<V64, V32>, eg, 256, 0, s->stream, n, k, ci, R, Rw);
     TG_CUDA(cudaMemsetAsync(X32, 0, nk * sizeof(V32), s->stream));
@@ -1211,9 +1310,11 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
                 launch(rel_compact_kernel, 1, 256, 0, s->stream, k, ci, idx, dcnt + 3);
                 s->bnc.fetch(hc + 3, dcnt + 3, sizeof(int), s->stream);
                 const int kf = hc[3];
+                const unsigned* cmax = nullptr;
                 if (kf == k) {
                     e64.spmm(k, X, R, nullptr, 0, nullptr, nullptr, 0);
                     launch(resid_kernel<V64>, eg, 256, 0, s->stream, n, k, k, B, R, nullptr);
+                    cmax = backward_error<V64>(s, k, k, nullptr, X, B, R);
                 } else if (kf > 0) {
                     const size_t nkf = (size_t)n * kf;
                     V64* Xc = (V64*)s->rel_xc.ensure(nkf * sizeof(V64));
@@ -1221,12 +1322,14 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
                     launch(gather_cols_kernel<V64>, cdiv_u(nkf, 256), 256, 0, s->stream, n, k, kf, idx, X, Xc);
                     e64.spmm(kf, Xc, Ac, nullptr, 0, nullptr, nullptr, 0);
                     launch(scatter_resid_kernel<V64>, cdiv_u(nkf, 256), 256, 0, s->stream, n, k, kf, idx, B, Ac, R);
+                    cmax = backward_error<V64>(s, k, kf, idx, X, B, R);
                 }
                 launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, R, R, nullptr,
                        nullptr, pt, 1, e64.ntiles(), nullptr);
                 e64.template finalize<1>(k, co, PH_RESID);
                 const int limit = at_limit ? 1 : 0;
-                launch(rel_outer_kernel, ek, 128, 0, s->stream, k, co, ci, limit, cocg ? 1 : 0, max_upd);
+                launch(rel_outer_kernel, ek, 128, 0, s->stream, k, co, ci, limit, cocg ? 1 : 0, max_upd, s->cw_tol,
+                       cmax);
                 launch(rel_replace_kernel<V64, V32>, eg, 256, 0, s->stream, n, k, ci, R, Rw, RD, P, Vv);
                 if (cocg) {
                     launch(rel_reactivate_kernel, ek, 128, 0, s->stream, k, ci);
@@ -1254,6 +1357,10 @@ static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co, boo
     launch(init_cols_kernel, cdiv_u(k, 128), 128, 0, s->stream, k, co, s->tol, maxit);
     Engine<V64>& e64 = engine<V64>(s);
     setup_engine(s, e64);
+    if (s->method == TG_SOLVER_DIRECT) {
+        e64.direct_solve(k, B, X, co);
+        return;
+    }
     if (s->precision == TG_PREC_FP64) {
         e64.solve(s->method, k, B, X, co, zero_guess);
         return;
@@ -1280,6 +1387,9 @@ static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co, boo
         e64.spmm(k, X, R, nullptr, false, nullptr, nullptr, 0);
         launch(resid_kernel<V64>, cdiv_u(nk, 256), 256, 0, s->stream, n, k, k, B, R, nullptr);
     }
+    // the reliable-update process tests the componentwise bound after each
+    // replacement; the restarted refinement below after each FP64 residual
+    const unsigned* cmax = nullptr;
     launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, B, B, nullptr, nullptr, pt, 1,
                                                                       e64.ntiles(), nullptr);
     e64.template finalize<1>(k, co, PH_BNORM);
@@ -1296,14 +1406,17 @@ static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co, boo
         launch(dot_tiles_kernel<V64>, e64.ntiles(), e64.rowblk(k), 0, s->stream, n, k, k, R, R, nullptr, nullptr, pt, 1,
                                                                           e64.ntiles(), nullptr);
         e64.template finalize<1>(k, co, PH_RESID);
-        launch(refine_check_kernel, cdiv_u(k, 128), 128, 0, s->stream, k, co, step ? ci : nullptr, step, max_outer);
+        if (step) cmax = backward_error<V64>(s, k, k, nullptr, X, B, R);
+        launch(refine_check_kernel, cdiv_u(k, 128), 128, 0, s->stream, k, co, step ? ci : nullptr, step, max_outer,
+               s->cw_tol, step ? cmax : nullptr);
         if (e64.count_active(k, co) == 0) break;
-        launch(cast_kernel<V32, V64>, cdiv_u(nk, 256), 256, 0, s->stream, nk, R, R32);
         TG_CUDA(cudaMemsetAsync(E32, 0, nk * sizeof(V32), s->stream));
         launch(init_inner_kernel, cdiv_u(k, 128), 128, 0, s->stream, k, co, ci, inner_tol, maxit);
+        launch(refine_scale_kernel, cdiv_u(k, 128), 128, 0, s->stream, k, co, ci);
+        launch(rel_scaled_cast_kernel<V64, V32>, cdiv_u(nk, 256), 256, 0, s->stream, n, k, ci, R, R32);
         e32.solve(s->method, k, R32, E32, ci, true);
         launch(mask_vec_kernel<V32>, cdiv_u(nk, 256), 256, 0, s->stream, n, k, co, E32);
-        launch(add_correction_kernel<V64, V32>, cdiv_u(nk, 256), 256, 0, s->stream, nk, X, E32);
+        launch(add_scaled_correction_kernel<V64, V32>, cdiv_u(nk, 256), 256, 0, s->stream, n, k, ci, X, E32);
         e64.spmm(k, X, R, nullptr, false, nullptr, nullptr, 0);
         launch(resid_kernel<V64>, cdiv_u(nk, 256), 256, 0, s->stream, n, k, k, B, R, nullptr);
     }
@@ -1419,15 +1532,16 @@ static void launch_jacobian(tg_solver s, int nq, const VC* F, int ldf, int nm, c
 }
 
 // Jacobian from node-major FP64 fields (F: nq columns at stride ldf, G: nm
-// columns at stride ldg); the mixed path computes it in FP32 from FP32 copies
-// of the refined fields.  ylin: device linear projections or null.
+// columns at stride ldg); an FP32 J of the mixed path is computed in FP32 from
+// FP32 copies of the refined fields, an FP64 J always in FP64 from the FP64
+// fields.  ylin: device linear projections or null.
 template <class V64, class V32>
 static void jacobian_nm(tg_solver s, int nq, const V64* F, int ldf, int nm, const V64* G, int ldg,
                         const LinkHost& L, const V64* ylin, void* J, int out_fp32)
 {
     const MeshDev& m = s->mesh->d;
     int n = m.n, nqm = (int)L.q.size();
-    if (s->precision == TG_PREC_MIXED) {
+    if (s->precision == TG_PREC_MIXED && out_fp32) {
         V32* F32 = (V32*)s->jF.ensure((size_t)n * nq * sizeof(V32));
         V32* G32 = (V32*)s->jG.ensure((size_t)n * nm * sizeof(V32));
         launch(strided_cast_kernel<V32, V64>, cdiv_u((size_t)n * nq, 256), 256, 0, s->stream, n, nq, F, ldf, F32);
@@ -2126,8 +2240,8 @@ int tg_solver_create(tg_mesh mesh, int is_complex, int method, int precon, doubl
     API_BEGIN
     TG_CHECK(mesh && out, TG_ERR_ARG, "NULL argument");
     *out = nullptr;
-    TG_CHECK(method == TG_SOLVER_CG || method == TG_SOLVER_BICGSTAB || method == TG_SOLVER_GMRES, TG_ERR_ARG,
-             "unknown solver method");
+    TG_CHECK(method == TG_SOLVER_CG || method == TG_SOLVER_BICGSTAB || method == TG_SOLVER_GMRES ||
+                 method == TG_SOLVER_DIRECT, TG_ERR_ARG, "unknown solver method");
     TG_CHECK(precon >= TG_PRECON_NONE && precon <= TG_PRECON_DILU, TG_ERR_ARG, "unknown preconditioner");
     TG_CHECK(precision == TG_PREC_FP64 || precision == TG_PREC_MIXED, TG_ERR_ARG, "unknown precision");
     TG_CHECK(tol > 0, TG_ERR_ARG, "tolerance must be positive");
@@ -2137,6 +2251,7 @@ int tg_solver_create(tg_mesh mesh, int is_complex, int method, int precon, doubl
     s->mesh = mesh->m.get();
     s->cplx = is_complex != 0; s->method = method; s->precon = precon; s->tol = tol;
     s->maxit = maxit; s->precision = precision;
+    if (method == TG_SOLVER_DIRECT) direct_setup(s.get());
     TG_CUDA(cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking));
     s->stream = s->own;
     *out = s.release();
@@ -2464,6 +2579,14 @@ int tg_solver_set_refinement(tg_solver s, double inner_tol, int max_outer, int i
     s->max_outer = max_outer;
     s->inner_colour = inner_ordering;
     s->reset_done = false;  // the factorisation ordering may change
+    API_END
+}
+
+int tg_solver_set_backward_error(tg_solver s, double cw_tol)
+{
+    API_BEGIN
+    TG_CHECK(s && cw_tol >= 0.0 && cw_tol < 1.0, TG_ERR_ARG, "invalid argument");
+    s->cw_tol = cw_tol;
     API_END
 }
 
