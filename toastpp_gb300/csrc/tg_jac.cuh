@@ -400,4 +400,298 @@ __global__ void __launch_bounds__(NT) jacobian_kernel(JacArgs<V> a)
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Nodal Jacobian with FP64 accuracy at FP32 throughput ("float-float").
+//
+// GB300 issues FP64 at about 1/60 of its FP32 rate, and the Jacobian's pair
+// loop (two complex products per neighbour, per (source, detector, node)) is
+// 44 GFLOP for the 30k cylinder, so the plain FP64 kernel is bound by the
+// FP64 pipe.  Here every FP64 quantity is carried as an unevaluated sum of
+// two floats hi + lo (|lo| <= ulp(hi)/2): products are made exact with a
+// fused multiply-add (p = a*b, e = fma(a, b, -p)), the cross terms a_hi b_lo
+// and a_lo b_hi join the error, and each sum is compensated (TwoSum: the
+// rounding error of every addition is recovered exactly and accumulated).
+// The result carries about 44 significant bits, well past what an FP64 J
+// from FP64 fields needs.  The mua and kappa parts share every field value,
+// so they travel as the two halves of packed f32x2 registers.  FP32 range:
+// the fields and their products stay within 1e-38..1e38 for these models
+// (they decay by at most e^-40 across a domain).
+// Layout as jacobian_kernel: tile of 32 nodes (lane = node), slots i*32+t.
+// ---------------------------------------------------------------------------
+typedef unsigned long long f2x;  // packed (mua, kappa) floats
+
+__device__ __forceinline__ f2x f2_add(f2x a, f2x b)
+{
+    f2x d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2x f2_sub(f2x a, f2x b)
+{
+    f2x d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2x f2_mul(f2x a, f2x b)
+{
+    f2x d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2x f2_neg(f2x a) { return a ^ 0x8000000080000000ull; }
+__device__ __forceinline__ f2x f2_bcast(float a) { return f2_pack(a, a); }
+
+// (sh, sl) += (ah, al) * (bh, bl), lane by lane: exact product by FMA plus
+// the cross terms, TwoSum of the leading parts, errors into sl
+__device__ __forceinline__ void ff2_mac(f2x& sh, f2x& sl, f2x ah, f2x al, f2x bh, f2x bl)
+{
+    const f2x p = f2_mul(ah, bh);
+    f2x e = f2_fma(ah, bh, f2_neg(p));
+    e = f2_fma(ah, bl, e);
+    e = f2_fma(al, bh, e);
+    const f2x t = f2_add(sh, p);
+    const f2x bp = f2_sub(t, sh);
+    const f2x err = f2_add(f2_sub(sh, f2_sub(t, bp)), f2_sub(p, bp));
+    sh = t;
+    sl = f2_add(sl, f2_add(err, e));
+}
+
+// hi + lo as a double: a TwoSum in FP32 first (so the parts no longer
+// overlap), then the two exact conversions and one FP64 addition
+__device__ __forceinline__ double ff_to_double(float h, float l)
+{
+    const float t = __fadd_rn(h, l);
+    const float bp = __fsub_rn(t, h);
+    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(t, bp)), __fsub_rn(l, bp));
+    return (double)t + (double)e;
+}
+
+// a double as (hi, lo)
+__device__ __forceinline__ float2 ff_split(double x)
+{
+    const float h = __double2float_rn(x);
+    return make_float2(h, __double2float_rn(x - (double)h));
+}
+
+// node-major FP64 fields (n rows, columns c < k at stride ld) as float-float:
+// complex -> float4 (re_hi, re_lo, im_hi, im_lo), real -> float2 (hi, lo)
+template <bool CPLX>
+__global__ void ff_split_fields_kernel(int n, int k, const double* __restrict__ a, int ld, void* __restrict__ out)
+{
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * k) return;
+    const size_t i = t / k, c = t % k;
+    if constexpr (CPLX) {
+        const double re = a[2 * (i * ld + c)], im = a[2 * (i * ld + c) + 1];
+        const float2 r = ff_split(re), q = ff_split(im);
+        ((float4*)out)[t] = make_float4(r.x, r.y, q.x, q.y);
+    } else {
+        ((float2*)out)[t] = ff_split(a[i * ld + c]);
+    }
+}
+
+// per-node weights (FP64, tile-interleaved) as packed float-float:
+// float4 (Wm_hi, Wk_hi, Wm_lo, Wk_lo)
+static __global__ void ff_split_weights_kernel(size_t cnt, const double* __restrict__ wm, const double* __restrict__ wk,
+                                               float4* __restrict__ out)
+{
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt) return;
+    const float2 a = ff_split(wm[t]), b = ff_split(wk[t]);
+    out[t] = make_float4(a.x, b.x, a.y, b.y);
+}
+
+struct JacFFArgs {
+    MeshDev m;
+    int nq, nm, nqm, cplx;
+    const void* F;                // float-float forward fields, node-major, ld nq
+    const void* G;                // float-float adjoint fields, node-major, ld nm
+    const int* pairidx;           // nq*nm -> link index or -1
+    const float4* yinv;           // per link 1/y as (re_hi, re_lo, im_hi, im_lo), or null
+    double* J;
+    const float4* W;              // packed float-float weights
+    int D, SP, nmc;
+};
+
+// CTA = one 32-node tile x JM detectors, sources streamed in chunks of JQ;
+// phase B forms H = W G for the JM detectors (packed mua/kappa, float-float),
+// phase C has one (source, detector) pair per warp, lane = node.
+template <bool CPLX, int JQ, int JM, int NT>
+__global__ void __launch_bounds__(NT) jacobian_ff_kernel(JacFFArgs a)
+{
+    // field items: complex float4 (re_hi, re_lo, im_hi, im_lo), real float2
+    using FI = typename std::conditional<CPLX, float4, float2>::type;
+    // H words: complex re_hi, re_lo, im_hi, im_lo; real hi, lo (packed f2x)
+    constexpr int HW = CPLX ? 4 : 2;
+    static_assert(JM <= JQ, "the adjoint block shares a source buffer");
+    extern __shared__ __align__(16) unsigned char jsm[];
+    const MeshDev& m = a.m;
+    const int SP = a.SP, D = a.D;
+    const int tile = blockIdx.x / a.nmc, m0 = (blockIdx.x % a.nmc) * JM;
+    const int k0 = tile * JKT;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    f2x* Hs = (f2x*)jsm;                                   // [HW][JM][SP]
+    FI* Fb = (FI*)(Hs + (size_t)JM * SP * HW);             // 2 x [JQ][SP]
+    float4* yis = (float4*)(Fb + (size_t)2 * JQ * SP);     // [nq][JM]
+    int* lidx = (int*)(yis + (size_t)a.nq * JM);           // [nq][JM]
+    int* sidx = lidx + (size_t)a.nq * JM;                  // [D * 32]
+    const FI* F = (const FI*)a.F;
+    const FI* G = (const FI*)a.G;
+    const int k = k0 + lane;
+    const bool kin = k < m.n;
+    const int deg = kin ? m.jrowptr[k + 1] - m.jrowptr[k] : 0;
+    const int dmax = __reduce_max_sync(0xffffffffu, deg);
+    const int nslot = dmax * JKT;
+    for (int s = tid; s < nslot; s += blockDim.x) {
+        const int i = s / JKT, kk = k0 + s % JKT;
+        int r = -1;
+        if (kk < m.n) {
+            const int b = m.jrowptr[kk];
+            if (i < m.jrowptr[kk + 1] - b) r = m.jcolidx[b + i];
+        }
+        sidx[s] = r;
+    }
+    for (int e = tid; e < a.nq * JM; e += blockDim.x) {
+        const int q = e / JM, mg = m0 + e % JM;
+        const int l = mg < a.nm ? a.pairidx[(size_t)q * a.nm + mg] : -1;
+        lidx[e] = l;
+        if (a.yinv) yis[e] = l >= 0 ? a.yinv[l] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    FI zero;
+    memset(&zero, 0, sizeof(FI));
+    auto load_chunk = [&](int q0, FI* Fs) {
+        for (int e = tid; e < JQ * nslot; e += blockDim.x) {
+            const int c = e % JQ, s = e / JQ, r = sidx[s];
+            FI* dst = Fs + (size_t)c * SP + s;
+            if (r >= 0 && q0 + c < a.nq) cp_async_val<sizeof(FI)>(dst, F + (size_t)r * a.nq + q0 + c);
+            else *dst = zero;
+        }
+        cp_async_commit();
+    };
+    load_chunk(0, Fb);
+    FI* Gs = Fb + (size_t)JQ * SP;
+    for (int e = tid; e < JM * nslot; e += blockDim.x) {
+        const int mm = e % JM, s = e / JM, r = sidx[s], mg = m0 + mm;
+        Gs[(size_t)mm * SP + s] = (r >= 0 && mg < a.nm) ? G[(size_t)r * a.nm + mg] : zero;
+    }
+    __syncthreads();
+    // Phase B: H[mm][slot(i)] = sum_j W[i][j] g[mm][slot(j)], packed (Wm, Wk)
+    {
+        const size_t tb = (size_t)tile * D * D * JKT + lane;
+        for (int i = warp; i < dmax; i += blockDim.x / 32) {
+            f2x h[JM][HW];
+#pragma unroll
+            for (int mm = 0; mm < JM; mm++)
+#pragma unroll
+                for (int w = 0; w < HW; w++) h[mm][w] = 0ull;
+            const float4* wr = a.W + tb + (size_t)i * D * JKT;
+#pragma unroll 2
+            for (int j = 0; j < dmax; j++) {
+                const float4 wv = wr[(size_t)j * JKT];
+                const f2x wh = f2_pack(wv.x, wv.y), wl = f2_pack(wv.z, wv.w);
+#pragma unroll
+                for (int mm = 0; mm < JM; mm++) {
+                    const FI g = Gs[(size_t)mm * SP + j * JKT + lane];
+                    if constexpr (CPLX) {
+                        ff2_mac(h[mm][0], h[mm][1], wh, wl, f2_bcast(g.x), f2_bcast(g.y));
+                        ff2_mac(h[mm][2], h[mm][3], wh, wl, f2_bcast(g.z), f2_bcast(g.w));
+                    } else {
+                        ff2_mac(h[mm][0], h[mm][1], wh, wl, f2_bcast(g.x), f2_bcast(g.y));
+                    }
+                }
+            }
+#pragma unroll
+            for (int mm = 0; mm < JM; mm++)
+#pragma unroll
+                for (int w = 0; w < HW; w++) Hs[((size_t)w * JM + mm) * SP + i * JKT + lane] = h[mm][w];
+        }
+    }
+    __syncthreads();
+    const int n = m.n;
+    constexpr int NG = JQ * JM;
+    const int nch = (a.nq + JQ - 1) / JQ;
+    for (int ch = 0; ch < nch; ch++) {
+        if (ch + 1 < nch) {
+            load_chunk((ch + 1) * JQ, Fb + (size_t)((ch + 1) & 1) * JQ * SP);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const FI* Fs = Fb + (size_t)(ch & 1) * JQ * SP;
+        const int q0 = ch * JQ;
+        for (int grp = warp; grp < NG; grp += blockDim.x / 32) {
+            const int qq = grp / JM, mm = grp % JM;
+            const int q = q0 + qq, mg = m0 + mm;
+            if (q >= a.nq || mg >= a.nm) continue;
+            const int l = lidx[q * JM + mm];
+            if (l < 0) continue;
+            // packed (mua, kappa) sums: re (hi, lo), im (hi, lo)
+            f2x srh = 0ull, srl = 0ull, sih = 0ull, sil = 0ull;
+            const FI* fp = Fs + (size_t)qq * SP + lane;
+            const f2x* hp = Hs + (size_t)mm * SP + lane;
+            const size_t hw = (size_t)JM * SP;  // stride between the H words
+#pragma unroll 2
+            for (int i = 0; i < dmax; i++) {
+                const FI f = fp[(size_t)i * JKT];
+                const f2x* hq = hp + (size_t)i * JKT;
+                if constexpr (CPLX) {
+                    const f2x hrh = hq[0], hrl = hq[hw], hih = hq[2 * hw], hil = hq[3 * hw];
+                    const f2x frh = f2_bcast(f.x), frl = f2_bcast(f.y), fih = f2_bcast(f.z), fil = f2_bcast(f.w);
+                    // re += fr hr - fi hi ; im += fr hi + fi hr (no conjugation)
+                    ff2_mac(srh, srl, frh, frl, hrh, hrl);
+                    ff2_mac(srh, srl, f2_neg(fih), f2_neg(fil), hih, hil);
+                    ff2_mac(sih, sil, frh, frl, hih, hil);
+                    ff2_mac(sih, sil, fih, fil, hrh, hrl);
+                } else {
+                    ff2_mac(srh, srl, f2_bcast(f.x), f2_bcast(f.y), hq[0], hq[hw]);
+                }
+            }
+            if (!kin) continue;
+            if constexpr (CPLX) {
+                if (a.yinv) {
+                    // (s_re + i s_im) (y_re + i y_im), float-float
+                    const float4 y = yis[q * JM + mm];
+                    f2x zrh = 0ull, zrl = 0ull, zih = 0ull, zil = 0ull;
+                    ff2_mac(zrh, zrl, srh, srl, f2_bcast(y.x), f2_bcast(y.y));
+                    ff2_mac(zrh, zrl, sih, sil, f2_bcast(-y.z), f2_bcast(-y.w));
+                    ff2_mac(zih, zil, srh, srl, f2_bcast(y.z), f2_bcast(y.w));
+                    ff2_mac(zih, zil, sih, sil, f2_bcast(y.x), f2_bcast(y.y));
+                    srh = zrh; srl = zrl; sih = zih; sil = zil;
+                }
+                const float2 rh = f2_unpack(srh), rl = f2_unpack(srl), ih = f2_unpack(sih), il = f2_unpack(sil);
+                const size_t r0 = (size_t)l * 2 * n + k, r1 = (size_t)(l + a.nqm) * 2 * n + k;
+                a.J[r0] = -ff_to_double(rh.x, rl.x);
+                a.J[r1] = -ff_to_double(ih.x, il.x);
+                a.J[r0 + n] = -ff_to_double(rh.y, rl.y);
+                a.J[r1 + n] = -ff_to_double(ih.y, il.y);
+            } else {
+                if (a.yinv) {
+                    const float4 y = yis[q * JM + mm];
+                    f2x zh = 0ull, zl = 0ull;
+                    ff2_mac(zh, zl, srh, srl, f2_bcast(y.x), f2_bcast(y.y));
+                    srh = zh; srl = zl;
+                }
+                const float2 rh = f2_unpack(srh), rl = f2_unpack(srl);
+                a.J[(size_t)l * n + k] = -ff_to_double(rh.x, rl.x);
+                a.J[(size_t)(l + a.nqm) * n + k] = -ff_to_double(rh.y, rl.y);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// 1/y per link as float-float (re_hi, re_lo, im_hi, im_lo); real: (hi, lo, 0, 0)
+template <class V>
+__global__ void ff_recip_kernel(int cnt, const V* __restrict__ y, float4* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cnt) return;
+    const V r = vrecip(y[i]);
+    const float2 a = ff_split(re(r)), b = ff_split(im(r));
+    out[i] = make_float4(a.x, a.y, b.x, b.y);
+}
+
 }  // namespace tg

@@ -1033,6 +1033,7 @@ struct tg_solver_s {
     DBuf gdata, gsd, ggrad, gofs, glm;    // data gradient: data, sd, gradient, link lists
     DBuf fp_bq, fp_xq, fp_bm, fp_xm, fp_lin, fp_log;
     DBuf jwm64, jwk64, jwm32, jwk32;  // per-node element weights of the Jacobian (geometry only)
+    DBuf jwff;                        // the same as packed float-float (float-float Jacobian kernel)
     DBuf rel_cnt, rel_idx, rel_xc, rel_ac;
     DBuf absA, berr_max;              // |entries| of F in FP32, per-column backward-error maxima
     // direct solver: the complete factor's pattern (host and device)
@@ -1040,7 +1041,7 @@ struct tg_solver_s {
     ICDev dd{};
     DBuf dbuf[14];
     Bounce bnc;                       // small device-to-host reads
-    int jw_D = 0, jw_ready = 0;       // slots per node; bit 0 FP64 weights built, bit 1 FP32
+    int jw_D = 0, jw_ready = 0;       // slots per node; bit 0 FP64 weights built, bit 1 FP32, bit 2 float-float
     Profiler prof;
     GraphCache graphs;
     std::mutex mu;
@@ -1531,6 +1532,63 @@ static void launch_jacobian(tg_solver s, int nq, const VC* F, int ldf, int nm, c
     throw Error{TG_ERR_UNSUPPORTED, "mesh node degree too high for the Jacobian tile"};
 }
 
+// FP64 Jacobian by the float-float kernel: fields, weights and 1/y split into
+// (hi, lo) floats once per call (weights once per solver)
+template <bool CPLX, int JQ, int JM, int NT>
+static bool try_launch_jacobian_ff(tg_solver s, JacFFArgs a)
+{
+    const MeshDev& m = s->mesh->d;
+    const int D = s->jw_D, SP = D * JKT + 1;
+    constexpr int HW = CPLX ? 4 : 2;
+    constexpr size_t FI = CPLX ? 16 : 8;
+    const size_t smem = (size_t)HW * JM * SP * 8 + (size_t)2 * JQ * SP * FI + (size_t)a.nq * JM * (16 + 4) +
+                        (size_t)D * JKT * 4;
+    if (smem > 227 * 1024) return false;
+    auto kern = jacobian_ff_kernel<CPLX, JQ, JM, NT>;
+    allow_smem((const void*)kern);
+    a.D = D; a.SP = SP; a.nmc = (int)cdiv_u(a.nm, JM);
+    const size_t nblk = (size_t)cdiv_u(m.n, JKT) * a.nmc;
+    ProfScope ps(&s->prof, PC_JAC, s->stream);
+    launch(kern, (unsigned)nblk, NT, smem, s->stream, a);
+    return true;
+}
+
+template <class V64>
+static void launch_jacobian_ff(tg_solver s, int nq, const V64* F, int ldf, int nm, const V64* G, int ldg,
+                               const LinkHost& L, const V64* ylin, double* J)
+{
+    constexpr bool CPLX = vt<V64>::cplx;
+    constexpr size_t FI = CPLX ? 16 : 8;
+    const MeshDev& m = s->mesh->d;
+    const int n = m.n, nqm = (int)L.q.size();
+    jac_weights<double>(s, 0);  // the FP64 weights (and jw_D)
+    const size_t cnt = (size_t)cdiv_u(m.n, JKT) * s->jw_D * s->jw_D * JKT;
+    if (!(s->jw_ready & 4)) {
+        launch(ff_split_weights_kernel, cdiv_u(cnt, 256), 256, 0, s->stream, cnt, s->jwm64.as<double>(),
+               s->jwk64.as<double>(), (float4*)s->jwff.ensure(cnt * sizeof(float4)));
+        s->jw_ready |= 4;
+    }
+    void* Ff = s->jF.ensure((size_t)n * nq * FI);
+    void* Gf = s->jG.ensure((size_t)n * nm * FI);
+    launch(ff_split_fields_kernel<CPLX>, cdiv_u((size_t)n * nq, 256), 256, 0, s->stream, n, nq, (const double*)F, ldf,
+           Ff);
+    launch(ff_split_fields_kernel<CPLX>, cdiv_u((size_t)n * nm, 256), 256, 0, s->stream, n, nm, (const double*)G, ldg,
+           Gf);
+    float4* yi = nullptr;
+    if (ylin) {
+        yi = (float4*)s->jyinv.ensure((size_t)std::max(nqm, 1) * sizeof(float4));
+        launch(ff_recip_kernel<V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, ylin, yi);
+    }
+    upload_async(s, s->jpair, L.pair);
+    JacFFArgs a;
+    a.m = m; a.nq = nq; a.nm = nm; a.nqm = nqm; a.cplx = CPLX;
+    a.F = Ff; a.G = Gf; a.pairidx = s->jpair.as<int>(); a.yinv = yi; a.J = J;
+    a.W = s->jwff.as<float4>();
+    if (try_launch_jacobian_ff<CPLX, 4, 4, 512>(s, a)) return;
+    if (try_launch_jacobian_ff<CPLX, 2, 2, 128>(s, a)) return;
+    throw Error{TG_ERR_UNSUPPORTED, "mesh node degree too high for the Jacobian tile"};
+}
+
 // Jacobian from node-major FP64 fields (F: nq columns at stride ldf, G: nm
 // columns at stride ldg); an FP32 J of the mixed path is computed in FP32 from
 // FP32 copies of the refined fields, an FP64 J always in FP64 from the FP64
@@ -1552,6 +1610,10 @@ static void jacobian_nm(tg_solver s, int nq, const V64* F, int ldf, int nm, cons
             launch(recip_cast_kernel<V32, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, ylin, yi);
         }
         launch_jacobian<V32>(s, nq, F32, nq, nm, G32, nm, L, yi, J, out_fp32);
+    } else if (!out_fp32 && !getenv("TOASTGPU_JAC_FP64")) {
+        // FP64 output: the float-float kernel (TOASTGPU_JAC_FP64 selects the
+        // plain FP64 kernel instead, for comparison runs)
+        launch_jacobian_ff<V64>(s, nq, F, ldf, nm, G, ldg, L, ylin, (double*)J);
     } else {
         V64* yi = nullptr;
         if (ylin) {
