@@ -7,7 +7,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = "/root/reference"
+# the reference tree for the tests that read its own golden data
+# (TOASTPP_REFERENCE; those tests skip where it is absent)
+REFERENCE = os.environ.get("TOASTPP_REFERENCE", "/root/reference")
 
 
 def pytest_configure(config):

@@ -13,7 +13,7 @@ def names(nodal_only=False):
     element-basis fixtures (*_el), whose solves use one coefficient per
     element."""
     out = sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-    out = [n for n in out if not n.startswith("qm_")]
+    out = [n for n in out if not n.startswith("qm_") and not n.startswith("ref_")]
     return [n for n in out if not n.endswith("_el")] if nodal_only else out
 
 

@@ -27,7 +27,7 @@ def _device(a):
 
 @pytest.mark.parametrize("make", [lambda: small_disc(100.0), lambda: small_cyl(100.0), lambda: small_disc(0.0)],
                          ids=["disc_fd", "cyl_fd", "disc_cw"])
-def test_noalloc_projection_matches_project_all(make):
+def test_noalloc_projection_matches_project_all(make, oracle_mod):
     import torch
     P = make()
     gm = capi.Mesh(P.coords, P.elems)
@@ -49,6 +49,29 @@ def test_noalloc_projection_matches_project_all(make):
         s.project_all_noalloc(d_phi, P.qm.nQ, d_m, P.qm.nM, L, scale, d_out)
         got = d_out.cpu().numpy().view(dt)
         assert relmax(got, ref) < 1e-12
+        # and the oracle's ProjectAll of the same fields
+        want = oracle_mod.project(phi.astype(dt), mvec.astype(dt), P.qm.link_ofs, P.qm.link_m,
+                                  logscale=scale == capi.DATA_LOG)
+        assert relmax(got, want) < 1e-12
+
+
+def test_noalloc_checks_its_buffers():
+    """Host tensors, float32 tensors and short buffers are refused before any
+    kernel could read past them."""
+    import torch
+    P = small_disc(100.0)
+    gm = capi.Mesh(P.coords, P.elems)
+    s = capi.FwdSolver(gm, "BICGSTAB", 1e-10, "ICH", True)
+    L = capi.Links(P.qm.link_ofs, P.qm.link_m)
+    nq, nm = P.qm.nQ, P.qm.nM
+    ok_phi = torch.zeros(2 * nq * gm.n, dtype=torch.float64, device="cuda")
+    ok_m = torch.zeros(2 * nm * gm.n, dtype=torch.float64, device="cuda")
+    ok_out = torch.zeros(2 * L.nqm, dtype=torch.float64, device="cuda")
+    for bad in (ok_phi.cpu(), ok_phi.float(), ok_phi[:-1]):
+        with pytest.raises(ValueError):
+            s.project_all_noalloc(bad, nq, ok_m, nm, L, capi.DATA_LIN, ok_out)
+    with pytest.raises(ValueError):
+        s.project_all_noalloc(ok_phi, nq, ok_m, nm, L, capi.DATA_LIN, ok_out[:-1])
 
 
 def test_noalloc_rejects_problems_beyond_the_fixed_scratch():

@@ -381,7 +381,17 @@ class FwdSolver:
 
     def project_all_noalloc(self, d_phi, nq, d_mvec, nm, links: Links, scale, d_proj):
         """tg_project_all_noalloc: device inputs/outputs, fixed device scratch,
-        no device allocation by the library."""
+        no device allocation by the library.  d_phi (nq x n), d_mvec (nm x n)
+        and d_proj (nQM) are float64 CUDA tensors, complex values as (re, im)
+        pairs on a complex solver."""
+        w = 2 if self.complex else 1
+        n = self.mesh.n
+        for name, t, need in (("d_phi", d_phi, nq * n * w), ("d_mvec", d_mvec, nm * n * w),
+                              ("d_proj", d_proj, links.nqm * w)):
+            if not hasattr(t, "data_ptr") or str(getattr(t, "dtype", "")) != "torch.float64" or not t.is_cuda:
+                raise ValueError(f"{name} must be a float64 CUDA tensor")
+            if not t.is_contiguous() or t.numel() < need:
+                raise ValueError(f"{name} must be contiguous with at least {need} float64 values")
         _check(lib().tg_project_all_noalloc(self._h, int(nq), _ptr(d_phi), int(nm), _ptr(d_mvec), _ptr(links.ofs),
                                             _ptr(links.m), int(scale), _ptr(d_proj)))
 

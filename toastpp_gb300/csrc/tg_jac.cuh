@@ -447,7 +447,7 @@ __device__ __forceinline__ f2x f2_bcast(float a) { return f2_pack(a, a); }
 __device__ __forceinline__ void ff2_mac(f2x& sh, f2x& sl, f2x ah, f2x al, f2x bh, f2x bl)
 {
     const f2x p = f2_mul(ah, bh);
-    f2x e = f2_fma(ah, bh, f2_neg(p));
+    f2x e = f2_fma(ah, bh, f2_neg(p));  // a*b - p, exact
     e = f2_fma(ah, bl, e);
     e = f2_fma(al, bh, e);
     const f2x t = f2_add(sh, p);
@@ -633,21 +633,31 @@ __global__ void __launch_bounds__(NT) jacobian_ff_kernel(JacFFArgs a)
             const FI* fp = Fs + (size_t)qq * SP + lane;
             const f2x* hp = Hs + (size_t)mm * SP + lane;
             const size_t hw = (size_t)JM * SP;  // stride between the H words
-#pragma unroll 2
+            // the loads of neighbour i + 1 are issued before the products of
+            // neighbour i (shared-memory latency off the critical path)
+            FI f = fp[0];
+            f2x h0 = hp[0], h1 = hp[hw], h2 = 0ull, h3 = 0ull;
+            if constexpr (CPLX) { h2 = hp[2 * hw]; h3 = hp[3 * hw]; }
             for (int i = 0; i < dmax; i++) {
-                const FI f = fp[(size_t)i * JKT];
-                const f2x* hq = hp + (size_t)i * JKT;
+                const int in = i + 1 < dmax ? i + 1 : i;
+                const FI fn = fp[(size_t)in * JKT];
+                const f2x* hq = hp + (size_t)in * JKT;
+                const f2x n0 = hq[0], n1 = hq[hw];
+                f2x n2 = 0ull, n3 = 0ull;
+                if constexpr (CPLX) { n2 = hq[2 * hw]; n3 = hq[3 * hw]; }
                 if constexpr (CPLX) {
-                    const f2x hrh = hq[0], hrl = hq[hw], hih = hq[2 * hw], hil = hq[3 * hw];
                     const f2x frh = f2_bcast(f.x), frl = f2_bcast(f.y), fih = f2_bcast(f.z), fil = f2_bcast(f.w);
+                    const f2x nih = f2_bcast(-f.z), nil = f2_bcast(-f.w);
                     // re += fr hr - fi hi ; im += fr hi + fi hr (no conjugation)
-                    ff2_mac(srh, srl, frh, frl, hrh, hrl);
-                    ff2_mac(srh, srl, f2_neg(fih), f2_neg(fil), hih, hil);
-                    ff2_mac(sih, sil, frh, frl, hih, hil);
-                    ff2_mac(sih, sil, fih, fil, hrh, hrl);
+                    ff2_mac(srh, srl, frh, frl, h0, h1);
+                    ff2_mac(sih, sil, frh, frl, h2, h3);
+                    ff2_mac(srh, srl, nih, nil, h2, h3);
+                    ff2_mac(sih, sil, fih, fil, h0, h1);
                 } else {
-                    ff2_mac(srh, srl, f2_bcast(f.x), f2_bcast(f.y), hq[0], hq[hw]);
+                    ff2_mac(srh, srl, f2_bcast(f.x), f2_bcast(f.y), h0, h1);
                 }
+                f = fn;
+                h0 = n0; h1 = n1; h2 = n2; h3 = n3;
             }
             if (!kin) continue;
             if constexpr (CPLX) {

@@ -608,9 +608,12 @@ __global__ void __launch_bounds__(256) spmm_halo_kernel(int n, const int* __rest
     tile_dots<V>(r0, r1, (w0 + cw) * P, ld, y, w, want_n2, part, np, ntiles, tile, st, w0 * P);
 }
 
-// IC(0) level kernel on the level's ELL entries (k >= 32): warp per slot;
-// the slot's entries sit at slot * w, so the row's indices, values, right-hand
-// side and pivot load in one round and the gathers in the next.
+// IC(0) level kernel on the level's ELL entries (k >= 32): warp per (slot,
+// column group); the slot's entries sit at slot * w, so the row's indices,
+// values, right-hand side and pivot load in one round and the gathers in the
+// next.  blockIdx.y selects the group of 32 * NJ columns a warp owns: a row's
+// columns split over gridDim.y warps, so a level of few rows still fills the
+// GPU and each warp carries fewer gathers.
 // Launched as a programmatic dependent of the previous level: it lets the
 // next level start at once (griddepcontrol.launch_dependents), loads what no
 // kernel of the sweep writes (the level's rows, ELL indices and values,
@@ -623,8 +626,9 @@ __global__ void __launch_bounds__(256) ic_level_ell(const int* __restrict__ rows
                                                     V* __restrict__ y, const ColState* __restrict__ st)
 {
     const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int c0 = blockIdx.y * 32 * NJ;  // this warp's first column
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    const bool live = slot < nrows;
+    const bool live = slot < nrows && c0 < k;
     int i = 0, my_c0 = -1;
     V di = vzero<V>(), my_v0 = vzero<V>();
     if (live) {
@@ -640,7 +644,7 @@ __global__ void __launch_bounds__(256) ic_level_ell(const int* __restrict__ rows
     V acc[NJ];
 #pragma unroll
     for (int j = 0; j < NJ; j++) {
-        int c = lane + 32 * j;
+        int c = c0 + lane + 32 * j;
         acc[j] = c < k ? (FWD ? b[(size_t)i * ld + c] : y[(size_t)i * ld + c]) : vzero<V>();
     }
     constexpr int UNR = 4;  // entries whose gathers are in flight together
@@ -669,7 +673,7 @@ __global__ void __launch_bounds__(256) ic_level_ell(const int* __restrict__ rows
             for (int u = 0; u < UNR; u++)
 #pragma unroll
                 for (int j = 0; j < NJ; j++) {
-                    int c = lane + 32 * j;
+                    int c = c0 + lane + 32 * j;
                     g[u][j] = (e + u < cnt && cc[u] >= 0 && c < k) ? y[(size_t)cc[u] * ld + c] : vzero<V>();
                 }
 #pragma unroll
@@ -681,7 +685,7 @@ __global__ void __launch_bounds__(256) ic_level_ell(const int* __restrict__ rows
     }
 #pragma unroll
     for (int j = 0; j < NJ; j++) {
-        int c = lane + 32 * j;
+        int c = c0 + lane + 32 * j;
         if (c < k && !(st && st[c].active != 1)) y[(size_t)i * ld + c] = vmul(acc[j], di);
     }
 }

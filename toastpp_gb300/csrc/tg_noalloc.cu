@@ -12,14 +12,16 @@
 // The array is TG_NOALLOC_SCRATCH_BYTES (8 MiB) and is held by every GPU that
 // loads the library until the process exits.  All calls share it and it keeps
 // the last call's contents, so calls that overlap on the GPU (different
-// streams, or different host threads) race; serialise them.
+// streams, or different host threads) race; serialise them.  A call holds the
+// solver's own lock, as the solver's other entry points do, and runs on the
+// solver's device (the caller's current device is restored on return).
 #include <cstdint>
 #include <mutex>
 
 #include "../../include/toastgpu.h"
 #include "tg_jac.cuh"
 
-extern "C" int tg_solver_internal(tg_solver s, int* n, int* cplx, cudaStream_t* stream);
+extern "C" int tg_solver_internal(tg_solver s, int* n, int* cplx, cudaStream_t* stream, int* device, void** mu);
 
 namespace tg {
 
@@ -145,12 +147,31 @@ static int run(cudaStream_t st, int n, int nq, const V* phi, int nm, const V* mv
 
 }  // namespace tg
 
-extern "C" int tg_project_all_noalloc(tg_solver s, int nq, const double* phi, int nm, const double* mvec,
-                                      const int* link_ofs, const int* link_m, int scale, double* proj)
+namespace {
+// makes the solver's device current for the call and restores the caller's
+struct DeviceScope {
+    int prev = -1;
+    bool ok = false;
+    explicit DeviceScope(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) { cudaGetLastError(); prev = -1; }
+        ok = cudaSetDevice(dev) == cudaSuccess;
+        if (!ok) cudaGetLastError();
+    }
+    ~DeviceScope()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+}  // namespace
+
+static int project_all_noalloc(tg_solver s, int nq, const double* phi, int nm, const double* mvec,
+                               const int* link_ofs, const int* link_m, int scale, double* proj)
 {
     using namespace tg;
-    int n = 0, cplx = 0;
+    int n = 0, cplx = 0, device = 0;
     cudaStream_t st = 0;
+    void* mu = nullptr;
     if (!s || !phi || !mvec || !link_ofs || !proj || nq <= 0 || nm <= 0) {
         set_error("tg_project_all_noalloc: invalid argument");
         return TG_ERR_ARG;
@@ -159,7 +180,16 @@ extern "C" int tg_project_all_noalloc(tg_solver s, int nq, const double* phi, in
         set_error("tg_project_all_noalloc: scale must be TG_DATA_LIN or TG_DATA_LOG");
         return TG_ERR_ARG;
     }
-    tg_solver_internal(s, &n, &cplx, &st);
+    if (tg_solver_internal(s, &n, &cplx, &st, &device, &mu) != TG_OK) {
+        set_error("tg_project_all_noalloc: invalid solver");
+        return TG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> hold(*(std::mutex*)mu);
+    DeviceScope ds(device);
+    if (!ds.ok) {
+        set_error("tg_project_all_noalloc: cannot make the solver's device %d current", device);
+        return TG_ERR_CUDA;
+    }
     if (link_ofs[0] != 0) { set_error("tg_project_all_noalloc: link_ofs must start at 0"); return TG_ERR_ARG; }
     for (int q = 0; q < nq; q++)
         if (link_ofs[q + 1] < link_ofs[q]) { set_error("tg_project_all_noalloc: link_ofs not ascending"); return TG_ERR_ARG; }
@@ -178,4 +208,17 @@ extern "C" int tg_project_all_noalloc(tg_solver s, int nq, const double* phi, in
         return run<cd>(st, n, nq, (const cd*)phi, nm, (const cd*)mvec, link_ofs, link_m, nqm, scale, (cd*)proj,
                        (unsigned char*)scratch);
     return run<double>(st, n, nq, phi, nm, mvec, link_ofs, link_m, nqm, scale, proj, (unsigned char*)scratch);
+}
+
+extern "C" int tg_project_all_noalloc(tg_solver s, int nq, const double* phi, int nm, const double* mvec,
+                                      const int* link_ofs, const int* link_m, int scale, double* proj)
+{
+    // no exception may cross the C boundary (a lock that cannot be taken
+    // throws std::system_error)
+    try {
+        return project_all_noalloc(s, nq, phi, nm, mvec, link_ofs, link_m, scale, proj);
+    } catch (...) {
+        tg::set_error("tg_project_all_noalloc: internal error");
+        return TG_ERR_CUDA;
+    }
 }

@@ -428,11 +428,25 @@ struct Engine {
     }
     static int colw(int k) { return k >= 32 ? 32 : (k >= 16 ? 16 : (k >= 8 ? 8 : (k >= 4 ? 4 : (k >= 2 ? 2 : 1)))); }
 
+    // columns of a row split over this many warps in the level kernels: one
+    // (measured on the 30k cylinder, k = 160: 10.9 ms of IC applies per
+    // request unsplit, 11.6 / 12.1 / 16.3 ms split 2 / 3 / 5 ways: every
+    // extra warp repeats the row's index and value loads); TOASTGPU_IC_SPLIT
+    // overrides, for tuning runs
+    static int ic_split(int k)
+    {
+        const int nw = (k + 31) / 32;
+        int cs = 1;
+        if (const char* e = getenv("TOASTGPU_IC_SPLIT")) cs = std::max(1, std::min(nw, atoi(e)));
+        return cs;
+    }
+
     // pdl: a programmatic dependent of the previous level
     void launch_level_ell(bool fwd, int l, int off, int nr, int k, const V* in, V* out, const ColState* cst, bool pdl)
     {
-        const MeshDev& m = mesh->d;
-        unsigned g = cdiv_u((size_t)nr * 32, 256);
+        const int cs = ic_split(k);
+        const int njw = ((k + 31) / 32 + cs - 1) / cs;  // words per lane in each warp
+        const dim3 g(cdiv_u((size_t)nr * 32, 256), (unsigned)cdiv_u(k, 32 * njw));
         const ICHost& ch = ic_host();
         const ICDev& cd_ = ic_dev();
         const int w = fwd ? ch.fwd_ell_w[l] : ch.bwd_ell_w[l];
@@ -441,7 +455,7 @@ struct Engine {
         const int* ec = (fwd ? cd_.fwd_ell_col : cd_.bwd_ell_col) + eo;
         const V* ev = (fwd ? Lef : Leb) + eo;
         const V* src = fwd ? in : out;
-        switch ((k + 31) / 32) {
+        switch (njw) {
 #define TG_LE(J) case J: \
             if (fwd) { \
                 if (pdl) launch_pdl(ic_level_ell<V, J, true>, g, 256, 0, st, rows, nr, w, ec, ev, k, k, dinv, src, out, cst); \
@@ -2704,13 +2718,17 @@ int tg_launch_count(long long* count)
     API_END
 }
 
-// internal accessor for the fixed-scratch entry point (tg_noalloc.cu)
-__attribute__((visibility("hidden"))) int tg_solver_internal(tg_solver s, int* n, int* cplx, cudaStream_t* stream)
+// internal accessor for the fixed-scratch entry point (tg_noalloc.cu): the
+// solver's size, value type, stream, device and its handle lock
+__attribute__((visibility("hidden"))) int tg_solver_internal(tg_solver s, int* n, int* cplx, cudaStream_t* stream,
+                                                             int* device, void** mu)
 {
-    if (!s) return TG_ERR_ARG;
+    if (!s || !s->mesh) return TG_ERR_ARG;
     *n = s->mesh->d.n;
     *cplx = s->cplx;
     *stream = s->stream;
+    *device = s->mesh->device;
+    *mu = &s->mu;
     return TG_OK;
 }
 
