@@ -590,7 +590,8 @@ Mesh::~Mesh()
     for (void* p : ptrs) if (p) cudaFree(p);
     for (auto& g : d.ic) {
         void* q[] = {g.key, g.Lrowptr, g.Lcolidx, g.Lapos, g.Lkey, g.Ucolptr, g.Urow, g.Umap, g.fwd_lev_rows,
-                     g.bwd_lev_rows, g.fwd_ell_col, g.fwd_ell_src, g.bwd_ell_col, g.bwd_ell_src};
+                     g.bwd_lev_rows, g.fwd_ell_col, g.fwd_ell_src, g.bwd_ell_col, g.bwd_ell_src, g.fwd_lev_ptr,
+                     g.bwd_lev_ptr, g.fwd_ell_w, g.bwd_ell_w, g.fwd_ell_off, g.bwd_ell_off};
         for (void* p : q) if (p) cudaFree(p);
     }
 }
@@ -669,6 +670,12 @@ Mesh* mesh_build(int dim, int n, const double* coords, int ne, const int* el)
         g.fwd_ell_src = upload(c.fwd_ell_src);
         g.bwd_ell_col = upload(c.bwd_ell_col);
         g.bwd_ell_src = upload(c.bwd_ell_src);
+        g.fwd_lev_ptr = upload(c.fwd_lev_ptr);
+        g.bwd_lev_ptr = upload(c.bwd_lev_ptr);
+        g.fwd_ell_w = upload(c.fwd_ell_w);
+        g.bwd_ell_w = upload(c.bwd_ell_w);
+        g.fwd_ell_off = upload(c.fwd_ell_off);
+        g.bwd_ell_off = upload(c.bwd_ell_off);
     }
     return M;
 }

@@ -34,6 +34,9 @@ struct ICDev {
     int *key, *Lrowptr, *Lcolidx, *Lapos, *Lkey, *Ucolptr, *Urow, *Umap;
     int *fwd_lev_rows, *bwd_lev_rows;
     int *fwd_ell_col, *fwd_ell_src, *bwd_ell_col, *bwd_ell_src;
+    // per level: first row (nlev + 1 entries), ELL width and ELL offset, for
+    // the persistent sweep kernel
+    int *fwd_lev_ptr, *bwd_lev_ptr, *fwd_ell_w, *bwd_ell_w, *fwd_ell_off, *bwd_ell_off;
 };
 
 struct MeshHost {

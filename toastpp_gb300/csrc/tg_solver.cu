@@ -40,6 +40,9 @@ static std::atomic<long long> g_nlaunch{0};
 // SpMM variant chosen per (mesh, value type, k), shared by every solver of the process
 static std::mutex g_tune_mu;
 static std::map<std::tuple<long long, int, int>, int> g_tune;
+// IC apply variant (persistent sweep or per-level launches) per (mesh and
+// pattern, value type, k), chosen like the SpMM variant
+static std::map<std::tuple<long long, int, int>, bool> g_ictune;
 static std::string g_tune_log;  // one line per decision: candidates with their best launch time
 static const char* spmm_name(int v)
 {
@@ -286,6 +289,7 @@ struct Engine {
     int precon = 0;            // 0 none, 1 diag, 2 ich
     Profiler* prof = nullptr;
     DBuf w[9], part, cs, cnt, gbasis, gcol;
+    DBuf sweep;  // persistent IC sweep: [0] error flag, [1] barrier count
     Bounce bnc;
     GraphCache graphs;
 
@@ -470,18 +474,141 @@ struct Engine {
         }
     }
 
+    // The persistent sweep (ic_sweep_persistent, one cooperative launch for
+    // the whole apply) or a launch per level: both compute every row with the
+    // same sums in the same order (bit-identical results).  The first apply
+    // of a (mesh, pattern, value type, k) in the process times both (best of
+    // three, in a graph each) and keeps the faster for the process;
+    // TOASTGPU_IC_PERSISTENT=0 / 1 fixes the choice.
+    bool ic_persistent(int k, const V* in, V* out, const ColState* cst)
+    {
+        const char* e = getenv("TOASTGPU_IC_PERSISTENT");
+        if (e && (e[0] == '0' || e[0] == '1')) return e[0] == '1';
+        const auto key = std::make_tuple(mesh->uid * 4 + (icd ? 2 : ico), (int)sizeof(V) * 2 + (int)vt<V>::cplx, k);
+        {
+            std::lock_guard<std::mutex> g(g_tune_mu);
+            auto it = g_ictune.find(key);
+            if (it != g_ictune.end()) return it->second;
+        }
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        TG_CUDA(cudaStreamIsCapturing(st, &cs));
+        if (cs != cudaStreamCaptureStatusNone) return false;
+        float best[2] = {1e30f, 1e30f};
+        cudaEvent_t ev[2];
+        for (auto& x : ev) TG_CUDA(cudaEventCreate(&x));
+        for (int r = 0; r < 4; r++)
+            for (int v = 0; v < 2; v++) {
+                TG_CUDA(cudaEventRecord(ev[0], st));
+                ic_apply_variant(k, in, out, cst, v == 1);
+                TG_CUDA(cudaEventRecord(ev[1], st));
+                TG_CUDA(cudaEventSynchronize(ev[1]));
+                float ms = 0.f;
+                TG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+                if (r) best[v] = std::min(best[v], ms);  // the first round captures the graphs
+            }
+        for (auto& x : ev) cudaEventDestroy(x);
+        const bool p = best[1] < best[0];
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        auto res = g_ictune.emplace(key, p);
+        if (res.second) {
+            char line[200];
+            snprintf(line, sizeof line, "mesh %lld %s k=%d: ic per-level %.1fus persistent %.1fus -> %s\n",
+                     (long long)mesh->uid, vt_name<V>(), k, best[0] * 1e3f, best[1] * 1e3f,
+                     p ? "persistent" : "per-level");
+            g_tune_log += line;
+        }
+        return res.first->second;
+    }
+    template <int NJ>
+    void launch_sweep_persistent(int k, const V* in, V* out, const ColState* cst)
+    {
+        const ICHost& ch = ic_host();
+        const ICDev& ic = ic_dev();
+        auto kern = ic_sweep_persistent<V, NJ>;
+        static int grid[64] = {};
+        int dev = 0;
+        TG_CUDA(cudaGetDevice(&dev));
+        if (dev < 0 || dev >= 64) throw Error{TG_ERR_CUDA, "device index out of range"};
+        if (!grid[dev]) {
+            int nb = 0, nsm = 0;
+            TG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 1024, 0));
+            TG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+            grid[dev] = std::max(1, nb) * nsm;
+        }
+        IcSweepArgs<V> a;
+        a.nlev_f = (int)ch.fwd_lev_ptr.size() - 1;
+        a.nlev_b = (int)ch.bwd_lev_ptr.size() - 1;
+        a.lev_f = ic.fwd_lev_ptr; a.lev_b = ic.bwd_lev_ptr;
+        a.w_f = ic.fwd_ell_w; a.w_b = ic.bwd_ell_w; a.off_f = ic.fwd_ell_off; a.off_b = ic.bwd_ell_off;
+        a.rows_f = ic.fwd_lev_rows; a.rows_b = ic.bwd_lev_rows;
+        a.ecol_f = ic.fwd_ell_col; a.ecol_b = ic.bwd_ell_col;
+        a.eval_f = Lef; a.eval_b = Leb;
+        a.k = k; a.ld = k; a.dinv = dinv; a.b = in; a.y = out; a.st = cst;
+        int* fl = sweep.as<int>();
+        a.err = fl;
+        a.bar = (unsigned*)(fl + 1);
+        TG_CUDA(cudaMemsetAsync(a.bar, 0, sizeof(unsigned), st));
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid[dev]);
+        cfg.blockDim = dim3(1024);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        TG_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
+        g_nlaunch.fetch_add(1, std::memory_order_relaxed);
+    }
+
+    // the barrier flag of the persistent sweep: set when a wait gave up
+    void check_sweep()
+    {
+        if (!sweep.p) return;
+        int h[2] = {0, 0};
+        bnc.fetch(h, sweep.p, sizeof(h), st);
+        if (h[0]) {
+            TG_CUDA(cudaMemsetAsync(sweep.p, 0, sizeof(int), st));
+            throw Error{TG_ERR_CUDA, "IC(0) sweep: a grid barrier wait gave up (results discarded)"};
+        }
+    }
+
     // out = M^-1 in for the IC(0) preconditioner: the forward and backward
     // level kernels, captured once per (k, buffers) and replayed as one graph
+    // (k in 32..256: one persistent cooperative launch for both sweeps)
     void ic_apply(int k, const V* in, V* out, const ColState* cst)
+    {
+        const bool wide = k >= 32 && k <= 256;
+        // (the tuning runs repeat the apply: they need in and out apart)
+        const bool persistent = wide && in != out && ic_persistent(k, in, out, cst);
+        ProfScope ps(prof, PC_SWEEP, st);
+        ic_apply_variant(k, in, out, cst, persistent);
+    }
+
+    void ic_apply_variant(int k, const V* in, V* out, const ColState* cst, bool persistent)
     {
         const MeshDev& m = mesh->d;
         const ICHost& ch = ic_host();
         const ICDev& ic = ic_dev();
-        ProfScope ps(prof, PC_SWEEP, st);
         int cw = colw(k), ncg = (k + cw - 1) / cw, rpw = 32 / cw;
         std::vector<const void*> key = {(const void*)(size_t)k, in, out, cst, L, dinv, Lef, Leb, mesh,
-                                        (const void*)(size_t)ico, (const void*)icd};
+                                        (const void*)(size_t)ico, (const void*)icd, (const void*)(size_t)persistent};
         const bool wide = k >= 32 && k <= 256;
+        if (persistent) {
+            if (!sweep.p) {
+                sweep.ensure(2 * sizeof(int));
+                TG_CUDA(cudaMemsetAsync(sweep.p, 0, 2 * sizeof(int), st));
+            }
+            graphs.run(st, key, [&] {
+                switch ((k + 31) / 32) {
+#define TG_SW(J) case J: launch_sweep_persistent<J>(k, in, out, cst); break;
+                TG_SW(1) TG_SW(2) TG_SW(3) TG_SW(4) TG_SW(5) TG_SW(6) TG_SW(7) TG_SW(8)
+#undef TG_SW
+                }
+            });
+            return;
+        }
         graphs.run(st, key, [&] {
             const std::vector<int>& fp = ch.fwd_lev_ptr;
             for (size_t l = 0; l + 1 < fp.size(); l++) {
@@ -1053,7 +1180,7 @@ struct tg_solver_s {
     // direct solver: the complete factor's pattern (host and device)
     std::unique_ptr<ICHost> dh;
     ICDev dd{};
-    DBuf dbuf[14];
+    DBuf dbuf[20];
     Bounce bnc;                       // small device-to-host reads
     int jw_D = 0, jw_ready = 0;       // slots per node; bit 0 FP64 weights built, bit 1 FP32, bit 2 float-float
     Profiler prof;
@@ -1088,12 +1215,14 @@ static void direct_setup(tg_solver s)
     g.nlev_bwd = (int)c.bwd_lev_ptr.size() - 1;
     g.nell_fwd = (int)c.fwd_ell_col.size();
     g.nell_bwd = (int)c.bwd_ell_col.size();
-    int** dst[14] = {&g.key, &g.Lrowptr, &g.Lcolidx, &g.Lapos, &g.Lkey, &g.Ucolptr, &g.Urow, &g.Umap,
-                     &g.fwd_lev_rows, &g.bwd_lev_rows, &g.fwd_ell_col, &g.fwd_ell_src, &g.bwd_ell_col, &g.bwd_ell_src};
-    const std::vector<int>* src[14] = {&c.key, &c.Lrowptr, &c.Lcolidx, &c.Lapos, &c.Lkey, &c.Ucolptr, &c.Urow, &c.Umap,
+    int** dst[20] = {&g.key, &g.Lrowptr, &g.Lcolidx, &g.Lapos, &g.Lkey, &g.Ucolptr, &g.Urow, &g.Umap,
+                     &g.fwd_lev_rows, &g.bwd_lev_rows, &g.fwd_ell_col, &g.fwd_ell_src, &g.bwd_ell_col, &g.bwd_ell_src,
+                     &g.fwd_lev_ptr, &g.bwd_lev_ptr, &g.fwd_ell_w, &g.bwd_ell_w, &g.fwd_ell_off, &g.bwd_ell_off};
+    const std::vector<int>* src[20] = {&c.key, &c.Lrowptr, &c.Lcolidx, &c.Lapos, &c.Lkey, &c.Ucolptr, &c.Urow, &c.Umap,
                                        &c.fwd_lev_rows, &c.bwd_lev_rows, &c.fwd_ell_col, &c.fwd_ell_src,
-                                       &c.bwd_ell_col, &c.bwd_ell_src};
-    for (int t = 0; t < 14; t++) {
+                                       &c.bwd_ell_col, &c.bwd_ell_src, &c.fwd_lev_ptr, &c.bwd_lev_ptr, &c.fwd_ell_w,
+                                       &c.bwd_ell_w, &c.fwd_ell_off, &c.bwd_ell_off};
+    for (int t = 0; t < 20; t++) {
         upload_sync(s->dbuf[t], *src[t]);
         *dst[t] = s->dbuf[t].as<int>();
     }
@@ -1363,7 +1492,19 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
 }
 
 template <class V64, class V32>
+static void solve_nm_body(tg_solver s, int k, const V64* B, V64* X, ColState* co, bool zero_guess);
+
+// solve_nm_body, then the persistent sweep's barrier flag of both engines
+template <class V64, class V32>
 static void solve_nm(tg_solver s, int k, const V64* B, V64* X, ColState* co, bool zero_guess = false)
+{
+    solve_nm_body<V64, V32>(s, k, B, X, co, zero_guess);
+    engine<V64>(s).check_sweep();
+    if (s->precision == TG_PREC_MIXED) engine<V32>(s).check_sweep();
+}
+
+template <class V64, class V32>
+static void solve_nm_body(tg_solver s, int k, const V64* B, V64* X, ColState* co, bool zero_guess)
 {
     const MeshDev& m = s->mesh->d;
     int n = m.n;
