@@ -30,8 +30,20 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 UNIT = "source-solves/s"
+# DRAM traffic per launch of the dominant kernel (ncu dram__bytes_read.sum +
+# dram__bytes_write.sum), captured on a smaller case of the same kernel and
+# scaled to the workload by the units one launch processes; the capture
+# commands and counters are in profiles/
+TRAFFIC = {
+    ("c2_cyl30k_fd", "jacobian_ff"): (
+        (179.457792e6 + 1477.513e6) * (12800 * 61620) / (12800 * 15008),
+        "ncu on the 7504-node cylinder (12800 x 15008 J: read 179.5 MB + write 1477.5 MB), scaled by the J "
+        "entries to 12800 x 61620 (profiles/jacobian_ff_kernel_cyl7k_fp64.md)"),
+}
 LABELS = {"c0_disc3k_cw": "2D 3.3k-node disc CW", "c1_disc13k_fd": "2D 13k-node disc 100 MHz",
-          "c2_cyl30k_fd": "3D 30k-node cylinder 100 MHz", "c3_box250k_fd": "3D 250k-node box 100 MHz"}
+          "c2_cyl30k_fd": "3D 30k-node cylinder 100 MHz", "c3_box250k_fd": "3D 250k-node box 100 MHz",
+          "c2s_cyl7k_fd": "3D 7.5k-node cylinder 100 MHz (profiling case)",
+          "c3s_box106k_fd": "3D 106k-node box 100 MHz (profiling case)"}
 
 
 def metric_of(cfg):
@@ -57,7 +69,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c2_cyl30k_fd",
-                    choices=["c0_disc3k_cw", "c1_disc13k_fd", "c2_cyl30k_fd", "c3_box250k_fd"])
+                    choices=["c0_disc3k_cw", "c1_disc13k_fd", "c2_cyl30k_fd", "c3_box250k_fd", "c2s_cyl7k_fd",
+                             "c3s_box106k_fd"])
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--e2e-slots", type=int, default=1, help="e2e leg: request-server slots")
     ap.add_argument("--grid", type=int, default=32,
@@ -78,9 +91,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--serving", action="store_true",
                     help="run the mixed-mesh request stream through the request server instead")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream leg of the default run")
     ap.add_argument("--requests", type=int, default=24, help="serving: requests in the stream")
     ap.add_argument("--rate", type=float, default=20.0, help="serving: mean arrival rate (1/s)")
     ap.add_argument("--slots", type=int, default=4, help="serving: concurrent requests on the device")
+    ap.add_argument("--src-max-large", type=int, default=64, help="serving: source cap on the 250k box")
     return ap.parse_args()
 
 
@@ -324,8 +339,9 @@ def run_gpu(args):
     nnz_l = (nnz - n) // 2
     names = {capi.PROF_SPMM: f"SpMM (autotuned spmm_halo/vec/wide kernel, k={nq + nm})",
              capi.PROF_SWEEP: "IC(0) apply: the level kernels of both sweeps (ic_level_ell) in one graph",
-             capi.PROF_JAC: "jacobian_kernel", capi.PROF_ASM: "assembly + IC(0) factor",
-             capi.PROF_PROJ: "project_kernel"}
+             capi.PROF_JAC: ("jacobian_kernel (FP32)" if j_fp32 else
+                             "jacobian_ff_kernel (FP64 Jacobian in float-float arithmetic)"),
+             capi.PROF_ASM: "assembly + IC(0) factor", capi.PROF_PROJ: "project_kernel"}
     dom = max(prof, key=lambda c: prof[c][0])
     vb = (8 if args.precision == "mixed" else 16) // (1 if cplx else 2)
     jb = 4 if j_fp32 else 8
@@ -352,6 +368,16 @@ def run_gpu(args):
                 "frac": ach / peak, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "traffic": None, "algorithmic_bytes_per_launch": alg_bytes,
                 "launch_ms": dom_ms / dom_cnt}
+        tr = TRAFFIC.get((args.config, dom == capi.PROF_JAC and not j_fp32 and "jacobian_ff"
+                          or dom == capi.PROF_SWEEP and "ic_level_ell" or None))
+        if tr:
+            # ncu dram__bytes_read.sum + dram__bytes_write.sum per launch,
+            # from a capture of a smaller case scaled by the units processed
+            roof["traffic"] = tr[0]
+            roof["traffic_source"] = tr[1]
+        if dom == capi.PROF_JAC and not j_fp32:
+            roof["note"] = ("the float-float Jacobian is bound by FP32 issue (packed f32x2 pipe), not by HBM: "
+                            "its J write is the only large traffic")
     shares = {names[c]: {"ms_per_step": prof[c][0] / psteps, "launches_or_scopes": prof[c][1] // psteps}
               for c in prof}
 
@@ -488,6 +514,16 @@ def run_gpu(args):
             info = cpu_request_time(P, tol=args.tol)
             cpu = {"value": nsolves / info["t_request"], "unit": UNIT, "cores": info["threads"], "kind": "port",
                    "sample": info["sample"], "its_per_src": info["its_per_src"]}
+        serving_leg = None
+        if not args.no_serving and ws == 1:
+            torch.cuda.synchronize()
+            wl, sv = serving_summary(args, 12, 10.0, args.slots)
+            serving_leg = {"workload": wl, "slots": args.slots,
+                           "mixed": {k: sv["mixed"][k] for k in ("p50_ms", "p99_ms", "solves_per_s", "requests")},
+                           "fp64": {k: sv["fp64"][k] for k in ("p50_ms", "p99_ms", "solves_per_s", "requests")},
+                           "saturated_solves_per_s": {"mixed": sv["mixed_saturated"]["solves_per_s"],
+                                                      "fp64": sv["fp64_saturated"]["solves_per_s"]},
+                           "per_mesh_p50_ms_mixed": sv["mixed"]["per_mesh_p50_ms"]}
         clocks = clk.summary()
         line = {
             "metric": metric_of(args.config), "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -511,7 +547,7 @@ def run_gpu(args):
             "roofline": roof, "kernel_time_per_step": shares,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "grid_jacobian": grid,
             "element_jacobian": element,
-            "clocks": clocks, "wall_s": wall, "compare": compare,
+            "clocks": clocks, "wall_s": wall, "compare": compare, "serving": serving_leg,
             "spmm_autotuner": capi.tuner_log().strip().splitlines(),
         }
         print(json.dumps(line), flush=True)
@@ -661,42 +697,52 @@ def compare_legs(args, P, gm, s, stream, dev, links, d_par, omega, d_src, h_src,
     return out
 
 
-def run_serving(args):
+def serving_summary(args, requests, rate, slots):
     """The serving stream (Poisson arrivals over the 2D 3.3k / 2D 13k / 3D 30k /
-    3D 250k meshes, 8-128 sources, CW or 100 MHz, fresh parameters per request)
-    through the request server, mixed precision and plain FP64."""
-    import torch
-    torch.cuda.set_device(0)
-    from toastpp_gb300 import build as B
-    B.build()
+    3D 250k meshes, 8-128 sources (at most --src-max-large on the box), CW or
+    100 MHz, fresh parameters per request) through the request server, mixed
+    precision and plain FP64: p50 / p99 latency and source-solves/s at the
+    given arrival rate, and the same requests all arriving at once."""
     from toastpp_gb300 import serving
     ms = serving.MeshSet()
     out = {}
     for prec in ("mixed", "fp64"):
-        spec = serving.StreamSpec(requests=args.requests, rate_hz=args.rate, seed=1, precision=prec, tol=1e-10)
-        # one pass over the same stream first, so that every solver and graph is resident
-        warm = serving.make_requests(ms, serving.StreamSpec(requests=min(8, args.requests), rate_hz=1e6, seed=2,
-                                                            precision=prec, tol=1e-10))
-        serving.run_stream(warm, slots=args.slots)
+        spec = serving.StreamSpec(requests=requests, rate_hz=rate, seed=1, precision=prec, tol=1e-10,
+                                  src_max_large=args.src_max_large)
+        # one pass over a short stream first, so that every solver and graph is resident
+        warm = serving.make_requests(ms, serving.StreamSpec(requests=min(8, requests), rate_hz=1e6, seed=2,
+                                                            precision=prec, tol=1e-10,
+                                                            src_max_large=args.src_max_large))
+        serving.run_stream(warm, slots=slots)
+        del warm
         reqs = serving.make_requests(ms, spec)
-        done, st, wall = serving.run_stream(reqs, slots=args.slots)
+        done, st, wall = serving.run_stream(reqs, slots=slots)
         out[prec] = serving.summarize(done, st, wall)
         del reqs, done
-        # the same requests all arriving at once: the server's capacity
-        sat = serving.make_requests(ms, serving.StreamSpec(requests=args.requests, rate_hz=1e6, seed=1,
-                                                           precision=prec, tol=1e-10))
-        done, st, wall = serving.run_stream(sat, slots=args.slots)
+        sat = serving.make_requests(ms, serving.StreamSpec(requests=requests, rate_hz=1e6, seed=1, precision=prec,
+                                                           tol=1e-10, src_max_large=args.src_max_large))
+        done, st, wall = serving.run_stream(sat, slots=slots)
         out[prec + "_saturated"] = serving.summarize(done, st, wall)
         del sat, done
+    workload = (f"Poisson arrivals {rate}/s, meshes 2D 3.3k/2D 13k/3D 30k/3D 250k (0.4/0.3/0.2/0.1), 8-128 sources "
+                f"(<= {args.src_max_large} on the 250k box: 16 GB FP32 Jacobian per request at 64), CW or 100 MHz, "
+                "forward + projections + nodal FP32 Jacobian per request, tol 1e-10")
+    return workload, out
+
+
+def run_serving(args):
+    """The serving stream alone, as its own JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    from toastpp_gb300 import build as B
+    B.build()
+    workload, out = serving_summary(args, args.requests, args.rate, args.slots)
     m = out["mixed"]
     line = {"metric": "serving stream: source-solves/s with p50/p99 request latency", "value": m["solves_per_s"],
             "unit": "source-solves/s", "n_gpus": 1, "steps": args.requests, "warmup": 8, "higher_is_better": True,
             "dtype": "complex-f32 inner / complex-f64 refinement (mixed); complex-f64 (fp64 leg)",
             "data": "synthetic (seeded meshes, optodes, parameter fields, arrivals)",
-            "config": {"workload": f"Poisson arrivals {args.rate}/s, meshes 2D 3.3k/2D 13k/3D 30k/3D 250k "
-                                   "(0.4/0.3/0.2/0.1), 8-128 sources (<=32 on the 250k box), CW or 100 MHz, "
-                                   "forward + projections + nodal Jacobian per request, tol 1e-10",
-                       "slots": args.slots},
+            "config": {"workload": workload, "slots": args.slots},
             "latency_ms": {"p50": m["p50_ms"], "p99": m["p99_ms"]}, "mixed": m, "fp64": out["fp64"],
             "saturated": {"mixed": out["mixed_saturated"], "fp64": out["fp64_saturated"]}}
     print(json.dumps(line), flush=True)

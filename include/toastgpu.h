@@ -165,7 +165,7 @@ int tg_solver_set_refinement(tg_solver s, double inner_tol, int max_outer, int i
 /* mixed precision only: the componentwise backward-error bound of every
    solution (default 1e-10; 0 turns the test off).  Besides |b - A x| <= tol |b|
    the FP64 refinement then continues until
-       max_i |b - A x|_i / (|A| |x| + |b|)_i <= cw_tol,  |z| = |Re z| + |Im z|,
+       max_i |b - A x|_i / (|A| |x| + |b|)_i <= cw_tol,  |z| = max(|Re z|, |Im z|),
    the Oettli-Prager measure that iterative refinement stops on.  The normwise
    test alone bounds the error of the large entries of a field; the far
    entries, e^-20 of the peak at the far detectors, keep an error of the order

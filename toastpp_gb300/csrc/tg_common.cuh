@@ -95,10 +95,33 @@ TGHD double nrm2(double a) { return a * a; }
 TGHD float nrm2(float a) { return a * a; }
 TGHD double nrm2(cd a) { return a.x * a.x + a.y * a.y; }
 TGHD float nrm2(cf a) { return a.x * a.x + a.y * a.y; }
-// |Re a| + |Im a| rounded to FP32: the magnitude the componentwise
-// backward-error test works with (within a factor sqrt 2 of |a|)
-TGHD float mag1f(double a) { return (float)fabs(a); }
-TGHD float mag1f(cd a) { return (float)(fabs(a.x) + fabs(a.y)); }
+// The magnitude the componentwise backward-error test works with:
+// max(|Re a|, |Im a|) as a float (within a factor sqrt 2 of |a|), formed
+// from the bit pattern with integer operations (mantissa truncated to 23
+// bits; below the FP32 range 0, above it inf), so the test costs no FP64
+// arithmetic on a GPU whose FP64 rate is low.
+TGHD float mag_bits(unsigned long long b)  // b: |x| as the bits of a double
+{
+    const int e = (int)(b >> 52) - 1023 + 127;
+    if (e <= 0) return 0.0f;
+    if (e >= 255) return __builtin_huge_valf();
+    unsigned u = ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu);
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+TGHD unsigned long long abs_bits(double a)
+{
+    unsigned long long b;
+    memcpy(&b, &a, 8);
+    return b & 0x7fffffffffffffffull;
+}
+TGHD float mag1f(double a) { return mag_bits(abs_bits(a)); }
+TGHD float mag1f(cd a)
+{
+    const unsigned long long x = abs_bits(a.x), y = abs_bits(a.y);  // non-negative: ordered as integers
+    return mag_bits(x > y ? x : y);
+}
 
 // value conversion between precisions
 template <class To, class From> TGHD To vcast(From a);

@@ -1418,7 +1418,7 @@ static __global__ void rel_flags_kernel(int k, const ColState* __restrict__ co, 
 // Componentwise backward error of an FP64 solution (the Oettli-Prager
 // measure that iterative refinement stops on): for each listed column c,
 //   berr_c = max_i |r_ic| / (|A| |x_c| + |b_c|)_i,   r = b - A x,
-// with |z| = |Re z| + |Im z| and the sums in FP32 (the test needs the
+// with |z| = max(|Re z|, |Im z|) and the sums in FP32 (the test needs the
 // magnitude of the denominator, not its digits).  A solution whose berr is at
 // the FP64 rounding level is exact for a matrix and right-hand side perturbed
 // by that relative amount entry by entry, so its small entries (far from the

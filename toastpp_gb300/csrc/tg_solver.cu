@@ -169,7 +169,20 @@ static inline unsigned cdiv_u(size_t a, size_t b) { return (unsigned)((a + b - 1
 // mapped page-locked memory instead of going through the copy engines: a
 // large copy in flight on another stream (a Jacobian going out while the
 // next request solves) would hold a copy-engine read up behind it.
+// small device reads: a kernel writes them into mapped page-locked memory
+// (never queued behind a large copy on a copy engine).  Host-mapped stores
+// are slow one word at a time, so whole 16-byte words go, from several
+// blocks when the read is large; the tail (nw not a multiple of 4) by words.
 static __global__ void bounce_kernel(const unsigned* __restrict__ src, unsigned* __restrict__ dst, int nw)
+{
+    const int n4 = nw >> 2;
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) d4[i] = s4[i];
+    if (blockIdx.x == 0 && threadIdx.x < (nw & 3)) dst[4 * n4 + threadIdx.x] = src[4 * n4 + threadIdx.x];
+}
+
+static __global__ void bounce_words_kernel(const unsigned* __restrict__ src, unsigned* __restrict__ dst, int nw)
 {
     for (int i = threadIdx.x; i < nw; i += blockDim.x) dst[i] = src[i];
 }
@@ -198,7 +211,14 @@ struct Bounce {
             TG_CUDA(cudaHostGetDevicePointer((void**)&d, h, 0));
             bytes = nb;
         }
-        launch(bounce_kernel, 1, 256, 0, st, (const unsigned*)src, d, (int)(b / 4));
+        const int nw = (int)(b / 4);
+        // 16-byte words need 16-byte aligned addresses (device buffers and
+        // the page-locked buffer are; a field of a struct may not be)
+        if (((size_t)src & 15) == 0)
+            launch(bounce_kernel, std::max(1u, std::min(64u, cdiv_u((size_t)nw / 4, 256))), 256, 0, st,
+                   (const unsigned*)src, d, nw);
+        else
+            launch(bounce_words_kernel, 1, 256, 0, st, (const unsigned*)src, d, nw);
         TG_CUDA(cudaStreamSynchronize(st));
         std::memcpy(dst, h, b);
     }
@@ -1177,6 +1197,7 @@ struct tg_solver_s {
     DBuf jwff;                        // the same as packed float-float (float-float Jacobian kernel)
     DBuf rel_cnt, rel_idx, rel_xc, rel_ac;
     DBuf absA, berr_max;              // |entries| of F in FP32, per-column backward-error maxima
+    DBuf results;                     // per-column results, compact, for the final read
     // direct solver: the complete factor's pattern (host and device)
     std::unique_ptr<ICHost> dh;
     ICDev dd{};
@@ -1578,14 +1599,30 @@ static void solve_nm_body(tg_solver s, int k, const V64* B, V64* X, ColState* co
     }
 }
 
+// per column: its, status, |r| / |b| (the tg_result fields), 16 bytes
+struct ColResult {
+    int its, status;
+    double rel_err;
+};
+static __global__ void col_results_kernel(int k, const ColState* __restrict__ co, ColResult* __restrict__ out)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    out[c].its = co[c].its;
+    out[c].status = co[c].status;
+    out[c].rel_err = co[c].bnorm > 0 ? co[c].err / co[c].bnorm : 0.0;
+}
+
 static void read_results(tg_solver s, int k, const ColState* co, tg_result* res)
 {
-    std::vector<ColState> h(k);
-    s->bnc.fetch(h.data(), co, sizeof(ColState) * k, s->stream);
+    ColResult* d = (ColResult*)s->results.ensure((size_t)k * sizeof(ColResult));
+    launch(col_results_kernel, cdiv_u(k, 128), 128, 0, s->stream, k, co, d);
+    std::vector<ColResult> h(k);
+    s->bnc.fetch(h.data(), d, sizeof(ColResult) * k, s->stream);
     for (int c = 0; c < k; c++) {
         res[c].it_count = h[c].its;
         res[c].status = h[c].status;
-        res[c].rel_err = h[c].bnorm > 0 ? h[c].err / h[c].bnorm : 0.0;
+        res[c].rel_err = h[c].rel_err;
     }
 }
 

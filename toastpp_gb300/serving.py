@@ -31,7 +31,8 @@ class StreamSpec:
     rate_hz: float = 20.0          # mean arrival rate
     src_min: int = 8
     src_max: int = 128
-    src_max_large: int = 32        # cap for the 250k mesh (its Jacobian is 2 x 2 nQM x 2n)
+    src_max_large: int = 64        # cap for the 250k mesh: its FP32 Jacobian is 2 nQM x 2n, 16 GB at 64
+                                   # sources and 65 GB at 128, against 199 GB of host memory on the GPU machine
     seed: int = 0
     precision: str = "mixed"
     tol: float = 1e-10

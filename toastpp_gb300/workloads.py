@@ -225,4 +225,10 @@ CONFIGS = {
     "c1_disc13k_fd": lambda seed=0: disc(64, seed, 100.0, 32),
     "c2_cyl30k_fd": lambda seed=0: cylinder(seed=seed),
     "c3_box250k_fd": lambda seed=0: box(seed=seed),
+    # the 30k cylinder's optode layout on a 7.5k-node cylinder: the small case
+    # of the profiling captures (a few GB on the device)
+    "c2s_cyl7k_fd": lambda seed=1: cylinder(rings=12, layers=16, seed=seed),
+    # a 106k-node box (inputs past L2, a few GB): profiling captures of the
+    # SpMM and IC(0) kernels at the 250k box's column count
+    "c3s_box106k_fd": lambda seed=0: box(nx=48, ny=48, nz=46, seed=seed),
 }
