@@ -1,0 +1,690 @@
+// fwdsolver_gpu.cc -- the reference's own TFwdSolver<T> class on the GPU.
+//
+// This translation unit takes the place of src/libstoast/fwdsolver.cc when a
+// Toast++ build links against libtoastgpu.so: it includes the reference's
+// fwdsolver.h unchanged and defines every member of TFwdSolver<T> (and the
+// free ProjectSingle / ProjectAll) by forwarding to the C ABI, so callers
+// such as src/supertoast/fwdfem.cc:180-250 or src/python/toastmodule.cc
+// compile and link unedited.  Every instantiation the header declares
+// (float, double, complex<float>, complex<double>) is provided; the single-
+// precision ones convert to FP64 at the boundary.
+//
+// The class layout is fixed by the header, so each solver's GPU handles live
+// in a side table keyed by the object's address.  The reference's public
+// members keep their meaning: F holds the system matrix after Reset (read
+// back from the GPU, as callers read FWS.F), iterative_tol / precontp /
+// solvertp / method are the settings.  Errors go through xERROR, as in the
+// reference.  Build recipe: toastpp_gb300/shim/Makefile.
+#define __FWDSOLVER_CC
+#define STOASTLIB_IMPLEMENTATION
+#include "stoastlib.h"
+
+#include <complex>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "toastgpu.h"
+#include "shim_common.h"
+
+using namespace std;
+
+namespace {
+
+// per-solver GPU state
+struct GpuSolver {
+    tg_mesh mesh = nullptr;
+    tg_solver solver = nullptr;
+    int n = 0;
+    bool reset = false;
+};
+std::mutex g_mu;
+std::map<const void*, GpuSolver> g_solvers;
+// per-mesh GPU meshes and solvers for the free functions
+struct GpuMesh {
+    tg_mesh mesh = nullptr;
+    tg_solver solver[2] = {nullptr, nullptr};  // real, complex
+    int n = 0, ne = 0;
+};
+std::map<const void*, GpuMesh> g_meshes;
+
+
+template <class T> struct Prec { typedef double D; static const bool cplx = false; };
+template <> struct Prec<std::complex<double> > { typedef std::complex<double> D; static const bool cplx = true; };
+template <> struct Prec<std::complex<float> > { typedef std::complex<double> D; static const bool cplx = true; };
+
+}  // namespace
+
+namespace tgshim {
+
+void check(int rc, const char* what)
+{
+    if (rc != TG_OK) xERROR("%s: %s", what, tg_last_error());
+}
+
+// the GPU mesh of a QMMesh: node coordinates and P1 elements (Triangle3 /
+// Tetrahedron4; other element types are outside this library)
+tg_mesh make_mesh(const QMMesh* mesh)
+{
+    const int n = mesh->nlen(), ne = mesh->elen(), dim = mesh->Dimension();
+    std::vector<double> xy((size_t)n * dim);
+    for (int i = 0; i < n; i++)
+        for (int d = 0; d < dim; d++) xy[(size_t)i * dim + d] = mesh->nlist[i][d];
+    const int nn = dim == 2 ? 3 : 4;
+    std::vector<int> el((size_t)ne * nn);
+    for (int e = 0; e < ne; e++) {
+        const Element* E = mesh->elist[e];
+        if (E->nNode() != nn || (E->Type() != ELID_TRI3 && E->Type() != ELID_TET4))
+            xERROR("libtoastgpu: element %d is not a 3-noded triangle or 4-noded tetrahedron", e);
+        for (int j = 0; j < nn; j++) el[(size_t)e * nn + j] = E->Node[j];
+    }
+    tg_mesh m = nullptr;
+    check(tg_mesh_create(dim, n, xy.data(), ne, el.data(), &m), "tg_mesh_create");
+    return m;
+}
+
+GpuMesh& mesh_gpu(const QMMesh* mesh, bool cplx)
+{
+    GpuMesh& g = g_meshes[mesh];
+    if (g.mesh && (g.n != mesh->nlen() || g.ne != mesh->elen())) {  // another mesh at the same address
+        for (auto& s : g.solver)
+            if (s) tg_solver_destroy(s);
+        tg_mesh_destroy(g.mesh);
+        g = GpuMesh();
+    }
+    if (!g.mesh) {
+        g.mesh = make_mesh(mesh);
+        g.n = mesh->nlen();
+        g.ne = mesh->elen();
+    }
+    if (!g.solver[cplx])
+        check(tg_solver_create(g.mesh, cplx, TG_SOLVER_BICGSTAB, TG_PRECON_ICH, 1e-10, 0, TG_PREC_FP64,
+                               &g.solver[cplx]),
+              "tg_solver_create");
+    return g;
+}
+
+// the QMMesh link list (qmmesh.h:24-36) as offsets and detector indices
+void links_of(const QMMesh* mesh, std::vector<int>& ofs, std::vector<int>& lm)
+{
+    ofs.assign(mesh->nQ + 1, 0);
+    lm.clear();
+    for (int q = 0; q < mesh->nQ; q++) {
+        for (int i = 0; i < mesh->nQMref[q]; i++) lm.push_back(mesh->QMref[q][i]);
+        ofs[q + 1] = (int)lm.size();
+    }
+}
+
+tg_solver mesh_solver(const QMMesh* mesh, bool cplx, tg_mesh* m)
+{
+    std::lock_guard<std::mutex> g(g_mu);
+    GpuMesh& gm = mesh_gpu(mesh, cplx);
+    if (m) *m = gm.mesh;
+    return gm.solver[cplx];
+}
+
+}  // namespace tgshim
+
+using namespace tgshim;
+
+namespace {
+
+// dense source-major FP64 copies (complex: interleaved re, im)
+template <class T>
+void put(double* dst, const T& v)
+{
+    dst[0] = (double)v;
+}
+template <class R>
+void put(double* dst, const std::complex<R>& v)
+{
+    dst[0] = (double)v.real();
+    dst[1] = (double)v.imag();
+}
+template <class T>
+T get(const double* src)
+{
+    return (T)src[0];
+}
+template <>
+std::complex<float> get<std::complex<float> >(const double* src)
+{
+    return std::complex<float>((float)src[0], (float)src[1]);
+}
+template <>
+std::complex<double> get<std::complex<double> >(const double* src)
+{
+    return std::complex<double>(src[0], src[1]);
+}
+
+template <class T>
+std::vector<double> dense_rows(const TCompRowMatrix<T>& A, int r0, int r1, int n)
+{
+    const int w = Prec<T>::cplx ? 2 : 1;
+    std::vector<double> out((size_t)(r1 - r0) * n * w, 0.0);
+    const T* val = A.ValPtr();
+    for (int r = r0; r < r1; r++)
+        for (int k = A.rowptr[r]; k < A.rowptr[r + 1]; k++)
+            put(&out[((size_t)(r - r0) * n + A.colidx[k]) * w], val[k]);
+    return out;
+}
+
+int method_of(IterativeMethod m)
+{
+    switch (m) {
+    case ITMETHOD_CG: return TG_SOLVER_CG;
+    case ITMETHOD_BICGSTAB: return TG_SOLVER_BICGSTAB;
+    case ITMETHOD_GMRES: return TG_SOLVER_GMRES;
+    default: xERROR("libtoastgpu: the BiCG and Gauss-Seidel solvers are not provided"); return -1;
+    }
+}
+
+int precon_of(PreconType p)
+{
+    switch (p) {
+    case PRECON_DIAG: return TG_PRECON_DIAG;
+    case PRECON_ICH: return TG_PRECON_ICH;
+    case PRECON_DILU: return TG_PRECON_DILU;  // built as none, as TFwdSolver::Allocate does
+    default: return TG_PRECON_NONE;
+    }
+}
+
+}  // namespace
+
+// =========================================================================
+// construction and settings (fwdsolver.cc:16-155, 1084-1290)
+
+template <class T>
+TFwdSolver<T>::TFwdSolver(const QMMesh* mesh, LSOLVER linsolver, double tol)
+{
+    Setup();
+    meshptr = mesh;
+    solvertp = linsolver;
+    iterative_tol = tol;
+}
+
+template <class T>
+TFwdSolver<T>::TFwdSolver(const QMMesh* mesh, const char* solver, double tol, int nth)
+{
+    Setup(nth);
+    meshptr = mesh;
+    SetLinSolver(solver, tol);
+}
+
+template <class T>
+TFwdSolver<T>::TFwdSolver(const QMMesh* mesh, ParamParser& pp)
+{
+    Setup();
+    meshptr = mesh;
+    ReadParams(pp);
+}
+
+template <class T>
+TFwdSolver<T>::~TFwdSolver()
+{
+    {
+        std::lock_guard<std::mutex> g(g_mu);
+        auto it = g_solvers.find(this);
+        if (it != g_solvers.end()) {
+            if (it->second.solver) tg_solver_destroy(it->second.solver);
+            if (it->second.mesh) tg_mesh_destroy(it->second.mesh);
+            g_solvers.erase(it);
+        }
+    }
+    if (F) delete F;
+    if (FL) delete FL;
+    if (Fd) delete Fd;
+    if (B) delete B;
+    if (pphi) delete[] pphi;
+    DeleteType();
+}
+
+template <class T>
+void TFwdSolver<T>::Setup(int nth)
+{
+    solvertp = LSOLVER_UNDEFINED;
+    method = ITMETHOD_CG;
+    iterative_tol = 1e-10;
+    iterative_maxit = 0;
+    precontp = PRECON_NULL;
+    dscale = DATA_LIN;
+    F = 0; FL = 0; Fd = 0; B = 0;
+    precon = 0;
+    SuperLU = 0;
+    meshptr = 0;
+    pphi = 0;
+    unwrap_phase = false;
+    (void)nth;
+}
+
+template <class T> void TFwdSolver<T>::SetupType(int) {}
+template <class T> void TFwdSolver<T>::DeleteType() {}
+
+template <class T>
+void TFwdSolver<T>::SetDataScaling(DataScale scl)
+{
+    xASSERT(scl != DATA_DEFAULT, "Invalid input argument");
+    dscale = scl;
+}
+
+template <class T>
+DataScale TFwdSolver<T>::GetDataScaling() const
+{
+    return dscale;
+}
+
+template <class T>
+void TFwdSolver<T>::SetPrecon(PreconType type)
+{
+    precontp = type;
+}
+
+template <class T>
+void TFwdSolver<T>::SetLinSolver(const char* solver, double tol)
+{
+    if (!strcasecmp(solver, "DIRECT")) {
+        solvertp = LSOLVER_DIRECT;
+    } else {
+        solvertp = LSOLVER_ITERATIVE;
+        iterative_tol = tol;
+        if (!strcasecmp(solver, "CG")) method = ITMETHOD_CG;
+        else if (!strcasecmp(solver, "BICG")) method = ITMETHOD_BICG;
+        else if (!strcasecmp(solver, "BICGSTAB")) method = ITMETHOD_BICGSTAB;
+        else if (!strcasecmp(solver, "GMRES")) method = ITMETHOD_GMRES;
+        else method = ITMETHOD_GAUSSSEIDEL;
+    }
+}
+
+// the same items and prompts as fwdsolver.cc:1084-1227, so scripted input
+// (the reference's test Makefiles) drives both alike
+template <class T>
+void TFwdSolver<T>::ReadParams(ParamParser& pp)
+{
+    char cbuf[256];
+    solvertp = LSOLVER_UNDEFINED;
+    dscale = DATA_DEFAULT;
+    if (pp.GetString("DATASCALE", cbuf)) {
+        if (!strcasecmp(cbuf, "LIN")) dscale = DATA_LIN;
+        else if (!strcasecmp(cbuf, "LOG")) dscale = DATA_LOG;
+    }
+    while (dscale == DATA_DEFAULT) {
+        int cmd;
+        cout << "\nSelect data scaling:\n(1) Linear\n(2) Logarithmic\n[1|2] >> ";
+        cin >> cmd;
+        if (cmd == 1) dscale = DATA_LIN;
+        else if (cmd == 2) dscale = DATA_LOG;
+    }
+    if (pp.GetString("LINSOLVER", cbuf)) {
+        if (!strcasecmp(cbuf, "DIRECT")) solvertp = LSOLVER_DIRECT;
+        else if (!strcasecmp(cbuf, "CG")) solvertp = LSOLVER_ITERATIVE, method = ITMETHOD_CG;
+        else if (!strcasecmp(cbuf, "BICGSTAB")) solvertp = LSOLVER_ITERATIVE, method = ITMETHOD_BICGSTAB;
+        else if (!strcasecmp(cbuf, "BICG")) solvertp = LSOLVER_ITERATIVE, method = ITMETHOD_BICG;
+        else if (!strcasecmp(cbuf, "GMRES")) solvertp = LSOLVER_ITERATIVE, method = ITMETHOD_GMRES;
+        else if (!strcasecmp(cbuf, "GAUSSSEIDEL")) solvertp = LSOLVER_ITERATIVE, method = ITMETHOD_GAUSSSEIDEL;
+    }
+    while (solvertp == LSOLVER_UNDEFINED) {
+        int cmd;
+        cout << "\nSelect linear solver:\n(1) Direct\n(2) CG (Conjugate gradient)\n"
+                "(3) BiCG (Bi-conjugate gradient)\n(4) BiCG-STAB (Bi-conjugate gradient stabilised)\n"
+                "(5) GMRES (generalised minimum residual)\n(6) GS (Gauss-Seidel)\n>> ";
+        cin >> cmd;
+        switch (cmd) {
+        case 1: solvertp = LSOLVER_DIRECT; break;
+        case 2: solvertp = LSOLVER_ITERATIVE, method = ITMETHOD_CG; break;
+        case 3: solvertp = LSOLVER_ITERATIVE, method = ITMETHOD_BICG; break;
+        case 4: solvertp = LSOLVER_ITERATIVE, method = ITMETHOD_BICGSTAB; break;
+        case 5: solvertp = LSOLVER_ITERATIVE, method = ITMETHOD_GMRES; break;
+        case 6: solvertp = LSOLVER_ITERATIVE, method = ITMETHOD_GAUSSSEIDEL; break;
+        }
+    }
+    if (solvertp == LSOLVER_ITERATIVE) {
+        if (!pp.GetReal("LINSOLVER_TOL", iterative_tol)) {
+            do {
+                cout << "\nLinear solver stopping criterion:\n>> ";
+                cin >> iterative_tol;
+            } while (iterative_tol <= 0.0);
+        }
+        if (!pp.GetInt("LINSOLVER_MAXIT", iterative_maxit)) {
+            cout << "\nLinear solver iteration limit (0=auto):\n>> ";
+            cin >> iterative_maxit;
+        }
+        precontp = (PreconType)-1;
+        if (pp.GetString("LINSOLVER_PRECON", cbuf)) {
+            if (!strcasecmp(cbuf, "NONE")) precontp = PRECON_NULL;
+            else if (!strcasecmp(cbuf, "DIAG")) precontp = PRECON_DIAG;
+            else if (!strcasecmp(cbuf, "ICH")) precontp = PRECON_ICH;
+            else if (!strcasecmp(cbuf, "DILU")) precontp = PRECON_DILU;
+        }
+        while (precontp == (PreconType)-1) {
+            int cmd;
+            cout << "\nSelect preconditioner for linear solver:\n(0) None\n(1) Diagonal\n"
+                    "(2) Incomplete Choleski\n(3) Diagonal incomplete LU\n";
+            cin >> cmd;
+            switch (cmd) {
+            case 0: precontp = PRECON_NULL; break;
+            case 1: precontp = PRECON_DIAG; break;
+            case 2: precontp = PRECON_ICH; break;
+            case 3: precontp = PRECON_DILU; break;
+            }
+        }
+    }
+}
+
+template <class T>
+void TFwdSolver<T>::WriteParams(ParamParser& pp)
+{
+    pp.PutString("DATASCALE", dscale == DATA_LIN ? "LIN" : "LOG");
+    if (solvertp == LSOLVER_DIRECT) {
+        pp.PutString("LINSOLVER", "DIRECT");
+    } else {
+        const char* nm[] = {"CG", "BICG", "BICGSTAB", "GMRES", "GAUSSSEIDEL"};
+        pp.PutString("LINSOLVER", nm[(int)method]);
+        pp.PutReal("LINSOLVER_TOL", iterative_tol);
+        pp.PutInt("LINSOLVER_MAXIT", iterative_maxit);
+        const char* pn = precontp == PRECON_DIAG ? "DIAG" : precontp == PRECON_ICH ? "ICH"
+                         : precontp == PRECON_DILU ? "DILU" : "NONE";
+        pp.PutString("LINSOLVER_PRECON", pn);
+    }
+}
+
+// =========================================================================
+// Allocate, assembly and reset (fwdsolver.cc:156-505)
+
+template <class T>
+void TFwdSolver<T>::Allocate()
+{
+    xASSERT(meshptr, "Mesh reference not defined.");
+    idxtype *rowptr, *colidx;
+    int nzero, n = meshptr->nlen();
+    meshptr->SparseRowStructure(rowptr, colidx, nzero);
+    if (F) delete F;
+    F = new TCompRowMatrix<T>(n, n, rowptr, colidx);
+    delete[] rowptr;
+    delete[] colidx;
+    std::lock_guard<std::mutex> g(g_mu);
+    GpuSolver& s = g_solvers[this];
+    if (s.solver) tg_solver_destroy(s.solver);
+    if (s.mesh) tg_mesh_destroy(s.mesh);
+    s = GpuSolver();
+    s.mesh = make_mesh(meshptr);
+    s.n = n;
+    const int m = solvertp == LSOLVER_DIRECT ? TG_SOLVER_DIRECT : method_of(method);
+    check(tg_solver_create(s.mesh, Prec<T>::cplx, m, precon_of(precontp), iterative_tol, iterative_maxit,
+                           TG_PREC_FP64, &s.solver),
+          "tg_solver_create");
+}
+
+template <class T>
+void TFwdSolver<T>::AssembleSystemMatrix(const Solution& sol, double omega, bool elbasis)
+{
+    GpuSolver* s;
+    {
+        std::lock_guard<std::mutex> g(g_mu);
+        auto it = g_solvers.find(this);
+        xASSERT(it != g_solvers.end() && it->second.solver, "Allocate() must come first");
+        s = &it->second;
+    }
+    RVector cmua = sol.GetParam(OT_CMUA), ckap = sol.GetParam(OT_CKAPPA), c2a = sol.GetParam(OT_C2A);
+    check(tg_solver_reset_basis(s->solver, cmua.data_buffer(), ckap.data_buffer(), c2a.data_buffer(), omega,
+                                TG_MEM_HOST, elbasis ? 1 : 0),
+          "tg_solver_reset_basis");
+    s->reset = true;
+    // F as the callers read it (FWS.F): the assembled system matrix
+    const int nz = F->rowptr[F->nRows()], w = Prec<T>::cplx ? 2 : 1;
+    std::vector<double> v((size_t)nz * w);
+    check(tg_solver_matrix(s->solver, v.data(), TG_MEM_HOST), "tg_solver_matrix");
+    T* val = F->ValPtr();
+    for (int k = 0; k < nz; k++) val[k] = get<T>(&v[(size_t)k * w]);
+}
+
+template <class T>
+void TFwdSolver<T>::Reset(const Solution& sol, double omega, bool elbasis)
+{
+    // assembly and the preconditioner (or the direct factor) in one call
+    AssembleSystemMatrix(sol, omega, elbasis);
+}
+
+template <class T>
+void TFwdSolver<T>::AssembleSystemMatrixComponent(const RVector&, int)
+{
+    xERROR("libtoastgpu: system matrix components are not provided (time-domain models)");
+}
+
+template <class T>
+void TFwdSolver<T>::AssembleMassMatrix(const Mesh*)
+{
+    xERROR("libtoastgpu: the mass matrix is not provided (time-domain models)");
+}
+
+// =========================================================================
+// fields (fwdsolver.cc:507-750)
+
+template <class T>
+void TFwdSolver<T>::CalcField(const TVector<T>& qvec, TVector<T>& phi, IterativeSolverResult* res, int) const
+{
+    GpuSolver* s;
+    {
+        std::lock_guard<std::mutex> g(g_mu);
+        auto it = g_solvers.find(this);
+        xASSERT(it != g_solvers.end() && it->second.reset, "Reset() must come first");
+        s = &it->second;
+    }
+    const int n = s->n, w = Prec<T>::cplx ? 2 : 1;
+    if (phi.Dim() != n) phi.New(n);
+    std::vector<double> q((size_t)n * w), x((size_t)n * w);
+    for (int i = 0; i < n; i++) {
+        put(&q[(size_t)i * w], qvec[i]);
+        put(&x[(size_t)i * w], phi[i]);
+    }
+    tg_result r;
+    check(tg_calc_fields(s->solver, 1, q.data(), x.data(), TG_MEM_HOST, &r), "tg_calc_fields");
+    for (int i = 0; i < n; i++) phi[i] = get<T>(&x[(size_t)i * w]);
+    if (res) {
+        res->it_count = r.it_count;
+        res->rel_err = r.rel_err;
+    }
+}
+
+template <class T>
+void TFwdSolver<T>::CalcFields(int q0, int q1, const TCompRowMatrix<T>& qvec, TVector<T>* phi,
+                               IterativeSolverResult* res) const
+{
+    GpuSolver* s;
+    {
+        std::lock_guard<std::mutex> g(g_mu);
+        auto it = g_solvers.find(this);
+        xASSERT(it != g_solvers.end() && it->second.reset, "Reset() must come first");
+        s = &it->second;
+    }
+    const int n = s->n, w = Prec<T>::cplx ? 2 : 1, k = q1 - q0;
+    if (k <= 0) return;
+    // all right-hand sides in one block solve; initial guesses from phi
+    std::vector<double> q = dense_rows(qvec, q0, q1, n), x((size_t)k * n * w);
+    for (int c = 0; c < k; c++) {
+        if (phi[c].Dim() != n) phi[c].New(n);
+        for (int i = 0; i < n; i++) put(&x[((size_t)c * n + i) * w], phi[c][i]);
+    }
+    std::vector<tg_result> r(k);
+    check(tg_calc_fields(s->solver, k, q.data(), x.data(), TG_MEM_HOST, r.data()), "tg_calc_fields");
+    for (int c = 0; c < k; c++)
+        for (int i = 0; i < n; i++) phi[c][i] = get<T>(&x[((size_t)c * n + i) * w]);
+    if (res) {  // total iterations, largest relative residual (CalcFields_engine)
+        res->it_count = 0;
+        res->rel_err = 0.0;
+        for (int c = 0; c < k; c++) {
+            res->it_count += r[c].it_count;
+            if (r[c].rel_err > res->rel_err) res->rel_err = r[c].rel_err;
+        }
+    }
+}
+
+template <class T>
+void TFwdSolver<T>::CalcFields(const TCompRowMatrix<T>& qvec, TVector<T>* phi, IterativeSolverResult* res) const
+{
+    CalcFields(0, qvec.nRows(), qvec, phi, res);
+}
+
+// =========================================================================
+// projections (fwdsolver.cc:826-993, 1415-1447)
+
+namespace {
+template <class T>
+TVector<T> project_gpu(tg_solver solver, const QMMesh* mesh, const TCompRowMatrix<T>& mvec, const TVector<T>* phi,
+                       int q0, int q1, DataScale scl)
+{
+    const int n = mesh->nlen(), w = Prec<T>::cplx ? 2 : 1, nq = q1 - q0;
+    std::vector<int> ofs, lm;
+    links_of(mesh, ofs, lm);
+    std::vector<int> o(nq + 1);
+    for (int q = 0; q <= nq; q++) o[q] = ofs[q0 + q] - ofs[q0];
+    std::vector<int> l(lm.begin() + ofs[q0], lm.begin() + ofs[q1]);
+    std::vector<double> f((size_t)nq * n * w);
+    for (int q = 0; q < nq; q++)
+        for (int i = 0; i < n; i++) put(&f[((size_t)q * n + i) * w], phi[q0 + q][i]);
+    std::vector<double> mv = dense_rows(mvec, 0, mvec.nRows(), n);
+    std::vector<double> out((size_t)std::max<int>((int)l.size(), 1) * w);
+    check(tg_project_all(solver, nq, f.data(), mvec.nRows(), mv.data(), o.data(), l.data(),
+                         scl == DATA_LOG ? TG_DATA_LOG : TG_DATA_LIN, out.data(), TG_MEM_HOST),
+          "tg_project_all");
+    TVector<T> proj((int)l.size());
+    for (size_t i = 0; i < l.size(); i++) proj[(int)i] = get<T>(&out[i * w]);
+    return proj;
+}
+}  // namespace
+
+template <class T>
+TVector<T> ProjectSingle(const QMMesh* mesh, int q, const TCompRowMatrix<T>& mvec, const TVector<T>& phi,
+                         DataScale dscale)
+{
+    tg_solver s = mesh_solver(mesh, Prec<T>::cplx, nullptr);
+    std::vector<TVector<T> > ph(mesh->nQ);
+    ph[q] = phi;
+    return project_gpu(s, mesh, mvec, ph.data(), q, q + 1, dscale);
+}
+
+template <class T>
+TVector<T> ProjectAll(const QMMesh* mesh, const TCompRowMatrix<T>& mvec, const TVector<T>* phi, DataScale dscale)
+{
+    tg_solver s = mesh_solver(mesh, Prec<T>::cplx, nullptr);
+    return project_gpu(s, mesh, mvec, phi, 0, mesh->nQ, dscale);
+}
+
+template <class T>
+TVector<T> TFwdSolver<T>::ProjectSingle(int q, const TCompRowMatrix<T>& mvec, const TVector<T>& phi,
+                                        DataScale scl) const
+{
+    xASSERT(meshptr, "Mesh reference not defined.");
+    if (scl == DATA_DEFAULT) scl = dscale;
+    return ::ProjectSingle(meshptr, q, mvec, phi, scl);
+}
+
+template <class T>
+TVector<T> TFwdSolver<T>::ProjectAll(const TCompRowMatrix<T>& mvec, const TVector<T>* dphi, DataScale scl)
+{
+    xASSERT(meshptr, "Mesh reference not defined.");
+    if (scl == DATA_DEFAULT) scl = dscale;
+    return ::ProjectAll(meshptr, mvec, dphi, scl);
+}
+
+template <class T>
+TVector<T> TFwdSolver<T>::ProjectAll(const TCompRowMatrix<T>& qvec, const TCompRowMatrix<T>& mvec,
+                                     const Solution& sol, double omega, DataScale scl)
+{
+    const int n = meshptr->nlen(), nq = meshptr->nQ;
+    if (!pphi) pphi = new TVector<T>[nq];
+    for (int i = 0; i < nq; i++) pphi[i].New(n);
+    Reset(sol, omega);
+    CalcFields(qvec, pphi);
+    return ProjectAll(mvec, pphi, scl);
+}
+
+template <class T>
+RVector TFwdSolver<T>::UnfoldComplex(const TVector<T>& vec) const
+{
+    const int len = vec.Dim();
+    if (!Prec<T>::cplx) {
+        RVector r(len);
+        for (int i = 0; i < len; i++) { double d[2]; put(d, vec[i]); r[i] = d[0]; }
+        return r;
+    }
+    RVector r(2 * len);
+    for (int i = 0; i < len; i++) {
+        double d[2];
+        put(d, vec[i]);
+        r[i] = d[0];
+        r[i + len] = d[1];
+    }
+    return r;
+}
+
+template <class T>
+FVector TFwdSolver<T>::UnfoldSComplex(const TVector<T>& vec) const
+{
+    RVector r = UnfoldComplex(vec);
+    FVector f(r.Dim());
+    for (int i = 0; i < r.Dim(); i++) f[i] = (float)r[i];
+    return f;
+}
+
+template <class T>
+RVector TFwdSolver<T>::ProjectAll_real(const TCompRowMatrix<T>& mvec, const TVector<T>* dphi, DataScale scl)
+{
+    if (scl == DATA_DEFAULT) scl = dscale;
+    RVector proj = UnfoldComplex(ProjectAll(mvec, dphi, scl));
+    // phase unwrapping of the log data: arg y > 0 moves down by 2 pi
+    // (fwdsolver.cc:981-988)
+    if (Prec<T>::cplx && unwrap_phase && scl != DATA_LIN) {
+        const int nqm = meshptr->nQM;
+        for (int i = 0; i < nqm; i++)
+            if (proj[nqm + i] > 0.0) proj[nqm + i] -= Pi2;
+    }
+    return proj;
+}
+
+template <class T>
+FVector TFwdSolver<T>::ProjectAll_singlereal(const TCompRowMatrix<T>& mvec, const TVector<T>* dphi, DataScale scl)
+{
+    RVector r = ProjectAll_real(mvec, dphi, scl);
+    FVector f(r.Dim());
+    for (int i = 0; i < r.Dim(); i++) f[i] = (float)r[i];
+    return f;
+}
+
+template <class T>
+RVector TFwdSolver<T>::ProjectAll_real(const TCompRowMatrix<T>& qvec, const TCompRowMatrix<T>& mvec,
+                                       const Solution& sol, double omega, DataScale scl)
+{
+    const int n = meshptr->nlen(), nq = meshptr->nQ;
+    if (!pphi) pphi = new TVector<T>[nq];
+    for (int i = 0; i < nq; i++) pphi[i].New(n);
+    Reset(sol, omega);
+    CalcFields(qvec, pphi);
+    return ProjectAll_real(mvec, pphi, scl);
+}
+
+template <class T>
+FVector TFwdSolver<T>::ProjectAll_singlereal(const TCompRowMatrix<T>& qvec, const TCompRowMatrix<T>& mvec,
+                                             const Solution& sol, double omega, DataScale scl)
+{
+    RVector r = ProjectAll_real(qvec, mvec, sol, omega, scl);
+    FVector f(r.Dim());
+    for (int i = 0; i < r.Dim(); i++) f[i] = (float)r[i];
+    return f;
+}
+
+// =========================================================================
+// instantiations (those fwdsolver.h declares extern)
+
+template class STOASTLIB TFwdSolver<float>;
+template class STOASTLIB TFwdSolver<double>;
+template class STOASTLIB TFwdSolver<std::complex<double> >;
+template class STOASTLIB TFwdSolver<std::complex<float> >;
+
+template STOASTLIB FVector ProjectSingle(const QMMesh*, int, const FCompRowMatrix&, const FVector&, DataScale);
+template STOASTLIB RVector ProjectSingle(const QMMesh*, int, const RCompRowMatrix&, const RVector&, DataScale);
+template STOASTLIB CVector ProjectSingle(const QMMesh*, int, const CCompRowMatrix&, const CVector&, DataScale);
+template STOASTLIB SCVector ProjectSingle(const QMMesh*, int, const SCCompRowMatrix&, const SCVector&, DataScale);
+template STOASTLIB FVector ProjectAll(const QMMesh*, const FCompRowMatrix&, const FVector*, DataScale);
+template STOASTLIB RVector ProjectAll(const QMMesh*, const RCompRowMatrix&, const RVector*, DataScale);
+template STOASTLIB SCVector ProjectAll(const QMMesh*, const SCCompRowMatrix&, const SCVector*, DataScale);
+template STOASTLIB CVector ProjectAll(const QMMesh*, const CCompRowMatrix&, const CVector*, DataScale);
