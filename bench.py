@@ -78,8 +78,9 @@ def parse():
     ap.add_argument("--element", action="store_true",
                     help="also time the element-basis Jacobian on the same fields")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--jac", default="fp64", choices=["fp64", "fp32"],
-                    help="Jacobian output (fp64: FP64 arithmetic from the FP64 fields; fp32: FP32)")
+    ap.add_argument("--jac", default="fp64", choices=["fp64", "fp32", "fp32acc"],
+                    help="Jacobian output: fp64 (FP64-accurate from the FP64 fields), fp32 (FP32 arithmetic), "
+                         "fp32acc (FP32 storage of the FP64-accurate sums)")
     ap.add_argument("--cw-tol", type=float, default=1e-10,
                     help="mixed path: componentwise backward-error bound of every solution (0: off)")
     ap.add_argument("--tol", type=float, default=1e-12)
@@ -266,7 +267,7 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)   # the library launches on this stream
     torch.cuda.set_stream(stream)
-    j_fp32 = args.jac == "fp32"
+    j_fp32 = {"fp64": 0, "fp32": 1, "fp32acc": 2}[args.jac]
 
     def dtensor(a):
         a = np.ascontiguousarray(a)
@@ -339,8 +340,8 @@ def run_gpu(args):
     nnz_l = (nnz - n) // 2
     names = {capi.PROF_SPMM: f"SpMM (autotuned spmm_halo/vec/wide kernel, k={nq + nm})",
              capi.PROF_SWEEP: "IC(0) apply: the level kernels of both sweeps (ic_level_ell) in one graph",
-             capi.PROF_JAC: ("jacobian_kernel (FP32)" if j_fp32 else
-                             "jacobian_ff_kernel (FP64 Jacobian in float-float arithmetic)"),
+             capi.PROF_JAC: ("jacobian_kernel (FP32)" if j_fp32 == 1 else
+                             "jacobian_ff_kernel (float-float arithmetic, %s J)" % ("FP32" if j_fp32 else "FP64")),
              capi.PROF_ASM: "assembly + IC(0) factor", capi.PROF_PROJ: "project_kernel"}
     dom = max(prof, key=lambda c: prof[c][0])
     vb = (8 if args.precision == "mixed" else 16) // (1 if cplx else 2)
@@ -368,14 +369,14 @@ def run_gpu(args):
                 "frac": ach / peak, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "traffic": None, "algorithmic_bytes_per_launch": alg_bytes,
                 "launch_ms": dom_ms / dom_cnt}
-        tr = TRAFFIC.get((args.config, dom == capi.PROF_JAC and not j_fp32 and "jacobian_ff"
+        tr = TRAFFIC.get((args.config, dom == capi.PROF_JAC and j_fp32 == 0 and "jacobian_ff"
                           or dom == capi.PROF_SWEEP and "ic_level_ell" or None))
         if tr:
             # ncu dram__bytes_read.sum + dram__bytes_write.sum per launch,
             # from a capture of a smaller case scaled by the units processed
             roof["traffic"] = tr[0]
             roof["traffic_source"] = tr[1]
-        if dom == capi.PROF_JAC and not j_fp32:
+        if dom == capi.PROF_JAC and j_fp32 != 1:
             roof["note"] = ("the float-float Jacobian is bound by FP32 issue (packed f32x2 pipe), not by HBM: "
                             "its J write is the only large traffic")
     shares = {names[c]: {"ms_per_step": prof[c][0] / psteps, "launches_or_scopes": prof[c][1] // psteps}
@@ -534,7 +535,7 @@ def run_gpu(args):
             "data": "synthetic (seeded mesh, optodes, inclusions)",
             "config": {"workload": workload_of(P, args.config, gm.ne, args.tol, args.precision,
                                                f" (inner FP32 tol {args.inner_tol}, componentwise backward error "
-                                               f"<= {args.cw_tol}, J {'fp32' if j_fp32 else 'fp64'})"
+                                               f"<= {args.cw_tol}, J {args.jac})"
                                                if args.precision == "mixed" else ""),
                        "parallelism": f"replicas x{ws} (one request per GPU)",
                        "l2": f"each step writes the {j_bytes / 1e9:.2f} GB Jacobian"
@@ -589,49 +590,77 @@ def compare_legs(args, P, gm, s, stream, dev, links, d_par, omega, d_src, h_src,
     val = om.assemble(ocm, ock, oca, P.freq_mhz * 2 * np.pi * 1e-6, cplx)
     oq = np.stack([om.qvec_gaussian(q, P.qwidth) for q in P.qm.Q]).astype(cdt)
     omv = np.stack([om.qvec_gaussian(m, P.mwidth) * oca for m in P.qm.M]).astype(cdt)
-    D = O.Direct(om.rowptr, om.colidx, val, "nd", om.coords)
     th = os.cpu_count() or 1
-    Xq = D.solve(oq, th)
-    Xm = D.solve(omv, th)
-    pref = O.project(Xq, omv, P.qm.link_ofs, P.qm.link_m, logscale=False)
-    lref = O.project(Xq, omv, P.qm.link_ofs, P.qm.link_m, logscale=True)
-    jq = min(4, nq)
-    lofs = np.asarray(P.qm.link_ofs, np.int32)[:jq + 1]
-    lm = np.asarray(P.qm.link_m, np.int32)[:lofs[-1]]
-    Jref = O.jacobian(om, Xq[:jq], Xm, pref[:lofs[-1]], lofs, lm, True, th)
+    if n <= 60000:
+        # every source and detector: the direct factorisation
+        D = O.Direct(om.rowptr, om.colidx, val, "nd", om.coords)
+        qs, ms = np.arange(nq), np.arange(nm)
+        Xq = D.solve(oq, th)
+        Xm = D.solve(omv, th)
+        how = "direct factorisation (nested-dissection order), every source and detector"
+    else:
+        # a sample: BiCGSTAB + ICH restarted from the true FP64 residual until
+        # the componentwise backward error is 1e-12 (too large to factor)
+        qs, ms = np.arange(min(8, nq)), np.arange(min(8, nm))
+        X, _ = O.solve_refined(om.rowptr, om.colidx, val, np.concatenate([oq[qs], omv[ms]]), nthreads=th)
+        Xq, Xm = X[:len(qs)], X[len(qs):]
+        how = (f"FP64 BiCGSTAB+ICH refined to componentwise backward error 1e-12, sources {len(qs)} and "
+               f"detectors {len(ms)} of {nq} + {nm}")
+    # links of the sampled sources (all detectors), and for the Jacobian the
+    # links of the first sampled sources to the sampled detectors
+    ofs_all = np.asarray(P.qm.link_ofs, np.int32)
+    lm_all = np.asarray(P.qm.link_m, np.int32)
+    lsel = np.concatenate([np.arange(ofs_all[q], ofs_all[q + 1]) for q in qs])
+    pofs = np.concatenate([[0], np.cumsum([ofs_all[q + 1] - ofs_all[q] for q in qs])]).astype(np.int32)
+    pref = O.project(Xq, omv, pofs, lm_all[lsel], logscale=False)
+    lref = O.project(Xq, omv, pofs, lm_all[lsel], logscale=True)
+    jq = min(4, len(qs))
+    mpos = {int(m): i for i, m in enumerate(ms)}
+    jl, jm = [], []
+    jofs = [0]
+    for q in qs[:jq]:
+        for l in range(ofs_all[q], ofs_all[q + 1]):
+            if int(lm_all[l]) in mpos:
+                jl.append(l)
+                jm.append(mpos[int(lm_all[l])])
+        jofs.append(len(jl))
+    jl = np.array(jl)
+    ylin = pref[[int(np.nonzero(lsel == l)[0][0]) for l in jl]]
+    Jref = O.jacobian(om, Xq[:jq], Xm, ylin, np.array(jofs, np.int32), np.array(jm, np.int32), True, th)
     t_oracle = time.perf_counter() - t0
 
     def errors(dphi, aphi, proj, lproj, J):
         e = {}
-        fq = dphi.cpu().numpy().view(cdt) if dphi is not None else None
+        fq = dphi.cpu().numpy().view(cdt)[qs] if dphi is not None else None
         if fq is not None:
-            fm = aphi.cpu().numpy().view(cdt)
+            fm = aphi.cpu().numpy().view(cdt)[ms]
             e["fields_l2"] = float(np.sqrt((np.linalg.norm(fq - Xq) ** 2 + np.linalg.norm(fm - Xm) ** 2) /
                                            (np.linalg.norm(Xq) ** 2 + np.linalg.norm(Xm) ** 2)))
-        pg = proj.cpu().numpy().view(cdt)
-        lg = lproj.cpu().numpy().view(cdt)
+        pg = proj.cpu().numpy().view(cdt)[lsel]
+        lg = lproj.cpu().numpy().view(cdt)[lsel]
         e["boundary_data_max_rel_linear"] = float(np.max(np.abs(pg - pref) / np.abs(pref)))
         e["boundary_data_l2_rel_linear"] = float(np.linalg.norm(pg - pref) / np.linalg.norm(pref))
         ok = np.isfinite(lg) & np.isfinite(lref)
         e["boundary_data_max_abs_log"] = float(np.max(np.abs(lg - lref)[ok]))
         if J is not None:
-            nl = int(lofs[-1])
-            rows = np.concatenate([np.arange(nl), nqm + np.arange(nl)])
+            nl = len(jl)
+            rows = np.concatenate([jl, nqm + jl])
             Jg = J[torch.as_tensor(rows, device=J.device)].double().cpu().numpy()
             Jr = Jref.reshape(2 * nl, -1)
             e["jacobian_l2_rel_sampled_rows"] = float(np.linalg.norm(Jg - Jr) / np.linalg.norm(Jr))
         return e
 
     f = fields
-    out["vs_oracle"] = {"oracle": "exact FP64 solve of the same request (direct factorisation, nested-dissection "
-                                  "order), projections, and Jacobian rows of the first %d sources' %d links" %
-                                  (jq, int(lofs[-1])),
+    out["vs_oracle"] = {"oracle": f"exact FP64 solve of the same request ({how}), projections of "
+                                  f"{len(lsel)} links, Jacobian rows of {len(jl)} links",
                         "oracle_s": t_oracle, **errors(f["dphi"], f["aphi"], f["proj"], f["lproj"], f["J"])}
     # ---- plain FP64 path, batched (the reference's recursion)
     s64 = capi.FwdSolver(gm, res_kind, args.tol, "ICH", cplx, precision="fp64")
     s64.set_stream(stream.cuda_stream)
     jcols = 2 * n if cplx else n
-    d_J64 = torch.empty((2 * nqm, jcols), dtype=torch.float64, device=dev)
+    # the FP64 path's Jacobian only where it is modest (16 GB)
+    d_J64 = (torch.empty((2 * nqm, jcols), dtype=torch.float64, device=dev) if 2 * nqm * jcols * 8 <= 16e9
+             else None)
     p64 = torch.empty_like(f["proj"])
     lp64 = torch.empty_like(f["lproj"])
     s64.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, p64, lp64, d_J64, 0,
@@ -672,7 +701,7 @@ def compare_legs(args, P, gm, s, stream, dev, links, d_par, omega, d_src, h_src,
     out["speedup_vs_fp64_per_source_solve"] = value / (1.0 / tps)
     del s1, d_phi1
     # ---- the same request with an FP32 Jacobian (FP32 products of the refined fields)
-    if args.precision == "mixed" and args.jac == "fp64":
+    if args.precision == "mixed" and args.jac == "fp64" and 2 * nqm * jcols * 4 <= 32e9:
         d_J32 = torch.empty((2 * nqm, jcols), dtype=torch.float32, device=dev)
         p32 = torch.empty_like(f["proj"])
         lp32 = torch.empty_like(f["lproj"])

@@ -216,7 +216,10 @@ int tg_project_all(tg_solver s, int nq, const double *phi, int nm, const double 
    [Re; Im] of -PMDF, columns [mua | kappa].  Real (CW): J is Jmua (nQM x n)
    followed by Jkap (nQM x n).  With scale = TG_DATA_LOG each row is divided by
    the linear projection proj[l] (complex for complex systems).
-   out_fp32 != 0 stores J as float instead of double. */
+   out_fp32: 0 an FP64 J (FP64-accurate arithmetic: float-float on the GPU's
+   FP32 pipes); 1 an FP32 J computed in FP32 (the mixed path's fast J); 2 an
+   FP32 J rounded once from the same FP64-accurate sums as 0 (FP32 storage
+   of an FP64-accumulated J).  The grid and element bases treat 2 as 1. */
 int tg_jacobian(tg_solver s, int nq, const double *dphi, int nm, const double *aphi,
                 const double *proj, const int *link_ofs, const int *link_m, int scale,
                 void *J, int out_fp32, int mem);

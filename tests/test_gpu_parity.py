@@ -182,6 +182,11 @@ def test_mixed_precision_boundary_data(case, oracle_mod):
     assert rel2(out["J"], ref.J) < 1e-8
     J32 = s.jacobian(out["dphi"], out["aphi"], out["proj"], L, fp32=True)
     assert rel2(J32, ref.J) < 1e-6
+    # FP32 storage of the FP64-accurate sums: each entry is the FP64 J
+    # rounded once to float
+    J32a = s.jacobian(out["dphi"], out["aphi"], out["proj"], L, fp32=2).astype(np.float64)
+    J64 = np.asarray(out["J"])
+    assert np.all(np.abs(J32a - J64) <= 6.0e-8 * np.abs(J64) + 1e-300)
 
 
 def test_componentwise_bound_off_is_normwise(case):

@@ -509,7 +509,8 @@ struct JacFFArgs {
     const void* G;                // float-float adjoint fields, node-major, ld nm
     const int* pairidx;           // nq*nm -> link index or -1
     const float4* yinv;           // per link 1/y as (re_hi, re_lo, im_hi, im_lo), or null
-    double* J;
+    double* J;                    // FP64 output, or
+    float* J32;                   // FP32 output (each hi + lo rounded once to float)
     const float4* W;              // packed float-float weights
     int D, SP, nmc;
 };
@@ -673,10 +674,17 @@ __global__ void __launch_bounds__(NT) jacobian_ff_kernel(JacFFArgs a)
                 }
                 const float2 rh = f2_unpack(srh), rl = f2_unpack(srl), ih = f2_unpack(sih), il = f2_unpack(sil);
                 const size_t r0 = (size_t)l * 2 * n + k, r1 = (size_t)(l + a.nqm) * 2 * n + k;
-                a.J[r0] = -ff_to_double(rh.x, rl.x);
-                a.J[r1] = -ff_to_double(ih.x, il.x);
-                a.J[r0 + n] = -ff_to_double(rh.y, rl.y);
-                a.J[r1 + n] = -ff_to_double(ih.y, il.y);
+                if (a.J32) {
+                    a.J32[r0] = -__fadd_rn(rh.x, rl.x);
+                    a.J32[r1] = -__fadd_rn(ih.x, il.x);
+                    a.J32[r0 + n] = -__fadd_rn(rh.y, rl.y);
+                    a.J32[r1 + n] = -__fadd_rn(ih.y, il.y);
+                } else {
+                    a.J[r0] = -ff_to_double(rh.x, rl.x);
+                    a.J[r1] = -ff_to_double(ih.x, il.x);
+                    a.J[r0 + n] = -ff_to_double(rh.y, rl.y);
+                    a.J[r1 + n] = -ff_to_double(ih.y, il.y);
+                }
             } else {
                 if (a.yinv) {
                     const float4 y = yis[q * JM + mm];
@@ -685,8 +693,13 @@ __global__ void __launch_bounds__(NT) jacobian_ff_kernel(JacFFArgs a)
                     srh = zh; srl = zl;
                 }
                 const float2 rh = f2_unpack(srh), rl = f2_unpack(srl);
-                a.J[(size_t)l * n + k] = -ff_to_double(rh.x, rl.x);
-                a.J[(size_t)(l + a.nqm) * n + k] = -ff_to_double(rh.y, rl.y);
+                if (a.J32) {
+                    a.J32[(size_t)l * n + k] = -__fadd_rn(rh.x, rl.x);
+                    a.J32[(size_t)(l + a.nqm) * n + k] = -__fadd_rn(rh.y, rl.y);
+                } else {
+                    a.J[(size_t)l * n + k] = -ff_to_double(rh.x, rl.x);
+                    a.J[(size_t)(l + a.nqm) * n + k] = -ff_to_double(rh.y, rl.y);
+                }
             }
         }
         __syncthreads();

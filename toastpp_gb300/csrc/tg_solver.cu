@@ -1747,7 +1747,7 @@ static bool try_launch_jacobian_ff(tg_solver s, JacFFArgs a)
 
 template <class V64>
 static void launch_jacobian_ff(tg_solver s, int nq, const V64* F, int ldf, int nm, const V64* G, int ldg,
-                               const LinkHost& L, const V64* ylin, double* J)
+                               const LinkHost& L, const V64* ylin, void* J, bool out_fp32)
 {
     constexpr bool CPLX = vt<V64>::cplx;
     constexpr size_t FI = CPLX ? 16 : 8;
@@ -1774,7 +1774,9 @@ static void launch_jacobian_ff(tg_solver s, int nq, const V64* F, int ldf, int n
     upload_async(s, s->jpair, L.pair);
     JacFFArgs a;
     a.m = m; a.nq = nq; a.nm = nm; a.nqm = nqm; a.cplx = CPLX;
-    a.F = Ff; a.G = Gf; a.pairidx = s->jpair.as<int>(); a.yinv = yi; a.J = J;
+    a.F = Ff; a.G = Gf; a.pairidx = s->jpair.as<int>(); a.yinv = yi;
+    a.J = out_fp32 ? nullptr : (double*)J;
+    a.J32 = out_fp32 ? (float*)J : nullptr;
     a.W = s->jwff.as<float4>();
     if (try_launch_jacobian_ff<CPLX, 4, 4, 512>(s, a)) return;
     if (try_launch_jacobian_ff<CPLX, 2, 2, 128>(s, a)) return;
@@ -1791,7 +1793,10 @@ static void jacobian_nm(tg_solver s, int nq, const V64* F, int ldf, int nm, cons
 {
     const MeshDev& m = s->mesh->d;
     int n = m.n, nqm = (int)L.q.size();
-    if (s->precision == TG_PREC_MIXED && out_fp32) {
+    if (out_fp32 == 2) {
+        // FP32 storage of float-float sums (J within FP32 rounding of the FP64 J)
+        launch_jacobian_ff<V64>(s, nq, F, ldf, nm, G, ldg, L, ylin, J, true);
+    } else if (s->precision == TG_PREC_MIXED && out_fp32) {
         V32* F32 = (V32*)s->jF.ensure((size_t)n * nq * sizeof(V32));
         V32* G32 = (V32*)s->jG.ensure((size_t)n * nm * sizeof(V32));
         launch(strided_cast_kernel<V32, V64>, cdiv_u((size_t)n * nq, 256), 256, 0, s->stream, n, nq, F, ldf, F32);
@@ -1805,7 +1810,7 @@ static void jacobian_nm(tg_solver s, int nq, const V64* F, int ldf, int nm, cons
     } else if (!out_fp32 && !getenv("TOASTGPU_JAC_FP64")) {
         // FP64 output: the float-float kernel (TOASTGPU_JAC_FP64 selects the
         // plain FP64 kernel instead, for comparison runs)
-        launch_jacobian_ff<V64>(s, nq, F, ldf, nm, G, ldg, L, ylin, (double*)J);
+        launch_jacobian_ff<V64>(s, nq, F, ldf, nm, G, ldg, L, ylin, J, false);
     } else {
         V64* yi = nullptr;
         if (ylin) {
