@@ -20,6 +20,8 @@
 #include "stoastlib.h"
 
 #include <complex>
+#include <cstdlib>
+#include <strings.h>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -409,8 +411,12 @@ void TFwdSolver<T>::Allocate()
     s.mesh = make_mesh(meshptr);
     s.n = n;
     const int m = solvertp == LSOLVER_DIRECT ? TG_SOLVER_DIRECT : method_of(method);
-    check(tg_solver_create(s.mesh, Prec<T>::cplx, m, precon_of(precontp), iterative_tol, iterative_maxit,
-                           TG_PREC_FP64, &s.solver),
+    // the reference's class has no precision setting: TOASTGPU_PRECISION=mixed
+    // selects the FP32-inner / FP64-refined path for unedited callers
+    const char* pe = getenv("TOASTGPU_PRECISION");
+    const int prec = pe && !strcasecmp(pe, "mixed") ? TG_PREC_MIXED : TG_PREC_FP64;
+    check(tg_solver_create(s.mesh, Prec<T>::cplx, m, precon_of(precontp), iterative_tol, iterative_maxit, prec,
+                           &s.solver),
           "tg_solver_create");
 }
 
