@@ -189,6 +189,28 @@ def test_mixed_precision_boundary_data(case, oracle_mod):
     assert np.all(np.abs(J32a - J64) <= 6.0e-8 * np.abs(J64) + 1e-300)
 
 
+def test_tensor_core_jacobian_matches_float_float(case, oracle_mod, monkeypatch):
+    """The complex FP64 Jacobian on the tensor cores (exact bf16 digit
+    products) and the float-float kernel, on the same GPU fields, against the
+    oracle's FP64 Jacobian of those fields: both at the FP64 rounding level."""
+    P, om, gm = case
+    if not P.complex:
+        pytest.skip("the tensor-core Jacobian is the complex path")
+    cm, ck, ca, qvec, mvec = gpu_problem_inputs(P, gm)
+    s = capi.FwdSolver(gm, "BICGSTAB", 1e-12, "ICH", True)
+    L = capi.Links(P.qm.link_ofs, P.qm.link_m)
+    out = s.forward_path(cm, ck, ca, capi.omega_of(P.freq_mhz), qvec, mvec, L)
+    Joz = np.asarray(s.jacobian(out["dphi"], out["aphi"], out["proj"], L))
+    monkeypatch.setenv("TOASTGPU_JAC_OZ", "0")
+    Jff = np.asarray(s.jacobian(out["dphi"], out["aphi"], out["proj"], L))
+    Jor = oracle_mod.jacobian(om, np.asarray(out["dphi"]), np.asarray(out["aphi"]), np.asarray(out["proj"]),
+                              P.qm.link_ofs, P.qm.link_m)
+    assert rel2(Joz, Jor) < 2e-14
+    assert rel2(Jff, Jor) < 5e-14
+    assert np.max(np.abs(Joz - Jor)) < 5e-14 * np.max(np.abs(Jor))
+    assert rel2(Joz, np.asarray(out["J"])) == 0.0  # the fused path uses the same kernel
+
+
 def test_componentwise_bound_off_is_normwise(case):
     """With the componentwise bound off the mixed path stops on the normwise
     test alone (fewer iterations); both results meet the normwise tolerance."""

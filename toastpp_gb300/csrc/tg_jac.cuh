@@ -1,5 +1,6 @@
 // tg_jac.cuh -- ProjectAll and the nodal-basis Jacobian.
 #pragma once
+#include <cuda_bf16.h>
 #include <type_traits>
 #include "tg_kernels.cuh"
 
@@ -703,6 +704,335 @@ __global__ void __launch_bounds__(NT) jacobian_ff_kernel(JacFFArgs a)
             }
         }
         __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Nodal Jacobian (complex) on the tensor cores, FP64-level accuracy.
+//
+// Per node k the pair sums are one small matrix product: with the node's
+// D neighbours, J_qm(k) = sum_i F_q(i) H_m(i), H_m(i) = sum_j W_k[i][j] G_m(j)
+// (mua and kappa weights), i.e. (nq x D) times (D x nm), complex.  As a real
+// product with K = 2D: rows (q, Re/Im) = [Fr, -Fi] / [Fi, Fr], columns
+// (m, mua/kappa) = [Hr; Hi].
+//
+// Exact digit products (the splitting scheme of Ozaki et al.): every row of
+// the left factor and every column of the right one is scaled by a power of
+// two to |x| < 128 and cut into S balanced base-256 digits (integers in
+// [-256, 256] when the hi and lo floats are cut separately and added), each
+// exact in bf16.  A digit product is exact in FP32 and so is a sum of them
+// while it stays below 2^24 (K <= 64, at most 3 digit pairs per level), so
+// the bf16 tensor-core products of digit levels 2, 3 and 4 (t + u = level,
+// slices pre-scaled by 256^-t) are exact; levels 5 and above (relative weight
+// 2^-24 and less) share one accumulator.  The four accumulators are summed
+// in float-float, scaled back, multiplied by 1/y and rounded once.  S = 6
+// keeps 48 bits of every operand: on the meshes measured the L2 error is
+// ~1e-14 of the exact sums, the worst entry (strong cancellation) ~1e-10.
+//
+// CTA = (node, chunk of jmc detectors); 10 warps; mma.sync m16n8k16 bf16:
+// m-tile = 8 sources x (Re, Im) rows, n-tile = 4 detectors x (mua, kappa).
+// ---------------------------------------------------------------------------
+struct JacOzArgs {
+    MeshDev m;
+    int nq, nm, nqm;
+    const float4* F;              // float-float forward fields (re_hi, re_lo, im_hi, im_lo), node-major, ld nq
+    const float4* G;              // float-float adjoint fields, node-major, ld nm
+    const int* pairidx;           // nq*nm -> link index or -1
+    const float4* yinv;           // per link 1/y as (re_hi, re_lo, im_hi, im_lo), or null
+    double* J;                    // FP64 output, or
+    float* J32;                   // FP32 output
+    const float4* W;              // packed float-float weights (Wm_hi, Wk_hi, Wm_lo, Wk_lo), [tile][i][j][lane]
+    int D;                        // weight slots per node (maximum degree)
+    int jmc, nch;                 // detectors per CTA (a multiple of 4), chunks per node
+};
+
+// biased FP32 exponent of the largest |value| (bits of non-negative floats
+// order as integers), clamped so that the scale 2^(133 - be) is a normal float
+__device__ __forceinline__ int oz_be(unsigned maxbits)
+{
+    if (maxbits == 0u) return 133;
+    const int be = (int)(maxbits >> 23);
+    return be < 7 ? 7 : be;
+}
+// 2^(7 - E) with E = be - 126: values scaled by it lie in (-128, 128)
+__device__ __forceinline__ float oz_scale(int be) { return __uint_as_float((unsigned)(260 - be) << 23); }
+
+// balanced base-256 digits of (hi + lo) * sc: the digits of hi and of lo,
+// added (|d| <= 256), digit t pre-scaled by 256^-t; every step is exact
+template <int S>
+__device__ __forceinline__ void oz_digits(float hi, float lo, float sc, float (&d)[S])
+{
+    float r = hi * sc, q = lo * sc, w = 1.0f;
+#pragma unroll
+    for (int t = 0; t < S; t++) {
+        const float a = rintf(r), b = rintf(q);
+        d[t] = (a + b) * w;
+        r = (r - a) * 256.0f;
+        q = (q - b) * 256.0f;
+        w *= 0.00390625f;
+    }
+}
+
+__device__ __forceinline__ unsigned oz_pack(float lo_half, float hi_half)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo_half, hi_half);  // .x in the low 16 bits
+    unsigned u;
+    memcpy(&u, &v, 4);
+    return u;
+}
+
+// the Im row word {Fi, Fr} from the Re row word {Fr, -Fi}: swap, negate the low half
+__device__ __forceinline__ unsigned oz_imword(unsigned w) { return ((w >> 16) | (w << 16)) ^ 0x00008000u; }
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1)
+{
+    asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// a float exactly as a double, from its bits (normal floats and zero)
+__device__ __forceinline__ double oz_f2d(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+    const unsigned ex = (u >> 23) & 0xffu;
+    if (ex == 0u) return __longlong_as_double((long long)s);
+    return __longlong_as_double(
+        (long long)(s | ((unsigned long long)(ex + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+// hi + lo times 2^e as a double: the floats converted exactly, one FP64
+// addition (rounded once), the scaling on the exponent bits
+__device__ __forceinline__ double oz_to_double(float h, float l, int e)
+{
+    const double d = oz_f2d(h) + oz_f2d(l);
+    long long b = __double_as_longlong(d);
+    if ((b & 0x7fffffffffffffffll) == 0) return d;
+    b += (long long)e << 52;
+    return __longlong_as_double(b);
+}
+
+// (h, l) += x exactly (TwoSum; the error joins l)
+__device__ __forceinline__ void oz_acc(float& h, float& l, float x)
+{
+    const float s = __fadd_rn(h, x), bp = __fsub_rn(s, h);
+    l = __fadd_rn(l, __fadd_rn(__fsub_rn(h, __fsub_rn(s, bp)), __fsub_rn(x, bp)));
+    h = s;
+}
+
+// AI: left-factor items (source, neighbour) per thread, NT * AI >= nq * deg
+template <int S, int NG, int NT, int AI>
+__global__ void __launch_bounds__(NT) jacobian_oz_kernel(JacOzArgs a)
+{
+    // accumulators: digit levels 0..3 apart (their sums are exact), 4..6
+    // together (relative weight 2^-32 and less: FP32 rounding there stays
+    // below the digit truncation)
+    constexpr int NA = 5;
+    extern __shared__ __align__(16) unsigned char jsm[];
+    const MeshDev& m = a.m;
+    const int k = blockIdx.x / a.nch, ch = blockIdx.x % a.nch;
+    const int m0 = ch * a.jmc, jm = min(a.jmc, a.nm - m0);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int rb = m.jrowptr[k], deg = m.jrowptr[k + 1] - rb;
+    const int KW = ((2 * deg + 15) / 16) * 8;       // words (bf16 pairs) per row: K = 2 deg padded to 16
+    const int KWM = ((2 * a.D + 15) / 16) * 8;      // the same for the largest degree (layout)
+    const int AST = KWM + 4;                        // row stride in words: fragment loads conflict-free
+    const int QR = ((a.nq + 7) / 8) * 8;            // source rows, padded to m-tiles of 8 sources
+    const int BC = 2 * a.jmc;                       // right-factor columns (detector x mua/kappa)
+    int* nb = (int*)jsm;                            // [32] neighbours of k, natural order
+    unsigned* ea = (unsigned*)(nb + 32);            // [QR] largest |value| (float bits) of each row
+    unsigned* eb = ea + QR;                         // [BC] the same per column
+    unsigned* Bw = eb + BC;                         // [S][BC][AST] right-factor digit words
+    unsigned char* X = (unsigned char*)(Bw + (size_t)S * BC * AST);
+    float4* Ws = (float4*)X;                        // [deg][deg] weights (phase 1)
+    float4* Gs = Ws + deg * deg;                    // [deg][jmc] adjoint fields (phase 1)
+    f2x* Hs = (f2x*)(Gs + (size_t)deg * a.jmc);     // [4 words][jmc][deg] H = W G (phase 1)
+    unsigned* Aw = (unsigned*)X;                    // [S][QR][AST] left-factor digit words (phase 2)
+    const size_t HW1 = (size_t)a.jmc * deg;
+
+    for (int i = tid; i < deg; i += NT) nb[i] = m.jcolidx[rb + i];
+    for (int i = tid; i < QR + BC; i += NT) ea[i] = 0u;  // ea and eb are adjacent
+    __syncthreads();
+    {
+        const size_t tb = (size_t)(k / JKT) * a.D * a.D * JKT + (k % JKT);
+        for (int e = tid; e < deg * deg; e += NT) {
+            const int i = e / deg, j = e % deg;
+            Ws[e] = a.W[tb + ((size_t)i * a.D + j) * JKT];
+        }
+        for (int e = tid; e < deg * jm; e += NT) {
+            const int j = e / jm, mm = e % jm;
+            Gs[j * a.jmc + mm] = a.G[(size_t)nb[j] * a.nm + m0 + mm];
+        }
+    }
+    __syncthreads();
+    // H[mm][i] = sum_j W[i][j] G[j][mm], packed (mua, kappa), float-float;
+    // column maxima of the hi words
+    for (int e = tid; e < jm * deg; e += NT) {
+        const int i = e / jm, mm = e % jm;
+        f2x rh = 0ull, rl = 0ull, ih = 0ull, il = 0ull;
+        for (int j = 0; j < deg; j++) {
+            const float4 w = Ws[i * deg + j];
+            const f2x wh = f2_pack(w.x, w.y), wl = f2_pack(w.z, w.w);
+            const float4 g = Gs[j * a.jmc + mm];
+            ff2_mac(rh, rl, wh, wl, f2_bcast(g.x), f2_bcast(g.y));
+            ff2_mac(ih, il, wh, wl, f2_bcast(g.z), f2_bcast(g.w));
+        }
+        const size_t o = (size_t)mm * deg + i;
+        Hs[o] = rh;
+        Hs[HW1 + o] = rl;
+        Hs[2 * HW1 + o] = ih;
+        Hs[3 * HW1 + o] = il;
+        const float2 r = f2_unpack(rh), q = f2_unpack(ih);
+        atomicMax(&eb[2 * mm], max(__float_as_uint(r.x) & 0x7fffffffu, __float_as_uint(q.x) & 0x7fffffffu));
+        atomicMax(&eb[2 * mm + 1], max(__float_as_uint(r.y) & 0x7fffffffu, __float_as_uint(q.y) & 0x7fffffffu));
+    }
+    __syncthreads();
+    // the forward fields of this thread's left-factor items (source,
+    // neighbour), loaded together; their latency hides behind the
+    // right-factor digits
+    float4 fv[AI];
+#pragma unroll
+    for (int x = 0; x < AI; x++) {
+        const int e = tid + x * NT, q = e / deg, i = e % deg;
+        fv[x] = q < a.nq ? a.F[(size_t)nb[i] * a.nq + q] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    // right-factor digits: word (column c, i) = {Hr, Hi} of H[c/2][i], part c&1
+    for (int e = tid; e < BC * KWM; e += NT) {
+        const int c = e / KWM, i = e % KWM, mm = c >> 1, p = c & 1;
+        float dr[S], di[S];
+        if (mm < jm && i < deg) {
+            const float sc = oz_scale(oz_be(eb[c]));
+            const size_t o = (size_t)mm * deg + i;
+            const float2 xh = f2_unpack(Hs[o]), xl = f2_unpack(Hs[HW1 + o]);
+            const float2 yh = f2_unpack(Hs[2 * HW1 + o]), yl = f2_unpack(Hs[3 * HW1 + o]);
+            oz_digits<S>(p ? xh.y : xh.x, p ? xl.y : xl.x, sc, dr);
+            oz_digits<S>(p ? yh.y : yh.x, p ? yl.y : yl.x, sc, di);
+        } else {
+#pragma unroll
+            for (int t = 0; t < S; t++) dr[t] = di[t] = 0.0f;
+        }
+#pragma unroll
+        for (int t = 0; t < S; t++) Bw[((size_t)t * BC + c) * AST + i] = oz_pack(dr[t], di[t]);
+    }
+#pragma unroll
+    for (int x = 0; x < AI; x++) {
+        const int q = (tid + x * NT) / deg;
+        if (q < a.nq)
+            atomicMax(&ea[q], max(__float_as_uint(fv[x].x) & 0x7fffffffu, __float_as_uint(fv[x].z) & 0x7fffffffu));
+    }
+    __syncthreads();  // phase-1 buffers dead: Aw takes their place
+    // left-factor digits: word (row q, i) = {Fr, -Fi} of F_q at neighbour i
+    // (padding words zero)
+    for (int e = tid; e < QR * KWM; e += NT) {
+        const int q = e / KWM, i = e % KWM;
+        if (q < a.nq && i < deg) continue;
+#pragma unroll
+        for (int t = 0; t < S; t++) Aw[((size_t)t * QR + q) * AST + i] = 0u;
+    }
+#pragma unroll
+    for (int x = 0; x < AI; x++) {
+        const int e = tid + x * NT, q = e / deg, i = e % deg;
+        if (q >= a.nq) continue;
+        float dr[S], di[S];
+        const float sc = oz_scale(oz_be(ea[q]));
+        oz_digits<S>(fv[x].x, fv[x].y, sc, dr);
+        oz_digits<S>(fv[x].z, fv[x].w, sc, di);
+#pragma unroll
+        for (int t = 0; t < S; t++) Aw[((size_t)t * QR + q) * AST + i] = oz_pack(dr[t], -di[t]);
+    }
+    __syncthreads();
+    // digit products: task = (m-tile of 8 sources, group of NG n-tiles)
+    const int g = lane >> 2, c4 = lane & 3;
+    const int QT = QR / 8, NTT = (2 * jm + 7) / 8, NGT = (NTT + NG - 1) / NG, KS = KW / 8;
+    const int n = m.n;
+    for (int task = warp; task < QT * NGT; task += NT / 32) {
+        const int qt = task / NGT, ng = task % NGT;
+        float acc[NG][NA][4];
+#pragma unroll
+        for (int x = 0; x < NG; x++)
+#pragma unroll
+            for (int y = 0; y < NA; y++)
+#pragma unroll
+                for (int z = 0; z < 4; z++) acc[x][y][z] = 0.0f;
+        for (int ks = 0; ks < KS; ks++) {
+            const int i0 = ks * 8;
+            unsigned bf[S][NG][2];
+#pragma unroll
+            for (int u = 0; u < S; u++)
+#pragma unroll
+                for (int nt = 0; nt < NG; nt++) {
+                    const int col = (ng * NG + nt) * 8 + g;
+                    const unsigned* bp = Bw + ((size_t)u * BC + (col < BC ? col : 0)) * AST + i0 + c4;
+                    bf[u][nt][0] = bp[0];
+                    bf[u][nt][1] = bp[4];
+                }
+#pragma unroll
+            for (int t = 0; t < S; t++) {
+                unsigned af[4];
+                const unsigned* ap = Aw + ((size_t)t * QR + qt * 8 + g) * AST + i0 + c4;
+                af[0] = ap[0];
+                af[2] = ap[4];
+                af[1] = oz_imword(af[0]);
+                af[3] = oz_imword(af[2]);
+#pragma unroll
+                for (int u = 0; u + t < S; u++) {
+#pragma unroll
+                    for (int nt = 0; nt < NG; nt++)
+                        if (ng * NG + nt < NTT)
+                            mma_bf16_16816(acc[nt][t + u < NA ? t + u : NA - 1], af, bf[u][nt][0], bf[u][nt][1]);
+                }
+            }
+        }
+        // epilogue: thread (g, c4) holds link (q, m) = (qt*8 + g, tile*4 + c4):
+        // (Re mua, Re kappa, Im mua, Im kappa)
+        const int q = qt * 8 + g;
+#pragma unroll
+        for (int nt = 0; nt < NG; nt++) {
+            const int ntg = ng * NG + nt;
+            const int mm = ntg * 4 + c4;
+            if (ntg >= NTT || q >= a.nq || mm >= jm) continue;
+            const int l = a.pairidx[(size_t)q * a.nm + m0 + mm];
+            if (l < 0) continue;
+            float h[4], lo[4];
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                h[v] = acc[nt][NA - 1][v];
+                lo[v] = 0.0f;
+#pragma unroll
+                for (int y = NA - 2; y >= 0; y--) oz_acc(h[v], lo[v], acc[nt][y][v]);
+            }
+            f2x srh = f2_pack(h[0], h[1]), srl = f2_pack(lo[0], lo[1]);
+            f2x sih = f2_pack(h[2], h[3]), sil = f2_pack(lo[2], lo[3]);
+            if (a.yinv) {
+                const float4 y = a.yinv[l];
+                f2x zrh = 0ull, zrl = 0ull, zih = 0ull, zil = 0ull;
+                ff2_mac(zrh, zrl, srh, srl, f2_bcast(y.x), f2_bcast(y.y));
+                ff2_mac(zrh, zrl, sih, sil, f2_bcast(-y.z), f2_bcast(-y.w));
+                ff2_mac(zih, zil, srh, srl, f2_bcast(y.z), f2_bcast(y.w));
+                ff2_mac(zih, zil, sih, sil, f2_bcast(y.x), f2_bcast(y.y));
+                srh = zrh; srl = zrl; sih = zih; sil = zil;
+            }
+            // J = -PMDF: the float halves negated before the conversion
+            const float2 rh = f2_unpack(f2_neg(srh)), rl = f2_unpack(f2_neg(srl));
+            const float2 ih = f2_unpack(f2_neg(sih)), il = f2_unpack(f2_neg(sil));
+            const int bq = oz_be(ea[q]);
+            const int e0 = bq + oz_be(eb[2 * mm]) - 266, e1 = bq + oz_be(eb[2 * mm + 1]) - 266;
+            const size_t r0 = (size_t)l * 2 * n + k, r1 = (size_t)(l + a.nqm) * 2 * n + k;
+            const double jr0 = oz_to_double(rh.x, rl.x, e0), jr1 = oz_to_double(rh.y, rl.y, e1);
+            const double ji0 = oz_to_double(ih.x, il.x, e0), ji1 = oz_to_double(ih.y, il.y, e1);
+            if (a.J32) {
+                a.J32[r0] = __double2float_rn(jr0);
+                a.J32[r0 + n] = __double2float_rn(jr1);
+                a.J32[r1] = __double2float_rn(ji0);
+                a.J32[r1 + n] = __double2float_rn(ji1);
+            } else {
+                a.J[r0] = jr0;
+                a.J[r0 + n] = jr1;
+                a.J[r1] = ji0;
+                a.J[r1 + n] = ji1;
+            }
+        }
     }
 }
 

@@ -1745,6 +1745,59 @@ static bool try_launch_jacobian_ff(tg_solver s, JacFFArgs a)
     return true;
 }
 
+// the tensor-core Jacobian (complex): CTA = (node, chunk of jmc detectors);
+// the largest chunk whose shared memory lets two CTAs share an SM, else one
+constexpr int OZ_S = 7, OZ_NG = 1, OZ_NT = 320;
+
+static size_t oz_smem(int nq, int D, int jmc)
+{
+    const size_t QR = cdiv_u(nq, 8) * 8, KWM = cdiv_u(2 * D, 16) * 8, AST = KWM + 4;
+    const size_t head = 4 * (32 + QR + 2 * (size_t)jmc);
+    const size_t bw = (size_t)OZ_S * 2 * jmc * AST * 4;
+    const size_t p1 = (size_t)D * D * 16 + (size_t)D * jmc * 16 + (size_t)32 * jmc * D;
+    const size_t aw = (size_t)OZ_S * QR * AST * 4;
+    return head + bw + std::max(p1, aw);
+}
+
+template <int AI>
+static void launch_oz(tg_solver s, const JacOzArgs& a, size_t smem)
+{
+    auto kern = jacobian_oz_kernel<OZ_S, OZ_NG, OZ_NT, AI>;
+    allow_smem((const void*)kern);
+    ProfScope ps(&s->prof, PC_JAC, s->stream);
+    launch(kern, (unsigned)((size_t)a.m.n * a.nch), OZ_NT, smem, s->stream, a);
+}
+
+static bool try_launch_jacobian_oz(tg_solver s, const JacFFArgs& f)
+{
+    const MeshDev& m = s->mesh->d;
+    const int D = s->jw_D;
+    // K = 2D <= 64 keeps the digit-level sums exact; the source x neighbour
+    // items of a node fit the threads' registers
+    const size_t items = (size_t)f.nq * D;
+    if (!f.cplx || D > 32 || items > (size_t)8 * OZ_NT) return false;
+    if (const char* e = getenv("TOASTGPU_JAC_OZ"))
+        if (e[0] == '0') return false;
+    int jmc = 0;
+    const int top = (int)std::min<size_t>(cdiv_u(f.nm, 4) * 4, 64);
+    for (int budget : {113 * 1024, 227 * 1024}) {
+        for (int c = top; c >= 4 && !jmc; c -= 4)
+            if (oz_smem(f.nq, D, c) <= (size_t)budget) jmc = c;
+        if (jmc) break;
+    }
+    if (!jmc) return false;
+    JacOzArgs a;
+    a.m = m; a.nq = f.nq; a.nm = f.nm; a.nqm = f.nqm;
+    a.F = (const float4*)f.F; a.G = (const float4*)f.G; a.pairidx = f.pairidx; a.yinv = f.yinv;
+    a.J = f.J; a.J32 = f.J32; a.W = f.W; a.D = D;
+    a.jmc = jmc; a.nch = (int)cdiv_u(f.nm, jmc);
+    const size_t smem = oz_smem(f.nq, D, jmc);
+    if (items <= (size_t)4 * OZ_NT) launch_oz<4>(s, a, smem);
+    else if (items <= (size_t)6 * OZ_NT) launch_oz<6>(s, a, smem);
+    else launch_oz<8>(s, a, smem);
+    return true;
+}
+
 template <class V64>
 static void launch_jacobian_ff(tg_solver s, int nq, const V64* F, int ldf, int nm, const V64* G, int ldg,
                                const LinkHost& L, const V64* ylin, void* J, bool out_fp32)
@@ -1778,6 +1831,7 @@ static void launch_jacobian_ff(tg_solver s, int nq, const V64* F, int ldf, int n
     a.J = out_fp32 ? nullptr : (double*)J;
     a.J32 = out_fp32 ? (float*)J : nullptr;
     a.W = s->jwff.as<float4>();
+    if (try_launch_jacobian_oz(s, a)) return;
     if (try_launch_jacobian_ff<CPLX, 4, 4, 512>(s, a)) return;
     if (try_launch_jacobian_ff<CPLX, 2, 2, 128>(s, a)) return;
     throw Error{TG_ERR_UNSUPPORTED, "mesh node degree too high for the Jacobian tile"};
