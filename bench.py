@@ -341,12 +341,20 @@ def run_gpu(args):
     names = {capi.PROF_SPMM: f"SpMM (autotuned spmm_halo/vec/wide kernel, k={nq + nm})",
              capi.PROF_SWEEP: "IC(0) apply: the level kernels of both sweeps (ic_level_ell) in one graph",
              capi.PROF_JAC: ("jacobian_kernel (FP32)" if j_fp32 == 1 else
-                             "jacobian_ff_kernel (float-float arithmetic, %s J)" % ("FP32" if j_fp32 else "FP64")),
+                             ("jacobian_oz_kernel (tensor cores: exact bf16 digit products, %s J)" if cplx else
+                              "jacobian_ff_kernel (float-float arithmetic, %s J)") % ("FP32" if j_fp32 else "FP64")),
              capi.PROF_ASM: "assembly + IC(0) factor", capi.PROF_PROJ: "project_kernel"}
     dom = max(prof, key=lambda c: prof[c][0])
     vb = (8 if args.precision == "mixed" else 16) // (1 if cplx else 2)
     jb = 4 if j_fp32 else 8
-    if dom == capi.PROF_JAC:
+    tc = dom == capi.PROF_JAC and cplx and j_fp32 != 1  # the tensor-core Jacobian
+    if tc:
+        # the digit products: per node a real (2nq x 2deg) x (2deg x 2nm)
+        # product per digit pair, 28 pairs (7 digits per operand); the sum of
+        # the node degrees is the number of CSR entries
+        alg_flops = 28 * 16.0 * nq * nm * nnz
+        alg_bytes = 2 * nqm * jcols * jb + (nq + nm) * n * vb + (n + 1 + nnz) * 4
+    elif dom == capi.PROF_JAC:
         # J write + fields read once + CSR pattern (per launch)
         alg_bytes = 2 * nqm * jcols * jb + (nq + nm) * n * vb + (n + 1 + nnz) * 4
     elif dom == capi.PROF_SPMM:
@@ -363,7 +371,23 @@ def run_gpu(args):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     roof = None
-    if alg_bytes and dom_cnt:
+    if tc and dom_cnt:
+        t_launch = dom_ms / dom_cnt / 1e3
+        tpeak = peaks.get("bf16_tflops", 1900.0)
+        ach = alg_flops / t_launch / 1e12
+        roof = {"bound": "tensor", "kernel": names[dom], "achieved": ach, "peak": tpeak, "unit": "TFLOP/s",
+                "frac": ach / tpeak, "peak_source": "measured" if "bf16_tflops" in peaks else "fallback",
+                "traffic": None, "algorithmic_flops_per_launch": alg_flops,
+                "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": dom_ms / dom_cnt,
+                "hbm_view": {"achieved_gbs": alg_bytes / t_launch / 1e9, "frac": alg_bytes / t_launch / 1e9 / peak},
+                "note": ("bf16 mma.sync digit products (measured ceiling of that instruction on this GPU: about "
+                         "600 TFLOP/s); the float-float digit preparation and the float-float recombination, "
+                         "1/y scaling and FP64 rounding of each entry run on the CUDA cores")}
+        tr = TRAFFIC.get((args.config, "jacobian_oz"))
+        if tr:
+            roof["traffic"] = tr[0]
+            roof["traffic_source"] = tr[1]
+    elif alg_bytes and dom_cnt:
         ach = alg_bytes / (dom_ms / dom_cnt / 1e3) / 1e9
         roof = {"bound": "hbm", "kernel": names[dom], "achieved": ach, "peak": peak, "unit": "GB/s",
                 "frac": ach / peak, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",

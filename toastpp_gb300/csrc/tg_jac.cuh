@@ -792,26 +792,19 @@ __device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const unsigned (&a
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// a float exactly as a double, from its bits (normal floats and zero)
-__device__ __forceinline__ double oz_f2d(float f)
+// f * 2^e exactly as a double, built from the bits of f (normal floats and
+// zero; the result stays in the normal double range)
+__device__ __forceinline__ double oz_f2d(float f, int e)
 {
     const unsigned u = __float_as_uint(f);
     const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
     const unsigned ex = (u >> 23) & 0xffu;
     if (ex == 0u) return __longlong_as_double((long long)s);
-    return __longlong_as_double(
-        (long long)(s | ((unsigned long long)(ex + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+    return __longlong_as_double((long long)(s | ((unsigned long long)(ex + 896u + e) << 52) |
+                                            ((unsigned long long)(u & 0x7fffffu) << 29)));
 }
-// hi + lo times 2^e as a double: the floats converted exactly, one FP64
-// addition (rounded once), the scaling on the exponent bits
-__device__ __forceinline__ double oz_to_double(float h, float l, int e)
-{
-    const double d = oz_f2d(h) + oz_f2d(l);
-    long long b = __double_as_longlong(d);
-    if ((b & 0x7fffffffffffffffll) == 0) return d;
-    b += (long long)e << 52;
-    return __longlong_as_double(b);
-}
+// (h + l) * 2^e as a double: one FP64 addition, rounded once
+__device__ __forceinline__ double oz_to_double(float h, float l, int e) { return oz_f2d(h, e) + oz_f2d(l, e); }
 
 // (h, l) += x exactly (TwoSum; the error joins l)
 __device__ __forceinline__ void oz_acc(float& h, float& l, float x)
@@ -821,9 +814,9 @@ __device__ __forceinline__ void oz_acc(float& h, float& l, float x)
     h = s;
 }
 
-// AI: left-factor items (source, neighbour) per thread, NT * AI >= nq * deg
+// AI: left-factor items per thread: NT / QR threads share a source row, AI * (NT / QR) >= deg
 template <int S, int NG, int NT, int AI>
-__global__ void __launch_bounds__(NT) jacobian_oz_kernel(JacOzArgs a)
+__global__ void __launch_bounds__(NT, 1024 / NT) jacobian_oz_kernel(JacOzArgs a)
 {
     // accumulators: digit levels 0..3 apart (their sums are exact), 4..6
     // together (relative weight 2^-32 and less: FP32 rounding there stays
@@ -888,18 +881,21 @@ __global__ void __launch_bounds__(NT) jacobian_oz_kernel(JacOzArgs a)
         atomicMax(&eb[2 * mm + 1], max(__float_as_uint(r.y) & 0x7fffffffu, __float_as_uint(q.y) & 0x7fffffffu));
     }
     __syncthreads();
-    // the forward fields of this thread's left-factor items (source,
-    // neighbour), loaded together; their latency hides behind the
-    // right-factor digits
+    // the forward fields of this thread's left-factor items (source q =
+    // tid % QR, neighbours i = tid / QR + r * (NT / QR)), loaded together
+    // (coalesced over q); their latency hides behind the right-factor digits
+    const int QP = NT / QR, aq = tid % QR, ai0 = tid / QR;
     float4 fv[AI];
 #pragma unroll
     for (int x = 0; x < AI; x++) {
-        const int e = tid + x * NT, q = e / deg, i = e % deg;
-        fv[x] = q < a.nq ? a.F[(size_t)nb[i] * a.nq + q] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int i = ai0 + x * QP;
+        fv[x] = ai0 < QP && aq < a.nq && i < deg ? a.F[(size_t)nb[i] * a.nq + aq] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    // right-factor digits: word (column c, i) = {Hr, Hi} of H[c/2][i], part c&1
-    for (int e = tid; e < BC * KWM; e += NT) {
-        const int c = e / KWM, i = e % KWM, mm = c >> 1, p = c & 1;
+    // right-factor digits: word (column c, i) = {Hr, Hi} of H[c/2][i], part
+    // c&1; a warp per column, lane = word (KWM <= 32)
+    for (int c = warp; c < BC; c += NT / 32) {
+        const int i = lane, mm = c >> 1, p = c & 1;
+        if (i >= KWM) continue;
         float dr[S], di[S];
         if (mm < jm && i < deg) {
             const float sc = oz_scale(oz_be(eb[c]));
@@ -915,31 +911,34 @@ __global__ void __launch_bounds__(NT) jacobian_oz_kernel(JacOzArgs a)
 #pragma unroll
         for (int t = 0; t < S; t++) Bw[((size_t)t * BC + c) * AST + i] = oz_pack(dr[t], di[t]);
     }
+    {
+        unsigned mx = 0u;
 #pragma unroll
-    for (int x = 0; x < AI; x++) {
-        const int q = (tid + x * NT) / deg;
-        if (q < a.nq)
-            atomicMax(&ea[q], max(__float_as_uint(fv[x].x) & 0x7fffffffu, __float_as_uint(fv[x].z) & 0x7fffffffu));
+        for (int x = 0; x < AI; x++)
+            mx = max(mx, max(__float_as_uint(fv[x].x) & 0x7fffffffu, __float_as_uint(fv[x].z) & 0x7fffffffu));
+        if (ai0 < QP && aq < a.nq) atomicMax(&ea[aq], mx);
     }
     __syncthreads();  // phase-1 buffers dead: Aw takes their place
-    // left-factor digits: word (row q, i) = {Fr, -Fi} of F_q at neighbour i
-    // (padding words zero)
-    for (int e = tid; e < QR * KWM; e += NT) {
-        const int q = e / KWM, i = e % KWM;
-        if (q < a.nq && i < deg) continue;
+    // left-factor digits: word (row q, i) = {Fr, -Fi} of F_q at neighbour i;
+    // padding words (i >= deg, or a padding row) zero, a warp per row
+    for (int q = warp; q < QR; q += NT / 32) {
+        const int i = lane;
+        if (i >= KWM || (q < a.nq && i < deg)) continue;
 #pragma unroll
         for (int t = 0; t < S; t++) Aw[((size_t)t * QR + q) * AST + i] = 0u;
     }
+    if (ai0 < QP && aq < a.nq) {
+        const float sc = oz_scale(oz_be(ea[aq]));
 #pragma unroll
-    for (int x = 0; x < AI; x++) {
-        const int e = tid + x * NT, q = e / deg, i = e % deg;
-        if (q >= a.nq) continue;
-        float dr[S], di[S];
-        const float sc = oz_scale(oz_be(ea[q]));
-        oz_digits<S>(fv[x].x, fv[x].y, sc, dr);
-        oz_digits<S>(fv[x].z, fv[x].w, sc, di);
+        for (int x = 0; x < AI; x++) {
+            const int i = ai0 + x * QP;
+            if (i >= deg) break;
+            float dr[S], di[S];
+            oz_digits<S>(fv[x].x, fv[x].y, sc, dr);
+            oz_digits<S>(fv[x].z, fv[x].w, sc, di);
 #pragma unroll
-        for (int t = 0; t < S; t++) Aw[((size_t)t * QR + q) * AST + i] = oz_pack(dr[t], -di[t]);
+            for (int t = 0; t < S; t++) Aw[((size_t)t * QR + aq) * AST + i] = oz_pack(dr[t], -di[t]);
+        }
     }
     __syncthreads();
     // digit products: task = (m-tile of 8 sources, group of NG n-tiles)
@@ -948,6 +947,16 @@ __global__ void __launch_bounds__(NT) jacobian_oz_kernel(JacOzArgs a)
     const int n = m.n;
     for (int task = warp; task < QT * NGT; task += NT / 32) {
         const int qt = task / NGT, ng = task % NGT;
+        // this thread's links and their 1/y, loaded before the products
+        // (their latency hides behind them)
+        int lk[NG];
+        float4 yk[NG];
+#pragma unroll
+        for (int nt = 0; nt < NG; nt++) {
+            const int q = qt * 8 + g, mm = (ng * NG + nt) * 4 + c4;
+            lk[nt] = q < a.nq && mm < jm ? a.pairidx[(size_t)q * a.nm + m0 + mm] : -1;
+            yk[nt] = a.yinv && lk[nt] >= 0 ? a.yinv[lk[nt]] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
         float acc[NG][NA][4];
 #pragma unroll
         for (int x = 0; x < NG; x++)
@@ -991,9 +1000,8 @@ __global__ void __launch_bounds__(NT) jacobian_oz_kernel(JacOzArgs a)
         for (int nt = 0; nt < NG; nt++) {
             const int ntg = ng * NG + nt;
             const int mm = ntg * 4 + c4;
-            if (ntg >= NTT || q >= a.nq || mm >= jm) continue;
-            const int l = a.pairidx[(size_t)q * a.nm + m0 + mm];
-            if (l < 0) continue;
+            const int l = lk[nt];
+            if (ntg >= NTT || l < 0) continue;
             float h[4], lo[4];
 #pragma unroll
             for (int v = 0; v < 4; v++) {
@@ -1005,7 +1013,7 @@ __global__ void __launch_bounds__(NT) jacobian_oz_kernel(JacOzArgs a)
             f2x srh = f2_pack(h[0], h[1]), srl = f2_pack(lo[0], lo[1]);
             f2x sih = f2_pack(h[2], h[3]), sil = f2_pack(lo[2], lo[3]);
             if (a.yinv) {
-                const float4 y = a.yinv[l];
+                const float4 y = yk[nt];
                 f2x zrh = 0ull, zrl = 0ull, zih = 0ull, zil = 0ull;
                 ff2_mac(zrh, zrl, srh, srl, f2_bcast(y.x), f2_bcast(y.y));
                 ff2_mac(zrh, zrl, sih, sil, f2_bcast(-y.z), f2_bcast(-y.w));

@@ -1747,7 +1747,7 @@ static bool try_launch_jacobian_ff(tg_solver s, JacFFArgs a)
 
 // the tensor-core Jacobian (complex): CTA = (node, chunk of jmc detectors);
 // the largest chunk whose shared memory lets two CTAs share an SM, else one
-constexpr int OZ_S = 7, OZ_NG = 1, OZ_NT = 320;
+constexpr int OZ_S = 7, OZ_NG = 1;
 
 static size_t oz_smem(int nq, int D, int jmc)
 {
@@ -1759,42 +1759,53 @@ static size_t oz_smem(int nq, int D, int jmc)
     return head + bw + std::max(p1, aw);
 }
 
-template <int AI>
+template <int NT, int AI>
 static void launch_oz(tg_solver s, const JacOzArgs& a, size_t smem)
 {
-    auto kern = jacobian_oz_kernel<OZ_S, OZ_NG, OZ_NT, AI>;
+    auto kern = jacobian_oz_kernel<OZ_S, OZ_NG, NT, AI>;
     allow_smem((const void*)kern);
     ProfScope ps(&s->prof, PC_JAC, s->stream);
-    launch(kern, (unsigned)((size_t)a.m.n * a.nch), OZ_NT, smem, s->stream, a);
+    launch(kern, (unsigned)((size_t)a.m.n * a.nch), NT, smem, s->stream, a);
 }
+
+template <int NT>
+static void launch_oz_ai(tg_solver s, const JacOzArgs& a, size_t smem, int AI)
+{
+    if (AI <= 4) launch_oz<NT, 4>(s, a, smem);
+    else if (AI <= 6) launch_oz<NT, 6>(s, a, smem);
+    else launch_oz<NT, 8>(s, a, smem);
+}
+// (one 1024-thread CTA per SM with all detectors of a node in one CTA was
+// measured slower: 13.1 against 12.3 ms per 30k request, the CTAs' phases
+// no longer overlapping)
 
 static bool try_launch_jacobian_oz(tg_solver s, const JacFFArgs& f)
 {
     const MeshDev& m = s->mesh->d;
     const int D = s->jw_D;
-    // K = 2D <= 64 keeps the digit-level sums exact; the source x neighbour
-    // items of a node fit the threads' registers
-    const size_t items = (size_t)f.nq * D;
-    if (!f.cplx || D > 32 || items > (size_t)8 * OZ_NT) return false;
+    // K = 2D <= 64 keeps the digit-level sums exact; every source row has a
+    // group of threads, whose registers hold the row's neighbour items
+    const int QR = (int)cdiv_u(f.nq, 8) * 8;
+    if (!f.cplx || D > 32 || QR > 512 || cdiv_u(D, 512 / QR) > 8) return false;
     if (const char* e = getenv("TOASTGPU_JAC_OZ"))
         if (e[0] == '0') return false;
-    int jmc = 0;
-    const int top = (int)std::min<size_t>(cdiv_u(f.nm, 4) * 4, 64);
-    for (int budget : {113 * 1024, 227 * 1024}) {
-        for (int c = top; c >= 4 && !jmc; c -= 4)
-            if (oz_smem(f.nq, D, c) <= (size_t)budget) jmc = c;
-        if (jmc) break;
-    }
-    if (!jmc) return false;
     JacOzArgs a;
     a.m = m; a.nq = f.nq; a.nm = f.nm; a.nqm = f.nqm;
     a.F = (const float4*)f.F; a.G = (const float4*)f.G; a.pairidx = f.pairidx; a.yinv = f.yinv;
     a.J = f.J; a.J32 = f.J32; a.W = f.W; a.D = D;
+    // two 512-thread CTAs per SM: the fewest equal detector chunks (multiples
+    // of 4) whose shared memory fits, else one CTA per SM
+    int jmc = 0;
+    for (int budget : {113 * 1024, 227 * 1024}) {
+        for (int nch = 1; nch <= f.nm && !jmc; nch++) {
+            const int c = (int)cdiv_u(cdiv_u(f.nm, nch), 4) * 4;
+            if (oz_smem(f.nq, D, c) <= (size_t)budget) jmc = c;
+        }
+        if (jmc) break;
+    }
+    if (!jmc) return false;
     a.jmc = jmc; a.nch = (int)cdiv_u(f.nm, jmc);
-    const size_t smem = oz_smem(f.nq, D, jmc);
-    if (items <= (size_t)4 * OZ_NT) launch_oz<4>(s, a, smem);
-    else if (items <= (size_t)6 * OZ_NT) launch_oz<6>(s, a, smem);
-    else launch_oz<8>(s, a, smem);
+    launch_oz_ai<512>(s, a, oz_smem(f.nq, D, jmc), (int)cdiv_u(D, 512 / QR));
     return true;
 }
 
