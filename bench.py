@@ -35,6 +35,10 @@ UNIT = "source-solves/s"
 # scaled to the workload by the units one launch processes; the capture
 # commands and counters are in profiles/
 TRAFFIC = {
+    ("c2_cyl30k_fd", "jacobian_oz"): (
+        (332.53632e6 + 1653.086e6) * (12800 * 61620) / (12800 * 15008),
+        "ncu on the 7504-node cylinder (12800 x 15008 J: read 332.5 MB + write 1653.1 MB), scaled by the J "
+        "entries to 12800 x 61620 (profiles/jacobian_oz_kernel_cyl7k_fp64.md)"),
     ("c2_cyl30k_fd", "jacobian_ff"): (
         (179.457792e6 + 1477.513e6) * (12800 * 61620) / (12800 * 15008),
         "ncu on the 7504-node cylinder (12800 x 15008 J: read 179.5 MB + write 1477.5 MB), scaled by the J "
