@@ -2168,6 +2168,25 @@ static void api_forward_path(tg_solver s, const double* cmua, const double* ckap
     V64* ylin = (V64*)s->fp_lin.ensure((size_t)std::max(nqm, 1) * sizeof(V64));
     V64* ylog = (V64*)s->fp_log.ensure((size_t)std::max(nqm, 1) * sizeof(V64));
     project_nm<V64>(s, X, k, nm, Ms, L, ylin, ylog);
+    // the fields and projections go out before the Jacobian: their copies
+    // must not queue behind a deferred Jacobian copy on the copy engine
+    auto out_field = [&](double* dst, const V64* src_nm, int kk, DBuf& stage) {
+        if (!dst) return;
+        size_t b = (size_t)kk * n * sizeof(V64);
+        V64* o = mem == TG_MEM_DEVICE ? (V64*)dst : (V64*)stage.ensure(b);
+        launch(to_srcmajor_kernel<V64, V64>, dim3(cdiv_u(n, 32), cdiv_u(kk, 32)), tb, 0, s->stream, n, kk, k, src_nm, o,
+               m.perm);
+        if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(dst, o, b, cudaMemcpyDeviceToHost, s->stream));
+    };
+    out_field(dphi, X, nq, s->io_a);
+    out_field(aphi, X + nq, nm, s->io_b);
+    auto out_small = [&](double* dst, const V64* src) {
+        if (!dst) return;
+        TG_CUDA(cudaMemcpyAsync(dst, src, (size_t)nqm * sizeof(V64),
+                                mem == TG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s->stream));
+    };
+    out_small(proj, ylin);
+    out_small(logproj, ylog);
     if (J) {
         size_t jbytes = (size_t)2 * nqm * (vt<V64>::cplx ? 2 * n : n) * (j_fp32 ? 4 : 8);
         cudaPointerAttributes pa = {};
@@ -2198,23 +2217,6 @@ static void api_forward_path(tg_solver s, const double* cmua, const double* ckap
             if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(J, Jd, jbytes, cudaMemcpyDeviceToHost, s->stream));
         }
     }
-    auto out_field = [&](double* dst, const V64* src_nm, int kk, DBuf& stage) {
-        if (!dst) return;
-        size_t b = (size_t)kk * n * sizeof(V64);
-        V64* o = mem == TG_MEM_DEVICE ? (V64*)dst : (V64*)stage.ensure(b);
-        launch(to_srcmajor_kernel<V64, V64>, dim3(cdiv_u(n, 32), cdiv_u(kk, 32)), tb, 0, s->stream, n, kk, k, src_nm, o,
-               m.perm);
-        if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpyAsync(dst, o, b, cudaMemcpyDeviceToHost, s->stream));
-    };
-    out_field(dphi, X, nq, s->io_a);
-    out_field(aphi, X + nq, nm, s->io_b);
-    auto out_small = [&](double* dst, const V64* src) {
-        if (!dst) return;
-        TG_CUDA(cudaMemcpyAsync(dst, src, (size_t)nqm * sizeof(V64),
-                                mem == TG_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s->stream));
-    };
-    out_small(proj, ylin);
-    out_small(logproj, ylog);
     TG_CUDA(cudaGetLastError());
     TG_CUDA(cudaStreamSynchronize(s->stream));
 }
