@@ -1044,6 +1044,99 @@ __global__ void __launch_bounds__(NT, 1024 / NT) jacobian_oz_kernel(JacOzArgs a)
     }
 }
 
+// ---------------------------------------------------------------------------
+// The true residual's product A x of the mixed path in float-float
+// arithmetic.  Each reliable update forms b - A x in FP64 for the columns
+// waiting then; as FP64 arithmetic that product is bound by GB300's FP64 rate
+// (about 350 us for 160 complex columns of the 30k cylinder).  Here A and x
+// are (hi, lo) float pairs and every product and sum is compensated (the
+// float-float arithmetic of the Jacobian), about 2^-46 of |A||x| per entry,
+// far below what the stopping tests (backward error 1e-10, relative residual
+// 1e-12) resolve; the result is rounded once to FP64.
+// ---------------------------------------------------------------------------
+// the waiting columns idx[0..kf) of the node-major FP64 block X (k columns) as
+// float-float, node-major with kf columns
+template <bool CPLX>
+__global__ void gather_cols_ff_kernel(int n, int k, int kf, const int* __restrict__ idx, const double* __restrict__ X,
+                                      void* __restrict__ out)
+{
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)n * kf) return;
+    const size_t i = t / kf;
+    const int c = idx[t % kf];
+    if constexpr (CPLX) {
+        const float2 r = ff_split(X[2 * (i * k + c)]), q = ff_split(X[2 * (i * k + c) + 1]);
+        ((float4*)out)[t] = make_float4(r.x, r.y, q.x, q.y);
+    } else {
+        ((float2*)out)[t] = ff_split(X[i * k + c]);
+    }
+}
+
+// Y = A X (FP64 out, node-major, kf columns): a warp per row, lane = column
+template <bool CPLX, int NJ>
+__global__ void __launch_bounds__(256) spmm_ff_kernel(int n, const int* __restrict__ rowptr,
+                                                      const int* __restrict__ colidx, const void* __restrict__ Aff,
+                                                      int kf, const void* __restrict__ Xff, double* __restrict__ Y)
+{
+    const int row = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const int b = rowptr[row], e = rowptr[row + 1];
+    if constexpr (CPLX) {
+        f2x h[NJ], l[NJ];  // packed (re, im)
+#pragma unroll
+        for (int j = 0; j < NJ; j++) h[j] = l[j] = 0ull;
+        for (int p = b; p < e; p++) {
+            const int col = colidx[p];
+            const float4 a = ((const float4*)Aff)[p];  // (re_hi, re_lo, im_hi, im_lo)
+            const f2x arh = f2_bcast(a.x), arl = f2_bcast(a.y);
+            const f2x aih = f2_pack(-a.z, a.z), ail = f2_pack(-a.w, a.w);
+#pragma unroll
+            for (int j = 0; j < NJ; j++) {
+                const int c = lane + 32 * j;
+                if (c < kf) {
+                    const float4 x = ((const float4*)Xff)[(size_t)col * kf + c];
+                    ff2_mac(h[j], l[j], arh, arl, f2_pack(x.x, x.z), f2_pack(x.y, x.w));  // (ar xr, ar xi)
+                    ff2_mac(h[j], l[j], aih, ail, f2_pack(x.z, x.x), f2_pack(x.w, x.y));  // (-ai xi, ai xr)
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NJ; j++) {
+            const int c = lane + 32 * j;
+            if (c < kf) {
+                const float2 hh = f2_unpack(h[j]), ll = f2_unpack(l[j]);
+                Y[2 * ((size_t)row * kf + c)] = oz_to_double(hh.x, ll.x, 0);
+                Y[2 * ((size_t)row * kf + c) + 1] = oz_to_double(hh.y, ll.y, 0);
+            }
+        }
+    } else {
+        f2x h[NJ], l[NJ];  // the low half carries the column, the high half is unused
+#pragma unroll
+        for (int j = 0; j < NJ; j++) h[j] = l[j] = 0ull;
+        for (int p = b; p < e; p++) {
+            const int col = colidx[p];
+            const float2 a = ((const float2*)Aff)[p];
+            const f2x ah = f2_bcast(a.x), al = f2_bcast(a.y);
+#pragma unroll
+            for (int j = 0; j < NJ; j++) {
+                const int c = lane + 32 * j;
+                if (c < kf) {
+                    const float2 x = ((const float2*)Xff)[(size_t)col * kf + c];
+                    ff2_mac(h[j], l[j], ah, al, f2_bcast(x.x), f2_bcast(x.y));
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NJ; j++) {
+            const int c = lane + 32 * j;
+            if (c < kf) {
+                const float2 hh = f2_unpack(h[j]), ll = f2_unpack(l[j]);
+                Y[(size_t)row * kf + c] = oz_to_double(hh.x, ll.x, 0);
+            }
+        }
+    }
+}
+
 // 1/y per link as float-float (re_hi, re_lo, im_hi, im_lo); real: (hi, lo, 0, 0)
 template <class V>
 __global__ void ff_recip_kernel(int cnt, const V* __restrict__ y, float4* __restrict__ out)

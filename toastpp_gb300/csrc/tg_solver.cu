@@ -1197,6 +1197,7 @@ struct tg_solver_s {
     DBuf jwff;                        // the same as packed float-float (float-float Jacobian kernel)
     DBuf rel_cnt, rel_idx, rel_xc, rel_ac;
     DBuf absA, berr_max;              // |entries| of F in FP32, per-column backward-error maxima
+    DBuf valff;                       // F as float-float (the mixed path's residual products)
     DBuf results;                     // per-column results, compact, for the final read
     // direct solver: the complete factor's pattern (host and device)
     std::unique_ptr<ICHost> dh;
@@ -1359,6 +1360,8 @@ static void do_reset(tg_solver s, const double* cmua, const double* ckap, const 
     if (mixed) {
         launch(abs_values_kernel<V64>, cdiv_u(m.nnz, 256), 256, 0, s->stream, m.nnz, A,
                (float*)s->absA.ensure((size_t)m.nnz * sizeof(float)));
+        launch(ff_split_fields_kernel<vt<V64>::cplx>, cdiv_u(m.nnz, 256), 256, 0, s->stream, m.nnz, 1,
+               (const double*)A, 1, s->valff.ensure((size_t)m.nnz * (vt<V64>::cplx ? 16 : 8)));
         launch(cast_kernel<V32, V64>, cdiv_u(m.nnz, 256), 256, 0, s->stream, (size_t)m.nnz, A,
                (V32*)s->val32.ensure(m.nnz * sizeof(V32)));
         launch(cast_kernel<V32, V64>, cdiv_u(m.n, 256), 256, 0, s->stream, (size_t)m.n, idg,
@@ -1423,6 +1426,27 @@ static const unsigned* backward_error(tg_solver s, int k, int kf, const int* idx
     return cmax;
 }
 
+// A X for the columns idx[0..kf) of the FP64 block X (k columns), in
+// float-float arithmetic (spmm_ff_kernel), into Ac (node-major, kf columns)
+template <class V64>
+static void residual_product_ff(tg_solver s, int k, int kf, const int* idx, const V64* X, void* Xff, V64* Ac)
+{
+    constexpr bool CPLX = vt<V64>::cplx;
+    const MeshDev& m = s->mesh->d;
+    const size_t nkf = (size_t)m.n * kf;
+    launch(gather_cols_ff_kernel<CPLX>, cdiv_u(nkf, 256), 256, 0, s->stream, m.n, k, kf, idx, (const double*)X, Xff);
+    ProfScope ps(&s->prof, PC_SPMM, s->stream);
+    const unsigned grid = cdiv_u((size_t)m.n * 32, 256);
+    const void* A = s->valff.p;
+    switch ((kf + 31) / 32) {
+#define TG_FF(J) case J: launch(spmm_ff_kernel<CPLX, J>, grid, 256, 0, s->stream, m.n, m.rowptr, m.colidx, A, kf, \
+                                (const void*)Xff, (double*)Ac); break;
+    TG_FF(1) TG_FF(2) TG_FF(3) TG_FF(4) TG_FF(5) TG_FF(6) TG_FF(7) TG_FF(8)
+#undef TG_FF
+    default: throw Error{TG_ERR_UNSUPPORTED, "float-float residual product over more than 256 columns"};
+    }
+}
+
 // Solve F X = B for k right-hand sides; X holds the initial guess.
 // Mixed precision with reliable updates: one FP32 Krylov process per column
 // (BiCGSTAB, or COCG for complex systems) that is never restarted; whenever
@@ -1476,16 +1500,19 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
                 s->bnc.fetch(hc + 3, dcnt + 3, sizeof(int), s->stream);
                 const int kf = hc[3];
                 const unsigned* cmax = nullptr;
-                if (kf == k) {
-                    e64.spmm(k, X, R, nullptr, 0, nullptr, nullptr, 0);
-                    launch(resid_kernel<V64>, eg, 256, 0, s->stream, n, k, k, B, R, nullptr);
-                    cmax = backward_error<V64>(s, k, k, nullptr, X, B, R);
-                } else if (kf > 0) {
+                if (kf > 0) {
+                    // the product in float-float arithmetic (residual_product_ff;
+                    // FP64 above 256 columns)
                     const size_t nkf = (size_t)n * kf;
-                    V64* Xc = (V64*)s->rel_xc.ensure(nkf * sizeof(V64));
+                    void* Xc = s->rel_xc.ensure(nkf * sizeof(V64));
                     V64* Ac = (V64*)s->rel_ac.ensure(nkf * sizeof(V64));
-                    launch(gather_cols_kernel<V64>, cdiv_u(nkf, 256), 256, 0, s->stream, n, k, kf, idx, X, Xc);
-                    e64.spmm(kf, Xc, Ac, nullptr, 0, nullptr, nullptr, 0);
+                    if (kf <= 256) {
+                        residual_product_ff<V64>(s, k, kf, idx, X, Xc, Ac);
+                    } else {
+                        launch(gather_cols_kernel<V64>, cdiv_u(nkf, 256), 256, 0, s->stream, n, k, kf, idx, X,
+                               (V64*)Xc);
+                        e64.spmm(kf, (V64*)Xc, Ac, nullptr, 0, nullptr, nullptr, 0);
+                    }
                     launch(scatter_resid_kernel<V64>, cdiv_u(nkf, 256), 256, 0, s->stream, n, k, kf, idx, B, Ac, R);
                     cmax = backward_error<V64>(s, k, kf, idx, X, B, R);
                 }
