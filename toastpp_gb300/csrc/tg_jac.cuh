@@ -806,15 +806,15 @@ __device__ __forceinline__ double oz_f2d(float f, int e)
 // (h + l) * 2^e as a double: one FP64 addition, rounded once
 __device__ __forceinline__ double oz_to_double(float h, float l, int e) { return oz_f2d(h, e) + oz_f2d(l, e); }
 
-// (h, l) += x exactly (TwoSum; the error joins l)
-__device__ __forceinline__ void oz_acc(float& h, float& l, float x)
+// AI: left-factor items per thread: NT / QR threads share a source row, AI * (NT / QR) >= deg
+// (h, l) += x exactly, lane by lane on packed pairs (TwoSum)
+__device__ __forceinline__ void oz_acc2(f2x& h, f2x& l, f2x x)
 {
-    const float s = __fadd_rn(h, x), bp = __fsub_rn(s, h);
-    l = __fadd_rn(l, __fadd_rn(__fsub_rn(h, __fsub_rn(s, bp)), __fsub_rn(x, bp)));
+    const f2x s = f2_add(h, x), bp = f2_sub(s, h);
+    l = f2_add(l, f2_add(f2_sub(h, f2_sub(s, bp)), f2_sub(x, bp)));
     h = s;
 }
 
-// AI: left-factor items per thread: NT / QR threads share a source row, AI * (NT / QR) >= deg
 template <int S, int NG, int NT, int AI>
 __global__ void __launch_bounds__(NT, 1024 / NT) jacobian_oz_kernel(JacOzArgs a)
 {
@@ -1002,16 +1002,15 @@ __global__ void __launch_bounds__(NT, 1024 / NT) jacobian_oz_kernel(JacOzArgs a)
             const int mm = ntg * 4 + c4;
             const int l = lk[nt];
             if (ntg >= NTT || l < 0) continue;
-            float h[4], lo[4];
+            // the level sums, smallest first, in float-float; (Re mua, Re kappa)
+            // and (Im mua, Im kappa) as packed pairs
+            f2x srh = f2_pack(acc[nt][NA - 1][0], acc[nt][NA - 1][1]), srl = 0ull;
+            f2x sih = f2_pack(acc[nt][NA - 1][2], acc[nt][NA - 1][3]), sil = 0ull;
 #pragma unroll
-            for (int v = 0; v < 4; v++) {
-                h[v] = acc[nt][NA - 1][v];
-                lo[v] = 0.0f;
-#pragma unroll
-                for (int y = NA - 2; y >= 0; y--) oz_acc(h[v], lo[v], acc[nt][y][v]);
+            for (int y = NA - 2; y >= 0; y--) {
+                oz_acc2(srh, srl, f2_pack(acc[nt][y][0], acc[nt][y][1]));
+                oz_acc2(sih, sil, f2_pack(acc[nt][y][2], acc[nt][y][3]));
             }
-            f2x srh = f2_pack(h[0], h[1]), srl = f2_pack(lo[0], lo[1]);
-            f2x sih = f2_pack(h[2], h[3]), sil = f2_pack(lo[2], lo[3]);
             if (a.yinv) {
                 const float4 y = yk[nt];
                 f2x zrh = 0ull, zrl = 0ull, zih = 0ull, zil = 0ull;
