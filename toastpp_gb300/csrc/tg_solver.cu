@@ -1501,12 +1501,15 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
                 const int kf = hc[3];
                 const unsigned* cmax = nullptr;
                 if (kf > 0) {
-                    // the product in float-float arithmetic (residual_product_ff;
-                    // FP64 above 256 columns)
+                    // the product in float-float arithmetic (residual_product_ff),
+                    // or in FP64
                     const size_t nkf = (size_t)n * kf;
                     void* Xc = s->rel_xc.ensure(nkf * sizeof(V64));
                     V64* Ac = (V64*)s->rel_ac.ensure(nkf * sizeof(V64));
-                    if (kf <= 256) {
+                    // (float-float carries about 2^-46 of |A||x|: stopping tests finer
+                    // than 1e-13 take the FP64 product)
+                    const bool ff = kf <= 256 && s->tol >= 1e-13 && (s->cw_tol == 0 || s->cw_tol >= 1e-13);
+                    if (ff) {
                         residual_product_ff<V64>(s, k, kf, idx, X, Xc, Ac);
                     } else {
                         launch(gather_cols_kernel<V64>, cdiv_u(nkf, 256), 256, 0, s->stream, n, k, kf, idx, X,
@@ -1602,6 +1605,8 @@ static void solve_nm_body(tg_solver s, int k, const V64* B, V64* X, ColState* co
     if (s->method == TG_SOLVER_BICGSTAB && s->reliable) {
         // complex systems: COCG inner process (one SpMM and one IC(0) apply
         // per iteration) unless BiCGSTAB was asked for (reliable mode 1)
+        // (CG requests keep restarted refinement: the reliable-update CG
+        // process measured slower on the 3.2k-node CW disc, 9.6 against 8.4 ms)
         const bool cocg = vt<V32>::cplx && s->reliable == 2;
         solve_reliable<V64, V32>(s, k, B, X, co, R, R32, E32, ci, e64, e32, maxit, cocg);
         return;
