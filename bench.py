@@ -76,7 +76,9 @@ def parse():
                     choices=["c0_disc3k_cw", "c1_disc13k_fd", "c2_cyl30k_fd", "c3_box250k_fd", "c2s_cyl7k_fd",
                              "c3s_box106k_fd"])
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
-    ap.add_argument("--e2e-slots", type=int, default=1, help="e2e leg: request-server slots")
+    ap.add_argument("--e2e-slots", type=int, default=2, help="e2e leg: request-server slots")
+    ap.add_argument("--no-concurrent", action="store_true",
+                    help="skip the leg with two requests on the device at once")
     ap.add_argument("--grid", type=int, default=32,
                     help="grid-basis Jacobian leg: raster points per axis (0: skip)")
     ap.add_argument("--element", action="store_true",
@@ -531,6 +533,13 @@ def run_gpu(args):
                "serial": {"value": serial, "steps": ksteps,
                           "api": "tg_forward_path, one request at a time, page-locked host buffers"}}
 
+    # ---- two requests on the device at once (two solvers, two streams, two
+    # host threads, inputs resident): what the request server's slots do
+    concurrent = None
+    if not args.no_concurrent and j_bytes <= 16e9:
+        concurrent = concurrent_leg(args, gm, meth, cplx, omega, nq, nm, (d_cm, d_ck, d_ca, d_q, d_m), links, dev,
+                                    j_fp32, (vmul * nqm, (2 * nqm, jcols)), nsolves, ws)
+
     line = None
     if rank == 0:
         # ---- FP64 comparison legs (same request, plain FP64)
@@ -577,6 +586,7 @@ def run_gpu(args):
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "grid_jacobian": grid,
             "element_jacobian": element,
             "clocks": clocks, "wall_s": wall, "compare": compare, "serving": serving_leg,
+            "concurrent_requests": concurrent,
             "spmm_autotuner": capi.tuner_log().strip().splitlines(),
         }
         print(json.dumps(line), flush=True)
@@ -584,6 +594,54 @@ def run_gpu(args):
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     return 0
+
+
+def concurrent_leg(args, gm, meth, cplx, omega, nq, nm, d_in, links, dev, j_fp32, shapes, nsolves, ws, nreq=2,
+                   rounds=6):
+    """nreq requests at once: one solver, stream and host thread each, the
+    same device-resident inputs; wall time of `rounds` requests per thread
+    after one untimed round (the GIL is released inside the library calls)."""
+    import torch
+    from toastpp_gb300 import capi
+    d_cm, d_ck, d_ca, d_q, d_m = d_in
+    (np_lin, jshape) = shapes
+    work = []
+    for _ in range(nreq):
+        st = torch.cuda.Stream(device=dev)
+        s = capi.FwdSolver(gm, meth, args.tol, "ICH", cplx, precision=args.precision)
+        s.set_stream(st.cuda_stream)
+        if args.precision == "mixed":
+            s.set_refinement(args.inner_tol, 12, args.inner_order)
+            s.set_reliable_updates({"restart": 0, "bicgstab": 1, "cocg": 2}[args.inner])
+            s.set_backward_error(args.cw_tol)
+        out = (torch.empty(np_lin, dtype=torch.float64, device=dev), torch.empty(np_lin, dtype=torch.float64, device=dev),
+               torch.empty(jshape, dtype=torch.float32 if j_fp32 else torch.float64, device=dev))
+        work.append((s, out))
+
+    def run(i, reps):
+        s, (pr, lp, J) = work[i]
+        for _ in range(reps):
+            s.forward_path_raw(d_cm, d_ck, d_ca, omega, nq, d_q, nm, d_m, links, None, None, pr, lp, J, j_fp32,
+                               capi.MEM_DEVICE)
+
+    def timed(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ths = [threading.Thread(target=run, args=(i, reps)) for i in range(nreq)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    timed(1)
+    dt = timed(rounds)
+    for s, _ in work:
+        s.close()
+    return {"value": ws * nreq * rounds * nsolves / dt, "unit": UNIT, "requests_at_once": nreq,
+            "ms_per_round": dt * 1e3 / rounds, "rounds": rounds,
+            "api": "tg_forward_path on two solvers and streams from two host threads, inputs on the device"}
 
 
 def compare_legs(args, P, gm, s, stream, dev, links, d_par, omega, d_src, h_src, fields, value, res_kind):
