@@ -645,8 +645,8 @@ def concurrent_leg(args, gm, meth, cplx, omega, nq, nm, d_in, links, dev, j_fp32
 
 
 def compare_legs(args, P, gm, s, stream, dev, links, d_par, omega, d_src, h_src, fields, value, res_kind):
-    """Error of the measured request against the FP64 oracle, and the GPU
-    baselines the benchmark spec names, all outside the timed region:
+    """Error of the measured request against the FP64 oracle, and the plain
+    FP64 GPU baselines, all outside the timed region:
 
     - vs_oracle: the oracle's exact FP64 solve of the same request (the
       direct factorisation in a nested-dissection ordering, every source and
