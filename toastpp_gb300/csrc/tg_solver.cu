@@ -242,6 +242,13 @@ struct GraphCache {
     template <class F>
     void run(cudaStream_t st, const std::vector<const void*>& key, F body)
     {
+        // inside another capture: record the body into that graph
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        TG_CUDA(cudaStreamIsCapturing(st, &cs));
+        if (cs != cudaStreamCaptureStatusNone) {
+            body();
+            return;
+        }
         for (auto& e : entries)
             if (e.key == key) {
                 TG_CUDA(cudaGraphLaunch(e.exec, st));
@@ -1478,11 +1485,33 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
     int* dcnt = (int*)s->rel_cnt.ensure(4 * sizeof(int));
     int hc[4] = {0, 0, 0, 0};
     const int max_upd = 4 * std::max(1, s->max_outer);  // residual replacements per column
+    // COCG: the four iterations between two checks (the pending second half
+    // of the last one, then four times both halves up to the next check) are
+    // captured once per (k, buffers) and replayed as one graph; not while the
+    // profiler times kernel classes (its events would be captured)
+    const bool unit_graph = cocg && !(s->prof.mask);
+    const std::vector<const void*> ukey = {(const void*)"cocg-unit", (const void*)(size_t)k, X32, ci, R32,
+                                           e32.vec(0, nk), e32.vec(1, nk), e32.vec(2, nk), e32.vec(3, nk),
+                                           e32.A, e32.L, e32.Lef, e32.Leb, e32.dinv, (const void*)(size_t)e32.ico,
+                                           e32.part.p};
     int it = 0;
+    bool pending = false;  // COCG: the second half (z, beta, p) of the last iteration
     for (;;) {
-        if (cocg) e32.cocg_step1(k, X32, ci);
-        else e32.bicg_iter(k, X32, ci, it == 0);
-        it++;
+        if (unit_graph && it >= 4 && (it & 3) == 0 && it + 4 < maxit) {
+            e32.graphs.run(s->stream, ukey, [&] {
+                for (int u = 0; u < 4; u++) {
+                    e32.cocg_step2(k, ci);
+                    e32.cocg_step1(k, X32, ci);
+                }
+            });
+            it += 4;
+        } else {
+            if (pending) e32.cocg_step2(k, ci);
+            if (cocg) e32.cocg_step1(k, X32, ci);
+            else e32.bicg_iter(k, X32, ci, it == 0);
+            it++;
+        }
+        pending = cocg;
         const bool at_limit = it >= maxit;
         if ((it & 3) == 0 || at_limit) {
             launch(rel_flags_kernel, 1, 256, 0, s->stream, k, co, ci, dcnt);
@@ -1537,7 +1566,6 @@ static void solve_reliable(tg_solver s, int k, const V64* B, V64* X, ColState* c
                 if (limit) break;
             }
         }
-        if (cocg) e32.cocg_step2(k, ci);
     }
     launch(rel_finish_kernel, ek, 128, 0, s->stream, k, co, ci);
 }
