@@ -918,10 +918,26 @@ struct Engine {
             finalize<2>(k, cst, PH_PCG_END);
             launch(pcg_d_kernel<V, S>, eg, 256, 0, st, m.n, k, k, cst, D, Z);
         };
-        for (int it = 0; it < maxit; it++) {
+        // the four iterations between two checks: captured once per (k,
+        // buffers) and replayed as one graph after the first four (which run
+        // the autotuners); not while the profiler times kernel classes
+        const bool unit_graph = !(prof && prof->mask);
+        const std::vector<const void*> ukey = {(const void*)"pcg-unit", (const void*)(size_t)k, X, cst, R, D, Q, Z, A,
+                                               L, Lef, Leb, dinv, idiag, (const void*)(size_t)precon,
+                                               (const void*)(size_t)ico, part.p};
+        for (int it = 0; it < maxit;) {
+            if (unit_graph && it >= 4 && (it & 3) == 0 && it + 4 <= maxit) {
+                graphs.run(st, ukey, [&] {
+                    for (int u = 0; u < 4; u++) iteration();
+                });
+                it += 4;
+                if (count_active(k, cst) == 0) break;
+                continue;
+            }
             iteration();
             if ((it & 3) == 3 || it + 1 == maxit)
                 if (count_active(k, cst) == 0) break;
+            it++;
         }
     }
 };
