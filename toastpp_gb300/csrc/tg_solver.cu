@@ -888,10 +888,27 @@ struct Engine {
     void bicgstab(int k, V* X, ColState* cst, int maxit)
     {
         bicg_begin(k, cst);
-        for (int it = 0; it < maxit; it++) {
+        // the four iterations between two checks as one captured graph, as in pcg
+        const bool unit_graph = !(prof && prof->mask);
+        const size_t nk = (size_t)mesh->d.n * k;
+        for (int it = 0; it < maxit;) {
+            if (unit_graph && it >= 4 && (it & 3) == 0 && it + 4 <= maxit) {
+                const std::vector<const void*> ukey = {(const void*)"bicg-unit", (const void*)(size_t)k, X, cst,
+                                                       vec(0, nk), vec(1, nk), vec(2, nk), vec(3, nk), vec(4, nk),
+                                                       vec(5, nk), vec(6, nk), vec(7, nk), A, L, Lef, Leb, dinv, idiag,
+                                                       (const void*)(size_t)precon, (const void*)(size_t)ico,
+                                                       parts(k, 2)};
+                graphs.run(st, ukey, [&] {
+                    for (int u = 0; u < 4; u++) bicg_iter(k, X, cst, 0);
+                });
+                it += 4;
+                if (count_active(k, cst) == 0) break;
+                continue;
+            }
             bicg_iter(k, X, cst, it == 0);
             if ((it & 3) == 3 || it + 1 == maxit)
                 if (count_active(k, cst) == 0) break;
+            it++;
         }
     }
 
