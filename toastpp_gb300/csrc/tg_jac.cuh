@@ -718,19 +718,22 @@ __global__ void __launch_bounds__(NT) jacobian_ff_kernel(JacFFArgs a)
 //
 // Exact digit products (the splitting scheme of Ozaki et al.): every row of
 // the left factor and every column of the right one is scaled by a power of
-// two to |x| < 128 and cut into S balanced base-256 digits (integers in
+// two to |x| < 128 and cut into S = 7 balanced base-256 digits (integers in
 // [-256, 256] when the hi and lo floats are cut separately and added), each
-// exact in bf16.  A digit product is exact in FP32 and so is a sum of them
-// while it stays below 2^24 (K <= 64, at most 3 digit pairs per level), so
-// the bf16 tensor-core products of digit levels 2, 3 and 4 (t + u = level,
-// slices pre-scaled by 256^-t) are exact; levels 5 and above (relative weight
-// 2^-24 and less) share one accumulator.  The four accumulators are summed
-// in float-float, scaled back, multiplied by 1/y and rounded once.  S = 6
-// keeps 48 bits of every operand: on the meshes measured the L2 error is
-// ~1e-14 of the exact sums, the worst entry (strong cancellation) ~1e-10.
+// exact in bf16 and pre-scaled by 256^-t.  A digit product is exact in FP32
+// and so is a sum of products of one level t + u while it stays below 2^24
+// units (K <= 64, at most four digit pairs per level): levels 0 to 3 have an
+// accumulator each and are exact; levels 4 to 6 (relative weight 2^-32 and
+// less) share one.  (Merging levels 3 and up measured 1e-12 instead of
+// 4e-15: the tensor core's sum of mixed-level products is not exact.)  The
+// five accumulators are summed in float-float on packed (mua, kappa) pairs,
+// multiplied by 1/y in float-float and rounded once, scaled back by the
+// exponents.  Against an FP64 Jacobian of the same fields: ~4e-15 in L2.
 //
-// CTA = (node, chunk of jmc detectors); 10 warps; mma.sync m16n8k16 bf16:
-// m-tile = 8 sources x (Re, Im) rows, n-tile = 4 detectors x (mua, kappa).
+// CTA = (node, chunk of jmc detectors), 512 threads, two CTAs per SM;
+// mma.sync m16n8k16 bf16 with m-tile = 8 sources x (Re, Im) rows and n-tile =
+// 4 detectors x (mua, kappa), so each thread ends with the four J entries of
+// one link.
 // ---------------------------------------------------------------------------
 struct JacOzArgs {
     MeshDev m;
