@@ -724,8 +724,8 @@ __global__ void __launch_bounds__(NT) jacobian_ff_kernel(JacFFArgs a)
 // and so is a sum of products of one level t + u while it stays below 2^24
 // units (K <= 64, at most four digit pairs per level): levels 0 to 3 have an
 // accumulator each and are exact; levels 4 to 6 (relative weight 2^-32 and
-// less) share one.  (Merging levels 3 and up measured 1e-12 instead of
-// 4e-15: the tensor core's sum of mixed-level products is not exact.)  The
+// less) share one.  (One accumulator for levels 3 and up measured 1.3e-12
+// instead of 4e-15: a sum of products of mixed levels is not exact.)  The
 // five accumulators are summed in float-float on packed (mua, kappa) pairs,
 // multiplied by 1/y in float-float and rounded once, scaled back by the
 // exponents.  Against an FP64 Jacobian of the same fields: ~4e-15 in L2.
