@@ -111,9 +111,14 @@ int tg_mesh_destroy(tg_mesh mesh);
    (Mesh::PullToBoundary, src/libfe/mesh.cc:1052-1111; where no boundary side
    takes the projection the reference keeps the position, and so does this);
    fixed positions outside every element are nudged by 1e-4 along an axis
-   (qmmesh.cc:112-127).  "external" lists give TG_ERR_UNSUPPORTED; a dimension
-   other than the mesh's, a missing section or a detector index out of range
-   give TG_ERR_ARG. */
+   (qmmesh.cc:112-127).  An "external" source list moves each source to the
+   boundary point Mesh::BndIntersect (mesh.cc:1369-1453) finds from q + |q| n
+   towards q, n the unit normal read with the position, or along -q when the
+   list's normals flag is "default" (qmmesh.cc:378-391); an "external"
+   measurement list is kept as read (LoadQM skips InitM).  A dimension other
+   than the mesh's, a missing section, a detector index out of range, a zero
+   normal in an external list whose normals are not "default", or an external
+   source whose line meets no boundary side give TG_ERR_ARG. */
 typedef struct tg_qm_s *tg_qm;
 int tg_qm_load(tg_mesh mesh, const char *path, tg_qm *out);
 int tg_qm_info(tg_qm qm, int *dim, int *nq, int *nm, int *nqm);

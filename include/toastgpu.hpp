@@ -101,7 +101,8 @@ private:
 };
 
 // QMMesh::LoadQM (src/libfe/qmmesh.cc:319-460) with InitM's detector
-// placement, against a mesh: positions Q, M (row-major, dim per point) and
+// placement and the boundary projection of "external" sources, against a
+// mesh: positions Q, M (row-major, dim per point) and
 // the link list (nQMref / QMref as offsets and detector indices)
 struct QMData {
     int dim = 0, nQ = 0, nM = 0, nQM = 0;

@@ -66,6 +66,10 @@ def lib():
         L.tor_direct_solve.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, C.c_int]
         L.tor_el_found.restype = C.c_int
         L.tor_el_found.argtypes = [C.c_void_p, _dp]
+        L.tor_bnd_intersect.restype = C.c_int
+        L.tor_bnd_intersect.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.tor_external_source.restype = C.c_int
+        L.tor_external_source.argtypes = [C.c_void_p, _dp, C.c_void_p, _dp]
         L.tor_qvec_gaussian.argtypes = [C.c_void_p, _dp, C.c_double, C.c_int, _dp]
         L.tor_assemble.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, C.c_int, _dp]
         L.tor_solve.restype = C.c_int
@@ -165,6 +169,34 @@ class Mesh:
                     out.append(self.pull_to_boundary(p))
                 except RuntimeError:
                     out.append(p.copy())
+        return np.array(out).reshape(-1, self.dim)
+
+    def bnd_intersect(self, p1, p2) -> np.ndarray:
+        """Mesh::BndIntersect (mesh.cc:1369-1453): the boundary point nearest
+        p1 on the segment p1-p2 (2D) or on the line through them (3D)."""
+        out = np.zeros(self.dim)
+        rc = lib().tor_bnd_intersect(self._h, np.ascontiguousarray(p1, np.float64),
+                                     np.ascontiguousarray(p2, np.float64), out)
+        if rc:
+            raise RuntimeError("BndIntersect: no boundary point found")
+        return out
+
+    def external_sources(self, Q, QN=None) -> np.ndarray:
+        """QMMesh::LoadQM's "external" source positions (qmmesh.cc:378-391):
+        each position moved to the boundary point BndIntersect finds from
+        q + |q| n towards q, n the unit normal read with the position (QN) or,
+        for a list marked "default" (QN None), the unit vector along -q."""
+        out = []
+        for i, q in enumerate(np.asarray(Q, np.float64)):
+            r = np.zeros(self.dim)
+            nrm = None if QN is None else np.ascontiguousarray(QN[i], np.float64)
+            rc = lib().tor_external_source(self._h, np.ascontiguousarray(q), None if nrm is None else
+                                           nrm.ctypes.data_as(C.c_void_p), r)
+            if rc == 2:
+                raise RuntimeError("no normal given for an external source")
+            if rc:
+                raise RuntimeError("BndIntersect: no boundary point found")
+            out.append(r)
         return np.array(out).reshape(-1, self.dim)
 
     def qvec_gaussian(self, cnt, w, neumann=True) -> np.ndarray:

@@ -1296,6 +1296,179 @@ int tor_el_found(const tor_mesh *m, const double *p)
     return 0;
 }
 
+/* Triangle3::Intersection (tri3.cc:698-780) with add_endpoints false and
+   boundary_only true, in the element's local frame.  The reference tests the
+   flag of side 1 against the edge x = 0 and the flag of side 2 against the
+   edge x + y = 1, although side 1 joins nodes 1-2 (x + y = 1) and side 2
+   nodes 2-0 (x = 0) (tri3.cc:121-127); the same pairing is kept.  The points
+   found are then kept only where they lie on the segment p1-p2. */
+static int tri_bnd_intersect(const unsigned char *bs, const double *p1, const double *p2, double s[4][3])
+{
+    const double EPS = 1e-12;
+    int k = 0;
+    if (bs[0] && p1[1] * p2[1] < 0.0) {
+        double xs = p1[0] - p1[1] / (p2[1] - p1[1]) * (p2[0] - p1[0]);
+        if (xs > -EPS && xs < 1.0 + EPS) { s[k][0] = xs; s[k][1] = 0.0; k++; }
+    }
+    if (bs[1] && p1[0] * p2[0] < 0.0) {
+        double ys = p1[1] - p1[0] / (p2[0] - p1[0]) * (p2[1] - p1[1]);
+        if (ys > -EPS && ys < 1.0 + EPS) { s[k][0] = 0.0; s[k][1] = ys; k++; }
+    }
+    if (bs[2]) {
+        double xs;
+        if (fabs(p1[0] - p2[0]) > EPS) {
+            double a = (p1[1] - p2[1]) / (p1[0] - p2[0]);
+            double c = p1[1] - a * p1[0];
+            xs = (1.0 - c) / (a + 1.0);
+        } else {
+            xs = p1[0];
+        }
+        if (xs > -EPS && xs < 1.0 + EPS) { s[k][0] = xs; s[k][1] = 1.0 - xs; k++; }
+    }
+    if (k) {
+        int d = 0, j = 0;
+        double dp = p2[0] - p1[0];
+        if (fabs(dp) < EPS) { d = 1; dp = p2[1] - p1[1]; }
+        for (int i = 0; i < k; i++) {
+            double a = (s[i][d] - p1[d]) / dp;
+            if (a < -EPS || a > 1.0 + EPS) continue;
+            s[j][0] = s[i][0]; s[j][1] = s[i][1]; j++;
+        }
+        k = j;
+    }
+    return k;
+}
+
+/* Tetrahedron4::Intersection (tet4.cc:1222-1283) with boundary_only true: the
+   line through p1 and p2 (not only the segment) against the planes of the
+   boundary faces, each point kept where it lies in the face's triangle. */
+static int tet_bnd_intersect(const unsigned char *bs, const double *p1, const double *p2, double s[4][3])
+{
+    int n = 0;
+    double a, rx, ry, rz;
+    double sx = p1[0], sy = p1[1], sz = p1[2];
+    double dx = p2[0] - p1[0], dy = p2[1] - p1[1], dz = p2[2] - p1[2];
+    if (bs[0] && dz != 0.0) {
+        a = -sz / dz; rx = sx + a * dx; ry = sy + a * dy;
+        if (rx >= 0 && ry >= 0 && rx + ry <= 1) { s[n][0] = rx; s[n][1] = ry; s[n][2] = 0.0; n++; }
+    }
+    if (bs[1] && dy != 0.0) {
+        a = -sy / dy; rx = sx + a * dx; rz = sz + a * dz;
+        if (rx >= 0 && rz >= 0 && rx + rz <= 1) { s[n][0] = rx; s[n][1] = 0.0; s[n][2] = rz; n++; }
+    }
+    if (bs[2] && dx != 0.0) {
+        a = -sx / dx; ry = sy + a * dy; rz = sz + a * dz;
+        if (ry >= 0 && rz >= 0 && ry + rz <= 1) { s[n][0] = 0.0; s[n][1] = ry; s[n][2] = rz; n++; }
+    }
+    if (bs[3] && (dx + dy + dz) != 0.0) {
+        a = (1 - sx - sy - sz) / (dx + dy + dz);
+        rx = sx + a * dx; ry = sy + a * dy; rz = sz + a * dz;
+        if (rx >= 0 && ry >= 0 && rx + ry <= 1) { s[n][0] = rx; s[n][1] = ry; s[n][2] = rz; n++; }
+    }
+    return n;
+}
+
+/* Mesh::BndIntersect (mesh.cc:1369-1453): in 3D the line must first cross
+   the mesh's bounding box (Mesh::BoundingBox, mesh.cc:1341-1360); then every
+   element with a boundary side intersects the line in its local frame
+   (Element::GlobalIntersection, element.cc:505-511), each point is mapped
+   back (Element::Global, element.cc:164-176) and the one nearest pt1 (the
+   first of equal distance) is the result.  Returns 0, or 1 when nothing is
+   found (the reference then returns an empty point). */
+int tor_bnd_intersect(const tor_mesh *m, const double *pt1, const double *pt2, double *out)
+{
+    const int dim = m->dim, nn = m->nn, nside = dim == 2 ? 3 : 4;
+    if (dim > 2) {
+        const double EPS = 1e-12;
+        double lo[3] = {1e6, 1e6, 1e6}, hi[3] = {-1e6, -1e6, -1e6};
+        for (int k = 0; k < m->n; k++)
+            for (int d = 0; d < 3; d++) {
+                double v = m->x[(size_t)k * 3 + d];
+                if (v < lo[d]) lo[d] = v;
+                if (v > hi[d]) hi[d] = v;
+            }
+        double d[3] = {pt2[0] - pt1[0], pt2[1] - pt1[1], pt2[2] - pt1[2]};
+        int hit = 0;
+        /* the faces z = const, then y = const, then x = const; u, v are the
+           two other axes */
+        static const int AX[3][3] = {{2, 0, 1}, {1, 0, 2}, {0, 1, 2}};
+        for (int f = 0; f < 3 && !hit; f++) {
+            int w = AX[f][0], u = AX[f][1], v = AX[f][2];
+            if (d[w] == 0.0) continue;
+            for (int side = 0; side < 2 && !hit; side++) {
+                double a = ((side ? hi[w] : lo[w]) - pt1[w]) / d[w];
+                double ru = pt1[u] + a * d[u], rv = pt1[v] + a * d[v];
+                if (ru > lo[u] - EPS && ru < hi[u] + EPS && rv > lo[v] - EPS && rv < hi[v] + EPS) hit = 1;
+            }
+        }
+        if (!hit) return 1;
+    }
+    double dstmin = 1e10;
+    int found = 0;
+    for (int e = 0; e < m->ne; e++) {
+        const unsigned char *bs = m->bndside + (size_t)e * nside;
+        int any = 0;
+        for (int s = 0; s < nside; s++) any |= bs[s];
+        if (!any) continue;
+        const int *nd = m->el + (size_t)e * nn;
+        const double *g = m->geo + (size_t)e * 16;
+        double l1[3], l2[3], s[4][3];
+        if (dim == 2) {  /* Triangle3::Local (tri3.cc:134-144) */
+            double scale = 1.0 / (g[0] + g[1] + g[2]);
+            l1[0] = (g[1] + g[4] * pt1[0] + g[7] * pt1[1]) * scale;
+            l1[1] = (g[2] + g[5] * pt1[0] + g[8] * pt1[1]) * scale;
+            l2[0] = (g[1] + g[4] * pt2[0] + g[7] * pt2[1]) * scale;
+            l2[1] = (g[2] + g[5] * pt2[0] + g[8] * pt2[1]) * scale;
+        } else {  /* Tetrahedron4::Local (tet4.cc:186-196) */
+            const double *a = g, *b = g + 4, *c = g + 8, *dd = g + 12;
+            double scale = 1.0 / (a[0] + a[1] + a[2] + a[3]);
+            for (int r = 0; r < 3; r++) {
+                l1[r] = (a[r + 1] + b[r + 1] * pt1[0] + c[r + 1] * pt1[1] + dd[r + 1] * pt1[2]) * scale;
+                l2[r] = (a[r + 1] + b[r + 1] * pt2[0] + c[r + 1] * pt2[1] + dd[r + 1] * pt2[2]) * scale;
+            }
+        }
+        int k = dim == 2 ? tri_bnd_intersect(bs, l1, l2, s) : tet_bnd_intersect(bs, l1, l2, s);
+        for (int j = 0; j < k; j++) {
+            double u[4], glob[3];
+            if (dim == 2) { u[0] = 1.0 - s[j][0] - s[j][1]; u[1] = s[j][0]; u[2] = s[j][1]; }
+            else { u[0] = 1.0 - s[j][0] - s[j][1] - s[j][2]; u[1] = s[j][0]; u[2] = s[j][1]; u[3] = s[j][2]; }
+            for (int c = 0; c < dim; c++) {
+                glob[c] = 0.0;
+                for (int i = 0; i < nn; i++) glob[c] += u[i] * m->x[(size_t)nd[i] * dim + c];
+            }
+            double dst = pt_dist(pt1, glob, dim);
+            if (dst < dstmin) {
+                dstmin = dst;
+                for (int c = 0; c < dim; c++) out[c] = glob[c];
+                found = 1;
+            }
+        }
+    }
+    return found ? 0 : 1;
+}
+
+/* An "external" source position of QMMesh::LoadQM (qmmesh.cc:378-391): the
+   unit direction n (the normal read with the position, or -q when the list
+   says "default"; TVector::operator/= multiplies by the reciprocal,
+   vector_imp.hpp:672-677; l2norm is the plain root of the sum of squares,
+   vector_imp.hpp:1117-1120, 1290-1298) and the boundary point that
+   BndIntersect finds from q + |q| n towards q.  nrm NULL: default normals.
+   Returns 0, 2 for a zero normal, 1 when no boundary point is found. */
+int tor_external_source(const tor_mesh *m, const double *q, const double *nrm, double *out)
+{
+    const int dim = m->dim;
+    double n[3], s = 0.0, sq = 0.0, p1[3];
+    for (int c = 0; c < dim; c++) n[c] = nrm ? nrm[c] : -q[c];
+    for (int c = 0; c < dim; c++) s += fabs(n[c]) * fabs(n[c]);
+    if (nrm && !(sqrt(s) > 0.0)) return 2;
+    double inv = 1.0 / sqrt(s);
+    for (int c = 0; c < dim; c++) n[c] *= inv;
+    for (int c = 0; c < dim; c++) sq += fabs(q[c]) * fabs(q[c]);
+    double len = sqrt(sq);
+    for (int c = 0; c < dim; c++) p1[c] = q[c] + len * n[c];
+    return tor_bnd_intersect(m, p1, q, out);
+}
+
 /* Raster_Pixel with the grid equal to the basis (raster.cc:18-83,
    raster_px.cc:10-48, the case bdim == gdim):
    - bounding box: Mesh::BoundingBox (mesh.cc:1341-1360), no padding;

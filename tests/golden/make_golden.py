@@ -24,7 +24,8 @@ The qm_* fixtures hold a QM file written here (seeded positions off the
 boundary, sparse link lists, normals on some lines), its mesh, and what the
 reference's QMMesh::LoadQM made of them: source positions, detector
 positions after InitM's placement (pulled to the boundary, or fixed and
-nudged into an element) and the link list.
+nudged into an element; "external" lists as LoadQM leaves them) and the
+link list.
 
 Usage:  make -f oracle/Makefile.ref REF=<reference tree> -j8
         python tests/golden/make_golden.py [fixture names]
@@ -187,20 +188,21 @@ def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradi
     print(name, "n", P.n, "links", len(res["proj"]), "its", res["it_fwd"], res["it_adj"])
 
 
-def qm_text(P, Q, M, links, mflag, seed):
+def qm_text(P, Q, M, links, mflag, seed, qflag="", QN=None, MN=None):
     """A QM file as QMMesh::LoadQM reads it (qmmesh.cc:319-460): every other
     position line also carries a normal, which the reader parses and drops
-    for non-external lists."""
+    for non-external lists; QN / MN, where given, are the normals of every
+    line of that list."""
     rng = np.random.default_rng(seed)
     dim = P.dim
-    out = [f"QM file {dim}D", f"Dimension {dim}", "", f"SourceList {len(Q)}"]
+    out = [f"QM file {dim}D", f"Dimension {dim}", "", f"SourceList {len(Q)}" + (" " + qflag if qflag else "")]
     for i, p in enumerate(Q):
-        vals = list(p) + (list(rng.standard_normal(dim)) if i % 2 else [])
-        out.append(" ".join(repr(float(v)) for v in vals))
+        nrm = list(QN[i]) if QN is not None else (list(rng.standard_normal(dim)) if i % 2 else [])
+        out.append(" ".join(repr(float(v)) for v in list(p) + nrm))
     out += ["", f"MeasurementList {len(M)}" + (" " + mflag if mflag else "")]
     for i, p in enumerate(M):
-        vals = list(p) + (list(rng.standard_normal(dim)) if i % 2 == 0 else [])
-        out.append(" ".join(repr(float(v)) for v in vals))
+        nrm = list(MN[i]) if MN is not None else (list(rng.standard_normal(dim)) if i % 2 == 0 else [])
+        out.append(" ".join(repr(float(v)) for v in list(p) + nrm))
     out += ["", "LinkList"]
     for ms in links:
         out.append(f"{len(ms)}: " + " ".join(str(m) for m in ms))
@@ -215,14 +217,37 @@ def _radial(P, pts, dr):
     return pts
 
 
+def _tilted_inward(rng, Q, deg):
+    """Unit normals along -q turned by up to deg degrees in the x-y plane,
+    scaled by a random length (the reader normalises them)."""
+    out = []
+    for q in Q:
+        n = -np.asarray(q, float) / np.linalg.norm(q)
+        t = np.radians(rng.uniform(-deg, deg))
+        c, s = np.cos(t), np.sin(t)
+        n[:2] = c * n[0] - s * n[1], s * n[0] + c * n[1]
+        out.append(n * rng.uniform(0.5, 2.0))
+    return np.array(out)
+
+
 def qm_case(kind):
     """Problem and QM text of a QM fixture: detectors pulled to the boundary
     (2D and 3D) or at fixed positions just inside (or, one of them, 5e-5
-    outside) the boundary; sparse link lists with a source without links."""
-    rng = np.random.default_rng({"qm_disc_pull": 31, "qm_cyl_pull": 32, "qm_disc_fixed": 33}[kind])
+    outside) the boundary; sparse link lists with a source without links.
+    The *_external cases put the sources outside the mesh in an "external"
+    list: 2D with the "default" normals (towards the origin), 3D with
+    normals read from the file, tilted from the inward radius; their
+    detectors are an "external" list too, kept where they were read."""
+    seeds = {"qm_disc_pull": 31, "qm_cyl_pull": 32, "qm_disc_fixed": 33, "qm_disc_external": 34,
+             "qm_cyl_external": 35}
+    rng = np.random.default_rng(seeds[kind])
     P = workloads.disc(8, 3, 0.0, 6) if kind.startswith("qm_disc") else small_cylinder(0.0, nopt=6)
     nq, nm = len(P.qm.Q), len(P.qm.M)
-    Q = _radial(P, P.qm.Q, rng.uniform(-0.3, 0.3, nq))
+    qflag, QN, MN = "", None, None
+    if kind.endswith("_external"):
+        Q = _radial(P, P.qm.Q, rng.uniform(0.05, 0.5, nq))
+    else:
+        Q = _radial(P, P.qm.Q, rng.uniform(-0.3, 0.3, nq))
     if kind == "qm_disc_fixed":
         # midpoints of boundary edges (edges of one triangle only), moved
         # inward 1e-3 (the last 5e-5 outward)
@@ -237,6 +262,14 @@ def qm_case(kind):
         M = mids[order[np.linspace(0, len(order) - 1, nm, endpoint=False).astype(int)]]
         M = _radial(P, np.array(M), np.array([-1e-3] * (nm - 1) + [5e-5]))
         flag = "fixed"
+    elif kind == "qm_disc_external":
+        M = _radial(P, P.qm.M, rng.uniform(-0.4, 0.4, nm))
+        qflag, flag = "external default", "external"
+        MN = rng.standard_normal((nm, P.dim))
+    elif kind == "qm_cyl_external":
+        M = _radial(P, P.qm.M, rng.uniform(-0.4, 0.4, nm))
+        qflag, flag = "external", "external default"
+        QN = _tilted_inward(rng, Q, 25.0)
     else:
         M = _radial(P, P.qm.M, rng.uniform(-0.4, 0.4, nm))
         flag = ""
@@ -247,7 +280,7 @@ def qm_case(kind):
         else:
             ms = [m for m in range(nm) if q == 0 or rng.uniform() < 0.7]
             links.append(ms)
-    return P, qm_text(P, Q, M, links, flag, rng.integers(1 << 30))
+    return P, qm_text(P, Q, M, links, flag, rng.integers(1 << 30), qflag, QN, MN)
 
 
 def run_qm(name):
@@ -270,7 +303,7 @@ def run_qm(name):
     print(name, "nQ", len(qpos), "nM", len(mpos), "nQM", len(qmref))
 
 
-QM_FIXTURES = ("qm_disc_pull", "qm_cyl_pull", "qm_disc_fixed")
+QM_FIXTURES = ("qm_disc_pull", "qm_cyl_pull", "qm_disc_fixed", "qm_disc_external", "qm_cyl_external")
 
 
 def main():

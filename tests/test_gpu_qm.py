@@ -1,6 +1,7 @@
-"""tg_qm_load (QMMesh::LoadQM with InitM's detector placement) against what
-the compiled reference's LoadQM made of the same files (tests/golden/qm_*.npz),
-its error paths, and its positions and links driving a forward request."""
+"""tg_qm_load (QMMesh::LoadQM with InitM's detector placement and the
+"external" lists' boundary projection) against what the compiled reference's
+LoadQM made of the same files (tests/golden/qm_*.npz), its error paths, and
+its positions and links driving a forward request."""
 import numpy as np
 import pytest
 
@@ -28,11 +29,13 @@ def _edit(text, old, new):
 @pytest.mark.parametrize("change,code", [
     (lambda t: _edit(t, "QM file", "XX file"), capi.ERR_ARG),
     (lambda t: _edit(t, "Dimension 2", "Dimension 3"), capi.ERR_ARG),
-    (lambda t: _edit(t, "MeasurementList 6", "MeasurementList 6 external"), capi.ERR_UNSUPPORTED),
+    (lambda t: _edit(t, "MeasurementList 6", "MeasurementList 6 external"), capi.ERR_ARG),
+    (lambda t: _edit(t, "SourceList 6", "SourceList 6 external"), capi.ERR_ARG),
     (lambda t: t[:t.index("LinkList")], capi.ERR_ARG),
     (lambda t: t.rstrip() + " 9\n", None),
     (lambda t: _edit(t, "LinkList\n6:", "LinkList\n6: 7"), capi.ERR_ARG),
-], ids=["header", "dimension", "external", "no_linklist", "trailing", "detector_range"])
+], ids=["header", "dimension", "external_detector_without_normal", "external_source_without_normal",
+        "no_linklist", "trailing", "detector_range"])
 def test_qm_load_errors(change, code, tmp_path):
     g, path = load_qm("qm_disc_pull", tmp_path)
     mesh = capi.Mesh(g["coords"], g["elems"])

@@ -100,11 +100,20 @@ def test_oracle_qm_placement_matches_reference(oracle_mod, name, tmp_path):
     places them (pulled to the boundary, or fixed and nudged into an
     element) equal what the compiled reference's LoadQM made, bit for bit.
     qm_disc_pull has two detectors whose projection no boundary side takes:
-    the reference keeps them where they were read."""
+    the reference keeps them where they were read.  The *_external files
+    move their sources to the boundary along the normals (2D: the segment
+    from near the origin; 3D: the whole line, where the reference takes the
+    crossing on the far side) and keep their detectors as read."""
     from toastpp_gb300 import meshio
     g, path = load_qm(name, tmp_path)
     qm = meshio.read_qm(path)
     mesh = oracle_mod.Mesh(g["coords"], g["elems"])
-    assert np.array_equal(qm.Q, g["qpos"])
-    assert np.array_equal(mesh.place_detectors(qm.M, qm.m_fixed), g["mpos"])
+    if qm.q_external:
+        Q = mesh.external_sources(qm.Q, None if qm.q_default_normals else qm.QN)
+        assert not np.array_equal(Q, qm.Q)
+    else:
+        Q = qm.Q
+    assert np.array_equal(Q, g["qpos"])
+    M = qm.M if qm.m_external else mesh.place_detectors(qm.M, qm.m_fixed)
+    assert np.array_equal(M, g["mpos"])
     assert np.array_equal(qm.link_ofs, g["link_ofs"]) and np.array_equal(qm.link_m, g["link_m"])

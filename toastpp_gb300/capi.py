@@ -476,7 +476,8 @@ def omega_of(freq_mhz):
 
 class QM:
     """tg_qm_load: a QM file read against a mesh (QMMesh::LoadQM with
-    InitM's detector placement).  Q, M: positions; links: the link list."""
+    InitM's detector placement; "external" sources moved to the boundary
+    along their normals).  Q, M: positions; links: the link list."""
 
     def __init__(self, mesh: Mesh, path: str):
         h = C.c_void_p()

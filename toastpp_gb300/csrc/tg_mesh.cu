@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <atomic>
 #include <array>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 #include "tg_mesh.cuh"
@@ -825,6 +826,171 @@ bool el_found(const MeshHost& m, const double* p)
     for (int e = 0; e < m.ne; e++)
         if (el_gcontains(m, e, p)) return true;
     return false;
+}
+
+// The line (or segment) p1-p2 against one element's boundary sides, in the
+// element's local frame; up to 4 points into s, their count returned.
+//  - Triangle3::Intersection (tri3.cc:698-780), boundary sides only: side 0
+//    is tested against the edge y = 0, the flag of side 1 against x = 0 and
+//    that of side 2 against x + y = 1 (the reference pairs them so, although
+//    side 1 joins nodes 1-2 and side 2 nodes 2-0, tri3.cc:121-127); points
+//    off the segment p1-p2 are dropped.
+//  - Tetrahedron4::Intersection (tet4.cc:1222-1283): the whole line against
+//    the boundary faces' planes, each point kept inside its face.
+static int side_intersections(const MeshHost& m, int e, const double* p1, const double* p2, double s[4][3])
+{
+    const unsigned char* bs = &m.bndside[(size_t)e * (m.dim == 2 ? 3 : 4)];
+    int k = 0;
+    if (m.dim == 2) {
+        const double EPS = 1e-12;
+        if (bs[0] && p1[1] * p2[1] < 0.0) {
+            const double xs = p1[0] - p1[1] / (p2[1] - p1[1]) * (p2[0] - p1[0]);
+            if (xs > -EPS && xs < 1.0 + EPS) { s[k][0] = xs; s[k][1] = 0.0; k++; }
+        }
+        if (bs[1] && p1[0] * p2[0] < 0.0) {
+            const double ys = p1[1] - p1[0] / (p2[0] - p1[0]) * (p2[1] - p1[1]);
+            if (ys > -EPS && ys < 1.0 + EPS) { s[k][0] = 0.0; s[k][1] = ys; k++; }
+        }
+        if (bs[2]) {
+            double xs = p1[0];
+            if (std::fabs(p1[0] - p2[0]) > EPS) {
+                const double a = (p1[1] - p2[1]) / (p1[0] - p2[0]);
+                const double c = p1[1] - a * p1[0];
+                xs = (1.0 - c) / (a + 1.0);
+            }
+            if (xs > -EPS && xs < 1.0 + EPS) { s[k][0] = xs; s[k][1] = 1.0 - xs; k++; }
+        }
+        if (k) {
+            int d = 0, j = 0;
+            double dp = p2[0] - p1[0];
+            if (std::fabs(dp) < EPS) { d = 1; dp = p2[1] - p1[1]; }
+            for (int i = 0; i < k; i++) {
+                const double a = (s[i][d] - p1[d]) / dp;
+                if (a < -EPS || a > 1.0 + EPS) continue;
+                s[j][0] = s[i][0];
+                s[j][1] = s[i][1];
+                j++;
+            }
+            k = j;
+        }
+        return k;
+    }
+    const double sx = p1[0], sy = p1[1], sz = p1[2];
+    const double dx = p2[0] - p1[0], dy = p2[1] - p1[1], dz = p2[2] - p1[2];
+    auto keep = [&](double x, double y, double z) { s[k][0] = x; s[k][1] = y; s[k][2] = z; k++; };
+    if (bs[0] && dz != 0.0) {
+        const double a = -sz / dz, rx = sx + a * dx, ry = sy + a * dy;
+        if (rx >= 0 && ry >= 0 && rx + ry <= 1) keep(rx, ry, 0.0);
+    }
+    if (bs[1] && dy != 0.0) {
+        const double a = -sy / dy, rx = sx + a * dx, rz = sz + a * dz;
+        if (rx >= 0 && rz >= 0 && rx + rz <= 1) keep(rx, 0.0, rz);
+    }
+    if (bs[2] && dx != 0.0) {
+        const double a = -sx / dx, ry = sy + a * dy, rz = sz + a * dz;
+        if (ry >= 0 && rz >= 0 && ry + rz <= 1) keep(0.0, ry, rz);
+    }
+    if (bs[3] && (dx + dy + dz) != 0.0) {
+        const double a = (1 - sx - sy - sz) / (dx + dy + dz);
+        const double rx = sx + a * dx, ry = sy + a * dy, rz = sz + a * dz;
+        if (rx >= 0 && ry >= 0 && rx + ry <= 1) keep(rx, ry, rz);
+    }
+    return k;
+}
+
+// Mesh::BndIntersect (mesh.cc:1369-1453): in 3D the line must cross the
+// mesh's bounding box (BoundingBox, mesh.cc:1341-1360, no padding) on one of
+// its faces; then every element with a boundary side intersects it in its
+// local frame (Element::GlobalIntersection, element.cc:505-511), the points
+// are mapped back (Element::Global, element.cc:164-176) and the one nearest
+// p1 (the first of equal distance, element order) is the result.
+static bool bnd_intersect(const MeshHost& m, const double* p1, const double* p2, double* out)
+{
+    const int dim = m.dim, nn = m.nn, nside = dim == 2 ? 3 : 4;
+    if (dim > 2) {
+        const double EPS = 1e-12;
+        double lo[3] = {1e6, 1e6, 1e6}, hi[3] = {-1e6, -1e6, -1e6};
+        for (int k = 0; k < m.n; k++)
+            for (int d = 0; d < 3; d++) {
+                const double v = m.coords[(size_t)k * 3 + d];
+                lo[d] = v < lo[d] ? v : lo[d];
+                hi[d] = v > hi[d] ? v : hi[d];
+            }
+        const double d[3] = {p2[0] - p1[0], p2[1] - p1[1], p2[2] - p1[2]};
+        // the box faces normal to z, then y, then x; (u, v) the other axes
+        static const int AX[3][3] = {{2, 0, 1}, {1, 0, 2}, {0, 1, 2}};
+        bool hit = false;
+        for (int f = 0; f < 3 && !hit; f++) {
+            const int w = AX[f][0], u = AX[f][1], v = AX[f][2];
+            if (d[w] == 0.0) continue;
+            for (int side = 0; side < 2 && !hit; side++) {
+                const double a = ((side ? hi[w] : lo[w]) - p1[w]) / d[w];
+                const double ru = p1[u] + a * d[u], rv = p1[v] + a * d[v];
+                hit = ru > lo[u] - EPS && ru < hi[u] + EPS && rv > lo[v] - EPS && rv < hi[v] + EPS;
+            }
+        }
+        if (!hit) return false;
+    }
+    double dmin = 1e10;
+    bool found = false;
+    for (int e = 0; e < m.ne; e++) {
+        bool any = false;
+        for (int sd = 0; sd < nside; sd++) any |= m.bndside[(size_t)e * nside + sd] != 0;
+        if (!any) continue;
+        const double* g = &m.geo[(size_t)e * 16];
+        double l1[3], l2[3], s[4][3];
+        if (dim == 2) {
+            const double scale = 1.0 / (g[0] + g[1] + g[2]);
+            l1[0] = (g[1] + g[4] * p1[0] + g[7] * p1[1]) * scale;
+            l1[1] = (g[2] + g[5] * p1[0] + g[8] * p1[1]) * scale;
+            l2[0] = (g[1] + g[4] * p2[0] + g[7] * p2[1]) * scale;
+            l2[1] = (g[2] + g[5] * p2[0] + g[8] * p2[1]) * scale;
+        } else {
+            const double *a = g, *b = g + 4, *c = g + 8, *dd = g + 12;
+            const double scale = 1.0 / (a[0] + a[1] + a[2] + a[3]);
+            for (int r = 0; r < 3; r++) {
+                l1[r] = (a[r + 1] + b[r + 1] * p1[0] + c[r + 1] * p1[1] + dd[r + 1] * p1[2]) * scale;
+                l2[r] = (a[r + 1] + b[r + 1] * p2[0] + c[r + 1] * p2[1] + dd[r + 1] * p2[2]) * scale;
+            }
+        }
+        const int k = side_intersections(m, e, l1, l2, s);
+        const int* nd = &m.el[(size_t)e * nn];
+        for (int j = 0; j < k; j++) {
+            double u[4], glob[3];
+            u[0] = dim == 2 ? 1.0 - s[j][0] - s[j][1] : 1.0 - s[j][0] - s[j][1] - s[j][2];
+            for (int r = 0; r < dim; r++) u[r + 1] = s[j][r];
+            for (int c = 0; c < dim; c++) {
+                glob[c] = 0.0;
+                for (int i = 0; i < nn; i++) glob[c] += u[i] * m.coords[(size_t)nd[i] * dim + c];
+            }
+            const double dst = dist(p1, glob, dim);
+            if (dst < dmin) {
+                dmin = dst;
+                for (int c = 0; c < dim; c++) out[c] = glob[c];
+                found = true;
+            }
+        }
+    }
+    return found;
+}
+
+// qmmesh.cc:378-391: n = the normal read (or -q), scaled by the reciprocal of
+// its length (TVector::operator/=, vector_imp.hpp:672-677); the start point
+// q + |q| n; lengths are plain roots of sums of squares (l2norm,
+// vector_imp.hpp:1117-1120, 1290-1298)
+int qm_external_source(const MeshHost& m, const double* q, const double* nrm, double* out)
+{
+    const int dim = m.dim;
+    double n[3], s = 0.0, sq = 0.0, p1[3];
+    for (int c = 0; c < dim; c++) n[c] = nrm ? nrm[c] : -q[c];
+    for (int c = 0; c < dim; c++) s += std::fabs(n[c]) * std::fabs(n[c]);
+    if (nrm && !(std::sqrt(s) > 0.0)) return 2;
+    const double inv = 1.0 / std::sqrt(s);
+    for (int c = 0; c < dim; c++) n[c] *= inv;
+    for (int c = 0; c < dim; c++) sq += std::fabs(q[c]) * std::fabs(q[c]);
+    const double len = std::sqrt(sq);
+    for (int c = 0; c < dim; c++) p1[c] = q[c] + len * n[c];
+    return bnd_intersect(m, p1, q, out) ? 0 : 1;
 }
 
 bool qm_place_detector(const MeshHost& m, bool fixed, double* p)

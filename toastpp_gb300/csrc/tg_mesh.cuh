@@ -112,5 +112,10 @@ bool el_gcontains(const MeshHost& m, int e, const double* p);
 // or nudged into an element; else pulled to the boundary); false if a fixed
 // position lies in no element
 bool qm_place_detector(const MeshHost& m, bool fixed, double* p);
+// QMMesh::LoadQM's "external" source position: the boundary point that
+// Mesh::BndIntersect finds from q + |q| n towards q, n the unit normal read
+// with the position (nrm) or the unit vector along -q (nrm NULL).  Returns
+// 0, 2 for a zero normal, 1 when no boundary point is found.
+int qm_external_source(const MeshHost& m, const double* q, const double* nrm, double* out);
 
 }  // namespace tg

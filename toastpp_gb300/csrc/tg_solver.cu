@@ -2429,10 +2429,13 @@ int tg_mesh_destroy(tg_mesh mesh)
 
 // QMMesh::LoadQM (src/libfe/qmmesh.cc:319-460) with InitM's detector
 // placement (105-147): the header "QM file", "Dimension d" (the mesh's), a
-// SourceList and a MeasurementList (count, optional "fixed" / "external" and
-// normal flags, then one line per position, normals parsed and dropped) and a
-// LinkList ("count: detector ..." per source).  Detector positions of a
-// non-fixed list are pulled to the boundary.
+// SourceList and a MeasurementList (count, optional "fixed" / "external" flag
+// and normals flag, then one line per position with an optional normal) and
+// a LinkList ("count: detector ..." per source).  Detector positions of a
+// list that is neither fixed nor external are pulled to the boundary.  An
+// "external" source list moves each source to the boundary along its normal
+// (or along -q when the normals flag is "default"); an "external"
+// measurement list is kept as read (LoadQM then skips InitM).
 struct tg_qm_s {
     int dim = 0, nq = 0, nm = 0;
     std::vector<double> Q, M;
@@ -2441,8 +2444,16 @@ struct tg_qm_s {
 
 namespace {
 
-// the section header line starting with tag, its count and flags
-void qm_section(std::istream& is, const char* tag, int& count, bool& fixed)
+struct QMList {
+    int count = 0;
+    bool fixed = false, external = false;
+    // normals are "specified" unless the third header token is "default"
+    // (qmmesh.cc:345, 406)
+    bool normals = true;
+};
+
+// the section header line starting with tag: its count and flags
+QMList qm_section(std::istream& is, const char* tag)
 {
     std::string line;
     const size_t tl = strlen(tag);
@@ -2454,27 +2465,36 @@ void qm_section(std::istream& is, const char* tag, int& count, bool& fixed)
         }
     TG_CHECK(ok, TG_ERR_ARG, std::string("QM file: ") + tag + " not found");
     std::istringstream h(line.substr(tl));
-    TG_CHECK(bool(h >> count) && count >= 0, TG_ERR_ARG, std::string("QM file: no count after ") + tag);
-    std::string flag;
-    fixed = false;
-    if (h >> flag) {
-        std::string f = flag;
+    QMList L;
+    TG_CHECK(bool(h >> L.count) && L.count >= 0, TG_ERR_ARG, std::string("QM file: no count after ") + tag);
+    auto lower = [](std::string f) {
         for (auto& c : f) c = (char)tolower((unsigned char)c);
-        TG_CHECK(f != "external", TG_ERR_UNSUPPORTED, "QM file: external positions are not supported");
-        fixed = f == "fixed";
+        return f;
+    };
+    std::string flag, nflag;
+    if (h >> flag) {
+        flag = lower(flag);
+        L.fixed = flag == "fixed";
+        L.external = flag == "external";
+        if (h >> nflag) L.normals = lower(nflag) != "default";
     }
+    return L;
 }
 
-void qm_positions(std::istream& is, int count, int dim, std::vector<double>& out, const char* what)
+// count position lines: dim coordinates, then up to dim normal components
+// (zero where absent)
+void qm_positions(std::istream& is, int count, int dim, std::vector<double>& out, std::vector<double>& nrm,
+                  const char* what)
 {
     std::string line;
     for (int i = 0; i < count; i++) {
         TG_CHECK(bool(std::getline(is, line)), TG_ERR_ARG, std::string("QM file: truncated ") + what);
-        double v[6];
+        double v[6] = {0, 0, 0, 0, 0, 0};
         const int k = dim == 2 ? sscanf(line.c_str(), "%lf%lf%lf%lf", v, v + 1, v + 2, v + 3)
                                : sscanf(line.c_str(), "%lf%lf%lf%lf%lf%lf", v, v + 1, v + 2, v + 3, v + 4, v + 5);
         TG_CHECK(k >= dim, TG_ERR_ARG, std::string("QM file: parse error in the ") + what);
         out.insert(out.end(), v, v + dim);
+        nrm.insert(nrm.end(), v + dim, v + 2 * dim);
     }
 }
 
@@ -2498,11 +2518,28 @@ int tg_qm_load(tg_mesh mesh, const char* path, tg_qm* out)
     TG_CHECK(dim == m.dim, TG_ERR_ARG, "QM dimension does not match mesh");
     std::unique_ptr<tg_qm_s> q(new tg_qm_s);
     q->dim = dim;
-    bool qfixed = false, mfixed = false;
-    qm_section(is, "SourceList", q->nq, qfixed);
-    qm_positions(is, q->nq, dim, q->Q, "source list");
-    qm_section(is, "MeasurementList", q->nm, mfixed);
-    qm_positions(is, q->nm, dim, q->M, "measurement list");
+    std::vector<double> QN, MN;
+    const QMList ql = qm_section(is, "SourceList");
+    q->nq = ql.count;
+    qm_positions(is, q->nq, dim, q->Q, QN, "source list");
+    if (ql.external)
+        for (int i = 0; i < q->nq; i++) {
+            double p[3];
+            const int rc = qm_external_source(m, &q->Q[(size_t)i * dim], ql.normals ? &QN[(size_t)i * dim] : nullptr, p);
+            TG_CHECK(rc != 2, TG_ERR_ARG, "QM file: no normal given for external source " + std::to_string(i));
+            TG_CHECK(rc == 0, TG_ERR_ARG,
+                     "QM file: no boundary point found along the normal of external source " + std::to_string(i));
+            std::copy(p, p + dim, &q->Q[(size_t)i * dim]);
+        }
+    const QMList ml = qm_section(is, "MeasurementList");
+    q->nm = ml.count;
+    qm_positions(is, q->nm, dim, q->M, MN, "measurement list");
+    if (ml.external && ml.normals)
+        for (int i = 0; i < q->nm; i++) {
+            double s = 0.0;
+            for (int c = 0; c < dim; c++) s += MN[(size_t)i * dim + c] * MN[(size_t)i * dim + c];
+            TG_CHECK(std::sqrt(s) > 0.0, TG_ERR_ARG, "QM file: no normal given for external measurement " + std::to_string(i));
+        }
     bool ok = false;
     while (std::getline(is, line))
         if (line.compare(0, 8, "LinkList") == 0) {
@@ -2524,9 +2561,10 @@ int tg_qm_load(tg_mesh mesh, const char* path, tg_qm* out)
         }
         q->ofs.push_back((int)q->lm.size());
     }
-    for (int i = 0; i < q->nm; i++)
-        TG_CHECK(qm_place_detector(m, mfixed, &q->M[(size_t)i * dim]), TG_ERR_ARG,
-                 "QM file: no element found to place measurement " + std::to_string(i));
+    if (!ml.external)
+        for (int i = 0; i < q->nm; i++)
+            TG_CHECK(qm_place_detector(m, ml.fixed, &q->M[(size_t)i * dim]), TG_ERR_ARG,
+                     "QM file: no element found to place measurement " + std::to_string(i));
     *out = q.release();
     API_END
 }

@@ -30,6 +30,17 @@ class QMSpec:
     link_m: np.ndarray       # nQM int32, detector index per measurement (QMref)
     q_fixed: bool = False
     m_fixed: bool = False
+    # "external" lists (qmmesh.cc:343-344, 404-405): sources are moved to the
+    # boundary along their normals when the mesh is attached, detectors stay
+    # where they were read.  QN / MN hold the normals read with the positions
+    # (zero where a line has none); *_default_normals is the "default" flag
+    # (the direction -q instead of the normal read)
+    q_external: bool = False
+    m_external: bool = False
+    QN: np.ndarray | None = None
+    MN: np.ndarray | None = None
+    q_default_normals: bool = False
+    m_default_normals: bool = False
 
     @property
     def nQ(self) -> int:
@@ -107,18 +118,22 @@ def read_qm(path: str) -> QMSpec:
         nonlocal i
         while not lines[i].startswith(tag):
             i += 1
-        hdr = lines[i].split()
-        cnt = int(hdr[1])
-        fixed = len(hdr) > 2 and hdr[2].lower() == "fixed"
-        pts = []
+        hdr = lines[i][len(tag):].split()
+        cnt = int(hdr[0])
+        flag = hdr[1].lower() if len(hdr) > 1 else ""
+        # normals are "specified" unless a third token says "default"
+        default_normals = len(hdr) > 2 and hdr[2].lower() == "default"
+        pts, nrm = [], []
         for k in range(cnt):
-            vals = [float(v) for v in lines[i + 1 + k].split()]
+            vals = [float(v) for v in lines[i + 1 + k].split()[:2 * dim]]
             pts.append(vals[:dim])
+            nrm.append((vals[dim:] + [0.0] * dim)[:dim])
         i += 1 + cnt
-        return np.asarray(pts, float), fixed
+        return (np.asarray(pts, float).reshape(-1, dim), np.asarray(nrm, float).reshape(-1, dim), flag,
+                default_normals)
 
-    Q, qf = section("SourceList")
-    M, mf = section("MeasurementList")
+    Q, QN, qflag, qdef = section("SourceList")
+    M, MN, mflag, mdef = section("MeasurementList")
     while not lines[i].startswith("LinkList"):
         i += 1
     rest = " ".join(lines[i + 1:])
@@ -132,7 +147,8 @@ def read_qm(path: str) -> QMSpec:
         lm.extend(int(t) for t in toks[:cnt])
         rest = toks[cnt] if len(toks) > cnt else ""
         ofs.append(ofs[-1] + cnt)
-    return QMSpec(Q, M, np.asarray(ofs, np.int32), np.asarray(lm, np.int32), qf, mf)
+    return QMSpec(Q, M, np.asarray(ofs, np.int32), np.asarray(lm, np.int32), qflag == "fixed", mflag == "fixed",
+                  qflag == "external", mflag == "external", QN, MN, qdef, mdef)
 
 
 def write_qm(path: str, qm: QMSpec) -> None:
