@@ -85,12 +85,18 @@ def lib():
         L.tor_assemble_el.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, C.c_int, _dp]
         L.tor_jacobian_el.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int, C.c_int, _dp]
         L.tor_gradient_weights.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp]
-        L.tor_gradient_grid.argtypes = [C.c_void_p, _ip, C.c_int, _dp, _dp, _dp]
+        L.tor_gradient_grid.argtypes = [C.c_void_p, _ip, _ip, C.c_int, _dp, _dp, _dp]
+        L.tor_linpix_map.restype = C.c_int
+        L.tor_linpix_map.argtypes = [C.c_int, _ip, _ip, _ip, C.c_int, _ip, C.c_void_p, C.c_void_p]
+        L.tor_basis_support.restype = C.c_int
+        L.tor_basis_support.argtypes = [C.c_int, _ip, _ip, _ip, _ip]
+        L.tor_csr_ab.restype = C.c_int
+        L.tor_csr_ab.argtypes = [C.c_int, C.c_int, _ip, _ip, _dp, _ip, _ip, _dp, _ip, C.c_void_p, C.c_void_p]
         L.tor_node_map.argtypes = [C.c_void_p, _ip, _dp, _dp, _ip, _ip, _ip, _dp]
         L.tor_raster_pixel.restype = C.c_int
         L.tor_raster_pixel.argtypes = [C.c_void_p, _ip, _dp, _dp, _ip, _ip, _ip, _dp]
         L.tor_jacobian_grid.restype = C.c_int
-        L.tor_jacobian_grid.argtypes = [C.c_void_p, _ip, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int,
+        L.tor_jacobian_grid.argtypes = [C.c_void_p, _ip, _ip, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int,
                                         C.c_int, _dp]
         _lib = L
     return _lib
@@ -411,11 +417,13 @@ def jacobian_el(mesh: Mesh, dphi, aphi, proj_lin, link_ofs, link_m, logscale=Tru
 
 
 def data_gradient(mesh: Mesh, bdim, sysval, dphi, mvec, proj_lin, proj_log, link_ofs, link_m, data, sd,
-                  method="BICGSTAB", precon="ICH", tol=1e-15):
-    """toast's Gradient on Raster_Pixel(bdim, bdim) given the fields: weights,
-    one adjoint solve per source with the weighted detector vectors, then the
-    grid products (src/python/toastmodule.cc:1745-1843).  Returns 2 slen."""
+                  method="BICGSTAB", precon="ICH", tol=1e-15, gdim=None):
+    """toast's Gradient on Raster_Pixel(bdim, gdim) (gdim None: bdim) given
+    the fields: weights, one adjoint solve per source with the weighted
+    detector vectors, then the grid products mapped to the solution basis
+    (src/python/toastmodule.cc:1745-1843).  Returns 2 slen."""
     bdim = np.ascontiguousarray(bdim, np.int32)
+    gdim = bdim if gdim is None else np.ascontiguousarray(gdim, np.int32)
     nq, n = dphi.shape
     W = np.zeros((nq, n), np.complex128)
     lib().tor_gradient_weights(nq, n, _cview(np.asarray(mvec, np.complex128)).ravel(), _cview(proj_lin).ravel(),
@@ -423,9 +431,9 @@ def data_gradient(mesh: Mesh, bdim, sysval, dphi, mvec, proj_lin, proj_log, link
                                np.ascontiguousarray(sd, np.float64), np.ascontiguousarray(link_ofs, np.int32),
                                np.ascontiguousarray(link_m, np.int32), W.view(np.float64).reshape(-1))
     wphi, _, _ = solve(mesh.rowptr, mesh.colidx, sysval, W, method, precon, tol)
-    slen = int((raster_pixel(mesh, bdim).elref >= 0).sum())
+    slen = len(raster_support(mesh, bdim, gdim))
     grad = np.zeros(2 * slen)
-    lib().tor_gradient_grid(mesh._h, bdim, nq, _cview(dphi).ravel(), _cview(wphi).ravel(), grad)
+    lib().tor_gradient_grid(mesh._h, bdim, gdim, nq, _cview(dphi).ravel(), _cview(wphi).ravel(), grad)
     return grad
 
 
@@ -460,6 +468,50 @@ def raster_pixel(mesh: Mesh, bdim) -> RasterPixel:
     return RasterPixel(bdim, bbmin, bbmax, elref, rp, col[:rp[-1]].copy(), val[:rp[-1]].copy())
 
 
+def raster_support(mesh: Mesh, bdim, gdim=None) -> np.ndarray:
+    """The solution points of Raster_Pixel(bdim, gdim) as basis indices:
+    without an intermediate grid the grid points inside the mesh; with one,
+    the basis points whose subsampled support is positive (raster.cc:55-77)."""
+    bdim = np.ascontiguousarray(bdim, np.int32)
+    if gdim is None or np.array_equal(np.asarray(gdim), bdim):
+        return raster_pixel(mesh, bdim).sol
+    gdim = np.ascontiguousarray(gdim, np.int32)
+    elref = raster_pixel(mesh, gdim).elref
+    out = np.zeros(int(np.prod(bdim)), np.int32)
+    slen = lib().tor_basis_support(mesh.dim, gdim, bdim, elref, out)
+    return out[:slen].copy()
+
+
+def linpix_map(dim, gdim, bdim, elref, by_grid):
+    """Grid2LinPixMatrix (by_grid False: basis x grid, rows normalised) or
+    LinPix2GridMatrix (True: grid x basis) as CSR (rowptr, col, val)."""
+    gdim = np.ascontiguousarray(gdim, np.int32)
+    bdim = np.ascontiguousarray(bdim, np.int32)
+    elref = np.ascontiguousarray(elref, np.int32)
+    rows = int(np.prod(gdim if by_grid else bdim))
+    rp = np.zeros(rows + 1, np.int32)
+    nz = lib().tor_linpix_map(dim, gdim, bdim, elref, int(by_grid), rp, None, None)
+    col = np.zeros(max(nz, 1), np.int32)
+    val = np.zeros(max(nz, 1))
+    nz = lib().tor_linpix_map(dim, gdim, bdim, elref, int(by_grid), rp, col.ctypes.data_as(C.c_void_p),
+                              val.ctypes.data_as(C.c_void_p))
+    return rp, col[:nz].copy(), val[:nz].copy()
+
+
+def csr_ab(a, b, nc):
+    """TCompRowMatrix::AB then Shrink of CSR triples a (nr x k) and b (k x nc)."""
+    arp, acol, aval = (np.ascontiguousarray(x) for x in a)
+    brp, bcol, bval = (np.ascontiguousarray(x) for x in b)
+    nr = len(arp) - 1
+    crp = np.zeros(nr + 1, np.int32)
+    cap = lib().tor_csr_ab(nr, nc, arp, acol, aval, brp, bcol, bval, crp, None, None)
+    ccol = np.zeros(max(cap, 1), np.int32)
+    cval = np.zeros(max(cap, 1))
+    nz = lib().tor_csr_ab(nr, nc, arp, acol, aval, brp, bcol, bval, crp, ccol.ctypes.data_as(C.c_void_p),
+                          cval.ctypes.data_as(C.c_void_p))
+    return crp, ccol[:nz].copy(), cval[:nz].copy()
+
+
 def _csr_apply(rp, col, val, x):
     """y = A x row by row in entry order from 0 (RCompRowMatrix::Ax)."""
     y = np.zeros(len(rp) - 1)
@@ -492,18 +544,83 @@ def raster_maps(mesh: Mesh, bdim, f_mesh, s_sol):
     return m2g, m2s, s2m, g2m
 
 
-def jacobian_grid(mesh: Mesh, bdim, dphi, aphi, proj_lin, link_ofs, link_m, logscale=True):
-    """Grid-basis Jacobian for Raster_Pixel(bdim, bdim): complex (2 nQM) x
-    (2 slen), real (2 nQM) x slen."""
+def _csr_apply_c(rp, col, val, x):
+    """RCompRowMatrix::Ax_cplx: real matrix, complex vector, the real and
+    imaginary sums kept apart (crmatrix_imp.hpp:1302-1327)."""
+    x = np.asarray(x, np.complex128)
+    return _csr_apply(rp, col, val, x.real) + 1j * _csr_apply(rp, col, val, x.imag)
+
+
+def raster_basis_maps(mesh: Mesh, bdim, gdim, mua, mus):
+    """Maps of Raster_Pixel(bdim, gdim) through its basis (toast.Raster.Map,
+    MapBasis src/python/toastmodule.cc:718-790; raster.cc:188-408,
+    raster_px.cc:10-176), on the vectors the reference driver maps: real
+    M->B (C = G B), B->M (CI = BI GI) of b + 1, G->B of the grid image of
+    mua, B->G (GI) of b + 1, G->S, S->G (GI of the scatter) of s + 1, and the
+    complex M->S (G after B, then the support) of mua + i mus and S->M (GI
+    then BI) of (s + 1) - 0.5 i s.  Also the solution points (sol2basis)."""
+    bdim = np.ascontiguousarray(bdim, np.int32)
+    gdim = np.ascontiguousarray(gdim, np.int32)
+    r = raster_pixel(mesh, gdim)
+    glen, blen, n = len(r.elref), int(np.prod(bdim)), mesh.n
+    nn = 1 << mesh.dim
+    nrp = np.zeros(n + 1, np.int32)
+    ncol = np.zeros(n * nn, np.int32)
+    nval = np.zeros(n * nn)
+    lib().tor_node_map(mesh._h, gdim, r.bbmin, r.bbmax, r.elref, nrp, ncol, nval)
+    BI = (nrp, ncol[:nrp[-1]].copy(), nval[:nrp[-1]].copy())
+    B = (r.browptr, r.bcol, r.bval)
+    G = linpix_map(mesh.dim, gdim, bdim, r.elref, False)
+    GI = linpix_map(mesh.dim, gdim, bdim, r.elref, True)
+    Cm = csr_ab(G, B, n)
+    CI = csr_ab(BI, GI, blen)
+    sol = raster_support(mesh, bdim, gdim)
+    slen = len(sol)
+    D = (np.arange(slen + 1, dtype=np.int32), sol, np.ones(slen))
+
+    def DT(s):  # D->ATx: 0 + 1 s at the solution points
+        b = np.zeros(blen)
+        b[sol] += 1.0 * np.asarray(s)
+        return b
+
+    bvec = np.arange(1, blen + 1, dtype=float)
+    svec = np.arange(1, slen + 1, dtype=float)
+    m2g = _csr_apply(*B, mua)
+    out = dict(sol2basis=sol,
+               m2b=_csr_apply(*Cm, mua),
+               b2m=_csr_apply(*CI, bvec),
+               g2b=_csr_apply(*G, m2g),
+               b2g=_csr_apply(*GI, bvec),
+               g2s=_csr_apply(*D, _csr_apply(*G, m2g)),
+               s2g=_csr_apply(*GI, DT(svec)),
+               m2s=_csr_apply(*D, _csr_apply(*Cm, mua)),
+               s2m=_csr_apply(*CI, DT(svec)))
+    cm = np.asarray(mua) + 1j * np.asarray(mus)
+    cb = _csr_apply_c(*G, _csr_apply_c(*B, cm))
+    out["cm2s"] = cb if slen == blen else cb[sol]
+    cs = np.arange(1, slen + 1) - 0.5j * np.arange(slen)
+    if slen == blen:
+        cbs = cs
+    else:
+        cbs = np.zeros(blen, np.complex128)
+        cbs[sol] = cs
+    out["cs2m"] = _csr_apply_c(*BI, _csr_apply_c(*GI, cbs))
+    return out
+
+
+def jacobian_grid(mesh: Mesh, bdim, dphi, aphi, proj_lin, link_ofs, link_m, logscale=True, gdim=None):
+    """Grid-basis Jacobian for Raster_Pixel(bdim, gdim) (gdim None: bdim):
+    complex (2 nQM) x (2 slen), real (2 nQM) x slen."""
     cplx = np.iscomplexobj(dphi)
     bdim = np.ascontiguousarray(bdim, np.int32)
+    gdim = bdim if gdim is None else np.ascontiguousarray(gdim, np.int32)
     nq, n = dphi.shape
     nm = aphi.shape[0]
     nqm = int(link_ofs[-1])
-    slen = int((raster_pixel(mesh, bdim).elref >= 0).sum())
+    slen = len(raster_support(mesh, bdim, gdim))
     J = np.zeros((2 * nqm, 2 * slen) if cplx else (2 * nqm, slen))
     f = (lambda a: _cview(a).ravel()) if cplx else (lambda a: np.ascontiguousarray(a, np.float64).ravel())
-    lib().tor_jacobian_grid(mesh._h, bdim, nq, nm, f(dphi), f(aphi), f(proj_lin),
+    lib().tor_jacobian_grid(mesh._h, bdim, gdim, nq, nm, f(dphi), f(aphi), f(proj_lin),
                             np.ascontiguousarray(link_ofs, np.int32), np.ascontiguousarray(link_m, np.int32),
                             int(cplx), int(logscale), J.reshape(-1))
     return J

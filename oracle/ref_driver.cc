@@ -29,10 +29,13 @@
 //              Gradient (GetGradient / AddDataGradient,
 //              src/python/toastmodule.cc:1745-1887) on the raster, run as that
 //              code runs it with this library's calls: PREFIX_grad.bin
-// grid       : also the grid-basis Jacobian for Raster_Pixel(bdim = gdim =
-//              grid) (src/python/toastmodule.cc:696, raster_px.cc:10-48),
+// grid       : also the grid-basis Jacobian for Raster_Pixel(bdim = grid,
+//              gdim) (src/python/toastmodule.cc:696, raster_px.cc:10-48),
 //              LOG data, written with the raster's element reference per grid
-//              point (PREFIX_Jgrid.bin, PREFIX_elref.bin).
+//              point (PREFIX_Jgrid.bin, PREFIX_elref.bin).  gdim=NX,NY[,NZ]
+//              gives the intermediate grid (default: the basis grid); with
+//              it the solution points' basis indices (PREFIX_sol2basis.bin)
+//              and the maps through the basis are written too.
 // qmdump     : with qm, write what QMMesh::LoadQM (qmmesh.cc:319-460, with
 //              InitM's detector placement) made of the file and stop:
 //              PREFIX_qpos.bin, PREFIX_mpos.bin (nQ / nM x dim doubles),
@@ -118,6 +121,44 @@ static void write_maps(Raster& raster, const RVector& mua, const string& out)
     wbin(out + "_s2m.bin", m.data_buffer(), n * sizeof(double));
     raster.Map_GridToMesh(g, m);
     wbin(out + "_g2m.bin", m.data_buffer(), n * sizeof(double));
+}
+
+// With an intermediate grid (gdim != bdim): the maps through the basis
+// (toast.Raster.Map "M->B", "B->M", "G->B", "B->G", "G->S", "S->G", and the
+// complex "M->S" / "S->M", which the pixel raster runs through the grid,
+// raster.cc:236-270, 374-408): PREFIX_m2b, _b2m (basis vector b + 1 at basis
+// point b), _g2b (of the grid image of mua), _b2g, _g2s, _s2g (s + 1), and
+// _cm2s, _cs2m (mua + i mus'-like second field, interleaved complex)
+static void write_basis_maps(Raster& raster, const RVector& mua, const RVector& mus, const string& out)
+{
+    const int glen = raster.GLen(), blen = raster.BLen(), slen = raster.SLen(), n = mua.Dim();
+    RVector g(glen), b(blen), m(n), sv(slen), bin(blen), sin(slen);
+    raster.Map_MeshToBasis(mua, b);
+    wbin(out + "_m2b.bin", b.data_buffer(), blen * sizeof(double));
+    for (int i = 0; i < blen; i++) bin[i] = i + 1.0;
+    raster.Map_BasisToMesh(bin, m);
+    wbin(out + "_b2m.bin", m.data_buffer(), n * sizeof(double));
+    raster.Map_MeshToGrid(mua, g);
+    raster.Map_GridToBasis(g, b);
+    wbin(out + "_g2b.bin", b.data_buffer(), blen * sizeof(double));
+    raster.Map_BasisToGrid(bin, g);
+    wbin(out + "_b2g.bin", g.data_buffer(), glen * sizeof(double));
+    raster.Map_MeshToGrid(mua, g);
+    raster.Map_GridToSol(g, sv);
+    wbin(out + "_g2s.bin", sv.data_buffer(), slen * sizeof(double));
+    for (int i = 0; i < slen; i++) sin[i] = i + 1.0;
+    raster.Map_SolToGrid(sin, g);
+    wbin(out + "_s2g.bin", g.data_buffer(), glen * sizeof(double));
+    CVector cm(n), cs(slen), cmo(n);
+    for (int i = 0; i < n; i++) cm[i] = std::complex<double>(mua[i], mus[i]);
+    raster.Map_MeshToSol(cm, cs);
+    wbin(out + "_cm2s.bin", (const double*)cs.data_buffer(), slen * 2 * sizeof(double));
+    for (int i = 0; i < slen; i++) cs[i] = std::complex<double>(i + 1.0, -0.5 * i);
+    raster.Map_SolToMesh(cs, cmo);
+    wbin(out + "_cs2m.bin", (const double*)cmo.data_buffer(), n * 2 * sizeof(double));
+    std::vector<int> s2b(slen);
+    for (int i = 0; i < slen; i++) s2b[i] = raster.Sol2Basis(i);
+    wbin(out + "_sol2basis.bin", s2b.data(), slen * sizeof(int));
 }
 
 // The data gradient on a raster, in the sequence of toast's GetGradient /
@@ -206,6 +247,16 @@ int main(int argc, char** argv) {
         }
     }
     int msub = atoi(arg("msub", "0").c_str());
+    std::vector<int> igrid;  // intermediate grid; empty: the basis grid
+    {
+        string g = arg("gdim", "");
+        for (size_t a = 0; a < g.size();) {
+            size_t b = g.find(',', a);
+            if (b == string::npos) b = g.size();
+            igrid.push_back(atoi(g.substr(a, b - a).c_str()));
+            a = b + 1;
+        }
+    }
 
     Task_Init(nth);
     toastVerbosity = 0;
@@ -351,7 +402,8 @@ int main(int argc, char** argv) {
             }
             if ((int)grid.size() == dim) {
                 IVector bdim(dim, grid.data());
-                Raster_Pixel raster(bdim, bdim, &mesh);
+                IVector gdim(dim, ((int)igrid.size() == dim ? igrid : grid).data());
+                Raster_Pixel raster(bdim, gdim, &mesh);
                 int slen = raster.SLen(), glen = raster.GLen();
                 RDenseMatrix Jg(2 * nQM, 2 * slen);
                 GenerateJacobian(&raster, &mesh, dphi, aphi, &proj, DATA_LOG, Jg);
@@ -359,6 +411,7 @@ int main(int argc, char** argv) {
                 wbin(out + "_elref.bin", raster.Elref(), (size_t)glen * sizeof(int));
                 fprintf(info, "slen %d\nglen %d\n", slen, glen);
                 write_maps(raster, mua, out);
+                if ((int)igrid.size() == dim) write_basis_maps(raster, mua, mus, out);
                 if (g_args.count("data")) {
                     std::vector<char> db = rbin(arg("data", "")), sb = rbin(arg("sd", ""));
                     RVector data(2 * nQM, (double*)db.data()), sd(2 * nQM, (double*)sb.data());
@@ -438,7 +491,8 @@ int main(int argc, char** argv) {
             }
             if ((int)grid.size() == dim) {
                 IVector bdim(dim, grid.data());
-                Raster_Pixel raster(bdim, bdim, &mesh);
+                IVector gdim(dim, ((int)igrid.size() == dim ? igrid : grid).data());
+                Raster_Pixel raster(bdim, gdim, &mesh);
                 int slen = raster.SLen(), glen = raster.GLen();
                 RDenseMatrix Jmua, Jkap;
                 GenerateJacobian_cw(&raster, &mesh, dphi, aphi, &proj, DATA_LOG, &Jmua, &Jkap);
@@ -449,6 +503,7 @@ int main(int argc, char** argv) {
                 wbin(out + "_elref.bin", raster.Elref(), (size_t)glen * sizeof(int));
                 fprintf(info, "slen %d\nglen %d\n", slen, glen);
                 write_maps(raster, mua, out);
+                if ((int)igrid.size() == dim) write_basis_maps(raster, mua, mus, out);
             }
         }
         if (want_fields) {

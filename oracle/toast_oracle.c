@@ -1662,44 +1662,334 @@ static void grid_map(int glen, const int *browptr, const int *bcol, const double
     }
 }
 
-/* Grid-basis Jacobian for Raster_Pixel with bdim == gdim.
+/* ------------------------------------------------------------------------ */
+/* Raster_Pixel with an intermediate grid (gdim != bdim)                      */
+/* ------------------------------------------------------------------------ */
+
+/* The basis-point / grid-point pairs of the linear pixel basis, in the loop
+   order of Grid2LinPixMatrix (mesh.cc:3138-3320), LinPix2GridMatrix
+   (3540-3640) and SubsampleLinPixel (3047-3136): basis points b in grid
+   order (x fastest); for each, the fine grid points of its window
+   [floor(x0 (g-1)), ceil(x1 (g-1))] per axis (z, then y, then x), kept where
+   the distance to the basis point in basis spacings is below 1 along every
+   axis and (elref given) the point lies in the mesh, with the weight
+   t = (1 - dx)(1 - dy)(1 - dz).  Window points past the grid's last index
+   (a window end rounded up from 1 + ulp) are skipped: the reference skips
+   them too, by the distance test.  fn(ctx, b, g, t) per pair. */
+typedef void (*linpix_fn)(void *ctx, int b, int g, double t);
+
+static void linpix_pairs(int dim, const int *gdim, const int *bdim, const int *elref, linpix_fn fn, void *ctx)
+{
+    const int gx = gdim[0], gy = gdim[1], gz = dim > 2 ? gdim[2] : 1;
+    const int bx = bdim[0], by = bdim[1], bz = dim > 2 ? bdim[2] : 1;
+    const double nbx = bx - 1.0, nby = by - 1.0, nbz = bz - 1.0;
+    const double dbx = 1.0 / nbx, dby = 1.0 / nby, dgx = 1.0 / (gx - 1.0), dgy = 1.0 / (gy - 1.0);
+    double dbz = 0.0, dgz = 0.0, z = 0.0;
+    if (bz > 1) { dbz = 1.0 / nbz; dgz = 1.0 / (gz - 1.0); }
+    int gz0 = 0, gz1 = 0;
+    for (int iz = 0; iz < bz; iz++) {
+        if (bz > 1) {
+            z = (double)iz * dbz;
+            double z0 = iz ? (iz - 1) * dbz : 0.0, z1 = iz < bz - 1 ? (iz + 1) * dbz : 1.0;
+            gz0 = (int)floor(z0 * (gz - 1));
+            gz1 = (int)ceil(z1 * (gz - 1));
+        }
+        for (int iy = 0; iy < by; iy++) {
+            double y = (double)iy * dby;
+            double y0 = iy ? (iy - 1) * dby : 0.0, y1 = iy < by - 1 ? (iy + 1) * dby : 1.0;
+            int gy0 = (int)floor(y0 * (gy - 1)), gy1 = (int)ceil(y1 * (gy - 1));
+            for (int ix = 0; ix < bx; ix++) {
+                double x = ix * dbx;
+                double x0 = ix ? (ix - 1) * dbx : 0.0, x1 = ix < bx - 1 ? (ix + 1) * dbx : 1.0;
+                int gx0 = (int)floor(x0 * (gx - 1)), gx1 = (int)ceil(x1 * (gx - 1));
+                const int b = ix + (iy + iz * by) * bx;
+                if (bz == 1) {
+                    for (int yy = gy0; yy <= gy1 && yy < gy; yy++) {
+                        double dy = fabs(yy * dgy - y) * nby;
+                        if (dy >= 1.0) continue;
+                        double idy = 1.0 - dy;
+                        for (int xx = gx0; xx <= gx1 && xx < gx; xx++) {
+                            int gidx = xx + yy * gx;
+                            if (elref && elref[gidx] < 0) continue;
+                            double dx = fabs(xx * dgx - x) * nbx;
+                            if (dx >= 1.0) continue;
+                            fn(ctx, b, gidx, (1.0 - dx) * idy);
+                        }
+                    }
+                } else {
+                    for (int zz = gz0; zz <= gz1 && zz < gz; zz++) {
+                        double dz = fabs(zz * dgz - z) * nbz;
+                        if (dz >= 1.0) continue;
+                        double idz = 1.0 - dz;
+                        for (int yy = gy0; yy <= gy1 && yy < gy; yy++) {
+                            double dy = fabs(yy * dgy - y) * nby;
+                            if (dy >= 1.0) continue;
+                            double idyz = (1.0 - dy) * idz;
+                            for (int xx = gx0; xx <= gx1 && xx < gx; xx++) {
+                                int gidx = xx + (yy + zz * gy) * gx;
+                                if (elref && elref[gidx] < 0) continue;
+                                double dx = fabs(xx * dgx - x) * nbx;
+                                if (dx >= 1.0) continue;
+                                fn(ctx, b, gidx, (1.0 - dx) * idyz);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+typedef struct { int *cnt, *rowptr, *col; double *val; int by_grid; } linpix_csr;
+
+static void linpix_count(void *c, int b, int g, double t)
+{
+    linpix_csr *L = c;
+    (void)t;
+    L->cnt[L->by_grid ? g : b]++;
+}
+
+static void linpix_fill(void *c, int b, int g, double t)
+{
+    linpix_csr *L = c;
+    const int r = L->by_grid ? g : b;
+    const int i = L->rowptr[r] + L->cnt[r]++;
+    L->col[i] = L->by_grid ? b : g;
+    L->val[i] = t;
+}
+
+/* TCompRowMatrix::Shrink (crmatrix_imp.hpp:1774-1804): zero entries
+   dropped, order kept.  Returns the new entry count. */
+static int csr_shrink(int rows, int *rowptr, int *col, double *val)
+{
+    int o = 0, r0 = 0;
+    for (int r = 0; r < rows; r++) {
+        const int r1 = rowptr[r + 1];
+        for (int i = r0; i < r1; i++)
+            if (val[i] != 0.0) { col[o] = col[i]; val[o++] = val[i]; }
+        r0 = r1;
+        rowptr[r + 1] = o;
+    }
+    return o;
+}
+
+/* Grid2LinPixMatrix (mesh.cc:3138-3320), shrunk (raster_px.cc:24-25): the
+   blen x glen map grid -> basis, row b the pairs of basis point b with their
+   weights divided by the row's weight sum (0 when it is 0); by_grid: the
+   LinPix2GridMatrix (mesh.cc:3540-3640, raster_px.cc:26-27), glen x blen,
+   row g the weights t of the basis points that take grid point g, basis
+   points ascending, not normalised.  col / val NULL: count only.  Returns
+   the entry count. */
+int tor_linpix_map(int dim, const int *gdim, const int *bdim, const int *elref, int by_grid, int *rowptr, int *col,
+                   double *val)
+{
+    int glen = 1, blen = 1;
+    for (int d = 0; d < dim; d++) { glen *= gdim[d]; blen *= bdim[d]; }
+    const int rows = by_grid ? glen : blen;
+    linpix_csr L = {calloc(rows, sizeof(int)), rowptr, col, val, by_grid};
+    linpix_pairs(dim, gdim, bdim, elref, linpix_count, &L);
+    rowptr[0] = 0;
+    for (int r = 0; r < rows; r++) rowptr[r + 1] = rowptr[r] + L.cnt[r];
+    if (!col) { free(L.cnt); return rowptr[rows]; }
+    memset(L.cnt, 0, sizeof(int) * rows);
+    linpix_pairs(dim, gdim, bdim, elref, linpix_fill, &L);
+    free(L.cnt);
+    if (!by_grid)
+        for (int r = 0; r < rows; r++) {
+            double wgt = 0.0;
+            for (int i = rowptr[r]; i < rowptr[r + 1]; i++) wgt += val[i];
+            for (int i = rowptr[r]; i < rowptr[r + 1]; i++) val[i] = wgt != 0.0 ? val[i] / wgt : 0.0;
+        }
+    return csr_shrink(rows, rowptr, col, val);
+}
+
+typedef struct { const double *gf; double *sum, *wgt; } subsample_ctx;
+
+static void subsample_acc(void *c, int b, int g, double t)
+{
+    subsample_ctx *S = c;
+    S->wgt[b] += t;
+    S->sum[b] += t * S->gf[g];
+}
+
+/* SubsampleLinPixel (mesh.cc:3047-3136) without a mask, as the raster calls
+   it for its support (raster.cc:58-64): bf[b] = sum t gf[g] / sum t over
+   the pairs of basis point b (0 when the weights sum to 0) */
+void tor_subsample_linpixel(int dim, const int *gdim, const int *bdim, const double *gf, double *bf)
+{
+    int blen = 1;
+    for (int d = 0; d < dim; d++) blen *= bdim[d];
+    double *wgt = calloc(blen, sizeof(double));
+    memset(bf, 0, sizeof(double) * blen);
+    subsample_ctx S = {gf, bf, wgt};
+    linpix_pairs(dim, gdim, bdim, NULL, subsample_acc, &S);
+    for (int b = 0; b < blen; b++) bf[b] = wgt[b] != 0.0 ? bf[b] / wgt[b] : 0.0;
+    free(wgt);
+}
+
+/* TCompRowMatrix::AB (crmatrix_imp.hpp:1453-1541) then Shrink: C = A B, each
+   row's entries in the order their columns first appear (A's row in order,
+   then B's rows), each the sum of the products a b in that order.  ccol /
+   cval hold at least the returned count (call once with ccol NULL for the
+   count before shrinking, an upper bound).  Returns the entry count. */
+int tor_csr_ab(int nr, int nc, const int *arp, const int *acol, const double *aval, const int *brp, const int *bcol,
+               const double *bval, int *crp, int *ccol, double *cval)
+{
+    int *pos = malloc(sizeof(int) * (nc > 0 ? nc : 1));
+    for (int j = 0; j < nc; j++) pos[j] = -1;
+    int nz = 0;
+    crp[0] = 0;
+    for (int i = 0; i < nr; i++) {
+        const int r0 = nz;
+        for (int ra = arp[i]; ra < arp[i + 1]; ra++) {
+            const int k = acol[ra];
+            for (int rb = brp[k]; rb < brp[k + 1]; rb++) {
+                const int j = bcol[rb];
+                if (pos[j] >= 0) {
+                    if (ccol) cval[pos[j]] += aval[ra] * bval[rb];
+                } else {
+                    pos[j] = nz;
+                    if (ccol) { ccol[nz] = j; cval[nz] = aval[ra] * bval[rb]; }
+                    nz++;
+                }
+            }
+        }
+        if (ccol)
+            for (int t = r0; t < nz; t++) pos[ccol[t]] = -1;
+        else  /* count pass: clear the marks by walking the row again */
+            for (int ra = arp[i]; ra < arp[i + 1]; ra++)
+                for (int rb = brp[acol[ra]]; rb < brp[acol[ra] + 1]; rb++) pos[bcol[rb]] = -1;
+        crp[i + 1] = nz;
+    }
+    free(pos);
+    return ccol ? csr_shrink(nr, crp, ccol, cval) : nz;
+}
+
+/* The basis side of Raster_Pixel(bdim, gdim) (raster.cc:18-83,
+   raster_px.cc:10-48): support s = 1 at grid points in the mesh, bsupport =
+   SubsampleLinPixel(s), solution points = basis points with bsupport > 0 in
+   basis order.  sol2basis: room for blen.  Returns slen. */
+int tor_basis_support(int dim, const int *gdim, const int *bdim, const int *elref, int *sol2basis)
+{
+    int glen = 1, blen = 1;
+    for (int d = 0; d < dim; d++) { glen *= gdim[d]; blen *= bdim[d]; }
+    double *s = malloc(sizeof(double) * glen), *bs = malloc(sizeof(double) * blen);
+    for (int g = 0; g < glen; g++) s[g] = elref[g] >= 0 ? 1.0 : 0.0;
+    tor_subsample_linpixel(dim, gdim, bdim, s, bs);
+    int slen = 0;
+    for (int b = 0; b < blen; b++)
+        if (bs[b] > 0.0) sol2basis[slen++] = b;
+    free(s); free(bs);
+    return slen;
+}
+
+/* The grid -> solution map of a Raster_Pixel (Map_GridToSol, raster.cc:
+   374-390): with an intermediate grid, G (Grid2LinPixMatrix) applied to the
+   grid vector (RCompRowMatrix::Ax / Ax_cplx, crmatrix_imp.hpp:1173-1190,
+   1302-1327: sums in entry order of val x), then the solution points'
+   basis values; without (G NULL) the grid values at the solution points.
+   The real path's selection is D->Ax (raster_px.cc:147-150), 0 + 1 x. */
+typedef struct {
+    int slen, blen;
+    const int *sol;                   /* grid index (G NULL) or basis index per solution point */
+    const int *grp, *gcol;            /* G: blen x glen, or NULL */
+    const double *gval;
+    zd *tmp;                          /* blen */
+} grid2sol_t;
+
+static void grid_to_sol(const grid2sol_t *M, const zd *x, int cplx, zd *out)
+{
+    const zd *b = x;
+    if (M->grp) {
+        for (int r = 0; r < M->blen; r++) {
+            double re = 0.0, im = 0.0;
+            for (int j = M->grp[r]; j < M->grp[r + 1]; j++) {
+                if (cplx) {
+                    re += creal(x[M->gcol[j]]) * M->gval[j];
+                    im += cimag(x[M->gcol[j]]) * M->gval[j];
+                } else {
+                    re += M->gval[j] * creal(x[M->gcol[j]]);
+                }
+            }
+            M->tmp[r] = re + I * im;
+        }
+        b = M->tmp;
+    }
+    for (int k = 0; k < M->slen; k++) out[k] = cplx ? b[M->sol[k]] : 0.0 + 1.0 * creal(b[M->sol[k]]);
+}
+
+/* the raster's grid -> solution map for basis bdim on grid gdim (equal:
+   no G); allocates into M (free with grid2sol_free) */
+static void grid2sol_init(int dim, const int *bdim, const int *gdim, const int *elref, grid2sol_t *M)
+{
+    int glen = 1, blen = 1, same = 1;
+    for (int d = 0; d < dim; d++) { glen *= gdim[d]; blen *= bdim[d]; same &= gdim[d] == bdim[d]; }
+    int *sol = malloc(sizeof(int) * (same ? glen : blen));
+    M->blen = blen;
+    M->grp = M->gcol = NULL;
+    M->gval = NULL;
+    M->tmp = NULL;
+    if (same) {
+        M->slen = 0;
+        for (int g = 0; g < glen; g++) if (elref[g] >= 0) sol[M->slen++] = g;
+    } else {
+        M->slen = tor_basis_support(dim, gdim, bdim, elref, sol);
+        int *rp = malloc(sizeof(int) * (blen + 1));
+        int nz = tor_linpix_map(dim, gdim, bdim, elref, 0, rp, NULL, NULL);
+        int *col = malloc(sizeof(int) * (nz > 0 ? nz : 1));
+        double *val = malloc(sizeof(double) * (nz > 0 ? nz : 1));
+        tor_linpix_map(dim, gdim, bdim, elref, 0, rp, col, val);
+        M->grp = rp; M->gcol = col; M->gval = val;
+        M->tmp = malloc(sizeof(zd) * blen);
+    }
+    M->sol = sol;
+}
+
+static void grid2sol_free(grid2sol_t *M)
+{
+    free((void *)M->sol); free((void *)M->grp); free((void *)M->gcol); free((void *)M->gval); free(M->tmp);
+}
+
+/* Grid-basis Jacobian for Raster_Pixel(bdim, gdim): the fields mapped on the
+   grid gdim (Map_MeshToGrid), their image gradients on it, the PMDFs per
+   grid point, then Map_GridToSol into the solution basis.
    Complex (GenerateJacobian_grid with projections, jacobian.cc:289-373):
    PMDF_mua = -(f a), PMDF_kap = -sum_d grad_d f grad_d a (jacobian.cc:58-72),
-   both gradients masked by elref; LOG divides by y (PMDF_log, 76-79); the
-   solution points are the grid points with elref >= 0 in grid order
-   (raster.cc:66-77, Map_BasisToSol 305-315); J(l, s) = Re, J(l+nQM, s) = Im,
-   kappa at column slen + s; then J *= prod gsize/(bdim-1).
+   both gradients masked by elref; LOG divides by y (PMDF_log, 76-79) before
+   the map; J(l, s) = Re, J(l+nQM, s) = Im, kappa at column slen + s; then
+   J *= prod gsize/(bdim-1).
    Real (GenerateJacobian_cw_grid, jacobian.cc:516-712, the threaded engine):
    the adjoint gradient is NOT masked; Jmua = PMDF_mua, Jkap = PMDF_kap (rows
-   nQM + l), times the voxel scale, then, for LOG data, each row times 1/y
-   (GenerateJacobian_cw, 178-193).
+   nQM + l) mapped, times the voxel scale, then, for LOG data, each row times
+   1/y (GenerateJacobian_cw, 178-193).
    J: complex (2 nQM) x (2 slen), real (2 nQM) x slen.  Returns slen. */
-int tor_jacobian_grid(const tor_mesh *m, const int *bdim, int nq, int nm, const double *dphi, const double *aphi,
-                      const double *proj, const int *link_ofs, const int *link_m, int cplx, int logscale,
-                      double *J)
+int tor_jacobian_grid(const tor_mesh *m, const int *bdim, const int *gdim, int nq, int nm, const double *dphi,
+                      const double *aphi, const double *proj, const int *link_ofs, const int *link_m, int cplx,
+                      int logscale, double *J)
 {
     const int dim = m->dim, nn = m->nn, n = m->n;
     int glen = 1;
-    for (int d = 0; d < dim; d++) glen *= bdim[d];
+    for (int d = 0; d < dim; d++) glen *= gdim[d];
     double bbmin[3], bbmax[3], gsize[3];
     int *elref = malloc(sizeof(int) * glen), *browptr = malloc(sizeof(int) * (glen + 1));
     int *bcol = malloc(sizeof(int) * (size_t)glen * nn);
     double *bval = malloc(sizeof(double) * (size_t)glen * nn);
-    tor_raster_pixel(m, bdim, bbmin, bbmax, elref, browptr, bcol, bval);
+    tor_raster_pixel(m, gdim, bbmin, bbmax, elref, browptr, bcol, bval);
     for (int d = 0; d < dim; d++) gsize[d] = bbmax[d] - bbmin[d];
-    int slen = 0;
-    int *sol = malloc(sizeof(int) * glen);
-    for (int i = 0; i < glen; i++) if (elref[i] >= 0) sol[slen++] = i;
+    grid2sol_t M;
+    grid2sol_init(dim, bdim, gdim, elref, &M);
+    const int slen = M.slen;
     const int nqm = link_ofs[nq];
     zd *fin = malloc(sizeof(zd) * n);
     zd *ag = malloc(sizeof(zd) * (size_t)nm * glen), *agr = malloc(sizeof(zd) * (size_t)nm * dim * glen);
     zd *dg = malloc(sizeof(zd) * glen), *dgr = malloc(sizeof(zd) * (size_t)dim * glen);
     zd *pm = malloc(sizeof(zd) * glen), *pk = malloc(sizeof(zd) * glen);
+    zd *sm = malloc(sizeof(zd) * (slen > 0 ? slen : 1)), *sk = malloc(sizeof(zd) * (slen > 0 ? slen : 1));
     for (int j = 0; j < nm; j++) {
         for (int i = 0; i < n; i++)
             fin[i] = cplx ? aphi[2 * ((size_t)j * n + i)] + I * aphi[2 * ((size_t)j * n + i) + 1] : aphi[(size_t)j * n + i];
         grid_map(glen, browptr, bcol, bval, fin, ag + (size_t)j * glen);
-        image_gradient(dim, bdim, gsize, ag + (size_t)j * glen, agr + (size_t)j * dim * glen, cplx ? elref : NULL);
+        image_gradient(dim, gdim, gsize, ag + (size_t)j * glen, agr + (size_t)j * dim * glen, cplx ? elref : NULL);
     }
     double sz = 1.0;
     for (int d = 0; d < dim; d++) sz *= gsize[d] / (bdim[d] - 1.0);
@@ -1708,38 +1998,39 @@ int tor_jacobian_grid(const tor_mesh *m, const int *bdim, int nq, int nm, const 
         for (int i = 0; i < n; i++)
             fin[i] = cplx ? dphi[2 * ((size_t)q * n + i)] + I * dphi[2 * ((size_t)q * n + i) + 1] : dphi[(size_t)q * n + i];
         grid_map(glen, browptr, bcol, bval, fin, dg);
-        image_gradient(dim, bdim, gsize, dg, dgr, elref);
+        image_gradient(dim, gdim, gsize, dg, dgr, elref);
         for (int l = link_ofs[q]; l < link_ofs[q + 1]; l++) {
             const int j = link_m[l];
             const zd *a = ag + (size_t)j * glen, *agj = agr + (size_t)j * dim * glen;
+            zd y = cplx ? proj[2 * l] + I * proj[2 * l + 1] : proj[l];
             for (int g = 0; g < glen; g++) {
                 pm[g] = -(dg[g] * a[g]);
                 zd kk = 0.0;
                 for (int d = 0; d < dim; d++) kk -= dgr[(size_t)d * glen + g] * agj[(size_t)d * glen + g];
                 pk[g] = kk;
+                if (cplx && logscale) { pm[g] = pm[g] / y; pk[g] = pk[g] / y; }
             }
+            grid_to_sol(&M, pm, cplx, sm);
+            grid_to_sol(&M, pk, cplx, sk);
+            double *r0 = J + (size_t)l * cols, *r1 = J + (size_t)(l + nqm) * cols;
             if (cplx) {
-                zd y = proj[2 * l] + I * proj[2 * l + 1];
-                double *r0 = J + (size_t)l * cols, *r1 = J + (size_t)(l + nqm) * cols;
                 for (int s = 0; s < slen; s++) {
-                    zd vm = pm[sol[s]], vk = pk[sol[s]];
-                    if (logscale) { vm = vm / y; vk = vk / y; }
-                    r0[s] = creal(vm) * sz; r1[s] = cimag(vm) * sz;
-                    r0[slen + s] = creal(vk) * sz; r1[slen + s] = cimag(vk) * sz;
+                    r0[s] = creal(sm[s]) * sz; r1[s] = cimag(sm[s]) * sz;
+                    r0[slen + s] = creal(sk[s]) * sz; r1[slen + s] = cimag(sk[s]) * sz;
                 }
             } else {
-                double iy = 1.0 / proj[l];
-                double *r0 = J + (size_t)l * cols, *r1 = J + (size_t)(l + nqm) * cols;
+                double iy = 1.0 / creal(y);
                 for (int s = 0; s < slen; s++) {
-                    double vm = creal(pm[sol[s]]) * sz, vk = creal(pk[sol[s]]) * sz;
+                    double vm = creal(sm[s]) * sz, vk = creal(sk[s]) * sz;
                     r0[s] = logscale ? vm * iy : vm;
                     r1[s] = logscale ? vk * iy : vk;
                 }
             }
         }
     }
-    free(elref); free(browptr); free(bcol); free(bval); free(sol); free(fin);
-    free(ag); free(agr); free(dg); free(dgr); free(pm); free(pk);
+    grid2sol_free(&M);
+    free(elref); free(browptr); free(bcol); free(bval); free(fin);
+    free(ag); free(agr); free(dg); free(dgr); free(pm); free(pk); free(sm); free(sk);
     return slen;
 }
 
@@ -1829,43 +2120,45 @@ void tor_gradient_weights(int nq, int n, const double *mvec, const double *ylin,
 }
 
 /* Grid part: per source, both fields resampled on the Raster_Pixel grid
-   (basis = grid), their masked image gradients, then at the solution points
-   grad_mua -= Re(f a) and grad_kappa -= Re(sum_d grad_d f grad_d a)
-   (no voxel scaling).  dphi, wphi: nq x n complex; grad: 2 slen, in/out. */
-void tor_gradient_grid(const tor_mesh *m, const int *bdim, int nq, const double *dphi, const double *wphi,
-                       double *grad)
+   gdim, their masked image gradients, then grad_mua -= Re(Map_GridToSol(f a))
+   and grad_kappa -= Re(Map_GridToSol(sum_d grad_d f grad_d a)) (no voxel
+   scaling).  dphi, wphi: nq x n complex; grad: 2 slen, in/out. */
+void tor_gradient_grid(const tor_mesh *m, const int *bdim, const int *gdim, int nq, const double *dphi,
+                       const double *wphi, double *grad)
 {
     const int dim = m->dim, nn = m->nn, n = m->n;
     int glen = 1;
-    for (int d = 0; d < dim; d++) glen *= bdim[d];
+    for (int d = 0; d < dim; d++) glen *= gdim[d];
     double bbmin[3], bbmax[3], gsize[3];
     int *elref = malloc(sizeof(int) * glen), *browptr = malloc(sizeof(int) * (glen + 1));
     int *bcol = malloc(sizeof(int) * (size_t)glen * nn);
     double *bval = malloc(sizeof(double) * (size_t)glen * nn);
-    tor_raster_pixel(m, bdim, bbmin, bbmax, elref, browptr, bcol, bval);
+    tor_raster_pixel(m, gdim, bbmin, bbmax, elref, browptr, bcol, bval);
     for (int d = 0; d < dim; d++) gsize[d] = bbmax[d] - bbmin[d];
-    int slen = 0;
-    int *sol = malloc(sizeof(int) * glen);
-    for (int i = 0; i < glen; i++) if (elref[i] >= 0) sol[slen++] = i;
-    zd *df = malloc(sizeof(zd) * glen), *af = malloc(sizeof(zd) * glen);
+    grid2sol_t M;
+    grid2sol_init(dim, bdim, gdim, elref, &M);
+    const int slen = M.slen;
+    zd *df = malloc(sizeof(zd) * glen), *af = malloc(sizeof(zd) * glen), *pr = malloc(sizeof(zd) * glen);
     zd *dg = malloc(sizeof(zd) * (size_t)dim * glen), *ag = malloc(sizeof(zd) * (size_t)dim * glen);
+    zd *sv = malloc(sizeof(zd) * (slen > 0 ? slen : 1));
     for (int q = 0; q < nq; q++) {
         grid_map(glen, browptr, bcol, bval, (const zd *)(dphi + 2 * (size_t)q * n), df);
-        image_gradient(dim, bdim, gsize, df, dg, elref);
+        image_gradient(dim, gdim, gsize, df, dg, elref);
         grid_map(glen, browptr, bcol, bval, (const zd *)(wphi + 2 * (size_t)q * n), af);
-        image_gradient(dim, bdim, gsize, af, ag, elref);
-        for (int s = 0; s < slen; s++) {
-            const int g = sol[s];
-            grad[s] -= creal(df[g] * af[g]);
-        }
-        for (int s = 0; s < slen; s++) {
-            const int g = sol[s];
+        image_gradient(dim, gdim, gsize, af, ag, elref);
+        for (int g = 0; g < glen; g++) pr[g] = df[g] * af[g];
+        grid_to_sol(&M, pr, 1, sv);
+        for (int s = 0; s < slen; s++) grad[s] -= creal(sv[s]);
+        for (int g = 0; g < glen; g++) {
             zd gk = 0.0;
             for (int d = 0; d < dim; d++) gk += dg[(size_t)d * glen + g] * ag[(size_t)d * glen + g];
-            grad[slen + s] -= creal(gk);
+            pr[g] = gk;
         }
+        grid_to_sol(&M, pr, 1, sv);
+        for (int s = 0; s < slen; s++) grad[slen + s] -= creal(sv[s]);
     }
-    free(elref); free(browptr); free(bcol); free(bval); free(sol); free(df); free(af); free(dg); free(ag);
+    grid2sol_free(&M);
+    free(elref); free(browptr); free(bcol); free(bval); free(df); free(af); free(pr); free(dg); free(ag); free(sv);
 }
 
 /* A_Keijzer (param.cc:24-32) */

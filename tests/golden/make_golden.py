@@ -16,6 +16,12 @@ src/python/toastmodule.cc:696), the raster's element reference per grid
 point and the reference's own fields, so the oracle's raster and grid
 Jacobian are checked on exactly the reference's inputs.
 
+The *_igrid fixtures (and *_igrad, the data gradient) use a Raster_Pixel
+with an intermediate grid finer than its basis (toast.Raster(mesh, grd,
+intgrd)): the grid Jacobian is mapped from the fine grid to the basis, and
+the fixtures add the solution points' basis indices and the maps through
+the basis.
+
 The *_el fixtures reset the solver in the element basis (one mua, mus',
 nref per element, seeded) and hold the reference's system matrix, fields,
 projections and element-basis Jacobian.
@@ -87,6 +93,17 @@ FIXTURES = {
     "disc_fd_grad": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (20, 20), False,
                      True),
     "cyl_fd_grad": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-15, False, (9, 9, 10), False, True),
+    # Raster_Pixel with an intermediate grid (toast.Raster(mesh, grd, intgrd)):
+    # basis grd, fine grid intgrd
+    "disc_cw_igrid": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "ICH", 1e-15, False, (12, 12), False, False,
+                      (24, 24)),
+    "disc_fd_igrid": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (11, 9), False,
+                      False, (31, 25)),
+    "cyl_cw_igrid": (lambda: small_cylinder(0.0), "CG", "ICH", 1e-15, False, (5, 6, 7), False, False, (11, 12, 13)),
+    "cyl_fd_igrid": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-15, False, (6, 5, 6), False, False,
+                     (14, 12, 11)),
+    "disc_fd_igrad": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (10, 10), False,
+                      True, (28, 28)),
 }
 
 
@@ -116,7 +133,7 @@ def synthetic_data(logproj, seed=17):
     return data, sd
 
 
-def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradient=False):
+def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradient=False, gdim=None):
     P = factory()
     cplx = P.complex
     with tempfile.TemporaryDirectory() as td:
@@ -135,6 +152,8 @@ def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradi
                 "maxit=0", f"freq={P.freq_mhz}", f"qwidth={P.qwidth}", f"mwidth={P.mwidth}", f"jac={int(jac)}"]
         if grid:
             args += ["grid=" + ",".join(str(g) for g in grid), "fields=1"]
+        if gdim:
+            args += ["gdim=" + ",".join(str(g) for g in gdim)]
         if elbasis:
             emua, emus, eref = element_params(P)
             epar = os.path.join(td, "elpar.bin")
@@ -179,6 +198,13 @@ def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradi
                 res["map_" + key] = rd(out + f"_{key}.bin", np.float64)
             res["elref"] = rd(out + "_elref.bin", np.int32)
             res["bdim"] = np.array(grid, np.int32)
+            if gdim:
+                res["gdim"] = np.array(gdim, np.int32)
+                res["sol2basis"] = rd(out + "_sol2basis.bin", np.int32)
+                for key in ("m2b", "b2m", "g2b", "b2g", "g2s", "s2g"):
+                    res["map_" + key] = rd(out + f"_{key}.bin", np.float64)
+                for key in ("cm2s", "cs2m"):
+                    res["map_" + key] = rd(out + f"_{key}.bin", np.complex128)
             res["dphi"] = rd(out + "_dphi.bin", ct).reshape(len(P.qm.Q), P.n)
             res["aphi"] = rd(out + "_aphi.bin", ct).reshape(len(P.qm.M), P.n)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), coords=P.coords, elems=P.elems, Q=P.qm.Q, M=P.qm.M,

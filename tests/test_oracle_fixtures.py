@@ -29,20 +29,40 @@ def test_oracle_matches_reference_fixture(oracle_mod, name):
 
 
 GRID = [n for n in names() if n.endswith("_grid")]
+# Raster_Pixel with an intermediate grid finer than the basis
+IGRID = [n for n in names() if "gdim" in load(n)]
 
 
-@pytest.mark.parametrize("name", GRID)
+@pytest.mark.parametrize("name", GRID + IGRID)
 def test_oracle_grid_jacobian_matches_reference(oracle_mod, name):
-    """Raster_Pixel (basis = grid) and the grid-basis Jacobian on the
-    reference's own fields: the element reference per grid point and every
-    Jacobian entry equal the reference's bit for bit."""
+    """Raster_Pixel (basis = grid, or an intermediate grid) and the
+    grid-basis Jacobian on the reference's own fields: the element reference
+    per grid point, the solution points and every Jacobian entry equal the
+    reference's bit for bit."""
     g = load(name)
     mesh = oracle_mod.Mesh(g["coords"], g["elems"])
-    r = oracle_mod.raster_pixel(mesh, g["bdim"])
+    gdim = g.get("gdim")
+    r = oracle_mod.raster_pixel(mesh, g["bdim"] if gdim is None else gdim)
     assert np.array_equal(r.elref, g["elref"])
-    J = oracle_mod.jacobian_grid(mesh, g["bdim"], g["dphi"], g["aphi"], g["proj"], g["link_ofs"], g["link_m"])
+    if gdim is not None:
+        assert np.array_equal(oracle_mod.raster_support(mesh, g["bdim"], gdim), g["sol2basis"])
+    J = oracle_mod.jacobian_grid(mesh, g["bdim"], g["dphi"], g["aphi"], g["proj"], g["link_ofs"], g["link_m"],
+                                 gdim=gdim)
     assert J.shape == g["Jgrid"].shape
     assert np.array_equal(J, g["Jgrid"])
+
+
+@pytest.mark.parametrize("name", IGRID)
+def test_oracle_basis_maps_match_reference(oracle_mod, name):
+    """With an intermediate grid the maps through the basis (Grid2LinPix G,
+    LinPix2Grid GI, the products C = G B and CI = BI GI in the reference's
+    entry order, the support D) equal the reference's bit for bit, the
+    complex M->S / S->M (run through the grid) included."""
+    g = load(name)
+    mesh = oracle_mod.Mesh(g["coords"], g["elems"])
+    maps = oracle_mod.raster_basis_maps(mesh, g["bdim"], g["gdim"], g["mua"], g["mus"])
+    for key in ("m2b", "b2m", "g2b", "b2g", "g2s", "s2g", "m2s", "s2m", "cm2s", "cs2m"):
+        assert np.array_equal(maps[key], g["map_" + key]), key
 
 
 ELEM = [n for n in names() if n.endswith("_el")]
@@ -63,7 +83,7 @@ def test_oracle_element_basis_matches_reference(oracle_mod, name):
     assert np.array_equal(J, g["Jel"])
 
 
-GRAD = [n for n in names() if n.endswith("_grad")]
+GRAD = [n for n in names() if n.endswith("_grad") or n.endswith("_igrad")]
 
 
 @pytest.mark.parametrize("name", GRAD)
@@ -77,21 +97,26 @@ def test_oracle_data_gradient_matches_reference(oracle_mod, name):
     val = m.assemble(cm, ck, ca, g["freq_mhz"] * 2 * np.pi * 1e-6, True)
     mvec = np.stack([m.qvec_gaussian(x, g["mwidth"]) * ca for x in g["M"]]).astype(np.complex128)
     grad = oracle_mod.data_gradient(m, g["bdim"], val, g["dphi"], mvec, g["proj"], g["logproj"], g["link_ofs"],
-                                    g["link_m"], g["data"], g["sd"], g["solver"], g["precon"], g["tol"])
+                                    g["link_m"], g["data"], g["sd"], g["solver"], g["precon"], g["tol"],
+                                    gdim=g.get("gdim"))
     assert np.array_equal(grad, g["grad"])
 
 
-@pytest.mark.parametrize("name", GRID)
+@pytest.mark.parametrize("name", GRID + IGRID)
 def test_oracle_raster_maps_match_reference(oracle_mod, name):
     """The pixel raster's basis maps (mesh -> grid, mesh -> solution,
     solution -> mesh through NodeMapMatrix, grid -> mesh) equal the
-    reference's bit for bit."""
+    reference's bit for bit (with an intermediate grid: mesh -> grid and
+    grid -> mesh; the rest run through the basis)."""
     g = load(name)
     mesh = oracle_mod.Mesh(g["coords"], g["elems"])
+    grid = g.get("gdim", g["bdim"])
     slen = int((g["elref"] >= 0).sum())
-    maps = oracle_mod.raster_maps(mesh, g["bdim"], g["mua"], np.arange(1, slen + 1, dtype=float))
-    for a, key in zip(maps, ("m2g", "m2s", "s2m", "g2m")):
-        assert np.array_equal(a, g["map_" + key]), key
+    maps = oracle_mod.raster_maps(mesh, grid, g["mua"], np.arange(1, slen + 1, dtype=float))
+    keys = ("m2g", "m2s", "s2m", "g2m") if "gdim" not in g else ("m2g", None, None, "g2m")
+    for a, key in zip(maps, keys):
+        if key:
+            assert np.array_equal(a, g["map_" + key]), key
 
 
 @pytest.mark.parametrize("name", qm_names())
