@@ -335,24 +335,37 @@ int tg_jacobian_el(tg_solver s, int nq, const double *dphi, int nm, const double
                    const int *link_ofs, const int *link_m, int scale, void *J, int out_fp32, int mem);
 
 /* ---- grid basis (pixel raster) ----
-   Raster_Pixel with the basis equal to the grid, as toast.Raster(mesh, grd)
-   builds it (src/python/toastmodule.cc:696; raster.cc:18-83,
-   raster_px.cc:10-48): a regular grid of bdim[0] x bdim[1] (x bdim[2])
-   points over the mesh's bounding box; the solution points are the grid
-   points inside the mesh, in grid order (x fastest).  A raster built on a
-   different intermediate grid (gdim != bdim) is not supported. */
+   Raster_Pixel(bdim, gdim), as toast.Raster(mesh, grd, intgrd) builds it
+   (src/python/toastmodule.cc:696; raster.cc:18-83, raster_px.cc:10-48): a
+   regular grid of gdim[0] x gdim[1] (x gdim[2]) points over the mesh's
+   bounding box carries the mapped fields, a basis of bdim points the
+   solution.  Without an intermediate grid (gdim NULL or equal to bdim) the
+   solution points are the grid points inside the mesh, in grid order (x
+   fastest).  With one, grid and basis are joined by the linear pixel maps
+   (Grid2LinPixMatrix / LinPix2GridMatrix, src/libfe/mesh.cc:3138-3320,
+   3540-3640) and the solution points are the basis points whose subsampled
+   mesh support is positive (SubsampleLinPixel, mesh.cc:3047-3136), in basis
+   order.  tg_raster_create(mesh, bdim, out) = tg_raster_create_ex(mesh,
+   bdim, NULL, out). */
 typedef struct tg_raster_s *tg_raster;
 int tg_raster_create(tg_mesh mesh, const int *bdim, tg_raster *out);
+int tg_raster_create_ex(tg_mesh mesh, const int *bdim, const int *gdim, tg_raster *out);
 int tg_raster_destroy(tg_raster r);
 /* glen grid points, slen solution points, bounding box (dim values each) */
 int tg_raster_info(tg_raster r, int *glen, int *slen, double *bbmin, double *bbmax);
 /* element containing each grid point, -1 outside (Raster::Elref) */
 int tg_raster_elref(tg_raster r, int *elref);
+/* blen basis points and the basis index of each solution point
+   (Raster::Sol2Basis, slen values); either may be NULL */
+int tg_raster_basis(tg_raster r, int *blen, int *sol2basis);
 /* toast.Raster.Map (MapBasis, src/python/toastmodule.cc:718-790): map is
-   "X->Y" with X, Y among M (mesh nodes), G (grid), B (basis, = G here), S
-   (solution points); nvec vectors back to back, width doubles per point
-   (1 real, 2 complex interleaved); src, dst in host or device memory.  Sums
-   in the reference's order without fused multiply-adds (bit-identical). */
+   "X->Y" with X, Y among M (mesh nodes), G (grid), B (basis; the grid itself
+   without an intermediate grid) and S (solution points); nvec vectors back
+   to back, width doubles per point (1 real, 2 complex interleaved); src,
+   dst in host or device memory.  Each map runs the chain the reference's
+   raster runs for that vector type (real: the pixel raster's product maps
+   G B and BI GI; complex: through the grid), summing in the reference's
+   order without fused multiply-adds (bit-identical). */
 int tg_raster_map(tg_raster r, const char *map, int nvec, const double *src, double *dst, int width, int mem);
 /* Grid-basis Jacobian (GenerateJacobian with a raster, jacobian.cc:105-123
    -> GenerateJacobian_grid 289-373; real systems GenerateJacobian_cw with a

@@ -272,19 +272,23 @@ void GenerateJacobian_el(const TFwdSolver<T>& fws, int nq, const T* dphi, int nm
                          L.ofs.data(), L.m.data(), dscale == DATA_LOG ? TG_DATA_LOG : TG_DATA_LIN, J, 0, TG_MEM_HOST));
 }
 
-// Raster_Pixel(bdim, bdim, mesh): a grid of bdim points per axis over the
-// mesh's bounding box; SLen() solution points (grid points inside the mesh)
+// Raster_Pixel(bdim, gdim, mesh): a grid of gdim points per axis over the
+// mesh's bounding box and a basis of bdim points; SLen() solution points
+// (without an intermediate grid: the grid points inside the mesh)
 class Raster_Pixel {
 public:
-    Raster_Pixel(const int* bdim, const Mesh& mesh)
+    Raster_Pixel(const int* bdim, const Mesh& mesh) : Raster_Pixel(bdim, nullptr, mesh) {}
+    Raster_Pixel(const int* bdim, const int* gdim, const Mesh& mesh)
     {
-        check(tg_raster_create(mesh.handle(), bdim, &h_));
+        check(tg_raster_create_ex(mesh.handle(), bdim, gdim, &h_));
         check(tg_raster_info(h_, &glen_, &slen_, nullptr, nullptr));
+        check(tg_raster_basis(h_, &blen_, nullptr));
     }
     ~Raster_Pixel() { tg_raster_destroy(h_); }
     Raster_Pixel(const Raster_Pixel&) = delete;
     Raster_Pixel& operator=(const Raster_Pixel&) = delete;
     int GLen() const { return glen_; }
+    int BLen() const { return blen_; }
     int SLen() const { return slen_; }
     std::vector<int> Elref() const
     {
@@ -296,7 +300,7 @@ public:
 
 private:
     tg_raster h_ = nullptr;
-    int glen_ = 0, slen_ = 0;
+    int glen_ = 0, blen_ = 0, slen_ = 0;
 };
 
 // GenerateJacobian(raster, mesh, dphi, aphi, proj, dscale, J) grid basis:

@@ -1,6 +1,7 @@
-"""Grid-basis Jacobian (pixel raster, basis = grid) on the GPU against the
-reference's own outputs (tests/golden/*_grid.npz, made by the compiled
-reference) and the oracle."""
+"""Grid-basis Jacobian (pixel raster: basis = grid, or a basis on an
+intermediate grid) on the GPU against the reference's own outputs
+(tests/golden/*_grid.npz, *_igrid.npz, made by the compiled reference) and
+the oracle."""
 import numpy as np
 import pytest
 
@@ -11,26 +12,33 @@ from toastpp_gb300 import capi
 pytestmark = pytest.mark.gpu
 
 GRID = [n for n in names() if n.endswith("_grid")]
+# Raster_Pixel with an intermediate grid finer than the basis
+IGRID = [n for n in names() if n.endswith("_igrid")]
 
 
 def setup(name):
     g = load(name)
     gm = capi.Mesh(g["coords"], g["elems"])
-    r = capi.Raster(gm, g["bdim"])
+    r = capi.Raster(gm, g["bdim"], g.get("gdim"))
     cplx = np.iscomplexobj(g["proj"])
     s = capi.FwdSolver(gm, g["solver"], 1e-15, g["precon"], cplx, precision="fp64")
     return g, gm, r, s, capi.Links(g["link_ofs"], g["link_m"])
 
 
-@pytest.mark.parametrize("name", GRID)
+@pytest.mark.parametrize("name", GRID + IGRID)
 def test_raster_matches_reference(name):
     g, gm, r, s, L = setup(name)
-    assert r.glen == int(np.prod(g["bdim"]))
+    assert r.glen == int(np.prod(g.get("gdim", g["bdim"])))
+    assert r.blen == int(np.prod(g["bdim"]))
     assert np.array_equal(r.elref(), g["elref"])
-    assert r.slen == int((g["elref"] >= 0).sum())
+    if "gdim" in g:
+        assert np.array_equal(r.sol2basis(), g["sol2basis"])
+    else:
+        assert r.slen == int((g["elref"] >= 0).sum())
+        assert np.array_equal(r.sol2basis(), np.nonzero(g["elref"] >= 0)[0])
 
 
-@pytest.mark.parametrize("name", GRID)
+@pytest.mark.parametrize("name", GRID + IGRID)
 def test_grid_jacobian_on_reference_fields(name):
     """Same fields as the reference: FP64 agrees to round-off, FP32 to FP32
     accuracy."""
@@ -45,17 +53,29 @@ def test_grid_jacobian_on_reference_fields(name):
     assert rel2(J32.astype(np.float64), ref) < 1e-5
 
 
-@pytest.mark.parametrize("name", GRID)
+@pytest.mark.parametrize("name", GRID + IGRID)
 def test_grid_jacobian_linear_data_against_oracle(name, oracle_mod):
     g, gm, r, s, L = setup(name)
     J = s.jacobian_grid(r, g["dphi"], g["aphi"], None, L, scale=capi.DATA_LIN)
     om = oracle_mod.Mesh(g["coords"], g["elems"])
     ref = oracle_mod.jacobian_grid(om, g["bdim"], g["dphi"], g["aphi"], g["proj"], g["link_ofs"], g["link_m"],
-                                   logscale=False)
+                                   logscale=False, gdim=g.get("gdim"))
     assert rel2(J, ref) < 1e-13
 
 
-@pytest.mark.parametrize("name", GRID)
+@pytest.mark.parametrize("name", IGRID)
+def test_grid_jacobian_chunks(name, monkeypatch):
+    """With an intermediate grid the rows are formed on the grid a chunk of
+    sources at a time and then mapped to the basis; one-source chunks give
+    the same J as one chunk."""
+    g, gm, r, s, L = setup(name)
+    J1 = s.jacobian_grid(r, g["dphi"], g["aphi"], g["proj"], L)
+    monkeypatch.setenv("TOASTGPU_GRID_CHUNK_BYTES", "1")
+    J2 = s.jacobian_grid(r, g["dphi"], g["aphi"], g["proj"], L)
+    assert np.array_equal(J1, J2)
+
+
+@pytest.mark.parametrize("name", GRID + IGRID)
 def test_grid_jacobian_end_to_end(name):
     """GPU fields (FP64 path) -> projections -> grid Jacobian, against the
     reference's Jacobian from its own fields."""
@@ -71,7 +91,7 @@ def test_grid_jacobian_end_to_end(name):
     assert rel2(J, g["Jgrid"]) < 1e-9
 
 
-@pytest.mark.parametrize("name", GRID)
+@pytest.mark.parametrize("name", GRID + IGRID)
 def test_grid_jacobian_sparse_links_against_oracle(name, oracle_mod):
     """Links missing for some (source, detector) pairs and a source without
     any, with a source count that leaves a partial group of sources."""
@@ -79,7 +99,8 @@ def test_grid_jacobian_sparse_links_against_oracle(name, oracle_mod):
     ofs, lm, keep = sparse_links(g)
     J = s.jacobian_grid(r, g["dphi"], g["aphi"], g["proj"][keep], capi.Links(ofs, lm))
     om = oracle_mod.Mesh(g["coords"], g["elems"])
-    ref = oracle_mod.jacobian_grid(om, g["bdim"], g["dphi"], g["aphi"], g["proj"][keep], ofs, lm)
+    ref = oracle_mod.jacobian_grid(om, g["bdim"], g["dphi"], g["aphi"], g["proj"][keep], ofs, lm,
+                                   gdim=g.get("gdim"))
     assert J.shape == ref.shape == (2 * len(keep), g["Jgrid"].shape[1])
     assert rel2(J, ref) < 1e-13
 
@@ -93,7 +114,7 @@ def test_raster_of_another_mesh_is_rejected():
         s.jacobian_grid(r2, g["dphi"], g["aphi"], g["proj"], L)
 
 
-GRAD = [n for n in names() if n.endswith("_grad")]
+GRAD = [n for n in names() if n.endswith("_grad") or n.endswith("_igrad")]
 
 
 @pytest.mark.parametrize("name", GRAD)
@@ -106,7 +127,7 @@ def test_data_gradient_against_reference(name, precision, tol):
     stopped at the same 1e-15 relative residual, agrees to 4e-7 on the disc."""
     g = load(name)
     gm = capi.Mesh(g["coords"], g["elems"])
-    r = capi.Raster(gm, g["bdim"])
+    r = capi.Raster(gm, g["bdim"], g.get("gdim"))
     s = capi.FwdSolver(gm, g["solver"], 1e-15, g["precon"], True, precision=precision)
     cm, ck, ca = capi.optical_coefficients(g["mua"], g["mus"], g["nref"])
     s.reset(cm, ck, ca, capi.omega_of(g["freq_mhz"]))
@@ -138,3 +159,30 @@ def test_raster_maps_match_reference(name):
     assert np.array_equal(z.real, g["map_m2s"]) and np.array_equal(z.imag, 2 * g["map_m2s"])
     st = r.map("S->M", np.stack([sin, 3 * sin]))
     assert np.array_equal(st[0], g["map_s2m"]) and np.array_equal(st[1], r.map("S->M", 3 * sin))
+
+
+@pytest.mark.parametrize("name", IGRID)
+def test_basis_maps_match_reference(name):
+    """With an intermediate grid: every map through the basis (G, GI, the
+    products G B and BI GI, the support) equals the reference's bit for bit,
+    real and complex; the grid maps too."""
+    g, gm, r, s, L = setup(name)
+    b = np.arange(1, r.blen + 1, dtype=float)
+    sv = np.arange(1, r.slen + 1, dtype=float)
+    m2g = r.map("M->G", g["mua"])
+    assert np.array_equal(m2g, g["map_m2g"])
+    assert np.array_equal(r.map("G->M", m2g), g["map_g2m"])
+    assert np.array_equal(r.map("M->B", g["mua"]), g["map_m2b"])
+    assert np.array_equal(r.map("B->M", b), g["map_b2m"])
+    assert np.array_equal(r.map("G->B", m2g), g["map_g2b"])
+    assert np.array_equal(r.map("B->G", b), g["map_b2g"])
+    assert np.array_equal(r.map("G->S", m2g), g["map_g2s"])
+    assert np.array_equal(r.map("S->G", sv), g["map_s2g"])
+    assert np.array_equal(r.map("M->S", g["mua"]), g["map_m2s"])
+    assert np.array_equal(r.map("S->M", sv), g["map_s2m"])
+    assert np.array_equal(r.map("B->S", b), b[r.sol2basis()])
+    sb = r.map("S->B", sv)
+    assert np.array_equal(sb[r.sol2basis()], sv) and np.count_nonzero(sb) == r.slen
+    assert np.array_equal(r.map("M->S", g["mua"] + 1j * g["mus"]), g["map_cm2s"])
+    cs = np.arange(1, r.slen + 1) - 0.5j * np.arange(r.slen)
+    assert np.array_equal(r.map("S->M", cs), g["map_cs2m"])

@@ -1,8 +1,10 @@
-// tg_grid.cuh -- the grid-basis Jacobian of a pixel raster (basis = grid).
+// tg_grid.cuh -- the grid-basis Jacobian of a pixel raster.
 //
 // Reference: GenerateJacobian_grid (src/libstoast/jacobian.cc:289-373,
 // complex, projections given) and GenerateJacobian_cw_grid (516-712, real)
-// with Raster_Pixel (raster_px.cc:10-48) whose basis equals its grid.
+// with Raster_Pixel (raster_px.cc:10-48).  The PMDFs are formed on the
+// raster's grid; where the basis is coarser than the grid (an intermediate
+// grid) the rows are then mapped to the basis by G (grid_to_sol_rows_kernel).
 //
 // Per request the fields (source-major, natural numbering) are resampled on
 // the grid column by column (gm[c * glen + g]), then the values and the
@@ -243,11 +245,12 @@ struct LinkTile {
 // division per entry would run on the FP64 pipe.  NP = 1 + dim planes.
 // pair[q * nm + m]: link index or -1.  J rows: complex [Re mua | Re kap] at l
 // and [Im mua | Im kap] at nQM + l (2 slen columns); real mua at l and kap at
-// nQM + l (slen).
+// nQM + l (slen).  With l0 > 0 the kernel serves the sources of one chunk
+// whose links are l0 .. l0 + nqm - 1: row l - l0 and nqm + l - l0.
 template <class V, class JT, int GQ, int NP>
 __global__ void __launch_bounds__(256) grid_jacobian_kernel(int slen, int nq, int nm, int nqm, const V* __restrict__ Fp,
                                                             const V* __restrict__ Ap, const int* __restrict__ pair,
-                                                            const V* __restrict__ ysc, JT* __restrict__ J)
+                                                            const V* __restrict__ ysc, JT* __restrict__ J, int l0)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x, q0 = blockIdx.y * GQ;
     if (s >= slen) return;
@@ -285,8 +288,8 @@ __global__ void __launch_bounds__(256) grid_jacobian_kernel(int slen, int nq, in
 #pragma unroll
             for (int d = 2; d < NP; d++) t = vfma(t, f[g][d], a[d]);
             const V pm = vmul(vmul(f[g][0], a[0]), y), pk = vmul(t, y);
-            JT* r0 = J + (size_t)l * cols + s;
-            JT* r1 = J + (size_t)(l + nqm) * cols + s;
+            JT* r0 = J + (size_t)(l - l0) * cols + s;
+            JT* r1 = J + (size_t)(l - l0 + nqm) * cols + s;
             if constexpr (CPLX) {
                 st_stream(r0, (JT)re(pm));
                 st_stream(r1, (JT)im(pm));
@@ -462,6 +465,36 @@ __global__ void gradient_accum_kernel(int dim, int slen, int nq, const cd* __res
     grad[slen + s] = gk;
 }
 
+// Map_GridToSol (raster.cc:374-390) of Jacobian rows computed on the grid of
+// a raster with an intermediate grid: row r of Jg (nb blocks of gslen grid
+// points inside the mesh) -> row row0(r) of J (nb blocks of slen solution
+// points): J[k] = sum over G's row of the solution point k of w Jg[col], in
+// the row's entry order (RCompRowMatrix::Ax).  Rows r < half go to row0 + r,
+// the others to row0 + r - half + hoff (the Im / kappa rows of a chunk of
+// links).  add: J += instead of J = (the data gradient).  A thread per
+// output entry.
+template <class JT>
+__global__ void grid_to_sol_rows_kernel(long long rows, int half, long long row0, long long hoff, int nb, int gslen,
+                                        int slen, const int* __restrict__ rp, const int* __restrict__ col,
+                                        const double* __restrict__ val, const JT* __restrict__ Jg,
+                                        JT* __restrict__ J, int add)
+{
+    const long long total = rows * nb * (long long)slen;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t % slen);
+        const long long rb = t / slen;
+        const int b = (int)(rb % nb);
+        const long long r = rb / nb;
+        const JT* x = Jg + (size_t)r * nb * gslen + (size_t)b * gslen;
+        JT acc = (JT)0;
+        for (int j = rp[k]; j < rp[k + 1]; j++) acc += (JT)val[j] * x[col[j]];
+        const long long orow = r < half ? row0 + r : row0 + r - half + hoff;
+        JT* y = J + (size_t)orow * nb * slen + (size_t)b * slen + k;
+        *y = add ? *y + acc : acc;
+    }
+}
+
 // Raster basis maps: y = A x row by row in entry order (RCompRowMatrix::Ax,
 // crmatrix_imp.hpp:1168-1189; complex vectors component by component,
 // Ax_cplx 1302-1327), one thread per (row, vector), `width` doubles per point
@@ -479,24 +512,31 @@ __global__ void csr_apply_kernel(int rows, int cols, int width, const int* __res
     }
 }
 
-// grid -> solution points (Map_BasisToSol, raster.cc:292-315)
+// basis -> solution points (Map_BasisToSol, raster.cc:292-315).  d: the
+// pixel raster's real map D->Ax (raster_px.cc:147-150), 0 + 1 x, which
+// turns -0 into +0
 __global__ void gather_points_kernel(int slen, int glen, int width, const int* __restrict__ sol,
-                                     const double* __restrict__ g, double* __restrict__ s)
+                                     const double* __restrict__ g, double* __restrict__ s, int d)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y;
     if (i >= slen) return;
-    for (int c = 0; c < width; c++)
-        s[((size_t)v * slen + i) * width + c] = g[((size_t)v * glen + sol[i]) * width + c];
+    for (int c = 0; c < width; c++) {
+        const double x = g[((size_t)v * glen + sol[i]) * width + c];
+        s[((size_t)v * slen + i) * width + c] = d ? __dadd_rn(0.0, x) : x;
+    }
 }
 
-// solution points -> grid, zeros elsewhere (Map_SolToBasis, raster.cc:318-345)
+// solution points -> basis, zeros elsewhere (Map_SolToBasis, raster.cc:
+// 318-345; d: the real D->ATx, 0 + 1 x)
 __global__ void scatter_points_kernel(int slen, int glen, int width, const int* __restrict__ sol,
-                                      const double* __restrict__ s, double* __restrict__ g)
+                                      const double* __restrict__ s, double* __restrict__ g, int d)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y;
     if (i >= slen) return;
-    for (int c = 0; c < width; c++)
-        g[((size_t)v * glen + sol[i]) * width + c] = s[((size_t)v * slen + i) * width + c];
+    for (int c = 0; c < width; c++) {
+        const double x = s[((size_t)v * slen + i) * width + c];
+        g[((size_t)v * glen + sol[i]) * width + c] = d ? __dadd_rn(0.0, x) : x;
+    }
 }
 
 // QVec_Gaussian (src/libstoast/source.cc:19-56) for npos positions on the

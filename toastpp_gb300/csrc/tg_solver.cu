@@ -1021,29 +1021,50 @@ struct tg_mesh_s {
     DBuf d_coords, d_intbff, d_pos, d_scale, d_out;
 };
 
-// Raster_Pixel with the basis equal to the grid (src/libstoast/raster.cc:18-83,
-// raster_px.cc:10-48; what toast.Raster(mesh, grd) builds,
-// src/python/toastmodule.cc:696).  Built on the host once per raster: the
-// bounding box, the element containing each grid point and the grid map
-// matrix B, then kept on the device.
+// A sparse matrix in CSR form on the host and its device copy
+struct CsrMat {
+    std::vector<int> rp, col;
+    std::vector<double> val;
+    DBuf d_rp, d_col, d_val;
+};
+
+// Raster_Pixel(bdim, gdim) (src/libstoast/raster.cc:18-83, raster_px.cc:
+// 10-48; what toast.Raster(mesh, grd, intgrd) builds,
+// src/python/toastmodule.cc:696): a grid of gdim points per axis over the
+// mesh's bounding box carries the mapped fields; the basis of bdim points
+// carries the solution.  Built on the host once per raster: the bounding
+// box, the element containing each grid point, the grid map matrix B and
+// the node map matrix BI; with an intermediate grid (gdim != bdim) also the
+// grid <-> basis maps G (Grid2LinPixMatrix) and GI (LinPix2GridMatrix),
+// their products with B and BI, and the solution points (the basis points
+// whose subsampled mesh support is positive).  Then kept on the device.
 struct tg_raster_s {
     Mesh* mesh = nullptr;
-    int dim = 0, bdim[3] = {1, 1, 1}, glen = 0, slen = 0;
+    int dim = 0, gdim[3] = {1, 1, 1}, bdim[3] = {1, 1, 1};
+    int glen = 0, blen = 0;
+    int gslen = 0;  // grid points inside the mesh (gsol: their grid indices)
+    int slen = 0;   // solution points (sol2basis: their basis indices)
+    bool inter = false;  // an intermediate grid (gdim != bdim)
     double bbmin[3] = {0, 0, 0}, bbmax[3] = {0, 0, 0};
-    std::vector<int> elref, sol, rowptr, col;  // col: natural node numbers
+    std::vector<int> elref, gsol, rowptr, col;  // col: natural node numbers
     std::vector<double> val;
     std::vector<int> nrowptr, ncol;              // NodeMapMatrix: grid -> mesh nodes
     std::vector<double> nval;
-    DBuf d_elref, d_sol, d_rowptr, d_col, d_val, d_nrowptr, d_ncol, d_nval, d_src, d_dst, d_tmp;
+    std::vector<int> sol2basis;
+    // intermediate grid only: G (blen x glen), GI (glen x blen), C = G B
+    // (blen x n), CI = BI GI (n x blen), and G's rows of the solution points
+    // with columns as positions in gsol (slen x gslen)
+    CsrMat G, GI, C, CI, GS;
+    DBuf d_elref, d_sol, d_rowptr, d_col, d_val, d_nrowptr, d_ncol, d_nval, d_src, d_dst, d_tmp, d_tmp2, d_s2b;
     GridDev dev() const
     {
-        GridDev G;
-        G.dim = dim; G.nx = bdim[0]; G.ny = bdim[1]; G.nz = dim > 2 ? bdim[2] : 1;
-        G.glen = glen; G.slen = slen;
-        for (int d = 0; d < 3; d++) G.ih[d] = d < dim ? 1.0 / ((bbmax[d] - bbmin[d]) / bdim[d]) : 0.0;
-        G.elref = d_elref.as<int>(); G.sol = d_sol.as<int>(); G.rowptr = d_rowptr.as<int>();
-        G.col = d_col.as<int>(); G.val = d_val.as<double>();
-        return G;
+        GridDev D;
+        D.dim = dim; D.nx = gdim[0]; D.ny = gdim[1]; D.nz = dim > 2 ? gdim[2] : 1;
+        D.glen = glen; D.slen = gslen;
+        for (int d = 0; d < 3; d++) D.ih[d] = d < dim ? 1.0 / ((bbmax[d] - bbmin[d]) / gdim[d]) : 0.0;
+        D.elref = d_elref.as<int>(); D.sol = d_sol.as<int>(); D.rowptr = d_rowptr.as<int>();
+        D.col = d_col.as<int>(); D.val = d_val.as<double>();
+        return D;
     }
     // prod gsize / (bdim - 1): the voxel scale of the grid Jacobian (jacobian.cc:365-370)
     double voxel() const
@@ -1071,9 +1092,9 @@ void raster_build(const MeshHost& m, tg_raster_s& r)
             r.bbmin[d] = std::min(r.bbmin[d], v);
             r.bbmax[d] = std::max(r.bbmax[d], v);
         }
-    const int nx = r.bdim[0], ny = r.bdim[1], nz = dim > 2 ? r.bdim[2] : 1;
+    const int nx = r.gdim[0], ny = r.gdim[1], nz = dim > 2 ? r.gdim[2] : 1;
     double dW[3] = {0, 0, 0};
-    for (int d = 0; d < dim; d++) dW[d] = (r.bbmax[d] - r.bbmin[d]) / (double)(r.bdim[d] - 1);
+    for (int d = 0; d < dim; d++) dW[d] = (r.bbmax[d] - r.bbmin[d]) / (double)(r.gdim[d] - 1);
     r.elref.assign(r.glen, -1);
     for (int e = 0; e < m.ne; e++) {
         const int* nd = &m.el[(size_t)e * nn];
@@ -1092,7 +1113,7 @@ void raster_build(const MeshHost& m, tg_raster_s& r)
             hi[d] += 1e-6;
             if (lo[d] > r.bbmax[d] || hi[d] < r.bbmin[d]) { skip = true; break; }
             rmin[d] = std::max(0, (int)std::ceil((lo[d] - r.bbmin[d]) / dW[d]));
-            rmax[d] = std::min(r.bdim[d], (int)std::floor((hi[d] - r.bbmin[d]) / dW[d]) + 1);
+            rmax[d] = std::min(r.gdim[d], (int)std::floor((hi[d] - r.bbmin[d]) / dW[d]) + 1);
         }
         if (skip) continue;
         double p[3] = {0.0, 0.0, 0.0};
@@ -1112,7 +1133,7 @@ void raster_build(const MeshHost& m, tg_raster_s& r)
     r.rowptr.assign(r.glen + 1, 0);
     r.col.clear();
     r.val.clear();
-    r.sol.clear();
+    r.gsol.clear();
     for (int iz = 0, i = 0; iz < nz; iz++) {
         double p[3] = {0.0, 0.0, 0.0};
         if (dim > 2) p[2] = iz * dW[2] + r.bbmin[2];
@@ -1121,7 +1142,7 @@ void raster_build(const MeshHost& m, tg_raster_s& r)
             for (int ix = 0; ix < nx; ix++, i++) {
                 const int e = r.elref[i];
                 if (e >= 0) {
-                    r.sol.push_back(i);
+                    r.gsol.push_back(i);
                     p[0] = ix * dW[0] + r.bbmin[0];
                     const int* nd = &m.el[(size_t)e * nn];
                     const double* g = &m.geo[(size_t)e * 16];
@@ -1143,7 +1164,7 @@ void raster_build(const MeshHost& m, tg_raster_s& r)
             }
         }
     }
-    r.slen = (int)r.sol.size();
+    r.gslen = (int)r.gsol.size();
     // NodeMapMatrix (mesh.cc:2695-2852): per node the bilinear / trilinear
     // weights of the grid points around it that lie in the mesh,
     // renormalised when some are missing (equal weights below 1e-8); zero
@@ -1160,7 +1181,7 @@ void raster_build(const MeshHost& m, tg_raster_s& r)
             if (!(p[d] >= r.bbmin[d] && p[d] <= r.bbmax[d])) { inside = false; break; }
             i0[d] = (int)((p[d] - r.bbmin[d]) / dW[d]);
             if (i0[d] < 0) i0[d] = 0;
-            else if (i0[d] >= r.bdim[d] - 1) i0[d] = r.bdim[d] - 2;
+            else if (i0[d] >= r.gdim[d] - 1) i0[d] = r.gdim[d] - 2;
             d0[d] = (p[d] - (i0[d] * dW[d] + r.bbmin[d])) / dW[d];
             if (d0[d] < 0.0) d0[d] = 0.0;
             else if (d0[d] > 1.0) d0[d] = 1.0;
@@ -1191,6 +1212,198 @@ void raster_build(const MeshHost& m, tg_raster_s& r)
             r.nval.resize(o);
         }
         r.nrowptr[k + 1] = (int)r.ncol.size();
+    }
+}
+
+// The basis-point / grid-point pairs of the linear pixel basis, in the loop
+// order of Grid2LinPixMatrix (mesh.cc:3138-3320), LinPix2GridMatrix
+// (3540-3640) and SubsampleLinPixel (3047-3136): basis points b in grid order
+// (x fastest); for each, the grid points of its window [floor(x0 (g-1)),
+// ceil(x1 (g-1))] per axis (z, then y, then x) whose distance to the basis
+// point, in basis spacings, is below 1 along every axis and (elref given)
+// that lie in the mesh, with the weight t = (1 - dx)(1 - dy)(1 - dz).
+// Window points past the grid's last index (a window end rounded up from
+// 1 + ulp) are skipped; the reference skips them by the distance test.
+template <class F>
+void linpix_pairs(int dim, const int* gd, const int* bd, const int* elref, F&& fn)
+{
+    const int gx = gd[0], gy = gd[1], gz = dim > 2 ? gd[2] : 1;
+    const int bx = bd[0], by = bd[1], bz = dim > 2 ? bd[2] : 1;
+    const double nbx = bx - 1.0, nby = by - 1.0, nbz = bz - 1.0;
+    const double dbx = 1.0 / nbx, dby = 1.0 / nby, dgx = 1.0 / (gx - 1.0), dgy = 1.0 / (gy - 1.0);
+    double dbz = 0.0, dgz = 0.0, z = 0.0;
+    if (bz > 1) {
+        dbz = 1.0 / nbz;
+        dgz = 1.0 / (gz - 1.0);
+    }
+    int gz0 = 0, gz1 = 0;
+    for (int iz = 0; iz < bz; iz++) {
+        if (bz > 1) {
+            z = (double)iz * dbz;
+            const double z0 = iz ? (iz - 1) * dbz : 0.0, z1 = iz < bz - 1 ? (iz + 1) * dbz : 1.0;
+            gz0 = (int)std::floor(z0 * (gz - 1));
+            gz1 = (int)std::ceil(z1 * (gz - 1));
+        }
+        for (int iy = 0; iy < by; iy++) {
+            const double y = (double)iy * dby;
+            const double y0 = iy ? (iy - 1) * dby : 0.0, y1 = iy < by - 1 ? (iy + 1) * dby : 1.0;
+            const int gy0 = (int)std::floor(y0 * (gy - 1)), gy1 = (int)std::ceil(y1 * (gy - 1));
+            for (int ix = 0; ix < bx; ix++) {
+                const double x = ix * dbx;
+                const double x0 = ix ? (ix - 1) * dbx : 0.0, x1 = ix < bx - 1 ? (ix + 1) * dbx : 1.0;
+                const int gx0 = (int)std::floor(x0 * (gx - 1)), gx1 = (int)std::ceil(x1 * (gx - 1));
+                const int b = ix + (iy + iz * by) * bx;
+                for (int zz = bz > 1 ? gz0 : 0; zz <= (bz > 1 ? gz1 : 0) && zz < gz; zz++) {
+                    double idz = 1.0;
+                    if (bz > 1) {
+                        const double dz = std::fabs(zz * dgz - z) * nbz;
+                        if (dz >= 1.0) continue;
+                        idz = 1.0 - dz;
+                    }
+                    for (int yy = gy0; yy <= gy1 && yy < gy; yy++) {
+                        const double dy = std::fabs(yy * dgy - y) * nby;
+                        if (dy >= 1.0) continue;
+                        // the 2D weight is (1 - dx)(1 - dy); the 3D one (1 - dx)((1 - dy)(1 - dz))
+                        const double w = bz > 1 ? (1.0 - dy) * idz : 1.0 - dy;
+                        for (int xx = gx0; xx <= gx1 && xx < gx; xx++) {
+                            const int gidx = xx + (yy + zz * gy) * gx;
+                            if (elref && elref[gidx] < 0) continue;
+                            const double dx = std::fabs(xx * dgx - x) * nbx;
+                            if (dx >= 1.0) continue;
+                            fn(b, gidx, (1.0 - dx) * w);
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+// TCompRowMatrix::Shrink (crmatrix_imp.hpp:1774-1804): zero entries dropped
+void csr_shrink(CsrMat& A)
+{
+    const int rows = (int)A.rp.size() - 1;
+    int o = 0, r0 = 0;
+    for (int r = 0; r < rows; r++) {
+        const int r1 = A.rp[r + 1];
+        for (int i = r0; i < r1; i++)
+            if (A.val[i] != 0.0) {
+                A.col[o] = A.col[i];
+                A.val[o++] = A.val[i];
+            }
+        r0 = r1;
+        A.rp[r + 1] = o;
+    }
+    A.col.resize(o);
+    A.val.resize(o);
+}
+
+// TCompRowMatrix::AB (crmatrix_imp.hpp:1453-1541) then Shrink: each row of
+// A B with its columns in the order they first appear (A's row in order,
+// then B's rows) and each entry the sum of the products a b in that order
+void csr_ab(const std::vector<int>& arp, const std::vector<int>& acol, const std::vector<double>& aval,
+            const std::vector<int>& brp, const std::vector<int>& bcol, const std::vector<double>& bval, int nc,
+            CsrMat& C)
+{
+    const int nr = (int)arp.size() - 1;
+    std::vector<int> pos(std::max(nc, 1), -1);
+    C.rp.assign(nr + 1, 0);
+    C.col.clear();
+    C.val.clear();
+    for (int i = 0; i < nr; i++) {
+        const size_t r0 = C.col.size();
+        for (int ra = arp[i]; ra < arp[i + 1]; ra++) {
+            const int k = acol[ra];
+            for (int rb = brp[k]; rb < brp[k + 1]; rb++) {
+                const int j = bcol[rb];
+                if (pos[j] >= 0) {
+                    C.val[pos[j]] += aval[ra] * bval[rb];
+                } else {
+                    pos[j] = (int)C.col.size();
+                    C.col.push_back(j);
+                    C.val.push_back(aval[ra] * bval[rb]);
+                }
+            }
+        }
+        for (size_t t = r0; t < C.col.size(); t++) pos[C.col[t]] = -1;
+        C.rp[i + 1] = (int)C.col.size();
+    }
+    csr_shrink(C);
+}
+
+// The basis side of the raster.  Without an intermediate grid the solution
+// points are the grid points inside the mesh.  With one: bsupport =
+// SubsampleLinPixel of the grid's mesh mask (raster.cc:55-64), solution
+// points the basis points with bsupport > 0 (66-77); G = Grid2LinPixMatrix
+// (rows divided by their weight sums), GI = LinPix2GridMatrix, both shrunk
+// (raster_px.cc:24-27); C = G B and CI = BI GI (raster_px.cc:29-34).
+void raster_basis(int n, tg_raster_s& r)
+{
+    if (!r.inter) {
+        r.sol2basis = r.gsol;
+        r.slen = r.gslen;
+        return;
+    }
+    const int dim = r.dim, glen = r.glen, blen = r.blen;
+    std::vector<double> wsum(blen, 0.0), ssum(blen, 0.0);
+    linpix_pairs(dim, r.gdim, r.bdim, nullptr, [&](int b, int g, double t) {
+        wsum[b] += t;
+        ssum[b] += t * (r.elref[g] >= 0 ? 1.0 : 0.0);
+    });
+    r.sol2basis.clear();
+    for (int b = 0; b < blen; b++)
+        if ((wsum[b] != 0.0 ? ssum[b] / wsum[b] : 0.0) > 0.0) r.sol2basis.push_back(b);
+    r.slen = (int)r.sol2basis.size();
+    // G: rows by basis point in pair order; GI: rows by grid point, basis
+    // points ascending (the pairs come in basis order)
+    CsrMat& G = r.G;
+    CsrMat& GI = r.GI;
+    G.rp.assign(blen + 1, 0);
+    GI.rp.assign(glen + 1, 0);
+    linpix_pairs(dim, r.gdim, r.bdim, r.elref.data(), [&](int b, int g, double) {
+        G.rp[b + 1]++;
+        GI.rp[g + 1]++;
+    });
+    for (int b = 0; b < blen; b++) G.rp[b + 1] += G.rp[b];
+    for (int g = 0; g < glen; g++) GI.rp[g + 1] += GI.rp[g];
+    G.col.resize(G.rp[blen]);
+    G.val.resize(G.rp[blen]);
+    GI.col.resize(GI.rp[glen]);
+    GI.val.resize(GI.rp[glen]);
+    std::vector<int> gfill(blen, 0), gifill(glen, 0);
+    linpix_pairs(dim, r.gdim, r.bdim, r.elref.data(), [&](int b, int g, double t) {
+        const int i = G.rp[b] + gfill[b]++;
+        G.col[i] = g;
+        G.val[i] = t;
+        const int k = GI.rp[g] + gifill[g]++;
+        GI.col[k] = b;
+        GI.val[k] = t;
+    });
+    for (int b = 0; b < blen; b++) {
+        double w = 0.0;
+        for (int i = G.rp[b]; i < G.rp[b + 1]; i++) w += G.val[i];
+        for (int i = G.rp[b]; i < G.rp[b + 1]; i++) G.val[i] = w != 0.0 ? G.val[i] / w : 0.0;
+    }
+    csr_shrink(G);
+    csr_shrink(GI);
+    csr_ab(G.rp, G.col, G.val, r.rowptr, r.col, r.val, n, r.C);
+    csr_ab(r.nrowptr, r.ncol, r.nval, GI.rp, GI.col, GI.val, blen, r.CI);
+    // G's rows of the solution points, columns as positions among the grid
+    // points inside the mesh (G only takes grid points inside the mesh)
+    std::vector<int> gpos(glen, -1);
+    for (int i = 0; i < r.gslen; i++) gpos[r.gsol[i]] = i;
+    CsrMat& S = r.GS;
+    S.rp.assign(1, 0);
+    S.col.clear();
+    S.val.clear();
+    for (int k = 0; k < r.slen; k++) {
+        const int b = r.sol2basis[k];
+        for (int i = G.rp[b]; i < G.rp[b + 1]; i++) {
+            TG_CHECK(gpos[G.col[i]] >= 0, TG_ERR_ARG, "raster: basis weight on a grid point outside the mesh");
+            S.col.push_back(gpos[G.col[i]]);
+            S.val.push_back(G.val[i]);
+        }
+        S.rp.push_back((int)S.col.size());
     }
 }
 
@@ -1231,6 +1444,7 @@ struct tg_solver_s {
     DBuf B, X, X32, B32, cs_outer, cs_inner, io_a, io_b, tmp, jout;
     DBuf jF, jG, jpair, jyinv, plink_q, plink_m, psup, pnsup, pflag, pMsup, plin, plog;
     DBuf gplanes_q, gplanes_m, gy, io_c;  // grid-basis Jacobian: field planes, 1/y, grid fields
+    DBuf gjf;                             // rows on the intermediate grid before the map to the basis
     DBuf gdata, gsd, ggrad, gofs, glm;    // data gradient: data, sd, gradient, link lists
     DBuf fp_bq, fp_xq, fp_bm, fp_xm, fp_lin, fp_log;
     DBuf jwm64, jwk64, jwm32, jwk32;  // per-node element weights of the Jacobian (geometry only)
@@ -2069,7 +2283,7 @@ static void grid_jac_run(tg_solver s, const tg_raster_s& r, int nq, const V64* F
     // planes of sources and detectors in one buffer; the reference masks the
     // adjoint gradient for complex data only (jacobian.cc:348-350 against 557)
     C* gm = (C*)s->io_c.ensure((size_t)r.glen * k * sizeof(C));
-    C* P = (C*)s->gplanes_q.ensure((size_t)k * np * r.slen * sizeof(C));
+    C* P = (C*)s->gplanes_q.ensure((size_t)k * np * r.gslen * sizeof(C));
     const dim3 mg(cdiv_u(r.glen, 256), cdiv_u(k, MAPC));
     if constexpr (std::is_same<C, V64>::value) {
         launch(grid_map_cm_kernel<C, V64>, mg, 256, 0, s->stream, G, n, k, nq, F, A, gm);
@@ -2081,21 +2295,64 @@ static void grid_jac_run(tg_solver s, const tg_raster_s& r, int nq, const V64* F
         launch(grid_map_cm_kernel<C, C>, mg, 256, 0, s->stream, G, n, k, nq, (const C*)X,
                (const C*)(X + (size_t)nq * n), gm);
     }
-    launch(grid_planes_cm_kernel<C>, dim3(cdiv_u(r.slen, 256), cdiv_u(k, MAPC)), 256, 0, s->stream, G, k, nq,
+    launch(grid_planes_cm_kernel<C>, dim3(cdiv_u(r.gslen, 256), cdiv_u(k, MAPC)), 256, 0, s->stream, G, k, nq,
            vt<V64>::cplx ? 1 : 0, (const C*)gm, P);
     C* ysc = (C*)s->gy.ensure((size_t)nqm * sizeof(C));
     launch(grid_yscale_kernel<C, V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, logscale ? yl : nullptr, -r.voxel(),
            ysc);
     using JT = typename vt<C>::R;
     constexpr int GQ = 4, TB = 256;
-    const dim3 jg(cdiv_u(r.slen, TB), cdiv_u(nq, GQ));
-    const C* Pm = P + (size_t)nq * np * r.slen;
-    if (r.dim == 3)
-        launch(grid_jacobian_kernel<C, JT, GQ, 4>, jg, TB, 0, s->stream, r.slen, nq, nm, nqm, (const C*)P, Pm,
-               (const int*)pr, (const C*)ysc, (JT*)Jd);
-    else
-        launch(grid_jacobian_kernel<C, JT, GQ, 3>, jg, TB, 0, s->stream, r.slen, nq, nm, nqm, (const C*)P, Pm,
-               (const int*)pr, (const C*)ysc, (JT*)Jd);
+    const C* Pm = P + (size_t)nq * np * r.gslen;
+    // the rows of the links l0 .. l0 + nqmc - 1 of sources q0 .. q0 + nqc - 1
+    // on the grid points inside the mesh
+    auto rows = [&](int q0, int nqc, int l0, int nqmc, JT* out) {
+        const dim3 jg(cdiv_u(r.gslen, TB), cdiv_u(nqc, GQ));
+        const C* Pq = P + (size_t)q0 * np * r.gslen;
+        const int* pq = pr + (size_t)q0 * nm;
+        if (r.dim == 3)
+            launch(grid_jacobian_kernel<C, JT, GQ, 4>, jg, TB, 0, s->stream, r.gslen, nqc, nm, nqmc, Pq, Pm, pq,
+                   (const C*)ysc, out, l0);
+        else
+            launch(grid_jacobian_kernel<C, JT, GQ, 3>, jg, TB, 0, s->stream, r.gslen, nqc, nm, nqmc, Pq, Pm, pq,
+                   (const C*)ysc, out, l0);
+    };
+    if (!r.inter) {
+        rows(0, nq, 0, nqm, (JT*)Jd);
+        return;
+    }
+    // intermediate grid: the rows of a chunk of sources on the grid, then
+    // Map_GridToSol (G) into J; chunks of at most 256 MB of grid rows
+    // (TOASTGPU_GRID_CHUNK_BYTES sets another bound; a source's links always
+    // form one chunk)
+    const int nb = vt<V64>::cplx ? 2 : 1;
+    const size_t rowb = (size_t)nb * r.gslen * sizeof(JT);
+    size_t cap = (size_t)256 << 20;
+    if (const char* e = getenv("TOASTGPU_GRID_CHUNK_BYTES")) cap = std::max(1ull, strtoull(e, nullptr, 10));
+    const int maxl = (int)std::min<size_t>(std::max<size_t>(1, cap / (2 * rowb)), (size_t)1 << 30);
+    std::vector<int> ofs(nq + 1, 0);
+    for (int l = 0; l < nqm; l++) ofs[L.q[l] + 1]++;
+    for (int q = 0; q < nq; q++) ofs[q + 1] += ofs[q];
+    int widest = 0;
+    for (int q0 = 0; q0 < nq;) {
+        int q1 = q0 + 1;
+        while (q1 < nq && ofs[q1 + 1] - ofs[q0] <= maxl) q1++;
+        widest = std::max(widest, ofs[q1] - ofs[q0]);
+        q0 = q1;
+    }
+    JT* Jg = (JT*)s->gjf.ensure(std::max<size_t>(1, (size_t)2 * widest * rowb));
+    for (int q0 = 0; q0 < nq;) {
+        int q1 = q0 + 1;
+        while (q1 < nq && ofs[q1 + 1] - ofs[q0] <= maxl) q1++;
+        const int l0 = ofs[q0], nqmc = ofs[q1] - l0;
+        if (nqmc > 0) {
+            rows(q0, q1 - q0, l0, nqmc, Jg);
+            const long long tot = (long long)2 * nqmc * nb * r.slen;
+            launch(grid_to_sol_rows_kernel<JT>, (unsigned)std::min<long long>((tot + 255) / 256, 152LL * 16), 256, 0,
+                   s->stream, (long long)2 * nqmc, nqmc, (long long)l0, (long long)nqm, nb, r.gslen, r.slen,
+                   r.GS.d_rp.as<int>(), r.GS.d_col.as<int>(), r.GS.d_val.as<double>(), (const JT*)Jg, (JT*)Jd, 0);
+        }
+        q0 = q1;
+    }
 }
 
 template <class V64, class V32>
@@ -2214,19 +2471,31 @@ static void api_gradient(tg_solver s, const tg_raster_s& r, int nq, const double
     if (res) read_results(s, nq, co, res + nq);
     // both fields on the grid with their gradients, then the sums
     const GridDev G = r.dev();
-    cd* Pf = (cd*)s->gplanes_q.ensure((size_t)nq * np * r.slen * sizeof(cd));
-    cd* Pa = (cd*)s->gplanes_m.ensure((size_t)nq * np * r.slen * sizeof(cd));
+    cd* Pf = (cd*)s->gplanes_q.ensure((size_t)nq * np * r.gslen * sizeof(cd));
+    cd* Pa = (cd*)s->gplanes_m.ensure((size_t)nq * np * r.gslen * sizeof(cd));
     auto planes = [&](const cd* x, cd* P) {
         cd* gm = (cd*)s->io_c.ensure((size_t)r.glen * nq * sizeof(cd));
         launch(grid_map_kernel<cd>, cdiv_u((size_t)r.glen * 32, 256), 256, 0, s->stream, G, nq, x, nq,
                (const int*)m.perm, gm);
-        launch(grid_planes_kernel<cd, cd>, dim3(cdiv_u(r.slen, 32), cdiv_u(nq, 32)), dim3(32, 8), 0, s->stream, G, nq,
-               (const cd*)gm, 1, P);
+        launch(grid_planes_kernel<cd, cd>, dim3(cdiv_u(r.gslen, 32), cdiv_u(nq, 32)), dim3(32, 8), 0, s->stream, G,
+               nq, (const cd*)gm, 1, P);
     };
     planes(X, Pf);
     planes(Y, Pa);
-    launch(gradient_accum_kernel, cdiv_u(r.slen, 256), 256, 0, s->stream, r.dim, r.slen, nq, (const cd*)Pf,
-           (const cd*)Pa, dg);
+    if (!r.inter) {
+        launch(gradient_accum_kernel, cdiv_u(r.gslen, 256), 256, 0, s->stream, r.dim, r.gslen, nq, (const cd*)Pf,
+               (const cd*)Pa, dg);
+    } else {
+        // the sums on the grid points inside the mesh, then Map_GridToSol
+        // (G) added into the gradient
+        double* fg = (double*)s->gjf.ensure((size_t)2 * r.gslen * sizeof(double));
+        TG_CUDA(cudaMemsetAsync(fg, 0, (size_t)2 * r.gslen * sizeof(double), s->stream));
+        launch(gradient_accum_kernel, cdiv_u(r.gslen, 256), 256, 0, s->stream, r.dim, r.gslen, nq, (const cd*)Pf,
+               (const cd*)Pa, fg);
+        launch(grid_to_sol_rows_kernel<double>, cdiv_u(2 * r.slen, 256), 256, 0, s->stream, 1LL, 1, 0LL, 0LL, 2,
+               r.gslen, r.slen, r.GS.d_rp.as<int>(), r.GS.d_col.as<int>(), r.GS.d_val.as<double>(),
+               (const double*)fg, dg, 1);
+    }
     if (mem != TG_MEM_DEVICE)
         TG_CUDA(cudaMemcpyAsync(grad, dg, (size_t)2 * r.slen * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     TG_CUDA(cudaGetLastError());
@@ -2849,7 +3118,14 @@ int tg_jacobian(tg_solver s, int nq, const double* dphi, int nm, const double* a
     API_END
 }
 
-int tg_raster_create(tg_mesh mesh, const int* bdim, tg_raster* out)
+static void upload_csr(CsrMat& A)
+{
+    upload_sync(A.d_rp, A.rp);
+    upload_sync(A.d_col, A.col);
+    upload_sync(A.d_val, A.val);
+}
+
+int tg_raster_create_ex(tg_mesh mesh, const int* bdim, const int* gdim, tg_raster* out)
 {
     API_BEGIN
     TG_CHECK(mesh && bdim && out, TG_ERR_ARG, "NULL argument");
@@ -2858,26 +3134,40 @@ int tg_raster_create(tg_mesh mesh, const int* bdim, tg_raster* out)
     auto r = std::make_unique<tg_raster_s>();
     r->mesh = mesh->m.get();
     r->dim = m.dim;
-    long long glen = 1;
+    long long glen = 1, blen = 1;
     for (int d = 0; d < m.dim; d++) {
-        TG_CHECK(bdim[d] >= 2, TG_ERR_ARG, "every grid dimension needs at least 2 points");
+        const int g = gdim ? gdim[d] : bdim[d];
+        TG_CHECK(bdim[d] >= 2 && g >= 2, TG_ERR_ARG, "every grid dimension needs at least 2 points");
         r->bdim[d] = bdim[d];
-        glen *= bdim[d];
+        r->gdim[d] = g;
+        r->inter |= g != bdim[d];
+        glen *= g;
+        blen *= bdim[d];
     }
-    TG_CHECK(glen < (1LL << 30), TG_ERR_ARG, "grid too large");
+    TG_CHECK(glen < (1LL << 30) && blen < (1LL << 30), TG_ERR_ARG, "grid too large");
     r->glen = (int)glen;
+    r->blen = (int)blen;
     raster_build(m, *r);
+    raster_basis(m.n, *r);
     TG_CUDA(cudaSetDevice(mesh->m->device));
     upload_sync(r->d_elref, r->elref);
-    upload_sync(r->d_sol, r->sol);
+    upload_sync(r->d_sol, r->gsol);
+    upload_sync(r->d_s2b, r->sol2basis);
     upload_sync(r->d_rowptr, r->rowptr);
     upload_sync(r->d_col, r->col);
     upload_sync(r->d_val, r->val);
     upload_sync(r->d_nrowptr, r->nrowptr);
     upload_sync(r->d_ncol, r->ncol);
     upload_sync(r->d_nval, r->nval);
+    if (r->inter)
+        for (CsrMat* A : {&r->G, &r->GI, &r->C, &r->CI, &r->GS}) upload_csr(*A);
     *out = r.release();
     API_END
+}
+
+int tg_raster_create(tg_mesh mesh, const int* bdim, tg_raster* out)
+{
+    return tg_raster_create_ex(mesh, bdim, nullptr, out);
 }
 
 int tg_raster_destroy(tg_raster r)
@@ -2908,47 +3198,99 @@ int tg_raster_elref(tg_raster r, int* elref)
     API_END
 }
 
+int tg_raster_basis(tg_raster r, int* blen, int* sol2basis)
+{
+    API_BEGIN
+    TG_CHECK(r, TG_ERR_ARG, "raster is NULL");
+    if (blen) *blen = r->blen;
+    if (sol2basis) std::memcpy(sol2basis, r->sol2basis.data(), r->sol2basis.size() * sizeof(int));
+    API_END
+}
+
 // toast.Raster.Map (MapBasis, src/python/toastmodule.cc:718-790) for the
-// pixel raster whose basis is its grid: mesh (M), grid / basis (G, B),
-// solution (S).  M -> G: B; G -> S: the support; S -> G: scatter with zeros;
-// G -> M: NodeMapMatrix; the rest compose these.  Each vector is `width`
-// doubles per point (1 real, 2 complex).
+// pixel raster: mesh (M), grid (G), basis (B), solution (S).  Each map is a
+// chain of steps as Raster / Raster_Pixel run it (raster.cc:188-458,
+// raster_px.cc:102-176): a sparse matrix (B: grid map, BI: node map, G, GI,
+// C = G B, CI = BI GI), the support (basis -> solution) or its scatter.
+// Real vectors take the pixel raster's own maps (C, CI, and D->Ax / D->ATx
+// for the support, 0 + 1 x); complex vectors the base class's chains
+// through the grid.  Without an intermediate grid G and GI are the identity
+// and C = B, CI = BI.  Each vector is `width` doubles per point (1 real, 2
+// complex).
 int tg_raster_map(tg_raster r, const char* map, int nvec, const double* src, double* dst, int width, int mem)
 {
     API_BEGIN
     TG_CHECK(r && map && src && dst && nvec > 0 && nvec <= 65535 && (width == 1 || width == 2), TG_ERR_ARG,
              "invalid argument");
     TG_CHECK(strlen(map) == 4 && map[1] == '-' && map[2] == '>', TG_ERR_ARG, "map must read \"X->Y\"");
-    auto kind = [](char c) { return c == 'B' ? 'G' : c; };
-    const char a = kind(map[0]), b = kind(map[3]);
-    auto len = [&](char c) { return c == 'M' ? r->mesh->d.n : c == 'G' ? r->glen : c == 'S' ? r->slen : -1; };
+    const char a = map[0], b = map[3];
+    const int n = r->mesh->d.n, glen = r->glen, blen = r->blen, slen = r->slen;
+    auto len = [&](char c) { return c == 'M' ? n : c == 'G' ? glen : c == 'B' ? blen : c == 'S' ? slen : -1; };
     TG_CHECK(len(a) > 0 && len(b) > 0 && a != b, TG_ERR_ARG, "map ids are M, G, B or S, source and target different");
+    const bool real = width == 1, I = r->inter;
+    // steps: 'B' grid map, 'N' node map, 'G' / 'I' grid <-> basis, 'C' / 'D'
+    // mesh <-> basis products, 's' support, 'x' its scatter, '=' copy
+    std::string steps;
+    const std::string key{a, b};
+    if (key == "MG") steps = "B";
+    else if (key == "GM") steps = "N";
+    else if (key == "MB") steps = I ? (real ? "C" : "BG") : "B";
+    else if (key == "MS") steps = I ? (real ? "Cs" : "BGs") : "Bs";
+    else if (key == "GB") steps = I ? "G" : "=";
+    else if (key == "GS") steps = I ? "Gs" : "s";
+    else if (key == "BG") steps = I ? "I" : "=";
+    else if (key == "BS") steps = "s";
+    else if (key == "BM") steps = I ? (real ? "D" : "IN") : "N";
+    else if (key == "SB") steps = "x";
+    else if (key == "SG") steps = I ? "xI" : "x";
+    else if (key == "SM") steps = I ? (real ? "xD" : "xIN") : "xN";
     TG_CUDA(cudaSetDevice(r->mesh->device));
     const size_t sb = (size_t)nvec * len(a) * width * sizeof(double), db = (size_t)nvec * len(b) * width * sizeof(double);
     const double* x = mem == TG_MEM_DEVICE ? src : (const double*)r->d_src.ensure(sb);
     if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpy((void*)x, src, sb, cudaMemcpyHostToDevice));
     double* y = mem == TG_MEM_DEVICE ? dst : (double*)r->d_dst.ensure(db);
-    const int glen = r->glen, slen = r->slen, n = r->mesh->d.n;
-    auto apply = [&](const DBuf& rp, const DBuf& cl, const DBuf& vl, int rows, int cols, const double* in, double* out) {
-        launch(csr_apply_kernel, dim3(cdiv_u(rows, 128), nvec), 128, 0, (cudaStream_t)0, rows, cols, width,
-               rp.as<int>(), cl.as<int>(), vl.as<double>(), in, out);
+    const size_t tb = (size_t)nvec * std::max({n, glen, blen, slen}) * width * sizeof(double);
+    double* tmp[2] = {(double*)r->d_tmp.ensure(tb), (double*)r->d_tmp2.ensure(tb)};
+    const cudaStream_t st = 0;
+    auto apply = [&](const int* rp, const int* cl, const double* vl, int rows, int cols, const double* in,
+                     double* out) {
+        launch(csr_apply_kernel, dim3(cdiv_u(rows, 128), nvec), 128, 0, st, rows, cols, width, rp, cl, vl, in, out);
     };
-    auto select = [&](const double* in, double* out) {
-        launch(gather_points_kernel, dim3(cdiv_u(slen, 128), nvec), 128, 0, (cudaStream_t)0, slen, glen, width,
-               r->d_sol.as<int>(), in, out);
+    auto mat = [&](const CsrMat& A, int rows, int cols, const double* in, double* out) {
+        apply(A.d_rp.as<int>(), A.d_col.as<int>(), A.d_val.as<double>(), rows, cols, in, out);
     };
-    auto scatter = [&](const double* in, double* out) {
-        TG_CUDA(cudaMemsetAsync(out, 0, (size_t)nvec * glen * width * sizeof(double), (cudaStream_t)0));
-        launch(scatter_points_kernel, dim3(cdiv_u(slen, 128), nvec), 128, 0, (cudaStream_t)0, slen, glen, width,
-               r->d_sol.as<int>(), in, out);
-    };
-    double* t = (double*)r->d_tmp.ensure((size_t)nvec * glen * width * sizeof(double));
-    if (a == 'M' && b == 'G') apply(r->d_rowptr, r->d_col, r->d_val, glen, n, x, y);
-    else if (a == 'M' && b == 'S') { apply(r->d_rowptr, r->d_col, r->d_val, glen, n, x, t); select(t, y); }
-    else if (a == 'G' && b == 'S') select(x, y);
-    else if (a == 'S' && b == 'G') scatter(x, y);
-    else if (a == 'G' && b == 'M') apply(r->d_nrowptr, r->d_ncol, r->d_nval, n, glen, x, y);
-    else if (a == 'S' && b == 'M') { scatter(x, t); apply(r->d_nrowptr, r->d_ncol, r->d_nval, n, glen, t, y); }
+    const double* cur = x;
+    char kind = a;  // the space cur lives in
+    for (size_t i = 0; i < steps.size(); i++) {
+        const char c = steps[i];
+        const char to = c == 'B' ? 'G' : c == 'N' ? 'M' : c == 'G' ? 'B' : c == 'I' ? 'G' : c == 'C' ? 'B'
+                      : c == 'D' ? 'M' : c == 's' ? 'S' : c == 'x' ? 'B' : b;
+        double* out = i + 1 == steps.size() ? y : tmp[i & 1];
+        switch (c) {
+        case 'B': apply(r->d_rowptr.as<int>(), r->d_col.as<int>(), r->d_val.as<double>(), glen, n, cur, out); break;
+        case 'N': apply(r->d_nrowptr.as<int>(), r->d_ncol.as<int>(), r->d_nval.as<double>(), n, glen, cur, out); break;
+        case 'G': mat(r->G, blen, glen, cur, out); break;
+        case 'I': mat(r->GI, glen, blen, cur, out); break;
+        case 'C': mat(r->C, blen, n, cur, out); break;
+        case 'D': mat(r->CI, n, blen, cur, out); break;
+        case 's':
+            if (slen > 0)
+                launch(gather_points_kernel, dim3(cdiv_u(slen, 128), nvec), 128, 0, st, slen, blen, width,
+                       r->d_s2b.as<int>(), cur, out, real ? 1 : 0);
+            break;
+        case 'x':
+            TG_CUDA(cudaMemsetAsync(out, 0, (size_t)nvec * blen * width * sizeof(double), st));
+            if (slen > 0)
+                launch(scatter_points_kernel, dim3(cdiv_u(slen, 128), nvec), 128, 0, st, slen, blen, width,
+                       r->d_s2b.as<int>(), cur, out, real ? 1 : 0);
+            break;
+        default:
+            TG_CUDA(cudaMemcpyAsync(out, cur, (size_t)nvec * len(kind) * width * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, st));
+        }
+        cur = out;
+        kind = to;
+    }
     TG_CUDA(cudaGetLastError());
     if (mem != TG_MEM_DEVICE) TG_CUDA(cudaMemcpy(dst, y, db, cudaMemcpyDeviceToHost));
     else TG_CUDA(cudaStreamSynchronize(0));

@@ -3,9 +3,9 @@
 //
 // Defines the five public functions of the reference's jacobian.h by
 // forwarding to the C ABI: the nodal basis (raster RASTER_NDBASIS), the
-// element basis (RASTER_ELBASIS) and the grid basis of a Raster_Pixel whose
-// intermediate grid equals its basis (the raster toast.Raster(mesh, grd)
-// builds); other rasters stop with xERROR.  The shim Makefile weakens these
+// element basis (RASTER_ELBASIS) and the grid basis of a Raster_Pixel, with
+// or without an intermediate grid (the raster toast.Raster(mesh, grd,
+// intgrd) builds); other rasters stop with xERROR.  The shim Makefile weakens these
 // five symbols in the reference's own jacobian object, which stays linked
 // for the rest of what it holds (ImageGradient, used by the regularisation
 // and raster code), so these definitions take their place.
@@ -29,17 +29,12 @@ using namespace tgshim;
 
 namespace {
 
-// the basis of a raster argument: 0 nodal, 1 element, 2 grid (Raster_Pixel
-// with gdim = bdim)
+// the basis of a raster argument: 0 nodal, 1 element, 2 grid (Raster_Pixel)
 int basis_of(const Raster* raster)
 {
     if (raster == RASTER_NDBASIS) return 0;
     if (raster == RASTER_ELBASIS) return 1;
-    const Raster_Pixel* px = dynamic_cast<const Raster_Pixel*>(raster);
-    if (!px) xERROR("libtoastgpu: only pixel rasters are provided");
-    const IVector &b = px->BDim(), &g = px->GDim();
-    for (int d = 0; d < b.Dim(); d++)
-        if (b[d] != g[d]) xERROR("libtoastgpu: rasters with an intermediate grid (gdim != bdim) are not provided");
+    if (!dynamic_cast<const Raster_Pixel*>(raster)) xERROR("libtoastgpu: only pixel rasters are provided");
     return 2;
 }
 
@@ -70,8 +65,10 @@ void jacobian(const Raster* raster, const QMMesh* mesh, bool cplx, const std::ve
     if (basis == 1) nsol = mesh->elen();
     if (basis == 2) {
         const IVector& b = raster->BDim();
+        const IVector& g = raster->GDim();
         int bdim[3] = {b[0], b[1], b.Dim() > 2 ? b[2] : 1};
-        check(tg_raster_create(gm, bdim, &r), "tg_raster_create");
+        int gdim[3] = {g[0], g[1], g.Dim() > 2 ? g[2] : 1};
+        check(tg_raster_create_ex(gm, bdim, gdim, &r), "tg_raster_create_ex");
         int glen = 0;
         check(tg_raster_info(r, &glen, &nsol, nullptr, nullptr), "tg_raster_info");
     }
