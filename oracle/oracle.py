@@ -85,7 +85,9 @@ def lib():
         L.tor_assemble_el.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, C.c_int, _dp]
         L.tor_jacobian_el.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int, C.c_int, _dp]
         L.tor_gradient_weights.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp]
-        L.tor_gradient_grid.argtypes = [C.c_void_p, _ip, _ip, C.c_int, _dp, _dp, _dp]
+        L.tor_gradient_grid.argtypes = [C.c_void_p, C.c_int, _ip, _ip, C.c_int, _dp, _dp, _dp]
+        L.tor_cubic_map.restype = C.c_int
+        L.tor_cubic_map.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _ip, C.c_int, _ip, C.c_void_p, C.c_void_p]
         L.tor_linpix_map.restype = C.c_int
         L.tor_linpix_map.argtypes = [C.c_int, _ip, _ip, _ip, C.c_int, _ip, C.c_void_p, C.c_void_p]
         L.tor_basis_support.restype = C.c_int
@@ -96,8 +98,8 @@ def lib():
         L.tor_raster_pixel.restype = C.c_int
         L.tor_raster_pixel.argtypes = [C.c_void_p, _ip, _dp, _dp, _ip, _ip, _ip, _dp]
         L.tor_jacobian_grid.restype = C.c_int
-        L.tor_jacobian_grid.argtypes = [C.c_void_p, _ip, _ip, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int,
-                                        C.c_int, _dp]
+        L.tor_jacobian_grid.argtypes = [C.c_void_p, C.c_int, _ip, _ip, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip,
+                                        C.c_int, C.c_int, _dp]
         _lib = L
     return _lib
 
@@ -417,8 +419,9 @@ def jacobian_el(mesh: Mesh, dphi, aphi, proj_lin, link_ofs, link_m, logscale=Tru
 
 
 def data_gradient(mesh: Mesh, bdim, sysval, dphi, mvec, proj_lin, proj_log, link_ofs, link_m, data, sd,
-                  method="BICGSTAB", precon="ICH", tol=1e-15, gdim=None):
-    """toast's Gradient on Raster_Pixel(bdim, gdim) (gdim None: bdim) given
+                  method="BICGSTAB", precon="ICH", tol=1e-15, gdim=None, kind="pixel"):
+    """toast's Gradient on Raster_Pixel(bdim, gdim) (gdim None: bdim; kind
+    "cubic": Raster_CubicPixel) given
     the fields: weights, one adjoint solve per source with the weighted
     detector vectors, then the grid products mapped to the solution basis
     (src/python/toastmodule.cc:1745-1843).  Returns 2 slen."""
@@ -431,9 +434,9 @@ def data_gradient(mesh: Mesh, bdim, sysval, dphi, mvec, proj_lin, proj_log, link
                                np.ascontiguousarray(sd, np.float64), np.ascontiguousarray(link_ofs, np.int32),
                                np.ascontiguousarray(link_m, np.int32), W.view(np.float64).reshape(-1))
     wphi, _, _ = solve(mesh.rowptr, mesh.colidx, sysval, W, method, precon, tol)
-    slen = len(raster_support(mesh, bdim, gdim))
+    slen = len(raster_support(mesh, bdim, gdim, kind))
     grad = np.zeros(2 * slen)
-    lib().tor_gradient_grid(mesh._h, bdim, gdim, nq, _cview(dphi).ravel(), _cview(wphi).ravel(), grad)
+    lib().tor_gradient_grid(mesh._h, _KIND[kind], bdim, gdim, nq, _cview(dphi).ravel(), _cview(wphi).ravel(), grad)
     return grad
 
 
@@ -468,11 +471,18 @@ def raster_pixel(mesh: Mesh, bdim) -> RasterPixel:
     return RasterPixel(bdim, bbmin, bbmax, elref, rp, col[:rp[-1]].copy(), val[:rp[-1]].copy())
 
 
-def raster_support(mesh: Mesh, bdim, gdim=None) -> np.ndarray:
-    """The solution points of Raster_Pixel(bdim, gdim) as basis indices:
+def raster_support(mesh: Mesh, bdim, gdim=None, kind="pixel") -> np.ndarray:
+    """The solution points of the raster as basis indices.  Raster_Pixel:
     without an intermediate grid the grid points inside the mesh; with one,
-    the basis points whose subsampled support is positive (raster.cc:55-77)."""
+    the basis points whose subsampled support is positive (raster.cc:55-77).
+    Raster_CubicPixel: the basis points whose row of G is not empty
+    (raster_cp.cc:170-178)."""
     bdim = np.ascontiguousarray(bdim, np.int32)
+    if kind == "cubic":
+        gdim = bdim if gdim is None else np.ascontiguousarray(gdim, np.int32)
+        r = raster_pixel(mesh, gdim)
+        rp = cubic_map(mesh.dim, gdim, bdim, r.bbmin, r.bbmax, r.elref, False)[0]
+        return np.nonzero(np.diff(rp) > 0)[0].astype(np.int32)
     if gdim is None or np.array_equal(np.asarray(gdim), bdim):
         return raster_pixel(mesh, bdim).sol
     gdim = np.ascontiguousarray(gdim, np.int32)
@@ -495,6 +505,27 @@ def linpix_map(dim, gdim, bdim, elref, by_grid):
     val = np.zeros(max(nz, 1))
     nz = lib().tor_linpix_map(dim, gdim, bdim, elref, int(by_grid), rp, col.ctypes.data_as(C.c_void_p),
                               val.ctypes.data_as(C.c_void_p))
+    return rp, col[:nz].copy(), val[:nz].copy()
+
+
+_KIND = {"pixel": 0, "cubic": 1}
+
+
+def cubic_map(dim, gdim, bdim, bbmin, bbmax, elref, by_grid):
+    """Raster_CubicPixel's G (by_grid False: basis x grid, rows normalised)
+    or GI (True: grid x basis, the basis values at the grid points) as CSR."""
+    gdim = np.ascontiguousarray(gdim, np.int32)
+    bdim = np.ascontiguousarray(bdim, np.int32)
+    elref = np.ascontiguousarray(elref, np.int32)
+    bbmin = np.ascontiguousarray(bbmin, np.float64)
+    bbmax = np.ascontiguousarray(bbmax, np.float64)
+    rows = int(np.prod(gdim if by_grid else bdim))
+    rp = np.zeros(rows + 1, np.int32)
+    nz = lib().tor_cubic_map(dim, gdim, bdim, bbmin, bbmax, elref, int(by_grid), rp, None, None)
+    col = np.zeros(max(nz, 1), np.int32)
+    val = np.zeros(max(nz, 1))
+    lib().tor_cubic_map(dim, gdim, bdim, bbmin, bbmax, elref, int(by_grid), rp, col.ctypes.data_as(C.c_void_p),
+                        val.ctypes.data_as(C.c_void_p))
     return rp, col[:nz].copy(), val[:nz].copy()
 
 
@@ -551,14 +582,16 @@ def _csr_apply_c(rp, col, val, x):
     return _csr_apply(rp, col, val, x.real) + 1j * _csr_apply(rp, col, val, x.imag)
 
 
-def raster_basis_maps(mesh: Mesh, bdim, gdim, mua, mus):
-    """Maps of Raster_Pixel(bdim, gdim) through its basis (toast.Raster.Map,
-    MapBasis src/python/toastmodule.cc:718-790; raster.cc:188-408,
-    raster_px.cc:10-176), on the vectors the reference driver maps: real
-    M->B (C = G B), B->M (CI = BI GI) of b + 1, G->B of the grid image of
-    mua, B->G (GI) of b + 1, G->S, S->G (GI of the scatter) of s + 1, and the
-    complex M->S (G after B, then the support) of mua + i mus and S->M (GI
-    then BI) of (s + 1) - 0.5 i s.  Also the solution points (sol2basis)."""
+def raster_basis_maps(mesh: Mesh, bdim, gdim, mua, mus, kind="pixel"):
+    """Maps of Raster_Pixel(bdim, gdim) (kind "cubic": Raster_CubicPixel)
+    through its basis (toast.Raster.Map, MapBasis src/python/toastmodule.cc:
+    718-790; raster.cc:188-408, raster_px.cc:10-176, raster_cp.cc:266-302),
+    on the vectors the reference driver maps: real M->B, B->M of b + 1, G->B
+    of the grid image of mua, B->G of b + 1, G->S, S->G of s + 1, and the
+    complex M->S of mua + i mus and S->M of (s + 1) - 0.5 i s.  The pixel
+    raster's real maps use its products C = G B, CI = BI GI and the support
+    map D (0 + 1 x); everything else runs the base class's chains through the
+    grid.  Also the solution points (sol2basis)."""
     bdim = np.ascontiguousarray(bdim, np.int32)
     gdim = np.ascontiguousarray(gdim, np.int32)
     r = raster_pixel(mesh, gdim)
@@ -570,31 +603,45 @@ def raster_basis_maps(mesh: Mesh, bdim, gdim, mua, mus):
     lib().tor_node_map(mesh._h, gdim, r.bbmin, r.bbmax, r.elref, nrp, ncol, nval)
     BI = (nrp, ncol[:nrp[-1]].copy(), nval[:nrp[-1]].copy())
     B = (r.browptr, r.bcol, r.bval)
-    G = linpix_map(mesh.dim, gdim, bdim, r.elref, False)
-    GI = linpix_map(mesh.dim, gdim, bdim, r.elref, True)
-    Cm = csr_ab(G, B, n)
-    CI = csr_ab(BI, GI, blen)
-    sol = raster_support(mesh, bdim, gdim)
+    if kind == "cubic":
+        G = cubic_map(mesh.dim, gdim, bdim, r.bbmin, r.bbmax, r.elref, False)
+        GI = cubic_map(mesh.dim, gdim, bdim, r.bbmin, r.bbmax, r.elref, True)
+    else:
+        G = linpix_map(mesh.dim, gdim, bdim, r.elref, False)
+        GI = linpix_map(mesh.dim, gdim, bdim, r.elref, True)
+    sol = raster_support(mesh, bdim, gdim, kind)
     slen = len(sol)
-    D = (np.arange(slen + 1, dtype=np.int32), sol, np.ones(slen))
 
-    def DT(s):  # D->ATx: 0 + 1 s at the solution points
+    def sel(b):  # Map_BasisToSol: the pixel raster's D->Ax, else a copy
+        return b[sol] + 0.0 if kind == "pixel" else (b if slen == blen else b[sol])
+
+    def sct(sv):  # Map_SolToBasis: the pixel raster's D->ATx, else a scatter
+        if kind != "pixel" and slen == blen:
+            return np.asarray(sv, float)
         b = np.zeros(blen)
-        b[sol] += 1.0 * np.asarray(s)
+        b[sol] += 1.0 * np.asarray(sv)
         return b
 
+    if kind == "pixel":
+        Cm = csr_ab(G, B, n)
+        CI = csr_ab(BI, GI, blen)
+        m2b = lambda m: _csr_apply(*Cm, m)  # noqa: E731
+        b2m = lambda b: _csr_apply(*CI, b)  # noqa: E731
+    else:
+        m2b = lambda m: _csr_apply(*G, _csr_apply(*B, m))  # noqa: E731
+        b2m = lambda b: _csr_apply(*BI, _csr_apply(*GI, b))  # noqa: E731
     bvec = np.arange(1, blen + 1, dtype=float)
     svec = np.arange(1, slen + 1, dtype=float)
     m2g = _csr_apply(*B, mua)
     out = dict(sol2basis=sol,
-               m2b=_csr_apply(*Cm, mua),
-               b2m=_csr_apply(*CI, bvec),
+               m2b=m2b(mua),
+               b2m=b2m(bvec),
                g2b=_csr_apply(*G, m2g),
                b2g=_csr_apply(*GI, bvec),
-               g2s=_csr_apply(*D, _csr_apply(*G, m2g)),
-               s2g=_csr_apply(*GI, DT(svec)),
-               m2s=_csr_apply(*D, _csr_apply(*Cm, mua)),
-               s2m=_csr_apply(*CI, DT(svec)))
+               g2s=sel(_csr_apply(*G, m2g)),
+               s2g=_csr_apply(*GI, sct(svec)),
+               m2s=sel(m2b(mua)),
+               s2m=b2m(sct(svec)))
     cm = np.asarray(mua) + 1j * np.asarray(mus)
     cb = _csr_apply_c(*G, _csr_apply_c(*B, cm))
     out["cm2s"] = cb if slen == blen else cb[sol]
@@ -608,19 +655,21 @@ def raster_basis_maps(mesh: Mesh, bdim, gdim, mua, mus):
     return out
 
 
-def jacobian_grid(mesh: Mesh, bdim, dphi, aphi, proj_lin, link_ofs, link_m, logscale=True, gdim=None):
-    """Grid-basis Jacobian for Raster_Pixel(bdim, gdim) (gdim None: bdim):
-    complex (2 nQM) x (2 slen), real (2 nQM) x slen."""
+def jacobian_grid(mesh: Mesh, bdim, dphi, aphi, proj_lin, link_ofs, link_m, logscale=True, gdim=None,
+                  kind="pixel"):
+    """Grid-basis Jacobian for Raster_Pixel(bdim, gdim) (gdim None: bdim;
+    kind "cubic": Raster_CubicPixel): complex (2 nQM) x (2 slen), real
+    (2 nQM) x slen."""
     cplx = np.iscomplexobj(dphi)
     bdim = np.ascontiguousarray(bdim, np.int32)
     gdim = bdim if gdim is None else np.ascontiguousarray(gdim, np.int32)
     nq, n = dphi.shape
     nm = aphi.shape[0]
     nqm = int(link_ofs[-1])
-    slen = len(raster_support(mesh, bdim, gdim))
+    slen = len(raster_support(mesh, bdim, gdim, kind))
     J = np.zeros((2 * nqm, 2 * slen) if cplx else (2 * nqm, slen))
     f = (lambda a: _cview(a).ravel()) if cplx else (lambda a: np.ascontiguousarray(a, np.float64).ravel())
-    lib().tor_jacobian_grid(mesh._h, bdim, gdim, nq, nm, f(dphi), f(aphi), f(proj_lin),
+    lib().tor_jacobian_grid(mesh._h, _KIND[kind], bdim, gdim, nq, nm, f(dphi), f(aphi), f(proj_lin),
                             np.ascontiguousarray(link_ofs, np.int32), np.ascontiguousarray(link_m, np.int32),
                             int(cplx), int(logscale), J.reshape(-1))
     return J

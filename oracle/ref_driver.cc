@@ -35,7 +35,8 @@
 //              point (PREFIX_Jgrid.bin, PREFIX_elref.bin).  gdim=NX,NY[,NZ]
 //              gives the intermediate grid (default: the basis grid); with
 //              it the solution points' basis indices (PREFIX_sol2basis.bin)
-//              and the maps through the basis are written too.
+//              and the maps through the basis are written too.  raster=cubic
+//              builds a Raster_CubicPixel(bdim, gdim) instead.
 // qmdump     : with qm, write what QMMesh::LoadQM (qmmesh.cc:319-460, with
 //              InitM's detector placement) made of the file and stop:
 //              PREFIX_qpos.bin, PREFIX_mpos.bin (nQ / nM x dim doubles),
@@ -47,6 +48,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -213,6 +215,14 @@ static void ref_data_gradient(QMMesh& mesh, Raster& raster, CFwdSolver& FWS, con
         omod += nl;
         oarg += nl;
     }
+}
+
+// the raster of the grid arguments: Raster_Pixel, or Raster_CubicPixel
+// (raster_cp.cc) with raster=cubic
+static Raster* make_raster(const IVector& bdim, const IVector& gdim, QMMesh& mesh)
+{
+    if (arg("raster", "pixel") == "cubic") return new Raster_CubicPixel(bdim, gdim, &mesh);
+    return new Raster_Pixel(bdim, gdim, &mesh);
 }
 
 int main(int argc, char** argv) {
@@ -403,7 +413,8 @@ int main(int argc, char** argv) {
             if ((int)grid.size() == dim) {
                 IVector bdim(dim, grid.data());
                 IVector gdim(dim, ((int)igrid.size() == dim ? igrid : grid).data());
-                Raster_Pixel raster(bdim, gdim, &mesh);
+                std::unique_ptr<Raster> rowner(make_raster(bdim, gdim, mesh));
+                Raster& raster = *rowner;
                 int slen = raster.SLen(), glen = raster.GLen();
                 RDenseMatrix Jg(2 * nQM, 2 * slen);
                 GenerateJacobian(&raster, &mesh, dphi, aphi, &proj, DATA_LOG, Jg);
@@ -411,7 +422,8 @@ int main(int argc, char** argv) {
                 wbin(out + "_elref.bin", raster.Elref(), (size_t)glen * sizeof(int));
                 fprintf(info, "slen %d\nglen %d\n", slen, glen);
                 write_maps(raster, mua, out);
-                if ((int)igrid.size() == dim) write_basis_maps(raster, mua, mus, out);
+                if ((int)igrid.size() == dim || arg("raster", "pixel") == "cubic")
+                    write_basis_maps(raster, mua, mus, out);
                 if (g_args.count("data")) {
                     std::vector<char> db = rbin(arg("data", "")), sb = rbin(arg("sd", ""));
                     RVector data(2 * nQM, (double*)db.data()), sd(2 * nQM, (double*)sb.data());
@@ -492,7 +504,8 @@ int main(int argc, char** argv) {
             if ((int)grid.size() == dim) {
                 IVector bdim(dim, grid.data());
                 IVector gdim(dim, ((int)igrid.size() == dim ? igrid : grid).data());
-                Raster_Pixel raster(bdim, gdim, &mesh);
+                std::unique_ptr<Raster> rowner(make_raster(bdim, gdim, mesh));
+                Raster& raster = *rowner;
                 int slen = raster.SLen(), glen = raster.GLen();
                 RDenseMatrix Jmua, Jkap;
                 GenerateJacobian_cw(&raster, &mesh, dphi, aphi, &proj, DATA_LOG, &Jmua, &Jkap);
@@ -503,7 +516,8 @@ int main(int argc, char** argv) {
                 wbin(out + "_elref.bin", raster.Elref(), (size_t)glen * sizeof(int));
                 fprintf(info, "slen %d\nglen %d\n", slen, glen);
                 write_maps(raster, mua, out);
-                if ((int)igrid.size() == dim) write_basis_maps(raster, mua, mus, out);
+                if ((int)igrid.size() == dim || arg("raster", "pixel") == "cubic")
+                    write_basis_maps(raster, mua, mus, out);
             }
         }
         if (want_fields) {

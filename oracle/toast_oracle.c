@@ -1883,6 +1883,116 @@ int tor_basis_support(int dim, const int *gdim, const int *bdim, const int *elre
     return slen;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Raster_CubicPixel (raster_cp.cc): the cubic B-spline basis                */
+/* ------------------------------------------------------------------------ */
+
+/* The cubic B-spline weight at distance dr (in basis spacings), in the
+   reference's form (raster_cp.cc:57-62, 204-209) */
+static double cubic_weight(double dr)
+{
+    double dm2 = dr - 2.0, dm1 = dr - 1.0, dp1 = dr + 1.0, dp2 = dr + 2.0;
+    return (fabs(dm2 * dm2 * dm2) - 4.0 * fabs(dm1 * dm1 * dm1) + 6.0 * fabs(dr * dr * dr) -
+            4.0 * fabs(dp1 * dp1 * dp1) + fabs(dp2 * dp2 * dp2)) / 12.0;
+}
+
+/* The maps of Raster_CubicPixel(bdim, gdim) (raster_cp.cc:10-186).
+   by_grid 0: G, blen x glen: row b holds the grid points inside the mesh
+   (elref >= 0) in the axis-wise support window of b with a positive
+   product of the axis weights (dr = |b_k - (j / iggrid) ibgrid|, < 2), in
+   grid order, each divided by the row's sum.  by_grid 1: GI, glen x blen:
+   row g (grid points inside the mesh only) holds Raster_CubicPixel::Value
+   (raster_cp.cc:189-214) of every basis point at the grid point, nonzero
+   ones in basis order.  ibgrid = (bdim - 1) / bbsize, iggrid = (gdim - 1) /
+   bbsize.  col / val NULL: count only.  Returns the entry count. */
+int tor_cubic_map(int dim, const int *gdim, const int *bdim, const double *bbmin, const double *bbmax,
+                  const int *elref, int by_grid, int *rowptr, int *col, double *val)
+{
+    int glen = 1, blen = 1;
+    for (int d = 0; d < dim; d++) { glen *= gdim[d]; blen *= bdim[d]; }
+    double ib[3], ig[3];
+    for (int d = 0; d < dim; d++) {
+        ib[d] = (bdim[d] - 1) / (bbmax[d] - bbmin[d]);
+        ig[d] = (gdim[d] - 1) / (bbmax[d] - bbmin[d]);
+    }
+    int nz = 0;
+    rowptr[0] = 0;
+    if (!by_grid) {
+        double *sw[3], *grow = calloc(glen, sizeof(double));
+        for (int d = 0; d < dim; d++) sw[d] = calloc(gdim[d], sizeof(double));
+        for (int i = 0; i < blen; i++) {
+            int bg[3] = {0, 0, 0}, r = i;
+            if (dim == 3) { bg[2] = r / (bdim[0] * bdim[1]); r -= bg[2] * bdim[0] * bdim[1]; }
+            bg[0] = r % bdim[0];
+            bg[1] = r / bdim[0];
+            int imin[3] = {100000, 100000, 0}, imax[3] = {-1, -1, 0};
+            for (int k = 0; k < dim; k++) {
+                imin[k] = 100000; imax[k] = -1;
+                for (int j = 0; j < gdim[k]; j++) {
+                    double dr = fabs(bg[k] - (j / ig[k]) * ib[k]);
+                    if (fabs(dr) < 2.0) {
+                        sw[k][j] = cubic_weight(dr);
+                        if (j < imin[k]) imin[k] = j;
+                        if (j > imax[k]) imax[k] = j;
+                    }
+                }
+            }
+            double gsum = 0.0;
+            for (int jz = imin[2]; jz <= imax[2]; jz++)
+                for (int jy = imin[1]; jy <= imax[1]; jy++)
+                    for (int jx = imin[0]; jx <= imax[0]; jx++) {
+                        int j = gdim[0] * gdim[1] * jz + jy * gdim[0] + jx, gr[3] = {jx, jy, jz};
+                        if (elref[j] < 0) continue;
+                        double v = 1.0;
+                        for (int k = 0; k < dim; k++) v *= sw[k][gr[k]];
+                        if (v > 0) { grow[j] = v; gsum += v; }
+                    }
+            for (int jz = imin[2]; jz <= imax[2]; jz++)
+                for (int jy = imin[1]; jy <= imax[1]; jy++)
+                    for (int jx = imin[0]; jx <= imax[0]; jx++) {
+                        int j = gdim[0] * gdim[1] * jz + jy * gdim[0] + jx;
+                        if (grow[j] != 0.0) {
+                            if (col) { col[nz] = j; val[nz] = grow[j] / gsum; }
+                            nz++;
+                            grow[j] = 0.0;
+                        }
+                    }
+            rowptr[i + 1] = nz;
+        }
+        for (int d = 0; d < dim; d++) free(sw[d]);
+        free(grow);
+    } else {
+        for (int j = 0; j < glen; j++) {
+            if (elref[j] >= 0) {
+                int gg[3] = {0, 0, 0}, r = j;
+                if (dim == 3) { gg[2] = r / (gdim[0] * gdim[1]); r -= gg[2] * gdim[0] * gdim[1]; }
+                gg[0] = r % gdim[0];
+                gg[1] = r / gdim[0];
+                double p[3];
+                for (int k = 0; k < dim; k++) p[k] = bbmin[k] + gg[k] / ig[k];
+                for (int i = 0; i < blen; i++) {
+                    int bg[3] = {0, 0, 0}, t = i;
+                    if (dim == 3) { bg[2] = t / (bdim[0] * bdim[1]); t -= bg[2] * bdim[0] * bdim[1]; }
+                    bg[0] = t % bdim[0];
+                    bg[1] = t / bdim[0];
+                    double v = 1.0;
+                    for (int k = 0; k < dim; k++) {
+                        double dr = fabs(bg[k] + (bbmin[k] - p[k]) * ib[k]);
+                        if (dr >= 2.0) { v = 0.0; break; }
+                        v *= cubic_weight(dr);
+                    }
+                    if (v != 0.0) {
+                        if (col) { col[nz] = i; val[nz] = v; }
+                        nz++;
+                    }
+                }
+            }
+            rowptr[j + 1] = nz;
+        }
+    }
+    return nz;
+}
+
 /* The grid -> solution map of a Raster_Pixel (Map_GridToSol, raster.cc:
    374-390): with an intermediate grid, G (Grid2LinPixMatrix) applied to the
    grid vector (RCompRowMatrix::Ax / Ax_cplx, crmatrix_imp.hpp:1173-1190,
@@ -1890,7 +2000,7 @@ int tor_basis_support(int dim, const int *gdim, const int *bdim, const int *elre
    basis values; without (G NULL) the grid values at the solution points.
    The real path's selection is D->Ax (raster_px.cc:147-150), 0 + 1 x. */
 typedef struct {
-    int slen, blen;
+    int slen, blen, kind;
     const int *sol;                   /* grid index (G NULL) or basis index per solution point */
     const int *grp, *gcol;            /* G: blen x glen, or NULL */
     const double *gval;
@@ -1915,33 +2025,48 @@ static void grid_to_sol(const grid2sol_t *M, const zd *x, int cplx, zd *out)
         }
         b = M->tmp;
     }
-    for (int k = 0; k < M->slen; k++) out[k] = cplx ? b[M->sol[k]] : 0.0 + 1.0 * creal(b[M->sol[k]]);
+    /* the pixel raster's real map is D->Ax; the cubic raster's the base
+       class's copy (raster.cc:292-303) */
+    for (int k = 0; k < M->slen; k++)
+        out[k] = (cplx || M->kind) ? b[M->sol[k]] : 0.0 + 1.0 * creal(b[M->sol[k]]);
 }
 
-/* the raster's grid -> solution map for basis bdim on grid gdim (equal:
-   no G); allocates into M (free with grid2sol_free) */
-static void grid2sol_init(int dim, const int *bdim, const int *gdim, const int *elref, grid2sol_t *M)
+/* the raster's grid -> solution map for basis bdim on grid gdim: kind 0
+   Raster_Pixel (no G when the grids are equal; else the linear pixel map
+   and the subsampled support), kind 1 Raster_CubicPixel (its G; the
+   solution points are the basis points whose row of G is not empty,
+   raster_cp.cc:170-178).  Allocates into M (free with grid2sol_free). */
+static void grid2sol_init(int dim, int kind, const int *bdim, const int *gdim, const double *bbmin,
+                          const double *bbmax, const int *elref, grid2sol_t *M)
 {
     int glen = 1, blen = 1, same = 1;
     for (int d = 0; d < dim; d++) { glen *= gdim[d]; blen *= bdim[d]; same &= gdim[d] == bdim[d]; }
-    int *sol = malloc(sizeof(int) * (same ? glen : blen));
+    int *sol = malloc(sizeof(int) * (same ? glen : blen) + sizeof(int) * blen);
     M->blen = blen;
     M->grp = M->gcol = NULL;
     M->gval = NULL;
     M->tmp = NULL;
-    if (same) {
+    if (same && kind == 0) {
         M->slen = 0;
         for (int g = 0; g < glen; g++) if (elref[g] >= 0) sol[M->slen++] = g;
     } else {
-        M->slen = tor_basis_support(dim, gdim, bdim, elref, sol);
         int *rp = malloc(sizeof(int) * (blen + 1));
-        int nz = tor_linpix_map(dim, gdim, bdim, elref, 0, rp, NULL, NULL);
+        int nz = kind ? tor_cubic_map(dim, gdim, bdim, bbmin, bbmax, elref, 0, rp, NULL, NULL)
+                      : tor_linpix_map(dim, gdim, bdim, elref, 0, rp, NULL, NULL);
         int *col = malloc(sizeof(int) * (nz > 0 ? nz : 1));
         double *val = malloc(sizeof(double) * (nz > 0 ? nz : 1));
-        tor_linpix_map(dim, gdim, bdim, elref, 0, rp, col, val);
+        if (kind) tor_cubic_map(dim, gdim, bdim, bbmin, bbmax, elref, 0, rp, col, val);
+        else tor_linpix_map(dim, gdim, bdim, elref, 0, rp, col, val);
         M->grp = rp; M->gcol = col; M->gval = val;
         M->tmp = malloc(sizeof(zd) * blen);
+        if (kind) {
+            M->slen = 0;
+            for (int b = 0; b < blen; b++) if (rp[b + 1] > rp[b]) sol[M->slen++] = b;
+        } else {
+            M->slen = tor_basis_support(dim, gdim, bdim, elref, sol);
+        }
     }
+    M->kind = kind;
     M->sol = sol;
 }
 
@@ -1950,7 +2075,8 @@ static void grid2sol_free(grid2sol_t *M)
     free((void *)M->sol); free((void *)M->grp); free((void *)M->gcol); free((void *)M->gval); free(M->tmp);
 }
 
-/* Grid-basis Jacobian for Raster_Pixel(bdim, gdim): the fields mapped on the
+/* Grid-basis Jacobian for Raster_Pixel(bdim, gdim) (kind 0) or
+   Raster_CubicPixel(bdim, gdim) (kind 1): the fields mapped on the
    grid gdim (Map_MeshToGrid), their image gradients on it, the PMDFs per
    grid point, then Map_GridToSol into the solution basis.
    Complex (GenerateJacobian_grid with projections, jacobian.cc:289-373):
@@ -1963,9 +2089,9 @@ static void grid2sol_free(grid2sol_t *M)
    nQM + l) mapped, times the voxel scale, then, for LOG data, each row times
    1/y (GenerateJacobian_cw, 178-193).
    J: complex (2 nQM) x (2 slen), real (2 nQM) x slen.  Returns slen. */
-int tor_jacobian_grid(const tor_mesh *m, const int *bdim, const int *gdim, int nq, int nm, const double *dphi,
-                      const double *aphi, const double *proj, const int *link_ofs, const int *link_m, int cplx,
-                      int logscale, double *J)
+int tor_jacobian_grid(const tor_mesh *m, int kind, const int *bdim, const int *gdim, int nq, int nm,
+                      const double *dphi, const double *aphi, const double *proj, const int *link_ofs,
+                      const int *link_m, int cplx, int logscale, double *J)
 {
     const int dim = m->dim, nn = m->nn, n = m->n;
     int glen = 1;
@@ -1977,7 +2103,7 @@ int tor_jacobian_grid(const tor_mesh *m, const int *bdim, const int *gdim, int n
     tor_raster_pixel(m, gdim, bbmin, bbmax, elref, browptr, bcol, bval);
     for (int d = 0; d < dim; d++) gsize[d] = bbmax[d] - bbmin[d];
     grid2sol_t M;
-    grid2sol_init(dim, bdim, gdim, elref, &M);
+    grid2sol_init(dim, kind, bdim, gdim, bbmin, bbmax, elref, &M);
     const int slen = M.slen;
     const int nqm = link_ofs[nq];
     zd *fin = malloc(sizeof(zd) * n);
@@ -2123,7 +2249,7 @@ void tor_gradient_weights(int nq, int n, const double *mvec, const double *ylin,
    gdim, their masked image gradients, then grad_mua -= Re(Map_GridToSol(f a))
    and grad_kappa -= Re(Map_GridToSol(sum_d grad_d f grad_d a)) (no voxel
    scaling).  dphi, wphi: nq x n complex; grad: 2 slen, in/out. */
-void tor_gradient_grid(const tor_mesh *m, const int *bdim, const int *gdim, int nq, const double *dphi,
+void tor_gradient_grid(const tor_mesh *m, int kind, const int *bdim, const int *gdim, int nq, const double *dphi,
                        const double *wphi, double *grad)
 {
     const int dim = m->dim, nn = m->nn, n = m->n;
@@ -2136,7 +2262,7 @@ void tor_gradient_grid(const tor_mesh *m, const int *bdim, const int *gdim, int 
     tor_raster_pixel(m, gdim, bbmin, bbmax, elref, browptr, bcol, bval);
     for (int d = 0; d < dim; d++) gsize[d] = bbmax[d] - bbmin[d];
     grid2sol_t M;
-    grid2sol_init(dim, bdim, gdim, elref, &M);
+    grid2sol_init(dim, kind, bdim, gdim, bbmin, bbmax, elref, &M);
     const int slen = M.slen;
     zd *df = malloc(sizeof(zd) * glen), *af = malloc(sizeof(zd) * glen), *pr = malloc(sizeof(zd) * glen);
     zd *dg = malloc(sizeof(zd) * (size_t)dim * glen), *ag = malloc(sizeof(zd) * (size_t)dim * glen);

@@ -22,6 +22,10 @@ intgrd)): the grid Jacobian is mapped from the fine grid to the basis, and
 the fixtures add the solution points' basis indices and the maps through
 the basis.
 
+The *_cgrid fixtures (and *_cgrad) use the cubic pixel basis
+(Raster_CubicPixel, raster_cp.cc) on its basis grid or on an intermediate
+grid, with the same contents.
+
 The *_el fixtures reset the solver in the element basis (one mua, mus',
 nref per element, seeded) and hold the reference's system matrix, fields,
 projections and element-basis Jacobian.
@@ -104,6 +108,18 @@ FIXTURES = {
                      (14, 12, 11)),
     "disc_fd_igrad": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (10, 10), False,
                       True, (28, 28)),
+    # Raster_CubicPixel (cubic B-spline basis), on its basis grid or an
+    # intermediate grid
+    "disc_cw_cgrid": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "ICH", 1e-15, False, (14, 14), False, False,
+                      (14, 14), "cubic"),
+    "disc_fd_cgrid": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (10, 9), False,
+                      False, (27, 25), "cubic"),
+    "cyl_cw_cgrid": (lambda: small_cylinder(0.0), "CG", "ICH", 1e-15, False, (5, 6, 6), False, False, (11, 12, 13),
+                     "cubic"),
+    "cyl_fd_cgrid": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-15, False, (6, 6, 5), False, False,
+                     (6, 6, 5), "cubic"),
+    "disc_fd_cgrad": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (9, 9), False,
+                      True, (25, 25), "cubic"),
 }
 
 
@@ -133,7 +149,8 @@ def synthetic_data(logproj, seed=17):
     return data, sd
 
 
-def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradient=False, gdim=None):
+def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradient=False, gdim=None,
+        raster="pixel"):
     P = factory()
     cplx = P.complex
     with tempfile.TemporaryDirectory() as td:
@@ -154,6 +171,8 @@ def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradi
             args += ["grid=" + ",".join(str(g) for g in grid), "fields=1"]
         if gdim:
             args += ["gdim=" + ",".join(str(g) for g in gdim)]
+        if raster != "pixel":
+            args += [f"raster={raster}"]
         if elbasis:
             emua, emus, eref = element_params(P)
             epar = os.path.join(td, "elpar.bin")
@@ -198,6 +217,8 @@ def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradi
                 res["map_" + key] = rd(out + f"_{key}.bin", np.float64)
             res["elref"] = rd(out + "_elref.bin", np.int32)
             res["bdim"] = np.array(grid, np.int32)
+            if raster != "pixel":
+                res["raster"] = raster
             if gdim:
                 res["gdim"] = np.array(gdim, np.int32)
                 res["sol2basis"] = rd(out + "_sol2basis.bin", np.int32)

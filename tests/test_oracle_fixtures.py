@@ -35,32 +35,34 @@ IGRID = [n for n in names() if "gdim" in load(n)]
 
 @pytest.mark.parametrize("name", GRID + IGRID)
 def test_oracle_grid_jacobian_matches_reference(oracle_mod, name):
-    """Raster_Pixel (basis = grid, or an intermediate grid) and the
-    grid-basis Jacobian on the reference's own fields: the element reference
-    per grid point, the solution points and every Jacobian entry equal the
-    reference's bit for bit."""
+    """Raster_Pixel (basis = grid, or an intermediate grid), Raster_CubicPixel,
+    and the grid-basis Jacobian on the reference's own fields: the element
+    reference per grid point, the solution points and every Jacobian entry
+    equal the reference's bit for bit."""
     g = load(name)
     mesh = oracle_mod.Mesh(g["coords"], g["elems"])
-    gdim = g.get("gdim")
+    gdim, kind = g.get("gdim"), str(g.get("raster", "pixel"))
     r = oracle_mod.raster_pixel(mesh, g["bdim"] if gdim is None else gdim)
     assert np.array_equal(r.elref, g["elref"])
     if gdim is not None:
-        assert np.array_equal(oracle_mod.raster_support(mesh, g["bdim"], gdim), g["sol2basis"])
+        assert np.array_equal(oracle_mod.raster_support(mesh, g["bdim"], gdim, kind), g["sol2basis"])
     J = oracle_mod.jacobian_grid(mesh, g["bdim"], g["dphi"], g["aphi"], g["proj"], g["link_ofs"], g["link_m"],
-                                 gdim=gdim)
+                                 gdim=gdim, kind=kind)
     assert J.shape == g["Jgrid"].shape
     assert np.array_equal(J, g["Jgrid"])
 
 
 @pytest.mark.parametrize("name", IGRID)
 def test_oracle_basis_maps_match_reference(oracle_mod, name):
-    """With an intermediate grid the maps through the basis (Grid2LinPix G,
-    LinPix2Grid GI, the products C = G B and CI = BI GI in the reference's
-    entry order, the support D) equal the reference's bit for bit, the
-    complex M->S / S->M (run through the grid) included."""
+    """With an intermediate grid (or the cubic basis) the maps through the
+    basis (Grid2LinPix G, LinPix2Grid GI, the products C = G B and CI = BI GI
+    in the reference's entry order, the support D; the cubic raster's G and
+    GI) equal the reference's bit for bit, the complex M->S / S->M (run
+    through the grid) included."""
     g = load(name)
     mesh = oracle_mod.Mesh(g["coords"], g["elems"])
-    maps = oracle_mod.raster_basis_maps(mesh, g["bdim"], g["gdim"], g["mua"], g["mus"])
+    maps = oracle_mod.raster_basis_maps(mesh, g["bdim"], g["gdim"], g["mua"], g["mus"],
+                                        str(g.get("raster", "pixel")))
     for key in ("m2b", "b2m", "g2b", "b2g", "g2s", "s2g", "m2s", "s2m", "cm2s", "cs2m"):
         assert np.array_equal(maps[key], g["map_" + key]), key
 
@@ -83,7 +85,7 @@ def test_oracle_element_basis_matches_reference(oracle_mod, name):
     assert np.array_equal(J, g["Jel"])
 
 
-GRAD = [n for n in names() if n.endswith("_grad") or n.endswith("_igrad")]
+GRAD = [n for n in names() if n.endswith(("_grad", "_igrad", "_cgrad"))]
 
 
 @pytest.mark.parametrize("name", GRAD)
@@ -98,7 +100,7 @@ def test_oracle_data_gradient_matches_reference(oracle_mod, name):
     mvec = np.stack([m.qvec_gaussian(x, g["mwidth"]) * ca for x in g["M"]]).astype(np.complex128)
     grad = oracle_mod.data_gradient(m, g["bdim"], val, g["dphi"], mvec, g["proj"], g["logproj"], g["link_ofs"],
                                     g["link_m"], g["data"], g["sd"], g["solver"], g["precon"], g["tol"],
-                                    gdim=g.get("gdim"))
+                                    gdim=g.get("gdim"), kind=str(g.get("raster", "pixel")))
     assert np.array_equal(grad, g["grad"])
 
 
