@@ -346,10 +346,19 @@ int tg_jacobian_el(tg_solver s, int nq, const double *dphi, int nm, const double
    3540-3640) and the solution points are the basis points whose subsampled
    mesh support is positive (SubsampleLinPixel, mesh.cc:3047-3136), in basis
    order.  tg_raster_create(mesh, bdim, out) = tg_raster_create_ex(mesh,
-   bdim, NULL, out). */
+   bdim, NULL, out).
+   tg_raster_create_typed with TG_RASTER_CUBICPIXEL builds
+   Raster_CubicPixel(bdim, gdim) (src/libstoast/raster_cp.cc:10-186): the
+   cubic B-spline basis, joined to the grid by its own G (normalised spline
+   weights of the grid points inside the mesh) and GI (the basis functions'
+   values at the grid points); its solution points are the basis points with
+   a nonempty row of G. */
+#define TG_RASTER_PIXEL 0
+#define TG_RASTER_CUBICPIXEL 1
 typedef struct tg_raster_s *tg_raster;
 int tg_raster_create(tg_mesh mesh, const int *bdim, tg_raster *out);
 int tg_raster_create_ex(tg_mesh mesh, const int *bdim, const int *gdim, tg_raster *out);
+int tg_raster_create_typed(tg_mesh mesh, int type, const int *bdim, const int *gdim, tg_raster *out);
 int tg_raster_destroy(tg_raster r);
 /* glen grid points, slen solution points, bounding box (dim values each) */
 int tg_raster_info(tg_raster r, int *glen, int *slen, double *bbmin, double *bbmax);
@@ -363,9 +372,9 @@ int tg_raster_basis(tg_raster r, int *blen, int *sol2basis);
    without an intermediate grid) and S (solution points); nvec vectors back
    to back, width doubles per point (1 real, 2 complex interleaved); src,
    dst in host or device memory.  Each map runs the chain the reference's
-   raster runs for that vector type (real: the pixel raster's product maps
-   G B and BI GI; complex: through the grid), summing in the reference's
-   order without fused multiply-adds (bit-identical). */
+   raster runs for that vector type (the pixel raster's real vectors: its
+   product maps G B and BI GI; otherwise through the grid), summing in the
+   reference's order without fused multiply-adds (bit-identical). */
 int tg_raster_map(tg_raster r, const char *map, int nvec, const double *src, double *dst, int width, int mem);
 /* Grid-basis Jacobian (GenerateJacobian with a raster, jacobian.cc:105-123
    -> GenerateJacobian_grid 289-373; real systems GenerateJacobian_cw with a

@@ -303,6 +303,29 @@ private:
     int glen_ = 0, blen_ = 0, slen_ = 0;
 };
 
+// Raster_CubicPixel(bdim, gdim, mesh) (src/libstoast/raster_cp.cc): the
+// cubic B-spline basis of bdim points over a grid of gdim points
+class Raster_CubicPixel {
+public:
+    Raster_CubicPixel(const int* bdim, const int* gdim, const Mesh& mesh)
+    {
+        check(tg_raster_create_typed(mesh.handle(), TG_RASTER_CUBICPIXEL, bdim, gdim, &h_));
+        check(tg_raster_info(h_, &glen_, &slen_, nullptr, nullptr));
+        check(tg_raster_basis(h_, &blen_, nullptr));
+    }
+    ~Raster_CubicPixel() { tg_raster_destroy(h_); }
+    Raster_CubicPixel(const Raster_CubicPixel&) = delete;
+    Raster_CubicPixel& operator=(const Raster_CubicPixel&) = delete;
+    int GLen() const { return glen_; }
+    int BLen() const { return blen_; }
+    int SLen() const { return slen_; }
+    tg_raster handle() const { return h_; }
+
+private:
+    tg_raster h_ = nullptr;
+    int glen_ = 0, blen_ = 0, slen_ = 0;
+};
+
 // GenerateJacobian(raster, mesh, dphi, aphi, proj, dscale, J) grid basis:
 // complex J (2 nQM) x (2 SLen) row-major [Re mua | Re kappa ; Im mua | Im
 // kappa] (jacobian.cc:289-373); real J (2 nQM) x SLen [mua ; kappa]

@@ -14,18 +14,24 @@ pytestmark = pytest.mark.gpu
 GRID = [n for n in names() if n.endswith("_grid")]
 # Raster_Pixel with an intermediate grid finer than the basis
 IGRID = [n for n in names() if n.endswith("_igrid")]
+# Raster_CubicPixel, on its basis grid or an intermediate grid
+CGRID = [n for n in names() if n.endswith("_cgrid")]
+
+
+def kind(g):
+    return str(g.get("raster", "pixel"))
 
 
 def setup(name):
     g = load(name)
     gm = capi.Mesh(g["coords"], g["elems"])
-    r = capi.Raster(gm, g["bdim"], g.get("gdim"))
+    r = capi.Raster(gm, g["bdim"], g.get("gdim"), kind=kind(g))
     cplx = np.iscomplexobj(g["proj"])
     s = capi.FwdSolver(gm, g["solver"], 1e-15, g["precon"], cplx, precision="fp64")
     return g, gm, r, s, capi.Links(g["link_ofs"], g["link_m"])
 
 
-@pytest.mark.parametrize("name", GRID + IGRID)
+@pytest.mark.parametrize("name", GRID + IGRID + CGRID)
 def test_raster_matches_reference(name):
     g, gm, r, s, L = setup(name)
     assert r.glen == int(np.prod(g.get("gdim", g["bdim"])))
@@ -38,7 +44,7 @@ def test_raster_matches_reference(name):
         assert np.array_equal(r.sol2basis(), np.nonzero(g["elref"] >= 0)[0])
 
 
-@pytest.mark.parametrize("name", GRID + IGRID)
+@pytest.mark.parametrize("name", GRID + IGRID + CGRID)
 def test_grid_jacobian_on_reference_fields(name):
     """Same fields as the reference: FP64 agrees to round-off, FP32 to FP32
     accuracy."""
@@ -53,17 +59,17 @@ def test_grid_jacobian_on_reference_fields(name):
     assert rel2(J32.astype(np.float64), ref) < 1e-5
 
 
-@pytest.mark.parametrize("name", GRID + IGRID)
+@pytest.mark.parametrize("name", GRID + IGRID + CGRID)
 def test_grid_jacobian_linear_data_against_oracle(name, oracle_mod):
     g, gm, r, s, L = setup(name)
     J = s.jacobian_grid(r, g["dphi"], g["aphi"], None, L, scale=capi.DATA_LIN)
     om = oracle_mod.Mesh(g["coords"], g["elems"])
     ref = oracle_mod.jacobian_grid(om, g["bdim"], g["dphi"], g["aphi"], g["proj"], g["link_ofs"], g["link_m"],
-                                   logscale=False, gdim=g.get("gdim"))
+                                   logscale=False, gdim=g.get("gdim"), kind=kind(g))
     assert rel2(J, ref) < 1e-13
 
 
-@pytest.mark.parametrize("name", IGRID)
+@pytest.mark.parametrize("name", IGRID + CGRID)
 def test_grid_jacobian_chunks(name, monkeypatch):
     """With an intermediate grid the rows are formed on the grid a chunk of
     sources at a time and then mapped to the basis; one-source chunks give
@@ -75,7 +81,7 @@ def test_grid_jacobian_chunks(name, monkeypatch):
     assert np.array_equal(J1, J2)
 
 
-@pytest.mark.parametrize("name", GRID + IGRID)
+@pytest.mark.parametrize("name", GRID + IGRID + CGRID)
 def test_grid_jacobian_end_to_end(name):
     """GPU fields (FP64 path) -> projections -> grid Jacobian, against the
     reference's Jacobian from its own fields."""
@@ -91,7 +97,7 @@ def test_grid_jacobian_end_to_end(name):
     assert rel2(J, g["Jgrid"]) < 1e-9
 
 
-@pytest.mark.parametrize("name", GRID + IGRID)
+@pytest.mark.parametrize("name", GRID + IGRID + CGRID)
 def test_grid_jacobian_sparse_links_against_oracle(name, oracle_mod):
     """Links missing for some (source, detector) pairs and a source without
     any, with a source count that leaves a partial group of sources."""
@@ -100,7 +106,7 @@ def test_grid_jacobian_sparse_links_against_oracle(name, oracle_mod):
     J = s.jacobian_grid(r, g["dphi"], g["aphi"], g["proj"][keep], capi.Links(ofs, lm))
     om = oracle_mod.Mesh(g["coords"], g["elems"])
     ref = oracle_mod.jacobian_grid(om, g["bdim"], g["dphi"], g["aphi"], g["proj"][keep], ofs, lm,
-                                   gdim=g.get("gdim"))
+                                   gdim=g.get("gdim"), kind=kind(g))
     assert J.shape == ref.shape == (2 * len(keep), g["Jgrid"].shape[1])
     assert rel2(J, ref) < 1e-13
 
@@ -114,7 +120,7 @@ def test_raster_of_another_mesh_is_rejected():
         s.jacobian_grid(r2, g["dphi"], g["aphi"], g["proj"], L)
 
 
-GRAD = [n for n in names() if n.endswith("_grad") or n.endswith("_igrad")]
+GRAD = [n for n in names() if n.endswith(("_grad", "_igrad", "_cgrad"))]
 
 
 @pytest.mark.parametrize("name", GRAD)
@@ -127,7 +133,7 @@ def test_data_gradient_against_reference(name, precision, tol):
     stopped at the same 1e-15 relative residual, agrees to 4e-7 on the disc."""
     g = load(name)
     gm = capi.Mesh(g["coords"], g["elems"])
-    r = capi.Raster(gm, g["bdim"], g.get("gdim"))
+    r = capi.Raster(gm, g["bdim"], g.get("gdim"), kind=kind(g))
     s = capi.FwdSolver(gm, g["solver"], 1e-15, g["precon"], True, precision=precision)
     cm, ck, ca = capi.optical_coefficients(g["mua"], g["mus"], g["nref"])
     s.reset(cm, ck, ca, capi.omega_of(g["freq_mhz"]))
@@ -161,11 +167,12 @@ def test_raster_maps_match_reference(name):
     assert np.array_equal(st[0], g["map_s2m"]) and np.array_equal(st[1], r.map("S->M", 3 * sin))
 
 
-@pytest.mark.parametrize("name", IGRID)
+@pytest.mark.parametrize("name", IGRID + CGRID)
 def test_basis_maps_match_reference(name):
-    """With an intermediate grid: every map through the basis (G, GI, the
-    products G B and BI GI, the support) equals the reference's bit for bit,
-    real and complex; the grid maps too."""
+    """With an intermediate grid or the cubic basis: every map through the
+    basis (G, GI, the pixel raster's products G B and BI GI, the support)
+    equals the reference's bit for bit, real and complex; the grid maps
+    too."""
     g, gm, r, s, L = setup(name)
     b = np.arange(1, r.blen + 1, dtype=float)
     sv = np.arange(1, r.slen + 1, dtype=float)

@@ -1030,21 +1030,26 @@ struct CsrMat {
 
 // Raster_Pixel(bdim, gdim) (src/libstoast/raster.cc:18-83, raster_px.cc:
 // 10-48; what toast.Raster(mesh, grd, intgrd) builds,
-// src/python/toastmodule.cc:696): a grid of gdim points per axis over the
-// mesh's bounding box carries the mapped fields; the basis of bdim points
-// carries the solution.  Built on the host once per raster: the bounding
+// src/python/toastmodule.cc:696) or Raster_CubicPixel(bdim, gdim)
+// (raster_cp.cc:10-186): a grid of gdim points per axis over the mesh's
+// bounding box carries the mapped fields; the basis of bdim points carries
+// the solution.  Built on the host once per raster: the bounding
 // box, the element containing each grid point, the grid map matrix B and
 // the node map matrix BI; with an intermediate grid (gdim != bdim) also the
 // grid <-> basis maps G (Grid2LinPixMatrix) and GI (LinPix2GridMatrix),
 // their products with B and BI, and the solution points (the basis points
-// whose subsampled mesh support is positive).  Then kept on the device.
+// whose subsampled mesh support is positive); the cubic basis has its own G
+// and GI.  Then kept on the device.
 struct tg_raster_s {
     Mesh* mesh = nullptr;
     int dim = 0, gdim[3] = {1, 1, 1}, bdim[3] = {1, 1, 1};
     int glen = 0, blen = 0;
     int gslen = 0;  // grid points inside the mesh (gsol: their grid indices)
     int slen = 0;   // solution points (sol2basis: their basis indices)
-    bool inter = false;  // an intermediate grid (gdim != bdim)
+    int type = TG_RASTER_PIXEL;
+    // the solution is mapped from the grid through G: an intermediate grid
+    // (gdim != bdim) or the cubic basis
+    bool hasG = false;
     double bbmin[3] = {0, 0, 0}, bbmax[3] = {0, 0, 0};
     std::vector<int> elref, gsol, rowptr, col;  // col: natural node numbers
     std::vector<double> val;
@@ -1331,19 +1336,136 @@ void csr_ab(const std::vector<int>& arp, const std::vector<int>& acol, const std
     csr_shrink(C);
 }
 
-// The basis side of the raster.  Without an intermediate grid the solution
-// points are the grid points inside the mesh.  With one: bsupport =
-// SubsampleLinPixel of the grid's mesh mask (raster.cc:55-64), solution
-// points the basis points with bsupport > 0 (66-77); G = Grid2LinPixMatrix
-// (rows divided by their weight sums), GI = LinPix2GridMatrix, both shrunk
-// (raster_px.cc:24-27); C = G B and CI = BI GI (raster_px.cc:29-34).
-void raster_basis(int n, tg_raster_s& r)
+// The cubic B-spline weight at distance dr in basis spacings, in the
+// reference's form (raster_cp.cc:57-62, 204-209)
+double cubic_weight(double dr)
 {
-    if (!r.inter) {
-        r.sol2basis = r.gsol;
-        r.slen = r.gslen;
-        return;
+    const double dm2 = dr - 2.0, dm1 = dr - 1.0, dp1 = dr + 1.0, dp2 = dr + 2.0;
+    return (std::fabs(dm2 * dm2 * dm2) - 4.0 * std::fabs(dm1 * dm1 * dm1) + 6.0 * std::fabs(dr * dr * dr) -
+            4.0 * std::fabs(dp1 * dp1 * dp1) + std::fabs(dp2 * dp2 * dp2)) / 12.0;
+}
+
+// Raster_CubicPixel's maps (raster_cp.cc:10-186).  G: per basis point, the
+// axis weights of the grid indices j whose distance |b - (j / iggrid)
+// ibgrid| is below 2, then the grid points inside the mesh of that window
+// with a positive product of weights, in grid order, divided by their sum.
+// GI: per grid point inside the mesh, Raster_CubicPixel::Value (189-214) of
+// the basis points, the nonzero ones in basis order.  The reference scans
+// every grid index per axis and every basis point per grid point; the scans
+// here cover index windows wider by one than the supports, where the same
+// tests decide.  Solution points: the basis points with a nonempty row of G
+// (170-178).
+void cubic_basis(tg_raster_s& r)
+{
+    const int dim = r.dim, blen = r.blen, glen = r.glen;
+    const int gd[3] = {r.gdim[0], r.gdim[1], dim > 2 ? r.gdim[2] : 1};
+    double ib[3] = {0, 0, 0}, ig[3] = {0, 0, 0};
+    for (int d = 0; d < dim; d++) {
+        ib[d] = (r.bdim[d] - 1) / (r.bbmax[d] - r.bbmin[d]);
+        ig[d] = (r.gdim[d] - 1) / (r.bbmax[d] - r.bbmin[d]);
     }
+    CsrMat& G = r.G;
+    G.rp.assign(1, 0);
+    G.col.clear();
+    G.val.clear();
+    std::vector<double> sw[3];
+    for (int d = 0; d < dim; d++) sw[d].assign(gd[d], 0.0);
+    for (int i = 0; i < blen; i++) {
+        int bg[3] = {0, 0, 0}, t = i;
+        if (dim == 3) {
+            bg[2] = t / (r.bdim[0] * r.bdim[1]);
+            t -= bg[2] * r.bdim[0] * r.bdim[1];
+        }
+        bg[0] = t % r.bdim[0];
+        bg[1] = t / r.bdim[0];
+        int imin[3] = {100000, 100000, 0}, imax[3] = {-1, -1, 0};
+        for (int k = 0; k < dim; k++) {
+            imin[k] = 100000;
+            imax[k] = -1;
+            const double c0 = (bg[k] - 2.0) * ig[k] / ib[k], c1 = (bg[k] + 2.0) * ig[k] / ib[k];
+            const int lo = std::max(0, (int)std::floor(c0) - 1), hi = std::min(gd[k] - 1, (int)std::ceil(c1) + 1);
+            for (int j = lo; j <= hi; j++) {
+                const double dr = std::fabs(bg[k] - (j / ig[k]) * ib[k]);
+                if (std::fabs(dr) < 2.0) {
+                    sw[k][j] = cubic_weight(dr);
+                    imin[k] = std::min(imin[k], j);
+                    imax[k] = std::max(imax[k], j);
+                }
+            }
+        }
+        const size_t r0 = G.col.size();
+        double gsum = 0.0;
+        for (int jz = imin[2]; jz <= imax[2]; jz++)
+            for (int jy = imin[1]; jy <= imax[1]; jy++)
+                for (int jx = imin[0]; jx <= imax[0]; jx++) {
+                    const int j = gd[0] * gd[1] * jz + jy * gd[0] + jx, gr[3] = {jx, jy, jz};
+                    if (r.elref[j] < 0) continue;
+                    double v = 1.0;
+                    for (int k = 0; k < dim; k++) v *= sw[k][gr[k]];
+                    if (v > 0) {
+                        G.col.push_back(j);
+                        G.val.push_back(v);
+                        gsum += v;
+                    }
+                }
+        for (size_t e = r0; e < G.col.size(); e++) G.val[e] = G.val[e] / gsum;
+        G.rp.push_back((int)G.col.size());
+    }
+    CsrMat& GI = r.GI;
+    GI.rp.assign(1, 0);
+    GI.col.clear();
+    GI.val.clear();
+    for (int j = 0; j < glen; j++) {
+        if (r.elref[j] >= 0) {
+            int gg[3] = {0, 0, 0}, t = j;
+            if (dim == 3) {
+                gg[2] = t / (gd[0] * gd[1]);
+                t -= gg[2] * gd[0] * gd[1];
+            }
+            gg[0] = t % gd[0];
+            gg[1] = t / gd[0];
+            double off[3] = {0, 0, 0};
+            int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+            for (int k = 0; k < dim; k++) {
+                const double p = r.bbmin[k] + gg[k] / ig[k];
+                off[k] = (r.bbmin[k] - p) * ib[k];
+                lo[k] = std::max(0, (int)std::floor(-2.0 - off[k]) - 1);
+                hi[k] = std::min(r.bdim[k] - 1, (int)std::ceil(2.0 - off[k]) + 1);
+            }
+            for (int iz = lo[2]; iz <= hi[2]; iz++)
+                for (int iy = lo[1]; iy <= hi[1]; iy++)
+                    for (int ix = lo[0]; ix <= hi[0]; ix++) {
+                        const int bi[3] = {ix, iy, iz};
+                        double v = 1.0;
+                        for (int k = 0; k < dim; k++) {
+                            const double dr = std::fabs(bi[k] + off[k]);
+                            if (dr >= 2.0) {
+                                v = 0.0;
+                                break;
+                            }
+                            v *= cubic_weight(dr);
+                        }
+                        if (v != 0.0) {
+                            GI.col.push_back(ix + (iy + iz * r.bdim[1]) * r.bdim[0]);
+                            GI.val.push_back(v);
+                        }
+                    }
+        }
+        GI.rp.push_back((int)GI.col.size());
+    }
+    r.sol2basis.clear();
+    for (int b = 0; b < blen; b++)
+        if (G.rp[b + 1] > G.rp[b]) r.sol2basis.push_back(b);
+    r.slen = (int)r.sol2basis.size();
+}
+
+// The pixel raster with an intermediate grid: bsupport = SubsampleLinPixel
+// of the grid's mesh mask (raster.cc:55-64), solution points the basis
+// points with bsupport > 0 (66-77); G = Grid2LinPixMatrix (rows divided by
+// their weight sums), GI = LinPix2GridMatrix, both shrunk (raster_px.cc:
+// 24-27); C = G B and CI = BI GI (raster_px.cc:29-34).
+void pixel_basis(int n, tg_raster_s& r)
+{
     const int dim = r.dim, glen = r.glen, blen = r.blen;
     std::vector<double> wsum(blen, 0.0), ssum(blen, 0.0);
     linpix_pairs(dim, r.gdim, r.bdim, nullptr, [&](int b, int g, double t) {
@@ -1388,9 +1510,29 @@ void raster_basis(int n, tg_raster_s& r)
     csr_shrink(GI);
     csr_ab(G.rp, G.col, G.val, r.rowptr, r.col, r.val, n, r.C);
     csr_ab(r.nrowptr, r.ncol, r.nval, GI.rp, GI.col, GI.val, blen, r.CI);
+}
+
+// The basis side of the raster: the pixel raster without an intermediate
+// grid has the grid points inside the mesh as its solution points; with one
+// (pixel_basis) and the cubic raster (cubic_basis) the solution is mapped
+// from the grid through G, whose rows of the solution points go to the
+// device as GS for the Jacobian and the data gradient.
+void raster_basis(int n, tg_raster_s& r)
+{
+    if (r.type == TG_RASTER_CUBICPIXEL) {
+        r.hasG = true;
+        cubic_basis(r);
+    } else if (!r.hasG) {
+        r.sol2basis = r.gsol;
+        r.slen = r.gslen;
+        return;
+    } else {
+        pixel_basis(n, r);
+    }
     // G's rows of the solution points, columns as positions among the grid
     // points inside the mesh (G only takes grid points inside the mesh)
-    std::vector<int> gpos(glen, -1);
+    const CsrMat& G = r.G;
+    std::vector<int> gpos(r.glen, -1);
     for (int i = 0; i < r.gslen; i++) gpos[r.gsol[i]] = i;
     CsrMat& S = r.GS;
     S.rp.assign(1, 0);
@@ -2316,7 +2458,7 @@ static void grid_jac_run(tg_solver s, const tg_raster_s& r, int nq, const V64* F
             launch(grid_jacobian_kernel<C, JT, GQ, 3>, jg, TB, 0, s->stream, r.gslen, nqc, nm, nqmc, Pq, Pm, pq,
                    (const C*)ysc, out, l0);
     };
-    if (!r.inter) {
+    if (!r.hasG) {
         rows(0, nq, 0, nqm, (JT*)Jd);
         return;
     }
@@ -2482,7 +2624,7 @@ static void api_gradient(tg_solver s, const tg_raster_s& r, int nq, const double
     };
     planes(X, Pf);
     planes(Y, Pa);
-    if (!r.inter) {
+    if (!r.hasG) {
         launch(gradient_accum_kernel, cdiv_u(r.gslen, 256), 256, 0, s->stream, r.dim, r.gslen, nq, (const cd*)Pf,
                (const cd*)Pa, dg);
     } else {
@@ -3125,22 +3267,24 @@ static void upload_csr(CsrMat& A)
     upload_sync(A.d_val, A.val);
 }
 
-int tg_raster_create_ex(tg_mesh mesh, const int* bdim, const int* gdim, tg_raster* out)
+int tg_raster_create_typed(tg_mesh mesh, int type, const int* bdim, const int* gdim, tg_raster* out)
 {
     API_BEGIN
     TG_CHECK(mesh && bdim && out, TG_ERR_ARG, "NULL argument");
+    TG_CHECK(type == TG_RASTER_PIXEL || type == TG_RASTER_CUBICPIXEL, TG_ERR_ARG, "unknown raster type");
     *out = nullptr;
     const MeshHost& m = mesh->m->h;
     auto r = std::make_unique<tg_raster_s>();
     r->mesh = mesh->m.get();
     r->dim = m.dim;
+    r->type = type;
     long long glen = 1, blen = 1;
     for (int d = 0; d < m.dim; d++) {
         const int g = gdim ? gdim[d] : bdim[d];
         TG_CHECK(bdim[d] >= 2 && g >= 2, TG_ERR_ARG, "every grid dimension needs at least 2 points");
         r->bdim[d] = bdim[d];
         r->gdim[d] = g;
-        r->inter |= g != bdim[d];
+        r->hasG |= g != bdim[d];
         glen *= g;
         blen *= bdim[d];
     }
@@ -3159,15 +3303,21 @@ int tg_raster_create_ex(tg_mesh mesh, const int* bdim, const int* gdim, tg_raste
     upload_sync(r->d_nrowptr, r->nrowptr);
     upload_sync(r->d_ncol, r->ncol);
     upload_sync(r->d_nval, r->nval);
-    if (r->inter)
-        for (CsrMat* A : {&r->G, &r->GI, &r->C, &r->CI, &r->GS}) upload_csr(*A);
+    if (r->hasG)
+        for (CsrMat* A : {&r->G, &r->GI, &r->C, &r->CI, &r->GS})
+            if (!A->rp.empty()) upload_csr(*A);
     *out = r.release();
     API_END
 }
 
+int tg_raster_create_ex(tg_mesh mesh, const int* bdim, const int* gdim, tg_raster* out)
+{
+    return tg_raster_create_typed(mesh, TG_RASTER_PIXEL, bdim, gdim, out);
+}
+
 int tg_raster_create(tg_mesh mesh, const int* bdim, tg_raster* out)
 {
-    return tg_raster_create_ex(mesh, bdim, nullptr, out);
+    return tg_raster_create_typed(mesh, TG_RASTER_PIXEL, bdim, nullptr, out);
 }
 
 int tg_raster_destroy(tg_raster r)
@@ -3207,16 +3357,16 @@ int tg_raster_basis(tg_raster r, int* blen, int* sol2basis)
     API_END
 }
 
-// toast.Raster.Map (MapBasis, src/python/toastmodule.cc:718-790) for the
-// pixel raster: mesh (M), grid (G), basis (B), solution (S).  Each map is a
-// chain of steps as Raster / Raster_Pixel run it (raster.cc:188-458,
-// raster_px.cc:102-176): a sparse matrix (B: grid map, BI: node map, G, GI,
-// C = G B, CI = BI GI), the support (basis -> solution) or its scatter.
-// Real vectors take the pixel raster's own maps (C, CI, and D->Ax / D->ATx
-// for the support, 0 + 1 x); complex vectors the base class's chains
-// through the grid.  Without an intermediate grid G and GI are the identity
-// and C = B, CI = BI.  Each vector is `width` doubles per point (1 real, 2
-// complex).
+// toast.Raster.Map (MapBasis, src/python/toastmodule.cc:718-790): mesh (M),
+// grid (G), basis (B), solution (S).  Each map is a chain of steps as Raster
+// and its subclass run it (raster.cc:188-458, raster_px.cc:102-176,
+// raster_cp.cc:266-302): a sparse matrix (B: grid map, BI: node map, G, GI,
+// C = G B, CI = BI GI), the support (basis -> solution) or its scatter.  The
+// pixel raster's real vectors take its own maps (C, CI, and D->Ax / D->ATx
+// for the support, 0 + 1 x); its complex vectors and every vector of the
+// cubic raster the base class's chains through the grid.  Without G (a
+// pixel raster on its basis grid) G and GI are the identity and C = B,
+// CI = BI.  Each vector is `width` doubles per point (1 real, 2 complex).
 int tg_raster_map(tg_raster r, const char* map, int nvec, const double* src, double* dst, int width, int mem)
 {
     API_BEGIN
@@ -3227,23 +3377,24 @@ int tg_raster_map(tg_raster r, const char* map, int nvec, const double* src, dou
     const int n = r->mesh->d.n, glen = r->glen, blen = r->blen, slen = r->slen;
     auto len = [&](char c) { return c == 'M' ? n : c == 'G' ? glen : c == 'B' ? blen : c == 'S' ? slen : -1; };
     TG_CHECK(len(a) > 0 && len(b) > 0 && a != b, TG_ERR_ARG, "map ids are M, G, B or S, source and target different");
-    const bool real = width == 1, I = r->inter;
+    // I: maps through G; P: the pixel raster's own real maps (products, D)
+    const bool I = r->hasG, P = width == 1 && r->type == TG_RASTER_PIXEL;
     // steps: 'B' grid map, 'N' node map, 'G' / 'I' grid <-> basis, 'C' / 'D'
     // mesh <-> basis products, 's' support, 'x' its scatter, '=' copy
     std::string steps;
     const std::string key{a, b};
     if (key == "MG") steps = "B";
     else if (key == "GM") steps = "N";
-    else if (key == "MB") steps = I ? (real ? "C" : "BG") : "B";
-    else if (key == "MS") steps = I ? (real ? "Cs" : "BGs") : "Bs";
+    else if (key == "MB") steps = I ? (P ? "C" : "BG") : "B";
+    else if (key == "MS") steps = I ? (P ? "Cs" : "BGs") : "Bs";
     else if (key == "GB") steps = I ? "G" : "=";
     else if (key == "GS") steps = I ? "Gs" : "s";
     else if (key == "BG") steps = I ? "I" : "=";
     else if (key == "BS") steps = "s";
-    else if (key == "BM") steps = I ? (real ? "D" : "IN") : "N";
+    else if (key == "BM") steps = I ? (P ? "D" : "IN") : "N";
     else if (key == "SB") steps = "x";
     else if (key == "SG") steps = I ? "xI" : "x";
-    else if (key == "SM") steps = I ? (real ? "xD" : "xIN") : "xN";
+    else if (key == "SM") steps = I ? (P ? "xD" : "xIN") : "xN";
     TG_CUDA(cudaSetDevice(r->mesh->device));
     const size_t sb = (size_t)nvec * len(a) * width * sizeof(double), db = (size_t)nvec * len(b) * width * sizeof(double);
     const double* x = mem == TG_MEM_DEVICE ? src : (const double*)r->d_src.ensure(sb);
@@ -3276,13 +3427,13 @@ int tg_raster_map(tg_raster r, const char* map, int nvec, const double* src, dou
         case 's':
             if (slen > 0)
                 launch(gather_points_kernel, dim3(cdiv_u(slen, 128), nvec), 128, 0, st, slen, blen, width,
-                       r->d_s2b.as<int>(), cur, out, real ? 1 : 0);
+                       r->d_s2b.as<int>(), cur, out, P ? 1 : 0);
             break;
         case 'x':
             TG_CUDA(cudaMemsetAsync(out, 0, (size_t)nvec * blen * width * sizeof(double), st));
             if (slen > 0)
                 launch(scatter_points_kernel, dim3(cdiv_u(slen, 128), nvec), 128, 0, st, slen, blen, width,
-                       r->d_s2b.as<int>(), cur, out, real ? 1 : 0);
+                       r->d_s2b.as<int>(), cur, out, P ? 1 : 0);
             break;
         default:
             TG_CUDA(cudaMemcpyAsync(out, cur, (size_t)nvec * len(kind) * width * sizeof(double),

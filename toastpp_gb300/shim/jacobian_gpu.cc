@@ -5,7 +5,8 @@
 // forwarding to the C ABI: the nodal basis (raster RASTER_NDBASIS), the
 // element basis (RASTER_ELBASIS) and the grid basis of a Raster_Pixel, with
 // or without an intermediate grid (the raster toast.Raster(mesh, grd,
-// intgrd) builds); other rasters stop with xERROR.  The shim Makefile weakens these
+// intgrd) builds), or of a Raster_CubicPixel; other rasters stop with
+// xERROR.  The shim Makefile weakens these
 // five symbols in the reference's own jacobian object, which stays linked
 // for the rest of what it holds (ImageGradient, used by the regularisation
 // and raster code), so these definitions take their place.
@@ -29,12 +30,14 @@ using namespace tgshim;
 
 namespace {
 
-// the basis of a raster argument: 0 nodal, 1 element, 2 grid (Raster_Pixel)
+// the basis of a raster argument: 0 nodal, 1 element, 2 grid (Raster_Pixel
+// or Raster_CubicPixel)
 int basis_of(const Raster* raster)
 {
     if (raster == RASTER_NDBASIS) return 0;
     if (raster == RASTER_ELBASIS) return 1;
-    if (!dynamic_cast<const Raster_Pixel*>(raster)) xERROR("libtoastgpu: only pixel rasters are provided");
+    if (!dynamic_cast<const Raster_Pixel*>(raster) && !dynamic_cast<const Raster_CubicPixel*>(raster))
+        xERROR("libtoastgpu: only pixel and cubic pixel rasters are provided");
     return 2;
 }
 
@@ -68,7 +71,8 @@ void jacobian(const Raster* raster, const QMMesh* mesh, bool cplx, const std::ve
         const IVector& g = raster->GDim();
         int bdim[3] = {b[0], b[1], b.Dim() > 2 ? b[2] : 1};
         int gdim[3] = {g[0], g[1], g.Dim() > 2 ? g[2] : 1};
-        check(tg_raster_create_ex(gm, bdim, gdim, &r), "tg_raster_create_ex");
+        const int type = dynamic_cast<const Raster_CubicPixel*>(raster) ? TG_RASTER_CUBICPIXEL : TG_RASTER_PIXEL;
+        check(tg_raster_create_typed(gm, type, bdim, gdim, &r), "tg_raster_create_typed");
         int glen = 0;
         check(tg_raster_info(r, &glen, &nsol, nullptr, nullptr), "tg_raster_info");
     }
