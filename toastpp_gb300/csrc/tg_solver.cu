@@ -1558,6 +1558,40 @@ void upload_sync(DBuf& b, const std::vector<T>& v)
 
 }  // namespace
 
+struct LinkHost {
+    std::vector<int> q, m, pair;
+};
+
+static LinkHost make_links(int nq, int nm, const int* link_ofs, const int* link_m)
+{
+    LinkHost L;
+    TG_CHECK(link_ofs[0] == 0, TG_ERR_ARG, "link_ofs must start at 0");
+    int nqm = link_ofs[nq];
+    TG_CHECK(nqm >= 0 && (nqm == 0 || link_m), TG_ERR_ARG, "bad link list");
+    L.q.resize(nqm); L.m.resize(nqm); L.pair.assign((size_t)nq * nm, -1);
+    for (int q = 0; q < nq; q++) {
+        TG_CHECK(link_ofs[q + 1] >= link_ofs[q], TG_ERR_ARG, "link_ofs not ascending");
+        for (int l = link_ofs[q]; l < link_ofs[q + 1]; l++) {
+            int m = link_m[l];
+            TG_CHECK(m >= 0 && m < nm, TG_ERR_ARG, "link detector index out of range");
+            TG_CHECK(L.pair[(size_t)q * nm + m] < 0, TG_ERR_ARG, "duplicate link");
+            L.q[l] = q; L.m[l] = m;
+            L.pair[(size_t)q * nm + m] = l;
+        }
+    }
+    return L;
+}
+
+// The link list of the last call on a solver, validated and in host form,
+// and whether the device copies (plink_q / plink_m, jpair) hold it: a call
+// with the same list skips the rebuild and the copies
+struct LinkCache {
+    int nq = -1, nm = -1;
+    std::vector<int> ofs, m;
+    LinkHost L;
+    bool qm_on_dev = false, pair_on_dev = false;
+};
+
 struct tg_solver_s {
     Mesh* mesh = nullptr;
     int cplx = 0, method = 1, precon = 2, precision = 0, maxit = 0;
@@ -1603,6 +1637,7 @@ struct tg_solver_s {
     int jw_D = 0, jw_ready = 0;       // slots per node; bit 0 FP64 weights built, bit 1 FP32, bit 2 float-float
     Profiler prof;
     GraphCache graphs;
+    LinkCache lc;
     std::mutex mu;
     ~tg_solver_s()
     {
@@ -1769,35 +1804,57 @@ static void do_reset(tg_solver s, const double* cmua, const double* ckap, const 
 
 
 
-struct LinkHost {
-    std::vector<int> q, m, pair;
-};
-
-static LinkHost make_links(int nq, int nm, const int* link_ofs, const int* link_m)
-{
-    LinkHost L;
-    TG_CHECK(link_ofs[0] == 0, TG_ERR_ARG, "link_ofs must start at 0");
-    int nqm = link_ofs[nq];
-    TG_CHECK(nqm >= 0 && (nqm == 0 || link_m), TG_ERR_ARG, "bad link list");
-    L.q.resize(nqm); L.m.resize(nqm); L.pair.assign((size_t)nq * nm, -1);
-    for (int q = 0; q < nq; q++) {
-        TG_CHECK(link_ofs[q + 1] >= link_ofs[q], TG_ERR_ARG, "link_ofs not ascending");
-        for (int l = link_ofs[q]; l < link_ofs[q + 1]; l++) {
-            int m = link_m[l];
-            TG_CHECK(m >= 0 && m < nm, TG_ERR_ARG, "link detector index out of range");
-            TG_CHECK(L.pair[(size_t)q * nm + m] < 0, TG_ERR_ARG, "duplicate link");
-            L.q[l] = q; L.m[l] = m;
-            L.pair[(size_t)q * nm + m] = l;
-        }
-    }
-    return L;
-}
-
 template <class T>
 static void upload_async(tg_solver s, DBuf& b, const std::vector<T>& v)
 {
     void* p = b.ensure(std::max<size_t>(v.size(), 1) * sizeof(T));
     if (!v.empty()) TG_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s->stream));
+}
+
+// the solver's link list for this call: the cached one when the arrays
+// equal the last call's, else built (and validated) anew
+static const LinkHost& links_of(tg_solver s, int nq, int nm, const int* link_ofs, const int* link_m)
+{
+    LinkCache& c = s->lc;
+    bool same = c.nq == nq && c.nm == nm && (int)c.ofs.size() == nq + 1 &&
+                std::equal(c.ofs.begin(), c.ofs.end(), link_ofs);
+    if (same) {
+        const size_t nqm = (size_t)link_ofs[nq];
+        same = c.m.size() == nqm && (nqm == 0 || std::equal(c.m.begin(), c.m.end(), link_m));
+    }
+    if (!same) {
+        LinkHost L = make_links(nq, nm, link_ofs, link_m);
+        c.nq = c.nm = -1;
+        c.L = std::move(L);
+        c.ofs.assign(link_ofs, link_ofs + nq + 1);
+        c.m.assign(link_m, link_m + c.L.q.size());
+        c.nq = nq;
+        c.nm = nm;
+        c.qm_on_dev = c.pair_on_dev = false;
+    }
+    return c.L;
+}
+
+// each link's source and detector (plink_q, plink_m), copied unless they
+// already hold the cached list
+static void links_qm_to_device(tg_solver s, const LinkHost& L)
+{
+    const bool cached = &L == &s->lc.L;
+    if (cached && s->lc.qm_on_dev) return;
+    upload_async(s, s->plink_q, L.q);
+    upload_async(s, s->plink_m, L.m);
+    s->lc.qm_on_dev = cached;
+}
+
+// the link index per (source, detector) (jpair), likewise
+static const int* links_pair_to_device(tg_solver s, const LinkHost& L)
+{
+    const bool cached = &L == &s->lc.L;
+    if (!(cached && s->lc.pair_on_dev)) {
+        upload_async(s, s->jpair, L.pair);
+        s->lc.pair_on_dev = cached;
+    }
+    return s->jpair.as<int>();
 }
 
 // ---------------------------------------------------------------------------
@@ -2091,8 +2148,7 @@ static void project_nm(tg_solver s, const V* X, int ldx, int nm, const V* mvec, 
     launch(support_flag_kernel<V>, cdiv_u(n, 256), 256, 0, s->stream, n, nm, mvec, flag);
     launch(support_scan_kernel, 1, 1024, 0, s->stream, n, flag, sup, nsup);
     launch(support_gather_kernel<V>, cdiv_u((size_t)n * nm, 256), 256, 0, s->stream, n, nm, nsup, sup, mvec, Msup);
-    upload_async(s, s->plink_q, L.q);
-    upload_async(s, s->plink_m, L.m);
+    links_qm_to_device(s, L);
     ProfScope ps(&s->prof, PC_PROJ, s->stream);
     launch(project_kernel<V>, cdiv_u((size_t)nqm * 32, 256), 256, 0, s->stream, nsup, sup, s->mesh->d.perm, X, ldx,
            Msup, nm, s->plink_q.as<int>(), s->plink_m.as<int>(), nqm, lg != nullptr, lin, lg);
@@ -2156,7 +2212,7 @@ static void launch_jacobian(tg_solver s, int nq, const VC* F, int ldf, int nm, c
                             const LinkHost& L, const VC* yinv, void* J, int out_fp32)
 {
     using S = typename vt<VC>::R;
-    upload_async(s, s->jpair, L.pair);
+    links_pair_to_device(s, L);
     JacArgs<VC> a;
     a.m = s->mesh->d; a.nq = nq; a.nm = nm; a.nqm = (int)L.q.size();
     a.F = F; a.ldf = ldf; a.G = G; a.ldg = ldg;
@@ -2284,7 +2340,7 @@ static void launch_jacobian_ff(tg_solver s, int nq, const V64* F, int ldf, int n
         yi = (float4*)s->jyinv.ensure((size_t)std::max(nqm, 1) * sizeof(float4));
         launch(ff_recip_kernel<V64>, cdiv_u(nqm, 256), 256, 0, s->stream, nqm, ylin, yi);
     }
-    upload_async(s, s->jpair, L.pair);
+    links_pair_to_device(s, L);
     JacFFArgs a;
     a.m = m; a.nq = nq; a.nm = nm; a.nqm = nqm; a.cplx = CPLX;
     a.F = Ff; a.G = Gf; a.pairidx = s->jpair.as<int>(); a.yinv = yi;
@@ -2418,8 +2474,7 @@ static void grid_jac_run(tg_solver s, const tg_raster_s& r, int nq, const V64* F
     const GridDev G = r.dev();
     // link index per (source, detector), from pageable memory: issued before
     // the launches, so a staging wait finds the stream idle
-    int* pr = (int*)s->jpair.ensure(L.pair.size() * sizeof(int));
-    TG_CUDA(cudaMemcpyAsync(pr, L.pair.data(), L.pair.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    const int* pr = links_pair_to_device(s, L);
     // fields resampled on the grid column by column in the Jacobian's
     // arithmetic type (an FP32 Jacobian casts the fields first), then the
     // planes of sources and detectors in one buffer; the reference masks the
@@ -2524,8 +2579,7 @@ static void element_jac_run(tg_solver s, int nq, const V64* F, int nm, const V64
 {
     const MeshDev& m = s->mesh->d;
     const int n = m.n, nqm = (int)L.q.size();
-    int* pr = (int*)s->jpair.ensure(L.pair.size() * sizeof(int));
-    TG_CUDA(cudaMemcpyAsync(pr, L.pair.data(), L.pair.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    const int* pr = links_pair_to_device(s, L);
     const C *Fc = (const C*)F, *Ac = (const C*)A;
     if constexpr (!std::is_same<C, V64>::value) {
         C* f = (C*)s->gplanes_q.ensure((size_t)nq * n * sizeof(C));
@@ -3149,7 +3203,12 @@ int tg_solver_set_stream(tg_solver s, void* stream)
 {
     API_BEGIN
     TG_CHECK(s, TG_ERR_ARG, "solver is NULL");
-    s->stream = stream ? (cudaStream_t)stream : s->own;
+    std::lock_guard<std::mutex> g(s->mu);
+    const cudaStream_t st = stream ? (cudaStream_t)stream : s->own;
+    // device copies made on the old stream are not ordered before the new
+    // stream's work: the next call copies the link list again
+    if (st != s->stream) s->lc.qm_on_dev = s->lc.pair_on_dev = false;
+    s->stream = st;
     API_END
 }
 
@@ -3239,7 +3298,7 @@ int tg_project_all(tg_solver s, int nq, const double* phi, int nm, const double*
     TG_CHECK(nq >= 0 && nm >= 0, TG_ERR_ARG, "negative count");
     TG_CHECK(scale == TG_DATA_LIN || scale == TG_DATA_LOG, TG_ERR_ARG, "scale must be TG_DATA_LIN or TG_DATA_LOG");
     std::lock_guard<std::mutex> g(s->mu);
-    LinkHost L = make_links(nq, nm, link_ofs, link_m);
+    const LinkHost& L = links_of(s, nq, nm, link_ofs, link_m);
     if (L.q.empty()) return TG_OK;
     if (s->cplx) api_project<cd>(s, nq, phi, nm, mvec, L, scale, proj, mem);
     else api_project<double>(s, nq, phi, nm, mvec, L, scale, proj, mem);
@@ -3253,7 +3312,7 @@ int tg_jacobian(tg_solver s, int nq, const double* dphi, int nm, const double* a
     TG_CHECK(s && dphi && aphi && link_ofs && J, TG_ERR_ARG, "NULL argument");
     TG_CHECK(scale == TG_DATA_LIN || (scale == TG_DATA_LOG && proj), TG_ERR_ARG, "log data needs the projections");
     std::lock_guard<std::mutex> g(s->mu);
-    LinkHost L = make_links(nq, nm, link_ofs, link_m);
+    const LinkHost& L = links_of(s, nq, nm, link_ofs, link_m);
     if (L.q.empty()) return TG_OK;
     if (s->cplx) api_jacobian<cd, cf>(s, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
     else api_jacobian<double, float>(s, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
@@ -3458,7 +3517,7 @@ int tg_jacobian_grid(tg_solver s, tg_raster r, int nq, const double* dphi, int n
     TG_CHECK(nq > 0 && nm > 0 && nq <= 65535 && nm <= 65535, TG_ERR_ARG, "source / detector count out of range");
     TG_CHECK(scale == TG_DATA_LIN || (scale == TG_DATA_LOG && proj), TG_ERR_ARG, "log data needs the projections");
     std::lock_guard<std::mutex> g(s->mu);
-    LinkHost L = make_links(nq, nm, link_ofs, link_m);
+    const LinkHost& L = links_of(s, nq, nm, link_ofs, link_m);
     if (L.q.empty() || r->slen == 0) return TG_OK;
     if (s->cplx) api_jacobian_grid<cd, cf>(s, *r, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
     else api_jacobian_grid<double, float>(s, *r, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
@@ -3476,7 +3535,7 @@ int tg_gradient(tg_solver s, tg_raster r, int nq, const double* qvec, int nm, co
     TG_CHECK(r->mesh == s->mesh, TG_ERR_ARG, "the raster was built on another mesh");
     TG_CHECK(nq > 0 && nm > 0 && nq <= 65535, TG_ERR_ARG, "source / detector count out of range");
     std::lock_guard<std::mutex> g(s->mu);
-    LinkHost L = make_links(nq, nm, link_ofs, link_m);
+    const LinkHost& L = links_of(s, nq, nm, link_ofs, link_m);
     if (L.q.empty() || r->slen == 0) return TG_OK;
     api_gradient(s, *r, nq, qvec, nm, mvec, L, data, sd, grad, mem, res);
     API_END
@@ -3490,7 +3549,7 @@ int tg_jacobian_el(tg_solver s, int nq, const double* dphi, int nm, const double
     TG_CHECK(nq > 0 && nm > 0 && nq <= 65535 * 4, TG_ERR_ARG, "source / detector count out of range");
     TG_CHECK(scale == TG_DATA_LIN || (scale == TG_DATA_LOG && proj), TG_ERR_ARG, "log data needs the projections");
     std::lock_guard<std::mutex> g(s->mu);
-    LinkHost L = make_links(nq, nm, link_ofs, link_m);
+    const LinkHost& L = links_of(s, nq, nm, link_ofs, link_m);
     if (L.q.empty()) return TG_OK;
     if (s->cplx) api_jacobian_el<cd, cf>(s, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
     else api_jacobian_el<double, float>(s, nq, dphi, nm, aphi, proj, L, scale, J, out_fp32, mem);
@@ -3507,7 +3566,7 @@ int tg_forward_path(tg_solver s, const double* cmua, const double* ckappa, const
     TG_CHECK(nq > 0 && nm > 0, TG_ERR_ARG, "need at least one source and one detector");
     TG_CHECK(s->cplx || omega == 0.0, TG_ERR_ARG, "nonzero omega for a real system");
     std::lock_guard<std::mutex> g(s->mu);
-    LinkHost L = make_links(nq, nm, link_ofs, link_m);
+    const LinkHost& L = links_of(s, nq, nm, link_ofs, link_m);
     if (s->cplx)
         api_forward_path<cd, cf>(s, cmua, ckappa, c2a, omega, nq, qvec, nm, mvec, L, dphi, aphi, proj, logproj, J,
                                  j_fp32, mem, res);
