@@ -86,6 +86,16 @@ def lib():
         L.tor_jacobian_el.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int, C.c_int, _dp]
         L.tor_gradient_weights.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _ip, _ip, _dp]
         L.tor_gradient_grid.argtypes = [C.c_void_p, C.c_int, _ip, _ip, C.c_int, _dp, _dp, _dp]
+        L.tor_blob_create.restype = C.c_void_p
+        L.tor_blob_create.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, _ip]
+        L.tor_blob_info.argtypes = [C.c_void_p, _ip, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                    _dp, _dp]
+        L.tor_blob_arrays.argtypes = [C.c_void_p, _ip, _ip, _ip, _ip, _dp]
+        L.tor_blob_free.argtypes = [C.c_void_p]
+        L.tor_jacobian_blob.restype = C.c_int
+        L.tor_jacobian_blob.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int,
+                                        C.c_int, _dp]
+        L.tor_gradient_blob.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _dp, _dp, _dp]
         L.tor_cubic_map.restype = C.c_int
         L.tor_cubic_map.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _ip, C.c_int, _ip, C.c_void_p, C.c_void_p]
         L.tor_linpix_map.restype = C.c_int
@@ -421,7 +431,7 @@ def jacobian_el(mesh: Mesh, dphi, aphi, proj_lin, link_ofs, link_m, logscale=Tru
 def data_gradient(mesh: Mesh, bdim, sysval, dphi, mvec, proj_lin, proj_log, link_ofs, link_m, data, sd,
                   method="BICGSTAB", precon="ICH", tol=1e-15, gdim=None, kind="pixel"):
     """toast's Gradient on Raster_Pixel(bdim, gdim) (gdim None: bdim; kind
-    "cubic": Raster_CubicPixel) given
+    "cubic": Raster_CubicPixel; kind a BlobRaster: that blob raster) given
     the fields: weights, one adjoint solve per source with the weighted
     detector vectors, then the grid products mapped to the solution basis
     (src/python/toastmodule.cc:1745-1843).  Returns 2 slen."""
@@ -434,6 +444,10 @@ def data_gradient(mesh: Mesh, bdim, sysval, dphi, mvec, proj_lin, proj_log, link
                                np.ascontiguousarray(sd, np.float64), np.ascontiguousarray(link_ofs, np.int32),
                                np.ascontiguousarray(link_m, np.int32), W.view(np.float64).reshape(-1))
     wphi, _, _ = solve(mesh.rowptr, mesh.colidx, sysval, W, method, precon, tol)
+    if isinstance(kind, BlobRaster):
+        grad = np.zeros(2 * kind.slen)
+        lib().tor_gradient_blob(mesh._h, kind._h, nq, _cview(dphi).ravel(), _cview(wphi).ravel(), grad)
+        return grad
     slen = len(raster_support(mesh, bdim, gdim, kind))
     grad = np.zeros(2 * slen)
     lib().tor_gradient_grid(mesh._h, _KIND[kind], bdim, gdim, nq, _cview(dphi).ravel(), _cview(wphi).ravel(), grad)
@@ -509,6 +523,107 @@ def linpix_map(dim, gdim, bdim, elref, by_grid):
 
 
 _KIND = {"pixel": 0, "cubic": 1}
+BLOB_KINDS = {"gauss": 1, "hanning": 2, "ramp": 3, "spline": 4}
+
+
+class BlobRaster:
+    """A blob raster (Raster_Blob, raster_bl.cc, with the Gaussian, Hanning,
+    ramp or spline blob of raster_gb.cc / raster_hb.cc / raster_rb.cc /
+    raster_sb.cc): basis bdim padded by the support radius, the element per
+    padded grid point, the solution points (basis indices) and the node
+    values (per node the blob values of the solution points, CSR)."""
+
+    def __init__(self, mesh: Mesh, kind, bdim, sup, sigma=1.0):
+        self.mesh = mesh
+        self.dim = mesh.dim
+        bdim = np.ascontiguousarray(bdim, np.int32)
+        self._h = lib().tor_blob_create(mesh._h, BLOB_KINDS[kind], float(sigma), float(sup), bdim)
+        pdim = np.zeros(3, np.int32)
+        sl, nz, sc = C.c_int(), C.c_int(), C.c_double()
+        self.bbmin, self.bbmax = np.zeros(3), np.zeros(3)
+        lib().tor_blob_info(self._h, pdim, C.byref(sl), C.byref(nz), C.byref(sc), self.bbmin, self.bbmax)
+        self.pdim = pdim[:self.dim].copy()
+        self.bbmin, self.bbmax = self.bbmin[:self.dim], self.bbmax[:self.dim]
+        self.slen, self.scale = sl.value, sc.value
+        self.blen = int(np.prod(self.pdim))
+        self.elref = np.zeros(self.blen, np.int32)
+        self.sol2basis = np.zeros(max(self.slen, 1), np.int32)
+        self.nrp = np.zeros(mesh.n + 1, np.int32)
+        self.ncol = np.zeros(max(nz.value, 1), np.int32)
+        self.nval = np.zeros(max(nz.value, 1))
+        lib().tor_blob_arrays(self._h, self.elref, self.sol2basis, self.nrp, self.ncol, self.nval)
+        self.sol2basis = self.sol2basis[:self.slen]
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().tor_blob_free(self._h)
+            self._h = None
+
+    def mesh_to_basis(self, f):
+        """Map_MeshToBasis (raster_bl.cc:170-204): per solution point the
+        node-value-weighted sum over the nodes (node order) over the sum of
+        the weights; 0 elsewhere."""
+        f = np.asarray(f)
+        cplx = np.iscomplexobj(f)
+        fr, fi, sm = np.zeros(self.slen), np.zeros(self.slen), np.zeros(self.slen)
+        for nd in range(self.mesh.n):
+            x = complex(f[nd])
+            for t in range(self.nrp[nd], self.nrp[nd + 1]):
+                j, v = int(self.ncol[t]), float(self.nval[t])
+                if cplx:
+                    fr[j] += x.real * v
+                    fi[j] += x.imag * v
+                else:
+                    fr[j] += v * x.real
+                sm[j] += v
+        b = np.zeros(self.blen, np.complex128 if cplx else np.float64)
+        for j in range(self.slen):
+            if sm[j] != 0.0:
+                b[self.sol2basis[j]] = fr[j] / sm[j] + 1j * (fi[j] / sm[j]) if cplx else fr[j] / sm[j]
+        return b
+
+    def sol_to_mesh(self, sv):
+        """Map_SolToMesh (raster_bl.cc:252-276): per node the sum over the
+        solution points of value x node value, in solution order."""
+        sv = np.asarray(sv)
+        cplx = np.iscomplexobj(sv)
+        out = np.zeros(self.mesh.n, np.complex128 if cplx else np.float64)
+        for nd in range(self.mesh.n):
+            acc = 0j if cplx else 0.0
+            for t in range(self.nrp[nd], self.nrp[nd + 1]):
+                acc += sv[self.ncol[t]] * float(self.nval[t])
+            out[nd] = acc
+        return out
+
+    def maps(self, mua, mus):
+        """The reference driver's map vectors through a blob raster (grid =
+        basis; toast.Raster.Map with raster_bl.cc:140-350): m2g (= M->B),
+        m2s, s2m of s + 1, g2m of m2g, m2b, b2m of b + 1, g2b, b2g (copies),
+        g2s, s2g of s + 1, complex cm2s of mua + i mus, cs2m of (s + 1) -
+        0.5 i s."""
+        b = np.arange(1, self.blen + 1, dtype=float)
+        sv = np.arange(1, self.slen + 1, dtype=float)
+        m2g = self.mesh_to_basis(mua)
+        s2g = np.zeros(self.blen)
+        s2g[self.sol2basis] = sv
+        cs = np.arange(1, self.slen + 1) - 0.5j * np.arange(self.slen)
+        return dict(m2g=m2g, m2s=m2g[self.sol2basis], s2m=self.sol_to_mesh(sv),
+                    g2m=self.sol_to_mesh(m2g[self.sol2basis]), m2b=m2g, b2m=self.sol_to_mesh(b[self.sol2basis]),
+                    g2b=m2g, b2g=b, g2s=m2g[self.sol2basis], s2g=s2g,
+                    cm2s=self.mesh_to_basis(np.asarray(mua) + 1j * np.asarray(mus))[self.sol2basis],
+                    cs2m=self.sol_to_mesh(cs))
+
+    def jacobian(self, dphi, aphi, proj_lin, link_ofs, link_m, logscale=True):
+        """Grid-basis Jacobian on the blob raster: complex (2 nQM) x (2 slen),
+        real (2 nQM) x slen."""
+        cplx = np.iscomplexobj(dphi)
+        nq, nm, nqm = dphi.shape[0], aphi.shape[0], int(link_ofs[-1])
+        J = np.zeros((2 * nqm, 2 * self.slen) if cplx else (2 * nqm, self.slen))
+        f = (lambda a: _cview(a).ravel()) if cplx else (lambda a: np.ascontiguousarray(a, np.float64).ravel())
+        lib().tor_jacobian_blob(self.mesh._h, self._h, nq, nm, f(dphi), f(aphi), f(proj_lin),
+                                np.ascontiguousarray(link_ofs, np.int32), np.ascontiguousarray(link_m, np.int32),
+                                int(cplx), int(logscale), J.reshape(-1))
+        return J
 
 
 def cubic_map(dim, gdim, bdim, bbmin, bbmax, elref, by_grid):

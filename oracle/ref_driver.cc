@@ -36,7 +36,9 @@
 //              gives the intermediate grid (default: the basis grid); with
 //              it the solution points' basis indices (PREFIX_sol2basis.bin)
 //              and the maps through the basis are written too.  raster=cubic
-//              builds a Raster_CubicPixel(bdim, gdim) instead.
+//              builds a Raster_CubicPixel(bdim, gdim) instead, raster=gauss
+//              (sigma=, sup=), hanning, ramp or spline (sup=) a blob basis;
+//              the raster's own grid size is written (PREFIX_rgdim.bin).
 // qmdump     : with qm, write what QMMesh::LoadQM (qmmesh.cc:319-460, with
 //              InitM's detector placement) made of the file and stop:
 //              PREFIX_qpos.bin, PREFIX_mpos.bin (nQ / nM x dim doubles),
@@ -161,6 +163,11 @@ static void write_basis_maps(Raster& raster, const RVector& mua, const RVector& 
     std::vector<int> s2b(slen);
     for (int i = 0; i < slen; i++) s2b[i] = raster.Sol2Basis(i);
     wbin(out + "_sol2basis.bin", s2b.data(), slen * sizeof(int));
+    // the raster's own grid and basis sizes (a blob basis pads both)
+    std::vector<int> dims;
+    for (int d = 0; d < raster.Dim(); d++) dims.push_back(raster.GDim()[d]);
+    for (int d = 0; d < raster.Dim(); d++) dims.push_back(raster.BDim()[d]);
+    wbin(out + "_rgdim.bin", dims.data(), dims.size() * sizeof(int));
 }
 
 // The data gradient on a raster, in the sequence of toast's GetGradient /
@@ -217,11 +224,19 @@ static void ref_data_gradient(QMMesh& mesh, Raster& raster, CFwdSolver& FWS, con
     }
 }
 
-// the raster of the grid arguments: Raster_Pixel, or Raster_CubicPixel
-// (raster_cp.cc) with raster=cubic
+// the raster of the grid arguments: Raster_Pixel, or with raster=cubic
+// Raster_CubicPixel (raster_cp.cc), raster=gauss|hanning|ramp|spline the
+// blob bases (raster_gb.cc, raster_hb.cc, raster_rb.cc, raster_sb.cc) of
+// support radius sup (and width sigma for gauss)
 static Raster* make_raster(const IVector& bdim, const IVector& gdim, QMMesh& mesh)
 {
-    if (arg("raster", "pixel") == "cubic") return new Raster_CubicPixel(bdim, gdim, &mesh);
+    const string kind = arg("raster", "pixel");
+    const double sup = atof(arg("sup", "2").c_str());
+    if (kind == "cubic") return new Raster_CubicPixel(bdim, gdim, &mesh);
+    if (kind == "gauss") return new Raster_GaussBlob(bdim, gdim, &mesh, atof(arg("sigma", "1").c_str()), sup);
+    if (kind == "hanning") return new Raster_HanningBlob(bdim, gdim, &mesh, sup);
+    if (kind == "ramp") return new Raster_RampBlob(bdim, gdim, &mesh, sup);
+    if (kind == "spline") return new Raster_SplineBlob(bdim, gdim, &mesh, sup);
     return new Raster_Pixel(bdim, gdim, &mesh);
 }
 
@@ -422,7 +437,7 @@ int main(int argc, char** argv) {
                 wbin(out + "_elref.bin", raster.Elref(), (size_t)glen * sizeof(int));
                 fprintf(info, "slen %d\nglen %d\n", slen, glen);
                 write_maps(raster, mua, out);
-                if ((int)igrid.size() == dim || arg("raster", "pixel") == "cubic")
+                if ((int)igrid.size() == dim || arg("raster", "pixel") != "pixel")
                     write_basis_maps(raster, mua, mus, out);
                 if (g_args.count("data")) {
                     std::vector<char> db = rbin(arg("data", "")), sb = rbin(arg("sd", ""));
@@ -516,7 +531,7 @@ int main(int argc, char** argv) {
                 wbin(out + "_elref.bin", raster.Elref(), (size_t)glen * sizeof(int));
                 fprintf(info, "slen %d\nglen %d\n", slen, glen);
                 write_maps(raster, mua, out);
-                if ((int)igrid.size() == dim || arg("raster", "pixel") == "cubic")
+                if ((int)igrid.size() == dim || arg("raster", "pixel") != "pixel")
                     write_basis_maps(raster, mua, mus, out);
             }
         }

@@ -1469,26 +1469,12 @@ int tor_external_source(const tor_mesh *m, const double *q, const double *nrm, d
     return tor_bnd_intersect(m, p1, q, out);
 }
 
-/* Raster_Pixel with the grid equal to the basis (raster.cc:18-83,
-   raster_px.cc:10-48, the case bdim == gdim):
-   - bounding box: Mesh::BoundingBox (mesh.cc:1341-1360), no padding;
-   - elref: GenerateElementPixelRef (mesh.cc:2944-3014), the first element
-     (in element order) containing each grid point, -1 outside;
-   - B: GridMapMatrix (mesh.cc:2486-2554), row g = the containing element's
-     global shape functions at the grid point (tri3.cc:231-240,
-     tet4.cc:302-313), in the element's node order.
-   Returns glen.  browptr: glen+1, bcol / bval: glen*nn (room for every row). */
-int tor_raster_pixel(const tor_mesh *m, const int *bdim, double *bbmin, double *bbmax, int *elref,
-                     int *browptr, int *bcol, double *bval)
+/* GenerateElementPixelRef (mesh.cc:2944-3014) on a grid of bdim points over
+   the box [bbmin, bbmax]: elements in order, each claims the unclaimed grid
+   points of its widened bounding box that it contains; -1 elsewhere */
+static void pixel_elref(const tor_mesh *m, const int *bdim, const double *bbmin, const double *bbmax, int *elref)
 {
     const int dim = m->dim, nn = m->nn;
-    for (int d = 0; d < dim; d++) { bbmin[d] = 1e6; bbmax[d] = -1e6; }
-    for (int k = 0; k < m->n; k++)
-        for (int d = 0; d < dim; d++) {
-            double v = m->x[(size_t)k * dim + d];
-            if (v < bbmin[d]) bbmin[d] = v;
-            if (v > bbmax[d]) bbmax[d] = v;
-        }
     const int nx = bdim[0], ny = bdim[1], nz = dim > 2 ? bdim[2] : 1;
     const int glen = nx * ny * nz;
     double dW[3];
@@ -1529,6 +1515,33 @@ int tor_raster_pixel(const tor_mesh *m, const int *bdim, double *bbmin, double *
             }
         }
     }
+}
+
+/* Raster_Pixel with the grid equal to the basis (raster.cc:18-83,
+   raster_px.cc:10-48, the case bdim == gdim):
+   - bounding box: Mesh::BoundingBox (mesh.cc:1341-1360), no padding;
+   - elref: GenerateElementPixelRef (mesh.cc:2944-3014), the first element
+     (in element order) containing each grid point, -1 outside;
+   - B: GridMapMatrix (mesh.cc:2486-2554), row g = the containing element's
+     global shape functions at the grid point (tri3.cc:231-240,
+     tet4.cc:302-313), in the element's node order.
+   Returns glen.  browptr: glen+1, bcol / bval: glen*nn (room for every row). */
+int tor_raster_pixel(const tor_mesh *m, const int *bdim, double *bbmin, double *bbmax, int *elref,
+                     int *browptr, int *bcol, double *bval)
+{
+    const int dim = m->dim, nn = m->nn;
+    for (int d = 0; d < dim; d++) { bbmin[d] = 1e6; bbmax[d] = -1e6; }
+    for (int k = 0; k < m->n; k++)
+        for (int d = 0; d < dim; d++) {
+            double v = m->x[(size_t)k * dim + d];
+            if (v < bbmin[d]) bbmin[d] = v;
+            if (v > bbmax[d]) bbmax[d] = v;
+        }
+    pixel_elref(m, bdim, bbmin, bbmax, elref);
+    const int nx = bdim[0], ny = bdim[1], nz = dim > 2 ? bdim[2] : 1;
+    const int glen = nx * ny * nz;
+    double dW[3];
+    for (int d = 0; d < dim; d++) dW[d] = (bbmax[d] - bbmin[d]) / (double)(bdim[d] - 1);
     int k = 0;
     browptr[0] = 0;
     for (int iz = 0, i = 0; iz < nz; iz++) {
@@ -1991,6 +2004,293 @@ int tor_cubic_map(int dim, const int *gdim, const int *bdim, const double *bbmin
         }
     }
     return nz;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The blob bases (Raster_Blob, raster_bl.cc, and its subclasses)            */
+/* ------------------------------------------------------------------------ */
+
+/* A blob raster (raster_bl.cc:9-75): the basis grid of bdim points over the
+   mesh's bounding box, padded by npad = ceil(sup - 1e-6) layers on every
+   side (igrid = (bdim - 1) / bbsize from the unpadded size); the element
+   per padded grid point over the padded box; the solution points are the
+   basis points within sup (in grid spacings) of a mesh node, in basis
+   order.  Blob values (Value_nomask) at a point p for basis point b:
+   r = (b - npad) + (bbmin - p) igrid,
+   kind 1 Gaussian (raster_gb.cc): scale exp(-|r|^2 / sigma^2), |r|^2 < sup^2;
+   kind 2 Hanning (raster_hb.cc): scale (1 + cos(pi |r| / sup)), |r| < sup;
+   kind 3 ramp (raster_rb.cc): scale (1 - |r| / sup);
+   kind 4 spline (raster_sb.cc): scale 4 sum over the knots xi_k = (k - 2)
+   sup / 2 left of -|r| (the first two) of (-|r| - xi_k)^3 omega_k, omega_k
+   = 1 / prod_{j != k} (xi_k - xi_j).  The scale: the subclass's start value
+   (1, or 0.5 for Hanning) times 1 / mean over the nodes of the sum of the
+   blob values there (ComputeBasisScale, raster_bl.cc:353-361).  nodevals:
+   per node the nonzero blob values of the solution points, in their order
+   (ComputeNodeValues, 82-114). */
+typedef struct {
+    int dim, kind, npad, pdim[3], blen, slen, n;
+    double sup, sigma, scale, a2, isigma2, fac, isup, xi[5], iomega[5];
+    double bbmin[3], bbmax[3], igrid[3], bbmin_pad[3], bbmax_pad[3];
+    int *elref, *basis2sol, *sol2basis;
+    int *nrp, *ncol;
+    double *nval;
+} tor_blob;
+
+static double blob_value(const tor_blob *B, const double *p, int j)
+{
+    int ib = B->sol2basis[j], bg[3] = {0, 0, 0};
+    if (B->dim == 3) { bg[2] = ib / (B->pdim[0] * B->pdim[1]); ib -= bg[2] * B->pdim[0] * B->pdim[1]; }
+    bg[0] = ib % B->pdim[0];
+    bg[1] = ib / B->pdim[0];
+    double r2 = 0.0;
+    for (int d = 0; d < B->dim; d++) {
+        double r = (bg[d] - B->npad) + (B->bbmin[d] - p[d]) * B->igrid[d];
+        r2 += fabs(r) * fabs(r);
+    }
+    if (B->kind == 1) {
+        if (r2 >= B->a2) return 0.0;
+        return B->scale * exp(-r2 * B->isigma2);
+    }
+    double rad = sqrt(r2);
+    if (rad >= B->sup) return 0.0;
+    if (B->kind == 2) return B->scale * (1.0 + cos(B->fac * rad));
+    if (B->kind == 3) return B->scale * (1.0 - rad * B->isup);
+    double x = -rad, dx = x - B->xi[0], d3 = dx * dx * dx, sum = d3 * B->iomega[0];
+    if (x > B->xi[1]) {
+        dx = x - B->xi[1];
+        d3 = dx * dx * dx;
+        sum += d3 * B->iomega[1];
+    }
+    sum *= 4.0;
+    return B->scale * sum;
+}
+
+tor_blob *tor_blob_create(const tor_mesh *m, int kind, double sigma, double sup, const int *bdim)
+{
+    const double eps = 1e-6, PI = 3.14159265358979323846;
+    const int dim = m->dim, n = m->n;
+    tor_blob *B = calloc(1, sizeof(tor_blob));
+    B->dim = dim; B->kind = kind; B->sup = sup; B->sigma = sigma; B->n = n;
+    for (int d = 0; d < dim; d++) { B->bbmin[d] = 1e6; B->bbmax[d] = -1e6; }
+    for (int k = 0; k < n; k++)
+        for (int d = 0; d < dim; d++) {
+            double v = m->x[(size_t)k * dim + d];
+            if (v < B->bbmin[d]) B->bbmin[d] = v;
+            if (v > B->bbmax[d]) B->bbmax[d] = v;
+        }
+    for (int d = 0; d < dim; d++) B->igrid[d] = (bdim[d] - 1.0) / (B->bbmax[d] - B->bbmin[d]);
+    B->npad = (int)ceil(sup - eps);
+    B->blen = 1;
+    for (int d = 0; d < 3; d++) B->pdim[d] = 1;
+    for (int d = 0; d < dim; d++) B->blen *= (B->pdim[d] = bdim[d] + 2 * B->npad);
+    for (int d = 0; d < dim; d++) {
+        B->bbmin_pad[d] = B->bbmin[d] - B->npad / B->igrid[d];
+        B->bbmax_pad[d] = B->bbmax[d] + B->npad / B->igrid[d];
+    }
+    B->elref = malloc(sizeof(int) * B->blen);
+    pixel_elref(m, B->pdim, B->bbmin_pad, B->bbmax_pad, B->elref);
+    /* solution points */
+    B->basis2sol = malloc(sizeof(int) * B->blen);
+    B->sol2basis = malloc(sizeof(int) * B->blen);
+    const double sup2 = sup * sup;
+    const int nx = B->pdim[0], ny = B->pdim[1], nz = dim > 2 ? B->pdim[2] : 1;
+    int idx = 0;
+    B->slen = 0;
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++, idx++) {
+                double r[3] = {(double)i, (double)j, (double)k};
+                B->basis2sol[idx] = -1;
+                for (int nd = 0; nd < n; nd++) {
+                    double rad2 = 0.0;
+                    for (int d = 0; d < dim; d++) {
+                        double dx = (m->x[(size_t)nd * dim + d] - B->bbmin[d]) * B->igrid[d] + B->npad - r[d];
+                        rad2 += dx * dx;
+                    }
+                    if (rad2 < sup2) { B->basis2sol[idx] = B->slen++; break; }
+                }
+                if (B->basis2sol[idx] >= 0) B->sol2basis[B->basis2sol[idx]] = idx;
+            }
+    /* the subclass's constants and start scale */
+    B->a2 = sup * sup;
+    B->scale = 1.0;
+    if (kind == 1) B->isigma2 = 1.0 / (sigma * sigma);
+    if (kind == 2) { B->fac = PI / sup; B->scale = 0.5; }
+    if (kind == 3) B->isup = 1.0 / sup;
+    if (kind == 4) {
+        for (int i = 0; i <= 4; i++) B->xi[i] = (i - 2) * 0.5 * sup;
+        for (int i = 0; i <= 4; i++) {
+            B->iomega[i] = 1.0;
+            for (int j = 0; j <= 4; j++)
+                if (i != j) B->iomega[i] /= B->xi[i] - B->xi[j];
+        }
+    }
+    /* ComputeBasisScale: 1 / mean over the nodes of the sum of the values */
+    double tot = 0.0;
+    for (int nd = 0; nd < n; nd++) {
+        double sum = 0.0;
+        for (int j = 0; j < B->slen; j++) sum += 1.0 * blob_value(B, m->x + (size_t)nd * dim, j);
+        tot += sum;
+    }
+    double cbs = 1.0 / (tot / n);
+    B->scale = kind == 1 ? cbs : B->scale * cbs;
+    /* ComputeNodeValues */
+    B->nrp = malloc(sizeof(int) * (n + 1));
+    size_t cap = 64, nz2 = 0;
+    B->ncol = malloc(sizeof(int) * cap);
+    B->nval = malloc(sizeof(double) * cap);
+    B->nrp[0] = 0;
+    for (int nd = 0; nd < n; nd++) {
+        for (int j = 0; j < B->slen; j++) {
+            double v = blob_value(B, m->x + (size_t)nd * dim, j);
+            if (v != 0.0) {
+                if (nz2 == cap) {
+                    cap *= 2;
+                    B->ncol = realloc(B->ncol, sizeof(int) * cap);
+                    B->nval = realloc(B->nval, sizeof(double) * cap);
+                }
+                B->ncol[nz2] = j;
+                B->nval[nz2++] = v;
+            }
+        }
+        B->nrp[nd + 1] = (int)nz2;
+    }
+    return B;
+}
+
+void tor_blob_info(const tor_blob *B, int *pdim, int *slen, int *nnz, double *scale, double *bbmin, double *bbmax)
+{
+    for (int d = 0; d < B->dim; d++) {
+        pdim[d] = B->pdim[d];
+        bbmin[d] = B->bbmin[d];
+        bbmax[d] = B->bbmax[d];
+    }
+    *slen = B->slen;
+    *nnz = B->nrp[B->n];
+    *scale = B->scale;
+}
+
+void tor_blob_arrays(const tor_blob *B, int *elref, int *sol2basis, int *nrp, int *ncol, double *nval)
+{
+    memcpy(elref, B->elref, sizeof(int) * B->blen);
+    memcpy(sol2basis, B->sol2basis, sizeof(int) * B->slen);
+    memcpy(nrp, B->nrp, sizeof(int) * (B->n + 1));
+    memcpy(ncol, B->ncol, sizeof(int) * B->nrp[B->n]);
+    memcpy(nval, B->nval, sizeof(double) * B->nrp[B->n]);
+}
+
+void tor_blob_free(tor_blob *B)
+{
+    if (!B) return;
+    free(B->elref); free(B->basis2sol); free(B->sol2basis); free(B->nrp); free(B->ncol); free(B->nval); free(B);
+}
+
+/* Raster_Blob::Map_MeshToBasis (raster_bl.cc:170-204): per solution point
+   the node-value-weighted sum of the field over the nodes, in node order,
+   divided by the sum of the weights (0 where that is 0); other basis
+   points 0.  Complex fields component by component. */
+static void blob_mesh_to_basis(const tor_blob *B, const zd *f, int cplx, zd *b)
+{
+    double *fr = calloc(B->slen, sizeof(double)), *fi = calloc(B->slen, sizeof(double));
+    double *sum = calloc(B->slen, sizeof(double));
+    for (int nd = 0; nd < B->n; nd++)
+        for (int t = B->nrp[nd]; t < B->nrp[nd + 1]; t++) {
+            const int j = B->ncol[t];
+            const double v = B->nval[t];
+            if (cplx) { fr[j] += creal(f[nd]) * v; fi[j] += cimag(f[nd]) * v; }
+            else fr[j] += v * creal(f[nd]);
+            sum[j] += v;
+        }
+    for (int i = 0; i < B->blen; i++) {
+        const int j = B->basis2sol[i];
+        if (j >= 0 && sum[j] != 0.0) b[i] = fr[j] / sum[j] + I * (fi[j] / sum[j]);
+        else b[i] = 0.0;
+    }
+    free(fr); free(fi); free(sum);
+}
+
+/* Grid-basis Jacobian with a blob raster (GenerateJacobian_grid and
+   GenerateJacobian_cw_grid as for the pixel raster): the fields mapped by
+   Map_MeshToGrid = Map_MeshToBasis, image gradients on the padded grid with
+   spacing bbsize / pdim (ImageGradient with the raster's GSize, the
+   unpadded size), masked as for the pixel raster, Map_GridToSol = the
+   solution points' values, J times prod bbsize / (pdim - 1). */
+int tor_jacobian_blob(const tor_mesh *m, const tor_blob *B, int nq, int nm, const double *dphi, const double *aphi,
+                      const double *proj, const int *link_ofs, const int *link_m, int cplx, int logscale, double *J)
+{
+    const int dim = m->dim, n = m->n, glen = B->blen, slen = B->slen, nqm = link_ofs[nq];
+    double gsize[3];
+    for (int d = 0; d < dim; d++) gsize[d] = B->bbmax[d] - B->bbmin[d];
+    zd *fin = malloc(sizeof(zd) * n);
+    zd *ag = malloc(sizeof(zd) * (size_t)nm * glen), *agr = malloc(sizeof(zd) * (size_t)nm * dim * glen);
+    zd *dg = malloc(sizeof(zd) * glen), *dgr = malloc(sizeof(zd) * (size_t)dim * glen);
+    zd *pm = malloc(sizeof(zd) * glen), *pk = malloc(sizeof(zd) * glen);
+    for (int j = 0; j < nm; j++) {
+        for (int i = 0; i < n; i++)
+            fin[i] = cplx ? aphi[2 * ((size_t)j * n + i)] + I * aphi[2 * ((size_t)j * n + i) + 1] : aphi[(size_t)j * n + i];
+        blob_mesh_to_basis(B, fin, cplx, ag + (size_t)j * glen);
+        image_gradient(dim, B->pdim, gsize, ag + (size_t)j * glen, agr + (size_t)j * dim * glen, cplx ? B->elref : NULL);
+    }
+    double sz = 1.0;
+    for (int d = 0; d < dim; d++) sz *= gsize[d] / (B->pdim[d] - 1.0);
+    const size_t cols = cplx ? 2 * (size_t)slen : (size_t)slen;
+    for (int q = 0; q < nq; q++) {
+        for (int i = 0; i < n; i++)
+            fin[i] = cplx ? dphi[2 * ((size_t)q * n + i)] + I * dphi[2 * ((size_t)q * n + i) + 1] : dphi[(size_t)q * n + i];
+        blob_mesh_to_basis(B, fin, cplx, dg);
+        image_gradient(dim, B->pdim, gsize, dg, dgr, B->elref);
+        for (int l = link_ofs[q]; l < link_ofs[q + 1]; l++) {
+            const int j = link_m[l];
+            const zd *a = ag + (size_t)j * glen, *agj = agr + (size_t)j * dim * glen;
+            zd y = cplx ? proj[2 * l] + I * proj[2 * l + 1] : proj[l];
+            double *r0 = J + (size_t)l * cols, *r1 = J + (size_t)(l + nqm) * cols;
+            for (int s = 0; s < slen; s++) {
+                const int g = B->sol2basis[s];
+                zd vm = -(dg[g] * a[g]), vk = 0.0;
+                for (int d = 0; d < dim; d++) vk -= dgr[(size_t)d * glen + g] * agj[(size_t)d * glen + g];
+                if (cplx) {
+                    if (logscale) { vm = vm / y; vk = vk / y; }
+                    r0[s] = creal(vm) * sz; r1[s] = cimag(vm) * sz;
+                    r0[slen + s] = creal(vk) * sz; r1[slen + s] = cimag(vk) * sz;
+                } else {
+                    double wm = creal(vm) * sz, wk = creal(vk) * sz, iy = 1.0 / creal(y);
+                    r0[s] = logscale ? wm * iy : wm;
+                    r1[s] = logscale ? wk * iy : wk;
+                }
+            }
+        }
+    }
+    free(fin); free(ag); free(agr); free(dg); free(dgr); free(pm); free(pk);
+    return slen;
+}
+
+/* The data gradient's grid part with a blob raster (tor_gradient_grid with
+   the blob's field map and solution points) */
+void tor_gradient_blob(const tor_mesh *m, const tor_blob *B, int nq, const double *dphi, const double *wphi,
+                       double *grad)
+{
+    const int dim = m->dim, n = m->n, glen = B->blen, slen = B->slen;
+    double gsize[3];
+    for (int d = 0; d < dim; d++) gsize[d] = B->bbmax[d] - B->bbmin[d];
+    zd *df = malloc(sizeof(zd) * glen), *af = malloc(sizeof(zd) * glen);
+    zd *dg = malloc(sizeof(zd) * (size_t)dim * glen), *ag = malloc(sizeof(zd) * (size_t)dim * glen);
+    for (int q = 0; q < nq; q++) {
+        blob_mesh_to_basis(B, (const zd *)(dphi + 2 * (size_t)q * n), 1, df);
+        image_gradient(dim, B->pdim, gsize, df, dg, B->elref);
+        blob_mesh_to_basis(B, (const zd *)(wphi + 2 * (size_t)q * n), 1, af);
+        image_gradient(dim, B->pdim, gsize, af, ag, B->elref);
+        for (int s = 0; s < slen; s++) {
+            const int g = B->sol2basis[s];
+            grad[s] -= creal(df[g] * af[g]);
+        }
+        for (int s = 0; s < slen; s++) {
+            const int g = B->sol2basis[s];
+            zd gk = 0.0;
+            for (int d = 0; d < dim; d++) gk += dg[(size_t)d * glen + g] * ag[(size_t)d * glen + g];
+            grad[slen + s] -= creal(gk);
+        }
+    }
+    free(df); free(af); free(dg); free(ag);
 }
 
 /* The grid -> solution map of a Raster_Pixel (Map_GridToSol, raster.cc:

@@ -26,6 +26,11 @@ The *_cgrid fixtures (and *_cgrad) use the cubic pixel basis
 (Raster_CubicPixel, raster_cp.cc) on its basis grid or on an intermediate
 grid, with the same contents.
 
+The *blob* fixtures use the blob bases (Raster_GaussBlob, Raster_HanningBlob,
+Raster_RampBlob, Raster_SplineBlob: raster_bl.cc and its subclasses), which
+pad the basis grid by the support radius; rgdim / rbdim hold the padded
+sizes.
+
 The *_el fixtures reset the solver in the element basis (one mua, mus',
 nref per element, seeded) and hold the reference's system matrix, fields,
 projections and element-basis Jacobian.
@@ -120,6 +125,18 @@ FIXTURES = {
                      (6, 6, 5), "cubic"),
     "disc_fd_cgrad": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (9, 9), False,
                       True, (25, 25), "cubic"),
+    # blob bases (Raster_Blob): Gaussian, Hanning, ramp and spline blobs on a
+    # padded grid of the basis size
+    "disc_fd_gblob": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (12, 11), False,
+                      False, (12, 11), "gauss:1.0:2.5"),
+    "disc_cw_hblob": (lambda: workloads.disc(8, 3, 0.0, 6), "CG", "ICH", 1e-15, False, (10, 10), False, False,
+                      (10, 10), "hanning::2.0"),
+    "cyl_fd_rblob": (lambda: small_cylinder(100.0), "BICGSTAB", "ICH", 1e-15, False, (5, 5, 6), False, False,
+                     (5, 5, 6), "ramp::1.5"),
+    "cyl_cw_sblob": (lambda: small_cylinder(0.0), "CG", "ICH", 1e-15, False, (5, 6, 5), False, False, (5, 6, 5),
+                     "spline::2.0"),
+    "disc_fd_sblob_grad": (lambda: workloads.disc(8, 3, 100.0, 6), "BICGSTAB", "ICH", 1e-15, False, (11, 11),
+                           False, True, (11, 11), "spline::2.0"),
 }
 
 
@@ -172,7 +189,8 @@ def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradi
         if gdim:
             args += ["gdim=" + ",".join(str(g) for g in gdim)]
         if raster != "pixel":
-            args += [f"raster={raster}"]
+            kind, sigma, sup = (raster.split(":") + ["", ""])[:3]
+            args += [f"raster={kind}"] + ([f"sigma={sigma}"] if sigma else []) + ([f"sup={sup}"] if sup else [])
         if elbasis:
             emua, emus, eref = element_params(P)
             epar = os.path.join(td, "elpar.bin")
@@ -218,7 +236,14 @@ def run(name, factory, solver, precon, tol, jac, grid=None, elbasis=False, gradi
             res["elref"] = rd(out + "_elref.bin", np.int32)
             res["bdim"] = np.array(grid, np.int32)
             if raster != "pixel":
-                res["raster"] = raster
+                kind, sigma, sup = (raster.split(":") + ["", ""])[:3]
+                res["raster"] = kind
+                if sigma:
+                    res["sigma"] = float(sigma)
+                if sup:
+                    res["sup"] = float(sup)
+                dims = rd(out + "_rgdim.bin", np.int32)
+                res["rgdim"], res["rbdim"] = dims[:P.dim], dims[P.dim:]
             if gdim:
                 res["gdim"] = np.array(gdim, np.int32)
                 res["sol2basis"] = rd(out + "_sol2basis.bin", np.int32)

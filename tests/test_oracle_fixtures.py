@@ -29,8 +29,33 @@ def test_oracle_matches_reference_fixture(oracle_mod, name):
 
 
 GRID = [n for n in names() if n.endswith("_grid")]
-# Raster_Pixel with an intermediate grid finer than the basis
-IGRID = [n for n in names() if "gdim" in load(n)]
+# Raster_Pixel with an intermediate grid finer than the basis, and
+# Raster_CubicPixel
+IGRID = [n for n in names() if "gdim" in load(n) and str(load(n).get("raster", "pixel")) in ("pixel", "cubic")]
+# the blob bases
+BLOB = [n for n in names() if str(load(n).get("raster", "pixel")) in ("gauss", "hanning", "ramp", "spline")]
+
+
+def blob_raster(oracle_mod, g, mesh):
+    return oracle_mod.BlobRaster(mesh, str(g["raster"]), g["bdim"], g["sup"], g.get("sigma", 1.0))
+
+
+@pytest.mark.parametrize("name", BLOB)
+def test_oracle_blob_raster_matches_reference(oracle_mod, name):
+    """The blob bases (Gaussian, Hanning, ramp, spline): the padded basis
+    grid, the element per grid point, the solution points, the grid-basis
+    Jacobian on the reference's fields and every basis map equal the
+    reference's bit for bit."""
+    g = load(name)
+    mesh = oracle_mod.Mesh(g["coords"], g["elems"])
+    B = blob_raster(oracle_mod, g, mesh)
+    assert np.array_equal(B.pdim, g["rbdim"]) and np.array_equal(B.pdim, g["rgdim"])
+    assert np.array_equal(B.elref, g["elref"])
+    assert np.array_equal(B.sol2basis, g["sol2basis"])
+    J = B.jacobian(g["dphi"], g["aphi"], g["proj"], g["link_ofs"], g["link_m"])
+    assert np.array_equal(J, g["Jgrid"])
+    for key, val in B.maps(g["mua"], g["mus"]).items():
+        assert np.array_equal(val, g["map_" + key]), key
 
 
 @pytest.mark.parametrize("name", GRID + IGRID)
@@ -98,9 +123,12 @@ def test_oracle_data_gradient_matches_reference(oracle_mod, name):
     cm, ck, ca = oracle_mod.optical_coefficients(g["mua"], g["mus"], g["nref"])
     val = m.assemble(cm, ck, ca, g["freq_mhz"] * 2 * np.pi * 1e-6, True)
     mvec = np.stack([m.qvec_gaussian(x, g["mwidth"]) * ca for x in g["M"]]).astype(np.complex128)
+    kind = str(g.get("raster", "pixel"))
+    if name in BLOB:
+        kind = blob_raster(oracle_mod, g, m)
     grad = oracle_mod.data_gradient(m, g["bdim"], val, g["dphi"], mvec, g["proj"], g["logproj"], g["link_ofs"],
                                     g["link_m"], g["data"], g["sd"], g["solver"], g["precon"], g["tol"],
-                                    gdim=g.get("gdim"), kind=str(g.get("raster", "pixel")))
+                                    gdim=g.get("gdim"), kind=kind)
     assert np.array_equal(grad, g["grad"])
 
 
