@@ -355,10 +355,24 @@ int tg_jacobian_el(tg_solver s, int nq, const double *dphi, int nm, const double
    a nonempty row of G. */
 #define TG_RASTER_PIXEL 0
 #define TG_RASTER_CUBICPIXEL 1
+#define TG_RASTER_GAUSSBLOB 2
+#define TG_RASTER_HANNINGBLOB 3
+#define TG_RASTER_RAMPBLOB 4
+#define TG_RASTER_SPLINEBLOB 5
 typedef struct tg_raster_s *tg_raster;
 int tg_raster_create(tg_mesh mesh, const int *bdim, tg_raster *out);
 int tg_raster_create_ex(tg_mesh mesh, const int *bdim, const int *gdim, tg_raster *out);
 int tg_raster_create_typed(tg_mesh mesh, int type, const int *bdim, const int *gdim, tg_raster *out);
+/* The blob bases (Raster_Blob, src/libstoast/raster_bl.cc:9-350, and
+   Raster_GaussBlob / HanningBlob / RampBlob / SplineBlob, raster_gb.cc,
+   raster_hb.cc, raster_rb.cc, raster_sb.cc): type TG_RASTER_GAUSSBLOB ..
+   TG_RASTER_SPLINEBLOB, support radius sup in basis spacings, width sigma
+   (Gaussian only).  The basis grid of bdim points is padded by
+   ceil(sup - 1e-6) points on every side and is also the grid (glen = blen
+   = the padded size); the solution points are the basis points within sup
+   of a mesh node.  Fields map to the basis as node-value-weighted averages,
+   the basis back to the nodes as node-value-weighted sums. */
+int tg_raster_create_blob(tg_mesh mesh, int type, const int *bdim, double sup, double sigma, tg_raster *out);
 int tg_raster_destroy(tg_raster r);
 /* glen grid points, slen solution points, bounding box (dim values each) */
 int tg_raster_info(tg_raster r, int *glen, int *slen, double *bbmin, double *bbmax);

@@ -28,7 +28,7 @@ ERR_ARG, ERR_STATE, ERR_CUDA, ERR_NOMEM, ERR_UNSUPPORTED, ERR_BREAKDOWN = 1, 2, 
 EXPORTS = ["tg_mesh_create", "tg_mesh_destroy", "tg_mesh_info", "tg_mesh_csr", "tg_mesh_boundary",
            "tg_qvec_gaussian", "tg_qvec_gaussian_ex", "tg_solver_create", "tg_solver_destroy", "tg_solver_set", "tg_solver_set_refinement", "tg_solver_set_backward_error", "tg_solver_set_reliable_updates", "tg_solver_set_stream", "tg_solver_set_output_stream",
            "tg_solver_sync", "tg_solver_reset", "tg_solver_matrix", "tg_calc_fields", "tg_project_all",
-           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_solver_reset_basis", "tg_jacobian_el", "tg_mesh_load", "tg_mesh_geometry", "tg_gradient", "tg_raster_create", "tg_raster_create_ex", "tg_raster_create_typed", "tg_raster_destroy", "tg_raster_map", "tg_raster_info", "tg_raster_elref", "tg_raster_basis", "tg_jacobian_grid",
+           "tg_jacobian", "tg_forward_path", "tg_project_all_noalloc", "tg_solver_profile", "tg_solver_profile_read", "tg_launch_count", "tg_tuner_log", "tg_solver_reset_basis", "tg_jacobian_el", "tg_mesh_load", "tg_mesh_geometry", "tg_gradient", "tg_raster_create", "tg_raster_create_ex", "tg_raster_create_typed", "tg_raster_create_blob", "tg_raster_destroy", "tg_raster_map", "tg_raster_info", "tg_raster_elref", "tg_raster_basis", "tg_jacobian_grid",
            "tg_qm_load", "tg_qm_info", "tg_qm_positions", "tg_qm_links", "tg_qm_destroy",
            "tg_server_create", "tg_server_destroy", "tg_submit", "tg_poll", "tg_wait", "tg_server_stats",
            "tg_server_reset_stats", "tg_last_error"]
@@ -102,6 +102,7 @@ def lib():
             "tg_raster_create": [vp, ip, C.POINTER(C.c_void_p)],
             "tg_raster_create_ex": [vp, ip, ip, C.POINTER(C.c_void_p)],
             "tg_raster_create_typed": [vp, i_, ip, ip, C.POINTER(C.c_void_p)],
+            "tg_raster_create_blob": [vp, i_, ip, C.c_double, C.c_double, C.POINTER(C.c_void_p)],
             "tg_raster_basis": [vp, ip, ip],
             "tg_raster_destroy": [vp],
             "tg_qm_load": [vp, C.c_char_p, C.POINTER(C.c_void_p)],
@@ -498,22 +499,30 @@ class QM:
             lib().tg_qm_destroy(h)
 
 
-RASTER_KINDS = {"pixel": 0, "cubic": 1}  # TG_RASTER_PIXEL, TG_RASTER_CUBICPIXEL
+# TG_RASTER_PIXEL, TG_RASTER_CUBICPIXEL, and the blob bases
+RASTER_KINDS = {"pixel": 0, "cubic": 1, "gauss": 2, "hanning": 3, "ramp": 4, "spline": 5}
 
 
 class Raster:
     """tg_raster: the pixel raster toast.Raster(mesh, grd, intgrd) builds
-    (kind "pixel"), or the cubic pixel raster (kind "cubic",
-    Raster_CubicPixel): basis bdim, grid gdim (None: the basis grid)."""
+    (kind "pixel"), the cubic pixel raster (kind "cubic",
+    Raster_CubicPixel), or a blob basis (kind "gauss", "hanning", "ramp",
+    "spline": Raster_*Blob, support radius sup, Gaussian width sigma; the
+    grid is the padded basis): basis bdim, grid gdim (None: the basis grid)."""
 
-    def __init__(self, mesh: Mesh, bdim, gdim=None, kind="pixel"):
+    def __init__(self, mesh: Mesh, bdim, gdim=None, kind="pixel", sup=2.0, sigma=1.0):
         self.mesh = mesh
         self.kind = kind
         self.bdim = np.ascontiguousarray(bdim, np.int32)
         self.gdim = self.bdim.copy() if gdim is None else np.ascontiguousarray(gdim, np.int32)
         h = C.c_void_p()
-        _check(lib().tg_raster_create_typed(mesh._h, RASTER_KINDS[kind], self.bdim.ctypes.data_as(C.POINTER(C.c_int)),
-                                            self.gdim.ctypes.data_as(C.POINTER(C.c_int)), C.byref(h)))
+        if RASTER_KINDS[kind] >= 2:
+            _check(lib().tg_raster_create_blob(mesh._h, RASTER_KINDS[kind], self.bdim.ctypes.data_as(C.POINTER(C.c_int)),
+                                               float(sup), float(sigma), C.byref(h)))
+        else:
+            _check(lib().tg_raster_create_typed(mesh._h, RASTER_KINDS[kind],
+                                                self.bdim.ctypes.data_as(C.POINTER(C.c_int)),
+                                                self.gdim.ctypes.data_as(C.POINTER(C.c_int)), C.byref(h)))
         self._h = h
         gl, sl, bl = C.c_int(), C.c_int(), C.c_int()
         self.bbmin, self.bbmax = np.zeros(len(self.bdim)), np.zeros(len(self.bdim))

@@ -67,8 +67,11 @@ __device__ __forceinline__ V grid_component(const GridDev& G, int k, const V* __
     const bool blo = co > 0 && (!masked || G.elref[g - st] >= 0);
     const bool bhi = co < len - 1 && (!masked || G.elref[g + st] >= 0);
     using R = typename vt<V>::R;
-    // the point itself is a solution point, so inside the mask
     if (blo && bhi) return vscale(vsub(gm[(size_t)(g + st) * k + c], gm[(size_t)(g - st) * k + c]), (R)(0.5 * G.ih[d]));
+    // a point outside the mask (a blob basis's solution point off the
+    // mesh) without both neighbours inside: 0 (ImageGradient,
+    // jacobian.cc:944-1060)
+    if (masked && G.elref[g] < 0) return vzero<V>();
     if (blo) return vscale(vsub(v0, gm[(size_t)(g - st) * k + c]), (R)G.ih[d]);
     if (bhi) return vscale(vsub(gm[(size_t)(g + st) * k + c], v0), (R)G.ih[d]);
     return vzero<V>();
@@ -162,9 +165,11 @@ __global__ void __launch_bounds__(256) grid_planes_cm_kernel(GridDev G, int k, i
             if (d >= G.dim) continue;
             const bool blo = co[d] > 0 && (!mk || G.elref[g - st[d]] >= 0);
             const bool bhi = co[d] < len[d] - 1 && (!mk || G.elref[g + st[d]] >= 0);
+            // one-sided differences only at points inside the mask
+            const bool in = !mk || G.elref[g] >= 0;
             if (blo) lo[mk][d] = g - st[d];
             if (bhi) hi[mk][d] = g + st[d];
-            if (blo || bhi) w[mk][d] = (R)((blo && bhi ? 0.5 : 1.0) * G.ih[d]);
+            if ((blo && bhi) || (in && (blo || bhi))) w[mk][d] = (R)((blo && bhi ? 0.5 : 1.0) * G.ih[d]);
         }
     const int c1 = min(k, (int)(blockIdx.y + 1) * MAPC);
     for (int c = blockIdx.y * MAPC; c < c1; c++) {
@@ -497,10 +502,12 @@ __global__ void grid_to_sol_rows_kernel(long long rows, int half, long long row0
 
 // Raster basis maps: y = A x row by row in entry order (RCompRowMatrix::Ax,
 // crmatrix_imp.hpp:1168-1189; complex vectors component by component,
-// Ax_cplx 1302-1327), one thread per (row, vector), `width` doubles per point
+// Ax_cplx 1302-1327), one thread per (row, vector), `width` doubles per point.
+// div (optional): each row's sum divided by div[row], 0 where that is 0 (a
+// blob basis's node average, raster_bl.cc:170-204).
 __global__ void csr_apply_kernel(int rows, int cols, int width, const int* __restrict__ rp,
                                  const int* __restrict__ col, const double* __restrict__ val,
-                                 const double* __restrict__ x, double* __restrict__ y)
+                                 const double* __restrict__ x, double* __restrict__ y, const double* __restrict__ div)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y;
     if (r >= rows) return;
@@ -508,6 +515,7 @@ __global__ void csr_apply_kernel(int rows, int cols, int width, const int* __res
     for (int c = 0; c < width; c++) {
         double acc = 0.0;
         for (int j = rp[r]; j < rp[r + 1]; j++) acc = __dadd_rn(acc, __dmul_rn(val[j], xv[(size_t)col[j] * width + c]));
+        if (div) acc = div[r] != 0.0 ? __ddiv_rn(acc, div[r]) : 0.0;
         y[((size_t)v * rows + r) * width + c] = acc;
     }
 }

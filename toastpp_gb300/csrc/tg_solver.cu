@@ -1060,6 +1060,16 @@ struct tg_raster_s {
     // (blen x n), CI = BI GI (n x blen), and G's rows of the solution points
     // with columns as positions in gsol (slen x gslen)
     CsrMat G, GI, C, CI, GS;
+    // blob bases: support radius, width (Gaussian), padding layers, inverse
+    // basis spacing of the unpadded basis, the blob scale; NV: per node the
+    // blob values of the solution points (n x slen), NB the same with basis
+    // columns (n x blen), AV: per basis point its node values in node order
+    // (blen x n) with their sums avsum (0 off the solution points)
+    double sup = 0.0, sigma = 0.0, bscale = 0.0, igrid[3] = {0, 0, 0};
+    int npad = 0;
+    CsrMat NV, NB, AV;
+    std::vector<double> avsum;
+    DBuf d_avsum;
     DBuf d_elref, d_sol, d_rowptr, d_col, d_val, d_nrowptr, d_ncol, d_nval, d_src, d_dst, d_tmp, d_tmp2, d_s2b;
     GridDev dev() const
     {
@@ -1087,7 +1097,7 @@ namespace {
 // claims the unclaimed grid points of its widened box that it contains) and
 // the grid map matrix (GridMapMatrix, mesh.cc:2486-2554: the element's global
 // shape functions at the point, tri3.cc:231-240, tet4.cc:302-313)
-void raster_build(const MeshHost& m, tg_raster_s& r)
+void raster_build(const MeshHost& m, tg_raster_s& r, const double* boxmin = nullptr, const double* boxmax = nullptr)
 {
     const int dim = m.dim, nn = m.nn;
     for (int d = 0; d < dim; d++) { r.bbmin[d] = 1e6; r.bbmax[d] = -1e6; }
@@ -1098,8 +1108,12 @@ void raster_build(const MeshHost& m, tg_raster_s& r)
             r.bbmax[d] = std::max(r.bbmax[d], v);
         }
     const int nx = r.gdim[0], ny = r.gdim[1], nz = dim > 2 ? r.gdim[2] : 1;
+    // the box the grid spans: the mesh's, or a given one (a blob basis's
+    // padded box), for the element search only
+    const double* bl = boxmin ? boxmin : r.bbmin;
+    const double* bh = boxmax ? boxmax : r.bbmax;
     double dW[3] = {0, 0, 0};
-    for (int d = 0; d < dim; d++) dW[d] = (r.bbmax[d] - r.bbmin[d]) / (double)(r.gdim[d] - 1);
+    for (int d = 0; d < dim; d++) dW[d] = (bh[d] - bl[d]) / (double)(r.gdim[d] - 1);
     r.elref.assign(r.glen, -1);
     for (int e = 0; e < m.ne; e++) {
         const int* nd = &m.el[(size_t)e * nn];
@@ -1116,25 +1130,26 @@ void raster_build(const MeshHost& m, tg_raster_s& r)
         for (int d = 0; d < dim && !skip; d++) {
             lo[d] -= 1e-6;
             hi[d] += 1e-6;
-            if (lo[d] > r.bbmax[d] || hi[d] < r.bbmin[d]) { skip = true; break; }
-            rmin[d] = std::max(0, (int)std::ceil((lo[d] - r.bbmin[d]) / dW[d]));
-            rmax[d] = std::min(r.gdim[d], (int)std::floor((hi[d] - r.bbmin[d]) / dW[d]) + 1);
+            if (lo[d] > bh[d] || hi[d] < bl[d]) { skip = true; break; }
+            rmin[d] = std::max(0, (int)std::ceil((lo[d] - bl[d]) / dW[d]));
+            rmax[d] = std::min(r.gdim[d], (int)std::floor((hi[d] - bl[d]) / dW[d]) + 1);
         }
         if (skip) continue;
         double p[3] = {0.0, 0.0, 0.0};
         for (int iz = rmin[2]; iz < rmax[2]; iz++) {
-            if (dim > 2) p[2] = iz * dW[2] + r.bbmin[2];
+            if (dim > 2) p[2] = iz * dW[2] + bl[2];
             for (int iy = rmin[1]; iy < rmax[1]; iy++) {
-                p[1] = iy * dW[1] + r.bbmin[1];
+                p[1] = iy * dW[1] + bl[1];
                 for (int ix = rmin[0]; ix < rmax[0]; ix++) {
                     const int idx = ix + nx * (iy + ny * iz);
                     if (r.elref[idx] >= 0) continue;
-                    p[0] = ix * dW[0] + r.bbmin[0];
+                    p[0] = ix * dW[0] + bl[0];
                     if (el_gcontains(m, e, p)) r.elref[idx] = e;
                 }
             }
         }
     }
+    if (boxmin) return;  // the blob basis builds its own maps
     r.rowptr.assign(r.glen + 1, 0);
     r.col.clear();
     r.val.clear();
@@ -1459,6 +1474,221 @@ void cubic_basis(tg_raster_s& r)
     r.slen = (int)r.sol2basis.size();
 }
 
+// A blob basis (Raster_Blob, raster_bl.cc:9-75, and its subclasses
+// raster_gb.cc, raster_hb.cc, raster_rb.cc, raster_sb.cc).  The basis grid
+// of bdim points over the mesh's box is padded by npad = ceil(sup - 1e-6)
+// layers on every side (igrid from the unpadded basis), and is also the
+// grid; the element per grid point comes from the padded box.  Solution
+// points: the basis points within sup grid spacings of a mesh node, in
+// basis order.  The blob value of basis point b at p, r = (b - npad) +
+// (bbmin - p) igrid: Gaussian scale exp(-|r|^2 / sigma^2) (|r|^2 < sup^2),
+// Hanning scale (1 + cos(pi |r| / sup)), ramp scale (1 - |r| / sup), spline
+// scale 4 sum over the first two knots xi_k = (k - 2) sup / 2 left of -|r|
+// of (-|r| - xi_k)^3 omega_k (|r| < sup).  The scale: the start value (1;
+// Hanning 0.5) times 1 / (mean over the nodes of the sum of the values),
+// ComputeBasisScale (353-361).  The reference tests every node against
+// every basis point; the scans here cover index windows wider by one than
+// the support, where the same tests decide.
+struct BlobForm {
+    int type, dim, npad, pdim[3];
+    double sup, a2, isigma2, fac, isup, xi[5], iomega[5], scale, bbmin[3], igrid[3];
+    double value(const int* b, const double* p) const
+    {
+        double r2 = 0.0;
+        for (int d = 0; d < dim; d++) {
+            const double r = (b[d] - npad) + (bbmin[d] - p[d]) * igrid[d];
+            r2 += std::fabs(r) * std::fabs(r);
+        }
+        if (type == TG_RASTER_GAUSSBLOB) return r2 >= a2 ? 0.0 : scale * std::exp(-r2 * isigma2);
+        const double rad = std::sqrt(r2);
+        if (rad >= sup) return 0.0;
+        if (type == TG_RASTER_HANNINGBLOB) return scale * (1.0 + std::cos(fac * rad));
+        if (type == TG_RASTER_RAMPBLOB) return scale * (1.0 - rad * isup);
+        const double x = -rad;
+        double dx = x - xi[0], d3 = dx * dx * dx, sum = d3 * iomega[0];
+        if (x > xi[1]) {
+            dx = x - xi[1];
+            d3 = dx * dx * dx;
+            sum += d3 * iomega[1];
+        }
+        sum *= 4.0;
+        return scale * sum;
+    }
+};
+
+void blob_basis(const MeshHost& m, tg_raster_s& r)
+{
+    const int dim = r.dim, n = m.n;
+    double bmin[3] = {1e6, 1e6, 1e6}, bmax[3] = {-1e6, -1e6, -1e6};
+    for (int k = 0; k < n; k++)
+        for (int d = 0; d < dim; d++) {
+            const double v = m.coords[(size_t)k * dim + d];
+            bmin[d] = std::min(bmin[d], v);
+            bmax[d] = std::max(bmax[d], v);
+        }
+    for (int d = 0; d < dim; d++) r.igrid[d] = (r.bdim[d] - 1.0) / (bmax[d] - bmin[d]);
+    r.npad = (int)std::ceil(r.sup - 1e-6);
+    long long blen = 1;
+    for (int d = 0; d < dim; d++) {
+        r.bdim[d] += 2 * r.npad;
+        r.gdim[d] = r.bdim[d];
+        blen *= r.bdim[d];
+    }
+    TG_CHECK(blen < (1LL << 30), TG_ERR_ARG, "grid too large");
+    r.blen = r.glen = (int)blen;
+    double pmin[3], pmax[3];
+    for (int d = 0; d < dim; d++) {
+        pmin[d] = bmin[d] - r.npad / r.igrid[d];
+        pmax[d] = bmax[d] + r.npad / r.igrid[d];
+    }
+    raster_build(m, r, pmin, pmax);
+    const int pd[3] = {r.bdim[0], r.bdim[1], dim > 2 ? r.bdim[2] : 1};
+    // index window of the basis points within `reach` of a point whose
+    // position in basis coordinates is c (per axis)
+    auto window = [&](const double* c, double reach, int* lo, int* hi) {
+        for (int d = 0; d < 3; d++) {
+            lo[d] = 0;
+            hi[d] = 0;
+        }
+        for (int d = 0; d < dim; d++) {
+            lo[d] = std::max(0, (int)std::floor(c[d] - reach) - 1);
+            hi[d] = std::min(pd[d] - 1, (int)std::ceil(c[d] + reach) + 1);
+        }
+    };
+    // solution points (raster_bl.cc:45-72)
+    std::vector<unsigned char> on(blen, 0);
+    const double sup2 = r.sup * r.sup;
+    for (int nd = 0; nd < n; nd++) {
+        const double* x = &m.coords[(size_t)nd * dim];
+        double c[3] = {0, 0, 0};
+        for (int d = 0; d < dim; d++) c[d] = (x[d] - bmin[d]) * r.igrid[d] + r.npad;
+        int lo[3], hi[3];
+        window(c, r.sup, lo, hi);
+        for (int iz = lo[2]; iz <= hi[2]; iz++)
+            for (int iy = lo[1]; iy <= hi[1]; iy++)
+                for (int ix = lo[0]; ix <= hi[0]; ix++) {
+                    const double rr[3] = {(double)ix, (double)iy, (double)iz};
+                    double rad2 = 0.0;
+                    for (int d = 0; d < dim; d++) {
+                        const double dx = (x[d] - bmin[d]) * r.igrid[d] + r.npad - rr[d];
+                        rad2 += dx * dx;
+                    }
+                    if (rad2 < sup2) on[ix + pd[0] * (iy + pd[1] * iz)] = 1;
+                }
+    }
+    std::vector<int> b2s(blen, -1);
+    r.sol2basis.clear();
+    for (int b = 0; b < (int)blen; b++)
+        if (on[b]) {
+            b2s[b] = (int)r.sol2basis.size();
+            r.sol2basis.push_back(b);
+        }
+    r.slen = (int)r.sol2basis.size();
+    r.gsol = r.sol2basis;
+    r.gslen = r.slen;
+    BlobForm F{};
+    F.type = r.type;
+    F.dim = dim;
+    F.npad = r.npad;
+    F.sup = r.sup;
+    F.a2 = r.sup * r.sup;
+    F.scale = 1.0;
+    for (int d = 0; d < dim; d++) {
+        F.bbmin[d] = bmin[d];
+        F.igrid[d] = r.igrid[d];
+    }
+    if (r.type == TG_RASTER_GAUSSBLOB) F.isigma2 = 1.0 / (r.sigma * r.sigma);
+    if (r.type == TG_RASTER_HANNINGBLOB) {
+        F.fac = 3.14159265358979323846 / r.sup;
+        F.scale = 0.5;
+    }
+    if (r.type == TG_RASTER_RAMPBLOB) F.isup = 1.0 / r.sup;
+    if (r.type == TG_RASTER_SPLINEBLOB) {
+        for (int i = 0; i <= 4; i++) F.xi[i] = (i - 2) * 0.5 * r.sup;
+        for (int i = 0; i <= 4; i++) {
+            F.iomega[i] = 1.0;
+            for (int j = 0; j <= 4; j++)
+                if (i != j) F.iomega[i] /= F.xi[i] - F.xi[j];
+        }
+    }
+    // the node values of the solution points near each node, in solution
+    // (= basis) order
+    auto node_values = [&](int nd, std::vector<int>& cols, std::vector<double>& vals) {
+        cols.clear();
+        vals.clear();
+        const double* x = &m.coords[(size_t)nd * dim];
+        double c[3] = {0, 0, 0};
+        for (int d = 0; d < dim; d++) c[d] = r.npad - (bmin[d] - x[d]) * r.igrid[d];
+        int lo[3], hi[3];
+        window(c, r.sup, lo, hi);
+        for (int iz = lo[2]; iz <= hi[2]; iz++)
+            for (int iy = lo[1]; iy <= hi[1]; iy++)
+                for (int ix = lo[0]; ix <= hi[0]; ix++) {
+                    const int b = ix + pd[0] * (iy + pd[1] * iz);
+                    if (b2s[b] < 0) continue;
+                    const int bi[3] = {ix, iy, iz};
+                    const double v = F.value(bi, x);
+                    if (v != 0.0) {
+                        cols.push_back(b2s[b]);
+                        vals.push_back(v);
+                    }
+                }
+    };
+    std::vector<int> cols;
+    std::vector<double> vals;
+    double tot = 0.0;
+    for (int nd = 0; nd < n; nd++) {
+        node_values(nd, cols, vals);
+        double sum = 0.0;
+        for (double v : vals) sum += 1.0 * v;
+        tot += sum;
+    }
+    const double cbs = 1.0 / (tot / n);
+    F.scale = r.type == TG_RASTER_GAUSSBLOB ? cbs : F.scale * cbs;
+    r.bscale = F.scale;
+    CsrMat& NV = r.NV;
+    NV.rp.assign(1, 0);
+    NV.col.clear();
+    NV.val.clear();
+    for (int nd = 0; nd < n; nd++) {
+        node_values(nd, cols, vals);
+        NV.col.insert(NV.col.end(), cols.begin(), cols.end());
+        NV.val.insert(NV.val.end(), vals.begin(), vals.end());
+        NV.rp.push_back((int)NV.col.size());
+    }
+    CsrMat& NB = r.NB;
+    NB.rp = NV.rp;
+    NB.val = NV.val;
+    NB.col.resize(NV.col.size());
+    for (size_t t = 0; t < NV.col.size(); t++) NB.col[t] = r.sol2basis[NV.col[t]];
+    // AV: rows by basis point, node order; the field map of the Jacobian is
+    // AV with each row divided by its sum
+    CsrMat& AV = r.AV;
+    AV.rp.assign(blen + 1, 0);
+    for (int b : NB.col) AV.rp[b + 1]++;
+    for (int b = 0; b < (int)blen; b++) AV.rp[b + 1] += AV.rp[b];
+    AV.col.resize(NB.col.size());
+    AV.val.resize(NB.col.size());
+    std::vector<int> fill(blen, 0);
+    for (int nd = 0; nd < n; nd++)
+        for (int t = NB.rp[nd]; t < NB.rp[nd + 1]; t++) {
+            const int b = NB.col[t], k = AV.rp[b] + fill[b]++;
+            AV.col[k] = nd;
+            AV.val[k] = NB.val[t];
+        }
+    r.avsum.assign(blen, 0.0);
+    for (int b = 0; b < (int)blen; b++)
+        for (int k = AV.rp[b]; k < AV.rp[b + 1]; k++) r.avsum[b] += AV.val[k];
+    r.rowptr = AV.rp;
+    r.col = AV.col;
+    r.val.resize(AV.val.size());
+    for (int b = 0; b < (int)blen; b++)
+        for (int k = AV.rp[b]; k < AV.rp[b + 1]; k++) r.val[k] = AV.val[k] / r.avsum[b];
+    r.nrowptr = NB.rp;
+    r.ncol = NB.col;
+    r.nval = NB.val;
+}
+
 // The pixel raster with an intermediate grid: bsupport = SubsampleLinPixel
 // of the grid's mesh mask (raster.cc:55-64), solution points the basis
 // points with bsupport > 0 (66-77); G = Grid2LinPixMatrix (rows divided by
@@ -1519,6 +1749,7 @@ void pixel_basis(int n, tg_raster_s& r)
 // device as GS for the Jacobian and the data gradient.
 void raster_basis(int n, tg_raster_s& r)
 {
+    if (r.type >= TG_RASTER_GAUSSBLOB) return;  // blob_basis built everything
     if (r.type == TG_RASTER_CUBICPIXEL) {
         r.hasG = true;
         cubic_basis(r);
@@ -3326,20 +3557,21 @@ static void upload_csr(CsrMat& A)
     upload_sync(A.d_val, A.val);
 }
 
-int tg_raster_create_typed(tg_mesh mesh, int type, const int* bdim, const int* gdim, tg_raster* out)
+static void raster_create(tg_mesh mesh, int type, const int* bdim, const int* gdim, double sup, double sigma,
+                          tg_raster* out)
 {
-    API_BEGIN
     TG_CHECK(mesh && bdim && out, TG_ERR_ARG, "NULL argument");
-    TG_CHECK(type == TG_RASTER_PIXEL || type == TG_RASTER_CUBICPIXEL, TG_ERR_ARG, "unknown raster type");
     *out = nullptr;
     const MeshHost& m = mesh->m->h;
     auto r = std::make_unique<tg_raster_s>();
     r->mesh = mesh->m.get();
     r->dim = m.dim;
     r->type = type;
+    const bool blob = type >= TG_RASTER_GAUSSBLOB;
     long long glen = 1, blen = 1;
     for (int d = 0; d < m.dim; d++) {
-        const int g = gdim ? gdim[d] : bdim[d];
+        // a blob basis ignores the intermediate grid (raster_bl.cc:11-12)
+        const int g = gdim && !blob ? gdim[d] : bdim[d];
         TG_CHECK(bdim[d] >= 2 && g >= 2, TG_ERR_ARG, "every grid dimension needs at least 2 points");
         r->bdim[d] = bdim[d];
         r->gdim[d] = g;
@@ -3350,8 +3582,16 @@ int tg_raster_create_typed(tg_mesh mesh, int type, const int* bdim, const int* g
     TG_CHECK(glen < (1LL << 30) && blen < (1LL << 30), TG_ERR_ARG, "grid too large");
     r->glen = (int)glen;
     r->blen = (int)blen;
-    raster_build(m, *r);
-    raster_basis(m.n, *r);
+    if (blob) {
+        TG_CHECK(sup > 0.0 && sup < 64.0, TG_ERR_ARG, "blob support radius out of range");
+        TG_CHECK(type != TG_RASTER_GAUSSBLOB || sigma > 0.0, TG_ERR_ARG, "Gaussian blob width must be positive");
+        r->sup = sup;
+        r->sigma = sigma;
+        blob_basis(m, *r);
+    } else {
+        raster_build(m, *r);
+        raster_basis(m.n, *r);
+    }
     TG_CUDA(cudaSetDevice(mesh->m->device));
     upload_sync(r->d_elref, r->elref);
     upload_sync(r->d_sol, r->gsol);
@@ -3365,7 +3605,27 @@ int tg_raster_create_typed(tg_mesh mesh, int type, const int* bdim, const int* g
     if (r->hasG)
         for (CsrMat* A : {&r->G, &r->GI, &r->C, &r->CI, &r->GS})
             if (!A->rp.empty()) upload_csr(*A);
+    if (blob) {
+        for (CsrMat* A : {&r->NV, &r->NB, &r->AV}) upload_csr(*A);
+        upload_sync(r->d_avsum, r->avsum);
+    }
     *out = r.release();
+}
+
+int tg_raster_create_typed(tg_mesh mesh, int type, const int* bdim, const int* gdim, tg_raster* out)
+{
+    API_BEGIN
+    TG_CHECK(type == TG_RASTER_PIXEL || type == TG_RASTER_CUBICPIXEL, TG_ERR_ARG,
+             "unknown raster type (blob bases: tg_raster_create_blob)");
+    raster_create(mesh, type, bdim, gdim, 0.0, 0.0, out);
+    API_END
+}
+
+int tg_raster_create_blob(tg_mesh mesh, int type, const int* bdim, double sup, double sigma, tg_raster* out)
+{
+    API_BEGIN
+    TG_CHECK(type >= TG_RASTER_GAUSSBLOB && type <= TG_RASTER_SPLINEBLOB, TG_ERR_ARG, "unknown blob type");
+    raster_create(mesh, type, bdim, nullptr, sup, sigma, out);
     API_END
 }
 
@@ -3436,8 +3696,12 @@ int tg_raster_map(tg_raster r, const char* map, int nvec, const double* src, dou
     const int n = r->mesh->d.n, glen = r->glen, blen = r->blen, slen = r->slen;
     auto len = [&](char c) { return c == 'M' ? n : c == 'G' ? glen : c == 'B' ? blen : c == 'S' ? slen : -1; };
     TG_CHECK(len(a) > 0 && len(b) > 0 && a != b, TG_ERR_ARG, "map ids are M, G, B or S, source and target different");
-    // I: maps through G; P: the pixel raster's own real maps (products, D)
+    // I: maps through G; P: the pixel raster's own real maps (products, D);
+    // blob bases: the node-value maps of raster_bl.cc:140-350 ('A' the
+    // weighted node average, 'V' / 'W' the node sums over the basis /
+    // solution points), grid = basis
     const bool I = r->hasG, P = width == 1 && r->type == TG_RASTER_PIXEL;
+    const bool blob = r->type >= TG_RASTER_GAUSSBLOB;
     // steps: 'B' grid map, 'N' node map, 'G' / 'I' grid <-> basis, 'C' / 'D'
     // mesh <-> basis products, 's' support, 'x' its scatter, '=' copy
     std::string steps;
@@ -3454,6 +3718,15 @@ int tg_raster_map(tg_raster r, const char* map, int nvec, const double* src, dou
     else if (key == "SB") steps = "x";
     else if (key == "SG") steps = I ? "xI" : "x";
     else if (key == "SM") steps = I ? (P ? "xD" : "xIN") : "xN";
+    if (blob) {
+        if (key == "MG" || key == "MB") steps = "A";
+        else if (key == "MS") steps = "As";
+        else if (key == "GM" || key == "BM") steps = "V";
+        else if (key == "SM") steps = "W";
+        else if (key == "GB" || key == "BG") steps = "=";
+        else if (key == "GS" || key == "BS") steps = "s";
+        else if (key == "SG" || key == "SB") steps = "x";
+    }
     TG_CUDA(cudaSetDevice(r->mesh->device));
     const size_t sb = (size_t)nvec * len(a) * width * sizeof(double), db = (size_t)nvec * len(b) * width * sizeof(double);
     const double* x = mem == TG_MEM_DEVICE ? src : (const double*)r->d_src.ensure(sb);
@@ -3464,7 +3737,8 @@ int tg_raster_map(tg_raster r, const char* map, int nvec, const double* src, dou
     const cudaStream_t st = 0;
     auto apply = [&](const int* rp, const int* cl, const double* vl, int rows, int cols, const double* in,
                      double* out) {
-        launch(csr_apply_kernel, dim3(cdiv_u(rows, 128), nvec), 128, 0, st, rows, cols, width, rp, cl, vl, in, out);
+        launch(csr_apply_kernel, dim3(cdiv_u(rows, 128), nvec), 128, 0, st, rows, cols, width, rp, cl, vl, in, out,
+               (const double*)nullptr);
     };
     auto mat = [&](const CsrMat& A, int rows, int cols, const double* in, double* out) {
         apply(A.d_rp.as<int>(), A.d_col.as<int>(), A.d_val.as<double>(), rows, cols, in, out);
@@ -3474,7 +3748,8 @@ int tg_raster_map(tg_raster r, const char* map, int nvec, const double* src, dou
     for (size_t i = 0; i < steps.size(); i++) {
         const char c = steps[i];
         const char to = c == 'B' ? 'G' : c == 'N' ? 'M' : c == 'G' ? 'B' : c == 'I' ? 'G' : c == 'C' ? 'B'
-                      : c == 'D' ? 'M' : c == 's' ? 'S' : c == 'x' ? 'B' : b;
+                      : c == 'D' ? 'M' : c == 's' ? 'S' : c == 'x' ? 'B' : c == 'A' ? 'B'
+                      : (c == 'V' || c == 'W') ? 'M' : b;
         double* out = i + 1 == steps.size() ? y : tmp[i & 1];
         switch (c) {
         case 'B': apply(r->d_rowptr.as<int>(), r->d_col.as<int>(), r->d_val.as<double>(), glen, n, cur, out); break;
@@ -3483,6 +3758,12 @@ int tg_raster_map(tg_raster r, const char* map, int nvec, const double* src, dou
         case 'I': mat(r->GI, glen, blen, cur, out); break;
         case 'C': mat(r->C, blen, n, cur, out); break;
         case 'D': mat(r->CI, n, blen, cur, out); break;
+        case 'A':
+            launch(csr_apply_kernel, dim3(cdiv_u(blen, 128), nvec), 128, 0, st, blen, n, width, r->AV.d_rp.as<int>(),
+                   r->AV.d_col.as<int>(), r->AV.d_val.as<double>(), cur, out, r->d_avsum.as<double>());
+            break;
+        case 'V': mat(r->NB, n, blen, cur, out); break;
+        case 'W': mat(r->NV, n, slen, cur, out); break;
         case 's':
             if (slen > 0)
                 launch(gather_points_kernel, dim3(cdiv_u(slen, 128), nvec), 128, 0, st, slen, blen, width,
