@@ -2050,8 +2050,9 @@ static const LinkHost& links_of(tg_solver s, int nq, int nm, const int* link_ofs
     bool same = c.nq == nq && c.nm == nm && (int)c.ofs.size() == nq + 1 &&
                 std::equal(c.ofs.begin(), c.ofs.end(), link_ofs);
     if (same) {
+        // a NULL detector list with links goes on to make_links, which rejects it
         const size_t nqm = (size_t)link_ofs[nq];
-        same = c.m.size() == nqm && (nqm == 0 || std::equal(c.m.begin(), c.m.end(), link_m));
+        same = c.m.size() == nqm && (nqm == 0 || (link_m && std::equal(c.m.begin(), c.m.end(), link_m)));
     }
     if (!same) {
         LinkHost L = make_links(nq, nm, link_ofs, link_m);
