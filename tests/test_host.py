@@ -27,6 +27,26 @@ def test_qm_file_round_trip(tmp_path):
     assert np.array_equal(qm.link_ofs, P.qm.link_ofs) and np.array_equal(qm.link_m, P.qm.link_m)
 
 
+def test_qm_list_flags_and_normals(tmp_path):
+    """The list flags and normals of a QM file (qmmesh.cc:338-347, 399-408):
+    "fixed" / "external" as the second header token, "default" normals as
+    the third; a normal read with a position where one is given, 0
+    elsewhere."""
+    f = tmp_path / "e.qm"
+    f.write_text("QM file 2D\nDimension 2\n\nSourceList 2 External default\n1 2 0.5 -0.5\n3 4\n\n"
+                 "MeasurementList 2 external\n5 6 0 1\n7 8 1 0\n\nLinkList\n1: 0\n2: 0 1\n")
+    qm = meshio.read_qm(str(f))
+    assert qm.q_external and qm.q_default_normals and not qm.q_fixed
+    assert qm.m_external and not qm.m_default_normals
+    assert np.array_equal(qm.Q, [[1, 2], [3, 4]]) and np.array_equal(qm.QN, [[0.5, -0.5], [0, 0]])
+    assert np.array_equal(qm.MN, [[0, 1], [1, 0]])
+    assert list(qm.link_ofs) == [0, 1, 3] and list(qm.link_m) == [0, 0, 1]
+    f.write_text("QM file 2D\nDimension 2\n\nSourceList 1 fixed\n1 2\n\nMeasurementList 1\n5 6\n\n"
+                 "LinkList\n1: 0\n")
+    qm = meshio.read_qm(str(f))
+    assert qm.q_fixed and not qm.q_external and not qm.m_fixed and not qm.m_external
+
+
 @pytest.mark.skipif(not has_reference(), reason="reference tree not available")
 def test_reads_reference_meshes():
     c, e = meshio.read_mesh(os.path.join(REFERENCE, "test", "2D", "meshes", "circle25_32.msh"))
